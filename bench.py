@@ -1,0 +1,380 @@
+"""Benchmark of the GB300 path-tracing core.
+
+Workload (one "step"): the ray-cast microbenchmark -- a 1M-triangle soup
+(uniform-random triangles in [-1,1]^3, edge lengths ~U(0.005, 0.05), FP32
+vertices, int32 indices) queried by 16M closest-hit rays (origins on a sphere
+of radius 3, directions towards random points of the unit ball, tmax = inf)
+and by an 8M any-hit subset (tmax = distance to a second random point).
+Metric: Mrays/s over all traversal queries (closest + any).
+
+  value   device-resident throughput: rays already in HBM, CUDA events on the
+          launching stream, L2 flushed between steps (the 512 MB ray buffer is
+          also larger than L2; the BVH stays resident like any scene)
+  e2e     the same rays through the C-ABI host-buffer calls
+          (bling_trace_closest / bling_trace_any) from pinned memory: H2D copy
+          of the rays and D2H copy of (t, prim) / hit flags inside the timed
+          region
+  cpu_baseline / --impl reference
+          the CPU oracle (a C++ restatement of the reference's Haskell
+          intersection code; the Haskell reference cannot be built here) on a
+          bounded sample of the same rays, all host cores
+
+Multi-GPU: the path does not shard -- `--gpus N` runs N independent replicas
+(one per rank, torchrun), `value` = all ranks' rays / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_TRIS = 1 << 20
+N_RAYS = 1 << 24
+N_ANY = N_RAYS // 2
+CPU_SAMPLE_RAYS = 1 << 20
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-i", str(self.dev), "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_oracle_rate(soup, rays_np, ra_np, n_sample: int):
+    """Mrays/s of the CPU oracle (closest + any over a bounded sample)."""
+    from oracle.oracle import OracleScene
+    o = OracleScene(soup)
+    nc = n_sample
+    na = n_sample // 2
+    rc = np.ascontiguousarray(rays_np[:, :nc])
+    rr = np.ascontiguousarray(ra_np[:, :na])
+    t0 = time.perf_counter()
+    o.closest(rc)
+    o.any(rr)
+    dt = time.perf_counter() - t0
+    cores = os.cpu_count() or 1
+    return (nc + na) / dt / 1e6, cores, dt, f"{nc} closest + {na} any-hit rays of the same workload"
+
+
+def run_reference(args):
+    """--impl reference: the reference's algorithm on the host cores (the CPU
+    oracle restatement; the Haskell reference has no toolchain here)."""
+    world, rank, _ = dist_env()
+    if world > 1 and rank != 0:
+        return
+    from bling_gb300 import scene as S
+    from oracle import build as ob
+    ob.build()
+    soup = S.triangle_soup(N_TRIS, seed=1)
+    rays = S.soup_rays(N_RAYS if args.full_rays else (args.cpu_rays * 2), seed=2)
+    ra = S.soup_rays(N_RAYS if args.full_rays else (args.cpu_rays * 2), seed=3, any_hit=True)
+    from oracle.oracle import OracleScene
+    o = OracleScene(soup)
+    n = args.cpu_rays
+    rc = np.ascontiguousarray(rays[:, :n])
+    rr = np.ascontiguousarray(ra[:, :n // 2])
+    for _ in range(args.warmup):
+        o.closest(rc[:, : max(1, n // 16)])
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.closest(rc)
+        o.any(rr)
+        times.append(time.perf_counter() - t0)
+    dt = float(np.mean(times))
+    val = (n + n // 2) / dt / 1e6
+    cores = os.cpu_count() or 1
+    line = {
+        "impl": "reference", "metric": "Mrays/s", "value": round(val, 3), "unit": "Mrays/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(args, world),
+        "cpu_baseline": {"value": round(val, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                         "sample": f"{n} closest + {n // 2} any-hit rays per step (of 16M + 8M)"},
+        "e2e": {"value": round(val, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "reference is Haskell (GHC absent); its algorithm runs as the C++ oracle restatement",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, world):
+    return {"workload": "ray-cast microbench: 1M-tri soup, 16M closest + 8M any-hit rays",
+            "triangles": N_TRIS, "rays_closest": N_RAYS, "rays_any": N_ANY,
+            "l2": "flushed between steps (256 MB write); ray buffers 768 MB > L2",
+            "parallelism": f"replicas x{world}"}
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from bling_gb300 import build as gb
+    gb.build()
+    from bling_gb300 import scene as S
+    from bling_gb300.api import Context
+
+    ctx = Context(device=local)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+    soup = S.triangle_soup(N_TRIS, seed=1)
+    rays = S.soup_rays(N_RAYS, seed=2)
+    ra = S.soup_rays(N_RAYS, seed=3, any_hit=True)
+    ra = np.ascontiguousarray(ra[:, :N_ANY])
+    g = ctx.scene(soup)
+    st = g.stats()
+
+    d_rays = torch.from_numpy(rays).to(dev)
+    d_any = torch.from_numpy(ra).to(dev)
+    d_t = torch.empty(N_RAYS, dtype=torch.float32, device=dev)
+    d_p = torch.empty(N_RAYS, dtype=torch.int32, device=dev)
+    d_h = torch.empty(N_ANY, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(stream)
+        g.closest_device(d_rays, d_t, d_p)
+        ev[1].record(stream)
+        g.any_device(d_any, d_h)
+        ev[2].record(stream)
+        return ev
+
+    for _ in range(args.warmup):
+        step()
+        flush.fill_(1)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    step_ms, closest_ms, any_ms = [], [], []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1)
+            ev = step()
+            torch.cuda.synchronize()
+            closest_ms.append(ev[0].elapsed_time(ev[1]))
+            any_ms.append(ev[1].elapsed_time(ev[2]))
+            step_ms.append(ev[0].elapsed_time(ev[2]))
+    torch.cuda.synchronize()
+    barrier(world)
+    total_s = sum(step_ms) / 1e3
+    total_s = max_over_ranks(total_s, world, dev)
+    rays_per_step = N_RAYS + N_ANY
+    value = world * rays_per_step * args.steps / total_s / 1e6
+    hit_frac = float((d_p >= 0).float().mean().item())
+
+    # ---- end to end: host buffers through the C ABI (pinned memory)
+    h_rays = torch.from_numpy(rays).pin_memory().numpy()
+    h_any = torch.from_numpy(ra).pin_memory().numpy()
+    h_t = torch.empty(N_RAYS, dtype=torch.float32).pin_memory().numpy()
+    h_p = torch.empty(N_RAYS, dtype=torch.int32).pin_memory().numpy()
+    h_h = torch.empty(N_ANY, dtype=torch.uint8).pin_memory().numpy()
+    import ctypes as C
+    from bling_gb300.api import lib
+    L = lib()
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+
+    def e2e_step():
+        ctx.check(L.bling_trace_closest(g.h, fp(h_rays), N_RAYS, fp(h_t),
+                                        h_p.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        C.POINTER(C.c_float)()))
+        ctx.check(L.bling_trace_any(g.h, fp(h_any), N_ANY, h_h.ctypes.data_as(C.POINTER(C.c_uint8))))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier(world)
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_total = max_over_ranks(sum(e2e_times), world, dev)
+    e2e_value = world * rays_per_step * args.steps / e2e_total / 1e6
+    h2d = N_RAYS * 32 + N_ANY * 32
+    d2h = N_RAYS * 8 + N_ANY * 1
+
+    # ---- roofline of the dominant kernel (closest hit)
+    hbm_peak, peak_kind = peaks()
+    counts = traversal_counts(g, rays)
+    bytes_per_ray = 32 + 8 + 64 * counts["nodes_per_ray"] + 48 * counts["slots_per_ray"]
+    closest_s = float(np.mean(closest_ms)) / 1e3
+    achieved = bytes_per_ray * N_RAYS / closest_s / 1e9
+    prof = profile_traffic()
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            rate, cores, dt, sample = cpu_oracle_rate(soup, rays, ra, args.cpu_rays)
+            cpu = {"value": round(rate, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
+                   "sample": sample}
+        line = {
+            "metric": "Mrays/s", "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(total_s * 1e3 / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(args, world),
+            "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
+                         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
+                         "traffic": prof.get("dram_bytes_per_launch") if prof else None,
+                         "peak_source": peak_kind,
+                         "kernel": "k_trace_closest",
+                         "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
+                         "nodes_per_ray": round(counts["nodes_per_ray"], 3),
+                         "slots_per_ray": round(counts["slots_per_ray"], 3),
+                         "kernel_ms": round(closest_s * 1e3, 4)},
+            "cpu_baseline": cpu,
+            "gpu_launches": 2 * args.steps,
+            "clocks": clk.summary(),
+            "closest_ms": round(float(np.mean(closest_ms)), 4),
+            "any_ms": round(float(np.mean(any_ms)), 4),
+            "hit_fraction": round(hit_frac, 4),
+            "bvh_build_ms": round(st["bvh_build_ms"], 1),
+            "bvh_nodes": st["bvh_nodes"],
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def traversal_counts(g, rays):
+    """Nodes visited and leaf slots tested per closest-hit ray, counted by the
+    instrumented traversal on a 256k-ray subsample."""
+    try:
+        return g.traversal_counts(np.ascontiguousarray(rays[:, : 1 << 18]))
+    except AttributeError:
+        return {"nodes_per_ray": float("nan"), "slots_per_ray": float("nan")}
+
+
+def profile_traffic():
+    """DRAM bytes per k_trace_closest launch from the committed ncu summary."""
+    p = ROOT / "profiles" / "trace_closest_soup1m.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except ValueError:
+            return None
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-rays", type=int, default=CPU_SAMPLE_RAYS)
+    ap.add_argument("--full-rays", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

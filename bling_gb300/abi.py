@@ -1,0 +1,98 @@
+"""ctypes mirrors of the C ABI structs declared in include/bling_gpu.h.
+
+The same layouts are consumed by the GPU library (libbling_gpu.so) and, in
+tests, by the CPU oracle; the descriptor is the flat hand-off that replaces
+bling's closure records (Primitive.hs:21-27, Reflection.hs:42).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+BANDS = 16
+F16 = C.c_float * BANDS
+M16 = C.c_float * 16
+
+BLING_OK = 0
+BLING_ERR_INVALID_ARG = -1
+BLING_ERR_OOM = -2
+BLING_ERR_CUDA = -3
+BLING_ERR_TIMEOUT = -4
+BLING_ERR_BOUNDS = -5
+BLING_ERR_STATE = -6
+
+MAT_MATTE, MAT_PLASTIC, MAT_METAL, MAT_GLASS = 0, 1, 2, 3
+SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_DISK, SHAPE_CYLINDER = 0, 1, 2, 3, 4
+LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE = 0, 1, 2
+FILTER_BOX, FILTER_GAUSS, FILTER_MITCHELL, FILTER_SINC, FILTER_TRIANGLE = 0, 1, 2, 3, 4
+
+
+class Opts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("flags", C.c_uint32), ("block_size", C.c_int32),
+                ("bvh_leaf_size", C.c_int32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("sigma", C.c_float), ("roughness", C.c_float),
+                ("ior", C.c_float), ("kd", F16), ("ks", F16), ("kt", F16), ("eta", F16),
+                ("k", F16)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("vertices", C.POINTER(C.c_float)), ("n_vertices", C.c_int64),
+                ("indices", C.POINTER(C.c_int32)), ("n_indices", C.c_int64),
+                ("normals", C.POINTER(C.c_float)), ("uvs", C.POINTER(C.c_float)),
+                ("material", C.c_int32), ("reserved", C.c_int32)]
+
+
+class ShapeDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("material", C.c_int32), ("params", C.c_float * 6),
+                ("o2w", M16), ("w2o", M16), ("emissive", C.c_int32), ("emission", F16)]
+
+
+class LightDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("spectrum", F16), ("vec", C.c_float * 3),
+                ("env", C.POINTER(C.c_float)), ("env_w", C.c_int32), ("env_h", C.c_int32),
+                ("w2l", M16), ("l2w", M16)]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("c2w", M16), ("c2w_inv", M16), ("r2c", M16), ("r2c_inv", M16),
+                ("lens_radius", C.c_float), ("focal_distance", C.c_float)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("meshes", C.POINTER(MeshDesc)), ("n_meshes", C.c_int32),
+                ("shapes", C.POINTER(ShapeDesc)), ("n_shapes", C.c_int32),
+                ("materials", C.POINTER(Material)), ("n_materials", C.c_int32),
+                ("lights", C.POINTER(LightDesc)), ("n_lights", C.c_int32),
+                ("prim_order", C.POINTER(C.c_int32)), ("camera", CameraDesc)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("strata_x", C.c_int32),
+                ("strata_y", C.c_int32), ("max_depth", C.c_int32), ("sample_depth", C.c_int32),
+                ("rr_depth", C.c_int32), ("filter_kind", C.c_int32),
+                ("filter_params", C.c_float * 4), ("seed", C.c_uint64)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("rays_closest", C.c_uint64), ("rays_any", C.c_uint64),
+                ("path_samples", C.c_uint64), ("nonfinite_drops", C.c_uint64),
+                ("bvh_build_ms", C.c_double), ("last_pass_ms", C.c_double),
+                ("bvh_nodes", C.c_uint64), ("bvh_leaf_prims", C.c_uint64),
+                ("device_bytes", C.c_uint64)]
+
+
+def fptr(a):
+    """float* of a C-contiguous float32 numpy array (or NULL for None)."""
+    if a is None:
+        return C.POINTER(C.c_float)()
+    assert a.dtype.name == "float32" and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def iptr(a):
+    if a is None:
+        return C.POINTER(C.c_int32)()
+    assert a.dtype.name == "int32" and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_int32))

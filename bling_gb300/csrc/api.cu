@@ -1,0 +1,651 @@
+// C ABI of the GB300 path-tracing core (include/bling_gpu.h).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/bling_gpu.h"
+#include "bvh.h"
+#include "integrator.h"
+#include "internal.h"
+#include "spectrum_tables.h"
+
+using namespace bgpu;
+
+struct bling_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;      // where work is enqueued
+  cudaStream_t own_stream = nullptr;  // the context's own stream
+  std::mutex mu;
+  std::string err;
+  bling_opts opts{};
+  // grow-only staging buffers for host-buffer queries
+  void* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  IntegratorWorkspace ws;
+};
+
+struct bling_scene {
+  bling_ctx* ctx = nullptr;
+  DevAccel accel{};
+  float4* d_nodes = nullptr;
+  float4* d_slots = nullptr;
+  DShape* d_shapes = nullptr;
+  DevShading shading{};
+  std::vector<void*> owned;  // other device allocations
+  bling_stats stats{};
+  int64_t n_nodes = 0, n_slots = 0;
+  int32_t root_ref = 0;
+};
+
+struct bling_film {
+  bling_ctx* ctx = nullptr;
+  int32_t width = 0, height = 0;
+  float* d_film = nullptr;  // width*height*4
+};
+
+namespace {
+
+int set_err(bling_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CK(ctx, call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return set_err((ctx), BLING_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                     __FILE__, __LINE__);                                               \
+  } while (0)
+
+int ensure_scratch(bling_ctx* c, size_t bytes) {
+  if (c->scratch_bytes >= bytes) return BLING_OK;
+  if (c->d_scratch) cudaFree(c->d_scratch);
+  c->d_scratch = nullptr;
+  c->scratch_bytes = 0;
+  size_t want = std::max(bytes, c->scratch_bytes * 2);
+  cudaError_t e = cudaMalloc(&c->d_scratch, want);
+  if (e != cudaSuccess) {
+    e = cudaMalloc(&c->d_scratch, bytes);
+    want = bytes;
+  }
+  if (e != cudaSuccess)
+    return set_err(c, e == cudaErrorMemoryAllocation ? BLING_ERR_OOM : BLING_ERR_CUDA,
+                   "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  c->scratch_bytes = want;
+  return BLING_OK;
+}
+
+template <class T>
+int upload(bling_ctx* c, std::vector<void*>& owned, const T* host, size_t count, T** out) {
+  *out = nullptr;
+  if (count == 0) return BLING_OK;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+  if (e != cudaSuccess)
+    return set_err(c, e == cudaErrorMemoryAllocation ? BLING_ERR_OOM : BLING_ERR_CUDA,
+                   "cudaMalloc(%zu): %s", count * sizeof(T), cudaGetErrorString(e));
+  owned.push_back(p);
+  CK(c, cudaMemcpyAsync(p, host, count * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+  *out = (T*)p;
+  return BLING_OK;
+}
+
+float fbits(uint32_t b) {
+  float f;
+  memcpy(&f, &b, 4);
+  return f;
+}
+
+// objectBounds (Shape.hs:295-311) and transBox (Transform.hs:281-292)
+void shape_world_bounds(const bling_shape_desc& s, float lo[3], float hi[3]) {
+  float olo[3], ohi[3];
+  const float* p = s.params;
+  switch (s.kind) {
+    case BLING_SHAPE_BOX:
+      for (int k = 0; k < 3; k++) {
+        olo[k] = p[k];
+        ohi[k] = p[3 + k];
+      }
+      break;
+    case BLING_SHAPE_CYLINDER:
+      olo[0] = olo[1] = -p[0];
+      ohi[0] = ohi[1] = p[0];
+      olo[2] = p[1];
+      ohi[2] = p[2];
+      break;
+    case BLING_SHAPE_DISK:
+      olo[0] = olo[1] = -p[1];
+      ohi[0] = ohi[1] = p[1];
+      olo[2] = ohi[2] = p[0];
+      break;
+    case BLING_SHAPE_QUAD:
+      olo[0] = -p[0];
+      olo[1] = -p[1];
+      ohi[0] = p[0];
+      ohi[1] = p[1];
+      olo[2] = ohi[2] = 0;
+      break;
+    default:
+      for (int k = 0; k < 3; k++) {
+        olo[k] = -p[0];
+        ohi[k] = p[0];
+      }
+  }
+  for (int k = 0; k < 3; k++) {
+    lo[k] = INFINITY;
+    hi[k] = -INFINITY;
+  }
+  for (int c = 0; c < 8; c++) {
+    V3 q{(c & 4) ? ohi[0] : olo[0], (c & 2) ? ohi[1] : olo[1], (c & 1) ? ohi[2] : olo[2]};
+    V3 w = transPoint(s.o2w, q);
+    float wv[3] = {w.x, w.y, w.z};
+    for (int k = 0; k < 3; k++) {
+      lo[k] = std::min(lo[k], wv[k]);
+      hi[k] = std::max(hi[k], wv[k]);
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int bling_abi_version(void) { return BLING_ABI_VERSION; }
+
+int bling_ctx_create(bling_ctx** out, const bling_opts* opts) {
+  if (!out) return BLING_ERR_INVALID_ARG;
+  *out = nullptr;
+  std::unique_ptr<bling_ctx> c(new bling_ctx());
+  if (opts) c->opts = *opts;
+  c->device = c->opts.device;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev <= 0) {
+    // keep the context so the caller can read the message
+    set_err(c.get(), BLING_ERR_CUDA, "no usable CUDA device: %s", cudaGetErrorString(e));
+    *out = c.release();
+    return BLING_ERR_CUDA;
+  }
+  if (c->device < 0 || c->device >= ndev) {
+    set_err(c.get(), BLING_ERR_INVALID_ARG, "device %d out of range (%d devices)", c->device, ndev);
+    *out = c.release();
+    return BLING_ERR_INVALID_ARG;
+  }
+  e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  c->stream = c->own_stream;
+  if (e != cudaSuccess) {
+    set_err(c.get(), BLING_ERR_CUDA, "stream creation failed: %s", cudaGetErrorString(e));
+    *out = c.release();
+    return BLING_ERR_CUDA;
+  }
+  *out = c.release();
+  return BLING_OK;
+}
+
+void bling_ctx_destroy(bling_ctx* c) {
+  if (!c) return;
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    if (c->own_stream) {
+      cudaSetDevice(c->device);
+      cudaStreamSynchronize(c->stream);
+      cudaStreamSynchronize(c->own_stream);
+      cudaStreamDestroy(c->own_stream);
+    }
+    if (c->d_scratch) cudaFree(c->d_scratch);
+    integrator_workspace_free(c->ws);
+  }
+  delete c;
+}
+
+const char* bling_last_error(bling_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int bling_ctx_set_stream(bling_ctx* c, void* stream) {
+  if (!c) return BLING_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!c->own_stream) return set_err(c, BLING_ERR_STATE, "context has no device");
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return BLING_OK;
+}
+
+int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** out) {
+  if (!c || !d || !out) return BLING_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  *out = nullptr;
+  if (!c->stream) return set_err(c, BLING_ERR_STATE, "context has no device");
+  CK(c, cudaSetDevice(c->device));
+  auto t0 = std::chrono::steady_clock::now();
+  // ---- validate (mkTriangleMesh checks, TriangleMesh.hs:48-55)
+  if (d->n_meshes < 0 || d->n_shapes < 0 || d->n_materials < 0 || d->n_lights < 0)
+    return set_err(c, BLING_ERR_INVALID_ARG, "negative counts");
+  for (int i = 0; i < d->n_meshes; i++) {
+    const bling_mesh_desc& m = d->meshes[i];
+    if (m.n_indices % 3 != 0)
+      return set_err(c, BLING_ERR_INVALID_ARG, "mesh %d: number of indices must be multiple of 3", i);
+    if (m.n_indices > 0 && (!m.indices || !m.vertices))
+      return set_err(c, BLING_ERR_INVALID_ARG, "mesh %d: null arrays", i);
+    for (int64_t k = 0; k < m.n_indices; k++) {
+      if (m.indices[k] < 0) return set_err(c, BLING_ERR_INVALID_ARG, "mesh %d: contains negative indices", i);
+      if (m.indices[k] >= m.n_vertices)
+        return set_err(c, BLING_ERR_INVALID_ARG, "mesh %d: contains out of bounds indices", i);
+    }
+    if (m.material < 0 || m.material >= d->n_materials)
+      return set_err(c, BLING_ERR_INVALID_ARG, "mesh %d: material %d out of range", i, m.material);
+  }
+  for (int i = 0; i < d->n_shapes; i++) {
+    const bling_shape_desc& s = d->shapes[i];
+    if (s.kind < BLING_SHAPE_SPHERE || s.kind > BLING_SHAPE_CYLINDER)
+      return set_err(c, BLING_ERR_INVALID_ARG, "shape %d: unknown kind %d", i, s.kind);
+    if (s.material < 0 || s.material >= d->n_materials)
+      return set_err(c, BLING_ERR_INVALID_ARG, "shape %d: material %d out of range", i, s.material);
+  }
+  std::vector<int32_t> order;
+  if (d->prim_order) {
+    order.assign(d->prim_order, d->prim_order + d->n_meshes + d->n_shapes);
+    std::vector<char> seen_m(d->n_meshes, 0), seen_s(d->n_shapes, 0);
+    for (int32_t v : order) {
+      if (v >= 0 ? v >= d->n_meshes : ~v >= d->n_shapes)
+        return set_err(c, BLING_ERR_INVALID_ARG, "prim_order entry %d out of range", v);
+      char& s = v >= 0 ? seen_m[v] : seen_s[~v];
+      if (s) return set_err(c, BLING_ERR_INVALID_ARG, "prim_order entry %d repeated", v);
+      s = 1;
+    }
+  } else {
+    for (int i = 0; i < d->n_meshes; i++) order.push_back(i);
+    for (int i = 0; i < d->n_shapes; i++) order.push_back(~i);
+  }
+  // ---- primitive list in primitive-ID order
+  int64_t n_prims = 0;
+  for (int32_t v : order) n_prims += v >= 0 ? d->meshes[v].n_indices / 3 : 1;
+  if (n_prims == 0) return set_err(c, BLING_ERR_INVALID_ARG, "scene has no primitives");
+  if (n_prims >= (int64_t(1) << 27)) return set_err(c, BLING_ERR_INVALID_ARG, "too many primitives");
+  std::vector<float> lo(3 * n_prims), hi(3 * n_prims);
+  // per primitive: kind/owner (mesh id or ~shape id) and triangle number
+  std::vector<int32_t> prim_owner(n_prims), prim_tri(n_prims);
+  {
+    int64_t p = 0;
+    for (int32_t v : order) {
+      if (v >= 0) {
+        const bling_mesh_desc& m = d->meshes[v];
+        for (int64_t t = 0; t < m.n_indices / 3; t++, p++) {
+          const float* a = m.vertices + 3 * m.indices[3 * t];
+          const float* b = m.vertices + 3 * m.indices[3 * t + 1];
+          const float* cc = m.vertices + 3 * m.indices[3 * t + 2];
+          for (int k = 0; k < 3; k++) {
+            lo[3 * p + k] = std::min(std::min(a[k], b[k]), cc[k]);
+            hi[3 * p + k] = std::max(std::max(a[k], b[k]), cc[k]);
+          }
+          prim_owner[p] = v;
+          prim_tri[p] = (int32_t)t;
+        }
+      } else {
+        shape_world_bounds(d->shapes[~v], &lo[3 * p], &hi[3 * p]);
+        prim_owner[p] = v;
+        prim_tri[p] = 0;
+        p++;
+      }
+    }
+  }
+  BvhBuildInput bi;
+  bi.n = n_prims;
+  bi.lo = lo.data();
+  bi.hi = hi.data();
+  bi.max_leaf = c->opts.bvh_leaf_size > 0 ? c->opts.bvh_leaf_size : 4;
+  BvhBuildOutput bo;
+  if (build_bvh(bi, bo) != 0) return set_err(c, BLING_ERR_INVALID_ARG, "BVH build failed (depth bound)");
+  // ---- leaf slots
+  size_t n_slots = bo.slot_prim.size();
+  std::vector<float> slots(12 * n_slots, 0.0f);
+  for (size_t s = 0; s < n_slots; s++) {
+    int32_t prim = bo.slot_prim[s];
+    float* o = &slots[12 * s];
+    int32_t flags = bo.slot_last[s] ? SLOT_LAST : 0;
+    int32_t v = prim_owner[prim];
+    if (v >= 0) {
+      const bling_mesh_desc& m = d->meshes[v];
+      int64_t t = prim_tri[prim];
+      const float* p1 = m.vertices + 3 * m.indices[3 * t];
+      const float* p2 = m.vertices + 3 * m.indices[3 * t + 1];
+      const float* p3 = m.vertices + 3 * m.indices[3 * t + 2];
+      // e1 = p2 - p1, e2 = p3 - p1 (one binary32 subtraction each, as the reference)
+      o[0] = p1[0];
+      o[1] = p1[1];
+      o[2] = p1[2];
+      o[3] = p2[0] - p1[0];
+      o[4] = p2[1] - p1[1];
+      o[5] = p2[2] - p1[2];
+      o[6] = p3[0] - p1[0];
+      o[7] = p3[1] - p1[1];
+      o[8] = p3[2] - p1[2];
+    } else {
+      int32_t si = ~v;
+      memcpy(&o[0], &si, 4);
+      flags |= SLOT_SHAPE;
+    }
+    memcpy(&o[9], &prim, 4);
+    memcpy(&o[10], &flags, 4);
+  }
+  std::unique_ptr<bling_scene> S(new bling_scene());
+  S->ctx = c;
+  int rc;
+  if ((rc = upload(c, S->owned, (const float4*)bo.nodes.data(), bo.nodes.size() / 4, &S->d_nodes)))
+    return rc;
+  if ((rc = upload(c, S->owned, (const float4*)slots.data(), slots.size() / 4, &S->d_slots)))
+    return rc;
+  // ---- shapes on the device
+  std::vector<DShape> shapes(d->n_shapes);
+  std::vector<int32_t> shape_light(d->n_shapes, -1);
+  {
+    int32_t nl = d->n_lights;
+    for (int32_t v : order)  // geometric lights follow the user lights, in primitive order
+      if (v < 0 && d->shapes[~v].emissive) shape_light[~v] = nl++;
+  }
+  for (int i = 0; i < d->n_shapes; i++) {
+    const bling_shape_desc& s = d->shapes[i];
+    DShape& o = shapes[i];
+    memset(&o, 0, sizeof o);
+    o.kind = s.kind;
+    o.material = s.material;
+    o.light_id = shape_light[i];
+    for (int k = 0; k < 6; k++) o.p[k] = s.params[k];
+    memcpy(o.o2w, s.o2w, 64);
+    memcpy(o.w2o, s.w2o, 64);
+  }
+  if ((rc = upload(c, S->owned, shapes.data(), shapes.size(), &S->d_shapes))) return rc;
+  S->accel.nodes = S->d_nodes;
+  S->accel.slots = S->d_slots;
+  S->accel.shapes = S->d_shapes;
+  S->accel.root_ref = bo.root_ref;
+  S->accel.n_shapes = d->n_shapes;
+  S->accel.n_prims = n_prims;
+  S->n_nodes = (int64_t)bo.nodes.size() / 16;
+  S->n_slots = (int64_t)n_slots;
+  // ---- shading data for the path integrator
+  if ((rc = integrator_upload_scene(c->stream, *d, order, prim_owner, prim_tri, shapes, shape_light,
+                                    S->owned, S->shading, c->err)))
+    return rc;
+  CK(c, cudaStreamSynchronize(c->stream));
+  auto t1 = std::chrono::steady_clock::now();
+  S->stats.bvh_build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  S->stats.bvh_nodes = (uint64_t)S->n_nodes;
+  S->stats.bvh_leaf_prims = (uint64_t)n_slots;
+  size_t bytes = bo.nodes.size() * 4 + slots.size() * 4 + shapes.size() * sizeof(DShape);
+  S->stats.device_bytes = bytes + S->shading.bytes;
+  *out = S.release();
+  return BLING_OK;
+}
+
+void bling_scene_destroy(bling_scene* s) {
+  if (!s) return;
+  bling_ctx* c = s->ctx;
+  {
+    std::lock_guard<std::mutex> g(c->mu);
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (void* p : s->owned) cudaFree(p);
+  }
+  delete s;
+}
+
+int bling_scene_stats(bling_scene* s, bling_stats* out) {
+  if (!s || !out) return BLING_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> g(s->ctx->mu);
+  *out = s->stats;
+  return BLING_OK;
+}
+
+int bling_trace_closest_device(bling_scene* s, const float* d_rays, size_t n, float* d_t,
+                               int32_t* d_prim, float* d_b1b2) {
+  if (!s || (n > 0 && (!d_rays || !d_t || !d_prim))) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = s->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, launch_trace_closest(s->accel, d_rays, (int64_t)n, d_t, d_prim, d_b1b2, c->opts.block_size,
+                             c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  s->stats.rays_closest += n;
+  return BLING_OK;
+}
+
+int bling_trace_any_device(bling_scene* s, const float* d_rays, size_t n, uint8_t* d_hit) {
+  if (!s || (n > 0 && (!d_rays || !d_hit))) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = s->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, launch_trace_any(s->accel, d_rays, (int64_t)n, d_hit, c->opts.block_size, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  s->stats.rays_any += n;
+  return BLING_OK;
+}
+
+int bling_trace_closest(bling_scene* s, const float* rays, size_t n, float* t, int32_t* prim,
+                        float* b1b2) {
+  if (!s || (n > 0 && (!rays || !t || !prim))) return BLING_ERR_INVALID_ARG;
+  if (n == 0) return BLING_OK;
+  bling_ctx* c = s->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  size_t rb = 8 * n * sizeof(float), tb = n * 4, pb = n * 4, bb = b1b2 ? 8 * n : 0;
+  int rc = ensure_scratch(c, rb + tb + pb + bb);
+  if (rc) return rc;
+  char* base = (char*)c->d_scratch;
+  float* d_r = (float*)base;
+  float* d_t = (float*)(base + rb);
+  int32_t* d_p = (int32_t*)(base + rb + tb);
+  float* d_b = b1b2 ? (float*)(base + rb + tb + pb) : nullptr;
+  CK(c, cudaMemcpyAsync(d_r, rays, rb, cudaMemcpyHostToDevice, c->stream));
+  CK(c, launch_trace_closest(s->accel, d_r, (int64_t)n, d_t, d_p, d_b, c->opts.block_size, c->stream));
+  CK(c, cudaMemcpyAsync(t, d_t, tb, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(prim, d_p, pb, cudaMemcpyDeviceToHost, c->stream));
+  if (b1b2) CK(c, cudaMemcpyAsync(b1b2, d_b, bb, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  s->stats.rays_closest += n;
+  return BLING_OK;
+}
+
+int bling_trace_any(bling_scene* s, const float* rays, size_t n, uint8_t* hit) {
+  if (!s || (n > 0 && (!rays || !hit))) return BLING_ERR_INVALID_ARG;
+  if (n == 0) return BLING_OK;
+  bling_ctx* c = s->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  size_t rb = 8 * n * sizeof(float);
+  int rc = ensure_scratch(c, rb + n);
+  if (rc) return rc;
+  float* d_r = (float*)c->d_scratch;
+  uint8_t* d_h = (uint8_t*)c->d_scratch + rb;
+  CK(c, cudaMemcpyAsync(d_r, rays, rb, cudaMemcpyHostToDevice, c->stream));
+  CK(c, launch_trace_any(s->accel, d_r, (int64_t)n, d_h, c->opts.block_size, c->stream));
+  CK(c, cudaMemcpyAsync(hit, d_h, n, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  s->stats.rays_any += n;
+  return BLING_OK;
+}
+
+int bling_trace_counts(bling_scene* s, const float* rays, size_t n, uint64_t* nodes,
+                       uint64_t* prims) {
+  if (!s || !nodes || !prims || (n > 0 && !rays)) return BLING_ERR_INVALID_ARG;
+  *nodes = *prims = 0;
+  if (n == 0) return BLING_OK;
+  bling_ctx* c = s->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  size_t rb = 8 * n * sizeof(float);
+  int rc = ensure_scratch(c, rb + 16);
+  if (rc) return rc;
+  float* d_r = (float*)c->d_scratch;
+  unsigned long long* d_tot = (unsigned long long*)((char*)c->d_scratch + rb);
+  CK(c, cudaMemcpyAsync(d_r, rays, rb, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemsetAsync(d_tot, 0, 16, c->stream));
+  CK(c, launch_trace_counts(s->accel, d_r, (int64_t)n, d_tot, c->stream));
+  unsigned long long tot[2];
+  CK(c, cudaMemcpyAsync(tot, d_tot, 16, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  *nodes = tot[0];
+  *prims = tot[1];
+  return BLING_OK;
+}
+
+// ---------------------------------------------------------------- films
+int bling_film_create(bling_ctx* c, int32_t w, int32_t h, bling_film** out) {
+  if (!c || !out || w <= 0 || h <= 0 || (int64_t)w * h > (int64_t(1) << 28)) return BLING_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> g(c->mu);
+  *out = nullptr;
+  CK(c, cudaSetDevice(c->device));
+  std::unique_ptr<bling_film> f(new bling_film());
+  f->ctx = c;
+  f->width = w;
+  f->height = h;
+  size_t bytes = (size_t)w * h * 4 * sizeof(float);
+  cudaError_t e = cudaMalloc(&f->d_film, bytes);
+  if (e != cudaSuccess)
+    return set_err(c, e == cudaErrorMemoryAllocation ? BLING_ERR_OOM : BLING_ERR_CUDA,
+                   "film allocation: %s", cudaGetErrorString(e));
+  e = cudaMemsetAsync(f->d_film, 0, bytes, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    cudaFree(f->d_film);
+    return set_err(c, BLING_ERR_CUDA, "film clear: %s", cudaGetErrorString(e));
+  }
+  *out = f.release();
+  return BLING_OK;
+}
+
+void bling_film_destroy(bling_film* f) {
+  if (!f) return;
+  {
+    std::lock_guard<std::mutex> g(f->ctx->mu);
+    cudaSetDevice(f->ctx->device);
+    cudaStreamSynchronize(f->ctx->stream);
+    cudaFree(f->d_film);
+  }
+  delete f;
+}
+
+int bling_film_clear(bling_film* f) {
+  if (!f) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = f->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaMemsetAsync(f->d_film, 0, (size_t)f->width * f->height * 16, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return BLING_OK;
+}
+
+int bling_film_read(bling_film* f, float* host) {
+  if (!f || !host) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = f->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaMemcpyAsync(host, f->d_film, (size_t)f->width * f->height * 16, cudaMemcpyDeviceToHost,
+                        c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return BLING_OK;
+}
+
+int bling_film_resolve(bling_film* f, float* host_rgb) {
+  if (!f || !host_rgb) return BLING_ERR_INVALID_ARG;
+  size_t np = (size_t)f->width * f->height;
+  std::vector<float> px(4 * np);
+  int rc = bling_film_read(f, px.data());
+  if (rc) return rc;
+  // getPixel with no splats (Image.hs:302-315), xyzToRgb (Spectrum.hs:162-168)
+  for (size_t i = 0; i < np; i++) {
+    float w = px[4 * i], x = px[4 * i + 1], y = px[4 * i + 2], z = px[4 * i + 3];
+    float r = 0, gg = 0, b = 0;
+    if (w != 0) {
+      float wi = 1.0f / w;
+      x = x * wi;
+      y = y * wi;
+      z = z * wi;
+    } else {
+      x = y = z = 0;
+    }
+    r = 3.240479f * x - 1.537150f * y - 0.498535f * z;
+    gg = (-0.969256f) * x + 1.875991f * y + 0.041556f * z;
+    b = 0.055648f * x - 0.204043f * y + 1.057311f * z;
+    host_rgb[3 * i] = r;
+    host_rgb[3 * i + 1] = gg;
+    host_rgb[3 * i + 2] = b;
+  }
+  return BLING_OK;
+}
+
+int bling_render_pass(bling_scene* s, bling_film* f, const bling_render_params* p, uint64_t pass) {
+  if (!s || !f || !p) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = s->ctx;
+  if (f->ctx != c) return set_err(c, BLING_ERR_INVALID_ARG, "film and scene belong to different contexts");
+  if (p->width != f->width || p->height != f->height)
+    return set_err(c, BLING_ERR_INVALID_ARG, "render size %dx%d does not match film %dx%d", p->width,
+                   p->height, f->width, f->height);
+  if (p->strata_x <= 0 || p->strata_y <= 0 || p->max_depth < 0 || p->sample_depth < 0 ||
+      p->strata_x * p->strata_y > 4096)
+    return set_err(c, BLING_ERR_INVALID_ARG, "invalid sampler/integrator parameters");
+  if (p->filter_kind < BLING_FILTER_BOX || p->filter_kind > BLING_FILTER_TRIANGLE)
+    return set_err(c, BLING_ERR_INVALID_ARG, "unknown filter kind %d", p->filter_kind);
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  PassResult res{};
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = integrator_render_pass(c->stream, s->accel, s->shading, *p, pass, f->d_film, f->width,
+                                  f->height, c->ws, res, c->err);
+  if (rc) return rc;
+  auto t1 = std::chrono::steady_clock::now();
+  s->stats.last_pass_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  s->stats.rays_closest += res.rays_closest;
+  s->stats.rays_any += res.rays_any;
+  s->stats.path_samples += res.path_samples;
+  s->stats.nonfinite_drops += res.nonfinite;
+  return BLING_OK;
+}
+
+// ---------------------------------------------------------------- host helpers
+void bling_rgb_to_spectrum(int32_t illum, float r, float g, float b, float out[BLING_BANDS]) {
+  const uint32_t* t = illum ? BLING_RGB_ILLUM_BITS : BLING_RGB_REFL_BITS;
+  auto B = [&](int which, int i) { return fbits(t[which * 16 + i]); };
+  for (int i = 0; i < 16; i++) {
+    float w = B(BLING_BASIS_WHITE, i), cy = B(BLING_BASIS_CYAN, i), m = B(BLING_BASIS_MAGENTA, i),
+          y = B(BLING_BASIS_YELLOW, i), rr = B(BLING_BASIS_RED, i), gg = B(BLING_BASIS_GREEN, i),
+          bb = B(BLING_BASIS_BLUE, i);
+    float v;
+    // rgbToSpectrum (Spectrum.hs:146-159), band by band
+    if (r <= g && r <= b)
+      v = w * r + (g <= b ? cy * (g - r) + bb * (b - g) : cy * (b - r) + gg * (g - b));
+    else if (g <= r && g <= b)
+      v = w * g + (r <= b ? m * (r - g) + bb * (b - r) : m * (b - g) + rr * (r - b));
+    else
+      v = w * b + (r <= b ? y * (r - b) + gg * (g - r) : y * (g - b) + rr * (r - g));
+    out[i] = v;
+  }
+}
+
+void bling_spectrum_to_xyz(const float s[BLING_BANDS], float xyz[3]) {
+  float a = 0, b = 0, cc = 0;
+  for (int i = 0; i < 16; i++) {
+    a = a + fbits(BLING_CIE_X_BITS[i]) * s[i];
+    b = b + fbits(BLING_CIE_Y_BITS[i]) * s[i];
+    cc = cc + fbits(BLING_CIE_Z_BITS[i]) * s[i];
+  }
+  float ys = fbits(BLING_CIE_Y_SUM_BITS);
+  xyz[0] = a / ys;
+  xyz[1] = b / ys;
+  xyz[2] = cc / ys;
+}
+
+}  // extern "C"

@@ -1,0 +1,86 @@
+// Wavefront path integrator: host-side interface (integrator.cu).
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/bling_gpu.h"
+#include "internal.h"
+
+namespace bgpu {
+
+struct DMaterial {
+  int kind;
+  float sigma, rough, ior;
+  float kd[16], ks[16], kt[16], eta[16], k[16];
+};
+
+struct DMesh {
+  const float* verts;   // 3 per vertex (world space)
+  const int32_t* idx;   // 3 per triangle
+  const float* normals; // 3 per vertex or null
+  const float* uvs;     // 2 per vertex or null
+  int32_t material;
+  int32_t pad;
+};
+
+enum { DLIGHT_DIRECTIONAL = 0, DLIGHT_POINT = 1, DLIGHT_INFINITE = 2, DLIGHT_AREA = 100 };
+
+struct DLight {
+  int kind;
+  int shape;   // area lights
+  int env_w, env_h;
+  float spec[16];
+  float vec[3];
+  float w2l[16], l2w[16];
+  const float* env;        // env_h * env_w * 16
+  const float* cond_func;  // env_h * env_w
+  const float* cond_cdf;   // env_h * (env_w + 1)
+  const float* cond_int;   // env_h
+  const float* marg_cdf;   // env_h + 1
+  float marg_int;
+  float pad;
+};
+
+struct DevShading {
+  const DMaterial* materials;
+  const DMesh* meshes;
+  const int2* prim_info;   // (owner, triangle): owner >= 0 mesh, < 0 ~shape
+  const float* shape_emission;  // 16 per shape
+  const DLight* lights;
+  int32_t n_lights;
+  int32_t n_materials;
+  bling_camera_desc camera;
+  size_t bytes;
+};
+
+struct PassResult {
+  uint64_t rays_closest, rays_any, path_samples, nonfinite;
+};
+
+// Device buffers reused across passes (grow-only), owned by a context.
+struct IntegratorWorkspace {
+  size_t capacity = 0;  // path slots
+  float* T = nullptr;   // 16 * capacity
+  float* L = nullptr;   // 16 * capacity
+  float* ray = nullptr; // 7 * capacity: o.xyz, d.xyz, tmin
+  float* hit_t = nullptr;
+  int32_t* hit_prim = nullptr;
+  float* hit_b = nullptr;  // 2 * capacity
+  int32_t* queue[2] = {nullptr, nullptr};
+  unsigned long long* counters = nullptr;  // [0..1] queue sizes, [2] closest, [3] any, [4] nonfinite
+  float* filter = nullptr;                  // 256 table
+};
+
+int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
+                            const std::vector<int32_t>& order, const std::vector<int32_t>& prim_owner,
+                            const std::vector<int32_t>& prim_tri, const std::vector<DShape>& shapes,
+                            const std::vector<int32_t>& shape_light, std::vector<void*>& owned,
+                            DevShading& out, std::string& err);
+
+int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S,
+                           const bling_render_params& p, uint64_t pass, float* d_film, int fw,
+                           int fh, IntegratorWorkspace& ws, PassResult& res, std::string& err);
+
+void integrator_workspace_free(IntegratorWorkspace& ws);
+
+}  // namespace bgpu

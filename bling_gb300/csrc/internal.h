@@ -1,0 +1,40 @@
+// Internal structures shared by the C ABI (api.cu) and the kernel files.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dshape.cuh"
+
+namespace bgpu {
+
+// leaf slot flags (third float4 .z of a slot, as int bits)
+enum : int { SLOT_LAST = 1, SLOT_SHAPE = 2 };
+
+// Device view of a scene's acceleration structure.
+//   nodes: 4 float4 per internal node (layout in bvh.h)
+//   slots: 3 float4 per leaf slot:
+//     triangle: (p1.xyz, e1.x) (e1.yz, e2.xy) (e2.z, prim, flags, 0)
+//               with e1 = p2 - p1, e2 = p3 - p1 rounded exactly as the
+//               reference computes them (TriangleMesh.hs:157-158, 169)
+//     shape:    (shape index, 0, 0, 0) (0...) (0, prim, flags|SLOT_SHAPE, 0)
+struct DevAccel {
+  const float4* nodes;
+  const float4* slots;
+  const DShape* shapes;
+  int32_t root_ref;
+  int32_t n_shapes;
+  int64_t n_prims;
+};
+
+// Launchers (kernels_trace.cu); all enqueue on `stream` and return the
+// launch status.
+cudaError_t launch_trace_closest(const DevAccel& A, const float* d_rays, int64_t n, float* d_t,
+                                 int32_t* d_prim, float* d_b1b2, int block, cudaStream_t stream);
+// instrumented closest-hit traversal: adds node visits and leaf-slot tests
+// into d_totals[0..1]
+cudaError_t launch_trace_counts(const DevAccel& A, const float* d_rays, int64_t n,
+                                unsigned long long* d_totals, cudaStream_t stream);
+cudaError_t launch_trace_any(const DevAccel& A, const float* d_rays, int64_t n, uint8_t* d_hit,
+                             int block, cudaStream_t stream);
+
+}  // namespace bgpu

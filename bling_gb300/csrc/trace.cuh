@@ -1,0 +1,145 @@
+// BVH traversal on the device: closest hit and any hit.
+//
+// Replaces the reference's kd-tree walk `traverse`/`traverse'` with the leaf
+// fold `nearest'` (Primitive/KdTree.hs:210-246, Primitive.hs:29-43).  The
+// answer is the reference's: the primitive with the smallest hit distance in
+// [tmin, tmax] computed with the reference's own intersection arithmetic, and
+// among equal distances the one with the larger primitive ID (a later
+// primitive with an equal t replaces the earlier one in the fold, because the
+// intersection tests reject only t > tmax, TriangleMesh.hs:146,166).
+//
+// Node boxes are tested with the robust form (lo - o) * (1/d), whose relative
+// error is a few ulp, and the box interval is widened by a relative 2^-16 so
+// that a primitive whose reference-arithmetic t lies on a box face is never
+// pruned.
+#pragma once
+#include "dmath.cuh"
+#include "dshape.cuh"
+#include "internal.h"
+
+namespace bgpu {
+
+constexpr int kTraversalStack = 64;
+constexpr float kBoxSlack = 1.0f / 65536.0f;
+
+// triangleIntersect / triangleIntersects (TriangleMesh.hs:140-181) on a
+// pre-gathered slot (p1, e1, e2)
+__device__ __forceinline__ bool triTest(const float4 s0, const float4 s1, const float4 s2,
+                                        const Ray& r, float tmax, float& t, float& b1o,
+                                        float& b2o) {
+  V3 p1{s0.x, s0.y, s0.z}, e1{s0.w, s1.x, s1.y}, e2{s1.z, s1.w, s2.x};
+  V3 s1v = cross(r.d, e2);
+  float divisor = dot(s1v, e1);
+  if (divisor == 0) return false;
+  float invDiv = 1.0f / divisor;
+  V3 d = r.o - p1;
+  float b1 = dot(d, s1v) * invDiv;
+  if (b1 < 0 || b1 > 1) return false;
+  V3 s2v = cross(d, e1);
+  float b2 = dot(r.d, s2v) * invDiv;
+  if (b2 < 0 || b1 + b2 > 1) return false;
+  float tt = dot(e2, s2v) * invDiv;
+  if (tt < r.tmin || tt > tmax) return false;
+  t = tt;
+  b1o = b1;
+  b2o = b2;
+  return true;
+}
+
+__device__ __forceinline__ void boxInterval(float lox, float hix, float loy, float hiy, float loz,
+                                            float hiz, const V3& o, const V3& inv, float& tn,
+                                            float& tf) {
+  float x0 = (lox - o.x) * inv.x, x1 = (hix - o.x) * inv.x;
+  float y0 = (loy - o.y) * inv.y, y1 = (hiy - o.y) * inv.y;
+  float z0 = (loz - o.z) * inv.z, z1 = (hiz - o.z) * inv.z;
+  float n = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
+  float f = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+  tn = n - fabsf(n) * kBoxSlack;
+  tf = f + fabsf(f) * kBoxSlack;
+}
+
+// work counters of one traversal (the instrumented variant only; the
+// reference's dbgTraverse counts the same things, Primitive/KdTree.hs:252-281)
+struct TraversalCounts {
+  unsigned nodes;  // internal nodes visited (64-byte node reads)
+  unsigned slots;  // leaf slots tested (48-byte primitive reads)
+};
+
+// Returns true on a hit.  ANY: stop at the first primitive hit in
+// [tmin, tmax].  Otherwise: best_t/best_prim/b1/b2 hold the closest hit.
+// COUNT: also accumulate node visits and primitive tests into *cnt.
+template <bool ANY, bool COUNT = false>
+__device__ __forceinline__ bool traverse(const DevAccel& A, const Ray& r, float& best_t,
+                                         int& best_prim, float& bb1, float& bb2,
+                                         TraversalCounts* cnt = nullptr) {
+  V3 inv{1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z};
+  best_t = r.tmax;
+  best_prim = -1;
+  bb1 = bb2 = 0.0f;
+  int stack[kTraversalStack];
+  int sp = 0;
+  int cur = A.root_ref;
+  for (;;) {
+    if (cur >= 0) {
+      if (COUNT) cnt->nodes++;
+      const float4* nd = A.nodes + 4 * (size_t)cur;
+      float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2);
+      float4 refs = __ldg(nd + 3);
+      float n0, f0, n1, f1;
+      boxInterval(a.x, a.y, a.z, a.w, c.x, c.y, r.o, inv, n0, f0);
+      boxInterval(b.x, b.y, b.z, b.w, c.z, c.w, r.o, inv, n1, f1);
+      bool h0 = fmaxf(n0, r.tmin) <= fminf(f0, best_t);
+      bool h1 = fmaxf(n1, r.tmin) <= fminf(f1, best_t);
+      int r0 = __float_as_int(refs.x), r1 = __float_as_int(refs.y);
+      if (h0 && h1) {
+        bool swap = n1 < n0;
+        cur = swap ? r1 : r0;
+        stack[sp++] = swap ? r0 : r1;
+        continue;
+      }
+      if (h0 || h1) {
+        cur = h0 ? r0 : r1;
+        continue;
+      }
+    } else {
+      int slot = ~cur;
+      for (;;) {
+        if (COUNT) cnt->slots++;
+        const float4* sl = A.slots + 3 * (size_t)slot;
+        float4 s0 = __ldg(sl), s1 = __ldg(sl + 1), s2 = __ldg(sl + 2);
+        int flags = __float_as_int(s2.z);
+        int prim = __float_as_int(s2.y);
+        bool hit;
+        float t = 0, b1 = 0, b2 = 0;
+        if (!(flags & SLOT_SHAPE)) {
+          hit = triTest(s0, s1, s2, r, best_t, t, b1, b2);
+        } else {
+          const DShape& sh = A.shapes[__float_as_int(s0.x)];
+          Ray ro = transRay(sh.w2o, Ray{r.o, r.d, r.tmin, ANY ? r.tmax : best_t});
+          if (ANY) {
+            hit = shapeIntersects(sh, ro);
+          } else {
+            float e;
+            hit = shapeIntersect<false>(sh, ro, t, e, nullptr);
+          }
+        }
+        if (hit) {
+          if (ANY) return true;
+          if (t < best_t || prim > best_prim) {
+            best_t = t;
+            best_prim = prim;
+            bb1 = b1;
+            bb2 = b2;
+          }
+        }
+        if (flags & SLOT_LAST) break;
+        slot++;
+      }
+    }
+    if (sp == 0) break;
+    cur = stack[--sp];
+  }
+  return best_prim >= 0;
+}
+
+}  // namespace bgpu

@@ -1,0 +1,267 @@
+"""Flat scene description and the synthetic workloads the core is measured on.
+
+A :class:`Scene` is the host-side record a bling front end (the ``.bling``
+parser, ``B/IO/RenderJob.hs``, or the DSL, ``Graphics/Bling.hs``) fills in
+alongside its closure-based ``Scene``: meshes, analytic shapes with their
+transforms, materials, lights and the camera, in primitive-list order.  It
+lowers to the ``bling_scene_desc`` of ``include/bling_gpu.h``.
+
+Workloads (all seeded, synthetic):
+
+* :func:`cornell_room` -- the Cornell-style room: a unit-cube room of 5 quads
+  (10 triangles), a 0.25 x 0.25 ceiling quad light of RGB radiance 15, two
+  white matte boxes 0.3 and 0.6 tall rotated +-18 degrees about y, pinhole
+  camera with a 40 degree field of view.
+* :func:`triangle_soup` / :func:`soup_rays` -- the ray-cast microbenchmark:
+  uniform-random triangles in [-1,1]^3 with edge lengths ~U(0.005, 0.05),
+  rays from a sphere of radius 3 towards random points of the unit ball.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from . import transform as xf
+from .spectrum import constant, rgb_to_spectrum
+
+F = np.float32
+
+
+@dataclass
+class Mesh:
+    vertices: np.ndarray          # (n, 3) float32, world space
+    indices: np.ndarray           # (m,) int32, multiple of 3
+    material: int
+    normals: np.ndarray | None = None
+    uvs: np.ndarray | None = None
+
+
+@dataclass
+class Shape:
+    kind: int
+    params: tuple
+    o2w: xf.Transform
+    material: int
+    emission: np.ndarray | None = None
+
+
+@dataclass
+class Light:
+    kind: int
+    spectrum: np.ndarray = field(default_factory=lambda: constant(0))
+    vec: tuple = (0.0, 0.0, 0.0)
+    env: np.ndarray | None = None  # (h, w, 16) float32
+    w2l: xf.Transform | None = None
+
+
+@dataclass
+class Scene:
+    materials: list = field(default_factory=list)
+    meshes: list = field(default_factory=list)
+    shapes: list = field(default_factory=list)
+    lights: list = field(default_factory=list)
+    prim_order: list | None = None
+    camera: abi.CameraDesc | None = None
+
+    # --- builders -------------------------------------------------------
+    def add_material(self, kind, kd=None, ks=None, kt=None, eta=None, k=None, sigma=0.0,
+                     roughness=0.0, ior=1.5) -> int:
+        m = abi.Material()
+        m.kind, m.sigma, m.roughness, m.ior = kind, sigma, roughness, ior
+        for name, v in (("kd", kd), ("ks", ks), ("kt", kt), ("eta", eta), ("k", k)):
+            arr = constant(0) if v is None else np.asarray(v, dtype=np.float32)
+            getattr(m, name)[:] = arr.tolist()
+        self.materials.append(m)
+        return len(self.materials) - 1
+
+    def add_mesh(self, vertices, indices, material, normals=None, uvs=None) -> int:
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1)
+        n = None if normals is None else np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 3)
+        uv = None if uvs is None else np.ascontiguousarray(uvs, dtype=np.float32).reshape(-1, 2)
+        self.meshes.append(Mesh(v, i, material, n, uv))
+        return len(self.meshes) - 1
+
+    def add_shape(self, kind, params, o2w, material, emission=None) -> int:
+        self.shapes.append(Shape(kind, tuple(params), o2w, material,
+                                 None if emission is None else np.asarray(emission, np.float32)))
+        return len(self.shapes) - 1
+
+    def set_camera(self, c2w: xf.Transform, r2c: xf.Transform, lens_radius=0.0, focal_distance=1.0):
+        c = abi.CameraDesc()
+        c.c2w[:] = c2w.m.tolist()
+        c.c2w_inv[:] = c2w.inv.tolist()
+        c.r2c[:] = r2c.m.tolist()
+        c.r2c_inv[:] = r2c.inv.tolist()
+        c.lens_radius, c.focal_distance = lens_radius, focal_distance
+        self.camera = c
+
+    @property
+    def n_triangles(self) -> int:
+        return sum(len(m.indices) // 3 for m in self.meshes)
+
+    # --- lowering -------------------------------------------------------
+    def desc(self):
+        """Returns (SceneDesc, keepalive); keep the second alive while the
+        descriptor is in use."""
+        keep = []
+        meshes = (abi.MeshDesc * max(1, len(self.meshes)))()
+        for k, m in enumerate(self.meshes):
+            d = meshes[k]
+            d.vertices = abi.fptr(m.vertices)
+            d.n_vertices = len(m.vertices)
+            d.indices = abi.iptr(m.indices)
+            d.n_indices = len(m.indices)
+            d.normals = abi.fptr(m.normals)
+            d.uvs = abi.fptr(m.uvs)
+            d.material = m.material
+            keep += [m.vertices, m.indices, m.normals, m.uvs]
+        shapes = (abi.ShapeDesc * max(1, len(self.shapes)))()
+        for k, s in enumerate(self.shapes):
+            d = shapes[k]
+            d.kind, d.material = s.kind, s.material
+            p = list(s.params) + [0.0] * (6 - len(s.params))
+            d.params[:] = p
+            d.o2w[:] = s.o2w.m.tolist()
+            d.w2o[:] = s.o2w.inv.tolist()
+            d.emissive = 0 if s.emission is None else 1
+            if s.emission is not None:
+                d.emission[:] = s.emission.tolist()
+        mats = (abi.Material * max(1, len(self.materials)))(*self.materials)
+        lights = (abi.LightDesc * max(1, len(self.lights)))()
+        for k, l in enumerate(self.lights):
+            d = lights[k]
+            d.kind = l.kind
+            d.spectrum[:] = np.asarray(l.spectrum, np.float32).tolist()
+            d.vec[:] = [float(x) for x in l.vec]
+            if l.env is not None:
+                env = np.ascontiguousarray(l.env, dtype=np.float32)
+                keep.append(env)
+                d.env = abi.fptr(env)
+                d.env_h, d.env_w = env.shape[0], env.shape[1]
+            w2l = l.w2l or xf.identity()
+            d.w2l[:] = w2l.m.tolist()
+            d.l2w[:] = w2l.inv.tolist()
+        order = None
+        if self.prim_order is not None:
+            order = np.asarray(self.prim_order, dtype=np.int32)
+            keep.append(order)
+        sd = abi.SceneDesc()
+        sd.meshes, sd.n_meshes = meshes, len(self.meshes)
+        sd.shapes, sd.n_shapes = shapes, len(self.shapes)
+        sd.materials, sd.n_materials = mats, len(self.materials)
+        sd.lights, sd.n_lights = lights, len(self.lights)
+        sd.prim_order = abi.iptr(order)
+        if self.camera is not None:
+            sd.camera = self.camera
+        keep += [meshes, shapes, mats, lights]
+        return sd, keep
+
+
+def render_params(width, height, strata=(4, 4), max_depth=5, sample_depth=3, rr_depth=7,
+                  filter_kind=abi.FILTER_BOX, filter_params=(0, 0, 0, 0), seed=1):
+    p = abi.RenderParams()
+    p.width, p.height = width, height
+    p.strata_x, p.strata_y = strata
+    p.max_depth, p.sample_depth, p.rr_depth = max_depth, sample_depth, rr_depth
+    p.filter_kind = filter_kind
+    p.filter_params[:] = [float(x) for x in filter_params]
+    p.seed = seed
+    return p
+
+
+# ---------------------------------------------------------------- Cornell room
+def _quad_tris(a, b, c, d):
+    """two triangles (a, b, c), (a, c, d) of the quad a-b-c-d"""
+    return [a, b, c, d], [0, 1, 2, 0, 2, 3]
+
+
+def cornell_room(width=256, height=256, fov=40.0) -> Scene:
+    s = Scene()
+    grey = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.75, 0.75, 0.75)))
+    red = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.63, 0.065, 0.05)))
+    green = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.14, 0.45, 0.09)))
+    white = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.75, 0.75, 0.75)))
+    # room: x in [0,1] (x = 0 red, x = 1 green), y up, z in [0,1] (z = 1 back wall)
+    walls_v, walls_i = [], []
+    for quad in (
+        [(0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1)],   # floor
+        [(0, 1, 0), (0, 1, 1), (1, 1, 1), (1, 1, 0)],   # ceiling
+        [(0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)],   # back wall
+    ):
+        v, i = _quad_tris(*quad)
+        walls_i += [x + len(walls_v) for x in i]
+        walls_v += v
+    m_grey = s.add_mesh(walls_v, walls_i, grey)
+    v, i = _quad_tris((0, 0, 0), (0, 0, 1), (0, 1, 1), (0, 1, 0))
+    m_red = s.add_mesh(v, i, red)
+    v, i = _quad_tris((1, 0, 0), (1, 1, 0), (1, 1, 1), (1, 0, 1))
+    m_green = s.add_mesh(v, i, green)
+    # ceiling light: Quad half-sizes 0.125 (area 4*sx*sy = 0.0625 = 0.25 x 0.25),
+    # rotateX -90 so the light-sampled side (local -z) faces down
+    light_xf = xf.rotate_x(-90) @ xf.translate(0.5, 0.999, 0.5)
+    q = s.add_shape(abi.SHAPE_QUAD, (0.125, 0.125), light_xf, white,
+                    emission=rgb_to_spectrum((15, 15, 15), illuminant=True))
+    # boxes, rotated about y then placed on the floor
+    tall = s.add_shape(abi.SHAPE_BOX, (-0.15, 0.0, -0.15, 0.15, 0.6, 0.15),
+                       xf.rotate_y(18) @ xf.translate(0.33, 0.0, 0.62), white)
+    short = s.add_shape(abi.SHAPE_BOX, (-0.15, 0.0, -0.15, 0.15, 0.3, 0.15),
+                        xf.rotate_y(-18) @ xf.translate(0.67, 0.0, 0.33), white)
+    s.prim_order = [m_grey, m_red, m_green, ~q, ~tall, ~short]
+    c2w = xf.look_at((0.5, 0.5, -1.4), (0.5, 0.5, 0.5), (0, 1, 0))
+    c2w, r2c = xf.perspective_camera(c2w, 0.0, 1.0, fov, width, height)
+    s.set_camera(c2w, r2c)
+    return s
+
+
+def cornell_params(width=256, height=256, spp_side=4, max_depth=5, rr_depth=3, seed=1):
+    """16 spp (stratified 4x4), max depth 5, Russian roulette after bounce 3,
+    box filter."""
+    return render_params(width, height, (spp_side, spp_side), max_depth=max_depth,
+                         sample_depth=3, rr_depth=rr_depth, filter_kind=abi.FILTER_BOX, seed=seed)
+
+
+# ---------------------------------------------------------------- triangle soup
+def _unit_vectors(rng, n):
+    v = rng.normal(size=(n, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
+
+
+def triangle_soup(n_tris=1 << 20, seed=1, material_scene=False) -> Scene:
+    """n_tris uniform-random triangles: centre ~U([-1,1]^3), two edges of
+    random direction and length ~U(0.005, 0.05)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    c = rng.uniform(-1, 1, size=(n_tris, 3))
+    e1 = _unit_vectors(rng, n_tris) * rng.uniform(0.005, 0.05, size=(n_tris, 1))
+    e2 = _unit_vectors(rng, n_tris) * rng.uniform(0.005, 0.05, size=(n_tris, 1))
+    verts = np.empty((n_tris, 3, 3), dtype=np.float32)
+    verts[:, 0] = c
+    verts[:, 1] = c + e1
+    verts[:, 2] = c + e2
+    s = Scene()
+    mat = s.add_material(abi.MAT_MATTE, kd=constant(0.5))
+    s.add_mesh(verts.reshape(-1, 3), np.arange(3 * n_tris, dtype=np.int32), mat)
+    return s
+
+
+def soup_rays(n_rays=1 << 24, seed=2, any_hit=False):
+    """SoA float32 (8, n): origins uniform on the sphere r=3, directions towards
+    uniform points of the unit ball, tmin 0, tmax inf.  With any_hit, tmax is
+    the distance to a second random point of the unit ball."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    o = _unit_vectors(rng, n_rays) * 3.0
+    q = _unit_vectors(rng, n_rays) * rng.uniform(0, 1, size=(n_rays, 1)) ** (1 / 3)
+    d = q - o
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.empty((8, n_rays), dtype=np.float32)
+    rays[0:3] = o.T
+    rays[3:6] = d.T
+    rays[6] = 0.0
+    rays[7] = np.inf
+    if any_hit:
+        q2 = _unit_vectors(rng, n_rays) * rng.uniform(0, 1, size=(n_rays, 1)) ** (1 / 3)
+        rays[7] = np.linalg.norm(q2 - o, axis=1)
+    return rays

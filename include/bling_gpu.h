@@ -1,0 +1,265 @@
+/*
+ * bling_gpu.h -- C ABI of the GB300 path-tracing core for bling.
+ *
+ * The reference renderer is Haskell; its drop-in point is the `Renderer`
+ * class (src/lib/Graphics/Bling/Rendering.hs:77-78), whose sampler renderer
+ * `prender` (Rendering.hs:111-140) runs the path integrator
+ * (src/lib/Graphics/Bling/Integrator/Path.hs) over 16x16 tiles, one pass at a
+ * time, and reports `PassDone` after each pass.  A `GpuPathRenderer` instance
+ * on the Haskell side calls this library through `foreign import ccall`:
+ * one `bling_render_pass` per pass, then `bling_film_read` for the image.
+ *
+ * Everything below `prender` -- kd-tree/BVH traversal, ray/triangle and
+ * ray/shape intersection, BSDF and light sampling, film accumulation -- runs
+ * on one GPU behind these entry points.  There is no CPU fallback: every call
+ * that needs the GPU fails with BLING_ERR_CUDA when none is usable.
+ *
+ * Conventions
+ *  - Return value: BLING_OK (0) or a negative BLING_ERR_*; the message is kept
+ *    per context (`bling_last_error`).  Nothing aborts.
+ *  - All host buffers are owned by the caller and only read/written during
+ *    the call.  Device memory is owned by the library until *_destroy.
+ *  - A context owns one CUDA stream; calls on one context are serialised by
+ *    an internal mutex, so a context may be shared between threads.
+ *  - Matrices are 4x4 float, row-major, in the reference's `Matrix` layout
+ *    (src/lib/Graphics/Bling/Transform.hs:29-42); a transform is the pair
+ *    (m, m^-1) as in `MkTransform` (Transform.hs:124-127).
+ *  - Spectra are 16 float bands over 400-700 nm (Spectrum.hs:33-46).
+ */
+#ifndef BLING_GPU_H
+#define BLING_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BLING_ABI_VERSION 1
+
+#define BLING_OK 0
+#define BLING_ERR_INVALID_ARG (-1)
+#define BLING_ERR_OOM (-2)
+#define BLING_ERR_CUDA (-3)
+#define BLING_ERR_TIMEOUT (-4)
+#define BLING_ERR_BOUNDS (-5)
+#define BLING_ERR_STATE (-6)
+
+#define BLING_BANDS 16
+
+typedef struct bling_ctx bling_ctx;
+typedef struct bling_scene bling_scene;
+typedef struct bling_film bling_film;
+
+typedef struct bling_opts {
+  int32_t device;        /* CUDA device ordinal */
+  uint32_t flags;        /* reserved, 0 */
+  int32_t block_size;    /* traversal block size, 0 = default */
+  int32_t bvh_leaf_size; /* max primitives per BVH leaf, 0 = default */
+} bling_opts;
+
+/* ---- scene description (flat; replaces the closure records of
+ *      Primitive.hs:21-27 / Reflection.hs:42 that cannot cross an FFI) ---- */
+
+/* Materials (src/lib/Graphics/Bling/Material.hs). Textures are constant. */
+enum {
+  BLING_MAT_MATTE = 0,   /* mkMatte kd sigma            (Material.hs:228-237) */
+  BLING_MAT_PLASTIC = 1, /* mkPlastic kd ks roughness   (Material.hs:272-282) */
+  BLING_MAT_METAL = 2,   /* mkMetal eta k roughness     (Material.hs:285-292) */
+  BLING_MAT_GLASS = 3    /* glassMaterial ior kr kt     (Material.hs:252-262) */
+};
+
+typedef struct bling_material {
+  int32_t kind;
+  float sigma;     /* matte: Oren-Nayar sigma, 0 = Lambertian */
+  float roughness; /* plastic/metal: Blinn exponent is 1/roughness */
+  float ior;       /* glass */
+  float kd[BLING_BANDS];  /* matte/plastic diffuse */
+  float ks[BLING_BANDS];  /* plastic specular, glass reflection */
+  float kt[BLING_BANDS];  /* glass transmission */
+  float eta[BLING_BANDS]; /* metal */
+  float k[BLING_BANDS];   /* metal */
+} bling_material;
+
+/* A triangle mesh (mkTriangleMesh, Primitive/TriangleMesh.hs:39-60).
+ * Vertices and normals are already in world space (the reference applies
+ * o2w once at build, TriangleMesh.hs:58-59).  Indices are validated like
+ * the reference does (TriangleMesh.hs:48-55). */
+typedef struct bling_mesh_desc {
+  const float* vertices; /* 3 * n_vertices */
+  int64_t n_vertices;
+  const int32_t* indices; /* n_indices, a multiple of 3 */
+  int64_t n_indices;
+  const float* normals; /* optional shading normals, 3 * n_vertices, or NULL */
+  const float* uvs;     /* optional 2 * n_vertices, or NULL (default uvs) */
+  int32_t material;
+  int32_t reserved;
+} bling_mesh_desc;
+
+/* Analytic shapes (Shape.hs:22-38) placed by mkGeom (Primitive/Geometry.hs:14-36). */
+enum {
+  BLING_SHAPE_SPHERE = 0,  /* params: radius */
+  BLING_SHAPE_QUAD = 1,    /* params: sx, sy */
+  BLING_SHAPE_BOX = 2,     /* params: pmin xyz, pmax xyz */
+  BLING_SHAPE_DISK = 3,    /* params: height, radius, inner radius, phimax (radians) */
+  BLING_SHAPE_CYLINDER = 4 /* params: radius, zmin, zmax, phimax (radians) */
+};
+
+typedef struct bling_shape_desc {
+  int32_t kind;
+  int32_t material;
+  float params[6];
+  float o2w[16];
+  float w2o[16];
+  int32_t emissive; /* nonzero: the shape is an area light (Light.hs:64-70) */
+  float emission[BLING_BANDS];
+} bling_shape_desc;
+
+/* Non-geometric lights (Light.hs:31-45). */
+enum {
+  BLING_LIGHT_DIRECTIONAL = 0, /* mkDirectional spectrum dir */
+  BLING_LIGHT_POINT = 1,       /* mkPointLight spectrum pos */
+  BLING_LIGHT_INFINITE = 2     /* mkInfiniteAreaLight map w2l */
+};
+
+typedef struct bling_light_desc {
+  int32_t kind;
+  float spectrum[BLING_BANDS]; /* directional/point radiance/intensity */
+  float vec[3];                /* directional: normalised direction; point: position */
+  const float* env;            /* infinite: env_w * env_h * 16 floats, row v, column u */
+  int32_t env_w, env_h;
+  float w2l[16];               /* infinite: world-to-light */
+  float l2w[16];               /* infinite: light-to-world */
+} bling_light_desc;
+
+/* A projective camera (Camera.hs:120-127, mkProjective Camera.hs:204-229). */
+typedef struct bling_camera_desc {
+  float c2w[16], c2w_inv[16];
+  float r2c[16], r2c_inv[16];
+  float lens_radius;
+  float focal_distance;
+} bling_camera_desc;
+
+/* The scene.  Primitive IDs follow the list handed to mkKdTree
+ * (Scene.hs:160-166): `prim_order` lists the meshes (v >= 0 -> mesh v, which
+ * expands to its triangles in index order) and shapes (v < 0 -> shape ~v) in
+ * that order; NULL means all meshes, then all shapes.  Lights follow
+ * `mkScene`: the non-geometric lights, then the emissive shapes in primitive
+ * order (Scene.hs:162,165). */
+typedef struct bling_scene_desc {
+  const bling_mesh_desc* meshes;
+  int32_t n_meshes;
+  const bling_shape_desc* shapes;
+  int32_t n_shapes;
+  const bling_material* materials;
+  int32_t n_materials;
+  const bling_light_desc* lights;
+  int32_t n_lights;
+  const int32_t* prim_order; /* n_meshes + n_shapes entries, or NULL */
+  bling_camera_desc camera;
+} bling_scene_desc;
+
+/* Pixel filters (Filter.hs:12-21). */
+enum {
+  BLING_FILTER_BOX = 0,
+  BLING_FILTER_GAUSS = 1,    /* params: w, h, alpha */
+  BLING_FILTER_MITCHELL = 2, /* params: w, h, B, C */
+  BLING_FILTER_SINC = 3,     /* params: w, h, tau */
+  BLING_FILTER_TRIANGLE = 4  /* params: w, h */
+};
+
+/* One render job: `SamplerRenderer (Stratified nu nv) (mkPathIntegrator md sd)`
+ * (Rendering.hs:96-103, Sampling.hs:112-132, Path.hs:30-39). */
+typedef struct bling_render_params {
+  int32_t width, height;
+  int32_t strata_x, strata_y; /* stratified nu x nv samples per pixel per pass */
+  int32_t max_depth;          /* path maxDepth */
+  int32_t sample_depth;       /* path sampleDepth (stratified dimensions) */
+  int32_t rr_depth;           /* Russian roulette after this depth; reference: 7 */
+  int32_t filter_kind;
+  float filter_params[4];
+  uint64_t seed;
+} bling_render_params;
+
+typedef struct bling_stats {
+  uint64_t rays_closest;    /* closest-hit queries (camera, continuation, BSDF-MIS) */
+  uint64_t rays_any;        /* any-hit queries (shadow) */
+  uint64_t path_samples;    /* completed camera paths */
+  uint64_t nonfinite_drops; /* NaN/Inf samples skipped by the film (Image.hs:253-256) */
+  double bvh_build_ms;
+  double last_pass_ms;
+  uint64_t bvh_nodes;
+  uint64_t bvh_leaf_prims;
+  uint64_t device_bytes;
+} bling_stats;
+
+/* ---- context ---- */
+int bling_ctx_create(bling_ctx** out, const bling_opts* opts);
+void bling_ctx_destroy(bling_ctx* ctx);
+const char* bling_last_error(bling_ctx* ctx);
+/* Runs the context's work on an external CUDA stream (a cudaStream_t, e.g.
+ * the caller's current stream) instead of its own; NULL restores the
+ * context's own stream.  Calls still synchronise that stream before return. */
+int bling_ctx_set_stream(bling_ctx* ctx, void* stream);
+int bling_abi_version(void);
+
+/* ---- scenes: copies the host arrays, builds and uploads the BVH ----
+ * replaces mkScene/mkKdTree (Scene.hs:160-166, Primitive/KdTree.hs:107-112) */
+int bling_scene_create(bling_ctx* ctx, const bling_scene_desc* desc, bling_scene** out);
+void bling_scene_destroy(bling_scene* scene);
+
+/* ---- ray queries over host buffers (SoA rays: ox oy oz dx dy dz tmin tmax,
+ *      each n floats, i.e. rays[k*n + i]) ----
+ * bling_trace_closest replaces `scIntersect` (Scene.hs:172-174) on a batch:
+ * the nearest hit, ties to the larger primitive ID as the reference's
+ * `nearest'` fold does (Primitive.hs:29-43, TriangleMesh.hs:166).
+ * prim[i] = -1 on a miss.  b1b2 may be NULL (2n floats: the barycentrics
+ * of triangle hits, 0 for shapes). */
+int bling_trace_closest(bling_scene* scene, const float* rays, size_t n, float* t,
+                        int32_t* prim, float* b1b2);
+/* replaces `occluded` (Scene.hs:168-170): hit[i] = 1 when any primitive is hit
+ * within [tmin, tmax]. */
+int bling_trace_any(bling_scene* scene, const float* rays, size_t n, uint8_t* hit);
+
+/* Device-pointer variants: the same queries over buffers already resident on
+ * the device (rays: 8*n floats SoA), launched on the context's stream and
+ * synchronised before return. */
+int bling_trace_closest_device(bling_scene* scene, const float* d_rays, size_t n, float* d_t,
+                               int32_t* d_prim, float* d_b1b2);
+int bling_trace_any_device(bling_scene* scene, const float* d_rays, size_t n, uint8_t* d_hit);
+
+/* Work of the closest-hit traversal on a batch of host rays, as the
+ * reference's dbgTraverse counts it (Primitive/KdTree.hs:252-281): BVH nodes
+ * visited and leaf primitives tested, summed over the batch. */
+int bling_trace_counts(bling_scene* scene, const float* rays, size_t n, uint64_t* nodes_visited,
+                       uint64_t* prims_tested);
+
+/* ---- films and passes ---- */
+int bling_film_create(bling_ctx* ctx, int32_t width, int32_t height, bling_film** out);
+void bling_film_destroy(bling_film* film);
+int bling_film_clear(bling_film* film);
+/* copies the (weight, X, Y, Z) film, width*height*4 floats (Image.hs:64-82) */
+int bling_film_read(bling_film* film, float* host_wxyz);
+/* resolves to linear sRGB floats, width*height*3 (getPixel/xyzToRgb,
+ * Image.hs:302-315, Spectrum.hs:162-168) */
+int bling_film_resolve(bling_film* film, float* host_rgb);
+
+/* One pass of `prender` (Rendering.hs:127-138): every pixel of the
+ * filter-padded sample extent gets strata_x*strata_y path samples, added to
+ * the film.  `pass` selects the random stream (seed, pass). */
+int bling_render_pass(bling_scene* scene, bling_film* film, const bling_render_params* params,
+                      uint64_t pass);
+
+int bling_scene_stats(bling_scene* scene, bling_stats* out);
+
+/* ---- host helpers for building scenes (no GPU needed) ---- */
+/* rgbToSpectrumRefl / rgbToSpectrumIllum (Spectrum.hs:140-159) */
+void bling_rgb_to_spectrum(int32_t illuminant, float r, float g, float b, float out[BLING_BANDS]);
+/* spectrumToXYZ (Spectrum.hs:349-355) */
+void bling_spectrum_to_xyz(const float s[BLING_BANDS], float xyz[3]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BLING_GPU_H */

@@ -1,0 +1,2329 @@
+// CPU oracle for the GB300 path-tracing core of bling.
+//
+// TEST INFRASTRUCTURE ONLY.  This file restates, function by function, the
+// reference's Haskell code for the hot path (file:line citations are to the
+// reference, src/lib/Graphics/Bling/...).  It is the parity checker for the
+// GPU library and the timed host-core baseline; the product never links it.
+//
+// Arithmetic: IEEE binary32, one rounding per operation in the reference's
+// order, no contraction (built with -ffp-contract=off).  Transcendentals call
+// the C library's float functions, as GHC's Float primops do.
+//
+// Randomness: the reference draws from mwc-random seeded from system entropy
+// per tile (Rendering.hs:128, Random.hs:61-62, 91-96), a stream that cannot be
+// reproduced.  The oracle and the GPU therefore share one counter-based
+// generator (SplitMix64 finaliser, Steele/Lea/Flood 2014) keyed by
+// (seed, pass, pixel, sample, dimension), and the stratified sample
+// dimensions use Kensler's hash permutation (Correlated Multi-Jittered
+// Sampling, 2013) in place of the reference's in-place shuffles
+// (Sampling.hs:134-152).  The sample structure -- which dimensions are
+// stratified, jittered and shuffled -- follows the reference.
+#include "oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstdlib>
+#include <thread>
+#include <vector>
+
+#include "../bling_gb300/csrc/spectrum_tables.h"
+#include "oracle_math.h"
+
+using namespace orc;
+
+namespace {
+
+// ---------------------------------------------------------------- spectra
+// Spectrum.hs:33-46: 16 bands
+struct Spec {
+  float v[16];
+};
+static inline Spec sConst(float c) {
+  Spec s;
+  for (int i = 0; i < 16; i++) s.v[i] = c;
+  return s;
+}
+static const Spec BLACK = sConst(0.0f);
+static const Spec WHITE = sConst(1.0f);
+static inline Spec operator+(const Spec& a, const Spec& b) {
+  Spec s;
+  for (int i = 0; i < 16; i++) s.v[i] = a.v[i] + b.v[i];
+  return s;
+}
+static inline Spec operator-(const Spec& a, const Spec& b) {
+  Spec s;
+  for (int i = 0; i < 16; i++) s.v[i] = a.v[i] - b.v[i];
+  return s;
+}
+static inline Spec operator*(const Spec& a, const Spec& b) {
+  Spec s;
+  for (int i = 0; i < 16; i++) s.v[i] = a.v[i] * b.v[i];
+  return s;
+}
+static inline Spec operator/(const Spec& a, const Spec& b) {
+  Spec s;
+  for (int i = 0; i < 16; i++) s.v[i] = a.v[i] / b.v[i];
+  return s;
+}
+// sScale (Spectrum.hs:448-450)
+static inline Spec sScale(const Spec& a, float f) {
+  Spec s;
+  for (int i = 0; i < 16; i++) s.v[i] = a.v[i] * f;
+  return s;
+}
+static inline bool isBlack(const Spec& s) {
+  for (int i = 0; i < 16; i++)
+    if (s.v[i] != 0) return false;
+  return true;
+}
+static inline bool sNaN(const Spec& s) {
+  for (int i = 0; i < 16; i++)
+    if (std::isnan(s.v[i])) return true;
+  return false;
+}
+static inline bool sInf(const Spec& s) {
+  for (int i = 0; i < 16; i++)
+    if (std::isinf(s.v[i])) return true;
+  return false;
+}
+static inline Spec sClamp(float lo, float hi, const Spec& a) {
+  Spec s;
+  for (int i = 0; i < 16; i++) s.v[i] = hmax(lo, hmin(hi, a.v[i]));
+  return s;
+}
+static inline float tbl(const uint32_t* bits, int i) { return __bling_f32(bits[i]); }
+
+// sY (Spectrum.hs:371-373)
+static float sY(const Spec& s) {
+  float acc = 0.0f;
+  for (int i = 0; i < 16; i++) acc = acc + s.v[i] * tbl(BLING_CIE_Y_BITS, i);
+  return acc / __bling_f32(BLING_CIE_Y_SUM_BITS);
+}
+// spectrumToXYZ (Spectrum.hs:349-355)
+static void spectrumToXYZ(const Spec& s, float& x, float& y, float& z) {
+  float a = 0, b = 0, c = 0;
+  for (int i = 0; i < 16; i++) {
+    float v = s.v[i];
+    a = a + tbl(BLING_CIE_X_BITS, i) * v;
+    b = b + tbl(BLING_CIE_Y_BITS, i) * v;
+    c = c + tbl(BLING_CIE_Z_BITS, i) * v;
+  }
+  float ys = __bling_f32(BLING_CIE_Y_SUM_BITS);
+  x = a / ys;
+  y = b / ys;
+  z = c / ys;
+}
+// rgbToSpectrum (Spectrum.hs:146-159)
+static Spec basis(bool illum, int which) {
+  Spec s;
+  const uint32_t* t = illum ? BLING_RGB_ILLUM_BITS : BLING_RGB_REFL_BITS;
+  for (int i = 0; i < 16; i++) s.v[i] = tbl(t, which * 16 + i);
+  return s;
+}
+static Spec rgbToSpectrum(bool illum, float r, float g, float b) {
+  Spec wb = basis(illum, BLING_BASIS_WHITE), cb = basis(illum, BLING_BASIS_CYAN),
+       mb = basis(illum, BLING_BASIS_MAGENTA), yb = basis(illum, BLING_BASIS_YELLOW),
+       rb = basis(illum, BLING_BASIS_RED), gb = basis(illum, BLING_BASIS_GREEN),
+       bb = basis(illum, BLING_BASIS_BLUE);
+  if (r <= g && r <= b) {
+    return sScale(wb, r) + (g <= b ? sScale(cb, g - r) + sScale(bb, b - g)
+                                   : sScale(cb, b - r) + sScale(gb, g - b));
+  }
+  if (g <= r && g <= b) {
+    return sScale(wb, g) + (r <= b ? sScale(mb, r - g) + sScale(bb, b - r)
+                                   : sScale(mb, b - g) + sScale(rb, r - b));
+  }
+  return sScale(wb, b) + (r <= b ? sScale(yb, r - b) + sScale(gb, g - r)
+                                 : sScale(yb, g - b) + sScale(rb, r - g));
+}
+// xyzToRgb (Spectrum.hs:162-168)
+static void xyzToRgb(float x, float y, float z, float& r, float& g, float& b) {
+  r = 3.240479f * x - 1.537150f * y - 0.498535f * z;
+  g = (-0.969256f) * x + 1.875991f * y + 0.041556f * z;
+  b = 0.055648f * x - 0.204043f * y + 1.057311f * z;
+}
+
+// ---------------------------------------------------------------- randomness
+static inline uint64_t mix64(uint64_t z) {
+  z ^= z >> 30;
+  z *= 0xbf58476d1ce4e5b9ULL;
+  z ^= z >> 27;
+  z *= 0x94d049bb133111ebULL;
+  z ^= z >> 31;
+  return z;
+}
+static inline uint64_t pixelKey(uint64_t seed, uint64_t pass, int px, int py) {
+  uint64_t k = mix64(seed ^ mix64(pass + 0x9e3779b97f4a7c15ULL));
+  return mix64(k ^ (((uint64_t)(uint32_t)px << 32) | (uint64_t)(uint32_t)py));
+}
+static inline uint32_t randU32(uint64_t key, uint32_t n, uint32_t dim) {
+  return (uint32_t)(mix64(key ^ mix64(((uint64_t)n << 32) | dim)) >> 32);
+}
+static inline float randF(uint64_t key, uint32_t n, uint32_t dim) {
+  return (float)(randU32(key, n, dim) >> 8) * (1.0f / 16777216.0f);
+}
+// Kensler's permute(i, l, p): a hashed bijection on [0, l)
+static uint32_t permute(uint32_t i, uint32_t l, uint32_t p) {
+  uint32_t w = l - 1;
+  w |= w >> 1;
+  w |= w >> 2;
+  w |= w >> 4;
+  w |= w >> 8;
+  w |= w >> 16;
+  do {
+    i ^= p;
+    i *= 0xe170893du;
+    i ^= p >> 16;
+    i ^= (i & w) >> 4;
+    i ^= p >> 8;
+    i *= 0x0929eb3fu;
+    i ^= p >> 23;
+    i ^= (i & w) >> 1;
+    i *= 1u | p >> 27;
+    i *= 0x6935fa69u;
+    i ^= (i & w) >> 11;
+    i *= 0x74dcb303u;
+    i ^= (i & w) >> 2;
+    i *= 0x9e501cc3u;
+    i ^= (i & w) >> 2;
+    i *= 0xc860a3dfu;
+    i &= w;
+    i ^= i >> 5;
+  } while (i >= l);
+  return (i + p) % l;
+}
+
+// dimension ids of the shared generator
+enum : uint32_t {
+  DIM_PIX_U = 0,
+  DIM_PIX_V = 1,
+  DIM_LENS_PERM = 2,
+  DIM_LENS_U = 3,
+  DIM_LENS_V = 4,
+  DIM_1D_BASE = 16,        // + 2*off (perm), + 2*off + 1 (jitter)
+  DIM_2D_BASE = 4096,      // + 4*off (perm), +1 (ju), +2 (jv)
+  DIM_FRESH_1D = 1u << 20, // | n
+  DIM_FRESH_2D = 2u << 20  // | 2n + {0,1}
+};
+static const float ALMOST_ONE = 0.9999999403953552f;  // Sampling.hs:154-155
+
+// One camera sample of the stratified sampler (Sampling.hs:112-132, 157-171)
+struct Sampler {
+  uint64_t key;
+  uint32_t n;       // sample index within the pixel
+  int nu, nv;       // strata
+  int n1d, n2d;     // precomputed dimension counts
+};
+// stratified2D entry i: (u, v) = quotRem i nu (Sampling.hs:164-171)
+static void strat2D(const Sampler& s, uint32_t i, uint32_t dju, uint32_t djv, float& u, float& v) {
+  float du = 1.0f / (float)s.nu, dv = 1.0f / (float)s.nv;
+  uint32_t qu = i / (uint32_t)s.nu, qv = i % (uint32_t)s.nu;
+  float ju = randF(s.key, i, dju), jv = randF(s.key, i, djv);
+  u = hmin(ALMOST_ONE, ((float)qu + ju) * du);
+  v = hmin(ALMOST_ONE, ((float)qv + jv) * dv);
+}
+// rnd' n (Sampling.hs:203-211)
+static float rnd1(const Sampler& s, int n) {
+  if (n < s.n1d) {
+    uint32_t N = (uint32_t)(s.nu * s.nv);
+    uint32_t p = randU32(s.key, 0xffffffffu, DIM_1D_BASE + 2 * n);
+    uint32_t st = permute(s.n, N, p);
+    float du = 1.0f / (float)N;
+    float j = randF(s.key, st, DIM_1D_BASE + 2 * n + 1);
+    return hmin(ALMOST_ONE, ((float)st + j) * du);
+  }
+  return randF(s.key, s.n, DIM_FRESH_1D | (uint32_t)n);
+}
+// rnd2D' n (Sampling.hs:213-221)
+static void rnd2(const Sampler& s, int n, float& u, float& v) {
+  if (n < s.n2d) {
+    uint32_t N = (uint32_t)(s.nu * s.nv);
+    uint32_t p = randU32(s.key, 0xffffffffu, DIM_2D_BASE + 4 * n);
+    uint32_t st = permute(s.n, N, p);
+    strat2D(s, st, DIM_2D_BASE + 4 * n + 1, DIM_2D_BASE + 4 * n + 2, u, v);
+    return;
+  }
+  u = randF(s.key, s.n, DIM_FRESH_2D | (uint32_t)(2 * n));
+  v = randF(s.key, s.n, DIM_FRESH_2D | (uint32_t)(2 * n + 1));
+}
+
+// ---------------------------------------------------------------- geometry
+struct DG {  // DifferentialGeometry (DifferentialGeometry.hs:26-36), the used fields
+  V p, n;
+  V dpdu, dpdv;
+  bool tri;
+  float b1, b2;
+};
+// mkDg: n = normalize (dpdu x dpdv) (DifferentialGeometry.hs:41-51)
+static DG mkDg(V p, V dpdu, V dpdv) {
+  DG g;
+  g.p = p;
+  g.n = normalize(cross(dpdu, dpdv));
+  g.dpdu = dpdu;
+  g.dpdv = dpdv;
+  g.tri = false;
+  g.b1 = g.b2 = 0;
+  return g;
+}
+// mkDg' p n: dpdu/dpdv from coordinateSystem n (DifferentialGeometry.hs:53-56)
+static DG mkDg2(V p, V n) {
+  LC c = coordinateSystem(n);
+  DG g;
+  g.p = p;
+  g.n = n;
+  g.dpdu = c.s;
+  g.dpdv = c.t;
+  g.tri = false;
+  g.b1 = g.b2 = 0;
+  return g;
+}
+// transDg (DifferentialGeometry.hs:72-81)
+static DG transDg(const float* m, const float* mi, const DG& g) {
+  DG r = g;
+  r.p = transPoint(m, g.p);
+  r.n = normalize(transNormal(mi, g.n));
+  r.dpdu = transVector(m, g.dpdu);
+  r.dpdv = transVector(m, g.dpdv);
+  return r;
+}
+
+// solveQuadric (Math.hs:124-139)
+static bool solveQuadric(float a, float b, float c, float& t0, float& t1) {
+  float discrim = b * b - 4.0f * a * c;
+  if (discrim < 0) return false;
+  float rootDiscrim = sqrtf(discrim);
+  float q = b < 0 ? -0.5f * (b - rootDiscrim) : -0.5f * (b + rootDiscrim);
+  float x0 = q / a, x1 = c / q;
+  t0 = hmin(x0, x1);
+  t1 = hmax(x0, x1);
+  return true;
+}
+
+// intersectAABB (AABB.hs:79-94)
+static bool intersectAABB(V bmin, V bmax, const Ray& r, float& n_out, float& f_out) {
+  float near = r.tmin, far = r.tmax;
+  for (int dim = 0; dim < 3; dim++) {
+    if (near > far) return false;
+    float dInv = 1.0f / comp(r.d, dim);
+    float oc = comp(r.o, dim);
+    float tFar = (comp(bmax, dim) - oc) * dInv;
+    float tNear = (comp(bmin, dim) - oc) * dInv;
+    float nn = tNear > tFar ? tFar : tNear, ff = tNear > tFar ? tNear : tFar;
+    near = hmax(near, nn);
+    far = hmin(far, ff);
+  }
+  if (near > far) return false;
+  n_out = near;
+  f_out = far;
+  return true;
+}
+
+struct Shape {
+  int kind;
+  float p[6];
+  Xf o2w;  // m = o2w, i = w2o
+  int material;
+  bool emissive;
+  Spec emission;
+  int light_id;  // index into the scene's light list when emissive
+};
+
+// area (Shape.hs:314-328)
+static float shapeArea(const Shape& s) {
+  switch (s.kind) {
+    case BLING_SHAPE_BOX: {
+      float h = s.p[3] - s.p[0], w = s.p[4] - s.p[1], l = s.p[5] - s.p[2];
+      return 2.0f * (h * w + h * l + w * l);
+    }
+    case BLING_SHAPE_CYLINDER: return 2.0f * PI * s.p[0] * (s.p[2] - s.p[1]);
+    case BLING_SHAPE_DISK: {
+      float rmin2 = s.p[2] * s.p[2], rmax2 = s.p[1] * s.p[1];
+      return PI * (rmax2 - rmin2);
+    }
+    case BLING_SHAPE_QUAD: return 4.0f * s.p[0] * s.p[1];
+    default: return s.p[0] * s.p[0] * 4.0f * PI;
+  }
+}
+
+// Shape.intersect in object space (Shape.hs:81-229); returns t, eps, dg
+static bool shapeIntersect(const Shape& s, const Ray& ray, float& t_out, float& e_out, DG& dg) {
+  const V& ro = ray.o;
+  const V& rd = ray.d;
+  float tmin = ray.tmin, tmax = ray.tmax;
+  switch (s.kind) {
+    case BLING_SHAPE_BOX: {
+      V pmin{s.p[0], s.p[1], s.p[2]}, pmax{s.p[3], s.p[4], s.p[5]};
+      float near = -INF, far = INF;
+      int dd = 0;
+      for (int dim = 0; dim < 3; dim++) {
+        if (near > far) return false;
+        float dInv = 1.0f / comp(rd, dim);
+        float oc = comp(ro, dim);
+        float t1p = (comp(pmax, dim) - oc) * dInv;
+        float t2p = (comp(pmin, dim) - oc) * dInv;
+        float t1 = t1p > t2p ? t2p : t1p, t2 = t1p > t2p ? t1p : t2p;
+        int ndd = near < t1 ? dim : dd;
+        near = hmax(near, t1);
+        far = hmin(far, t2);
+        dd = ndd;
+      }
+      if (near > far) return false;
+      float t0 = hmin(near, far), t1 = hmax(near, far);
+      if (t0 > tmax || t0 < tmin) return false;
+      float t = t0 < tmin ? t1 : t0;
+      if (t > tmax) return false;
+      V p = rayAt(ray, t);
+      float half = (comp(pmin, dd) + comp(pmax, dd)) / 2.0f;
+      float dir = comp(p, dd) > half ? 1.0f : -1.0f;
+      V n = normalize(setComp(dd, dir, mkV(0, 0, 0)));
+      t_out = t;
+      e_out = 5e-4f * t;
+      dg = mkDg2(p, n);
+      return true;
+    }
+    case BLING_SHAPE_CYLINDER: {
+      float r = s.p[0], zmin = s.p[1], zmax = s.p[2], phimax = s.p[3];
+      float a = rd.x * rd.x + rd.y * rd.y;
+      float b = 2.0f * (rd.x * ro.x + rd.y * ro.y);
+      float c = ro.x * ro.x + ro.y * ro.y - r * r;
+      float t0, t1;
+      if (!solveQuadric(a, b, c, t0, t1)) return false;
+      if (t0 > tmax) return false;
+      if (t1 < tmin) return false;
+      V ph0 = rayAt(ray, t0), ph1 = rayAt(ray, t1);
+      float phi0 = atan2p(ph0.y, ph0.x), phi1 = atan2p(ph1.y, ph1.x);
+      V ph;
+      float t;
+      if (t0 > tmin && ph0.z > zmin && ph0.z < zmax && phi0 <= phimax) {
+        ph = ph0;
+        t = t0;
+      } else if (t1 <= tmax && ph1.z > zmin && ph1.z < zmax && phi1 <= phimax) {
+        ph = ph1;
+        t = t1;
+      } else {
+        return false;
+      }
+      V dpdu{-phimax * ph.y, phimax * ph.x, 0};
+      V dpdv{0, 0, zmax - zmin};
+      t_out = t;
+      e_out = 5e-4f * t;
+      dg = mkDg2(ph, normalize(cross(dpdu, dpdv)));
+      return true;
+    }
+    case BLING_SHAPE_DISK: {
+      float h = s.p[0], rad = s.p[1], irad = s.p[2], phimax = s.p[3];
+      if (fabsf(rd.z) < 1e-7f) return false;
+      float t = (h - ro.z) / rd.z;
+      if (t < tmin || t > tmax) return false;
+      V p = rayAt(ray, t);
+      float d2 = p.x * p.x + p.y * p.y;
+      if (d2 > rad * rad || d2 < irad * irad) return false;
+      float phi = atan2p(p.y, p.x);
+      if (phi > phimax) return false;
+      t_out = t;
+      e_out = 5e-4f * t;
+      dg = mkDg2(p, mkV(0, 0, -1));
+      return true;
+    }
+    case BLING_SHAPE_QUAD: {
+      float sx = s.p[0], sy = s.p[1];
+      if (fabsf(rd.z) < 1e-7f) return false;
+      float t = -(ro.z) / rd.z;
+      if (t < tmin || t > tmax) return false;
+      V p = rayAt(ray, t);
+      if (fabsf(p.x) > sx || fabsf(p.y) > sy) return false;
+      t_out = t;
+      e_out = 5e-4f * t;
+      dg = mkDg(p, mkV(sx, 0, 0), mkV(0, sy, 0));
+      return true;
+    }
+    default: {  // sphere
+      float r = s.p[0];
+      float a = sqLen(rd);
+      float b = 2.0f * dot(ro, rd);
+      float c = sqLen(ro) - r * r;
+      float t1, t2;
+      if (!solveQuadric(a, b, c, t1, t2)) return false;
+      if (t1 > tmax) return false;
+      if (t2 < tmin) return false;
+      float t = t1 < tmin ? t2 : t1;
+      if (t > tmax) return false;
+      V p = rayAt(ray, t);
+      const float thetaMax = 0.0f, thetaMin = PI, phiMax = TWO_PI;
+      float theta = acosf(clampf(p.z / r, -1, 1));
+      float zradius = sqrtf(p.x * p.x + p.y * p.y);
+      float invz = 1.0f / zradius;
+      float cosphi = p.x * invz, sinphi = p.y * invz;
+      V dpdu{-phiMax * p.y, phiMax * p.x, 0};
+      V dpdv = V{p.z * cosphi, p.z * sinphi, -r * sinf(theta)} * V{thetaMax - thetaMin,
+                                                                 thetaMax - thetaMin,
+                                                                 thetaMax - thetaMin};
+      t_out = t;
+      e_out = 5e-4f * t;
+      dg = mkDg(p, dpdu, dpdv);
+      return true;
+    }
+  }
+}
+
+// Shape.intersects in object space (Shape.hs:231-284)
+static bool shapeIntersects(const Shape& s, const Ray& ray) {
+  const V& ro = ray.o;
+  const V& rd = ray.d;
+  float tmin = ray.tmin, tmax = ray.tmax;
+  switch (s.kind) {
+    case BLING_SHAPE_BOX: {
+      float n, f;
+      return intersectAABB(V{s.p[0], s.p[1], s.p[2]}, V{s.p[3], s.p[4], s.p[5]}, ray, n, f);
+    }
+    case BLING_SHAPE_CYLINDER: {
+      float r = s.p[0], zmin = s.p[1], zmax = s.p[2], phimax = s.p[3];
+      float a = rd.x * rd.x + rd.y * rd.y;
+      float b = 2.0f * (rd.x * ro.x + rd.y * ro.y);
+      float c = ro.x * ro.x + ro.y * ro.y - r * r;
+      float t0, t1;
+      if (!solveQuadric(a, b, c, t0, t1)) return false;
+      if (t0 > tmax) return false;
+      if (t1 < tmin) return false;
+      V ph0 = rayAt(ray, t0), ph1 = rayAt(ray, t1);
+      float phi0 = atan2p(ph0.y, ph0.x), phi1 = atan2p(ph1.y, ph1.x);
+      if (t0 > tmin && ph0.z > zmin && ph0.z < zmax && phi0 <= phimax) return true;
+      if (t1 < tmax && ph1.z > zmin && ph1.z < zmax && phi1 <= phimax && t1 <= tmax) return true;
+      return false;
+    }
+    case BLING_SHAPE_DISK: {
+      float h = s.p[0], rad = s.p[1], irad = s.p[2], phimax = s.p[3];
+      if (fabsf(rd.z) < 1e-7f) return false;
+      float t = (h - ro.z) / rd.z;
+      if (t < tmin || t > tmax) return false;
+      V p = rayAt(ray, t);
+      float d2 = p.x * p.x + p.y * p.y;
+      if (d2 > rad * rad || d2 < irad * irad) return false;
+      return !(atan2p(p.y, p.x) > phimax);
+    }
+    case BLING_SHAPE_QUAD: {
+      if (fabsf(rd.z) < 1e-7f) return false;
+      float t = -(ro.z) / rd.z;
+      if (t < tmin || t > tmax) return false;
+      V p = rayAt(ray, t);
+      return !(fabsf(p.x) > s.p[0] || fabsf(p.y) > s.p[1]);
+    }
+    default: {
+      float r = s.p[0];
+      float a = sqLen(rd);
+      float b = 2.0f * dot(ro, rd);
+      float c = sqLen(ro) - r * r;
+      float t0, t1;
+      if (!solveQuadric(a, b, c, t0, t1)) return false;
+      if (t0 > tmax || t1 < tmin) return false;
+      if (t0 < tmin) return t1 < tmax;
+      return true;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- scene
+struct Mesh {
+  std::vector<V> p;
+  std::vector<int32_t> idx;
+  std::vector<V> n;       // empty: no shading normals
+  std::vector<float> uv;  // empty: default uvs
+  int material;
+};
+
+enum BxKind { BX_LAMBERT, BX_OREN, BX_SPEC_REFL, BX_SPEC_TRANS, BX_MICRO };
+enum { T_REFL = 1, T_TRANS = 2, T_DIFF = 4, T_GLOSSY = 8, T_SPEC = 16 };
+enum FrKind { FR_NOOP, FR_DIEL, FR_COND };
+
+struct Fresnel {
+  int kind;
+  float ei, et;    // dielectric
+  Spec eta, k;     // conductor
+};
+
+struct BxDF {
+  int kind;
+  int type;
+  Spec r;
+  float A, B;       // Oren-Nayar
+  float ei, et;     // specular transmission
+  float e;          // Blinn exponent
+  Fresnel fr;
+};
+
+struct Material {
+  int kind;
+  float sigma, rough, ior;
+  Spec kd, ks, kt, eta, k;
+};
+
+struct Prim {
+  int is_shape;
+  int index;  // mesh triangle: mesh id; shape: shape id
+  int tri;    // triangle number within the mesh
+  V p1, p2, p3;
+};
+
+struct Light {
+  int kind;  // BLING_LIGHT_* or 100 = area
+  Spec spec;
+  V vec;
+  int shape;  // area lights
+  int id;
+  // infinite
+  std::vector<Spec> env;
+  int w, h;
+  Xf w2l;
+  // Dist2D (Montecarlo.hs:303-333)
+  std::vector<std::vector<float>> cfunc, ccdf;
+  std::vector<float> cint;
+  std::vector<float> mfunc, mcdf;
+  float mint;
+};
+static const int LIGHT_AREA = 100;
+
+struct AabbF {
+  V lo, hi;
+};
+
+struct BvhNode {
+  double lo[3], hi[3];
+  int left, right;  // right < 0: leaf; left = first, -right-1 = count
+};
+
+}  // namespace
+
+struct orc_scene {
+  std::vector<Mesh> meshes;
+  std::vector<Shape> shapes;
+  std::vector<Material> mats;
+  std::vector<Light> lights;
+  std::vector<Prim> prims;
+  bling_camera_desc cam;
+  // oracle BVH
+  std::vector<BvhNode> nodes;
+  std::vector<int> order;
+};
+
+namespace {
+
+// ---------------------------------------------------------------- triangles
+// triangleIntersects / triangleIntersect (Primitive/TriangleMesh.hs:140-207)
+static inline bool triIntersect(const Prim& pr, const Ray& r, float& t_out, float& b1_out,
+                                float& b2_out) {
+  V e1 = pr.p2 - pr.p1, e2 = pr.p3 - pr.p1;
+  V s1 = cross(r.d, e2);
+  float divisor = dot(s1, e1);
+  if (divisor == 0) return false;
+  float invDiv = 1.0f / divisor;
+  V d = r.o - pr.p1;
+  float b1 = dot(d, s1) * invDiv;
+  if (b1 < 0 || b1 > 1) return false;
+  V s2 = cross(d, e1);
+  float b2 = dot(r.d, s2) * invDiv;
+  if (b2 < 0 || b1 + b2 > 1) return false;
+  float t = dot(e2, s2) * invDiv;
+  if (t < r.tmin || t > r.tmax) return false;
+  t_out = t;
+  b1_out = b1;
+  b2_out = b2;
+  return true;
+}
+
+// the rest of triangleIntersect: partial derivatives and the DG (TriangleMesh.hs:182-207)
+static void triHitDG(const orc_scene& S, const Prim& pr, const Ray& r, float t, float b1, float b2,
+                     DG& dg, float& eps) {
+  const Mesh& m = S.meshes[pr.index];
+  float uv00 = 0, uv01 = 0, uv10 = 1, uv11 = 0, uv20 = 1, uv21 = 1;  // triangleDefaultUVs
+  int o1 = m.idx[3 * pr.tri], o2 = m.idx[3 * pr.tri + 1], o3 = m.idx[3 * pr.tri + 2];
+  if (!m.uv.empty()) {
+    uv00 = m.uv[2 * o1];
+    uv01 = m.uv[2 * o1 + 1];
+    uv10 = m.uv[2 * o2];
+    uv11 = m.uv[2 * o2 + 1];
+    uv20 = m.uv[2 * o3];
+    uv21 = m.uv[2 * o3 + 1];
+  }
+  V e1 = pr.p2 - pr.p1, e2 = pr.p3 - pr.p1;
+  V n = normalize(cross(e1, e2));
+  float du1 = uv00 - uv20, du2 = uv10 - uv20, dv1 = uv01 - uv21, dv2 = uv11 - uv21;
+  V dp1 = pr.p1 - pr.p3, dp2 = pr.p2 - pr.p3;
+  float determinant = du1 * dv2 - dv1 * du2;
+  V dpdu, dpdv;
+  if (determinant == 0) {
+    LC c = coordinateSystem(n);
+    dpdu = c.s;
+    dpdv = c.t;
+  } else {
+    float invDet = 1.0f / determinant;
+    dpdu = sv(invDet, sv(dv2, dp1) - sv(dv1, dp2));
+    dpdv = sv(invDet, sv(-du2, dp1) + sv(du1, dp2));
+  }
+  dg = mkDg(rayAt(r, t), dpdu, dpdv);
+  dg.tri = true;
+  dg.b1 = b1;
+  dg.b2 = b2;
+  eps = 1e-3f * t;
+}
+
+// triangleShadingGeometry with o2w = identity (TriangleMesh.hs:122-134);
+// Primitive.shadingGeometry is `const` for shapes and normal-less meshes.
+static DG shadingGeometry(const orc_scene& S, const Prim& pr, const DG& dgg) {
+  if (pr.is_shape) return dgg;
+  const Mesh& m = S.meshes[pr.index];
+  if (m.n.empty()) return dgg;
+  int o1 = m.idx[3 * pr.tri], o2 = m.idx[3 * pr.tri + 1], o3 = m.idx[3 * pr.tri + 2];
+  float b1 = dgg.b1, b2 = dgg.b2;
+  float b0 = 1.0f - b1 - b2;
+  V nsp = sv(b0, m.n[o1]) + sv(b1, m.n[o2]) + sv(b2, m.n[o3]);
+  static const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  V ns = normalize(transNormal(ident, nsp));
+  V ssp = normalize(dgg.dpdu);
+  V tsp = cross(ssp, ns);
+  V ss, ts;
+  if (sqLen(tsp) > 0) {
+    ss = cross(normalize(tsp), ns);
+    ts = normalize(tsp);
+  } else {
+    LC c = coordinateSystem(ns);
+    ss = c.s;
+    ts = c.t;
+  }
+  DG r = dgg;
+  r.n = ns;
+  r.dpdu = ss;
+  r.dpdv = ts;
+  return r;
+}
+
+struct Hit {
+  float t, eps;
+  int prim;
+  float b1, b2;
+};
+
+// Primitive.intersect for primitive i, without building the DG (cheap path):
+// returns the hit distance only.
+static inline bool primHitT(const orc_scene& S, int i, const Ray& r, float& t, float& b1,
+                            float& b2) {
+  const Prim& pr = S.prims[i];
+  if (!pr.is_shape) return triIntersect(pr, r, t, b1, b2);
+  const Shape& s = S.shapes[pr.index];
+  Ray ro = transRay(s.o2w.i, r);  // mkGeom: transRay w2o (Geometry.hs:33-36)
+  float e;
+  DG dg;
+  b1 = b2 = 0;
+  return shapeIntersect(s, ro, t, e, dg);
+}
+static inline bool primHitAny(const orc_scene& S, int i, const Ray& r) {
+  const Prim& pr = S.prims[i];
+  if (!pr.is_shape) {
+    float t, b1, b2;
+    return triIntersect(pr, r, t, b1, b2);
+  }
+  const Shape& s = S.shapes[pr.index];
+  return shapeIntersects(s, transRay(s.o2w.i, r));
+}
+
+// closest: the `near` fold over primitives in order (Primitive.hs:29-43)
+static bool closestBrute(const orc_scene& S, Ray r, Hit& h) {
+  bool any = false;
+  for (int i = 0; i < (int)S.prims.size(); i++) {
+    float t, b1, b2;
+    if (primHitT(S, i, r, t, b1, b2)) {
+      r.tmax = t;  // near: rayMax := intDist
+      h.t = t;
+      h.prim = i;
+      h.b1 = b1;
+      h.b2 = b2;
+      any = true;
+    }
+  }
+  return any;
+}
+static bool anyBrute(const orc_scene& S, const Ray& r) {
+  for (int i = 0; i < (int)S.prims.size(); i++)
+    if (primHitAny(S, i, r)) return true;
+  return false;
+}
+
+// ---- oracle BVH: median split over centroids, boxes widened so traversal
+// never prunes a primitive the fold above would hit; ties resolved exactly
+// as the fold (smaller t wins, equal t -> larger primitive index).
+static AabbF primBounds(const orc_scene& S, int i) {
+  const Prim& pr = S.prims[i];
+  AabbF b;
+  if (!pr.is_shape) {
+    b.lo = V{hmin(hmin(pr.p1.x, pr.p2.x), pr.p3.x), hmin(hmin(pr.p1.y, pr.p2.y), pr.p3.y),
+             hmin(hmin(pr.p1.z, pr.p2.z), pr.p3.z)};
+    b.hi = V{hmax(hmax(pr.p1.x, pr.p2.x), pr.p3.x), hmax(hmax(pr.p1.y, pr.p2.y), pr.p3.y),
+             hmax(hmax(pr.p1.z, pr.p2.z), pr.p3.z)};
+    return b;
+  }
+  const Shape& s = S.shapes[pr.index];
+  V lo, hi;
+  switch (s.kind) {  // objectBounds (Shape.hs:295-311)
+    case BLING_SHAPE_BOX: lo = V{s.p[0], s.p[1], s.p[2]}; hi = V{s.p[3], s.p[4], s.p[5]}; break;
+    case BLING_SHAPE_CYLINDER: lo = V{-s.p[0], -s.p[0], s.p[1]}; hi = V{s.p[0], s.p[0], s.p[2]}; break;
+    case BLING_SHAPE_DISK: lo = V{-s.p[1], -s.p[1], s.p[0]}; hi = V{s.p[1], s.p[1], s.p[0]}; break;
+    case BLING_SHAPE_QUAD: lo = V{-s.p[0], -s.p[1], 0}; hi = V{s.p[0], s.p[1], 0}; break;
+    default: lo = V{-s.p[0], -s.p[0], -s.p[0]}; hi = V{s.p[0], s.p[0], s.p[0]}; break;
+  }
+  b.lo = V{INF, INF, INF};
+  b.hi = V{-INF, -INF, -INF};
+  for (int c = 0; c < 8; c++) {  // transBox (Transform.hs:281-292)
+    V q{(c & 4) ? hi.x : lo.x, (c & 2) ? hi.y : lo.y, (c & 1) ? hi.z : lo.z};
+    V w = transPoint(s.o2w.m, q);
+    b.lo = V{hmin(b.lo.x, w.x), hmin(b.lo.y, w.y), hmin(b.lo.z, w.z)};
+    b.hi = V{hmax(b.hi.x, w.x), hmax(b.hi.y, w.y), hmax(b.hi.z, w.z)};
+  }
+  return b;
+}
+
+static void buildOracleBvh(orc_scene& S) {
+  int n = (int)S.prims.size();
+  S.order.resize(n);
+  std::vector<AabbF> bb(n);
+  std::vector<V> cen(n);
+  for (int i = 0; i < n; i++) {
+    S.order[i] = i;
+    bb[i] = primBounds(S, i);
+    cen[i] = sv(0.5f, bb[i].lo + bb[i].hi);
+  }
+  S.nodes.clear();
+  if (n == 0) return;
+  struct Task {
+    int node, b, e;
+  };
+  std::vector<Task> st;
+  S.nodes.push_back(BvhNode{});
+  st.push_back(Task{0, 0, n});
+  while (!st.empty()) {
+    Task tk = st.back();
+    st.pop_back();
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    double clo[3] = {1e300, 1e300, 1e300}, chi[3] = {-1e300, -1e300, -1e300};
+    for (int k = tk.b; k < tk.e; k++) {
+      const AabbF& a = bb[S.order[k]];
+      const V& c = cen[S.order[k]];
+      for (int d = 0; d < 3; d++) {
+        lo[d] = std::min(lo[d], (double)comp(a.lo, d));
+        hi[d] = std::max(hi[d], (double)comp(a.hi, d));
+        clo[d] = std::min(clo[d], (double)comp(c, d));
+        chi[d] = std::max(chi[d], (double)comp(c, d));
+      }
+    }
+    BvhNode& nd = S.nodes[tk.node];
+    for (int d = 0; d < 3; d++) {
+      // widen: hits computed in binary32 may land slightly outside the exact box
+      double pad = 1e-4 * (hi[d] - lo[d]) + 1e-5 * std::max(std::fabs(lo[d]), std::fabs(hi[d])) + 1e-30;
+      nd.lo[d] = lo[d] - pad;
+      nd.hi[d] = hi[d] + pad;
+    }
+    int cnt = tk.e - tk.b;
+    if (cnt <= 4) {
+      nd.left = tk.b;
+      nd.right = -cnt - 1;
+      continue;
+    }
+    int ax = 0;
+    for (int d = 1; d < 3; d++)
+      if (chi[d] - clo[d] > chi[ax] - clo[ax]) ax = d;
+    int mid = tk.b + cnt / 2;
+    std::nth_element(S.order.begin() + tk.b, S.order.begin() + mid, S.order.begin() + tk.e,
+                     [&](int a, int b) { return comp(cen[a], ax) < comp(cen[b], ax); });
+    int l = (int)S.nodes.size();
+    S.nodes.push_back(BvhNode{});
+    S.nodes.push_back(BvhNode{});
+    S.nodes[tk.node].left = l;
+    S.nodes[tk.node].right = l + 1;
+    st.push_back(Task{l, tk.b, mid});
+    st.push_back(Task{l + 1, mid, tk.e});
+  }
+}
+
+// slab test in double precision against the widened box
+static inline bool nodeHit(const BvhNode& nd, const double o[3], const double inv[3], double t0,
+                           double t1) {
+  for (int d = 0; d < 3; d++) {
+    double a = (nd.lo[d] - o[d]) * inv[d], b = (nd.hi[d] - o[d]) * inv[d];
+    if (std::isnan(a) || std::isnan(b)) continue;  // direction 0 and origin on the slab plane
+    if (a > b) std::swap(a, b);
+    t0 = std::max(t0, a);
+    t1 = std::min(t1, b);
+  }
+  return t0 <= t1;
+}
+
+static bool closestBvh(const orc_scene& S, const Ray& r, Hit& h) {
+  if (S.nodes.empty()) return false;
+  double o[3] = {r.o.x, r.o.y, r.o.z};
+  double inv[3] = {1.0 / (double)r.d.x, 1.0 / (double)r.d.y, 1.0 / (double)r.d.z};
+  bool any = false;
+  float best = r.tmax;
+  int bestp = -1;
+  int stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  Ray q = r;
+  while (sp) {
+    const BvhNode& nd = S.nodes[stack[--sp]];
+    double tlim = (double)best;
+    tlim = tlim + 1e-4 * std::fabs(tlim) + 1e-6;
+    if (!nodeHit(nd, o, inv, (double)r.tmin - 1e-6 - 1e-4 * std::fabs((double)r.tmin), tlim)) continue;
+    if (nd.right < 0) {
+      int cnt = -nd.right - 1;
+      for (int k = 0; k < cnt; k++) {
+        int pi = S.order[nd.left + k];
+        float t, b1, b2;
+        q.tmax = best;
+        if (primHitT(S, pi, q, t, b1, b2)) {
+          if (!any || t < best || (t == best && pi > bestp)) {
+            best = t;
+            bestp = pi;
+            h.t = t;
+            h.prim = pi;
+            h.b1 = b1;
+            h.b2 = b2;
+            any = true;
+          }
+        }
+      }
+    } else {
+      if (sp + 2 > 128) abort();
+      stack[sp++] = nd.left;
+      stack[sp++] = nd.right;
+    }
+  }
+  return any;
+}
+
+static bool anyBvh(const orc_scene& S, const Ray& r) {
+  if (S.nodes.empty()) return false;
+  double o[3] = {r.o.x, r.o.y, r.o.z};
+  double inv[3] = {1.0 / (double)r.d.x, 1.0 / (double)r.d.y, 1.0 / (double)r.d.z};
+  double tlo = (double)r.tmin - 1e-6 - 1e-4 * std::fabs((double)r.tmin);
+  double thi = (double)r.tmax + 1e-6 + 1e-4 * std::fabs((double)r.tmax);
+  int stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp) {
+    const BvhNode& nd = S.nodes[stack[--sp]];
+    if (!nodeHit(nd, o, inv, tlo, thi)) continue;
+    if (nd.right < 0) {
+      int cnt = -nd.right - 1;
+      for (int k = 0; k < cnt; k++)
+        if (primHitAny(S, S.order[nd.left + k], r)) return true;
+    } else {
+      if (sp + 2 > 128) abort();
+      stack[sp++] = nd.left;
+      stack[sp++] = nd.right;
+    }
+  }
+  return false;
+}
+
+struct Isect {
+  float t, eps;
+  int prim;
+  DG dg;  // intGeometry: world-space true geometry
+};
+// scIntersect returning the full Intersection (Primitive.hs:57-65, Geometry.hs:33-36)
+static bool sceneIntersect(const orc_scene& S, const Ray& r, Isect& it) {
+  Hit h;
+  if (!closestBvh(S, r, h)) return false;
+  const Prim& pr = S.prims[h.prim];
+  it.t = h.t;
+  it.prim = h.prim;
+  if (!pr.is_shape) {
+    triHitDG(S, pr, r, h.t, h.b1, h.b2, it.dg, it.eps);
+  } else {
+    const Shape& s = S.shapes[pr.index];
+    Ray ro = transRay(s.o2w.i, r);
+    float t, e;
+    DG dg;
+    shapeIntersect(s, ro, t, e, dg);
+    it.eps = e;
+    it.dg = transDg(s.o2w.m, s.o2w.i, dg);
+  }
+  return true;
+}
+static bool occluded(const orc_scene& S, const Ray& r) { return anyBvh(S, r); }
+
+// ---------------------------------------------------------------- Monte Carlo
+// concentricSampleDisk (Montecarlo.hs:389-406)
+static void concentricSampleDisk(float u1, float u2, float& ox, float& oy) {
+  float sx = u1 * 2.0f - 1.0f, sy = u2 * 2.0f - 1.0f;
+  if (sx == 0 && sy == 0) {
+    ox = 0;
+    oy = 0;
+    return;
+  }
+  float r, thp;
+  if (sx >= -sy) {
+    if (sx > sy) {
+      if (sy > 0) {
+        r = sx;
+        thp = sy / sx;
+      } else {
+        r = sx;
+        thp = 8.0f + sy / sx;
+      }
+    } else {
+      r = sy;
+      thp = 2.0f - sx / sy;
+    }
+  } else if (sx <= sy) {
+    r = -sx;
+    thp = 4.0f - sy / (-sx);
+  } else {
+    r = -sy;
+    thp = 6.0f + sx / (-sy);
+  }
+  float theta = thp * PI / 4.0f;
+  ox = r * cosf(theta);
+  oy = r * sinf(theta);
+}
+// cosineSampleHemisphere (Montecarlo.hs:375-378)
+static V cosineSampleHemisphere(float u1, float u2) {
+  float x, y;
+  concentricSampleDisk(u1, u2, x, y);
+  return V{x, y, sqrtf(hmax(0.0f, 1.0f - x * x - y * y))};
+}
+// uniformSampleSphere (Montecarlo.hs:410-415)
+static V uniformSampleSphere(float u1, float u2) {
+  float u = u1 * 2.0f - 1.0f;
+  float s = sqrtf(1.0f - (u * u));
+  float omega = u2 * 2.0f * PI;
+  return V{s * cosf(omega), s * sinf(omega), u};
+}
+// uniformConePdf / uniformSampleCone (Montecarlo.hs:356-373)
+static float uniformConePdf(float cosThetaMax) {
+  if (cosThetaMax >= 1) return 0;
+  return 1.0f / (TWO_PI * (1.0f - cosThetaMax));
+}
+static V uniformSampleCone(const LC& c, float cosThetaMax, float u1, float u2) {
+  float cosTheta = lerp(u1, cosThetaMax, 1.0f);
+  float sinTheta = sqrtf(1.0f - cosTheta * cosTheta);
+  float phi = u2 * TWO_PI;
+  float a = cosf(phi) * sinTheta, b = sinf(phi) * sinTheta;
+  return V{c.s.x * a, c.s.y * a, c.s.z * a} + V{c.t.x * b, c.t.y * b, c.t.z * b} +
+         V{c.n.x * cosTheta, c.n.y * cosTheta, c.n.z * cosTheta};
+}
+// powerHeuristic (Montecarlo.hs:342-345)
+static float powerHeuristic(float fPdf, float gPdf) {
+  float f = 1.0f * fPdf, g = 1.0f * gPdf;
+  return (f * f) / (f * f + g * g);
+}
+// Dist1D (Montecarlo.hs:263-301)
+static void mkDist1D(const std::vector<float>& func, std::vector<float>& cdf, float& fi) {
+  int n = (int)func.size();
+  std::vector<float> i(n + 1);
+  i[0] = 0;
+  for (int k = 0; k < n; k++) i[k + 1] = i[k] + func[k] / (float)n;
+  fi = i[n];
+  cdf.resize(n + 1);
+  for (int k = 0; k <= n; k++) cdf[k] = fi != 0 ? i[k] / fi : (float)k / (float)n;
+}
+static int upperBound(const std::vector<float>& v, float u) {
+  int n = (int)v.size();
+  int found = -1;
+  for (int k = 0; k < n; k++)
+    if (v[k] >= u) {
+      found = k;
+      break;
+    }
+  int x = found < 0 ? n - 1 : found - 1;
+  return std::min(n - 2, std::max(0, x));
+}
+static void sampleContinuous1D(const std::vector<float>& func, const std::vector<float>& cdf,
+                               float fi, float u, float& x, float& pdf, int& off) {
+  off = upperBound(cdf, u);
+  pdf = fi == 0 ? 0 : func[off] / fi;
+  float du = (u - cdf[off]) / (cdf[off + 1] - cdf[off]);
+  x = ((float)off + du) / (float)func.size();
+}
+
+// ---------------------------------------------------------------- BSDFs
+// Reflection.hs:48-88 helpers
+static inline float cosTheta(V v) { return v.z; }
+static inline float absCosTheta(V v) { return fabsf(v.z); }
+static inline float sinTheta2(V v) { return hmax(0.0f, 1.0f - v.z * v.z); }
+static inline float sinTheta(V v) { return sqrtf(sinTheta2(v)); }
+static inline float cosPhi(V v) {
+  float st = sinTheta(v);
+  return st == 0 ? 1.0f : clampf(v.x / st, -1, 1);
+}
+static inline float sinPhi(V v) {
+  float st = sinTheta(v);
+  return st == 0 ? 0.0f : clampf(v.y / st, -1, 1);
+}
+static inline bool sameHemisphere(V a, V b) { return a.z * b.z > 0; }
+static inline V toSameHemisphere(V wo, V wi) { return wo.z < 0 ? V{wi.x, wi.y, -wi.z} : wi; }
+
+// Fresnel (Fresnel.hs:146-195)
+static float frDielScalar(float etai, float etat, float cosi) {
+  float c = hmax(0.0f, 1.0f - cosi * cosi);
+  float costp = cosi > 0 ? c / (etat * etat) : c * (etat * etat);
+  float cost = sqrtf(1.0f - clampf(costp, 0, 1));
+  float ac = fabsf(cosi);
+  float eta = etat / etai;  // frDiel: etat / etai
+  float rParlp = eta * ac;
+  float rParl = (cost - rParlp) / (cost + rParlp);
+  float rPerpp = eta * cost;
+  float rPerp = (ac - rPerpp) / (ac + rPerpp);
+  return (rParl * rParl + rPerp * rPerp) * 0.5f;
+}
+static Spec frEval(const Fresnel& f, float cosi) {
+  if (f.kind == FR_NOOP) return WHITE;
+  if (f.kind == FR_DIEL) return sConst(frDielScalar(f.ei, f.et, cosi));
+  float acosi = fabsf(cosi);
+  Spec s;
+  for (int i = 0; i < 16; i++) {
+    float eta = f.eta.v[i], k = f.k.v[i];
+    float tmpF = eta * eta + k * k;
+    float tmp = (eta * eta + k * k) * (acosi * acosi);
+    float ec2 = eta * (2.0f * acosi);
+    float a2 = acosi * acosi;
+    float rPer2 = (tmpF - ec2 + a2) / (tmpF + ec2 + a2);
+    float rPar2 = (tmp - ec2 + 1.0f) / (tmp + ec2 + 1.0f);
+    s.v[i] = (rPer2 + rPar2) / 2.0f;
+  }
+  return s;
+}
+
+// Blinn distribution (Microfacet.hs:113-195)
+static float mfG(V wo, V wi, V wh) {
+  float nDotWh = absCosTheta(wh), nDotWo = absCosTheta(wo), nDotWi = absCosTheta(wi);
+  float woDotWh = absDot(wo, wh);
+  return hmin(1.0f, hmin(2.0f * nDotWh * nDotWo / woDotWh, 2.0f * nDotWh * nDotWi / woDotWh));
+}
+static float blinnPdf(float e, V wh) {
+  return (e + 1.0f) * powf(absCosTheta(wh), e) * INV_TWO_PI;
+}
+static float blinnD(float e, V wh) {
+  return (e + 2.0f) * INV_TWO_PI * powf(absCosTheta(wh), e);
+}
+static void blinnSample(float e, float u1, float u2, V& wh, float& d, float& pdf) {
+  float cost = powf(u1, 1.0f / (e + 1.0f));
+  float sint = sqrtf(hmax(0.0f, 1.0f - cost * cost));
+  float phi = u2 * 2.0f * PI;
+  wh = V{sint * cosf(phi), sint * sinf(phi), cost};
+  float f = powf(cost, e) * INV_TWO_PI;
+  d = (e + 2.0f) * f;
+  pdf = (e + 1.0f) * f;
+}
+static float fixExponent(float e) { return (e > 10000 || std::isnan(e)) ? 10000.0f : e; }
+
+// Oren-Nayar core (Diffuse.hs:53-65)
+static Spec orenNayar(const BxDF& b, V wo, V wi) {
+  float sinti = sinTheta(wi), sinto = sinTheta(wo);
+  float sina, tanb;
+  if (absCosTheta(wi) > absCosTheta(wo)) {
+    sina = sinto;
+    tanb = sinti / absCosTheta(wi);
+  } else {
+    sina = sinti;
+    tanb = sinto / absCosTheta(wo);
+  }
+  float maxcos = 0;
+  if (sinti > 1e-4f && sinto > 1e-4f) {
+    float sinpi = sinPhi(wi), cospi = cosPhi(wi), sinpo = sinPhi(wo), cospo = cosPhi(wo);
+    maxcos = hmax(0.0f, cospi * cospo + sinpi * sinpo);
+  }
+  return sScale(b.r, b.A + b.B * maxcos * sina * tanb);
+}
+
+// bxdfEval b wo wi
+static Spec bxEval(const BxDF& b, V wo, V wi) {
+  switch (b.kind) {
+    case BX_LAMBERT: return sScale(b.r, INV_PI * absCosTheta(wo));  // Diffuse.hs:26
+    case BX_OREN: return sScale(orenNayar(b, wo, wi), INV_PI * absCosTheta(wo));
+    case BX_MICRO: {  // Microfacet.hs:21-32
+      float costo = absCosTheta(wo), costi = absCosTheta(wi);
+      if (costi == 0 || costo == 0) return BLACK;
+      V whp = wi + wo;
+      if (whp.x == 0 && whp.y == 0 && whp.z == 0) return BLACK;
+      V wh = normalize(whp);
+      if (cosTheta(wh) < 0) return BLACK;
+      float costh = dot(wi, wh);
+      float x = blinnD(b.e, wh) * mfG(wo, wi, wh) / (4.0f * costi);
+      return sScale(b.r * frEval(b.fr, costh), x);
+    }
+    default: return BLACK;  // specular: e _ _ = black
+  }
+}
+// bxdfPdf b wo wi
+static float bxPdf(const BxDF& b, V wo, V wi) {
+  switch (b.kind) {
+    case BX_LAMBERT:
+    case BX_OREN: return sameHemisphere(wo, wi) ? INV_PI * absCosTheta(wi) : 0.0f;  // cosPdf
+    case BX_MICRO: {
+      V whp = wo + wi;
+      if (sqLen(whp) == 0) return 0;
+      V wh = normalize(whp);
+      if (cosTheta(wh) < 0) return 0;
+      return blinnPdf(b.e, wh) / (4.0f * absDot(wo, wh));
+    }
+    default: return 0;
+  }
+}
+// bxdfSample b False wo u -> (f, wi, pdf)
+static void bxSample(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf) {
+  switch (b.kind) {
+    case BX_LAMBERT: {  // cosSample (Diffuse.hs:14-22)
+      wi = toSameHemisphere(wo, cosineSampleHemisphere(u1, u2));
+      if (sameHemisphere(wo, wi)) {
+        f = b.r;
+        pdf = bxPdf(b, wo, wi);
+      } else {
+        f = BLACK;
+        wi = wo;
+        pdf = 0;
+      }
+      return;
+    }
+    case BX_OREN: {  // Diffuse.hs:38-42
+      wi = toSameHemisphere(wo, cosineSampleHemisphere(u1, u2));
+      if (sameHemisphere(wo, wi)) {
+        f = orenNayar(b, wo, wi);
+        pdf = bxPdf(b, wo, wi);
+      } else {
+        f = BLACK;
+        pdf = 0;
+      }
+      return;
+    }
+    case BX_SPEC_REFL: {  // Specular.hs:86-87
+      f = b.r * frEval(b.fr, cosTheta(wo));
+      wi = V{-wo.x, -wo.y, wo.z};
+      pdf = 1;
+      return;
+    }
+    case BX_SPEC_TRANS: {  // sampleSpecTrans (Specular.hs:100-124), adj = False
+      bool entering = cosTheta(wo) > 0;
+      float ei = entering ? b.ei : b.et, et = entering ? b.et : b.ei;
+      float sini2 = sinTheta2(wo);
+      float eta = ei / et;
+      float eta2 = eta * eta;
+      float sint2 = eta2 * sini2;
+      if (sint2 >= 1) {
+        f = BLACK;
+        wi = wo;
+        pdf = 0;
+        return;
+      }
+      float c = sqrtf(hmax(0.0f, 1.0f - sint2));
+      float cost = entering ? -c : c;
+      wi = V{eta * (-wo.x), eta * (-wo.y), cost};
+      Spec fr = sConst(frDielScalar(ei, et, cost));
+      f = sScale((WHITE - fr) * b.r, eta2);
+      pdf = 1;
+      return;
+    }
+    default: {  // microfacet (Microfacet.hs:42-54)
+      V whp;
+      float d, p;
+      blinnSample(b.e, u1, u2, whp, d, p);
+      V wh = cosTheta(whp) < 0 ? -whp : whp;
+      wi = sv(2.0f * dot(wo, wh), wh) - wo;
+      float costH = dot(wo, wh);
+      float fact = d * fabsf(costH) / p * mfG(wo, wi, wh);
+      Spec fp = b.r * frEval(b.fr, costH);
+      if (sameHemisphere(wo, wi)) {
+        f = sScale(fp, fact / absCosTheta(wi));
+        pdf = p / (4.0f * fabsf(costH));
+      } else {
+        f = BLACK;
+        wi = wo;
+        pdf = 0;
+      }
+      return;
+    }
+  }
+}
+
+struct Bsdf {  // Reflection.hs:201-218
+  BxDF c[2];
+  int n;
+  LC cs;
+  V p;
+  V ng;
+};
+
+// mkBsdf' with the material's BxDFs (Material.hs:228-292)
+static Bsdf materialBsdf(const Material& m, const DG& dgg, const DG& dgs) {
+  Bsdf b;
+  b.n = 0;
+  V nn = dgs.n, sn = normalize(dgs.dpdu);
+  b.cs = LC{sn, cross(nn, sn), nn};
+  b.p = dgs.p;
+  b.ng = dgg.n;
+  auto add = [&](const BxDF& x) { b.c[b.n++] = x; };
+  BxDF x{};
+  switch (m.kind) {
+    case BLING_MAT_MATTE:
+      if (m.sigma == 0) {
+        x.kind = BX_LAMBERT;
+        x.type = T_REFL | T_DIFF;
+        x.r = m.kd;
+      } else {
+        x.kind = BX_OREN;
+        x.type = T_REFL | T_DIFF;
+        x.r = m.kd;
+        float s = clampf(m.sigma, 0, 1);
+        float sig2 = s * s;
+        x.A = 1.0f - (sig2 / (2.0f * (sig2 + 0.33f)));
+        x.B = 0.45f * sig2 / (sig2 + 0.09f);
+      }
+      add(x);
+      break;
+    case BLING_MAT_PLASTIC: {
+      x.kind = BX_LAMBERT;
+      x.type = T_REFL | T_DIFF;
+      x.r = m.kd;
+      add(x);
+      BxDF y{};
+      y.kind = BX_MICRO;
+      y.type = T_REFL | T_GLOSSY;
+      y.r = m.ks;
+      y.e = fixExponent(1.0f / m.rough);
+      y.fr.kind = FR_DIEL;
+      y.fr.ei = 1.0f;
+      y.fr.et = 1.5f;
+      add(y);
+      break;
+    }
+    case BLING_MAT_METAL: {
+      x.kind = BX_MICRO;
+      x.type = T_REFL | T_GLOSSY;
+      x.r = WHITE;
+      x.e = fixExponent(1.0f / m.rough);
+      x.fr.kind = FR_COND;
+      x.fr.eta = m.eta;
+      x.fr.k = m.k;
+      add(x);
+      break;
+    }
+    default: {  // glass
+      x.kind = BX_SPEC_REFL;
+      x.type = T_REFL | T_SPEC;
+      x.r = sClamp(0, 1, m.ks);
+      x.fr.kind = FR_DIEL;
+      x.fr.ei = 1.0f;
+      x.fr.et = m.ior;
+      add(x);
+      BxDF y{};
+      y.kind = BX_SPEC_TRANS;
+      y.type = T_TRANS | T_SPEC;
+      y.r = sClamp(0, 1, m.kt);
+      y.ei = 1.0f;
+      y.et = m.ior;
+      add(y);
+      break;
+    }
+  }
+  return b;
+}
+
+struct BsdfSample {
+  int type;
+  float pdf;
+  Spec f;
+  V wi;
+};
+
+// sampleBsdf'' False bxdfAll (Reflection.hs:278-316)
+static BsdfSample sampleBsdf(const Bsdf& b, V woW, float uComp, float u1, float u2) {
+  BsdfSample empty{T_REFL | T_DIFF, 0, BLACK, V{0, 1, 0}};
+  if (b.n == 0) return empty;
+  V wo = worldToLocal(b.cs, woW);
+  int cntm = b.n;
+  float cntf = (float)cntm;
+  float invCnt = 1.0f / cntf;
+  int sNum = std::max(0, std::min(cntm - 1, (int)floorf(uComp * cntf)));
+  const BxDF& bx = b.c[sNum];
+  Spec fSample;
+  V wi;
+  float pdfp;
+  bxSample(bx, wo, u1, u2, fSample, wi, pdfp);
+  V wiW = localToWorld(b.cs, wi);
+  float sideTest = dot(wiW, b.ng) / dot(woW, b.ng);
+  if (pdfp == 0 || sideTest == 0) return empty;
+  bool wantTrans = sideTest < 0;
+  auto flt = [&](const BxDF& x) { return wantTrans ? (x.type & T_TRANS) != 0 : (x.type & T_REFL) != 0; };
+  if (!flt(bx)) return empty;
+  if (bx.type & T_SPEC) return BsdfSample{bx.type, pdfp * invCnt, sScale(fSample, cntf), wiW};
+  if (cntm == 1) return BsdfSample{bx.type, pdfp, fSample, wiW};
+  float others = 0.0f;
+  for (int i = 0; i < cntm; i++)
+    if (i != sNum) others = others + bxPdf(b.c[i], wo, wi);
+  float pdf = (pdfp + others) * invCnt;
+  Spec fOthers = BLACK;
+  for (int i = 0; i < cntm; i++)
+    if (i != sNum && flt(b.c[i])) fOthers = fOthers + bxEval(b.c[i], wi, wo);  // flip
+  Spec fSum = sScale(sScale(fSample, pdfp) + fOthers, 1.0f / pdf);
+  return BsdfSample{bx.type, pdf, fSum, wiW};
+}
+// evalBsdf False (Reflection.hs:318-332)
+static Spec evalBsdf(const Bsdf& b, V woW, V wiW) {
+  float cosWo = dot(woW, b.ng);
+  float sideTest = dot(wiW, b.ng) / cosWo;
+  if (sideTest == 0) return BLACK;
+  if (fabsf(cosWo) < 1e-5f) return BLACK;
+  bool wantTrans = sideTest < 0;
+  V wo = worldToLocal(b.cs, woW), wi = worldToLocal(b.cs, wiW);
+  Spec f = BLACK;
+  for (int i = 0; i < b.n; i++) {
+    const BxDF& x = b.c[i];
+    bool ok = wantTrans ? (x.type & T_TRANS) != 0 : (x.type & T_REFL) != 0;
+    if (ok) f = f + bxEval(x, wi, wo);  // flip (bxdfEval b) wo wi
+  }
+  return f;
+}
+// bsdfPdf (Reflection.hs:251-257)
+static float bsdfPdf(const Bsdf& b, V woW, V wiW) {
+  if (b.n == 0) return 0;
+  V wo = worldToLocal(b.cs, woW), wi = worldToLocal(b.cs, wiW);
+  float s = 0.0f;
+  for (int i = 0; i < b.n; i++) s = s + bxPdf(b.c[i], wo, wi);
+  return s / (float)b.n;
+}
+
+// ---------------------------------------------------------------- lights
+// sampleShape' / sampleShape (Shape.hs:362-409), local space
+static bool insideSphere(float r, V p) { return sqLen(p) - r * r < 1e-4f; }
+static void sampleShapeP(const Shape& s, float u1, float u2, V& p, V& n) {
+  switch (s.kind) {
+    case BLING_SHAPE_BOX: {
+      int axis = std::min(2, (int)floorf(u1 * 3.0f));
+      float u1p = (u1 - (float)axis / 3.0f) * 3.0f;  // remapRand 3 (Math.hs:113-121)
+      int nf = std::min(1, (int)floorf(u2 * 2.0f));
+      float u2p = (u2 - (float)nf / 2.0f) * 2.0f;
+      n = setComp(axis, (float)nf * 2.0f - 1.0f, mkV(0, 0, 0));
+      int oa0 = (axis + 1) % 3, oa1 = (axis + 2) % 3;
+      V pmin{s.p[0], s.p[1], s.p[2]}, pmax{s.p[3], s.p[4], s.p[5]};
+      V base = nf == 0 ? pmin : pmax;
+      p = setComp(oa0, lerp(u1p, comp(pmin, oa0), comp(pmax, oa0)),
+                  setComp(oa1, lerp(u2p, comp(pmin, oa1), comp(pmax, oa1)), base));
+      return;
+    }
+    case BLING_SHAPE_CYLINDER: {
+      float z = lerp(u1, s.p[1], s.p[2]);
+      float phi = lerp(u2, 0, TWO_PI);
+      p = V{s.p[0] * cosf(phi), s.p[0] * sinf(phi), z};
+      n = normalize(V{p.x, p.y, 0});
+      return;
+    }
+    case BLING_SHAPE_DISK: {
+      float r = lerp(u1, s.p[2], s.p[1]);
+      float phi = lerp(u2, 0, s.p[3]);
+      p = V{r * cosf(phi), r * sinf(phi), s.p[0]};
+      n = V{0, 0, -1};
+      return;
+    }
+    case BLING_SHAPE_QUAD:
+      p = V{lerp(u1, -s.p[0], s.p[0]), lerp(u2, -s.p[1], s.p[1]), 0};
+      n = V{0, 0, -1};
+      return;
+    default: {
+      V q = uniformSampleSphere(u1, u2);
+      p = q * V{s.p[0], s.p[0], s.p[0]};
+      n = q;
+      return;
+    }
+  }
+}
+static void sampleShape(const Shape& s, V pt, float u1, float u2, V& ps, V& ns) {
+  if (s.kind == BLING_SHAPE_SPHERE && !insideSphere(s.p[0], pt)) {
+    float r = s.p[0];
+    V dn = normalize(-pt);
+    LC cs = coordinateSystem(dn);
+    float cosThetaMax = sqrtf(hmax(0.0f, 1.0f - (r * r) / sqLen(pt)));
+    V d = uniformSampleCone(cs, cosThetaMax, u1, u2);
+    Ray ray{pt, d, 0, INF};
+    float t, e;
+    DG dg;
+    ps = shapeIntersect(s, ray, t, e, dg) ? rayAt(ray, t) : dn * V{r, r, r};
+    ns = normalize(ps);
+    return;
+  }
+  sampleShapeP(s, u1, u2, ps, ns);
+}
+// shapePdf / generalPdf (Shape.hs:333-350)
+static float generalPdf(const Shape& s, V p, V wi) {
+  Ray r{p, wi, 1e-3f, INF};
+  float t, e;
+  DG dg;
+  if (!shapeIntersect(s, r, t, e, dg)) return 0;
+  float pd = sqLen(p - rayAt(r, t)) / (absDot(dg.n, -wi) * shapeArea(s));
+  return std::isinf(pd) ? 0.0f : pd;
+}
+static float shapePdf(const Shape& s, V p, V wi) {
+  if (s.kind == BLING_SHAPE_SPHERE && !insideSphere(s.p[0], p)) {
+    float r = s.p[0];
+    float sinThetaMax2 = r * r / sqLen(p);
+    float cosThetaMax = sqrtf(hmax(0.0f, 1.0f - sinThetaMax2));
+    return uniformConePdf(cosThetaMax);
+  }
+  return generalPdf(s, p, wi);
+}
+
+// spherical helpers (Math.hs:141-169, Types.hs:31-39)
+static V sphericalDirection(float sint, float cost, float phi) {
+  return V{sint * cosf(phi), sint * sinf(phi), cost};
+}
+static float sphericalTheta(V v) { return acosf(hmax(-1.0f, hmin(1.0f, v.z))); }
+static float sphericalPhi(V v) {
+  float p = hatan2(v.y, v.x);
+  return p < 0 ? p + 2.0f * PI : p;
+}
+// the lat-long map lookup: nearest texel (u in [0,1) across, v in [0,1) down)
+static Spec envLookup(const Light& l, float u, float v) {
+  int x = (int)floorf(u * (float)l.w), y = (int)floorf(v * (float)l.h);
+  x = std::max(0, std::min(l.w - 1, x));
+  y = std::max(0, std::min(l.h - 1, y));
+  return l.env[(size_t)y * l.w + x];
+}
+
+struct LightSample {  // Light.hs:23-29
+  Spec li;
+  V wi;
+  Ray ray;
+  float pdf;
+  bool delta;
+};
+
+// Light.sample (Light.hs:122-160)
+static LightSample lightSample(const orc_scene& S, const Light& l, V p, float eps, V n, float u1,
+                               float u2) {
+  LightSample ls;
+  if (l.kind == LIGHT_AREA) {
+    const Shape& s = S.shapes[l.shape];
+    V pl = transPoint(s.o2w.i, p);  // w2l
+    V ps, ns;
+    sampleShape(s, pl, u1, u2, ps, ns);
+    V wi = normalize(ps - pl);
+    ls.li = dot(ns, wi) < 0 ? s.emission : BLACK;
+    ls.wi = transVector(s.o2w.m, wi);
+    ls.pdf = shapePdf(s, pl, wi);
+    Ray rl{pl, wi, eps, len(ps - pl) - eps};
+    ls.ray = transRay(s.o2w.m, rl);
+    ls.delta = false;
+    return ls;
+  }
+  if (l.kind == BLING_LIGHT_DIRECTIONAL) {
+    ls.li = sScale(l.spec, absDot(n, l.vec));
+    ls.wi = l.vec;
+    ls.ray = Ray{p, l.vec, eps, INF};
+    ls.pdf = 1;
+    ls.delta = true;
+    return ls;
+  }
+  if (l.kind == BLING_LIGHT_POINT) {
+    ls.li = sScale(l.spec, 1.0f / sqLen(l.vec - p));
+    ls.wi = normalize(l.vec - p);
+    ls.ray = Ray{p, l.vec - p, eps, INF};
+    ls.pdf = 1;
+    ls.delta = true;
+    return ls;
+  }
+  // infinite (Light.hs:130-141)
+  float v, pdf1, u, pdf0;
+  int im, iu;
+  sampleContinuous1D(l.mfunc, l.mcdf, l.mint, u2, v, pdf1, im);
+  sampleContinuous1D(l.cfunc[im], l.ccdf[im], l.cint[im], u1, u, pdf0, iu);
+  float mapPdf = pdf0 * pdf1;
+  LightSample none{BLACK, V{0, 1, 0}, Ray{V{0, 0, 0}, V{0, 1, 0}, 0, 1}, 0, false};
+  if (mapPdf == 0) return none;
+  float phi = u * 2.0f * PI, theta = v * PI;  // cartToSph
+  float sint = sinf(theta);
+  if (sint == 0) return none;
+  ls.li = envLookup(l, u, v);
+  V dl = sphericalDirection(sinf(theta), cosf(theta), phi);
+  ls.wi = transVector(l.w2l.i, dl);  // inverse w2l
+  ls.ray = Ray{p, ls.wi, eps, INF};
+  ls.pdf = mapPdf / (2.0f * PI * PI * sint);
+  ls.delta = false;
+  return ls;
+}
+// Light.le (Light.hs:98-106)
+static Spec lightLe(const Light& l, const Ray& r) {
+  if (l.kind != BLING_LIGHT_INFINITE) return BLACK;
+  V wh = normalize(transVector(l.w2l.m, r.d));
+  float phi = sphericalPhi(wh), theta = sphericalTheta(wh);
+  return envLookup(l, phi / (2.0f * PI), theta / PI);  // sphToCart
+}
+// Light.pdf (Light.hs:215-229)
+static float lightPdf(const orc_scene& S, const Light& l, V p, V wi) {
+  if (l.kind == LIGHT_AREA) {
+    const Shape& s = S.shapes[l.shape];
+    return shapePdf(s, transPoint(s.o2w.i, p), transVector(s.o2w.i, wi));
+  }
+  if (l.kind != BLING_LIGHT_INFINITE) return 0;
+  V d = transVector(l.w2l.m, wi);
+  float theta = sphericalTheta(d), phi = sphericalPhi(d);
+  float sint = sinf(theta);
+  if (sint == 0) return 0;
+  float u = phi / (2.0f * PI), v = theta / PI;
+  // pdfDist2D (Montecarlo.hs:324-333)
+  int nu = (int)l.cfunc[0].size(), nv = (int)l.mfunc.size();
+  int iu = std::max(0, std::min(nu - 1, (int)floorf(u * (float)nu)));
+  int iv = std::max(0, std::min(nv - 1, (int)floorf(v * (float)nv)));
+  float pd;
+  if (l.mint * l.cint[iv] == 0)
+    pd = 0;
+  else
+    pd = (l.cfunc[iv][iu] * l.mfunc[iv]) / (l.cint[iv] * l.mint);
+  return pd / (2.0f * PI * PI * sint);
+}
+
+// ---------------------------------------------------------------- integrator
+struct Counters {
+  uint64_t closest = 0, any = 0;
+};
+
+// intLe (Primitive.hs:68-76) + lEmit (Light.hs:85-96)
+static Spec intLe(const orc_scene& S, const Isect& it, V wo) {
+  const Prim& pr = S.prims[it.prim];
+  if (!pr.is_shape) return BLACK;
+  const Shape& s = S.shapes[pr.index];
+  if (!s.emissive) return BLACK;
+  return dot(it.dg.n, wo) > 0 ? s.emission : BLACK;
+}
+static int intLightId(const orc_scene& S, const Isect& it) {
+  const Prim& pr = S.prims[it.prim];
+  if (!pr.is_shape) return -1;
+  const Shape& s = S.shapes[pr.index];
+  return s.emissive ? s.light_id : -1;
+}
+
+// estimateDirect = sampleLightMis + sampleBsdfMis (Scene.hs:184-222)
+static Spec estimateDirect(const orc_scene& S, int li, V p, float eps, V n, V wo, const Bsdf& bsdf,
+                           float ld1, float ld2, float ubc, float ubd1, float ubd2, Counters& C) {
+  const Light& l = S.lights[li];
+  Spec ls = BLACK;
+  {
+    LightSample smp = lightSample(S, l, p, eps, n, ld1, ld2);
+    if (!(smp.pdf == 0 || isBlack(smp.li))) {
+      Spec f = evalBsdf(bsdf, wo, smp.wi);
+      if (!isBlack(f)) {
+        C.any++;
+        if (!occluded(S, smp.ray)) {
+          if (smp.delta)
+            ls = sScale(f * smp.li, 1.0f / smp.pdf);
+          else {
+            float w = powerHeuristic(smp.pdf, bsdfPdf(bsdf, wo, smp.wi));
+            ls = sScale(f * smp.li, w / smp.pdf);
+          }
+        }
+      }
+    }
+  }
+  Spec bs = BLACK;
+  {
+    BsdfSample b = sampleBsdf(bsdf, wo, ubc, ubd1, ubd2);
+    if (!(b.pdf == 0 || isBlack(b.f))) {
+      Ray ray{p, b.wi, eps, INF};
+      Isect hit;
+      C.closest++;
+      bool h = sceneIntersect(S, ray, hit);
+      auto sc = [&](const Spec& lr) {
+        float lPdf = lightPdf(S, l, p, b.wi);
+        return sScale(b.f * lr, powerHeuristic(b.pdf, lPdf));
+      };
+      if (h) {
+        int lid = intLightId(S, hit);
+        if (lid >= 0 && l.kind == LIGHT_AREA && lid == l.id) bs = sc(intLe(S, hit, -b.wi));
+      } else {
+        bs = sc(lightLe(l, ray));
+      }
+    }
+  }
+  return ls + bs;
+}
+
+// Path.hs:41-87, iterated instead of recursed; returns L
+static Spec pathLi(const orc_scene& S, const Sampler& smp, Ray ray, int md, int rrDepth,
+                   Counters& C) {
+  Spec t = WHITE, l = BLACK;
+  bool spec = true;
+  Isect it;
+  C.closest++;
+  bool hit = sceneIntersect(S, ray, it);
+  for (int depth = 0;; depth++) {
+    if (!hit) {
+      if (spec) {
+        Spec sum = BLACK;
+        for (const Light& lt : S.lights) sum = sum + lightLe(lt, ray);
+        return l + t * sum;
+      }
+      return l;
+    }
+    if (depth == md) return l;
+    float lNumU = rnd1(smp, 1 + 4 * depth);
+    float ld1, ld2;
+    rnd2(smp, 1 + 3 * depth, ld1, ld2);
+    float lBsdfCompU = rnd1(smp, 2 + 4 * depth);
+    float lb1, lb2;
+    rnd2(smp, 2 + 3 * depth, lb1, lb2);
+    V rd = ray.d;
+    Spec intl = spec ? intLe(S, it, rd) : BLACK;
+    V wo = -rd;
+    const Prim& pr = S.prims[it.prim];
+    int mat = pr.is_shape ? S.shapes[pr.index].material : S.meshes[pr.index].material;
+    DG dgs = shadingGeometry(S, pr, it.dg);
+    Bsdf bsdf = materialBsdf(S.mats[mat], it.dg, dgs);
+    V n = bsdf.cs.n;
+    V p = bsdf.p;
+    float eps = it.eps;
+    // sampleOneLight (Scene.hs:233-241)
+    Spec direct = BLACK;
+    int lc = (int)S.lights.size();
+    if (lc == 1) {
+      direct = estimateDirect(S, 0, p, eps, n, wo, bsdf, ld1, ld2, lBsdfCompU, lb1, lb2, C);
+    } else if (lc > 1) {
+      int ln = std::min((int)floorf(lNumU * (float)lc), lc - 1);
+      direct = sScale(estimateDirect(S, ln, p, eps, n, wo, bsdf, ld1, ld2, lBsdfCompU, lb1, lb2, C),
+                      (float)lc);
+    }
+    Spec lHere = intl + direct;
+    l = l + t * lHere;
+    float pc = depth <= rrDepth ? 1.0f : hmin(0.75f, sY(t));
+    float x = rnd1(smp, 3 + 4 * depth);
+    if (x > pc) return l;
+    float uc = rnd1(smp, 0 + 4 * depth);
+    float ud1, ud2;
+    rnd2(smp, 0 + 3 * depth, ud1, ud2);
+    BsdfSample bs = sampleBsdf(bsdf, wo, uc, ud1, ud2);
+    if (bs.pdf == 0 || isBlack(bs.f)) return l;
+    t = sScale(bs.f * t, 1.0f / pc);
+    spec = (bs.type & T_SPEC) != 0;
+    ray = Ray{p, bs.wi, eps, INF};
+    C.closest++;
+    hit = sceneIntersect(S, ray, it);
+  }
+}
+
+// ---------------------------------------------------------------- film
+// evalFilter (Filter.hs:68-96)
+static float evalFilter(int kind, const float* fp, float x, float y) {
+  switch (kind) {
+    case BLING_FILTER_GAUSS: {
+      float w = fp[0], h = fp[1], a = fp[2];
+      float ex = expf(-a * w * w), ey = expf(-a * h * h);
+      float gx = hmax(0.0f, expf(-a * x * x) - ex), gy = hmax(0.0f, expf(-a * y * y) - ey);
+      return gx * gy;
+    }
+    case BLING_FILTER_MITCHELL: {
+      float w = fp[0], h = fp[1], b = fp[2], c = fp[3];
+      float iw = 1.0f / w, ih = 1.0f / h;
+      auto m1d = [&](float xp) {
+        float xx = fabsf(2.0f * xp);
+        if (xx > 1)
+          return (((-b) - 6.0f * c) * xx * xx * xx + (6.0f * b + 30.0f * c) * xx * xx +
+                  ((-12.0f) * b - 48.0f * c) * xx + (8.0f * b + 24.0f * c)) *
+                 (1.0f / 6.0f);
+        return ((12.0f - 9.0f * b - 6.0f * c) * xx * xx * xx +
+                ((-18.0f) + 12.0f * b + 6.0f * c) * xx * xx + (6.0f - 2.0f * b)) *
+               (1.0f / 6.0f);
+      };
+      return m1d(x * iw) * m1d(y * ih);
+    }
+    case BLING_FILTER_SINC: {
+      float ix = 1.0f / fp[0], iy = 1.0f / fp[1], tau = fp[2];
+      auto s1 = [&](float xx) {
+        if (fabsf(xx) > 1) return 0.0f;
+        if (fabsf(xx) < 1e-5f) return 1.0f;
+        float xp = fabsf(xx) * PI;
+        float lanczos = sinf(xp * tau) / (xp * tau);
+        float sinc = sinf(xp) / xp;
+        return sinc * lanczos;
+      };
+      return s1(x * ix) * s1(y * iy);
+    }
+    case BLING_FILTER_TRIANGLE: {
+      float w = fp[0], h = fp[1];
+      float v = hmax(0.0f, w - fabsf(x * 2.0f)) * hmax(0.0f, h - fabsf(y * 2.0f));
+      return v / (w * h);
+    }
+    default: return (fabsf(x) < 0.5f && fabsf(y) < 0.5f) ? 1.0f : 0.0f;
+  }
+}
+static void filterSize(int kind, const float* fp, float& fw, float& fh) {
+  if (kind == BLING_FILTER_BOX) {
+    fw = fh = 0.5f;
+  } else {
+    fw = fp[0];
+    fh = fp[1];
+  }
+}
+// mkTableFilter (Image.hs:48-61)
+static void filterTable(int kind, const float* fp, float* out) {
+  float fw, fh;
+  filterSize(kind, fp, fw, fh);
+  for (int y = 0; y < 16; y++) {
+    float fy = ((float)y + 0.5f) * fh / 16.0f;
+    for (int x = 0; x < 16; x++) {
+      float fx = ((float)x + 0.5f) * fw / 16.0f;
+      out[y * 16 + x] = evalFilter(kind, fp, fx, fy);
+    }
+  }
+}
+
+struct FilmImg {  // MImage (Image.hs:64-71), pixel part
+  int w, h, ox, oy;
+  float* p;
+};
+// addSample (Image.hs:250-299); returns false when dropped as NaN/Inf
+static bool addSample(FilmImg& img, const float* tblv, float fw, float fh, float sx, float sy,
+                      const Spec& ss) {
+  if (sNaN(ss) || sInf(ss)) return false;
+  float smx, smy, smz;
+  spectrumToXYZ(ss, smx, smy, smz);
+  float ifw = 1.0f / fw, ifh = 1.0f / fw;  // sic (Image.hs:263)
+  float dx = sx - 0.5f, dy = sy - 0.5f;
+  int x0 = std::max(img.ox, (int)ceilf(dx - fw));
+  int x1 = std::min(img.ox + img.w - 1, (int)floorf(dx + fw));
+  int y0 = std::max(img.oy, (int)ceilf(dy - fh));
+  int y1 = std::min(img.oy + img.h - 1, (int)floorf(dy + fh));
+  if (x1 - x0 < 0 || y1 - y0 < 0) return true;
+  for (int y = y0; y <= y1; y++) {
+    float fy = fabsf(((float)y - dy) * ifh * 16.0f);
+    int iy = std::min((int)floorf(fy), 15);
+    for (int x = x0; x <= x1; x++) {
+      float fx = fabsf(((float)x - dx) * ifw * 16.0f);
+      int ix = std::min((int)floorf(fx), 15);
+      float w = tblv[iy * 16 + ix];
+      float* px = img.p + 4 * ((size_t)(x - img.ox) + (size_t)(y - img.oy) * img.w);
+      px[0] = px[0] + w;
+      px[1] = px[1] + smx * w;
+      px[2] = px[2] + smy * w;
+      px[3] = px[3] + smz * w;
+    }
+  }
+  return true;
+}
+
+static int nthreadsOf(int n) {
+  if (n > 0) return n;
+  unsigned h = std::thread::hardware_concurrency();
+  return h ? (int)h : 1;
+}
+template <class F>
+static void parallelFor(size_t n, int nth, F f) {
+  nth = nthreadsOf(nth);
+  if (nth <= 1 || n < 64) {
+    for (size_t i = 0; i < n; i++) f(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> ts;
+  for (int k = 0; k < nth; k++)
+    ts.emplace_back([&]() {
+      for (;;) {
+        size_t b = next.fetch_add(256);
+        if (b >= n) break;
+        size_t e = std::min(n, b + 256);
+        for (size_t i = b; i < e; i++) f(i);
+      }
+    });
+  for (auto& t : ts) t.join();
+}
+
+static Ray rayOf(const float* rays, size_t n, size_t i) {
+  return Ray{V{rays[i], rays[n + i], rays[2 * n + i]}, V{rays[3 * n + i], rays[4 * n + i], rays[5 * n + i]},
+             rays[6 * n + i], rays[7 * n + i]};
+}
+
+// ---------------------------------------------------------------- transforms
+// the matrix algebra of Transform.hs:44-110
+static void mmul(const float* m1, const float* m2, float* out) {  // mul m1 m2 (Transform.hs:102-105)
+  for (int n = 0; n < 16; n++) {
+    int i = n / 4, j = n % 4;
+    float s = 0.0f;
+    for (int k = 0; k < 4; k++) s = s + m1[k * 4 + j] * m2[i * 4 + k];
+    out[n] = s;
+  }
+}
+static void minvert(const float* m, float* out) {  // invert (Transform.hs:44-87)
+  float a[16];
+  memcpy(a, m, sizeof a);
+  auto idx = [](int r, int c) { return c * 4 + r; };
+  std::vector<int> ipiv = {0, 1, 2, 3};
+  int indx_r[4], indx_c[4];
+  for (int step = 0; step < 4; step++) {
+    int irow = -1, icol = -1;
+    float best = 0;
+    bool first = true;
+    for (int j : ipiv)
+      for (int k : ipiv) {
+        // maximumBy (compare `on` abs): a later element wins unless strictly smaller
+        float v = fabsf(a[idx(j, k)]);
+        if (first || best < v || best == v) {
+          best = v;
+          irow = j;
+          icol = k;
+        }
+        first = false;
+      }
+    ipiv.erase(std::remove(ipiv.begin(), ipiv.end(), icol), ipiv.end());
+    if (irow != icol)
+      for (int k = 0; k < 4; k++) std::swap(a[idx(irow, k)], a[idx(icol, k)]);
+    float pivinv = 1.0f / a[idx(icol, icol)];
+    a[idx(icol, icol)] = 1.0f;
+    for (int j = 0; j < 4; j++) a[idx(icol, j)] = a[idx(icol, j)] * pivinv;
+    for (int j = 0; j < 4; j++) {
+      if (j == icol) continue;
+      float save = a[idx(j, icol)];
+      a[idx(j, icol)] = 0.0f;
+      for (int k = 0; k < 4; k++) {
+        float x = a[idx(icol, k)];
+        float old = a[idx(j, k)];
+        a[idx(j, k)] = old - x * save;
+      }
+    }
+    indx_r[step] = irow;
+    indx_c[step] = icol;
+  }
+  for (int s = 3; s >= 0; s--) {
+    int ir = indx_r[s], ic = indx_c[s];
+    if (ir != ic)
+      for (int k = 0; k < 4; k++) std::swap(a[idx(k, ir)], a[idx(k, ic)]);
+  }
+  memcpy(out, a, sizeof a);
+}
+static void setm(float* m, float a, float b, float c, float d, float e, float f, float g, float h,
+                 float i, float j, float k, float l, float mm, float n, float o, float p) {
+  float v[16] = {a, b, c, d, e, f, g, h, i, j, k, l, mm, n, o, p};
+  memcpy(m, v, sizeof v);
+}
+
+}  // namespace
+
+// ================================================================ C API
+extern "C" {
+
+int orc_scene_create(const bling_scene_desc* d, orc_scene** out) {
+  if (!d || !out) return BLING_ERR_INVALID_ARG;
+  orc_scene* S = new orc_scene();
+  for (int i = 0; i < d->n_materials; i++) {
+    const bling_material& bm = d->materials[i];
+    Material m;
+    m.kind = bm.kind;
+    m.sigma = bm.sigma;
+    m.rough = bm.roughness;
+    m.ior = bm.ior;
+    memcpy(m.kd.v, bm.kd, 64);
+    memcpy(m.ks.v, bm.ks, 64);
+    memcpy(m.kt.v, bm.kt, 64);
+    memcpy(m.eta.v, bm.eta, 64);
+    memcpy(m.k.v, bm.k, 64);
+    S->mats.push_back(m);
+  }
+  for (int i = 0; i < d->n_meshes; i++) {
+    const bling_mesh_desc& md = d->meshes[i];
+    Mesh m;
+    if (md.n_indices % 3 != 0) {
+      delete S;
+      return BLING_ERR_INVALID_ARG;
+    }
+    m.p.resize(md.n_vertices);
+    for (int64_t k = 0; k < md.n_vertices; k++)
+      m.p[k] = V{md.vertices[3 * k], md.vertices[3 * k + 1], md.vertices[3 * k + 2]};
+    m.idx.assign(md.indices, md.indices + md.n_indices);
+    for (int32_t v : m.idx)
+      if (v < 0 || v >= md.n_vertices) {
+        delete S;
+        return BLING_ERR_INVALID_ARG;
+      }
+    if (md.normals) {
+      m.n.resize(md.n_vertices);
+      for (int64_t k = 0; k < md.n_vertices; k++)
+        m.n[k] = V{md.normals[3 * k], md.normals[3 * k + 1], md.normals[3 * k + 2]};
+    }
+    if (md.uvs) m.uv.assign(md.uvs, md.uvs + 2 * md.n_vertices);
+    m.material = md.material;
+    S->meshes.push_back(std::move(m));
+  }
+  for (int i = 0; i < d->n_shapes; i++) {
+    const bling_shape_desc& sd = d->shapes[i];
+    Shape s;
+    s.kind = sd.kind;
+    memcpy(s.p, sd.params, sizeof s.p);
+    memcpy(s.o2w.m, sd.o2w, 64);
+    memcpy(s.o2w.i, sd.w2o, 64);
+    s.material = sd.material;
+    s.emissive = sd.emissive != 0;
+    memcpy(s.emission.v, sd.emission, 64);
+    s.light_id = -1;
+    S->shapes.push_back(s);
+  }
+  // user lights first (Scene.hs:162)
+  for (int i = 0; i < d->n_lights; i++) {
+    const bling_light_desc& ld = d->lights[i];
+    Light l;
+    l.kind = ld.kind;
+    memcpy(l.spec.v, ld.spectrum, 64);
+    l.vec = V{ld.vec[0], ld.vec[1], ld.vec[2]};
+    l.shape = -1;
+    l.id = -1;
+    l.w = l.h = 0;
+    if (ld.kind == BLING_LIGHT_INFINITE) {
+      l.w = ld.env_w;
+      l.h = ld.env_h;
+      l.env.resize((size_t)l.w * l.h);
+      for (size_t k = 0; k < l.env.size(); k++) memcpy(l.env[k].v, ld.env + 16 * k, 64);
+      memcpy(l.w2l.m, ld.w2l, 64);
+      memcpy(l.w2l.i, ld.l2w, 64);
+      // mkInfiniteAreaLight: dist = mkDist2D (texSize) (sY . eval) (Light.hs:76-82)
+      l.cfunc.resize(l.h);
+      l.ccdf.resize(l.h);
+      l.cint.resize(l.h);
+      for (int v = 0; v < l.h; v++) {
+        l.cfunc[v].resize(l.w);
+        for (int u = 0; u < l.w; u++)
+          l.cfunc[v][u] = sY(envLookup(l, (float)u / (float)l.w, (float)v / (float)l.h));
+        mkDist1D(l.cfunc[v], l.ccdf[v], l.cint[v]);
+      }
+      l.mfunc = l.cint;
+      mkDist1D(l.mfunc, l.mcdf, l.mint);
+    }
+    S->lights.push_back(std::move(l));
+  }
+  // primitive list
+  std::vector<int32_t> order;
+  if (d->prim_order) {
+    order.assign(d->prim_order, d->prim_order + d->n_meshes + d->n_shapes);
+  } else {
+    for (int i = 0; i < d->n_meshes; i++) order.push_back(i);
+    for (int i = 0; i < d->n_shapes; i++) order.push_back(~i);
+  }
+  for (int32_t v : order) {
+    if (v >= 0) {
+      const Mesh& m = S->meshes[v];
+      for (size_t t = 0; t < m.idx.size() / 3; t++) {
+        Prim p;
+        p.is_shape = 0;
+        p.index = v;
+        p.tri = (int)t;
+        p.p1 = m.p[m.idx[3 * t]];
+        p.p2 = m.p[m.idx[3 * t + 1]];
+        p.p3 = m.p[m.idx[3 * t + 2]];
+        S->prims.push_back(p);
+      }
+    } else {
+      Prim p{};
+      p.is_shape = 1;
+      p.index = ~v;
+      S->prims.push_back(p);
+      Shape& s = S->shapes[~v];
+      if (s.emissive) {  // geometric lights in primitive order (Scene.hs:165)
+        Light l;
+        l.kind = LIGHT_AREA;
+        l.shape = ~v;
+        l.id = (int)S->lights.size();
+        s.light_id = l.id;
+        l.w = l.h = 0;
+        S->lights.push_back(std::move(l));
+      }
+    }
+  }
+  S->cam = d->camera;
+  buildOracleBvh(*S);
+  *out = S;
+  return BLING_OK;
+}
+
+void orc_scene_destroy(orc_scene* s) { delete s; }
+int64_t orc_scene_prim_count(const orc_scene* s) { return (int64_t)s->prims.size(); }
+
+void orc_trace_closest_brute(const orc_scene* s, const float* rays, size_t n, float* t,
+                             int32_t* prim, float* b1b2, int nth) {
+  parallelFor(n, nth, [&](size_t i) {
+    Hit h;
+    Ray r = rayOf(rays, n, i);
+    if (closestBrute(*s, r, h)) {
+      t[i] = h.t;
+      prim[i] = h.prim;
+      if (b1b2) {
+        b1b2[2 * i] = h.b1;
+        b1b2[2 * i + 1] = h.b2;
+      }
+    } else {
+      t[i] = INF;
+      prim[i] = -1;
+      if (b1b2) b1b2[2 * i] = b1b2[2 * i + 1] = 0;
+    }
+  });
+}
+void orc_trace_any_brute(const orc_scene* s, const float* rays, size_t n, uint8_t* hit, int nth) {
+  parallelFor(n, nth, [&](size_t i) { hit[i] = anyBrute(*s, rayOf(rays, n, i)) ? 1 : 0; });
+}
+void orc_trace_closest_bvh(const orc_scene* s, const float* rays, size_t n, float* t,
+                           int32_t* prim, float* b1b2, int nth) {
+  parallelFor(n, nth, [&](size_t i) {
+    Hit h;
+    Ray r = rayOf(rays, n, i);
+    if (closestBvh(*s, r, h)) {
+      t[i] = h.t;
+      prim[i] = h.prim;
+      if (b1b2) {
+        b1b2[2 * i] = h.b1;
+        b1b2[2 * i + 1] = h.b2;
+      }
+    } else {
+      t[i] = INF;
+      prim[i] = -1;
+      if (b1b2) b1b2[2 * i] = b1b2[2 * i + 1] = 0;
+    }
+  });
+}
+void orc_trace_any_bvh(const orc_scene* s, const float* rays, size_t n, uint8_t* hit, int nth) {
+  parallelFor(n, nth, [&](size_t i) { hit[i] = anyBvh(*s, rayOf(rays, n, i)) ? 1 : 0; });
+}
+
+// sample extent (imageWindow', Image.hs:170-176)
+static void sampleExtent(const bling_render_params* p, int& x0, int& x1, int& y0, int& y1) {
+  float fw, fh;
+  filterSize(p->filter_kind, p->filter_params, fw, fh);
+  x0 = (int)floorf(0.5f - fw);
+  x1 = (int)floorf(0.5f + (float)p->width + fw);
+  y0 = (int)floorf(0.5f - fh);
+  y1 = (int)floorf(0.5f + (float)p->height + fh);
+}
+
+// camera ray of one sample (fireRay, Camera.hs:146-164)
+static Ray cameraRay(const orc_scene* S, float ix, float iy, float lu, float lv) {
+  const bling_camera_desc& c = S->cam;
+  V pCamera = transPoint(c.r2c, V{ix, iy, 0});
+  Ray ray{V{0, 0, 0}, normalize(pCamera), 0, INF};
+  if (c.lens_radius > 0) {
+    float u, v;
+    concentricSampleDisk(lu, lv, u, v);
+    V ro{u * c.lens_radius, v * c.lens_radius, 0};
+    V pFocus = rayAt(ray, c.focal_distance / ray.d.z);
+    ray = Ray{ro, normalize(pFocus - ro), 0, INF};
+  }
+  return transRay(c.c2w, ray);
+}
+
+static Sampler mkSampler(const bling_render_params* p, uint64_t pass, int px, int py, int n) {
+  Sampler s;
+  s.key = pixelKey(p->seed, pass, px, py);
+  s.n = (uint32_t)n;
+  s.nu = p->strata_x;
+  s.nv = p->strata_y;
+  s.n1d = 4 * p->sample_depth;  // Path.hs:34-36
+  s.n2d = 3 * p->sample_depth;
+  return s;
+}
+
+static Spec traceSample(const orc_scene* S, const bling_render_params* p, const Sampler& smp,
+                        int px, int py, float& sx, float& sy, Counters& C) {
+  float ox, oy;
+  strat2D(smp, smp.n, DIM_PIX_U, DIM_PIX_V, ox, oy);  // pixel samples are not shuffled
+  uint32_t N = (uint32_t)(p->strata_x * p->strata_y);
+  uint32_t lp = permute(smp.n, N, randU32(smp.key, 0xffffffffu, DIM_LENS_PERM));
+  float lu, lv;
+  strat2D(smp, lp, DIM_LENS_U, DIM_LENS_V, lu, lv);  // lens samples are shuffled
+  sx = (float)px + ox;
+  sy = (float)py + oy;
+  Ray r = cameraRay(S, sx, sy, lu, lv);
+  return pathLi(*S, smp, r, p->max_depth, p->rr_depth, C);
+}
+
+int orc_sample_li(const orc_scene* s, const bling_render_params* p, uint64_t pass, int px, int py,
+                  int n, float* out_xyz, float* out_raster, float* out_spectrum) {
+  Counters C;
+  Sampler smp = mkSampler(p, pass, px, py, n);
+  float sx, sy;
+  Spec L = traceSample(s, p, smp, px, py, sx, sy, C);
+  spectrumToXYZ(L, out_xyz[0], out_xyz[1], out_xyz[2]);
+  out_raster[0] = sx;
+  out_raster[1] = sy;
+  if (out_spectrum) memcpy(out_spectrum, L.v, 64);
+  return BLING_OK;
+}
+
+int orc_render_pass(const orc_scene* S, const bling_render_params* p, uint64_t pass, float* film,
+                    int row_begin, int row_end, int nth, uint64_t* path_samples,
+                    uint64_t* rays_closest, uint64_t* rays_any) {
+  if (p->strata_x <= 0 || p->strata_y <= 0 || p->width <= 0 || p->height <= 0)
+    return BLING_ERR_INVALID_ARG;
+  int x0, x1, y0, y1;
+  sampleExtent(p, x0, x1, y0, y1);
+  float fw, fh;
+  filterSize(p->filter_kind, p->filter_params, fw, fh);
+  float tblv[256];
+  filterTable(p->filter_kind, p->filter_params, tblv);
+  int nsp = p->strata_x * p->strata_y;
+  // tiles (splitWindow, Sampling.hs:55-58)
+  struct Tile {
+    int xs, xe, ys, ye;
+  };
+  std::vector<Tile> tiles;
+  for (int y = y0; y <= y1; y += 16)
+    for (int x = x0; x <= x1; x += 16) tiles.push_back(Tile{x, std::min(x + 15, x1), y, std::min(y + 15, y1)});
+  int rb = row_begin, re = row_end;
+  if (re <= rb) {
+    rb = y0;
+    re = y1 + 1;
+  }
+  std::vector<std::vector<float>> timgs(tiles.size());
+  std::vector<int> tw(tiles.size()), th(tiles.size()), tox(tiles.size()), toy(tiles.size());
+  std::atomic<uint64_t> nps{0}, ncl{0}, nany{0};
+  parallelFor(tiles.size(), nth, [&](size_t ti) {
+    const Tile& T = tiles[ti];
+    if (T.ye < rb || T.ys >= re) return;
+    // mkImageTile (Image.hs:108-120)
+    int px0 = std::max(0, T.xs), py0 = std::max(0, T.ys);
+    int w = T.xe - px0 + (int)floorf(0.5f + fw);
+    int h = T.ye - py0 + (int)floorf(0.5f + fh);
+    tw[ti] = w;
+    th[ti] = h;
+    tox[ti] = px0;
+    toy[ti] = py0;
+    if (w <= 0 || h <= 0) return;
+    timgs[ti].assign((size_t)w * h * 4, 0.0f);
+    FilmImg img{w, h, px0, py0, timgs[ti].data()};
+    Counters C;
+    uint64_t ps = 0;
+    for (int iy = T.ys; iy <= T.ye; iy++) {
+      if (iy < rb || iy >= re) continue;
+      for (int ix = T.xs; ix <= T.xe; ix++)
+        for (int n = 0; n < nsp; n++) {
+          Sampler smp = mkSampler(p, pass, ix, iy, n);
+          float sx, sy;
+          Spec L = traceSample(S, p, smp, ix, iy, sx, sy, C);
+          ps++;
+          addSample(img, tblv, fw, fh, sx, sy, L);  // NaN/Inf samples are skipped
+        }
+    }
+    nps += ps;
+    ncl += C.closest;
+    nany += C.any;
+  });
+  // addTile in tile order (Rendering.hs:130-134, Image.hs:178-199)
+  for (size_t ti = 0; ti < tiles.size(); ti++) {
+    if (timgs[ti].empty()) continue;
+    int w = tw[ti], h = th[ti], dx = tox[ti], dy = toy[ti];
+    for (int y = 0; y < h; y++)
+      for (int x = 0; x < w; x++) {
+        if (y + dy >= p->height || x + dx >= p->width) continue;
+        size_t od = 4 * ((size_t)p->width * (y + dy) + (x + dx));
+        size_t os = 4 * ((size_t)w * y + x);
+        for (int o = 0; o < 4; o++) film[od + o] = film[od + o] + timgs[ti][os + o];
+      }
+  }
+  if (path_samples) *path_samples = nps;
+  if (rays_closest) *rays_closest = ncl;
+  if (rays_any) *rays_any = nany;
+  return BLING_OK;
+}
+
+void orc_rgb_to_spectrum(int illum, float r, float g, float b, float out[16]) {
+  Spec s = rgbToSpectrum(illum != 0, r, g, b);
+  memcpy(out, s.v, 64);
+}
+void orc_spectrum_to_xyz(const float s[16], float xyz[3]) {
+  Spec sp;
+  memcpy(sp.v, s, 64);
+  spectrumToXYZ(sp, xyz[0], xyz[1], xyz[2]);
+}
+void orc_xyz_to_rgb(const float xyz[3], float rgb[3]) {
+  xyzToRgb(xyz[0], xyz[1], xyz[2], rgb[0], rgb[1], rgb[2]);
+}
+float orc_filter_eval(int kind, const float* params, float x, float y) {
+  return evalFilter(kind, params, x, y);
+}
+void orc_filter_table(int kind, const float* params, float out[256]) { filterTable(kind, params, out); }
+void orc_random_floats(uint64_t seed, uint64_t pass, int px, int py, uint32_t n, uint32_t dim,
+                       int count, float* out) {
+  uint64_t k = pixelKey(seed, pass, px, py);
+  for (int i = 0; i < count; i++) out[i] = randF(k, n, dim + (uint32_t)i);
+}
+uint32_t orc_permute(uint32_t i, uint32_t l, uint32_t p) { return permute(i, l, p); }
+
+void orc_xf_translate(float dx, float dy, float dz, float out[32]) {
+  setm(out, 1, 0, 0, dx, 0, 1, 0, dy, 0, 0, 1, dz, 0, 0, 0, 1);
+  setm(out + 16, 1, 0, 0, -dx, 0, 1, 0, -dy, 0, 0, 1, -dz, 0, 0, 0, 1);
+}
+void orc_xf_scale(float sx, float sy, float sz, float out[32]) {
+  setm(out, sx, 0, 0, 0, 0, sy, 0, 0, 0, 0, sz, 0, 0, 0, 0, 1);
+  setm(out + 16, 1.0f / sx, 0, 0, 0, 0, 1.0f / sy, 0, 0, 0, 0, 1.0f / sz, 0, 0, 0, 0, 1);
+}
+void orc_xf_rotate(int axis, float deg, float out[32]) {
+  float s = sinf(radians(deg)), c = cosf(radians(deg));
+  if (axis == 0)
+    setm(out, 1, 0, 0, 0, 0, c, -s, 0, 0, s, c, 0, 0, 0, 0, 1);
+  else if (axis == 1)
+    setm(out, c, 0, s, 0, 0, 1, 0, 0, -s, 0, c, 0, 0, 0, 0, 1);
+  else
+    setm(out, c, -s, 0, 0, s, c, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1);
+  for (int i = 0; i < 4; i++)  // transMatrix m
+    for (int j = 0; j < 4; j++) out[16 + i * 4 + j] = out[j * 4 + i];
+}
+void orc_xf_look_at(const float pos[3], const float look[3], const float up[3], float out[32]) {
+  V p{pos[0], pos[1], pos[2]}, l{look[0], look[1], look[2]}, u{up[0], up[1], up[2]};
+  V dir = normalize(l - p);
+  V left = normalize(cross(normalize(u), dir));
+  V uu = cross(dir, left);
+  setm(out, left.x, uu.x, dir.x, p.x, left.y, uu.y, dir.y, p.y, left.z, uu.z, dir.z, p.z, 0, 0, 0, 1);
+  minvert(out, out + 16);
+}
+void orc_xf_concat(const float a[32], const float b[32], float out[32]) {
+  float m[16], i[16];
+  mmul(a, b, m);            // mul m1 m2
+  mmul(b + 16, a + 16, i);  // mul i2 i1
+  memcpy(out, m, 64);
+  memcpy(out + 16, i, 64);
+}
+void orc_xf_perspective(float fov, float n, float f, float out[32]) {
+  float iTanAng = 1.0f / tanf(radians(fov) / 2.0f);
+  float sc[32];
+  orc_xf_scale(iTanAng, iTanAng, 1.0f, sc);
+  float pm[32];
+  setm(pm, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, f / (f - n), -f * n / (f - n), 0, 0, 1, 0);
+  minvert(pm, pm + 16);
+  orc_xf_concat(sc, pm, out);
+}
+void orc_camera_perspective(const float c2w[32], float lr, float fd, float fov, float sx, float sy,
+                            bling_camera_desc* out) {
+  float p[32];
+  orc_xf_perspective(fov, 1e-2f, 1000.0f, p);
+  float aspect = sx / sy;
+  float s0, s1, s2, s3;
+  if (aspect > 1) {
+    s0 = -aspect;
+    s1 = aspect;
+    s2 = -1;
+    s3 = 1;
+  } else {
+    s0 = -1;
+    s1 = 1;
+    s2 = -1.0f / aspect;
+    s3 = 1.0f / aspect;
+  }
+  float st1[32], st2[32], t[32], tmp[32], s2r[32];
+  orc_xf_scale(sx, sy, 1, st1);
+  orc_xf_scale(1.0f / (s1 - s0), 1.0f / (s2 - s3), 1, st2);
+  orc_xf_translate(-s0, -s3, 0, t);
+  orc_xf_concat(st2, st1, tmp);  // t <> (st2 <> st1): <> is infixr
+  orc_xf_concat(t, tmp, s2r);
+  float r2s[32], pinv[32], r2c[32];
+  memcpy(r2s, s2r + 16, 64);
+  memcpy(r2s + 16, s2r, 64);
+  memcpy(pinv, p + 16, 64);
+  memcpy(pinv + 16, p, 64);
+  orc_xf_concat(r2s, pinv, r2c);
+  memcpy(out->c2w, c2w, 64);
+  memcpy(out->c2w_inv, c2w + 16, 64);
+  memcpy(out->r2c, r2c, 64);
+  memcpy(out->r2c_inv, r2c + 16, 64);
+  out->lens_radius = lr;
+  out->focal_distance = fd;
+}
+
+}  // extern "C"

@@ -1,0 +1,129 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent))
+
+from bling_gb300 import abi  # noqa: E402
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        from oracle.build import build  # noqa: WPS433
+        path = build()
+        L = C.CDLL(str(path))
+        P = C.POINTER
+        L.orc_scene_create.argtypes = [P(abi.SceneDesc), P(C.c_void_p)]
+        L.orc_scene_destroy.argtypes = [C.c_void_p]
+        L.orc_scene_prim_count.argtypes = [C.c_void_p]
+        L.orc_scene_prim_count.restype = C.c_int64
+        for fn in ("orc_trace_closest_brute", "orc_trace_closest_bvh"):
+            getattr(L, fn).argtypes = [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_float),
+                                       P(C.c_int32), P(C.c_float), C.c_int]
+        for fn in ("orc_trace_any_brute", "orc_trace_any_bvh"):
+            getattr(L, fn).argtypes = [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_uint8), C.c_int]
+        L.orc_render_pass.argtypes = [C.c_void_p, P(abi.RenderParams), C.c_uint64, P(C.c_float),
+                                      C.c_int, C.c_int, C.c_int, P(C.c_uint64), P(C.c_uint64),
+                                      P(C.c_uint64)]
+        L.orc_sample_li.argtypes = [C.c_void_p, P(abi.RenderParams), C.c_uint64, C.c_int, C.c_int,
+                                    C.c_int, P(C.c_float), P(C.c_float), P(C.c_float)]
+        L.orc_rgb_to_spectrum.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, P(C.c_float)]
+        L.orc_spectrum_to_xyz.argtypes = [P(C.c_float), P(C.c_float)]
+        L.orc_xyz_to_rgb.argtypes = [P(C.c_float), P(C.c_float)]
+        L.orc_filter_eval.argtypes = [C.c_int, P(C.c_float), C.c_float, C.c_float]
+        L.orc_filter_eval.restype = C.c_float
+        L.orc_filter_table.argtypes = [C.c_int, P(C.c_float), P(C.c_float)]
+        L.orc_random_floats.argtypes = [C.c_uint64, C.c_uint64, C.c_int, C.c_int, C.c_uint32,
+                                        C.c_uint32, C.c_int, P(C.c_float)]
+        L.orc_permute.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
+        L.orc_permute.restype = C.c_uint32
+        L.orc_xf_translate.argtypes = [C.c_float, C.c_float, C.c_float, P(C.c_float)]
+        L.orc_xf_scale.argtypes = [C.c_float, C.c_float, C.c_float, P(C.c_float)]
+        L.orc_xf_rotate.argtypes = [C.c_int, C.c_float, P(C.c_float)]
+        L.orc_xf_look_at.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float), P(C.c_float)]
+        L.orc_xf_perspective.argtypes = [C.c_float, C.c_float, C.c_float, P(C.c_float)]
+        L.orc_xf_concat.argtypes = [P(C.c_float), P(C.c_float), P(C.c_float)]
+        L.orc_camera_perspective.argtypes = [P(C.c_float), C.c_float, C.c_float, C.c_float,
+                                             C.c_float, C.c_float, P(abi.CameraDesc)]
+        _lib = L
+    return _lib
+
+
+def fp(a):
+    return abi.fptr(a)
+
+
+class OracleScene:
+    def __init__(self, scene):
+        self._desc, self._keep = scene.desc()
+        self.h = C.c_void_p()
+        rc = lib().orc_scene_create(C.byref(self._desc), C.byref(self.h))
+        if rc != 0:
+            raise ValueError(f"orc_scene_create failed: {rc}")
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_scene_destroy(self.h)
+            self.h = None
+
+    @property
+    def prim_count(self) -> int:
+        return lib().orc_scene_prim_count(self.h)
+
+    def closest(self, rays, brute=False, nthreads=0):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[1]
+        t = np.empty(n, np.float32)
+        prim = np.empty(n, np.int32)
+        b = np.empty(2 * n, np.float32)
+        fn = lib().orc_trace_closest_brute if brute else lib().orc_trace_closest_bvh
+        fn(self.h, fp(rays), n, fp(t), prim.ctypes.data_as(C.POINTER(C.c_int32)), fp(b), nthreads)
+        return t, prim, b.reshape(n, 2)
+
+    def any(self, rays, brute=False, nthreads=0):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[1]
+        hit = np.empty(n, np.uint8)
+        fn = lib().orc_trace_any_brute if brute else lib().orc_trace_any_bvh
+        fn(self.h, fp(rays), n, hit.ctypes.data_as(C.POINTER(C.c_uint8)), nthreads)
+        return hit
+
+    def render_pass(self, params, pass_index=0, film=None, rows=None, nthreads=0):
+        if film is None:
+            film = np.zeros((params.height, params.width, 4), np.float32)
+        ps, rc_, ra = C.c_uint64(), C.c_uint64(), C.c_uint64()
+        rb, re = rows if rows is not None else (0, 0)
+        rc = lib().orc_render_pass(self.h, C.byref(params), pass_index, fp(film), rb, re, nthreads,
+                                   C.byref(ps), C.byref(rc_), C.byref(ra))
+        if rc != 0:
+            raise ValueError(f"orc_render_pass failed: {rc}")
+        return film, {"path_samples": ps.value, "rays_closest": rc_.value, "rays_any": ra.value}
+
+    def sample_li(self, params, pass_index, px, py, n):
+        xyz = np.zeros(3, np.float32)
+        ras = np.zeros(2, np.float32)
+        spec = np.zeros(16, np.float32)
+        lib().orc_sample_li(self.h, C.byref(params), pass_index, px, py, n, fp(xyz), fp(ras), fp(spec))
+        return xyz, ras, spec
+
+
+def resolve(film):
+    """film (w, X, Y, Z) -> linear sRGB (getPixel with no splats, Image.hs:302-315)."""
+    from bling_gb300.spectrum import xyz_to_rgb
+    w = film[..., 0]
+    inv = np.where(w != 0, np.float32(1) / np.where(w != 0, w, 1), 0).astype(np.float32)
+    r, g, b = xyz_to_rgb(film[..., 1] * inv, film[..., 2] * inv, film[..., 3] * inv)
+    return np.stack([r, g, b], -1)

@@ -1,0 +1,165 @@
+"""Parity of the GPU ray queries with the CPU oracle (closest hit, any hit).
+
+The oracle's answer is the reference's `nearest'` fold over all primitives in
+primitive-ID order with the reference's intersection arithmetic: the smallest
+t, ties to the larger primitive ID.  The GPU must reproduce it bit for bit:
+same primitive, same t, same barycentrics.
+"""
+import numpy as np
+import pytest
+
+from bling_gb300 import abi
+from bling_gb300 import scene as S
+from bling_gb300 import transform as xf
+from bling_gb300.api import BlingError
+from bling_gb300.spectrum import constant
+from oracle.oracle import OracleScene
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+
+
+def _check_closest(g, o, rays, brute=True):
+    t, p, b = g.closest(rays)
+    to, po, bo = o.closest(rays, brute=brute)
+    assert np.array_equal(p, po), f"{np.count_nonzero(p != po)} primitive mismatches"
+    h = p >= 0
+    assert np.array_equal(_bits(t[h]), _bits(to[h]))
+    assert np.array_equal(_bits(b[h]), _bits(bo[h]))
+    assert np.all(np.isinf(t[~h]))
+    return t, p
+
+
+def test_soup_closest_and_any_vs_brute_force(gpu_ctx):
+    soup = S.triangle_soup(30000, seed=5)
+    g, o = gpu_ctx.scene(soup), OracleScene(soup)
+    rays = S.soup_rays(4096, seed=6)
+    t, p = _check_closest(g, o, rays)
+    assert 0.3 < (p >= 0).mean() < 1.0
+    ra = S.soup_rays(4096, seed=7, any_hit=True)
+    assert np.array_equal(g.any(ra), o.any(ra, brute=True))
+
+
+def test_1m_soup_vs_oracle_bvh(gpu_ctx):
+    soup = S.triangle_soup(1 << 20, seed=1)
+    g, o = gpu_ctx.scene(soup), OracleScene(soup)
+    rays = S.soup_rays(1 << 17, seed=2)
+    _check_closest(g, o, rays, brute=False)
+    ra = S.soup_rays(1 << 17, seed=3, any_hit=True)
+    assert np.array_equal(g.any(ra), o.any(ra))
+    # a brute-force spot check at full scene size
+    sub = np.ascontiguousarray(rays[:, :512])
+    _check_closest(g, o, sub, brute=True)
+
+
+def test_full_size_closest_is_closest(gpu_ctx):
+    """16M rays over the 1M soup: any-hit with tmax just below the reported
+    closest t finds nothing, with tmax = t finds the hit."""
+    soup = S.triangle_soup(1 << 20, seed=1)
+    g = gpu_ctx.scene(soup)
+    rays = S.soup_rays(1 << 24, seed=2)
+    t, p, _ = g.closest(rays, with_bary=False)
+    h = p >= 0
+    assert h.mean() > 0.5
+    below = rays.copy()
+    below[7] = np.where(h, np.nextafter(t, np.float32(0)), np.inf)
+    assert not g.any(below)[h].any()
+    at = rays.copy()
+    at[7] = np.where(h, t, np.inf)
+    any_at = g.any(at)
+    assert any_at[h].all() and not any_at[~h].any()
+
+
+def _shape_scene(seed, n_tris=200, n_shapes=60):
+    rng = np.random.default_rng(seed)
+    s = S.Scene()
+    m = s.add_material(abi.MAT_MATTE, kd=constant(0.5))
+    c = rng.uniform(-1, 1, (n_tris, 3))
+    v = np.stack([c, c + rng.normal(0, 0.2, (n_tris, 3)), c + rng.normal(0, 0.2, (n_tris, 3))], 1)
+    s.add_mesh(v.reshape(-1, 3), np.arange(3 * n_tris), m)
+    order = [0]
+    kinds = [abi.SHAPE_SPHERE, abi.SHAPE_QUAD, abi.SHAPE_BOX, abi.SHAPE_DISK, abi.SHAPE_CYLINDER]
+    for k in range(n_shapes):
+        kind = kinds[k % 5]
+        if kind == abi.SHAPE_SPHERE:
+            prm = (rng.uniform(0.05, 0.3),)
+        elif kind == abi.SHAPE_QUAD:
+            prm = tuple(rng.uniform(0.05, 0.3, 2))
+        elif kind == abi.SHAPE_BOX:
+            lo = rng.uniform(-0.2, 0, 3)
+            prm = tuple(lo) + tuple(lo + rng.uniform(0.05, 0.3, 3))
+        elif kind == abi.SHAPE_DISK:
+            prm = (rng.uniform(-0.1, 0.1), rng.uniform(0.1, 0.3), rng.uniform(0, 0.05),
+                   rng.uniform(1, 2 * np.pi))
+        else:
+            prm = (rng.uniform(0.05, 0.2), -0.1, rng.uniform(0, 0.3), rng.uniform(1, 2 * np.pi))
+        o2w = xf.rotate_x(rng.uniform(-180, 180)) @ xf.rotate_y(rng.uniform(-180, 180)) @ \
+            xf.translate(*rng.uniform(-1, 1, 3))
+        idx = s.add_shape(kind, prm, o2w, m)
+        order.insert(int(rng.integers(0, len(order) + 1)), ~idx)
+    s.prim_order = order
+    return s
+
+
+@pytest.mark.parametrize("seed", [21, 22])
+def test_analytic_shapes_vs_brute_force(gpu_ctx, seed):
+    sc = _shape_scene(seed)
+    g, o = gpu_ctx.scene(sc), OracleScene(sc)
+    rays = S.soup_rays(8192, seed=seed + 100)
+    rays[0:3] *= 0.7  # some origins inside shapes
+    _check_closest(g, o, rays)
+    ra = S.soup_rays(8192, seed=seed + 200, any_hit=True)
+    assert np.array_equal(g.any(ra), o.any(ra, brute=True))
+
+
+def test_ties_go_to_the_larger_primitive_id(gpu_ctx):
+    rng = np.random.default_rng(3)
+    c = rng.uniform(-1, 1, (500, 3))
+    v = np.stack([c, c + [0.1, 0, 0], c + [0, 0.1, 0]], 1).reshape(-1, 3)
+    v = np.concatenate([v, v, v])  # every triangle three times
+    s = S.Scene()
+    m = s.add_material(abi.MAT_MATTE, kd=constant(0.5))
+    s.add_mesh(v, np.arange(len(v)), m)
+    g, o = gpu_ctx.scene(s), OracleScene(s)
+    rays = np.zeros((8, 4096), np.float32)
+    tgt = c[rng.integers(0, 500, 4096)] + [0.02, 0.02, 0]
+    rays[0:3] = (tgt + [0, 0, -3]).T
+    rays[3:6] = np.array([0, 0, 1], np.float32)[:, None]
+    rays[7] = np.inf
+    t, p = _check_closest(g, o, rays)
+    assert (p[p >= 0] >= 1000).all()  # the third copy wins
+
+
+def test_edge_cases(gpu_ctx):
+    soup = S.triangle_soup(5000, seed=8)
+    g, o = gpu_ctx.scene(soup), OracleScene(soup)
+    empty = np.zeros((8, 0), np.float32)
+    t, p, _ = g.closest(empty)
+    assert t.size == 0 and g.any(empty).size == 0
+    rng = np.random.default_rng(9)
+    rays = np.zeros((8, 3000), np.float32)
+    rays[0:3] = rng.uniform(-1.2, 1.2, (3, 3000))
+    d = np.zeros((3, 3000), np.float32)
+    axis = rng.integers(0, 3, 3000)
+    d[axis, np.arange(3000)] = rng.choice([-1.0, 1.0], 3000)  # axis-aligned: two zero components
+    rays[3:6] = d
+    rays[6] = rng.choice([0.0, 0.5], 3000)
+    rays[7] = rng.choice([np.inf, 0.3, 0.0], 3000)  # includes tmin > tmax
+    _check_closest(g, o, rays)
+    assert np.array_equal(g.any(rays), o.any(rays, brute=True))
+
+
+@pytest.mark.parametrize("bad", ["negative", "not_multiple_of_3", "out_of_range"])
+def test_mesh_validation(gpu_ctx, bad):
+    s = S.Scene()
+    m = s.add_material(abi.MAT_MATTE, kd=constant(0.5))
+    v = np.zeros((4, 3), np.float32)
+    idx = {"negative": [0, 1, -1], "not_multiple_of_3": [0, 1, 2, 3],
+           "out_of_range": [0, 1, 4]}[bad]
+    s.add_mesh(v, idx, m)
+    with pytest.raises(BlingError) as e:
+        gpu_ctx.scene(s)
+    assert e.value.code == abi.BLING_ERR_INVALID_ARG
