@@ -39,8 +39,14 @@ def _render_both(gpu_ctx, sc, params, passes=1):
     return film.read(), fo, g.stats(), stats_o
 
 
-def _compare(fg, fo, rel=1e-3, frac=0.97):
-    assert np.array_equal(fg[..., 0], fo[..., 0]), "film weights differ"
+def _compare(fg, fo, rel=1e-3, frac=0.97, exact_weights=False):
+    # weights depend only on sample positions and the filter table; with the
+    # box filter they are sums of 1.0 and equal exactly, otherwise the GPU's
+    # atomic summation order changes the last bits
+    if exact_weights:
+        assert np.array_equal(fg[..., 0], fo[..., 0]), "film weights differ"
+    else:
+        assert np.allclose(fg[..., 0], fo[..., 0], rtol=1e-5, atol=1e-6), "film weights differ"
     xyz_g, xyz_o = fg[..., 1:], fo[..., 1:]
     scale = np.abs(xyz_o).mean() + 1e-12
     err = np.abs(xyz_g - xyz_o) / (np.abs(xyz_o) + 1e-3 * scale)
@@ -54,7 +60,7 @@ def test_cornell_room_vs_oracle(gpu_ctx):
     sc = S.cornell_room(96, 96)
     p = S.cornell_params(96, 96, spp_side=4)
     fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p)
-    _compare(fg, fo)
+    _compare(fg, fo, exact_weights=True)
     assert st_g["path_samples"] == st_o[0]["path_samples"] == 98 * 98 * 16
     assert abs(st_g["rays_closest"] - st_o[0]["rays_closest"]) <= 0.01 * st_o[0]["rays_closest"]
     assert abs(st_g["rays_any"] - st_o[0]["rays_any"]) <= 0.01 * st_o[0]["rays_any"]
@@ -116,5 +122,5 @@ def test_passes_accumulate(gpu_ctx):
     sc = S.cornell_room(32, 32)
     p = S.cornell_params(32, 32, spp_side=2)
     fg, fo, st_g, _ = _render_both(gpu_ctx, sc, p, passes=3)
-    _compare(fg, fo)
+    _compare(fg, fo, exact_weights=True)
     assert st_g["path_samples"] == 3 * 34 * 34 * 4
