@@ -198,6 +198,45 @@ def workload_config(args, world):
             "parallelism": f"replicas x{world}"}
 
 
+def measure_e2e(ctx, g, rays, ra, flush, args, world, dev):
+    """The same rays end to end through the host-buffer C-ABI calls: H2D copy
+    of the rays from pinned memory, traversal, D2H copy of (t, prim) and of
+    the any-hit flags, all inside the timed region."""
+    import ctypes as C
+
+    import torch
+
+    from bling_gb300.api import lib
+    h_rays = torch.from_numpy(rays).pin_memory().numpy()
+    h_any = torch.from_numpy(ra).pin_memory().numpy()
+    h_t = torch.empty(N_RAYS, dtype=torch.float32).pin_memory().numpy()
+    h_p = torch.empty(N_RAYS, dtype=torch.int32).pin_memory().numpy()
+    h_h = torch.empty(N_ANY, dtype=torch.uint8).pin_memory().numpy()
+    L = lib()
+    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
+
+    def e2e_step():
+        ctx.check(L.bling_trace_closest(g.h, fp(h_rays), N_RAYS, fp(h_t),
+                                        h_p.ctypes.data_as(C.POINTER(C.c_int32)),
+                                        C.POINTER(C.c_float)()))
+        ctx.check(L.bling_trace_any(g.h, fp(h_any), N_ANY, h_h.ctypes.data_as(C.POINTER(C.c_uint8))))
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier(world)
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_total = max_over_ranks(sum(e2e_times), world, dev)
+    value = world * (N_RAYS + N_ANY) * args.steps / e2e_total / 1e6
+    return {"value": round(value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": N_RAYS * 32 + N_ANY * 32,
+            "d2h_bytes_per_step": N_RAYS * 8 + N_ANY * 1}
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -245,6 +284,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     step_ms, closest_ms, any_ms = [], [], []
     with ClockSampler(local) as clk:
+        time.sleep(0.3)  # let the sampler start before the timed steps
         for _ in range(args.steps):
             flush.fill_(1)
             ev = step()
@@ -260,37 +300,9 @@ def run_ours(args):
     value = world * rays_per_step * args.steps / total_s / 1e6
     hit_frac = float((d_p >= 0).float().mean().item())
 
-    # ---- end to end: host buffers through the C ABI (pinned memory)
-    h_rays = torch.from_numpy(rays).pin_memory().numpy()
-    h_any = torch.from_numpy(ra).pin_memory().numpy()
-    h_t = torch.empty(N_RAYS, dtype=torch.float32).pin_memory().numpy()
-    h_p = torch.empty(N_RAYS, dtype=torch.int32).pin_memory().numpy()
-    h_h = torch.empty(N_ANY, dtype=torch.uint8).pin_memory().numpy()
-    import ctypes as C
-    from bling_gb300.api import lib
-    L = lib()
-    fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))  # noqa: E731
-
-    def e2e_step():
-        ctx.check(L.bling_trace_closest(g.h, fp(h_rays), N_RAYS, fp(h_t),
-                                        h_p.ctypes.data_as(C.POINTER(C.c_int32)),
-                                        C.POINTER(C.c_float)()))
-        ctx.check(L.bling_trace_any(g.h, fp(h_any), N_ANY, h_h.ctypes.data_as(C.POINTER(C.c_uint8))))
-
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    barrier(world)
-    e2e_times = []
-    for _ in range(args.steps):
-        flush.fill_(1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_step()
-        e2e_times.append(time.perf_counter() - t0)
-    e2e_total = max_over_ranks(sum(e2e_times), world, dev)
-    e2e_value = world * rays_per_step * args.steps / e2e_total / 1e6
-    h2d = N_RAYS * 32 + N_ANY * 32
-    d2h = N_RAYS * 8 + N_ANY * 1
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(ctx, g, rays, ra, flush, args, world, dev)
 
     # ---- roofline of the dominant kernel (closest hit)
     hbm_peak, peak_kind = peaks()
@@ -312,8 +324,7 @@ def run_ours(args):
             "ms_per_step": round(total_s * 1e3 / args.steps, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config(args, world),
-            "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
+            "e2e": e2e,
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
                          "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
                          "traffic": prof.get("dram_bytes_per_launch") if prof else None,
@@ -359,15 +370,20 @@ def profile_traffic():
 
 
 def main():
+    global N_RAYS, N_ANY
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-rays", type=int, default=CPU_SAMPLE_RAYS)
     ap.add_argument("--full-rays", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--rays", type=int, default=N_RAYS,
+                    help="closest-hit rays per step (any-hit: half); smaller for profiling")
     args = ap.parse_args()
+    N_RAYS, N_ANY = args.rays, args.rays // 2
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
