@@ -615,6 +615,36 @@ int bling_render_pass(bling_scene* s, bling_film* f, const bling_render_params* 
   return BLING_OK;
 }
 
+// The no-allocation pass: the caller owns the film's device memory and the
+// library's path state sits in a static device array (integrator.cu), so
+// nothing here calls cudaMalloc/cudaFree.  See bling_gpu.h for the limits.
+int bling_render_pass_noalloc(bling_scene* s, const bling_render_params* p, uint64_t pass,
+                              float* d_film) {
+  if (!s || !p || !d_film) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = s->ctx;
+  if (p->width <= 0 || p->height <= 0)
+    return set_err(c, BLING_ERR_INVALID_ARG, "invalid image size %dx%d", p->width, p->height);
+  if (p->strata_x <= 0 || p->strata_y <= 0 || p->max_depth < 0 || p->sample_depth < 0 ||
+      p->strata_x * p->strata_y > 4096)
+    return set_err(c, BLING_ERR_INVALID_ARG, "invalid sampler/integrator parameters");
+  if (p->filter_kind < BLING_FILTER_BOX || p->filter_kind > BLING_FILTER_TRIANGLE)
+    return set_err(c, BLING_ERR_INVALID_ARG, "unknown filter kind %d", p->filter_kind);
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  PassResult res{};
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = integrator_render_pass_noalloc(c->stream, s->accel, s->shading, *p, pass, d_film,
+                                          p->width, p->height, res, c->err);
+  if (rc) return rc;
+  auto t1 = std::chrono::steady_clock::now();
+  s->stats.last_pass_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  s->stats.rays_closest += res.rays_closest;
+  s->stats.rays_any += res.rays_any;
+  s->stats.path_samples += res.path_samples;
+  s->stats.nonfinite_drops += res.nonfinite;
+  return BLING_OK;
+}
+
 // ---------------------------------------------------------------- host helpers
 void bling_rgb_to_spectrum(int32_t illum, float r, float g, float b, float out[BLING_BANDS]) {
   const uint32_t* t = illum ? BLING_RGB_ILLUM_BITS : BLING_RGB_REFL_BITS;

@@ -21,6 +21,7 @@
 // shared with the CPU oracle (see the sampler section below).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -1656,6 +1657,137 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
   }
   unsigned long long cnt[8];
   RET_CUDA(cudaMemcpyAsync(cnt, ws.counters, sizeof cnt, cudaMemcpyDeviceToHost, stream));
+  RET_CUDA(cudaStreamSynchronize(stream));
+  res.rays_closest = cnt[2];
+  res.rays_any = cnt[3];
+  res.nonfinite = cnt[4];
+  res.path_samples = total;
+  return BLING_OK;
+}
+
+// ------------------------------------------------------------------ no-allocation pass
+// Path state for bling_render_pass_noalloc, in one file-scope device array:
+// the wavefront of one pass of at most kNoAllocSlots path samples.  Every GPU
+// that loads the library holds these 11.5 MiB (plus 64 bytes of counters)
+// until the process exits.  All calls share the array; the counters are
+// cleared at the start of every call, the path state is written before it is
+// read.  Two calls whose work overlaps on the GPU (different streams or
+// contexts on one device) race on it.
+constexpr size_t kNoAllocSlots = size_t(1) << 16;
+// per slot: T (16 f), L (16 f), ray (7 f), hit t (1 f), hit prim (1 i),
+// hit barycentrics (2 f), two queue entries (2 i)
+constexpr size_t kNoAllocWordsPerSlot = 16 + 16 + 7 + 1 + 1 + 2 + 2;
+constexpr size_t kNoAllocCounterBytes = 256;
+constexpr size_t kNoAllocBytes = kNoAllocCounterBytes + kNoAllocWordsPerSlot * 4 * kNoAllocSlots;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+constexpr int kMaxDevices = 64;
+unsigned char* g_noalloc_ptr[kMaxDevices] = {nullptr};
+}  // namespace
+
+size_t integrator_noalloc_max_samples() { return kNoAllocSlots; }
+
+int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const DevShading& S,
+                                   const bling_render_params& p, uint64_t pass, float* d_film,
+                                   int fw, int fh, PassResult& res, std::string& err) {
+  int device = 0;
+  RET_CUDA(cudaGetDevice(&device));
+  if (device < 0 || device >= kMaxDevices) {
+    err = "device ordinal out of range for the no-allocation pass";
+    return BLING_ERR_INVALID_ARG;
+  }
+  // set-up, once per device with that device current: the host-side name of
+  // a __device__ array is not a device address, so fetch the address
+  if (!g_noalloc_ptr[device]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) {
+      err = std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e);
+      return BLING_ERR_CUDA;
+    }
+    g_noalloc_ptr[device] = (unsigned char*)ptr;
+  }
+  RET_CUDA(ensureConstants(device));
+  PassParams P;
+  memset(&P, 0, sizeof P);
+  P.seed = p.seed;
+  P.pass = pass;
+  float fwid, fhei;
+  if (p.filter_kind == BLING_FILTER_BOX) {
+    fwid = fhei = 0.5f;
+  } else {
+    fwid = p.filter_params[0];
+    fhei = p.filter_params[1];
+  }
+  if (!(fwid > 0) || !(fhei > 0) || fwid > 16 || fhei > 16) {
+    err = "filter extent must be in (0, 16]";
+    return BLING_ERR_INVALID_ARG;
+  }
+  P.fw = fwid;
+  P.fh = fhei;
+  P.x0 = (int)floorf(0.5f - fwid);
+  P.x1 = (int)floorf(0.5f + (float)p.width + fwid);
+  P.y0 = (int)floorf(0.5f - fhei);
+  P.y1 = (int)floorf(0.5f + (float)p.height + fhei);
+  P.nx = P.x1 - P.x0 + 1;
+  P.ny = P.y1 - P.y0 + 1;
+  P.nu = p.strata_x;
+  P.nv = p.strata_y;
+  P.spp = p.strata_x * p.strata_y;
+  P.n1d = 4 * p.sample_depth;
+  P.n2d = 3 * p.sample_depth;
+  P.max_depth = p.max_depth;
+  P.rr_depth = p.rr_depth;
+  P.width = fw;
+  P.height = fh;
+  uint64_t total = (uint64_t)P.nx * P.ny * P.spp;
+  if (total > kNoAllocSlots) {
+    char buf[256];
+    snprintf(buf, sizeof buf,
+             "pass needs %llu path samples (%d x %d sample extent x %d strata); the "
+             "no-allocation pass holds at most %llu",
+             (unsigned long long)total, P.nx, P.ny, P.spp, (unsigned long long)kNoAllocSlots);
+    err = buf;
+    return BLING_ERR_BOUNDS;
+  }
+  float tbl[256];
+  for (int y = 0; y < 16; y++) {
+    float fy = ((float)y + 0.5f) * fhei / 16.0f;
+    for (int x = 0; x < 16; x++) {
+      float fx = ((float)x + 0.5f) * fwid / 16.0f;
+      tbl[y * 16 + x] = evalFilterHost(p.filter_kind, p.filter_params, fx, fy);
+    }
+  }
+  RET_CUDA(cudaMemcpyToSymbolAsync(c_filter, tbl, sizeof tbl, 0, cudaMemcpyHostToDevice, stream));
+  // carve the path state out of the array
+  const size_t cap = kNoAllocSlots;
+  unsigned char* base = g_noalloc_ptr[device];
+  unsigned long long* counters = (unsigned long long*)base;
+  float* words = (float*)(base + kNoAllocCounterBytes);
+  Slots st{words, words + 16 * cap, words + 32 * cap, words + 39 * cap,
+           (int32_t*)(words + 40 * cap), words + 41 * cap, cap};
+  int32_t* queue[2] = {(int32_t*)(words + 43 * cap), (int32_t*)(words + 44 * cap)};
+  RET_CUDA(cudaMemsetAsync(counters, 0, 8 * sizeof(unsigned long long), stream));
+  int sms = 0;
+  RET_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int block = 128;
+  int64_t count = (int64_t)total;
+  P.chunk_base = 0;
+  unsigned g = (unsigned)std::min<int64_t>((count + block - 1) / block, std::max(1, sms * 8));
+  k_raygen<<<g, block, 0, stream>>>(P, S.camera, st, count, queue[0], counters);
+  RET_CUDA(cudaGetLastError());
+  for (int depth = 0; depth <= p.max_depth; depth++) {
+    int in = depth & 1;
+    k_trace<<<g, block, 0, stream>>>(A, st, queue[in], counters + in, counters);
+    RET_CUDA(cudaGetLastError());
+    k_reset_count<<<1, 1, 0, stream>>>(counters + (1 - in));
+    k_shade<<<g, block, 0, stream>>>(A, S, P, st, depth, queue[in], counters + in, queue[1 - in],
+                                      counters + (1 - in), d_film, counters);
+    RET_CUDA(cudaGetLastError());
+  }
+  unsigned long long cnt[8];
+  RET_CUDA(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, stream));
   RET_CUDA(cudaStreamSynchronize(stream));
   res.rays_closest = cnt[2];
   res.rays_any = cnt[3];

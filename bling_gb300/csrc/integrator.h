@@ -83,4 +83,11 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
 
 void integrator_workspace_free(IntegratorWorkspace& ws);
 
+// One pass whose path state lives in a file-scope device array (no device
+// allocation); at most integrator_noalloc_max_samples() path samples.
+int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const DevShading& S,
+                                   const bling_render_params& p, uint64_t pass, float* d_film,
+                                   int fw, int fh, PassResult& res, std::string& err);
+size_t integrator_noalloc_max_samples();
+
 }  // namespace bgpu

@@ -253,6 +253,30 @@ int bling_render_pass(bling_scene* scene, bling_film* film, const bling_render_p
 
 int bling_scene_stats(bling_scene* scene, bling_stats* out);
 
+/* One render pass, like bling_render_pass, that allocates no device memory.
+ * No counterpart in the reference: it serves callers that cannot call
+ * cudaMalloc while rendering -- for instance a render server whose device
+ * memory is reserved up front for resident scenes and films (a fixed HBM
+ * budget), or a host that shares the GPU with another caching allocator --
+ * where an allocation in the middle of a frame could fail for lack of memory,
+ * and cudaMalloc/cudaFree would stall work on the device.
+ *
+ *  - The film is the caller's device buffer `d_film_wxyz`, width*height*4
+ *    floats (w, X, Y, Z), accumulated in place (zero it before the first pass).
+ *  - The path state lives in a static device array inside the library,
+ *    reserved in every process that loads it on every GPU it runs on (about
+ *    11.5 MiB), so one call renders at most 65536 path samples: sample-extent
+ *    pixels x strata_x x strata_y.  Larger passes return BLING_ERR_BOUNDS
+ *    with the sizes in the message; split the image or use bling_render_pass.
+ *  - The first call on a device looks up that array's device address (set-up,
+ *    once per device); make that first call before any stream capture.
+ *  - All calls share the array.  Calls whose work overlaps on the GPU -- on
+ *    different contexts or streams of one device -- race on it and must be
+ *    serialised by the caller; calls on one context already are.
+ *  - Counters, statistics and errors are as for bling_render_pass. */
+int bling_render_pass_noalloc(bling_scene* scene, const bling_render_params* params, uint64_t pass,
+                              float* d_film_wxyz);
+
 /* ---- host helpers for building scenes (no GPU needed) ---- */
 /* rgbToSpectrumRefl / rgbToSpectrumIllum (Spectrum.hs:140-159) */
 void bling_rgb_to_spectrum(int32_t illuminant, float r, float g, float b, float out[BLING_BANDS]);
