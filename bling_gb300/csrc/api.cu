@@ -28,6 +28,8 @@ struct bling_ctx {
   // grow-only staging buffers for host-buffer queries
   void* d_scratch = nullptr;
   size_t scratch_bytes = 0;
+  // next-ray counter of the persistent traversal kernels (calls are serialised)
+  unsigned long long* d_counter = nullptr;
   IntegratorWorkspace ws;
 };
 
@@ -186,6 +188,7 @@ int bling_ctx_create(bling_ctx** out, const bling_opts* opts) {
   }
   e = cudaSetDevice(c->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_counter, 256);
   c->stream = c->own_stream;
   if (e != cudaSuccess) {
     set_err(c.get(), BLING_ERR_CUDA, "stream creation failed: %s", cudaGetErrorString(e));
@@ -207,6 +210,7 @@ void bling_ctx_destroy(bling_ctx* c) {
       cudaStreamDestroy(c->own_stream);
     }
     if (c->d_scratch) cudaFree(c->d_scratch);
+    if (c->d_counter) cudaFree(c->d_counter);
     integrator_workspace_free(c->ws);
   }
   delete c;
@@ -416,7 +420,7 @@ int bling_trace_closest_device(bling_scene* s, const float* d_rays, size_t n, fl
   bling_ctx* c = s->ctx;
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
-  CK(c, launch_trace_closest(s->accel, d_rays, (int64_t)n, d_t, d_prim, d_b1b2, c->opts.block_size,
+  CK(c, launch_trace_closest(s->accel, d_rays, (int64_t)n, d_t, d_prim, d_b1b2, c->d_counter,
                              c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   s->stats.rays_closest += n;
@@ -428,7 +432,7 @@ int bling_trace_any_device(bling_scene* s, const float* d_rays, size_t n, uint8_
   bling_ctx* c = s->ctx;
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
-  CK(c, launch_trace_any(s->accel, d_rays, (int64_t)n, d_hit, c->opts.block_size, c->stream));
+  CK(c, launch_trace_any(s->accel, d_rays, (int64_t)n, d_hit, c->d_counter, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   s->stats.rays_any += n;
   return BLING_OK;
@@ -450,7 +454,7 @@ int bling_trace_closest(bling_scene* s, const float* rays, size_t n, float* t, i
   int32_t* d_p = (int32_t*)(base + rb + tb);
   float* d_b = b1b2 ? (float*)(base + rb + tb + pb) : nullptr;
   CK(c, cudaMemcpyAsync(d_r, rays, rb, cudaMemcpyHostToDevice, c->stream));
-  CK(c, launch_trace_closest(s->accel, d_r, (int64_t)n, d_t, d_p, d_b, c->opts.block_size, c->stream));
+  CK(c, launch_trace_closest(s->accel, d_r, (int64_t)n, d_t, d_p, d_b, c->d_counter, c->stream));
   CK(c, cudaMemcpyAsync(t, d_t, tb, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaMemcpyAsync(prim, d_p, pb, cudaMemcpyDeviceToHost, c->stream));
   if (b1b2) CK(c, cudaMemcpyAsync(b1b2, d_b, bb, cudaMemcpyDeviceToHost, c->stream));
@@ -471,7 +475,7 @@ int bling_trace_any(bling_scene* s, const float* rays, size_t n, uint8_t* hit) {
   float* d_r = (float*)c->d_scratch;
   uint8_t* d_h = (uint8_t*)c->d_scratch + rb;
   CK(c, cudaMemcpyAsync(d_r, rays, rb, cudaMemcpyHostToDevice, c->stream));
-  CK(c, launch_trace_any(s->accel, d_r, (int64_t)n, d_h, c->opts.block_size, c->stream));
+  CK(c, launch_trace_any(s->accel, d_r, (int64_t)n, d_h, c->d_counter, c->stream));
   CK(c, cudaMemcpyAsync(hit, d_h, n, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   s->stats.rays_any += n;

@@ -1083,24 +1083,31 @@ __device__ __forceinline__ Ray loadSlotRay(const Slots& st, int s) {
              INFINITY};
 }
 
-// closest hit of the queued bounce rays (scIntersect)
-__global__ void k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
-                        const unsigned long long* __restrict__ qcount,
-                        unsigned long long* __restrict__ counters) {
+// closest hit of the queued bounce rays (scIntersect), persistent warps that
+// take queue entries from counters[5] (zeroed before each launch)
+__global__ void __launch_bounds__(128) k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
+                                               const unsigned long long* __restrict__ qcount,
+                                               unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)*qcount;
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
-       q += (int64_t)gridDim.x * blockDim.x) {
-    int s = queue[q];
-    Ray r = loadSlotRay(st, s);
-    float t, b1, b2;
-    int prim;
-    bool hit = traverse<false>(A, r, t, prim, b1, b2);
-    st.hit_t[s] = t;
-    st.hit_prim[s] = hit ? prim : -1;
-    st.hit_b[2 * s] = b1;
-    st.hit_b[2 * s + 1] = b2;
-  }
+  traceWarpPersistent<false>(
+      A, n, counters + 5, [&](int64_t q) { return loadSlotRay(st, queue[q]); },
+      [&](int64_t q, const RayQueryResult& res) {
+        int s = queue[q];
+        st.hit_t[s] = res.t;
+        st.hit_prim[s] = res.hit ? res.prim : -1;
+        st.hit_b[2 * s] = res.b1;
+        st.hit_b[2 * s + 1] = res.b2;
+      });
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + 2, (unsigned long long)n);
+}
+
+static unsigned traceGrid(int sms) {
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace, 128, 0);
+    per_sm = std::max(1, per_sm);
+  }
+  return (unsigned)(std::max(1, sms) * per_sm);
 }
 
 __device__ __forceinline__ Spec loadBands(const float* base, size_t cap, int s) {
@@ -1646,7 +1653,9 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
     RET_CUDA(cudaGetLastError());
     for (int depth = 0; depth <= p.max_depth; depth++) {
       int in = depth & 1;
-      k_trace<<<g, block, 0, stream>>>(A, st, ws.queue[in], ws.counters + in, ws.counters);
+      RET_CUDA(cudaMemsetAsync(ws.counters + 5, 0, sizeof(unsigned long long), stream));
+      k_trace<<<std::min(g, traceGrid(sms)), block, 0, stream>>>(A, st, ws.queue[in],
+                                                                 ws.counters + in, ws.counters);
       RET_CUDA(cudaGetLastError());
       k_reset_count<<<1, 1, 0, stream>>>(ws.counters + (1 - in));
       k_shade<<<g, block, 0, stream>>>(A, S, P, st, depth, ws.queue[in], ws.counters + in,
@@ -1779,7 +1788,9 @@ int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const
   RET_CUDA(cudaGetLastError());
   for (int depth = 0; depth <= p.max_depth; depth++) {
     int in = depth & 1;
-    k_trace<<<g, block, 0, stream>>>(A, st, queue[in], counters + in, counters);
+    RET_CUDA(cudaMemsetAsync(counters + 5, 0, sizeof(unsigned long long), stream));
+    k_trace<<<std::min(g, traceGrid(sms)), block, 0, stream>>>(A, st, queue[in], counters + in,
+                                                               counters);
     RET_CUDA(cudaGetLastError());
     k_reset_count<<<1, 1, 0, stream>>>(counters + (1 - in));
     k_shade<<<g, block, 0, stream>>>(A, S, P, st, depth, queue[in], counters + in, queue[1 - in],

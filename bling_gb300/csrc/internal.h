@@ -27,14 +27,16 @@ struct DevAccel {
 };
 
 // Launchers (kernels_trace.cu); all enqueue on `stream` and return the
-// launch status.
+// launch status.  The persistent kernels take the next ray from *d_counter,
+// which the launcher zeroes first (one counter per stream at a time).
 cudaError_t launch_trace_closest(const DevAccel& A, const float* d_rays, int64_t n, float* d_t,
-                                 int32_t* d_prim, float* d_b1b2, int block, cudaStream_t stream);
+                                 int32_t* d_prim, float* d_b1b2, unsigned long long* d_counter,
+                                 cudaStream_t stream);
 // instrumented closest-hit traversal: adds node visits and leaf-slot tests
 // into d_totals[0..1]
 cudaError_t launch_trace_counts(const DevAccel& A, const float* d_rays, int64_t n,
                                 unsigned long long* d_totals, cudaStream_t stream);
 cudaError_t launch_trace_any(const DevAccel& A, const float* d_rays, int64_t n, uint8_t* d_hit,
-                             int block, cudaStream_t stream);
+                             unsigned long long* d_counter, cudaStream_t stream);
 
 }  // namespace bgpu

@@ -1,4 +1,8 @@
-// Ray-query kernels: one thread per ray over SoA ray buffers.
+// Ray-query kernels over SoA ray buffers: persistent warps (trace.cuh,
+// traceWarpPersistent) plus an instrumented one-thread-per-ray variant that
+// counts the traversal work.
+#include <mutex>
+
 #include "internal.h"
 #include "trace.cuh"
 
@@ -10,31 +14,30 @@ __device__ __forceinline__ Ray loadRay(const float* __restrict__ rays, int64_t n
              __ldg(rays + 6 * n + i), __ldg(rays + 7 * n + i)};
 }
 
-__global__ void k_trace_closest(DevAccel A, const float* __restrict__ rays, int64_t n,
-                                float* __restrict__ out_t, int32_t* __restrict__ out_prim,
-                                float* __restrict__ out_b) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  Ray r = loadRay(rays, n, i);
-  float t, b1, b2;
-  int prim;
-  bool hit = traverse<false>(A, r, t, prim, b1, b2);
-  out_t[i] = hit ? t : INFINITY;
-  out_prim[i] = hit ? prim : -1;
-  if (out_b) {
-    out_b[2 * i] = b1;
-    out_b[2 * i + 1] = b2;
-  }
+constexpr int kTraceBlock = 128;
+
+__global__ void __launch_bounds__(kTraceBlock)
+    k_trace_closest(DevAccel A, const float* __restrict__ rays, int64_t n,
+                    float* __restrict__ out_t, int32_t* __restrict__ out_prim,
+                    float* __restrict__ out_b, unsigned long long* __restrict__ next_ray) {
+  traceWarpPersistent<false>(
+      A, n, next_ray, [&](int64_t i) { return loadRay(rays, n, i); },
+      [&](int64_t i, const RayQueryResult& q) {
+        out_t[i] = q.hit ? q.t : INFINITY;
+        out_prim[i] = q.hit ? q.prim : -1;
+        if (out_b) {
+          out_b[2 * i] = q.b1;
+          out_b[2 * i + 1] = q.b2;
+        }
+      });
 }
 
-__global__ void k_trace_any(DevAccel A, const float* __restrict__ rays, int64_t n,
-                            uint8_t* __restrict__ out_hit) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  Ray r = loadRay(rays, n, i);
-  float t, b1, b2;
-  int prim;
-  out_hit[i] = traverse<true>(A, r, t, prim, b1, b2) ? 1 : 0;
+__global__ void __launch_bounds__(kTraceBlock)
+    k_trace_any(DevAccel A, const float* __restrict__ rays, int64_t n,
+                uint8_t* __restrict__ out_hit, unsigned long long* __restrict__ next_ray) {
+  traceWarpPersistent<true>(
+      A, n, next_ray, [&](int64_t i) { return loadRay(rays, n, i); },
+      [&](int64_t i, const RayQueryResult& q) { out_hit[i] = q.hit ? 1 : 0; });
 }
 
 __global__ void k_trace_counts(DevAccel A, const float* __restrict__ rays, int64_t n,
@@ -58,6 +61,18 @@ __global__ void k_trace_counts(DevAccel A, const float* __restrict__ rays, int64
   }
 }
 
+// resident blocks for a persistent launch: SMs x blocks per SM at full occupancy
+template <class K>
+static unsigned persistentGrid(K kernel, int64_t n) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTraceBlock, 0);
+  int64_t g = (int64_t)std::max(1, sms) * std::max(1, per_sm);
+  int64_t need = (n + kTraceBlock - 1) / kTraceBlock;
+  return (unsigned)std::max<int64_t>(1, std::min(g, need));
+}
+
 cudaError_t launch_trace_counts(const DevAccel& A, const float* d_rays, int64_t n,
                                 unsigned long long* d_totals, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
@@ -67,20 +82,23 @@ cudaError_t launch_trace_counts(const DevAccel& A, const float* d_rays, int64_t 
 }
 
 cudaError_t launch_trace_closest(const DevAccel& A, const float* d_rays, int64_t n, float* d_t,
-                                 int32_t* d_prim, float* d_b1b2, int block, cudaStream_t stream) {
+                                 int32_t* d_prim, float* d_b1b2, unsigned long long* d_counter,
+                                 cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  if (block <= 0) block = 128;
-  int64_t grid = (n + block - 1) / block;
-  k_trace_closest<<<(unsigned)grid, block, 0, stream>>>(A, d_rays, n, d_t, d_prim, d_b1b2);
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  unsigned grid = persistentGrid(k_trace_closest, n);
+  k_trace_closest<<<grid, kTraceBlock, 0, stream>>>(A, d_rays, n, d_t, d_prim, d_b1b2, d_counter);
   return cudaGetLastError();
 }
 
 cudaError_t launch_trace_any(const DevAccel& A, const float* d_rays, int64_t n, uint8_t* d_hit,
-                             int block, cudaStream_t stream) {
+                             unsigned long long* d_counter, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  if (block <= 0) block = 128;
-  int64_t grid = (n + block - 1) / block;
-  k_trace_any<<<(unsigned)grid, block, 0, stream>>>(A, d_rays, n, d_hit);
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  unsigned grid = persistentGrid(k_trace_any, n);
+  k_trace_any<<<grid, kTraceBlock, 0, stream>>>(A, d_rays, n, d_hit, d_counter);
   return cudaGetLastError();
 }
 

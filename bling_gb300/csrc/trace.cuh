@@ -142,4 +142,158 @@ __device__ __forceinline__ bool traverse(const DevAccel& A, const Ray& r, float&
   return best_prim >= 0;
 }
 
+// ---------------------------------------------------------------------------
+// Warp-synchronous persistent traversal.
+//
+// The same query as traverse<ANY>, restructured for SIMT efficiency:
+//  * every warp loops over rays it fetches itself: lanes whose ray finished
+//    take the next rays from a global counter (one atomicAdd per warp,
+//    __ballot_sync/__popc to rank the lanes), so lanes never idle while rays
+//    remain;
+//  * each round runs a node phase and a leaf phase for the whole warp (the
+//    "while-while" order): in the node phase a lane that meets a leaf
+//    postpones it and keeps walking inner nodes until every lane holds a leaf
+//    or has finished, then the warp tests leaves together.
+// All votes use the full warp mask: every lane runs every iteration of the
+// uniform loops and does work only when it has some.
+constexpr int kSentinel = INT32_MIN;
+
+struct RayQueryResult {
+  bool hit;
+  float t, b1, b2;
+  int prim;
+};
+
+template <bool ANY, class LoadRay, class Emit>
+__device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n,
+                                                    unsigned long long* __restrict__ next_ray,
+                                                    LoadRay load, Emit emit) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  int64_t rid = -1;
+  bool exhausted = false;
+  Ray r;
+  V3 inv;
+  float best_t = 0, bb1 = 0, bb2 = 0;
+  int best_prim = -1;
+  int stack[kTraversalStack];
+  int sp = 0;
+  int cur = kSentinel;
+  int leaf = kSentinel;  // postponed leaf
+  for (;;) {
+    // ---- refill lanes that have no ray
+    bool need = rid < 0 && !exhausted;
+    unsigned m = __ballot_sync(FULL, need);
+    if (m) {
+      int leader = __ffs(m) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(next_ray, (unsigned long long)__popc(m));
+      base = __shfl_sync(FULL, base, leader);
+      if (need) {
+        unsigned long long my = base + (unsigned long long)__popc(m & lt_mask);
+        if ((int64_t)my < n) {
+          rid = (int64_t)my;
+          r = load(rid);
+          inv = V3{1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z};
+          best_t = r.tmax;
+          best_prim = -1;
+          bb1 = bb2 = 0.0f;
+          sp = 0;
+          cur = A.root_ref;
+          leaf = kSentinel;
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (!__any_sync(FULL, rid >= 0)) return;
+    // ---- node phase
+    for (;;) {
+      bool work = rid >= 0 && cur >= 0;
+      if (!__any_sync(FULL, work)) break;
+      if (work) {
+        const float4* nd = A.nodes + 4 * (size_t)cur;
+        float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2);
+        float4 refs = __ldg(nd + 3);
+        float n0, f0, n1, f1;
+        boxInterval(a.x, a.y, a.z, a.w, c.x, c.y, r.o, inv, n0, f0);
+        boxInterval(b.x, b.y, b.z, b.w, c.z, c.w, r.o, inv, n1, f1);
+        bool h0 = fmaxf(n0, r.tmin) <= fminf(f0, best_t);
+        bool h1 = fmaxf(n1, r.tmin) <= fminf(f1, best_t);
+        int r0 = __float_as_int(refs.x), r1 = __float_as_int(refs.y);
+        if (h0 && h1) {
+          bool swap = n1 < n0;
+          cur = swap ? r1 : r0;
+          stack[sp++] = swap ? r0 : r1;
+        } else if (h0 || h1) {
+          cur = h0 ? r0 : r1;
+        } else {
+          cur = sp > 0 ? stack[--sp] : kSentinel;
+        }
+        // postpone the first leaf met; keep walking inner nodes
+        if (cur < 0 && cur != kSentinel && leaf == kSentinel) {
+          leaf = cur;
+          cur = sp > 0 ? stack[--sp] : kSentinel;
+        }
+      }
+      // leave the node phase once no lane both lacks a leaf and has nodes to visit
+      if (!__any_sync(FULL, rid >= 0 && leaf == kSentinel && cur >= 0)) break;
+    }
+    // ---- leaf phase
+    for (;;) {
+      bool work = rid >= 0 && (leaf != kSentinel || (cur < 0 && cur != kSentinel));
+      if (!__any_sync(FULL, work)) break;
+      if (work) {
+        if (leaf == kSentinel) {
+          leaf = cur;
+          cur = sp > 0 ? stack[--sp] : kSentinel;
+        }
+        int slot = ~leaf;
+        leaf = kSentinel;
+        for (;;) {
+          const float4* sl = A.slots + 3 * (size_t)slot;
+          float4 s0 = __ldg(sl), s1 = __ldg(sl + 1), s2 = __ldg(sl + 2);
+          int flags = __float_as_int(s2.z);
+          int prim = __float_as_int(s2.y);
+          bool hit;
+          float t = 0, b1 = 0, b2 = 0;
+          if (!(flags & SLOT_SHAPE)) {
+            hit = triTest(s0, s1, s2, r, best_t, t, b1, b2);
+          } else {
+            const DShape& sh = A.shapes[__float_as_int(s0.x)];
+            Ray ro = transRay(sh.w2o, Ray{r.o, r.d, r.tmin, ANY ? r.tmax : best_t});
+            if (ANY) {
+              hit = shapeIntersects(sh, ro);
+            } else {
+              float e;
+              hit = shapeIntersect<false>(sh, ro, t, e, nullptr);
+            }
+          }
+          if (hit) {
+            if (ANY) {
+              best_prim = prim;
+              cur = kSentinel;  // done: any hit suffices
+              break;
+            }
+            if (t < best_t || prim > best_prim) {
+              best_t = t;
+              best_prim = prim;
+              bb1 = b1;
+              bb2 = b2;
+            }
+          }
+          if (flags & SLOT_LAST) break;
+          slot++;
+        }
+      }
+    }
+    // ---- finished rays
+    if (rid >= 0 && cur == kSentinel && leaf == kSentinel) {
+      emit(rid, RayQueryResult{best_prim >= 0, best_t, bb1, bb2, best_prim});
+      rid = -1;
+    }
+  }
+}
+
 }  // namespace bgpu

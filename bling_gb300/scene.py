@@ -265,3 +265,155 @@ def soup_rays(n_rays=1 << 24, seed=2, any_hit=False):
         q2 = _unit_vectors(rng, n_rays) * rng.uniform(0, 1, size=(n_rays, 1)) ** (1 / 3)
         rays[7] = np.linalg.norm(q2 - o, axis=1)
     return rays
+
+
+# ---------------------------------------------------------------- heightfield + spheres
+def value_noise(x, z, seed=7, octaves=6, amplitude=0.2, base_cells=4):
+    """Seeded fractal value noise on [0,1]^2: `octaves` octaves of lattice
+    values with smoothstep interpolation, frequency doubling and amplitude
+    halving per octave, scaled so the sum spans +-`amplitude`."""
+    x = np.asarray(x, np.float64)
+    z = np.asarray(z, np.float64)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    total = np.zeros(np.broadcast(x, z).shape)
+    norm = 0.0
+    amp = 1.0
+    cells = base_cells
+    for _ in range(octaves):
+        lat = rng.uniform(-1, 1, size=(cells + 2, cells + 2))
+        fx, fz = np.clip(x, 0, 1) * cells, np.clip(z, 0, 1) * cells
+        ix, iz = np.floor(fx).astype(np.int64), np.floor(fz).astype(np.int64)
+        ix, iz = np.minimum(ix, cells), np.minimum(iz, cells)
+        tx, tz = fx - ix, fz - iz
+        sx, sz = tx * tx * (3 - 2 * tx), tz * tz * (3 - 2 * tz)
+        v00, v10 = lat[iz, ix], lat[iz, ix + 1]
+        v01, v11 = lat[iz + 1, ix], lat[iz + 1, ix + 1]
+        total += amp * ((v00 * (1 - sx) + v10 * sx) * (1 - sz) + (v01 * (1 - sx) + v11 * sx) * sz)
+        norm += amp
+        amp *= 0.5
+        cells *= 2
+    return amplitude * total / norm
+
+
+def heightmap_mesh(ns, nt, elev):
+    """The reference's heightMap (Primitive/Heightmap.hs:15-49) in object space:
+    vertices (x, elev(x, z), z) over [0,1]^2, two triangles per cell, shading
+    normals -(normalize (dx, ex + ez, dz)) from central differences, and uvs
+    (x/(ns-1), z/(ns-1))."""
+    fns, fnt = float(ns), float(nt)
+    xs = np.arange(ns, dtype=np.float64) / (fns - 1)
+    zs = np.arange(nt, dtype=np.float64) / (fnt - 1)
+    X, Z = np.meshgrid(xs, zs)  # [z, x]
+    Y = elev(X, Z)
+    verts = np.stack([X, Y, Z], -1).reshape(-1, 3).astype(np.float32)
+    ex, ez = 1 / fns, 1 / fnt
+    dx = elev(X - ex, Z) - elev(X + ex, Z)
+    dz = elev(X, Z - ez) - elev(X, Z + ez)
+    n = np.stack([dx, np.full_like(dx, ex + ez), dz], -1)
+    n = -(n / np.linalg.norm(n, axis=-1, keepdims=True))
+    uvs = np.stack([X / (fns - 1), Z / (fns - 1)], -1).reshape(-1, 2).astype(np.float32)
+    x = np.arange(ns - 1)
+    y = np.arange(nt - 1)
+    XX, YY = np.meshgrid(x, y)
+    v = lambda a, b: (a + b * ns).astype(np.int64)  # noqa: E731
+    tri = np.stack([v(XX, YY), v(XX + 1, YY), v(XX + 1, YY + 1),
+                    v(XX, YY), v(XX + 1, YY + 1), v(XX, YY + 1)], -1)
+    return verts, tri.reshape(-1).astype(np.int32), n.reshape(-1, 3).astype(np.float32), uvs
+
+
+def _apply_o2w(t: xf.Transform, pts, normals=None):
+    """transPoint / transNormal of a whole mesh (TriangleMesh.hs:58-59)."""
+    m = t.m.reshape(4, 4).astype(np.float64)
+    p = pts.astype(np.float64) @ m[:3, :3].T + m[:3, 3]
+    out_n = None
+    if normals is not None:
+        mi = t.inv.reshape(4, 4).astype(np.float64)
+        out_n = (normals.astype(np.float64) @ mi[:3, :3]).astype(np.float32)
+    return p.astype(np.float32), out_n
+
+
+def sky_env(width=1024, height=512, sun_dir=(0.4, 0.7, 0.3)):
+    """Procedural lat-long sky (light space: +z up): zenith blue to a bright
+    horizon, dark ground below, and a glow around the sun; 16-band
+    illuminant spectra, (height, width, 16) float32."""
+    from .spectrum import rgb_to_spectrum_array
+    v = (np.arange(height) + 0.5) / height
+    u = (np.arange(width) + 0.5) / width
+    theta = v * np.pi
+    phi = u * 2 * np.pi
+    T, P = np.meshgrid(theta, phi, indexing="ij")
+    d = np.stack([np.sin(T) * np.cos(P), np.sin(T) * np.sin(P), np.cos(T)], -1)
+    up = np.clip(d[..., 2], -1, 1)
+    zen = np.array([0.25, 0.45, 1.0])
+    hor = np.array([0.9, 0.9, 1.0])
+    gnd = np.array([0.18, 0.16, 0.14])
+    k = np.clip(up, 0, 1)[..., None] ** 0.5
+    rgb = np.where(up[..., None] >= 0, hor * (1 - k) + zen * k, gnd)
+    s = np.asarray(sun_dir, np.float64)
+    s = np.array([s[0], s[2], s[1]]) / np.linalg.norm(s)  # world (x, y up, z) -> light (x, z, y up)
+    c = np.clip((d * s).sum(-1), -1, 1)
+    rgb = rgb + (np.clip(c, 0, 1) ** 64)[..., None] * np.array([6.0, 5.0, 3.5])
+    return rgb_to_spectrum_array(rgb.astype(np.float32), illuminant=True)
+
+
+def heightfield_scene(ns=2048, n_spheres=4096, seed=3, width=1920, height=1080, fov=45.0,
+                      env_size=(1024, 512)) -> Scene:
+    """ns x ns-vertex heightfield (2 (ns-1)^2 triangles) of 6-octave value noise
+    (amplitude 0.2) over a 10 x 10 patch, n_spheres spheres of radius
+    ~U(0.02, 0.1) scattered above it, materials per object from the seed
+    (40% matte, 30% plastic with roughness ~U(0.05, 0.5), 20% metal with
+    roughness ~U(0.01, 0.3), 10% glass with IOR 1.5), a procedural sky and a
+    directional sun.  Metal is spectrally flat with eta = 1.2, k = 7.0
+    (an aluminium-like conductor; the workload does not fix eta/k)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene()
+    ground = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.35, 0.4, 0.28)))
+
+    def elev(x, z):
+        return value_noise(x, z, seed=seed)
+
+    verts, idx, normals, uvs = heightmap_mesh(ns, ns, elev)
+    o2w = xf.scale(10, 1, 10) @ xf.translate(-5, 0, -5)
+    wv, wn = _apply_o2w(o2w, verts, normals)
+    m_ground = s.add_mesh(wv, idx, ground, normals=wn, uvs=uvs)
+    order = [m_ground]
+    kinds = rng.choice(4, size=n_spheres, p=[0.4, 0.3, 0.2, 0.1])
+    px, pz = rng.uniform(-5, 5, n_spheres), rng.uniform(-5, 5, n_spheres)
+    r = rng.uniform(0.02, 0.1, n_spheres)
+    py = elev((px + 5) / 10, (pz + 5) / 10) + r + rng.uniform(0, 0.3, n_spheres)
+    cols = rng.uniform(0.1, 0.9, (n_spheres, 3))
+    for k in range(n_spheres):
+        kind = int(kinds[k])
+        if kind == 0:
+            mat = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum(tuple(cols[k])))
+        elif kind == 1:
+            mat = s.add_material(abi.MAT_PLASTIC, kd=rgb_to_spectrum(tuple(cols[k])),
+                                 ks=constant(0.5), roughness=float(rng.uniform(0.05, 0.5)))
+        elif kind == 2:
+            mat = s.add_material(abi.MAT_METAL, eta=constant(1.2), k=constant(7.0),
+                                 roughness=float(rng.uniform(0.01, 0.3)))
+        else:
+            mat = s.add_material(abi.MAT_GLASS, ks=constant(1.0), kt=constant(1.0), ior=1.5)
+        sh = s.add_shape(abi.SHAPE_SPHERE, (float(r[k]),),
+                         xf.translate(float(px[k]), float(py[k]), float(pz[k])), mat)
+        order.insert(0, ~sh)  # bling's parser prepends each prim block
+    s.prim_order = order
+    sun = (0.4, 0.7, 0.3)
+    sd = np.asarray(sun) / np.linalg.norm(sun)
+    env = sky_env(env_size[0], env_size[1], sun)
+    s.lights = [S_light(abi.LIGHT_DIRECTIONAL, rgb_to_spectrum((2.6, 2.4, 2.1), illuminant=True),
+                        tuple(float(v) for v in sd)),
+                Light(abi.LIGHT_INFINITE, env=env, w2l=xf.rotate_x(90))]
+    c2w = xf.look_at((0.0, 3.0, -8.0), (0.0, 0.0, 0.5), (0, 1, 0))
+    c2w, r2c = xf.perspective_camera(c2w, 0.0, 1.0, fov, width, height)
+    s.set_camera(c2w, r2c)
+    return s
+
+
+def S_light(kind, spectrum, vec):
+    return Light(kind, spectrum, vec=vec)
+
+
+def heightfield_params(width=1920, height=1080, spp_side=8, max_depth=8, rr_depth=3, seed=1):
+    return render_params(width, height, (spp_side, spp_side), max_depth=max_depth, sample_depth=3,
+                         rr_depth=rr_depth, filter_kind=abi.FILTER_BOX, seed=seed)

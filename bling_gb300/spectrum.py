@@ -52,6 +52,27 @@ def rgb_to_spectrum(rgb, illuminant: bool = False) -> np.ndarray:
     return (sc("white", b) + rest).astype(np.float32)
 
 
+def rgb_to_spectrum_array(rgb, illuminant: bool = False) -> np.ndarray:
+    """rgb_to_spectrum for an (..., 3) array; per element the same binary32
+    operations as the scalar version."""
+    rgb = np.asarray(rgb, dtype=np.float32)
+    r, g, b = (rgb[..., k][..., None] for k in range(3))
+    B = {n: _basis(illuminant, n) for n in BASES}
+
+    def sc(name, f):
+        return (B[name] * f).astype(np.float32)
+
+    c1 = (sc("white", r) + np.where(g <= b, sc("cyan", g - r) + sc("blue", b - g),
+                                    sc("cyan", b - r) + sc("green", g - b))).astype(np.float32)
+    c2 = (sc("white", g) + np.where(r <= b, sc("magenta", r - g) + sc("blue", b - r),
+                                    sc("magenta", b - g) + sc("red", r - b))).astype(np.float32)
+    c3 = (sc("white", b) + np.where(r <= b, sc("yellow", r - b) + sc("green", g - r),
+                                    sc("yellow", g - b) + sc("red", r - g))).astype(np.float32)
+    case1 = (r <= g) & (r <= b)
+    case2 = (g <= r) & (g <= b)
+    return np.where(case1, c1, np.where(case2, c2, c3)).astype(np.float32)
+
+
 def constant(v: float) -> np.ndarray:
     return np.full(16, F(v), dtype=np.float32)
 
