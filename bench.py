@@ -237,6 +237,58 @@ def measure_e2e(ctx, g, rays, ra, flush, args, world, dev):
             "d2h_bytes_per_step": N_RAYS * 8 + N_ANY * 1}
 
 
+def measure_render(ctx, stream, args):
+    """The path integrator on the two render workloads (secondary lines):
+    path samples/s and Mrays/s (camera, continuation, BSDF-MIS and shadow
+    queries, counted on the device) per pass, CUDA events on the stream."""
+    import torch
+
+    from bling_gb300 import scene as S
+    out = {}
+    cases = [("cornell_256x256_16spp_depth5", S.cornell_room(256, 256),
+              S.cornell_params(256, 256, spp_side=4, max_depth=5, rr_depth=3), 10)]
+    if not args.no_heightfield:
+        cases.append(("heightfield_8.4Mtri_4096spheres_1920x1080_64spp_depth8",
+                      S.heightfield_scene(), S.heightfield_params(1920, 1080, spp_side=8), 2))
+    for name, sc, p, passes in cases:
+        t0 = time.perf_counter()
+        g = ctx.scene(sc)
+        build_s = time.perf_counter() - t0
+        film = ctx.film(p.width, p.height)
+        g.render_pass(film, p, 0)  # warm-up pass
+        s0 = g.stats()
+        times = []
+        for k in range(passes):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record(stream)
+            g.render_pass(film, p, k + 1)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            times.append(ev[0].elapsed_time(ev[1]) / 1e3)
+        s1 = g.stats()
+        tot = sum(times)
+        rays = (s1["rays_closest"] - s0["rays_closest"]) + (s1["rays_any"] - s0["rays_any"])
+        out[name] = {
+            "path_samples_per_s": round((s1["path_samples"] - s0["path_samples"]) / tot, 1),
+            "mrays_per_s": round(rays / tot / 1e6, 2),
+            "ms_per_pass": round(tot / passes * 1e3, 3), "passes": passes,
+            "rays_per_path": round(rays / max(1, s1["path_samples"] - s0["path_samples"]), 3),
+            "scene_build_s": round(build_s, 3), "bvh_build_ms": round(s1["bvh_build_ms"], 1),
+            "nonfinite_drops": s1["nonfinite_drops"]}
+        if name.startswith("cornell") and not args.no_cpu_baseline:
+            from oracle.oracle import OracleScene
+            o = OracleScene(sc)
+            t0 = time.perf_counter()
+            _, st = o.render_pass(p, 0, rows=(0, 48))
+            dt = time.perf_counter() - t0
+            out[name]["cpu_baseline"] = {
+                "value": round(st["path_samples"] / dt, 1), "unit": "path samples/s",
+                "cores": os.cpu_count() or 1, "kind": "port",
+                "sample": "rows 0-47 of the 258 x 258 sample extent, 16 spp, one pass"}
+        del g, film
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -303,6 +355,9 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         e2e = measure_e2e(ctx, g, rays, ra, flush, args, world, dev)
+    render = None
+    if not args.no_render and rank == 0:
+        render = measure_render(ctx, stream, args)
 
     # ---- roofline of the dominant kernel (closest hit)
     hbm_peak, peak_kind = peaks()
@@ -342,6 +397,7 @@ def run_ours(args):
             "hit_fraction": round(hit_frac, 4),
             "bvh_build_ms": round(st["bvh_build_ms"], 1),
             "bvh_nodes": st["bvh_nodes"],
+            "path_integrator": render,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -380,6 +436,8 @@ def main():
     ap.add_argument("--full-rays", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-render", action="store_true", help="skip the path-integrator workloads")
+    ap.add_argument("--no-heightfield", action="store_true")
     ap.add_argument("--rays", type=int, default=N_RAYS,
                     help="closest-hit rays per step (any-hit: half); smaller for profiling")
     args = ap.parse_args()

@@ -268,47 +268,80 @@ def soup_rays(n_rays=1 << 24, seed=2, any_hit=False):
 
 
 # ---------------------------------------------------------------- heightfield + spheres
+def _noise_lattices(seed, octaves, base_cells):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out, cells = [], base_cells
+    for _ in range(octaves):
+        out.append((cells, rng.uniform(-1, 1, size=(cells + 2, cells + 2))))
+        cells *= 2
+    return out
+
+
+def _axis_weights(c, cells):
+    """bilinear-with-smoothstep weights of 1D coordinates on a lattice axis"""
+    f = np.clip(np.asarray(c, np.float64), 0, 1) * cells
+    i = np.minimum(np.floor(f).astype(np.int64), cells)
+    t = f - i
+    s = t * t * (3 - 2 * t)
+    return i, s
+
+
 def value_noise(x, z, seed=7, octaves=6, amplitude=0.2, base_cells=4):
     """Seeded fractal value noise on [0,1]^2: `octaves` octaves of lattice
     values with smoothstep interpolation, frequency doubling and amplitude
-    halving per octave, scaled so the sum spans +-`amplitude`."""
+    halving per octave, scaled so the sum spans +-`amplitude`.  x and z are
+    broadcast point coordinates."""
     x = np.asarray(x, np.float64)
     z = np.asarray(z, np.float64)
-    rng = np.random.Generator(np.random.PCG64(seed))
     total = np.zeros(np.broadcast(x, z).shape)
-    norm = 0.0
-    amp = 1.0
-    cells = base_cells
-    for _ in range(octaves):
-        lat = rng.uniform(-1, 1, size=(cells + 2, cells + 2))
-        fx, fz = np.clip(x, 0, 1) * cells, np.clip(z, 0, 1) * cells
-        ix, iz = np.floor(fx).astype(np.int64), np.floor(fz).astype(np.int64)
-        ix, iz = np.minimum(ix, cells), np.minimum(iz, cells)
-        tx, tz = fx - ix, fz - iz
-        sx, sz = tx * tx * (3 - 2 * tx), tz * tz * (3 - 2 * tz)
+    norm, amp = 0.0, 1.0
+    for cells, lat in _noise_lattices(seed, octaves, base_cells):
+        ix, sx = _axis_weights(x, cells)
+        iz, sz = _axis_weights(z, cells)
         v00, v10 = lat[iz, ix], lat[iz, ix + 1]
         v01, v11 = lat[iz + 1, ix], lat[iz + 1, ix + 1]
         total += amp * ((v00 * (1 - sx) + v10 * sx) * (1 - sz) + (v01 * (1 - sx) + v11 * sx) * sz)
         norm += amp
         amp *= 0.5
-        cells *= 2
     return amplitude * total / norm
 
 
-def heightmap_mesh(ns, nt, elev):
+def value_noise_grid(xs, zs, seed=7, octaves=6, amplitude=0.2, base_cells=4):
+    """value_noise on the grid zs x xs (result [z, x]); the bilinear lattice
+    interpolation factorises per axis, so each octave is two small matrix
+    products."""
+    total = np.zeros((len(zs), len(xs)))
+    norm, amp = 0.0, 1.0
+    for cells, lat in _noise_lattices(seed, octaves, base_cells):
+        mats = []
+        for c in (xs, zs):
+            i, s = _axis_weights(c, cells)
+            W = np.zeros((len(c), cells + 2))
+            np.add.at(W, (np.arange(len(c)), i), 1 - s)
+            np.add.at(W, (np.arange(len(c)), i + 1), s)
+            mats.append(W)
+        Wx, Wz = mats
+        total += amp * (Wz @ lat @ Wx.T)
+        norm += amp
+        amp *= 0.5
+    return amplitude * total / norm
+
+
+def heightmap_mesh(ns, nt, elev_grid):
     """The reference's heightMap (Primitive/Heightmap.hs:15-49) in object space:
     vertices (x, elev(x, z), z) over [0,1]^2, two triangles per cell, shading
     normals -(normalize (dx, ex + ez, dz)) from central differences, and uvs
-    (x/(ns-1), z/(ns-1))."""
+    (x/(ns-1), z/(ns-1)).  elev_grid(xs, zs) evaluates the elevation on the
+    grid zs x xs."""
     fns, fnt = float(ns), float(nt)
     xs = np.arange(ns, dtype=np.float64) / (fns - 1)
     zs = np.arange(nt, dtype=np.float64) / (fnt - 1)
     X, Z = np.meshgrid(xs, zs)  # [z, x]
-    Y = elev(X, Z)
+    Y = elev_grid(xs, zs)
     verts = np.stack([X, Y, Z], -1).reshape(-1, 3).astype(np.float32)
     ex, ez = 1 / fns, 1 / fnt
-    dx = elev(X - ex, Z) - elev(X + ex, Z)
-    dz = elev(X, Z - ez) - elev(X, Z + ez)
+    dx = elev_grid(xs - ex, zs) - elev_grid(xs + ex, zs)
+    dz = elev_grid(xs, zs - ez) - elev_grid(xs, zs + ez)
     n = np.stack([dx, np.full_like(dx, ex + ez), dz], -1)
     n = -(n / np.linalg.norm(n, axis=-1, keepdims=True))
     uvs = np.stack([X / (fns - 1), Z / (fns - 1)], -1).reshape(-1, 2).astype(np.float32)
@@ -372,7 +405,10 @@ def heightfield_scene(ns=2048, n_spheres=4096, seed=3, width=1920, height=1080, 
     def elev(x, z):
         return value_noise(x, z, seed=seed)
 
-    verts, idx, normals, uvs = heightmap_mesh(ns, ns, elev)
+    def elev_grid(xs, zs):
+        return value_noise_grid(xs, zs, seed=seed)
+
+    verts, idx, normals, uvs = heightmap_mesh(ns, ns, elev_grid)
     o2w = xf.scale(10, 1, 10) @ xf.translate(-5, 0, -5)
     wv, wn = _apply_o2w(o2w, verts, normals)
     m_ground = s.add_mesh(wv, idx, ground, normals=wn, uvs=uvs)
