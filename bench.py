@@ -289,6 +289,36 @@ def measure_render(ctx, stream, args):
     return out
 
 
+def run_render_profile(args):
+    """A small render of the large-mesh workload for profiling (full
+    geometry, reduced image): one warm-up pass and `--steps` timed passes."""
+    import torch
+
+    from bling_gb300 import build as gb
+    gb.build()
+    from bling_gb300 import scene as S
+    from bling_gb300.api import Context
+    w, h, side = args.render_size
+    ctx = Context(device=0)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    g = ctx.scene(S.heightfield_scene(width=w, height=h))
+    p = S.heightfield_params(w, h, spp_side=side)
+    film = ctx.film(w, h)
+    g.render_pass(film, p, 0)
+    s0 = g.stats()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        g.render_pass(film, p, k + 1)
+    dt = time.perf_counter() - t0
+    s1 = g.stats()
+    print(json.dumps({"workload": f"heightfield {w}x{h} {side * side}spp", "passes": args.steps,
+                      "ms_per_pass": dt / args.steps * 1e3,
+                      "path_samples_per_s": (s1["path_samples"] - s0["path_samples"]) / dt,
+                      "rays_closest": s1["rays_closest"] - s0["rays_closest"],
+                      "rays_any": s1["rays_any"] - s0["rays_any"]}), flush=True)
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_env()
@@ -438,13 +468,17 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the path-integrator workloads")
     ap.add_argument("--no-heightfield", action="store_true")
+    ap.add_argument("--render-size", type=int, nargs=3, metavar=("W", "H", "STRATA"),
+                    help="only render the large-mesh workload at W x H, STRATA^2 spp (profiling)")
     ap.add_argument("--rays", type=int, default=N_RAYS,
                     help="closest-hit rays per step (any-hit: half); smaller for profiling")
     args = ap.parse_args()
     N_RAYS, N_ANY = args.rays, args.rays // 2
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.render_size:
+        run_render_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

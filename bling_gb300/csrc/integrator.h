@@ -57,18 +57,12 @@ struct PassResult {
   uint64_t rays_closest, rays_any, path_samples, nonfinite;
 };
 
-// Device buffers reused across passes (grow-only), owned by a context.
+// Device buffer reused across passes (grow-only), owned by a context: the
+// path slots, queues and counters of one wavefront chunk, laid out by
+// integrator.cu.
 struct IntegratorWorkspace {
   size_t capacity = 0;  // path slots
-  float* T = nullptr;   // 16 * capacity
-  float* L = nullptr;   // 16 * capacity
-  float* ray = nullptr; // 7 * capacity: o.xyz, d.xyz, tmin
-  float* hit_t = nullptr;
-  int32_t* hit_prim = nullptr;
-  float* hit_b = nullptr;  // 2 * capacity
-  int32_t* queue[2] = {nullptr, nullptr};
-  unsigned long long* counters = nullptr;  // [0..1] queue sizes, [2] closest, [3] any, [4] nonfinite
-  float* filter = nullptr;                  // 256 table
+  void* buffer = nullptr;
 };
 
 int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,

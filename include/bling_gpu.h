@@ -265,7 +265,7 @@ int bling_scene_stats(bling_scene* scene, bling_stats* out);
  *    floats (w, X, Y, Z), accumulated in place (zero it before the first pass).
  *  - The path state lives in a static device array inside the library,
  *    reserved in every process that loads it on every GPU it runs on (about
- *    11.5 MiB), so one call renders at most 65536 path samples: sample-extent
+ *    35 MiB), so one call renders at most 65536 path samples: sample-extent
  *    pixels x strata_x x strata_y.  Larger passes return BLING_ERR_BOUNDS
  *    with the sizes in the message; split the image or use bling_render_pass.
  *  - The first call on a device looks up that array's device address (set-up,
