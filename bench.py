@@ -332,7 +332,7 @@ def run_ours(args):
     from bling_gb300 import scene as S
     from bling_gb300.api import Context
 
-    ctx = Context(device=local)
+    ctx = Context(device=local, wide_bvh=args.wide_bvh)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
     soup = S.triangle_soup(N_TRIS, seed=1)
@@ -392,7 +392,8 @@ def run_ours(args):
     # ---- roofline of the dominant kernel (closest hit)
     hbm_peak, peak_kind = peaks()
     counts = traversal_counts(g, rays)
-    bytes_per_ray = 32 + 8 + 64 * counts["nodes_per_ray"] + 48 * counts["slots_per_ray"]
+    node_bytes = 80 if args.wide_bvh else 64
+    bytes_per_ray = 32 + 8 + node_bytes * counts["nodes_per_ray"] + 48 * counts["slots_per_ray"]
     closest_s = float(np.mean(closest_ms)) / 1e3
     achieved = bytes_per_ray * N_RAYS / closest_s / 1e9
     prof = profile_traffic()
@@ -415,6 +416,7 @@ def run_ours(args):
                          "traffic": prof.get("dram_bytes_per_launch") if prof else None,
                          "peak_source": peak_kind,
                          "kernel": "k_trace_closest",
+                         "bvh_layout": "wide8" if args.wide_bvh else "binary",
                          "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
                          "nodes_per_ray": round(counts["nodes_per_ray"], 3),
                          "slots_per_ray": round(counts["slots_per_ray"], 3),
@@ -468,6 +470,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-render", action="store_true", help="skip the path-integrator workloads")
     ap.add_argument("--no-heightfield", action="store_true")
+    ap.add_argument("--wide-bvh", action="store_true", help="8-wide quantised BVH layout")
     ap.add_argument("--render-size", type=int, nargs=3, metavar=("W", "H", "STRATA"),
                     help="only render the large-mesh workload at W x H, STRATA^2 spp (profiling)")
     ap.add_argument("--rays", type=int, default=N_RAYS,

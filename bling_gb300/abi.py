@@ -20,6 +20,8 @@ BLING_ERR_TIMEOUT = -4
 BLING_ERR_BOUNDS = -5
 BLING_ERR_STATE = -6
 
+FLAG_WIDE_BVH = 1
+
 MAT_MATTE, MAT_PLASTIC, MAT_METAL, MAT_GLASS = 0, 1, 2, 3
 SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_DISK, SHAPE_CYLINDER = 0, 1, 2, 3, 4
 LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE = 0, 1, 2
@@ -78,6 +80,7 @@ class RenderParams(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("rays_closest", C.c_uint64), ("rays_any", C.c_uint64),
                 ("path_samples", C.c_uint64), ("nonfinite_drops", C.c_uint64),
+                ("degenerate_rays", C.c_uint64),
                 ("bvh_build_ms", C.c_double), ("last_pass_ms", C.c_double),
                 ("bvh_nodes", C.c_uint64), ("bvh_leaf_prims", C.c_uint64),
                 ("device_bytes", C.c_uint64)]

@@ -13,6 +13,7 @@ needs it raises :class:`BlingUnavailable`; nothing falls back to the CPU.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 from dataclasses import dataclass
 from pathlib import Path
 
@@ -83,11 +84,14 @@ def _fp(a):
 class Context:
     """A CUDA device plus one stream (``bling_ctx``)."""
 
-    def __init__(self, device: int = 0, block_size: int = 0, bvh_leaf_size: int = 0):
+    def __init__(self, device: int = 0, block_size: int = 0, bvh_leaf_size: int = 0,
+                 wide_bvh: bool = False):
         L = lib()
         o = abi.Opts()
-        o.device, o.flags, o.block_size, o.bvh_leaf_size = device, 0, block_size, bvh_leaf_size
+        o.device, o.block_size, o.bvh_leaf_size = device, block_size, bvh_leaf_size
+        o.flags = abi.FLAG_WIDE_BVH if wide_bvh else 0
         self.h = C.c_void_p()
+        self._children = weakref.WeakSet()  # scenes and films, closed before the context
         rc = L.bling_ctx_create(C.byref(self.h), C.byref(o))
         if rc != 0:
             msg = L.bling_last_error(self.h).decode() if self.h else "context creation failed"
@@ -106,6 +110,8 @@ class Context:
 
     def close(self):
         if getattr(self, "h", None):
+            for child in list(self._children):
+                child.close()
             lib().bling_ctx_destroy(self.h)
             self.h = None
 
@@ -130,6 +136,7 @@ class GpuScene:
         desc, keep = scene.desc()
         self.h = C.c_void_p()
         ctx.check(lib().bling_scene_create(ctx.h, C.byref(desc), C.byref(self.h)))
+        ctx._children.add(self)
 
     def close(self):
         if getattr(self, "h", None):
@@ -199,6 +206,7 @@ class Film:
         self.ctx, self.width, self.height = ctx, width, height
         self.h = C.c_void_p()
         ctx.check(lib().bling_film_create(ctx.h, width, height, C.byref(self.h)))
+        ctx._children.add(self)
 
     def close(self):
         if getattr(self, "h", None):

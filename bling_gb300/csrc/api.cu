@@ -37,6 +37,7 @@ struct bling_scene {
   bling_ctx* ctx = nullptr;
   DevAccel accel{};
   float4* d_nodes = nullptr;
+  uint4* d_nodes8 = nullptr;
   float4* d_slots = nullptr;
   DShape* d_shapes = nullptr;
   DevShading shading{};
@@ -311,15 +312,20 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   bi.lo = lo.data();
   bi.hi = hi.data();
   bi.max_leaf = c->opts.bvh_leaf_size > 0 ? c->opts.bvh_leaf_size : 4;
+  bi.wide = (c->opts.flags & BLING_FLAG_WIDE_BVH) != 0;
   BvhBuildOutput bo;
   if (build_bvh(bi, bo) != 0) return set_err(c, BLING_ERR_INVALID_ARG, "BVH build failed (depth bound)");
+  // the wide layout when it was built (it is skipped for very deep trees)
+  const bool wide = bi.wide && bo.wide_depth >= 0;
+  const std::vector<int32_t>& slot_prim = wide ? bo.slot_prim8 : bo.slot_prim;
+  const std::vector<uint8_t>& slot_last = wide ? bo.slot_last8 : bo.slot_last;
   // ---- leaf slots
-  size_t n_slots = bo.slot_prim.size();
+  size_t n_slots = slot_prim.size();
   std::vector<float> slots(12 * n_slots, 0.0f);
   for (size_t s = 0; s < n_slots; s++) {
-    int32_t prim = bo.slot_prim[s];
+    int32_t prim = slot_prim[s];
     float* o = &slots[12 * s];
-    int32_t flags = bo.slot_last[s] ? SLOT_LAST : 0;
+    int32_t flags = slot_last[s] ? SLOT_LAST : 0;
     int32_t v = prim_owner[prim];
     if (v >= 0) {
       const bling_mesh_desc& m = d->meshes[v];
@@ -348,8 +354,13 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   std::unique_ptr<bling_scene> S(new bling_scene());
   S->ctx = c;
   int rc;
-  if ((rc = upload(c, S->owned, (const float4*)bo.nodes.data(), bo.nodes.size() / 4, &S->d_nodes)))
-    return rc;
+  if (wide) {
+    if ((rc = upload(c, S->owned, (const uint4*)bo.nodes8.data(), bo.nodes8.size() / 4, &S->d_nodes8)))
+      return rc;
+  } else {
+    if ((rc = upload(c, S->owned, (const float4*)bo.nodes.data(), bo.nodes.size() / 4, &S->d_nodes)))
+      return rc;
+  }
   if ((rc = upload(c, S->owned, (const float4*)slots.data(), slots.size() / 4, &S->d_slots)))
     return rc;
   // ---- shapes on the device
@@ -373,12 +384,15 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   }
   if ((rc = upload(c, S->owned, shapes.data(), shapes.size(), &S->d_shapes))) return rc;
   S->accel.nodes = S->d_nodes;
+  S->accel.nodes8 = S->d_nodes8;
   S->accel.slots = S->d_slots;
   S->accel.shapes = S->d_shapes;
   S->accel.root_ref = bo.root_ref;
+  S->accel.root8 = bo.root8;
+  S->accel.wide = wide ? 1 : 0;
   S->accel.n_shapes = d->n_shapes;
   S->accel.n_prims = n_prims;
-  S->n_nodes = (int64_t)bo.nodes.size() / 16;
+  S->n_nodes = wide ? (int64_t)bo.nodes8.size() / 20 : (int64_t)bo.nodes.size() / 16;
   S->n_slots = (int64_t)n_slots;
   // ---- shading data for the path integrator
   if ((rc = integrator_upload_scene(c->stream, *d, order, prim_owner, prim_tri, shapes, shape_light,
@@ -389,7 +403,8 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   S->stats.bvh_build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   S->stats.bvh_nodes = (uint64_t)S->n_nodes;
   S->stats.bvh_leaf_prims = (uint64_t)n_slots;
-  size_t bytes = bo.nodes.size() * 4 + slots.size() * 4 + shapes.size() * sizeof(DShape);
+  size_t bytes = (wide ? bo.nodes8.size() : bo.nodes.size()) * 4 + slots.size() * 4 +
+                 shapes.size() * sizeof(DShape);
   S->stats.device_bytes = bytes + S->shading.bytes;
   *out = S.release();
   return BLING_OK;
@@ -491,7 +506,7 @@ int bling_trace_counts(bling_scene* s, const float* rays, size_t n, uint64_t* no
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
   size_t rb = 8 * n * sizeof(float);
-  int rc = ensure_scratch(c, rb + 16);
+  int rc = ensure_scratch(c, rb + 32);
   if (rc) return rc;
   float* d_r = (float*)c->d_scratch;
   unsigned long long* d_tot = (unsigned long long*)((char*)c->d_scratch + rb);
@@ -616,6 +631,7 @@ int bling_render_pass(bling_scene* s, bling_film* f, const bling_render_params* 
   s->stats.rays_any += res.rays_any;
   s->stats.path_samples += res.path_samples;
   s->stats.nonfinite_drops += res.nonfinite;
+  s->stats.degenerate_rays += res.degenerate;
   return BLING_OK;
 }
 
@@ -646,10 +662,29 @@ int bling_render_pass_noalloc(bling_scene* s, const bling_render_params* p, uint
   s->stats.rays_any += res.rays_any;
   s->stats.path_samples += res.path_samples;
   s->stats.nonfinite_drops += res.nonfinite;
+  s->stats.degenerate_rays += res.degenerate;
   return BLING_OK;
 }
 
 // ---------------------------------------------------------------- host helpers
+int bling_bvh_selftest(const float* lo, const float* hi, int64_t n, int32_t max_leaf,
+                       int64_t* stats) {
+  if (!lo || !hi || n <= 0 || !stats) return BLING_ERR_INVALID_ARG;
+  BvhBuildInput bi;
+  bi.n = n;
+  bi.lo = lo;
+  bi.hi = hi;
+  bi.max_leaf = max_leaf > 0 ? max_leaf : 4;
+  bi.wide = true;
+  BvhBuildOutput bo;
+  if (build_bvh(bi, bo) != 0) return BLING_ERR_INVALID_ARG;
+  stats[0] = (int64_t)bo.nodes.size() / 16;
+  stats[1] = bo.wide_depth >= 0 ? (int64_t)bo.nodes8.size() / 20 : 0;
+  stats[2] = bo.max_depth;
+  stats[3] = bo.wide_depth;
+  stats[4] = bo.leaves;
+  return validate_bvh(bi, bo);
+}
 void bling_rgb_to_spectrum(int32_t illum, float r, float g, float b, float out[BLING_BANDS]) {
   const uint32_t* t = illum ? BLING_RGB_ILLUM_BITS : BLING_RGB_REFL_BITS;
   auto B = [&](int which, int i) { return fbits(t[which * 16 + i]); };

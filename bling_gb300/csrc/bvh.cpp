@@ -191,6 +191,160 @@ struct Builder {
   }
 };
 
+// ---- 8-wide quantised layout
+struct WideItem {
+  int64_t bnode;
+  int64_t wide;
+  int depth;
+};
+
+static float box_area(const Box& b) { return b.area(); }
+
+// collapse: replace the internal child of largest area by its two children
+// until there are eight children or only leaves
+static int collapse(const Builder& B, int64_t b, int64_t kids[8]) {
+  int n = 2;
+  kids[0] = B.nodes[b].left;
+  kids[1] = B.nodes[b].right;
+  while (n < 8) {
+    int best = -1;
+    float best_a = -1;
+    for (int i = 0; i < n; i++) {
+      const BNode& k = B.nodes[kids[i]];
+      if (k.count > 0) continue;
+      float a = box_area(k.box);
+      if (a > best_a) {
+        best_a = a;
+        best = i;
+      }
+    }
+    if (best < 0) break;
+    int64_t x = kids[best];
+    kids[best] = B.nodes[x].left;
+    kids[n++] = B.nodes[x].right;
+  }
+  return n;
+}
+
+static bool build_wide(const Builder& B, BvhBuildOutput& out) {
+  out.nodes8.clear();
+  out.slot_prim8.clear();
+  out.slot_last8.clear();
+  out.wide_depth = 0;
+  auto add_leaf = [&](const BNode& nd) {
+    for (int64_t k = 0; k < nd.count; k++) {
+      out.slot_prim8.push_back(B.refs[nd.begin + k]);
+      out.slot_last8.push_back(k + 1 == nd.count ? 1 : 0);
+    }
+  };
+  const BNode& root = B.nodes[0];
+  if (root.count > 0) {
+    out.root8 = ~(int32_t)out.slot_prim8.size();
+    add_leaf(root);
+    return true;
+  }
+  out.root8 = 0;
+  out.nodes8.resize(20);
+  std::vector<WideItem> queue;
+  queue.push_back(WideItem{0, 0, 1});
+  for (size_t qi = 0; qi < queue.size(); qi++) {
+    WideItem it = queue[qi];
+    out.wide_depth = std::max(out.wide_depth, it.depth);
+    int64_t kids[8];
+    int n = collapse(B, it.bnode, kids);
+    const Box& nb = B.nodes[it.bnode].box;
+    // octant slot assignment: slot s gets the child that comes first along the
+    // diagonal of octant s (bit k of s set: direction component k negative)
+    double nc[3];
+    for (int a = 0; a < 3; a++) nc[a] = 0.5 * ((double)nb.lo[a] + nb.hi[a]);
+    int64_t slot_kid[8];
+    bool used[8] = {false};
+    for (int s = 0; s < 8; s++) slot_kid[s] = -1;
+    for (int s = 0; s < 8; s++) {
+      int best = -1;
+      double best_d = 0;
+      for (int i = 0; i < n; i++) {
+        if (used[i]) continue;
+        const Box& kb = B.nodes[kids[i]].box;
+        double d = 0;
+        for (int a = 0; a < 3; a++) {
+          double c = 0.5 * ((double)kb.lo[a] + kb.hi[a]) - nc[a];
+          d += (s >> a & 1) ? -c : c;
+        }
+        if (best < 0 || d < best_d) {
+          best = i;
+          best_d = d;
+        }
+      }
+      if (best < 0) break;
+      used[best] = true;
+      slot_kid[s] = kids[best];
+    }
+    // children: internal ones become consecutive wide nodes, leaves consecutive slots
+    uint32_t child_base = (uint32_t)(out.nodes8.size() / 20);
+    uint32_t slot_base = (uint32_t)out.slot_prim8.size();
+    uint8_t meta[8];
+    int rank = 0;
+    for (int s = 0; s < 8; s++) {
+      meta[s] = 0xFF;
+      if (slot_kid[s] < 0) continue;
+      const BNode& k = B.nodes[slot_kid[s]];
+      if (k.count == 0) {
+        meta[s] = (uint8_t)(0x80 | rank);
+        queue.push_back(WideItem{slot_kid[s], (int64_t)child_base + rank, it.depth + 1});
+        rank++;
+      } else {
+        size_t off = out.slot_prim8.size() - slot_base;
+        if (off > 127) return false;
+        meta[s] = (uint8_t)off;
+        add_leaf(k);
+      }
+    }
+    out.nodes8.resize(out.nodes8.size() + 20 * (size_t)rank);
+    // quantisation: origin p = node minimum, scale 2^e with 255 * 2^e covering the extent
+    uint32_t* w = &out.nodes8[20 * it.wide];
+    uint8_t q[6][8];
+    uint32_t ebits = 0;
+    for (int a = 0; a < 3; a++) {
+      double lo = nb.lo[a], hi = nb.hi[a];
+      double ext = hi - lo;
+      int e = -100;
+      if (ext > 0) {
+        e = (int)std::ceil(std::log2(ext * (1.0 + 1.0 / 1024.0) / 255.0));
+        while (std::ldexp(255.0, e) < ext * (1.0 + 1.0 / 1024.0)) e++;
+      }
+      e = std::max(-126, std::min(127, e));
+      ebits |= (uint32_t)(e + 127) << (8 * a);
+      double scale = std::ldexp(1.0, e);
+      for (int s = 0; s < 8; s++) {
+        if (slot_kid[s] < 0) {
+          q[a][s] = 255;
+          q[3 + a][s] = 0;
+          continue;
+        }
+        const Box& kb = B.nodes[slot_kid[s]].box;
+        double ql = std::floor(((double)kb.lo[a] - lo) / scale) - 1;
+        double qh = std::ceil(((double)kb.hi[a] - lo) / scale) + 1;
+        ql = std::max(0.0, std::min(255.0, ql));
+        qh = std::max(0.0, std::min(255.0, qh));
+        // the decoded box must contain the child box
+        if (lo + ql * scale > (double)kb.lo[a] || lo + qh * scale < (double)kb.hi[a]) return false;
+        q[a][s] = (uint8_t)ql;
+        q[3 + a][s] = (uint8_t)qh;
+      }
+    }
+    float p[3] = {nb.lo[0], nb.lo[1], nb.lo[2]};
+    memcpy(&w[0], p, 12);
+    w[3] = ebits;
+    w[4] = child_base;
+    w[5] = slot_base;
+    memcpy(&w[6], meta, 8);
+    // qlo.x qlo.y qlo.z qhi.x qhi.y qhi.z, 8 bytes each
+    for (int r = 0; r < 6; r++) memcpy(&w[8 + 2 * r], q[r], 8);
+  }
+  return out.wide_depth <= kWideStack / 7 - 1;
+}
+
 }  // namespace
 
 int build_bvh(const BvhBuildInput& in, BvhBuildOutput& out) {
@@ -199,6 +353,12 @@ int build_bvh(const BvhBuildInput& in, BvhBuildOutput& out) {
   B.build(0, 0, in.n, 0);
   out.max_depth = B.max_depth.load();
   if (out.max_depth >= kBvhMaxDepth) return -1;
+  if (!in.wide || !build_wide(B, out)) {
+    out.nodes8.clear();
+    out.slot_prim8.clear();
+    out.slot_last8.clear();
+    out.wide_depth = -1;  // the wide layout is not available for this tree
+  }
   out.nodes.clear();
   out.slot_prim.clear();
   out.slot_last.clear();
@@ -265,6 +425,173 @@ int build_bvh(const BvhBuildInput& in, BvhBuildOutput& out) {
     // siblings are allocated together, so both children of a node are adjacent
     if (pending[1] >= 0) stack.push_back(Item{nd.right, pending[1]});
     if (pending[0] >= 0) stack.push_back(Item{nd.left, pending[0]});
+  }
+  return 0;
+}
+
+namespace {
+
+struct DBox {
+  double lo[3], hi[3];
+  void reset() {
+    for (int k = 0; k < 3; k++) {
+      lo[k] = INFINITY;
+      hi[k] = -INFINITY;
+    }
+  }
+  void grow(const DBox& b) {
+    for (int k = 0; k < 3; k++) {
+      lo[k] = std::min(lo[k], b.lo[k]);
+      hi[k] = std::max(hi[k], b.hi[k]);
+    }
+  }
+  bool contains(const DBox& b) const {
+    for (int k = 0; k < 3; k++)
+      if (b.lo[k] < lo[k] || b.hi[k] > hi[k]) return false;
+    return true;
+  }
+};
+
+struct Validator {
+  const BvhBuildInput& in;
+  const std::vector<int32_t>& slot_prim;
+  const std::vector<uint8_t>& slot_last;
+  std::vector<int> prim_seen;
+  std::vector<int> slot_seen;
+  int err = 0;
+
+  Validator(const BvhBuildInput& i, const std::vector<int32_t>& sp, const std::vector<uint8_t>& sl)
+      : in(i), slot_prim(sp), slot_last(sl), prim_seen(i.n, 0), slot_seen(sp.size(), 0) {}
+
+  DBox leaf(int32_t ref) {
+    DBox b;
+    b.reset();
+    int64_t s = ~(int64_t)ref;
+    for (;;) {
+      if (s < 0 || s >= (int64_t)slot_prim.size()) {
+        err = -10;
+        return b;
+      }
+      if (slot_seen[s]++) err = -11;
+      int32_t p = slot_prim[s];
+      if (p < 0 || p >= in.n) {
+        err = -12;
+        return b;
+      }
+      prim_seen[p]++;
+      DBox pb;
+      for (int k = 0; k < 3; k++) {
+        pb.lo[k] = in.lo[3 * p + k];
+        pb.hi[k] = in.hi[3 * p + k];
+      }
+      b.grow(pb);
+      if (slot_last[s]) break;
+      s++;
+    }
+    return b;
+  }
+
+  int finish() {
+    if (err) return err;
+    for (int v : prim_seen)
+      if (v != 1) return -13;
+    for (int v : slot_seen)
+      if (v != 1) return -14;
+    return 0;
+  }
+};
+
+DBox validate_binary(Validator& V, const BvhBuildOutput& out, int32_t ref, int depth) {
+  if (ref < 0) return V.leaf(ref);
+  DBox un;
+  un.reset();
+  if (depth > kBvhMaxDepth || (int64_t)ref * 16 + 16 > (int64_t)out.nodes.size()) {
+    V.err = -20;
+    return un;
+  }
+  const float* o = &out.nodes[16 * (size_t)ref];
+  int32_t refs[2];
+  memcpy(&refs[0], &o[12], 4);
+  memcpy(&refs[1], &o[13], 4);
+  for (int c = 0; c < 2; c++) {
+    DBox cb = validate_binary(V, out, refs[c], depth + 1);
+    DBox stored;
+    const int xo = c ? 4 : 0, zo = c ? 10 : 8;
+    stored.lo[0] = o[xo];
+    stored.hi[0] = o[xo + 1];
+    stored.lo[1] = o[xo + 2];
+    stored.hi[1] = o[xo + 3];
+    stored.lo[2] = o[zo];
+    stored.hi[2] = o[zo + 1];
+    if (!stored.contains(cb)) V.err = -21;
+    un.grow(cb);
+  }
+  return un;
+}
+
+DBox validate_wide(Validator& V, const BvhBuildOutput& out, int32_t ref, int depth) {
+  if (ref < 0) return V.leaf(ref);
+  DBox un;
+  un.reset();
+  size_t n_nodes = out.nodes8.size() / 20;
+  if (depth > out.wide_depth || (size_t)ref >= n_nodes) {
+    V.err = -30;
+    return un;
+  }
+  const uint32_t* w = &out.nodes8[20 * (size_t)ref];
+  float p[3];
+  memcpy(p, w, 12);
+  uint8_t meta[8], q[6][8];
+  memcpy(meta, &w[6], 8);
+  for (int r = 0; r < 6; r++) memcpy(q[r], &w[8 + 2 * r], 8);
+  int internal = 0;
+  for (int s = 0; s < 8; s++)
+    if (meta[s] != 0xFF && (meta[s] & 0x80)) internal++;
+  for (int s = 0; s < 8; s++) {
+    if (meta[s] == 0xFF) continue;
+    int32_t cref;
+    if (meta[s] & 0x80) {
+      int rank = meta[s] & 0x7f;
+      if (rank >= internal) {
+        V.err = -31;
+        return un;
+      }
+      cref = (int32_t)(w[4] + rank);
+    } else {
+      cref = ~(int32_t)(w[5] + meta[s]);
+    }
+    DBox cb = validate_wide(V, out, cref, depth + 1);
+    DBox dec;
+    for (int a = 0; a < 3; a++) {
+      double scale = std::ldexp(1.0, (int)((w[3] >> (8 * a)) & 0xff) - 127);
+      dec.lo[a] = (double)p[a] + q[a][s] * scale;
+      dec.hi[a] = (double)p[a] + q[3 + a][s] * scale;
+    }
+    if (!dec.contains(cb)) V.err = -32;
+    un.grow(cb);
+  }
+  return un;
+}
+
+}  // namespace
+
+int validate_bvh(const BvhBuildInput& in, const BvhBuildOutput& out) {
+  {
+    Validator V(in, out.slot_prim, out.slot_last);
+    validate_binary(V, out, out.root_ref, 0);
+    int rc = V.finish();
+    if (rc) return rc;
+  }
+  if (out.wide_depth >= 0 && !out.nodes8.empty()) {
+    Validator V(in, out.slot_prim8, out.slot_last8);
+    validate_wide(V, out, out.root8, 1);
+    int rc = V.finish();
+    if (rc) return rc - 100;
+  } else if (out.wide_depth >= 0 && out.root8 < 0) {
+    Validator V(in, out.slot_prim8, out.slot_last8);
+    V.leaf(out.root8);
+    int rc = V.finish();
+    if (rc) return rc - 100;
   }
   return 0;
 }

@@ -19,6 +19,7 @@ struct BvhBuildInput {
   const float* hi = nullptr;    // 3n: box maximum
   int max_leaf = 4;             // primitives per leaf at most (when splittable)
   int threads = 0;              // 0: hardware concurrency
+  bool wide = true;             // also produce the 8-wide quantised layout
 };
 
 struct BvhBuildOutput {
@@ -34,10 +35,36 @@ struct BvhBuildOutput {
   int32_t root_ref = 0;             // like a child ref
   int max_depth = 0;
   int64_t leaves = 0;
+
+  // The same tree collapsed to 8-wide nodes with 8-bit quantised child boxes
+  // (filled when BvhBuildInput::wide).  20 words (80 bytes) per node:
+  //   w0: origin p.xyz (float), biased exponents ex|ey<<8|ez<<16 (scale 2^(e-127))
+  //   w1: first internal child node, first leaf slot, meta[0..3], meta[4..7]
+  //       meta: 0x80|rank internal child (node child_base + rank),
+  //             offset of a leaf child's first slot from the slot base, 0xFF empty
+  //   w2..w4: qlo.x[8] qlo.y[8] | qlo.z[8] qhi.x[8] | qhi.y[8] qhi.z[8]
+  // child box = p + q * scale, widened by one quantum where possible.
+  // Child slots are ordered so that visiting slot k ^ octant(ray) for
+  // k = 0..7 is roughly front to back.  The leaf slots follow a different
+  // order than the binary layout's, so they come in their own arrays.
+  std::vector<uint32_t> nodes8;
+  std::vector<int32_t> slot_prim8;
+  std::vector<uint8_t> slot_last8;
+  int32_t root8 = 0;      // node 0, or a leaf ref when the whole scene is one leaf
+  int wide_depth = 0;     // longest root-to-leaf path in wide nodes
 };
+
+constexpr int kWideStack = 128;  // per-lane stack entries of the wide traversal
 
 // Returns 0 on success, -1 if the input is empty/invalid.
 int build_bvh(const BvhBuildInput& in, BvhBuildOutput& out);
+
+// Structural check of a built tree against the primitive boxes: every
+// primitive is in exactly one leaf slot of each layout, slots end with a
+// SLOT_LAST flag, every inner box contains its children and every decoded
+// quantised child box contains the child (exact arithmetic).  Returns 0, or a
+// negative code naming the first violation.
+int validate_bvh(const BvhBuildInput& in, const BvhBuildOutput& out);
 
 // Depth bound honoured by the builder; traversal stacks are sized from it.
 constexpr int kBvhMaxDepth = 60;

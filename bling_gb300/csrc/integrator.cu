@@ -71,7 +71,8 @@ struct Queues {
 // counters (unsigned long long): queue sizes and statistics
 enum : int {
   C_LIVE0 = 0, C_LIVE1 = 1, C_CLOSEST = 2, C_ANY = 3, C_NONFINITE = 4, C_NEXT_TRACE = 5,
-  C_SHADOW = 6, C_MIS = 7, C_RESOLVE = 8, C_NEXT_SHADOW = 9, C_NEXT_MIS = 10, C_COUNT = 16
+  C_SHADOW = 6, C_MIS = 7, C_RESOLVE = 8, C_NEXT_SHADOW = 9, C_NEXT_MIS = 10, C_DEGENERATE = 11,
+  C_COUNT = 16
 };
 
 constexpr size_t kSlotWords = 16 * 6 + 7 + 4 + 3 + 8 + 1 + 7 + 4;  // per slot, 4-byte words
@@ -236,11 +237,12 @@ __global__ void k_bounce_reset(unsigned long long* counters, int next_live) {
 }
 
 // closest hit of the live paths' rays (scIntersect)
+template <bool WIDE>
 __global__ void __launch_bounds__(128) k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
                                                const unsigned long long* __restrict__ qcount,
                                                unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)*qcount;
-  traceWarpPersistent<false>(
+  traceWarpPersistent<false, WIDE, false>(
       A, n, counters + C_NEXT_TRACE, [&](int64_t q) { return loadRay7(st.ray, st.cap, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         int s = queue[q];
@@ -253,11 +255,12 @@ __global__ void __launch_bounds__(128) k_trace(DevAccel A, Slots st, const int32
 }
 
 // occlusion of the shadow rays (occluded, Scene.hs:168-170)
+template <bool WIDE>
 __global__ void __launch_bounds__(128) k_trace_shadow(DevAccel A, Slots st,
                                                       const int32_t* __restrict__ queue,
                                                       unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_SHADOW];
-  traceWarpPersistent<true>(
+  traceWarpPersistent<true, WIDE, false>(
       A, n, counters + C_NEXT_SHADOW,
       [&](int64_t q) {
         int s = queue[q];
@@ -266,16 +269,20 @@ __global__ void __launch_bounds__(128) k_trace_shadow(DevAccel A, Slots st,
                    V3{st.sray[3 * c + s], st.sray[4 * c + s], st.sray[5 * c + s]},
                    st.sray[6 * c + s], st.sray[7 * c + s]};
       },
-      [&](int64_t q, const RayQueryResult& res) { st.svis[queue[q]] = res.hit ? 0 : 1; });
+      [&](int64_t q, const RayQueryResult& res) {
+        st.svis[queue[q]] = res.hit ? 0 : 1;
+        if (res.prim == kDegenerateRay) atomicAdd(counters + C_DEGENERATE, 1ull);
+      });
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_ANY, (unsigned long long)n);
 }
 
 // closest hit of the BSDF-sampled MIS rays
+template <bool WIDE>
 __global__ void __launch_bounds__(128) k_trace_mis(DevAccel A, Slots st,
                                                    const int32_t* __restrict__ queue,
                                                    unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_MIS];
-  traceWarpPersistent<false>(
+  traceWarpPersistent<false, WIDE, false>(
       A, n, counters + C_NEXT_MIS, [&](int64_t q) { return loadRay7(st.mray, st.cap, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         int s = queue[q];
@@ -323,7 +330,11 @@ __global__ void __launch_bounds__(128) k_shade(DevAccel A, DevShading S, PassPar
       Ray ray = loadRay7(st.ray, c, s);
       bool specular = depth == 0 || signbit(st.ray[6 * c + s]);
       int prim = st.hit_prim[s];
-      if (prim < 0 || depth == P.max_depth) {
+      if (prim == kDegenerateRay) {
+        // a NaN ray: the reference's sample ends NaN and is dropped by the film
+        atomicAdd(counters + C_DEGENERATE, 1ull);
+        finishPath(film, P, s, sConst(NAN), counters);
+      } else if (prim < 0 || depth == P.max_depth) {
         Spec Lr = loadBands(st.L, c, s);
         if (prim < 0 && specular) {  // nothing hit after a specular bounce: l + t * sum le
           Spec sum = sConst(0);
@@ -433,7 +444,11 @@ __global__ void __launch_bounds__(128) k_resolve(DevAccel A, DevShading S, PassP
         int mp = st.mhit_prim[s];
         bool use = false;
         Spec lr;
-        if (mp >= 0) {
+        if (mp == kDegenerateRay) {
+          atomicAdd(counters + C_DEGENERATE, 1ull);
+          lr = sConst(NAN);  // a NaN ray poisons the sample, which the film then drops
+          use = true;
+        } else if (mp >= 0) {
           if (l.kind == DLIGHT_AREA) {
             int2 info = __ldg(S.prim_info + mp);
             if (info.x < 0 && ~info.x == l.shape) {  // Eq Light: the same area light
@@ -511,9 +526,10 @@ bool g_grids_ready[64] = {false};
 Grids grids(int device, int sms) {
   if (device >= 0 && device < 64 && g_grids_ready[device]) return g_grids[device];
   Grids g;
-  g.trace = residentGrid(k_trace, sms);
-  g.shadow = residentGrid(k_trace_shadow, sms);
-  g.mis = residentGrid(k_trace_mis, sms);
+  // both layouts' kernels use the same registers within a few; take the smaller grid
+  g.trace = std::min(residentGrid(k_trace<true>, sms), residentGrid(k_trace<false>, sms));
+  g.shadow = std::min(residentGrid(k_trace_shadow<true>, sms), residentGrid(k_trace_shadow<false>, sms));
+  g.mis = std::min(residentGrid(k_trace_mis<true>, sms), residentGrid(k_trace_mis<false>, sms));
   g.shade = residentGrid(k_shade, sms);
   g.resolve = residentGrid(k_resolve, sms);
   g.raygen = (unsigned)std::max(1, sms * 8);
@@ -574,12 +590,21 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
   for (int depth = 0; depth <= max_depth; depth++) {
     int in = depth & 1;
     k_bounce_reset<<<1, 32, 0, stream>>>(counters, C_LIVE0 + (1 - in));
-    k_trace<<<std::min(G.trace, cap_blocks), block, 0, stream>>>(A, st, Q.live[in],
-                                                                  counters + C_LIVE0 + in, counters);
+    unsigned gt = std::min(G.trace, cap_blocks), gs = std::min(G.shadow, cap_blocks),
+             gm = std::min(G.mis, cap_blocks);
+    if (A.wide)
+      k_trace<true><<<gt, block, 0, stream>>>(A, st, Q.live[in], counters + C_LIVE0 + in, counters);
+    else
+      k_trace<false><<<gt, block, 0, stream>>>(A, st, Q.live[in], counters + C_LIVE0 + in, counters);
     k_shade<<<std::min(G.shade, cap_blocks), block, 0, stream>>>(A, S, P, st, Q, depth,
                                                                   C_LIVE0 + in, d_film, counters);
-    k_trace_shadow<<<std::min(G.shadow, cap_blocks), block, 0, stream>>>(A, st, Q.shadow, counters);
-    k_trace_mis<<<std::min(G.mis, cap_blocks), block, 0, stream>>>(A, st, Q.mis, counters);
+    if (A.wide) {
+      k_trace_shadow<true><<<gs, block, 0, stream>>>(A, st, Q.shadow, counters);
+      k_trace_mis<true><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);
+    } else {
+      k_trace_shadow<false><<<gs, block, 0, stream>>>(A, st, Q.shadow, counters);
+      k_trace_mis<false><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);
+    }
     k_resolve<<<std::min(G.resolve, cap_blocks), block, 0, stream>>>(A, S, P, st, Q,
                                                                       C_LIVE0 + (1 - in), d_film,
                                                                       counters);
@@ -651,6 +676,7 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
   res.rays_closest = cnt[C_CLOSEST];
   res.rays_any = cnt[C_ANY];
   res.nonfinite = cnt[C_NONFINITE];
+  res.degenerate = cnt[C_DEGENERATE];
   res.path_samples = total;
   return BLING_OK;
 }
@@ -727,6 +753,7 @@ int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const
   res.rays_closest = cnt[C_CLOSEST];
   res.rays_any = cnt[C_ANY];
   res.nonfinite = cnt[C_NONFINITE];
+  res.degenerate = cnt[C_DEGENERATE];
   res.path_samples = total;
   return BLING_OK;
 }

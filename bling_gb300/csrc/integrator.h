@@ -54,7 +54,7 @@ struct DevShading {
 };
 
 struct PassResult {
-  uint64_t rays_closest, rays_any, path_samples, nonfinite;
+  uint64_t rays_closest, rays_any, path_samples, nonfinite, degenerate;
 };
 
 // Device buffer reused across passes (grow-only), owned by a context: the

@@ -10,18 +10,23 @@ namespace bgpu {
 // leaf slot flags (third float4 .z of a slot, as int bits)
 enum : int { SLOT_LAST = 1, SLOT_SHAPE = 2 };
 
-// Device view of a scene's acceleration structure.
-//   nodes: 4 float4 per internal node (layout in bvh.h)
-//   slots: 3 float4 per leaf slot:
+// Device view of a scene's acceleration structure.  One of two node layouts
+// (bvh.h) is resident:
+//   binary (wide == 0): nodes, 4 float4 per inner node, root_ref
+//   wide   (wide != 0): nodes8, 5 uint4 per 8-wide quantised node, root8
+//   slots: 3 float4 per leaf slot, in the resident layout's leaf order:
 //     triangle: (p1.xyz, e1.x) (e1.yz, e2.xy) (e2.z, prim, flags, 0)
 //               with e1 = p2 - p1, e2 = p3 - p1 rounded exactly as the
 //               reference computes them (TriangleMesh.hs:157-158, 169)
 //     shape:    (shape index, 0, 0, 0) (0...) (0, prim, flags|SLOT_SHAPE, 0)
 struct DevAccel {
   const float4* nodes;
+  const uint4* nodes8;
   const float4* slots;
   const DShape* shapes;
   int32_t root_ref;
+  int32_t root8;
+  int32_t wide;
   int32_t n_shapes;
   int64_t n_prims;
 };

@@ -1,7 +1,7 @@
 // Ray-query kernels over SoA ray buffers: persistent warps (trace.cuh,
-// traceWarpPersistent) plus an instrumented one-thread-per-ray variant that
-// counts the traversal work.
-#include <mutex>
+// traceWarpPersistent), one instantiation per node layout, plus the
+// instrumented variant that counts the traversal work.
+#include <algorithm>
 
 #include "internal.h"
 #include "trace.cuh"
@@ -16,11 +16,12 @@ __device__ __forceinline__ Ray loadRay(const float* __restrict__ rays, int64_t n
 
 constexpr int kTraceBlock = 128;
 
+template <bool WIDE>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_closest(DevAccel A, const float* __restrict__ rays, int64_t n,
                     float* __restrict__ out_t, int32_t* __restrict__ out_prim,
                     float* __restrict__ out_b, unsigned long long* __restrict__ next_ray) {
-  traceWarpPersistent<false>(
+  traceWarpPersistent<false, WIDE, false>(
       A, n, next_ray, [&](int64_t i) { return loadRay(rays, n, i); },
       [&](int64_t i, const RayQueryResult& q) {
         out_t[i] = q.hit ? q.t : INFINITY;
@@ -32,24 +33,24 @@ __global__ void __launch_bounds__(kTraceBlock)
       });
 }
 
+template <bool WIDE>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_any(DevAccel A, const float* __restrict__ rays, int64_t n,
                 uint8_t* __restrict__ out_hit, unsigned long long* __restrict__ next_ray) {
-  traceWarpPersistent<true>(
+  traceWarpPersistent<true, WIDE, false>(
       A, n, next_ray, [&](int64_t i) { return loadRay(rays, n, i); },
       [&](int64_t i, const RayQueryResult& q) { out_hit[i] = q.hit ? 1 : 0; });
 }
 
-__global__ void k_trace_counts(DevAccel A, const float* __restrict__ rays, int64_t n,
-                               unsigned long long* __restrict__ totals) {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// totals[0] nodes visited, totals[1] leaf slots tested, totals[2] the next-ray counter
+template <bool WIDE>
+__global__ void __launch_bounds__(kTraceBlock)
+    k_trace_counts(DevAccel A, const float* __restrict__ rays, int64_t n,
+                   unsigned long long* __restrict__ totals) {
   TraversalCounts c{0, 0};
-  if (i < n) {
-    Ray r = loadRay(rays, n, i);
-    float t, b1, b2;
-    int prim;
-    traverse<false, true>(A, r, t, prim, b1, b2, &c);
-  }
+  traceWarpPersistent<false, WIDE, true>(
+      A, n, totals + 2, [&](int64_t i) { return loadRay(rays, n, i); },
+      [&](int64_t, const RayQueryResult&) {}, &c);
   // warp reduction, one atomic per warp
   for (int o = 16; o > 0; o >>= 1) {
     c.nodes += __shfl_down_sync(0xffffffffu, c.nodes, o);
@@ -76,8 +77,14 @@ static unsigned persistentGrid(K kernel, int64_t n) {
 cudaError_t launch_trace_counts(const DevAccel& A, const float* d_rays, int64_t n,
                                 unsigned long long* d_totals, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  int64_t grid = (n + 127) / 128;
-  k_trace_counts<<<(unsigned)grid, 128, 0, stream>>>(A, d_rays, n, d_totals);
+  cudaError_t e = cudaMemsetAsync(d_totals, 0, 3 * sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  if (A.wide)
+    k_trace_counts<true><<<persistentGrid(k_trace_counts<true>, n), kTraceBlock, 0, stream>>>(
+        A, d_rays, n, d_totals);
+  else
+    k_trace_counts<false><<<persistentGrid(k_trace_counts<false>, n), kTraceBlock, 0, stream>>>(
+        A, d_rays, n, d_totals);
   return cudaGetLastError();
 }
 
@@ -87,8 +94,12 @@ cudaError_t launch_trace_closest(const DevAccel& A, const float* d_rays, int64_t
   if (n <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  unsigned grid = persistentGrid(k_trace_closest, n);
-  k_trace_closest<<<grid, kTraceBlock, 0, stream>>>(A, d_rays, n, d_t, d_prim, d_b1b2, d_counter);
+  if (A.wide)
+    k_trace_closest<true><<<persistentGrid(k_trace_closest<true>, n), kTraceBlock, 0, stream>>>(
+        A, d_rays, n, d_t, d_prim, d_b1b2, d_counter);
+  else
+    k_trace_closest<false><<<persistentGrid(k_trace_closest<false>, n), kTraceBlock, 0, stream>>>(
+        A, d_rays, n, d_t, d_prim, d_b1b2, d_counter);
   return cudaGetLastError();
 }
 
@@ -97,8 +108,12 @@ cudaError_t launch_trace_any(const DevAccel& A, const float* d_rays, int64_t n, 
   if (n <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  unsigned grid = persistentGrid(k_trace_any, n);
-  k_trace_any<<<grid, kTraceBlock, 0, stream>>>(A, d_rays, n, d_hit, d_counter);
+  if (A.wide)
+    k_trace_any<true><<<persistentGrid(k_trace_any<true>, n), kTraceBlock, 0, stream>>>(
+        A, d_rays, n, d_hit, d_counter);
+  else
+    k_trace_any<false><<<persistentGrid(k_trace_any<false>, n), kTraceBlock, 0, stream>>>(
+        A, d_rays, n, d_hit, d_counter);
   return cudaGetLastError();
 }
 

@@ -8,18 +8,19 @@
 // primitive with an equal t replaces the earlier one in the fold, because the
 // intersection tests reject only t > tmax, TriangleMesh.hs:146,166).
 //
-// Node boxes are tested with the robust form (lo - o) * (1/d), whose relative
-// error is a few ulp, and the box interval is widened by a relative 2^-16 so
-// that a primitive whose reference-arithmetic t lies on a box face is never
-// pruned.
+// Box tests are conservative: the slab distances carry a relative error of a
+// few ulp, and every box interval is widened by a relative 2^-16 so that a
+// primitive whose reference-arithmetic t lies on a box face is never pruned
+// (the quantised wide layout also widens each child box by one quantum).
 #pragma once
+#include "bvh.h"
 #include "dmath.cuh"
 #include "dshape.cuh"
 #include "internal.h"
 
 namespace bgpu {
 
-constexpr int kTraversalStack = 64;
+constexpr int kTraversalStack = 64;  // binary layout: depth < kBvhMaxDepth
 constexpr float kBoxSlack = 1.0f / 65536.0f;
 
 // triangleIntersect / triangleIntersects (TriangleMesh.hs:140-181) on a
@@ -58,94 +59,40 @@ __device__ __forceinline__ void boxInterval(float lox, float hix, float loy, flo
   tf = f + fabsf(f) * kBoxSlack;
 }
 
-// work counters of one traversal (the instrumented variant only; the
+// work counters of a traversal (the instrumented variant only; the
 // reference's dbgTraverse counts the same things, Primitive/KdTree.hs:252-281)
 struct TraversalCounts {
-  unsigned nodes;  // internal nodes visited (64-byte node reads)
+  unsigned nodes;  // inner nodes visited (64-byte binary or 80-byte wide node reads)
   unsigned slots;  // leaf slots tested (48-byte primitive reads)
 };
 
-// Returns true on a hit.  ANY: stop at the first primitive hit in
-// [tmin, tmax].  Otherwise: best_t/best_prim/b1/b2 hold the closest hit.
-// COUNT: also accumulate node visits and primitive tests into *cnt.
-template <bool ANY, bool COUNT = false>
-__device__ __forceinline__ bool traverse(const DevAccel& A, const Ray& r, float& best_t,
-                                         int& best_prim, float& bb1, float& bb2,
-                                         TraversalCounts* cnt = nullptr) {
-  V3 inv{1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z};
-  best_t = r.tmax;
-  best_prim = -1;
-  bb1 = bb2 = 0.0f;
-  int stack[kTraversalStack];
-  int sp = 0;
-  int cur = A.root_ref;
-  for (;;) {
-    if (cur >= 0) {
-      if (COUNT) cnt->nodes++;
-      const float4* nd = A.nodes + 4 * (size_t)cur;
-      float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2);
-      float4 refs = __ldg(nd + 3);
-      float n0, f0, n1, f1;
-      boxInterval(a.x, a.y, a.z, a.w, c.x, c.y, r.o, inv, n0, f0);
-      boxInterval(b.x, b.y, b.z, b.w, c.z, c.w, r.o, inv, n1, f1);
-      bool h0 = fmaxf(n0, r.tmin) <= fminf(f0, best_t);
-      bool h1 = fmaxf(n1, r.tmin) <= fminf(f1, best_t);
-      int r0 = __float_as_int(refs.x), r1 = __float_as_int(refs.y);
-      if (h0 && h1) {
-        bool swap = n1 < n0;
-        cur = swap ? r1 : r0;
-        stack[sp++] = swap ? r0 : r1;
-        continue;
-      }
-      if (h0 || h1) {
-        cur = h0 ? r0 : r1;
-        continue;
-      }
-    } else {
-      int slot = ~cur;
-      for (;;) {
-        if (COUNT) cnt->slots++;
-        const float4* sl = A.slots + 3 * (size_t)slot;
-        float4 s0 = __ldg(sl), s1 = __ldg(sl + 1), s2 = __ldg(sl + 2);
-        int flags = __float_as_int(s2.z);
-        int prim = __float_as_int(s2.y);
-        bool hit;
-        float t = 0, b1 = 0, b2 = 0;
-        if (!(flags & SLOT_SHAPE)) {
-          hit = triTest(s0, s1, s2, r, best_t, t, b1, b2);
-        } else {
-          const DShape& sh = A.shapes[__float_as_int(s0.x)];
-          Ray ro = transRay(sh.w2o, Ray{r.o, r.d, r.tmin, ANY ? r.tmax : best_t});
-          if (ANY) {
-            hit = shapeIntersects(sh, ro);
-          } else {
-            float e;
-            hit = shapeIntersect<false>(sh, ro, t, e, nullptr);
-          }
-        }
-        if (hit) {
-          if (ANY) return true;
-          if (t < best_t || prim > best_prim) {
-            best_t = t;
-            best_prim = prim;
-            bb1 = b1;
-            bb2 = b2;
-          }
-        }
-        if (flags & SLOT_LAST) break;
-        slot++;
-      }
-    }
-    if (sp == 0) break;
-    cur = stack[--sp];
-  }
-  return best_prim >= 0;
+struct RayQueryResult {
+  bool hit;
+  float t, b1, b2;
+  int prim;
+};
+
+// A ray with a NaN component makes every slab test pass (fminf/fmaxf drop
+// NaN), so its walk would visit the whole tree; the reference's kd-tree walk
+// does the same (`tp > tmax || tp <= 0` and `tp < tmin` are all False for NaN,
+// KdTree.hs:212-215) and its NaN-distance "hit" ends in a sample that addSample
+// drops (Image.hs:253-256).  Such rays are answered without traversal:
+// occluded for any-hit queries (triangleIntersects is True for NaN), and the
+// degenerate primitive ID kDegenerateRay for closest-hit queries.
+constexpr int kDegenerateRay = -2;
+
+__device__ __forceinline__ bool degenerateRay(const Ray& r) {
+  return isnan(r.o.x) || isnan(r.o.y) || isnan(r.o.z) || isnan(r.d.x) || isnan(r.d.y) ||
+         isnan(r.d.z) || isnan(r.tmin) || isnan(r.tmax);
+}
+
+// u8 -> float without a conversion instruction: 0x4B0000bb is 2^23 + bb
+__device__ __forceinline__ float qbyte(uint32_t word, uint32_t sel) {
+  return __uint_as_float(__byte_perm(word, 0x4B000000u, sel)) - 8388608.0f;
 }
 
 // ---------------------------------------------------------------------------
 // Warp-synchronous persistent traversal.
-//
-// The same query as traverse<ANY>, restructured for SIMT efficiency:
 //  * every warp loops over rays it fetches itself: lanes whose ray finished
 //    take the next rays from a global counter (one atomicAdd per warp,
 //    __ballot_sync/__popc to rank the lanes), so lanes never idle while rays
@@ -154,30 +101,29 @@ __device__ __forceinline__ bool traverse(const DevAccel& A, const Ray& r, float&
 //    "while-while" order): in the node phase a lane that meets a leaf
 //    postpones it and keeps walking inner nodes until every lane holds a leaf
 //    or has finished, then the warp tests leaves together.
-// All votes use the full warp mask: every lane runs every iteration of the
-// uniform loops and does work only when it has some.
+// WIDE selects the 8-wide quantised layout (bvh.h): each visit tests eight
+// child boxes and pushes the hit ones in the octant order of the ray, so the
+// nearest is taken next.  All votes use the full warp mask: every lane runs
+// every iteration of the uniform loops and does work only when it has some.
 constexpr int kSentinel = INT32_MIN;
 
-struct RayQueryResult {
-  bool hit;
-  float t, b1, b2;
-  int prim;
-};
-
-template <bool ANY, class LoadRay, class Emit>
+template <bool ANY, bool WIDE, bool COUNT, class LoadRay, class Emit>
 __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n,
                                                     unsigned long long* __restrict__ next_ray,
-                                                    LoadRay load, Emit emit) {
+                                                    LoadRay load, Emit emit,
+                                                    TraversalCounts* cnt = nullptr) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
+  constexpr int kStack = WIDE ? kWideStack : kTraversalStack;
   int64_t rid = -1;
   bool exhausted = false;
   Ray r;
   V3 inv;
+  int oct = 0;
   float best_t = 0, bb1 = 0, bb2 = 0;
   int best_prim = -1;
-  int stack[kTraversalStack];
+  int stack[kStack];
   int sp = 0;
   int cur = kSentinel;
   int leaf = kSentinel;  // postponed leaf
@@ -195,41 +141,99 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
         if ((int64_t)my < n) {
           rid = (int64_t)my;
           r = load(rid);
-          inv = V3{1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z};
-          best_t = r.tmax;
-          best_prim = -1;
-          bb1 = bb2 = 0.0f;
-          sp = 0;
-          cur = A.root_ref;
-          leaf = kSentinel;
+          if (degenerateRay(r)) {
+            emit(rid, RayQueryResult{true, NAN, 0.0f, 0.0f, kDegenerateRay});
+            rid = -1;  // take another ray next round
+          } else {
+            inv = V3{1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z};
+            oct = (signbit(inv.x) ? 1 : 0) | (signbit(inv.y) ? 2 : 0) | (signbit(inv.z) ? 4 : 0);
+            best_t = r.tmax;
+            best_prim = -1;
+            bb1 = bb2 = 0.0f;
+            sp = 0;
+            cur = WIDE ? A.root8 : A.root_ref;
+            leaf = kSentinel;
+          }
         } else {
           exhausted = true;
         }
       }
     }
-    if (!__any_sync(FULL, rid >= 0)) return;
+    if (!__any_sync(FULL, rid >= 0 || !exhausted)) return;
     // ---- node phase
     for (;;) {
       bool work = rid >= 0 && cur >= 0;
       if (!__any_sync(FULL, work)) break;
       if (work) {
-        const float4* nd = A.nodes + 4 * (size_t)cur;
-        float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2);
-        float4 refs = __ldg(nd + 3);
-        float n0, f0, n1, f1;
-        boxInterval(a.x, a.y, a.z, a.w, c.x, c.y, r.o, inv, n0, f0);
-        boxInterval(b.x, b.y, b.z, b.w, c.z, c.w, r.o, inv, n1, f1);
-        bool h0 = fmaxf(n0, r.tmin) <= fminf(f0, best_t);
-        bool h1 = fmaxf(n1, r.tmin) <= fminf(f1, best_t);
-        int r0 = __float_as_int(refs.x), r1 = __float_as_int(refs.y);
-        if (h0 && h1) {
-          bool swap = n1 < n0;
-          cur = swap ? r1 : r0;
-          stack[sp++] = swap ? r0 : r1;
-        } else if (h0 || h1) {
-          cur = h0 ? r0 : r1;
+        if (COUNT) cnt->nodes++;
+        if (WIDE) {
+          const uint4* nd = A.nodes8 + 5 * (size_t)cur;
+          uint4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3),
+                w4 = __ldg(nd + 4);
+          // child box slab distances: t = q * (scale / d) + (p - o) / d
+          float sx = __uint_as_float((w0.w & 0xffu) << 23) * inv.x;
+          float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23) * inv.y;
+          float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23) * inv.z;
+          float bx = (__uint_as_float(w0.x) - r.o.x) * inv.x;
+          float by = (__uint_as_float(w0.y) - r.o.y) * inv.y;
+          float bz = (__uint_as_float(w0.z) - r.o.z) * inv.z;
+          // near/far planes by the direction's sign
+          uint32_t nx0 = (oct & 1) ? w3.z : w2.x, nx1 = (oct & 1) ? w3.w : w2.y;
+          uint32_t fx0 = (oct & 1) ? w2.x : w3.z, fx1 = (oct & 1) ? w2.y : w3.w;
+          uint32_t ny0 = (oct & 2) ? w4.x : w2.z, ny1 = (oct & 2) ? w4.y : w2.w;
+          uint32_t fy0 = (oct & 2) ? w2.z : w4.x, fy1 = (oct & 2) ? w2.w : w4.y;
+          uint32_t nz0 = (oct & 4) ? w4.z : w3.x, nz1 = (oct & 4) ? w4.w : w3.y;
+          uint32_t fz0 = (oct & 4) ? w3.x : w4.z, fz1 = (oct & 4) ? w3.y : w4.w;
+          uint32_t hits = 0;
+#pragma unroll
+          for (int i = 0; i < 8; i++) {
+            const uint32_t sel = 0x7650u | (uint32_t)(i & 3);
+            float tnx = fmaf(qbyte(i < 4 ? nx0 : nx1, sel), sx, bx);
+            float tny = fmaf(qbyte(i < 4 ? ny0 : ny1, sel), sy, by);
+            float tnz = fmaf(qbyte(i < 4 ? nz0 : nz1, sel), sz, bz);
+            float tfx = fmaf(qbyte(i < 4 ? fx0 : fx1, sel), sx, bx);
+            float tfy = fmaf(qbyte(i < 4 ? fy0 : fy1, sel), sy, by);
+            float tfz = fmaf(qbyte(i < 4 ? fz0 : fz1, sel), sz, bz);
+            float tn = fmaxf(fmaxf(tnx, tny), tnz);
+            float tf = fminf(fminf(tfx, tfy), tfz);
+            tn = tn - fabsf(tn) * kBoxSlack;
+            tf = tf + fabsf(tf) * kBoxSlack;
+            uint32_t meta = ((i < 4 ? w1.z : w1.w) >> (8 * (i & 3))) & 0xffu;
+            bool h = meta != 0xffu && fmaxf(tn, r.tmin) <= fminf(tf, best_t);
+            hits |= (h ? 1u : 0u) << i;
+          }
+          // push all hit children but the nearest, far ones first
+          int first = kSentinel;
+#pragma unroll
+          for (int k = 7; k >= 0; k--) {
+            int slot = k ^ oct;
+            if (hits >> slot & 1u) {
+              uint32_t meta = ((slot < 4 ? w1.z : w1.w) >> (8 * (slot & 3))) & 0xffu;
+              int ref = (meta & 0x80u) ? (int)(w1.x + (meta & 0x7fu)) : ~(int)(w1.y + meta);
+              if (first != kSentinel) stack[sp++] = first;
+              first = ref;
+            }
+          }
+          cur = first != kSentinel ? first : (sp > 0 ? stack[--sp] : kSentinel);
         } else {
-          cur = sp > 0 ? stack[--sp] : kSentinel;
+          const float4* nd = A.nodes + 4 * (size_t)cur;
+          float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2);
+          float4 refs = __ldg(nd + 3);
+          float n0, f0, n1, f1;
+          boxInterval(a.x, a.y, a.z, a.w, c.x, c.y, r.o, inv, n0, f0);
+          boxInterval(b.x, b.y, b.z, b.w, c.z, c.w, r.o, inv, n1, f1);
+          bool h0 = fmaxf(n0, r.tmin) <= fminf(f0, best_t);
+          bool h1 = fmaxf(n1, r.tmin) <= fminf(f1, best_t);
+          int r0 = __float_as_int(refs.x), r1 = __float_as_int(refs.y);
+          if (h0 && h1) {
+            bool swap = n1 < n0;
+            cur = swap ? r1 : r0;
+            stack[sp++] = swap ? r0 : r1;
+          } else if (h0 || h1) {
+            cur = h0 ? r0 : r1;
+          } else {
+            cur = sp > 0 ? stack[--sp] : kSentinel;
+          }
         }
         // postpone the first leaf met; keep walking inner nodes
         if (cur < 0 && cur != kSentinel && leaf == kSentinel) {
@@ -252,6 +256,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
         int slot = ~leaf;
         leaf = kSentinel;
         for (;;) {
+          if (COUNT) cnt->slots++;
           const float4* sl = A.slots + 3 * (size_t)slot;
           float4 s0 = __ldg(sl), s1 = __ldg(sl + 1), s2 = __ldg(sl + 2);
           int flags = __float_as_int(s2.z);

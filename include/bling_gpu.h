@@ -52,9 +52,12 @@ typedef struct bling_ctx bling_ctx;
 typedef struct bling_scene bling_scene;
 typedef struct bling_film bling_film;
 
+/* bling_opts.flags */
+#define BLING_FLAG_WIDE_BVH 1u /* 8-wide quantised BVH layout instead of the binary one */
+
 typedef struct bling_opts {
   int32_t device;        /* CUDA device ordinal */
-  uint32_t flags;        /* reserved, 0 */
+  uint32_t flags;        /* BLING_FLAG_* */
   int32_t block_size;    /* traversal block size, 0 = default */
   int32_t bvh_leaf_size; /* max primitives per BVH leaf, 0 = default */
 } bling_opts;
@@ -187,6 +190,7 @@ typedef struct bling_stats {
   uint64_t rays_any;        /* any-hit queries (shadow) */
   uint64_t path_samples;    /* completed camera paths */
   uint64_t nonfinite_drops; /* NaN/Inf samples skipped by the film (Image.hs:253-256) */
+  uint64_t degenerate_rays; /* rays with a NaN component, answered without traversal */
   double bvh_build_ms;
   double last_pass_ms;
   uint64_t bvh_nodes;
@@ -196,6 +200,7 @@ typedef struct bling_stats {
 
 /* ---- context ---- */
 int bling_ctx_create(bling_ctx** out, const bling_opts* opts);
+/* Destroy every scene and film of a context before the context itself. */
 void bling_ctx_destroy(bling_ctx* ctx);
 const char* bling_last_error(bling_ctx* ctx);
 /* Runs the context's work on an external CUDA stream (a cudaStream_t, e.g.
@@ -215,7 +220,10 @@ void bling_scene_destroy(bling_scene* scene);
  * the nearest hit, ties to the larger primitive ID as the reference's
  * `nearest'` fold does (Primitive.hs:29-43, TriangleMesh.hs:166).
  * prim[i] = -1 on a miss.  b1b2 may be NULL (2n floats: the barycentrics
- * of triangle hits, 0 for shapes). */
+ * of triangle hits, 0 for shapes).  A ray with a NaN component gets
+ * prim[i] = -2 and t[i] = NaN without traversal (the reference's walk would
+ * visit every node and report a NaN-distance hit); bling_trace_any reports
+ * such rays as occluded, as triangleIntersects does for NaN. */
 int bling_trace_closest(bling_scene* scene, const float* rays, size_t n, float* t,
                         int32_t* prim, float* b1b2);
 /* replaces `occluded` (Scene.hs:168-170): hit[i] = 1 when any primitive is hit
@@ -278,6 +286,15 @@ int bling_render_pass_noalloc(bling_scene* scene, const bling_render_params* par
                               float* d_film_wxyz);
 
 /* ---- host helpers for building scenes (no GPU needed) ---- */
+/* Builds the BVH of n primitive boxes (lo/hi: 3n floats each) on the host and
+ * checks its structure: each primitive in exactly one leaf, every stored box
+ * (binary and quantised 8-wide) containing its subtree.  stats (5 entries):
+ * binary inner nodes, wide nodes (0 when the wide layout was skipped), binary
+ * depth, wide depth, leaves.  Returns 0 or a negative code of the first
+ * violation.  The replacement of mkKdTree (Primitive/KdTree.hs:107-112) as a
+ * testable unit. */
+int bling_bvh_selftest(const float* lo, const float* hi, int64_t n, int32_t max_leaf,
+                       int64_t* stats);
 /* rgbToSpectrumRefl / rgbToSpectrumIllum (Spectrum.hs:140-159) */
 void bling_rgb_to_spectrum(int32_t illuminant, float r, float g, float b, float out[BLING_BANDS]);
 /* spectrumToXYZ (Spectrum.hs:349-355) */

@@ -698,9 +698,9 @@ static DG shadingGeometry(const orc_scene& S, const Prim& pr, const DG& dgg) {
 }
 
 struct Hit {
-  float t, eps;
-  int prim;
-  float b1, b2;
+  float t = 0.0f, eps = 0.0f;
+  int prim = -1;
+  float b1 = 0.0f, b2 = 0.0f;
 };
 
 // Primitive.intersect for primitive i, without building the DG (cheap path):

@@ -133,6 +133,20 @@ def test_heightfield_scene_vs_oracle(gpu_ctx):
     assert st_g["nonfinite_drops"] == 0
 
 
+def test_wide_bvh_layout_renders_like_the_oracle(gpu_ctx):
+    """the integrator's traversal kernels over the 8-wide quantised layout"""
+    from bling_gb300.api import Context
+    sc = S.heightfield_scene(ns=257, n_spheres=256, width=80, height=45, env_size=(128, 64))
+    p = S.heightfield_params(80, 45, spp_side=2, max_depth=8, rr_depth=3)
+    wide = Context(device=0, wide_bvh=True)
+    try:
+        fg, fo, st_g, _ = _render_both(wide, sc, p)
+    finally:
+        wide.close()
+    _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
+    assert st_g["nonfinite_drops"] == 0
+
+
 def test_heightfield_full_geometry_small_image(gpu_ctx):
     """8.4M-triangle heightfield and 4096 spheres, cropped to a small image"""
     sc = S.heightfield_scene(ns=2048, n_spheres=4096, width=48, height=27, env_size=(256, 128))

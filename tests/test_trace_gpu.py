@@ -18,6 +18,21 @@ from oracle.oracle import OracleScene
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(scope="module")
+def wide_ctx():
+    """A second context whose scenes use the 8-wide quantised BVH layout."""
+    from bling_gb300.api import Context
+    ctx = Context(device=0, wide_bvh=True)
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(params=["binary", "wide"])
+def ctx(request, gpu_ctx):
+    """Both BVH layouts must give the oracle's answers."""
+    return gpu_ctx if request.param == "binary" else request.getfixturevalue("wide_ctx")
+
+
 def _bits(a):
     return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
 
@@ -33,9 +48,9 @@ def _check_closest(g, o, rays, brute=True):
     return t, p
 
 
-def test_soup_closest_and_any_vs_brute_force(gpu_ctx):
+def test_soup_closest_and_any_vs_brute_force(ctx):
     soup = S.triangle_soup(30000, seed=5)
-    g, o = gpu_ctx.scene(soup), OracleScene(soup)
+    g, o = ctx.scene(soup), OracleScene(soup)
     rays = S.soup_rays(4096, seed=6)
     t, p = _check_closest(g, o, rays)
     assert 0.3 < (p >= 0).mean() < 1.0
@@ -43,9 +58,9 @@ def test_soup_closest_and_any_vs_brute_force(gpu_ctx):
     assert np.array_equal(g.any(ra), o.any(ra, brute=True))
 
 
-def test_1m_soup_vs_oracle_bvh(gpu_ctx):
+def test_1m_soup_vs_oracle_bvh(ctx):
     soup = S.triangle_soup(1 << 20, seed=1)
-    g, o = gpu_ctx.scene(soup), OracleScene(soup)
+    g, o = ctx.scene(soup), OracleScene(soup)
     rays = S.soup_rays(1 << 17, seed=2)
     _check_closest(g, o, rays, brute=False)
     ra = S.soup_rays(1 << 17, seed=3, any_hit=True)
@@ -105,9 +120,9 @@ def _shape_scene(seed, n_tris=200, n_shapes=60):
 
 
 @pytest.mark.parametrize("seed", [21, 22])
-def test_analytic_shapes_vs_brute_force(gpu_ctx, seed):
+def test_analytic_shapes_vs_brute_force(ctx, seed):
     sc = _shape_scene(seed)
-    g, o = gpu_ctx.scene(sc), OracleScene(sc)
+    g, o = ctx.scene(sc), OracleScene(sc)
     rays = S.soup_rays(8192, seed=seed + 100)
     rays[0:3] *= 0.7  # some origins inside shapes
     _check_closest(g, o, rays)
@@ -115,7 +130,7 @@ def test_analytic_shapes_vs_brute_force(gpu_ctx, seed):
     assert np.array_equal(g.any(ra), o.any(ra, brute=True))
 
 
-def test_ties_go_to_the_larger_primitive_id(gpu_ctx):
+def test_ties_go_to_the_larger_primitive_id(ctx):
     rng = np.random.default_rng(3)
     c = rng.uniform(-1, 1, (500, 3))
     v = np.stack([c, c + [0.1, 0, 0], c + [0, 0.1, 0]], 1).reshape(-1, 3)
@@ -123,7 +138,7 @@ def test_ties_go_to_the_larger_primitive_id(gpu_ctx):
     s = S.Scene()
     m = s.add_material(abi.MAT_MATTE, kd=constant(0.5))
     s.add_mesh(v, np.arange(len(v)), m)
-    g, o = gpu_ctx.scene(s), OracleScene(s)
+    g, o = ctx.scene(s), OracleScene(s)
     rays = np.zeros((8, 4096), np.float32)
     tgt = c[rng.integers(0, 500, 4096)] + [0.02, 0.02, 0]
     rays[0:3] = (tgt + [0, 0, -3]).T
@@ -133,9 +148,9 @@ def test_ties_go_to_the_larger_primitive_id(gpu_ctx):
     assert (p[p >= 0] >= 1000).all()  # the third copy wins
 
 
-def test_edge_cases(gpu_ctx):
+def test_edge_cases(ctx):
     soup = S.triangle_soup(5000, seed=8)
-    g, o = gpu_ctx.scene(soup), OracleScene(soup)
+    g, o = ctx.scene(soup), OracleScene(soup)
     empty = np.zeros((8, 0), np.float32)
     t, p, _ = g.closest(empty)
     assert t.size == 0 and g.any(empty).size == 0
@@ -150,6 +165,23 @@ def test_edge_cases(gpu_ctx):
     rays[7] = rng.choice([np.inf, 0.3, 0.0], 3000)  # includes tmin > tmax
     _check_closest(g, o, rays)
     assert np.array_equal(g.any(rays), o.any(rays, brute=True))
+
+
+def test_nan_rays_are_degenerate_and_cheap(ctx):
+    soup = S.triangle_soup(1 << 20, seed=1)
+    g = ctx.scene(soup)
+    rays = S.soup_rays(4096, seed=4)
+    rays[3, ::7] = np.nan  # NaN direction component
+    rays[0, 3::11] = np.nan  # NaN origin component
+    bad = np.isnan(rays).any(0)
+    t, p, _ = g.closest(rays)
+    assert (p[bad] == -2).all() and np.isnan(t[bad]).all()
+    assert (p[~bad] != -2).all()
+    assert g.any(rays)[bad].all()
+    # the good rays still get the oracle's answers
+    o = OracleScene(soup)
+    good = np.ascontiguousarray(rays[:, ~bad][:, :512])
+    _check_closest(g, o, good, brute=False)
 
 
 @pytest.mark.parametrize("bad", ["negative", "not_multiple_of_3", "out_of_range"])
