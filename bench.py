@@ -289,6 +289,183 @@ def measure_render(ctx, stream, args):
     return out
 
 
+def _extent_samples(p):
+    from bling_gb300.autotune import extent_samples
+    return extent_samples(p)
+
+
+def _films_equal(a, b):
+    """equal samples up to the order of float additions (box-filter weights exact)"""
+    if not np.array_equal(a[..., 0], b[..., 0]):
+        return False
+    scale = float(np.abs(b[..., 1:]).max()) + 1e-30
+    return bool(np.allclose(a[..., 1:], b[..., 1:], rtol=1e-5, atol=1e-6 * scale))
+
+
+def measure_batched(args):
+    """The batched workload: `--batch-instances` scene instances (seeded soup
+    plus spheres, triangle counts log-uniform in [10k, 2M], square images with
+    sides uniform in [128, 1024], 4-256 spp, max depth 3-10), one pass each.
+    Plain: one bling_render_pass per job, back to back.  Batched: one batch
+    of all jobs (path regeneration, a CUDA graph per iteration) in the
+    configuration the autotuner picks on a trial at 1 spp.  Both sides trace
+    the same samples with the same random numbers, so the images, and their
+    RMSE against any reference, are equal up to the order of float additions;
+    `equal_images` reports the check."""
+    import torch
+
+    from bling_gb300 import autotune
+    from bling_gb300 import scene as S
+    from bling_gb300.api import Batch, Context
+    t0 = time.perf_counter()
+    inst = S.batch_instances(n=args.batch_instances)
+    gen_s = time.perf_counter() - t0
+    params = [i.params for i in inst]
+    samples = sum(_extent_samples(p) for p in params)
+    # autotune on a quarter of the instances (leaf sizes rebuild those scenes)
+    sub = inst[:: max(1, len(inst) // 16)][:16]
+    t0 = time.perf_counter()
+    best, trials = autotune.autotune([i.scene for i in sub], [i.params for i in sub],
+                                     scene_factory=lambda sc, c: c.scene(sc))
+    tune_s = time.perf_counter() - t0
+    ctx = Context(device=0, bvh_leaf_size=best.leaf_size)
+    t0 = time.perf_counter()
+    gs = [ctx.scene(i.scene) for i in inst]
+    build_s = time.perf_counter() - t0
+    films = [ctx.film(p.width, p.height) for p in params]
+    gs[0].render_pass(films[0], params[0], 0)  # warm-up
+    films[0].clear()
+    st0 = [g.stats() for g in gs]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for g, p, f in zip(gs, params, films):
+        g.render_pass(f, p, 1)
+    plain_s = time.perf_counter() - t0
+    st1 = [g.stats() for g in gs]
+    rays = sum((b["rays_closest"] - a["rays_closest"]) + (b["rays_any"] - a["rays_any"])
+               for a, b in zip(st0, st1))
+    ref = [f.read() for f in films]
+    b = Batch(ctx, **best.batch_kwargs())
+    b.submit(gs[0], films[0], params[0], 0)  # warm-up (graph capture)
+    b.run()
+    for f in films:
+        f.clear()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for g, p, f in zip(gs, params, films):
+        b.submit(g, f, p, 1)
+    b.run()
+    batch_s = time.perf_counter() - t0
+    bst = b.stats()
+    equal = all(_films_equal(f.read(), r) for f, r in zip(films, ref))
+    b.close()
+    out = {
+        "instances": len(inst), "triangles": sum(i.n_tris for i in inst),
+        "path_samples": samples, "scene_gen_s": round(gen_s, 2), "bvh_build_s": round(build_s, 2),
+        "plain_per_job": {"s": round(plain_s, 3), "path_samples_per_s": round(samples / plain_s, 1),
+                          "mrays_per_s": round(rays / plain_s / 1e6, 2)},
+        "batched": {"s": round(batch_s, 3), "path_samples_per_s": round(samples / batch_s, 1),
+                    "mrays_per_s": round((bst["rays_closest"] + bst["rays_any"]) / batch_s / 1e6, 2),
+                    "iterations": bst["iterations"]},
+        "speedup": round(plain_s / batch_s, 3), "equal_images": equal,
+        "autotuned": {**best.__dict__, "trials": len(trials), "tune_s": round(tune_s, 1),
+                      "trial": "1 spp, every 4th instance, leaf sizes 2/4/8"},
+    }
+    ctx.close()
+    return out
+
+
+def _pct(xs, q):
+    return float(np.percentile(np.asarray(xs), q)) if xs else None
+
+
+def measure_serving(args):
+    """The serving workload: eight resident scenes (6M triangles), jobs
+    arriving as a Poisson process at 200/s, each on one scene at a square
+    size log-uniform in [128, 1024] and 16-512 spp (log-uniform), admitted
+    under a 40 GiB budget and merged into one wavefront by the render server.
+    Reported: p50/p99 latency (arrival to film on the host) and path
+    samples/s over the run, next to the same jobs run alone one after the
+    other through bling_render_pass (latency of that FIFO from the same
+    arrivals, each job's service time measured)."""
+    import threading
+
+    import torch
+
+    from bling_gb300 import scene as S
+    from bling_gb300.api import Context, Server
+    ctx = Context(device=0)
+    t0 = time.perf_counter()
+    scenes = S.serving_scenes()
+    gs = [ctx.scene(s) for s in scenes]
+    build_s = time.perf_counter() - t0
+    jobs = S.serving_jobs(n=args.serving_jobs)
+    cams = [scenes[j.scene].camera_for(j.params.width, j.params.height) for j in jobs]
+    samples = [_extent_samples(j.params) for j in jobs]
+    # plain: each job alone, in arrival order
+    warm = ctx.film(64, 64)
+    gs[0].render_pass(warm, S.render_params(64, 64, (1, 1)), 0, camera=scenes[0].camera_for(64, 64))
+    service, refs = [], []
+    for j, cam in zip(jobs, cams):
+        f = ctx.film(j.params.width, j.params.height)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        gs[j.scene].render_pass(f, j.params, j.pass_index, camera=cam)
+        service.append(time.perf_counter() - t)
+        refs.append(f.read())
+        f.close()
+    plain_lat, free_at = [], 0.0
+    for j, s in zip(jobs, service):
+        start = max(j.arrival, free_at)
+        free_at = start + s
+        plain_lat.append(free_at - j.arrival)
+    # served: arrivals replayed in real time from a producer thread
+    srv = Server(ctx, hbm_budget_bytes=40 << 30, iters_per_step=args.serving_iters)
+    w = srv.submit(gs[0], S.render_params(64, 64, (1, 1)), 0, camera=scenes[0].camera_for(64, 64))
+    srv.wait(w)  # warm-up (graph capture)
+    tickets = [None] * len(jobs)
+
+    def producer():
+        t_start = time.perf_counter()
+        for k, (j, cam) in enumerate(zip(jobs, cams)):
+            d = t_start + j.arrival - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            tickets[k] = srv.submit(gs[j.scene], j.params, j.pass_index, camera=cam)
+
+    th = threading.Thread(target=producer)
+    th.start()
+    th.join()
+    res = [srv.wait(t) for t in tickets]
+    st = srv.stats()
+    srv.close()
+    first = min(r[1]["submitted"] for r in res)
+    last = max(r[1]["finished"] for r in res)
+    lat = [r[1]["finished"] - r[1]["submitted"] for r in res]
+    equal = all(_films_equal(r[0], ref) for r, ref in zip(res, refs))
+    tot = sum(samples)
+    plain_span = max(j.arrival for j in jobs) + 0.0
+    plain_make = max(plain_lat[k] + jobs[k].arrival for k in range(len(jobs)))
+    ctx.close()
+    return {
+        "scenes": len(scenes), "triangles": sum(s.n_triangles for s in scenes) +
+        sum(len(s.shapes) for s in scenes), "scene_build_s": round(build_s, 2),
+        "jobs": len(jobs), "arrival_rate_per_s": 200, "arrivals_span_s": round(plain_span, 3),
+        "path_samples": tot,
+        "served": {"p50_latency_s": round(_pct(lat, 50), 4), "p99_latency_s": round(_pct(lat, 99), 4),
+                   "makespan_s": round(last - first, 3),
+                   "path_samples_per_s": round(tot / (last - first), 1),
+                   "peak_bytes_in_use": st["peak_bytes_in_use"], "iterations": st["iterations"],
+                   "iters_per_step": args.serving_iters},
+        "plain_per_job": {"p50_latency_s": round(_pct(plain_lat, 50), 4),
+                          "p99_latency_s": round(_pct(plain_lat, 99), 4),
+                          "makespan_s": round(plain_make, 3),
+                          "path_samples_per_s": round(tot / sum(service), 1)},
+        "speedup": round((tot / (last - first)) / (tot / sum(service)), 3),
+        "equal_images": equal,
+    }
+
+
 def run_render_profile(args):
     """A small render of the large-mesh workload for profiling (full
     geometry, reduced image): one warm-up pass and `--steps` timed passes."""
@@ -388,6 +565,11 @@ def run_ours(args):
     render = None
     if not args.no_render and rank == 0:
         render = measure_render(ctx, stream, args)
+    batched = served = None
+    if not args.no_batch and rank == 0:
+        batched = measure_batched(args)
+    if not args.no_serving and rank == 0:
+        served = measure_serving(args)
 
     # ---- roofline of the dominant kernel (closest hit)
     hbm_peak, peak_kind = peaks()
@@ -430,6 +612,8 @@ def run_ours(args):
             "bvh_build_ms": round(st["bvh_build_ms"], 1),
             "bvh_nodes": st["bvh_nodes"],
             "path_integrator": render,
+            "batched_wavefront": batched,
+            "serving": served,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -471,6 +655,12 @@ def main():
     ap.add_argument("--no-render", action="store_true", help="skip the path-integrator workloads")
     ap.add_argument("--no-heightfield", action="store_true")
     ap.add_argument("--wide-bvh", action="store_true", help="8-wide quantised BVH layout")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched workload")
+    ap.add_argument("--batch-instances", type=int, default=64)
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
+    ap.add_argument("--serving-jobs", type=int, default=32)
+    ap.add_argument("--serving-iters", type=int, default=4,
+                    help="wavefront iterations between admission rounds")
     ap.add_argument("--render-size", type=int, nargs=3, metavar=("W", "H", "STRATA"),
                     help="only render the large-mesh workload at W x H, STRATA^2 spp (profiling)")
     ap.add_argument("--rays", type=int, default=N_RAYS,

@@ -86,6 +86,24 @@ class Stats(C.Structure):
                 ("device_bytes", C.c_uint64)]
 
 
+BATCH_PLAIN_LAUNCHES, BATCH_GRAPH, BATCH_DEVICE_LOOP = 0, 1, 2
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("slots", C.c_int64), ("block_size", C.c_int32), ("max_jobs", C.c_int32),
+                ("sort_rays", C.c_int32), ("graph_mode", C.c_int32),
+                ("iters_per_launch", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("rays_closest", C.c_uint64), ("rays_any", C.c_uint64),
+                ("path_samples", C.c_uint64), ("nonfinite_drops", C.c_uint64),
+                ("degenerate_rays", C.c_uint64), ("iterations", C.c_uint64),
+                ("samples_submitted", C.c_uint64), ("samples_started", C.c_uint64),
+                ("jobs_submitted", C.c_int64), ("jobs_done", C.c_int64),
+                ("jobs_active", C.c_int64), ("device_bytes", C.c_uint64)]
+
+
 def fptr(a):
     """float* of a C-contiguous float32 numpy array (or NULL for None)."""
     if a is None:
@@ -99,3 +117,24 @@ def iptr(a):
         return C.POINTER(C.c_int32)()
     assert a.dtype.name == "int32" and a.flags.c_contiguous
     return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class ServerOpts(C.Structure):
+    _fields_ = [("batch", BatchOpts), ("hbm_budget_bytes", C.c_uint64),
+                ("iters_per_step", C.c_int32), ("reserved", C.c_int32)]
+
+
+class JobTimes(C.Structure):
+    _fields_ = [("submitted", C.c_double), ("admitted", C.c_double), ("finished", C.c_double),
+                ("samples", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("jobs_submitted", C.c_int64), ("jobs_admitted", C.c_int64),
+                ("jobs_done", C.c_int64), ("jobs_failed", C.c_int64),
+                ("jobs_running", C.c_int64), ("jobs_pending", C.c_int64),
+                ("samples_done", C.c_uint64), ("rays_closest", C.c_uint64),
+                ("rays_any", C.c_uint64), ("iterations", C.c_uint64),
+                ("budget_bytes", C.c_uint64), ("bytes_in_use", C.c_uint64),
+                ("peak_bytes_in_use", C.c_uint64)]
+FILM_FP64 = 1

@@ -61,17 +61,46 @@ def lib():
     L.bling_trace_counts.argtypes = [vp, P(C.c_float), C.c_size_t, P(C.c_uint64), P(C.c_uint64)]
     L.bling_trace_counts.restype = C.c_int
     L.bling_film_create.argtypes = [vp, C.c_int32, C.c_int32, P(vp)]
+    L.bling_film_create_ex.argtypes = [vp, C.c_int32, C.c_int32, C.c_uint32, P(vp)]
+    L.bling_film_fold.argtypes = [vp]
+    L.bling_film_read_f64.argtypes = [vp, P(C.c_double)]
+    for fn in ("bling_film_create_ex", "bling_film_fold", "bling_film_read_f64"):
+        getattr(L, fn).restype = C.c_int
     L.bling_film_destroy.argtypes = [vp]
     L.bling_film_clear.argtypes = [vp]
     L.bling_film_read.argtypes = [vp, P(C.c_float)]
     L.bling_film_resolve.argtypes = [vp, P(C.c_float)]
     L.bling_render_pass.argtypes = [vp, vp, P(abi.RenderParams), C.c_uint64]
+    L.bling_render_pass_camera.argtypes = [vp, vp, P(abi.RenderParams), P(abi.CameraDesc),
+                                           C.c_uint64]
+    L.bling_render_pass_camera.restype = C.c_int
     L.bling_rgb_to_spectrum.argtypes = [C.c_int32, C.c_float, C.c_float, C.c_float, P(C.c_float)]
     L.bling_spectrum_to_xyz.argtypes = [P(C.c_float), P(C.c_float)]
+    L.bling_batch_create.argtypes = [vp, P(abi.BatchOpts), P(vp)]
+    L.bling_batch_destroy.argtypes = [vp]
+    L.bling_batch_submit.argtypes = [vp, vp, vp, P(abi.RenderParams), P(abi.CameraDesc), C.c_uint64,
+                                     P(C.c_int64)]
+    L.bling_batch_step.argtypes = [vp, C.c_int32]
+    L.bling_batch_run.argtypes = [vp]
+    L.bling_batch_job_status.argtypes = [vp, C.c_int64, P(C.c_uint64), P(C.c_uint64)]
+    L.bling_batch_stats_get.argtypes = [vp, P(abi.BatchStats)]
+    L.bling_server_create.argtypes = [vp, P(abi.ServerOpts), P(vp)]
+    L.bling_server_destroy.argtypes = [vp]
+    L.bling_server_submit.argtypes = [vp, vp, P(abi.RenderParams), P(abi.CameraDesc), C.c_uint64,
+                                      P(C.c_int64)]
+    L.bling_server_wait.argtypes = [vp, C.c_int64, C.c_int32, P(C.c_float), P(abi.JobTimes)]
+    L.bling_server_stats_get.argtypes = [vp, P(abi.ServerStats)]
+    L.bling_server_last_error.argtypes = [vp]
+    L.bling_server_last_error.restype = C.c_char_p
+    for fn in ("bling_server_create", "bling_server_submit", "bling_server_wait",
+               "bling_server_stats_get"):
+        getattr(L, fn).restype = C.c_int
     for fn in ("bling_ctx_create", "bling_ctx_set_stream", "bling_scene_create", "bling_scene_stats",
                "bling_trace_closest", "bling_trace_any", "bling_trace_closest_device",
                "bling_trace_any_device", "bling_film_create", "bling_film_clear", "bling_film_read",
-               "bling_film_resolve", "bling_render_pass"):
+               "bling_film_resolve", "bling_render_pass", "bling_batch_create", "bling_batch_submit",
+               "bling_batch_step", "bling_batch_run", "bling_batch_job_status",
+               "bling_batch_stats_get"):
         getattr(L, fn).restype = C.c_int
     _lib = L
     return L
@@ -124,8 +153,8 @@ class Context:
     def scene(self, scene) -> "GpuScene":
         return GpuScene(self, scene)
 
-    def film(self, width: int, height: int) -> "Film":
-        return Film(self, width, height)
+    def film(self, width: int, height: int, fp64: bool = False) -> "Film":
+        return Film(self, width, height, fp64)
 
 
 class GpuScene:
@@ -195,18 +224,33 @@ class GpuScene:
         self.ctx.check(lib().bling_trace_any_device(self.h, C.c_void_p(d_rays.data_ptr()), n,
                                                     C.c_void_p(d_hit.data_ptr())))
 
-    def render_pass(self, film: "Film", params, pass_index: int = 0):
-        self.ctx.check(lib().bling_render_pass(self.h, film.h, C.byref(params), pass_index))
+    def render_pass(self, film: "Film", params, pass_index: int = 0, camera=None):
+        """one pass into the film; camera: an abi.CameraDesc (None: the scene's)"""
+        if camera is None:
+            self.ctx.check(lib().bling_render_pass(self.h, film.h, C.byref(params), pass_index))
+        else:
+            self.ctx.check(lib().bling_render_pass_camera(self.h, film.h, C.byref(params),
+                                                          C.byref(camera), pass_index))
 
 
 class Film:
     """A (weight, X, Y, Z) film resident on the device (Image.hs:64-82)."""
 
-    def __init__(self, ctx: Context, width: int, height: int):
-        self.ctx, self.width, self.height = ctx, width, height
+    def __init__(self, ctx: Context, width: int, height: int, fp64: bool = False):
+        self.ctx, self.width, self.height, self.fp64 = ctx, width, height, fp64
         self.h = C.c_void_p()
-        ctx.check(lib().bling_film_create(ctx.h, width, height, C.byref(self.h)))
+        ctx.check(lib().bling_film_create_ex(ctx.h, width, height,
+                                             abi.FILM_FP64 if fp64 else 0, C.byref(self.h)))
         ctx._children.add(self)
+
+    def fold(self):
+        """adds the FP32 samples into the FP64 totals (BLING_FILM_FP64 films)"""
+        self.ctx.check(lib().bling_film_fold(self.h))
+
+    def read_f64(self) -> np.ndarray:
+        out = np.empty((self.height, self.width, 4), np.float64)
+        self.ctx.check(lib().bling_film_read_f64(self.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
 
     def close(self):
         if getattr(self, "h", None):
@@ -231,6 +275,123 @@ class Film:
         out = np.empty((self.height, self.width, 3), np.float32)
         self.ctx.check(lib().bling_film_resolve(self.h, _fp(out)))
         return out
+
+
+class Batch:
+    """Many render jobs in one persistent wavefront (``bling_batch``).
+
+    A job is one pass (``GpuScene.render_pass``) of a scene into a film; jobs
+    may be submitted between steps while others are in flight."""
+
+    def __init__(self, ctx: Context, slots: int = 0, block_size: int = 0, max_jobs: int = 0,
+                 sort_rays: bool = False, graph_mode: int = abi.BATCH_GRAPH,
+                 iters_per_launch: int = 0):
+        self.ctx = ctx
+        o = abi.BatchOpts()
+        o.slots, o.block_size, o.max_jobs = slots, block_size, max_jobs
+        o.sort_rays, o.graph_mode, o.iters_per_launch = int(sort_rays), graph_mode, iters_per_launch
+        self.h = C.c_void_p()
+        ctx.check(lib().bling_batch_create(ctx.h, C.byref(o), C.byref(self.h)))
+        ctx._children.add(self)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().bling_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    def submit(self, scene: GpuScene, film: Film, params, pass_index: int = 0,
+               camera=None) -> int:
+        """camera: an abi.CameraDesc for this job (None: the scene's camera)."""
+        job = C.c_int64()
+        cam = C.byref(camera) if camera is not None else None
+        self.ctx.check(lib().bling_batch_submit(self.h, scene.h, film.h, C.byref(params), cam,
+                                                pass_index, C.byref(job)))
+        return job.value
+
+    def step(self, iterations: int = 1):
+        self.ctx.check(lib().bling_batch_step(self.h, iterations))
+
+    def run(self):
+        self.ctx.check(lib().bling_batch_run(self.h))
+
+    def status(self, job: int) -> tuple[int, int]:
+        done, total = C.c_uint64(), C.c_uint64()
+        self.ctx.check(lib().bling_batch_job_status(self.h, job, C.byref(done), C.byref(total)))
+        return done.value, total.value
+
+    def done(self, job: int) -> bool:
+        d, t = self.status(job)
+        return d == t
+
+    def stats(self) -> dict:
+        s = abi.BatchStats()
+        self.ctx.check(lib().bling_batch_stats_get(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in abi.BatchStats._fields_}
+
+
+class Server:
+    """Continuous batching of render jobs (``bling_server``): submit from any
+    thread, wait for the film.  The context must outlive the server."""
+
+    def __init__(self, ctx: Context, hbm_budget_bytes: int = 0, iters_per_step: int = 0,
+                 slots: int = 0, block_size: int = 0, max_jobs: int = 0, sort_rays: bool = False,
+                 graph_mode: int = 0, iters_per_launch: int = 0):
+        self.ctx = ctx
+        o = abi.ServerOpts()
+        o.batch.slots, o.batch.block_size, o.batch.max_jobs = slots, block_size, max_jobs
+        o.batch.sort_rays, o.batch.graph_mode = int(sort_rays), graph_mode
+        o.batch.iters_per_launch = iters_per_launch
+        o.hbm_budget_bytes, o.iters_per_step = hbm_budget_bytes, iters_per_step
+        self.h = C.c_void_p()
+        ctx.check(lib().bling_server_create(ctx.h, C.byref(o), C.byref(self.h)))
+        ctx._children.add(self)
+        self._sizes = {}
+
+    def _check(self, rc):
+        if rc != 0:
+            raise BlingError(rc, lib().bling_server_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().bling_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    def submit(self, scene: GpuScene, params, pass_index: int = 0, camera=None) -> int:
+        t = C.c_int64()
+        cam = C.byref(camera) if camera is not None else None
+        self._check(lib().bling_server_submit(self.h, scene.h, C.byref(params), cam, pass_index,
+                                              C.byref(t)))
+        self._sizes[t.value] = (params.height, params.width)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1, want_film: bool = True):
+        """(film (h, w, 4) float32 or None, times dict)"""
+        size = self._sizes.get(ticket)  # None: not submitted here; the library reports it
+        film = np.empty((*size, 4), np.float32) if want_film and size else None
+        times = abi.JobTimes()
+        rc = lib().bling_server_wait(self.h, ticket, timeout_ms,
+                                     _fp(film) if film is not None else None, C.byref(times))
+        if rc != abi.BLING_ERR_TIMEOUT:
+            self._sizes.pop(ticket, None)
+        self._check(rc)
+        return film, {k: getattr(times, k) for k, _ in abi.JobTimes._fields_}
+
+    def stats(self) -> dict:
+        s = abi.ServerStats()
+        self._check(lib().bling_server_stats_get(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in abi.ServerStats._fields_}
 
 
 # ---------------------------------------------------------------- Renderer

@@ -21,7 +21,8 @@ BUILD = PKG / "_build"
 LIB = PKG / "libbling_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SRCS = ["api.cu", "kernels_trace.cu", "integrator.cu", "scene_upload.cu"]
+CU_SRCS = ["api.cu", "kernels_trace.cu", "integrator.cu", "scene_upload.cu", "batch.cu",
+           "server.cu"]
 CPP_SRCS = ["bvh.cpp"]
 HEADERS = ["dmath.cuh", "dshape.cuh", "trace.cuh", "internal.h", "integrator.h", "bvh.h",
            "spectrum_tables.h", "integrator_device.cuh", "filter_host.h"]

@@ -1,5 +1,6 @@
 // C ABI of the GB300 path-tracing core (include/bling_gpu.h).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -11,47 +12,16 @@
 #include <vector>
 
 #include "../../include/bling_gpu.h"
+#include "batch.h"
 #include "bvh.h"
+#include "handles.h"
 #include "integrator.h"
 #include "internal.h"
 #include "spectrum_tables.h"
 
 using namespace bgpu;
 
-struct bling_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;      // where work is enqueued
-  cudaStream_t own_stream = nullptr;  // the context's own stream
-  std::mutex mu;
-  std::string err;
-  bling_opts opts{};
-  // grow-only staging buffers for host-buffer queries
-  void* d_scratch = nullptr;
-  size_t scratch_bytes = 0;
-  // next-ray counter of the persistent traversal kernels (calls are serialised)
-  unsigned long long* d_counter = nullptr;
-  IntegratorWorkspace ws;
-};
-
-struct bling_scene {
-  bling_ctx* ctx = nullptr;
-  DevAccel accel{};
-  float4* d_nodes = nullptr;
-  uint4* d_nodes8 = nullptr;
-  float4* d_slots = nullptr;
-  DShape* d_shapes = nullptr;
-  DevShading shading{};
-  std::vector<void*> owned;  // other device allocations
-  bling_stats stats{};
-  int64_t n_nodes = 0, n_slots = 0;
-  int32_t root_ref = 0;
-};
-
-struct bling_film {
-  bling_ctx* ctx = nullptr;
-  int32_t width = 0, height = 0;
-  float* d_film = nullptr;  // width*height*4
-};
+static std::atomic<uint64_t> g_scene_serial{0};
 
 namespace {
 
@@ -162,7 +132,43 @@ void shape_world_bounds(const bling_shape_desc& s, float lo[3], float hi[3]) {
   }
 }
 
+// sampler/integrator/filter parameters of a pass (the checks of bling_render_pass)
+int check_params(bling_ctx* c, const bling_render_params* p) {
+  if (p->width <= 0 || p->height <= 0)
+    return set_err(c, BLING_ERR_INVALID_ARG, "invalid image size %dx%d", p->width, p->height);
+  if (p->strata_x <= 0 || p->strata_y <= 0 || p->max_depth < 0 || p->sample_depth < 0 ||
+      p->strata_x * p->strata_y > 4096)
+    return set_err(c, BLING_ERR_INVALID_ARG, "invalid sampler/integrator parameters");
+  if (p->filter_kind < BLING_FILTER_BOX || p->filter_kind > BLING_FILTER_TRIANGLE)
+    return set_err(c, BLING_ERR_INVALID_ARG, "unknown filter kind %d", p->filter_kind);
+  return BLING_OK;
+}
+
 }  // namespace
+
+int bgpu::check_render_params(bling_ctx* c, const bling_render_params* p) {
+  return check_params(c, p);
+}
+
+// acc += pass; pass = 0 (the FP64 accumulator of a BLING_FILM_FP64 film)
+__global__ void k_film_fold(float* __restrict__ pass, double* __restrict__ acc, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    float v = pass[i];
+    if (v != 0.0f) {
+      acc[i] += (double)v;
+      pass[i] = 0.0f;
+    }
+  }
+}
+
+static cudaError_t film_fold(bling_film* f, cudaStream_t stream) {
+  if (!f->d_acc) return cudaSuccess;
+  size_t n = (size_t)f->width * f->height * 4;
+  unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
+  k_film_fold<<<grid, 256, 0, stream>>>(f->d_film, f->d_acc, n);
+  return cudaGetLastError();
+}
 
 extern "C" {
 
@@ -353,6 +359,16 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   }
   std::unique_ptr<bling_scene> S(new bling_scene());
   S->ctx = c;
+  S->serial = ++g_scene_serial;
+  for (int k = 0; k < 3; k++) {
+    S->lo[k] = INFINITY;
+    S->hi[k] = -INFINITY;
+  }
+  for (int64_t p = 0; p < n_prims; p++)
+    for (int k = 0; k < 3; k++) {
+      S->lo[k] = std::min(S->lo[k], lo[3 * p + k]);
+      S->hi[k] = std::max(S->hi[k], hi[3 * p + k]);
+    }
   int rc;
   if (wide) {
     if ((rc = upload(c, S->owned, (const uint4*)bo.nodes8.data(), bo.nodes8.size() / 4, &S->d_nodes8)))
@@ -522,8 +538,10 @@ int bling_trace_counts(bling_scene* s, const float* rays, size_t n, uint64_t* no
 }
 
 // ---------------------------------------------------------------- films
-int bling_film_create(bling_ctx* c, int32_t w, int32_t h, bling_film** out) {
-  if (!c || !out || w <= 0 || h <= 0 || (int64_t)w * h > (int64_t(1) << 28)) return BLING_ERR_INVALID_ARG;
+int bling_film_create_ex(bling_ctx* c, int32_t w, int32_t h, uint32_t flags, bling_film** out) {
+  if (!c || !out || w <= 0 || h <= 0 || (int64_t)w * h > (int64_t(1) << 28) ||
+      (flags & ~BLING_FILM_FP64))
+    return BLING_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> g(c->mu);
   *out = nullptr;
   CK(c, cudaSetDevice(c->device));
@@ -533,17 +551,28 @@ int bling_film_create(bling_ctx* c, int32_t w, int32_t h, bling_film** out) {
   f->height = h;
   size_t bytes = (size_t)w * h * 4 * sizeof(float);
   cudaError_t e = cudaMalloc(&f->d_film, bytes);
-  if (e != cudaSuccess)
+  if (e == cudaSuccess && (flags & BLING_FILM_FP64)) {
+    e = cudaMalloc(&f->d_acc, 2 * bytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(f->d_acc, 0, 2 * bytes, c->stream);
+  }
+  if (e != cudaSuccess) {
+    cudaFree(f->d_film);
     return set_err(c, e == cudaErrorMemoryAllocation ? BLING_ERR_OOM : BLING_ERR_CUDA,
                    "film allocation: %s", cudaGetErrorString(e));
+  }
   e = cudaMemsetAsync(f->d_film, 0, bytes, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) {
     cudaFree(f->d_film);
+    cudaFree(f->d_acc);
     return set_err(c, BLING_ERR_CUDA, "film clear: %s", cudaGetErrorString(e));
   }
   *out = f.release();
   return BLING_OK;
+}
+
+int bling_film_create(bling_ctx* c, int32_t w, int32_t h, bling_film** out) {
+  return bling_film_create_ex(c, w, h, 0, out);
 }
 
 void bling_film_destroy(bling_film* f) {
@@ -553,8 +582,32 @@ void bling_film_destroy(bling_film* f) {
     cudaSetDevice(f->ctx->device);
     cudaStreamSynchronize(f->ctx->stream);
     cudaFree(f->d_film);
+    cudaFree(f->d_acc);
   }
   delete f;
+}
+
+int bling_film_fold(bling_film* f) {
+  if (!f) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = f->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, film_fold(f, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return BLING_OK;
+}
+
+int bling_film_read_f64(bling_film* f, double* host) {
+  if (!f || !host) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = f->ctx;
+  if (!f->d_acc) return set_err(c, BLING_ERR_STATE, "film has no FP64 accumulator");
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, film_fold(f, c->stream));
+  CK(c, cudaMemcpyAsync(host, f->d_acc, (size_t)f->width * f->height * 4 * sizeof(double),
+                        cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return BLING_OK;
 }
 
 int bling_film_clear(bling_film* f) {
@@ -563,6 +616,8 @@ int bling_film_clear(bling_film* f) {
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
   CK(c, cudaMemsetAsync(f->d_film, 0, (size_t)f->width * f->height * 16, c->stream));
+  if (f->d_acc)
+    CK(c, cudaMemsetAsync(f->d_acc, 0, (size_t)f->width * f->height * 32, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   return BLING_OK;
 }
@@ -572,8 +627,18 @@ int bling_film_read(bling_film* f, float* host) {
   bling_ctx* c = f->ctx;
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
-  CK(c, cudaMemcpyAsync(host, f->d_film, (size_t)f->width * f->height * 16, cudaMemcpyDeviceToHost,
-                        c->stream));
+  size_t n = (size_t)f->width * f->height * 4;
+  if (f->d_acc) {
+    // the FP64 totals, rounded once to float
+    CK(c, film_fold(f, c->stream));
+    std::vector<double> acc(n);
+    CK(c, cudaMemcpyAsync(acc.data(), f->d_acc, n * sizeof(double), cudaMemcpyDeviceToHost,
+                          c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; i++) host[i] = (float)acc[i];
+    return BLING_OK;
+  }
+  CK(c, cudaMemcpyAsync(host, f->d_film, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   return BLING_OK;
 }
@@ -607,6 +672,11 @@ int bling_film_resolve(bling_film* f, float* host_rgb) {
 }
 
 int bling_render_pass(bling_scene* s, bling_film* f, const bling_render_params* p, uint64_t pass) {
+  return bling_render_pass_camera(s, f, p, nullptr, pass);
+}
+
+int bling_render_pass_camera(bling_scene* s, bling_film* f, const bling_render_params* p,
+                             const bling_camera_desc* camera, uint64_t pass) {
   if (!s || !f || !p) return BLING_ERR_INVALID_ARG;
   bling_ctx* c = s->ctx;
   if (f->ctx != c) return set_err(c, BLING_ERR_INVALID_ARG, "film and scene belong to different contexts");
@@ -622,9 +692,15 @@ int bling_render_pass(bling_scene* s, bling_film* f, const bling_render_params* 
   CK(c, cudaSetDevice(c->device));
   PassResult res{};
   auto t0 = std::chrono::steady_clock::now();
-  int rc = integrator_render_pass(c->stream, s->accel, s->shading, *p, pass, f->d_film, f->width,
+  DevShading sh = s->shading;
+  if (camera) sh.camera = *camera;
+  int rc = integrator_render_pass(c->stream, s->accel, sh, *p, pass, f->d_film, f->width,
                                   f->height, c->ws, res, c->err);
   if (rc) return rc;
+  if (f->d_acc) {  // the pass's FP32 sums into the FP64 totals
+    CK(c, film_fold(f, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+  }
   auto t1 = std::chrono::steady_clock::now();
   s->stats.last_pass_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   s->stats.rays_closest += res.rays_closest;
@@ -663,6 +739,107 @@ int bling_render_pass_noalloc(bling_scene* s, const bling_render_params* p, uint
   s->stats.path_samples += res.path_samples;
   s->stats.nonfinite_drops += res.nonfinite;
   s->stats.degenerate_rays += res.degenerate;
+  return BLING_OK;
+}
+
+// ---------------------------------------------------------------- batched jobs
+int bling_batch_create(bling_ctx* c, const bling_batch_opts* o, bling_batch** out) {
+  if (!c || !out) return BLING_ERR_INVALID_ARG;
+  *out = nullptr;
+  std::lock_guard<std::mutex> g(c->mu);
+  if (!c->stream) return set_err(c, BLING_ERR_STATE, "context has no device");
+  CK(c, cudaSetDevice(c->device));
+  BatchConfig cfg;
+  if (o) {
+    if (o->slots) cfg.slots = o->slots;
+    if (o->block_size) cfg.block = o->block_size;
+    if (o->max_jobs) cfg.max_jobs = o->max_jobs;
+    cfg.sort_rays = o->sort_rays != 0;
+    cfg.graph_mode = o->graph_mode;
+    if (o->iters_per_launch) cfg.iters_per_launch = o->iters_per_launch;
+  } else {
+    cfg.graph_mode = BLING_BATCH_PLAIN_LAUNCHES;
+  }
+  BatchEngine* e = nullptr;
+  int rc = batch_create(c->device, c->stream, cfg, &e, c->err);
+  if (rc) return rc;
+  bling_batch* b = new bling_batch();
+  b->ctx = c;
+  b->eng = e;
+  *out = b;
+  return BLING_OK;
+}
+
+void bling_batch_destroy(bling_batch* b) {
+  if (!b) return;
+  {
+    std::lock_guard<std::mutex> g(b->ctx->mu);
+    cudaSetDevice(b->ctx->device);
+    batch_destroy(b->eng);
+  }
+  delete b;
+}
+
+int bling_batch_submit(bling_batch* b, bling_scene* s, bling_film* f, const bling_render_params* p,
+                       const bling_camera_desc* camera, uint64_t pass, int64_t* job_id) {
+  if (!b || !s || !f || !p || !job_id) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = b->ctx;
+  if (s->ctx != c || f->ctx != c)
+    return set_err(c, BLING_ERR_INVALID_ARG, "scene, film and batch belong to different contexts");
+  if (p->width != f->width || p->height != f->height)
+    return set_err(c, BLING_ERR_INVALID_ARG, "render size %dx%d does not match film %dx%d", p->width,
+                   p->height, f->width, f->height);
+  int rc = check_params(c, p);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  int idx = 0;
+  rc = batch_scene(b->eng, s->serial, s->accel, s->shading, s->lo, s->hi, idx, c->err);
+  if (rc) return rc;
+  const bling_camera_desc& cam = camera ? *camera : s->shading.camera;
+  return batch_submit(b->eng, idx, cam, f->d_film, f->width, f->height, *p, pass, *job_id, c->err);
+}
+
+int bling_batch_step(bling_batch* b, int32_t iterations) {
+  if (!b) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = b->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  return batch_step(b->eng, iterations, c->err);
+}
+
+int bling_batch_run(bling_batch* b) {
+  if (!b) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = b->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  return batch_run(b->eng, c->err);
+}
+
+int bling_batch_job_status(bling_batch* b, int64_t job_id, uint64_t* done, uint64_t* total) {
+  if (!b || !done || !total) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = b->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  return batch_job_status(b->eng, job_id, *done, *total, c->err);
+}
+
+int bling_batch_stats_get(bling_batch* b, bling_batch_stats* out) {
+  if (!b || !out) return BLING_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> g(b->ctx->mu);
+  BatchStats st;
+  batch_stats(b->eng, st);
+  out->rays_closest = st.rays_closest;
+  out->rays_any = st.rays_any;
+  out->path_samples = st.path_samples;
+  out->nonfinite_drops = st.nonfinite;
+  out->degenerate_rays = st.degenerate;
+  out->iterations = st.iterations;
+  out->samples_submitted = st.samples_submitted;
+  out->samples_started = st.samples_started;
+  out->jobs_submitted = st.jobs_submitted;
+  out->jobs_done = st.jobs_done;
+  out->jobs_active = st.jobs_active;
+  out->device_bytes = (uint64_t)st.device_bytes;
   return BLING_OK;
 }
 

@@ -30,168 +30,30 @@
 #include <vector>
 
 #include "filter_host.h"
-#include "integrator_device.cuh"
+#include "wavefront.cuh"
 
 namespace bgpu {
 
-// ------------------------------------------------------------------ slot state
-enum : int { VF_SHADOW = 1, VF_MIS = 2, VF_CONT = 4 };
-
-struct Slots {
-  size_t cap;
-  float* T;          // 16 x cap
-  float* L;          // 16 x cap
-  float* ray;        // 7 x cap: o, d, tmin (sign bit of tmin: the previous bounce was specular)
-  float* hit_t;      // cap
-  int32_t* hit_prim; // cap
-  float* hit_b;      // 2 x cap
-  // the current vertex, deferred until its shadow and MIS rays are traced
-  float* intl;       // 16 x cap: emission seen on a specular path
-  float* ls;         // 16 x cap: light-sample term before visibility
-  float* bsf;        // 16 x cap: MIS BSDF sample throughput
-  float* fc;         // 16 x cap: continuation BSDF sample throughput
-  float* bsw;        // cap: MIS weight of the BSDF sample
-  float* invpc;      // cap: 1 / continuation probability
-  int32_t* vflags;   // cap: VF_* | light index << 8
-  float* sray;       // 8 x cap: shadow ray o, d, tmin, tmax
-  int32_t* svis;     // cap: shadow ray unoccluded
-  float* mray;       // 7 x cap: MIS ray o, d, tmin
-  float* mhit_t;     // cap
-  int32_t* mhit_prim;// cap
-  float* mhit_b;     // 2 x cap
-};
-
-struct Queues {
-  int32_t* live[2];  // paths to trace this bounce / next bounce
-  int32_t* shadow;
-  int32_t* mis;
-  int32_t* resolve;
-};
-
-// counters (unsigned long long): queue sizes and statistics
-enum : int {
-  C_LIVE0 = 0, C_LIVE1 = 1, C_CLOSEST = 2, C_ANY = 3, C_NONFINITE = 4, C_NEXT_TRACE = 5,
-  C_SHADOW = 6, C_MIS = 7, C_RESOLVE = 8, C_NEXT_SHADOW = 9, C_NEXT_MIS = 10, C_DEGENERATE = 11,
-  C_COUNT = 16
-};
-
-constexpr size_t kSlotWords = 16 * 6 + 7 + 4 + 3 + 8 + 1 + 7 + 4;  // per slot, 4-byte words
-constexpr size_t kQueueWords = 5;
-constexpr size_t kCounterBytes = 256;
-
+// lays slots, queues and counters out in one buffer of slotBytes(cap) bytes
 static size_t slotBytes(size_t cap) { return kCounterBytes + (kSlotWords + kQueueWords) * 4 * cap; }
 
-// lays slots, queues and counters out in one buffer of slotBytes(cap) bytes
 static void carve(unsigned char* base, size_t cap, Slots& st, Queues& q,
                   unsigned long long*& counters) {
   counters = (unsigned long long*)base;
   float* w = (float*)(base + kCounterBytes);
-  auto take = [&](size_t words) {
-    float* p = w;
-    w += words * cap;
-    return p;
-  };
-  st.cap = cap;
-  st.T = take(16);
-  st.L = take(16);
-  st.ray = take(7);
-  st.hit_t = take(1);
-  st.hit_prim = (int32_t*)take(1);
-  st.hit_b = take(2);
-  st.intl = take(16);
-  st.ls = take(16);
-  st.bsf = take(16);
-  st.fc = take(16);
-  st.bsw = take(1);
-  st.invpc = take(1);
-  st.vflags = (int32_t*)take(1);
-  st.sray = take(8);
-  st.svis = (int32_t*)take(1);
-  st.mray = take(7);
-  st.mhit_t = take(1);
-  st.mhit_prim = (int32_t*)take(1);
-  st.mhit_b = take(2);
-  q.live[0] = (int32_t*)take(1);
-  q.live[1] = (int32_t*)take(1);
-  q.shadow = (int32_t*)take(1);
-  q.mis = (int32_t*)take(1);
-  q.resolve = (int32_t*)take(1);
+  carveSlots(w, cap, st);
+  int32_t* qw = (int32_t*)w;
+  q.live[0] = qw;
+  q.live[1] = qw + cap;
+  q.shadow = qw + 2 * cap;
+  q.mis = qw + 3 * cap;
+  q.resolve = qw + 4 * cap;
 }
 
-__device__ __forceinline__ void decodeSample(const PassParams& P, uint64_t g, int& ix, int& iy,
-                                             uint32_t& n) {
-  uint64_t pix = g / (uint64_t)P.spp;
-  n = (uint32_t)(g % (uint64_t)P.spp);
-  ix = P.x0 + (int)(pix % (uint64_t)P.nx);
-  iy = P.y0 + (int)(pix / (uint64_t)P.nx);
-}
-__device__ __forceinline__ Sampler mkSampler(const PassParams& P, int ix, int iy, uint32_t n) {
-  Sampler s;
-  s.key = pixelKey(P.seed, P.pass, ix, iy);
-  s.n = n;
-  s.nu = P.nu;
-  s.nv = P.nv;
-  s.n1d = P.n1d;
-  s.n2d = P.n2d;
-  return s;
-}
-__device__ __forceinline__ void pixelSample(const PassParams& P, const Sampler& s, int ix, int iy,
-                                            float& sx, float& sy, float& lu, float& lv) {
-  float ox, oy;
-  strat2D(s, s.n, DIM_PIX_U, DIM_PIX_V, ox, oy);
-  uint32_t N = (uint32_t)P.spp;
-  uint32_t lp = permute(s.n, N, randU32(s.key, 0xffffffffu, DIM_LENS_PERM));
-  strat2D(s, lp, DIM_LENS_U, DIM_LENS_V, lu, lv);
-  sx = (float)ix + ox;
-  sy = (float)iy + oy;
-}
-
-__device__ __forceinline__ Spec loadBands(const float* base, size_t cap, int s) {
-  Spec v;
-#pragma unroll
-  for (int b = 0; b < 16; b++) v.v[b] = base[b * cap + s];
-  return v;
-}
-__device__ __forceinline__ void storeBands(float* base, size_t cap, int s, const Spec& v) {
-#pragma unroll
-  for (int b = 0; b < 16; b++) base[b * cap + s] = v.v[b];
-}
-__device__ __forceinline__ void storeRay(float* base, size_t cap, int s, const Ray& r, bool tmax) {
-  base[s] = r.o.x;
-  base[cap + s] = r.o.y;
-  base[2 * cap + s] = r.o.z;
-  base[3 * cap + s] = r.d.x;
-  base[4 * cap + s] = r.d.y;
-  base[5 * cap + s] = r.d.z;
-  base[6 * cap + s] = r.tmin;
-  if (tmax) base[7 * cap + s] = r.tmax;
-}
-__device__ __forceinline__ Ray loadRay7(const float* base, size_t cap, int s) {
-  return Ray{V3{base[s], base[cap + s], base[2 * cap + s]},
-             V3{base[3 * cap + s], base[4 * cap + s], base[5 * cap + s]}, fabsf(base[6 * cap + s]),
-             INFINITY};
-}
-
-// warp-aggregated append (every lane of the warp calls it)
-__device__ __forceinline__ void queueAppend(bool live, int slot, int32_t* __restrict__ queue,
-                                            unsigned long long* count) {
-  const unsigned mask = 0xffffffffu;
-  __syncwarp();
-  unsigned ballot = __ballot_sync(mask, live);
-  if (!ballot) return;
-  int lane = threadIdx.x & 31;
-  int leader = __ffs(ballot) - 1;
-  unsigned long long base = 0;
-  if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(ballot));
-  base = __shfl_sync(mask, base, leader);
-  if (live) queue[base + __popc(ballot & ((1u << lane) - 1))] = slot;
-}
-
-// intLe (Primitive.hs:68-76) + lEmit (Light.hs:85-96)
-__device__ __forceinline__ Spec intLe(const DevShading& S, const HitGeom& g, V3 wo) {
-  if (g.light_id < 0) return sConst(0);
-  return dot(g.n, wo) > 0 ? sLoad(S.shape_emission + 16 * g.shape) : sConst(0);
-}
+// the pass's filter table, in constant memory
+struct PassFilter {
+  __device__ __forceinline__ float operator()(int i) const { return c_filter[i]; }
+};
 
 // ------------------------------------------------------------------ kernels
 // camera rays (fireRay, Camera.hs:146-164) for samples [chunk_base, chunk_base + count)
@@ -199,23 +61,7 @@ __global__ void k_raygen(PassParams P, bling_camera_desc cam, Slots st, int64_t 
                          int32_t* __restrict__ queue, unsigned long long* counters) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
        i += (int64_t)gridDim.x * blockDim.x) {
-    uint64_t g = P.chunk_base + (uint64_t)i;
-    int ix, iy;
-    uint32_t n;
-    decodeSample(P, g, ix, iy, n);
-    Sampler s = mkSampler(P, ix, iy, n);
-    float sx, sy, lu, lv;
-    pixelSample(P, s, ix, iy, sx, sy, lu, lv);
-    V3 pCamera = transPoint(cam.r2c, V3{sx, sy, 0});
-    Ray ray{V3{0, 0, 0}, normalize(pCamera), 0, INFINITY};
-    if (cam.lens_radius > 0) {
-      float u, v;
-      concentricSampleDisk(lu, lv, u, v);
-      V3 ro{u * cam.lens_radius, v * cam.lens_radius, 0};
-      V3 pFocus = rayAt(ray, cam.focal_distance / ray.d.z);
-      ray = Ray{ro, normalize(pFocus - ro), 0, INFINITY};
-    }
-    ray = transRay(cam.c2w, ray);
+    Ray ray = cameraRay(P, cam, P.chunk_base + (uint64_t)i);
     storeRay(st.ray, st.cap, (int)i, ray, false);
     storeBands(st.T, st.cap, (int)i, sConst(1.0f));
     storeBands(st.L, st.cap, (int)i, sConst(0.0f));
@@ -261,14 +107,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(DevAccel A, Slots st,
                                                       unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_SHADOW];
   traceWarpPersistent<true, WIDE, false>(
-      A, n, counters + C_NEXT_SHADOW,
-      [&](int64_t q) {
-        int s = queue[q];
-        size_t c = st.cap;
-        return Ray{V3{st.sray[s], st.sray[c + s], st.sray[2 * c + s]},
-                   V3{st.sray[3 * c + s], st.sray[4 * c + s], st.sray[5 * c + s]},
-                   st.sray[6 * c + s], st.sray[7 * c + s]};
-      },
+      A, n, counters + C_NEXT_SHADOW, [&](int64_t q) { return loadShadowRay(st, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         st.svis[queue[q]] = res.hit ? 0 : 1;
         if (res.prim == kDegenerateRay) atomicAdd(counters + C_DEGENERATE, 1ull);
@@ -294,19 +133,6 @@ __global__ void __launch_bounds__(128) k_trace_mis(DevAccel A, Slots st,
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_CLOSEST, (unsigned long long)n);
 }
 
-// the splat of a finished path (the raster position is recomputed from the sampler)
-__device__ __forceinline__ void finishPath(float* film, const PassParams& P, int slot,
-                                           const Spec& L, unsigned long long* counters) {
-  uint64_t g = P.chunk_base + (uint64_t)slot;  // slots never move
-  int ix, iy;
-  uint32_t sn;
-  decodeSample(P, g, ix, iy, sn);
-  Sampler smp = mkSampler(P, ix, iy, sn);
-  float sx, sy, lu, lv;
-  pixelSample(P, smp, ix, iy, sx, sy, lu, lv);
-  filmAdd(film, P, ix, iy, sx, sy, L, counters + C_NONFINITE);
-}
-
 // one vertex of every live path, up to its shadow and MIS rays (Path.hs:49-87)
 __global__ void __launch_bounds__(128) k_shade(DevAccel A, DevShading S, PassParams P, Slots st,
                                                Queues Q, int depth, int live_in,
@@ -317,106 +143,18 @@ __global__ void __launch_bounds__(128) k_shade(DevAccel A, DevShading S, PassPar
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;  // whole warps stay together for the appends
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
-    bool want_shadow = false, want_mis = false, want_resolve = false;
+    VertexOut o{false, false, false};
     int s = 0;
     if (q < n) {
       s = qin[q];
-      uint64_t g = P.chunk_base + (uint64_t)s;
-      int ix, iy;
-      uint32_t sn;
-      decodeSample(P, g, ix, iy, sn);
-      Sampler smp = mkSampler(P, ix, iy, sn);
-      size_t c = st.cap;
-      Ray ray = loadRay7(st.ray, c, s);
-      bool specular = depth == 0 || signbit(st.ray[6 * c + s]);
-      int prim = st.hit_prim[s];
-      if (prim == kDegenerateRay) {
-        // a NaN ray: the reference's sample ends NaN and is dropped by the film
-        atomicAdd(counters + C_DEGENERATE, 1ull);
-        finishPath(film, P, s, sConst(NAN), counters);
-      } else if (prim < 0 || depth == P.max_depth) {
-        Spec Lr = loadBands(st.L, c, s);
-        if (prim < 0 && specular) {  // nothing hit after a specular bounce: l + t * sum le
-          Spec sum = sConst(0);
-          for (int k = 0; k < S.n_lights; k++) sum = sum + lightLe(S.lights[k], ray.d);
-          Lr = Lr + loadBands(st.T, c, s) * sum;
-        }
-        finishPath(film, P, s, Lr, counters);
-      } else {
-        float thit = st.hit_t[s], b1 = st.hit_b[2 * s], b2 = st.hit_b[2 * s + 1];
-        float lNumU = rnd1(smp, 1 + 4 * depth);
-        float ld1, ld2;
-        rnd2(smp, 1 + 3 * depth, ld1, ld2);
-        float lBsdfCompU = rnd1(smp, 2 + 4 * depth);
-        float lb1, lb2;
-        rnd2(smp, 2 + 3 * depth, lb1, lb2);
-        HitGeom gm = hitGeometry(A, S, ray, prim, thit, b1, b2);
-        V3 rd = ray.d;
-        storeBands(st.intl, c, s, specular ? intLe(S, gm, rd) : sConst(0));
-        V3 wo = -rd;
-        Bsdf bsdf = materialBsdf(S.materials, gm.material, gm.n, gm.sp, gm.sn, gm.sdpdu);
-        V3 nn = bsdf.cs.n, p = bsdf.p;
-        float eps = gm.eps;
-        int flags = 0;
-        int lc = S.n_lights;
-        int ln = 0;
-        if (lc > 0) {
-          // sampleOneLight (Scene.hs:233-241) -> estimateDirect (Scene.hs:218-222)
-          if (lc > 1) ln = min((int)floorf(lNumU * (float)lc), lc - 1);
-          const DLight& l = S.lights[ln];
-          // sampleLightMis (Scene.hs:184-192), visibility deferred
-          LightSample smpl = lightSample(A, S, l, p, eps, nn, ld1, ld2);
-          if (!(smpl.pdf == 0 || isBlack(smpl.li))) {
-            Spec f = evalBsdf(bsdf, wo, smpl.wi);
-            if (!isBlack(f)) {
-              Spec lsv;
-              if (smpl.delta) {
-                lsv = sScale(f * smpl.li, 1.0f / smpl.pdf);
-              } else {
-                float w = powerHeuristic(smpl.pdf, bsdfPdf(bsdf, wo, smpl.wi));
-                lsv = sScale(f * smpl.li, w / smpl.pdf);
-              }
-              storeBands(st.ls, c, s, lsv);
-              Ray sr = smpl.ray;
-              storeRay(st.sray, c, s, sr, true);
-              flags |= VF_SHADOW;
-            }
-          }
-          // sampleBsdfMis (Scene.hs:194-205), the hit deferred
-          BsdfSample bm = sampleBsdf(bsdf, wo, lBsdfCompU, lb1, lb2);
-          if (!(bm.pdf == 0 || isBlack(bm.f))) {
-            storeBands(st.bsf, c, s, bm.f);
-            st.bsw[s] = powerHeuristic(bm.pdf, lightPdf(A, l, p, bm.wi));
-            storeRay(st.mray, c, s, Ray{p, bm.wi, eps, INFINITY}, false);
-            flags |= VF_MIS;
-          }
-        }
-        // Russian roulette and the continuation (Path.hs:68-87)
-        Spec T = loadBands(st.T, c, s);
-        float pc = depth <= P.rr_depth ? 1.0f : hmin(0.75f, sY(T));
-        float x = rnd1(smp, 3 + 4 * depth);
-        if (!(x > pc)) {
-          float uc = rnd1(smp, 0 + 4 * depth);
-          float ud1, ud2;
-          rnd2(smp, 0 + 3 * depth, ud1, ud2);
-          BsdfSample bc = sampleBsdf(bsdf, wo, uc, ud1, ud2);
-          if (!(bc.pdf == 0 || isBlack(bc.f))) {
-            storeBands(st.fc, c, s, bc.f);
-            st.invpc[s] = 1.0f / pc;
-            bool spec2 = (bc.type & T_SPEC) != 0;
-            storeRay(st.ray, c, s, Ray{p, bc.wi, spec2 ? -eps : eps, INFINITY}, false);
-            flags |= VF_CONT;
-          }
-        }
-        st.vflags[s] = flags | (ln << 8);
-        want_shadow = (flags & VF_SHADOW) != 0;
-        want_mis = (flags & VF_MIS) != 0;
-        want_resolve = true;
-      }
+      uint64_t g = P.chunk_base + (uint64_t)s;  // slots never move
+      o = shadeVertex(A, S, P, st, s, g, depth, counters, [&](const Spec& L) {
+        splatSample(film, P, g, L, counters + C_NONFINITE, PassFilter{});
+      });
     }
-    queueAppend(want_shadow, s, Q.shadow, counters + C_SHADOW);
-    queueAppend(want_mis, s, Q.mis, counters + C_MIS);
-    queueAppend(want_resolve, s, Q.resolve, counters + C_RESOLVE);
+    queueAppend(o.shadow, s, Q.shadow, counters + C_SHADOW);
+    queueAppend(o.mis, s, Q.mis, counters + C_MIS);
+    queueAppend(o.resolve, s, Q.resolve, counters + C_RESOLVE);
   }
 }
 
@@ -432,49 +170,15 @@ __global__ void __launch_bounds__(128) k_resolve(DevAccel A, DevShading S, PassP
     int s = 0;
     if (q < n) {
       s = Q.resolve[q];
-      size_t c = st.cap;
-      int vf = st.vflags[s];
-      int lc = S.n_lights;
-      Spec ed = sConst(0);  // estimateDirect = ls + bs (Scene.hs:218)
-      Spec lsv = sConst(0), bsv = sConst(0);
-      if ((vf & VF_SHADOW) && st.svis[s]) lsv = loadBands(st.ls, c, s);
-      if (vf & VF_MIS) {
-        const DLight& l = S.lights[vf >> 8];
-        Ray mr = loadRay7(st.mray, c, s);
-        int mp = st.mhit_prim[s];
-        bool use = false;
-        Spec lr;
-        if (mp == kDegenerateRay) {
-          atomicAdd(counters + C_DEGENERATE, 1ull);
-          lr = sConst(NAN);  // a NaN ray poisons the sample, which the film then drops
-          use = true;
-        } else if (mp >= 0) {
-          if (l.kind == DLIGHT_AREA) {
-            int2 info = __ldg(S.prim_info + mp);
-            if (info.x < 0 && ~info.x == l.shape) {  // Eq Light: the same area light
-              HitGeom gm = hitGeometry(A, S, mr, mp, st.mhit_t[s], st.mhit_b[2 * s],
-                                       st.mhit_b[2 * s + 1]);
-              lr = intLe(S, gm, -mr.d);
-              use = true;
-            }
-          }
-        } else {
-          lr = lightLe(l, mr.d);
-          use = true;
-        }
-        if (use) bsv = sScale(loadBands(st.bsf, c, s) * lr, st.bsw[s]);
-      }
-      ed = lsv + bsv;
-      Spec direct = lc == 1 ? ed : (lc > 1 ? sScale(ed, (float)lc) : sConst(0));
-      Spec lHere = loadBands(st.intl, c, s) + direct;
-      Spec T = loadBands(st.T, c, s);
-      Spec Lr = loadBands(st.L, c, s) + T * lHere;
-      if (vf & VF_CONT) {
-        storeBands(st.T, c, s, sScale(loadBands(st.fc, c, s) * T, st.invpc[s]));
-        storeBands(st.L, c, s, Lr);
-        cont = true;
-      } else {
-        finishPath(film, P, s, Lr, counters);
+      uint64_t g = P.chunk_base + (uint64_t)s;
+      Spec Tn, Ln;
+      cont = resolveVertex(
+          A, S, st, s, counters,
+          [&](const Spec& L) { splatSample(film, P, g, L, counters + C_NONFINITE, PassFilter{}); },
+          Tn, Ln);
+      if (cont) {
+        storeBands(st.T, st.cap, s, Tn);
+        storeBands(st.L, st.cap, s, Ln);
       }
     }
     queueAppend(cont, s, Q.live[live_out], counters + live_out);
@@ -483,32 +187,6 @@ __global__ void __launch_bounds__(128) k_resolve(DevAccel A, DevShading S, PassP
 
 // ------------------------------------------------------------------ host side
 namespace {
-
-bool g_const_ready[64] = {false};
-
-float fbitsHost(uint32_t b) {
-  float f;
-  memcpy(&f, &b, 4);
-  return f;
-}
-
-cudaError_t ensureConstants(int device) {
-  if (device >= 0 && device < 64 && g_const_ready[device]) return cudaSuccess;
-  float x[16], y[16], z[16];
-  for (int i = 0; i < 16; i++) {
-    x[i] = fbitsHost(BLING_CIE_X_BITS[i]);
-    y[i] = fbitsHost(BLING_CIE_Y_BITS[i]);
-    z[i] = fbitsHost(BLING_CIE_Z_BITS[i]);
-  }
-  float ys = fbitsHost(BLING_CIE_Y_SUM_BITS);
-  cudaError_t e;
-  if ((e = cudaMemcpyToSymbol(c_cieX, x, sizeof x)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyToSymbol(c_cieY, y, sizeof y)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyToSymbol(c_cieZ, z, sizeof z)) != cudaSuccess) return e;
-  if ((e = cudaMemcpyToSymbol(c_cieYSum, &ys, sizeof ys)) != cudaSuccess) return e;
-  if (device >= 0 && device < 64) g_const_ready[device] = true;
-  return cudaSuccess;
-}
 
 template <class K>
 unsigned residentGrid(K kernel, int sms) {
@@ -540,42 +218,6 @@ Grids grids(int device, int sms) {
   return g;
 }
 
-// the pass constants (imageWindow', Image.hs:170-176; Path.hs:34-36)
-int passParams(const bling_render_params& p, uint64_t pass, int fw, int fh, PassParams& P,
-               std::string& err) {
-  memset(&P, 0, sizeof P);
-  P.seed = p.seed;
-  P.pass = pass;
-  float fwid, fhei;
-  if (p.filter_kind == BLING_FILTER_BOX) {
-    fwid = fhei = 0.5f;
-  } else {
-    fwid = p.filter_params[0];
-    fhei = p.filter_params[1];
-  }
-  if (!(fwid > 0) || !(fhei > 0) || fwid > 16 || fhei > 16) {
-    err = "filter extent must be in (0, 16]";
-    return BLING_ERR_INVALID_ARG;
-  }
-  P.fw = fwid;
-  P.fh = fhei;
-  P.x0 = (int)floorf(0.5f - fwid);
-  P.x1 = (int)floorf(0.5f + (float)p.width + fwid);
-  P.y0 = (int)floorf(0.5f - fhei);
-  P.y1 = (int)floorf(0.5f + (float)p.height + fhei);
-  P.nx = P.x1 - P.x0 + 1;
-  P.ny = P.y1 - P.y0 + 1;
-  P.nu = p.strata_x;
-  P.nv = p.strata_y;
-  P.spp = p.strata_x * p.strata_y;
-  P.n1d = 4 * p.sample_depth;
-  P.n2d = 3 * p.sample_depth;
-  P.max_depth = p.max_depth;
-  P.rr_depth = p.rr_depth;
-  P.width = fw;
-  P.height = fh;
-  return BLING_OK;
-}
 
 // the bounces of one chunk of path samples
 cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S, PassParams P,
@@ -615,6 +257,43 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
 
 }  // namespace
 
+// the pass constants (imageWindow', Image.hs:170-176; Path.hs:34-36)
+int integrator_pass_params(const bling_render_params& p, uint64_t pass, int fw, int fh, PassParams& P,
+               std::string& err) {
+  memset(&P, 0, sizeof P);
+  P.seed = p.seed;
+  P.pass = pass;
+  float fwid, fhei;
+  if (p.filter_kind == BLING_FILTER_BOX) {
+    fwid = fhei = 0.5f;
+  } else {
+    fwid = p.filter_params[0];
+    fhei = p.filter_params[1];
+  }
+  if (!(fwid > 0) || !(fhei > 0) || fwid > 16 || fhei > 16) {
+    err = "filter extent must be in (0, 16]";
+    return BLING_ERR_INVALID_ARG;
+  }
+  P.fw = fwid;
+  P.fh = fhei;
+  P.x0 = (int)floorf(0.5f - fwid);
+  P.x1 = (int)floorf(0.5f + (float)p.width + fwid);
+  P.y0 = (int)floorf(0.5f - fhei);
+  P.y1 = (int)floorf(0.5f + (float)p.height + fhei);
+  P.nx = P.x1 - P.x0 + 1;
+  P.ny = P.y1 - P.y0 + 1;
+  P.nu = p.strata_x;
+  P.nv = p.strata_y;
+  P.spp = p.strata_x * p.strata_y;
+  P.n1d = 4 * p.sample_depth;
+  P.n2d = 3 * p.sample_depth;
+  P.max_depth = p.max_depth;
+  P.rr_depth = p.rr_depth;
+  P.width = fw;
+  P.height = fh;
+  return BLING_OK;
+}
+
 #define RET_CUDA(call)                                                      \
   do {                                                                      \
     cudaError_t e_ = (call);                                                \
@@ -642,9 +321,9 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
                            int fh, IntegratorWorkspace& ws, PassResult& res, std::string& err) {
   int device = 0;
   RET_CUDA(cudaGetDevice(&device));
-  RET_CUDA(ensureConstants(device));
+  RET_CUDA(loadCieConstants(device));
   PassParams P;
-  int rc = passParams(p, pass, fw, fh, P, err);
+  int rc = integrator_pass_params(p, pass, fw, fh, P, err);
   if (rc) return rc;
   uint64_t total = (uint64_t)P.nx * P.ny * P.spp;
   if (total >= (uint64_t(1) << 40)) {
@@ -720,9 +399,9 @@ int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const
     }
     g_noalloc_ptr[device] = (unsigned char*)ptr;
   }
-  RET_CUDA(ensureConstants(device));
+  RET_CUDA(loadCieConstants(device));
   PassParams P;
-  int rc = passParams(p, pass, fw, fh, P, err);
+  int rc = integrator_pass_params(p, pass, fw, fh, P, err);
   if (rc) return rc;
   uint64_t total = (uint64_t)P.nx * P.ny * P.spp;
   if (total > kNoAllocSlots) {

@@ -1,9 +1,9 @@
 // Device helpers of the wavefront path integrator: spectra, the sampler and
 // its counter-based generator, Monte Carlo warps, BSDFs and materials, hit
 // geometry, lights and the film splat.  Each restates the reference function it
-// names (src/lib/Graphics/Bling/...).  Included by integrator.cu only; every
-// translation unit that uses it is built with -fmad=false so the arithmetic
-// rounds like the reference's binary32.
+// names (src/lib/Graphics/Bling/...).  Every translation unit that includes it
+// is built with -fmad=false so the arithmetic rounds like the reference's
+// binary32, and has its own copy of the constant tables below.
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -72,8 +72,33 @@ __device__ __forceinline__ Spec sClamp01(const Spec& a) {
   return s;
 }
 
-__constant__ float c_cieX[16], c_cieY[16], c_cieZ[16];
-__constant__ float c_cieYSum;
+static __constant__ float c_cieX[16], c_cieY[16], c_cieZ[16];
+static __constant__ float c_cieYSum;
+
+// fills this translation unit's CIE tables on the current device (once per device)
+static cudaError_t loadCieConstants(int device) {
+  static bool ready[64] = {false};
+  if (device >= 0 && device < 64 && ready[device]) return cudaSuccess;
+  auto bits = [](uint32_t b) {
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+  };
+  float x[16], y[16], z[16];
+  for (int i = 0; i < 16; i++) {
+    x[i] = bits(BLING_CIE_X_BITS[i]);
+    y[i] = bits(BLING_CIE_Y_BITS[i]);
+    z[i] = bits(BLING_CIE_Z_BITS[i]);
+  }
+  float ys = bits(BLING_CIE_Y_SUM_BITS);
+  cudaError_t e;
+  if ((e = cudaMemcpyToSymbol(c_cieX, x, sizeof x)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_cieY, y, sizeof y)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_cieZ, z, sizeof z)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyToSymbol(c_cieYSum, &ys, sizeof ys)) != cudaSuccess) return e;
+  if (device >= 0 && device < 64) ready[device] = true;
+  return cudaSuccess;
+}
 
 // sY (Spectrum.hs:371-373)
 __device__ __forceinline__ float sY(const Spec& s) {
@@ -370,7 +395,7 @@ __device__ __forceinline__ float orenNayarScale(const BxDF& b, V3 wo, V3 wi) {
 }
 
 // bxdfEval b wo wi
-__device__ Spec bxEval(const BxDF& b, V3 wo, V3 wi) {
+static __device__ Spec bxEval(const BxDF& b, V3 wo, V3 wi) {
   switch (b.kind) {
     case BX_LAMBERT: return sScale(bxR(b), kInvPi * absCosTheta(wo));
     case BX_OREN: return sScale(sScale(bxR(b), orenNayarScale(b, wo, wi)), kInvPi * absCosTheta(wo));
@@ -388,7 +413,7 @@ __device__ Spec bxEval(const BxDF& b, V3 wo, V3 wi) {
     default: return sConst(0);
   }
 }
-__device__ float bxPdf(const BxDF& b, V3 wo, V3 wi) {
+static __device__ float bxPdf(const BxDF& b, V3 wo, V3 wi) {
   switch (b.kind) {
     case BX_LAMBERT:
     case BX_OREN: return sameHemisphere(wo, wi) ? kInvPi * absCosTheta(wi) : 0.0f;
@@ -402,7 +427,7 @@ __device__ float bxPdf(const BxDF& b, V3 wo, V3 wi) {
     default: return 0;
   }
 }
-__device__ void bxSample(const BxDF& b, V3 wo, float u1, float u2, Spec& f, V3& wi, float& pdf) {
+static __device__ void bxSample(const BxDF& b, V3 wo, float u1, float u2, Spec& f, V3& wi, float& pdf) {
   switch (b.kind) {
     case BX_LAMBERT:
     case BX_OREN: {
@@ -477,7 +502,7 @@ struct Bsdf {
 };
 
 // mkBsdf' with the material's BxDFs (Material.hs:228-292)
-__device__ Bsdf materialBsdf(const DMaterial* __restrict__ mats, int mi, V3 dgg_n, V3 dgs_p,
+static __device__ Bsdf materialBsdf(const DMaterial* __restrict__ mats, int mi, V3 dgg_n, V3 dgs_p,
                              V3 dgs_n, V3 dgs_dpdu) {
   const DMaterial& m = mats[mi];
   Bsdf b;
@@ -560,7 +585,7 @@ struct BsdfSample {
 };
 
 // sampleBsdf'' False bxdfAll (Reflection.hs:278-316)
-__device__ BsdfSample sampleBsdf(const Bsdf& b, V3 woW, float uComp, float u1, float u2) {
+static __device__ BsdfSample sampleBsdf(const Bsdf& b, V3 woW, float uComp, float u1, float u2) {
   BsdfSample out;
   out.type = T_REFL | T_DIFF;
   out.pdf = 0;
@@ -610,7 +635,7 @@ __device__ BsdfSample sampleBsdf(const Bsdf& b, V3 woW, float uComp, float u1, f
   return out;
 }
 // evalBsdf False (Reflection.hs:318-332)
-__device__ Spec evalBsdf(const Bsdf& b, V3 woW, V3 wiW) {
+static __device__ Spec evalBsdf(const Bsdf& b, V3 woW, V3 wiW) {
   float cosWo = dot(woW, b.ng);
   float sideTest = dot(wiW, b.ng) / cosWo;
   if (sideTest == 0) return sConst(0);
@@ -625,7 +650,7 @@ __device__ Spec evalBsdf(const Bsdf& b, V3 woW, V3 wiW) {
   return f;
 }
 // bsdfPdf (Reflection.hs:251-257)
-__device__ float bsdfPdf(const Bsdf& b, V3 woW, V3 wiW) {
+static __device__ float bsdfPdf(const Bsdf& b, V3 woW, V3 wiW) {
   if (b.n == 0) return 0;
   V3 wo = worldToLocal(b.cs, woW), wi = worldToLocal(b.cs, wiW);
   float s = 0.0f;
@@ -645,7 +670,7 @@ struct HitGeom {
 
 // builds the intersection's DG for primitive `prim` hit at t (TriangleMesh.hs:182-207,
 // Geometry.hs:33-36, triangleShadingGeometry TriangleMesh.hs:122-134)
-__device__ HitGeom hitGeometry(const DevAccel& A, const DevShading& S, const Ray& r, int prim,
+static __device__ HitGeom hitGeometry(const DevAccel& A, const DevShading& S, const Ray& r, int prim,
                                float t, float b1, float b2) {
   HitGeom g;
   int2 info = __ldg(S.prim_info + prim);
@@ -730,7 +755,7 @@ __device__ HitGeom hitGeometry(const DevAccel& A, const DevShading& S, const Ray
 // ------------------------------------------------------------------ lights
 __device__ __forceinline__ bool insideSphere(float r, V3 p) { return sqLen(p) - r * r < 1e-4f; }
 
-__device__ void sampleShapeP(const DShape& s, float u1, float u2, V3& p, V3& n) {
+static __device__ void sampleShapeP(const DShape& s, float u1, float u2, V3& p, V3& n) {
   switch (s.kind) {
     case SHAPE_BOX: {
       int axis = min(2, (int)floorf(u1 * 3.0f));
@@ -771,7 +796,7 @@ __device__ void sampleShapeP(const DShape& s, float u1, float u2, V3& p, V3& n) 
     }
   }
 }
-__device__ void sampleShape(const DShape& s, V3 pt, float u1, float u2, V3& ps, V3& ns) {
+static __device__ void sampleShape(const DShape& s, V3 pt, float u1, float u2, V3& ps, V3& ns) {
   if (s.kind == SHAPE_SPHERE && !insideSphere(s.p[0], pt)) {
     float r = s.p[0];
     V3 dn = normalize(-pt);
@@ -786,7 +811,7 @@ __device__ void sampleShape(const DShape& s, V3 pt, float u1, float u2, V3& ps, 
   }
   sampleShapeP(s, u1, u2, ps, ns);
 }
-__device__ float shapePdf(const DShape& s, V3 p, V3 wi) {
+static __device__ float shapePdf(const DShape& s, V3 p, V3 wi) {
   if (s.kind == SHAPE_SPHERE && !insideSphere(s.p[0], p)) {
     float r = s.p[0];
     float sinThetaMax2 = r * r / sqLen(p);
@@ -814,7 +839,7 @@ __device__ __forceinline__ const float* envTexel(const DLight& l, float u, float
 }
 // upperBound + sampleContinuous1D (Montecarlo.hs:282-301); findIndex (>= u)
 // on a non-decreasing CDF is its lower bound
-__device__ void sampleContinuous1D(const float* func, const float* cdf, int n, float fi, float u,
+static __device__ void sampleContinuous1D(const float* func, const float* cdf, int n, float fi, float u,
                                    float& x, float& pdf, int& off) {
   int lo = 0, hi = n + 1;  // first index with cdf >= u, n + 1 if none
   while (lo < hi) {
@@ -840,7 +865,7 @@ struct LightSample {
   bool delta;
 };
 
-__device__ LightSample lightSample(const DevAccel& A, const DevShading& S, const DLight& l, V3 p,
+static __device__ LightSample lightSample(const DevAccel& A, const DevShading& S, const DLight& l, V3 p,
                                    float eps, V3 n, float u1, float u2) {
   LightSample ls;
   ls.delta = false;
@@ -897,14 +922,14 @@ __device__ LightSample lightSample(const DevAccel& A, const DevShading& S, const
   return ls;
 }
 // le (Light.hs:98-106)
-__device__ Spec lightLe(const DLight& l, V3 d) {
+static __device__ Spec lightLe(const DLight& l, V3 d) {
   if (l.kind != DLIGHT_INFINITE) return sConst(0);
   V3 wh = normalize(transVector(l.w2l, d));
   float phi = sphericalPhi(wh), theta = sphericalTheta(wh);
   return sLoad(envTexel(l, phi / (2.0f * kPi), theta / kPi));
 }
 // pdf (Light.hs:215-229)
-__device__ float lightPdf(const DevAccel& A, const DLight& l, V3 p, V3 wi) {
+static __device__ float lightPdf(const DevAccel& A, const DLight& l, V3 p, V3 wi) {
   if (l.kind == DLIGHT_AREA) {
     const DShape& s = A.shapes[l.shape];
     return shapePdf(s, transPoint(s.w2o, p), transVector(s.w2o, wi));
@@ -928,13 +953,15 @@ __device__ float lightPdf(const DevAccel& A, const DLight& l, V3 p, V3 wi) {
 }
 
 // ------------------------------------------------------------------ film
-__constant__ float c_filter[256];
+static __constant__ float c_filter[256];
 
 // addSample (Image.hs:250-299) into the tile image of the sample's tile
 // (mkImageTile/addTile, Image.hs:108-120,178-199): the footprint is clipped to
-// the tile's pixel range and to the film.
-__device__ void filmAdd(float* __restrict__ film, const PassParams& P, int ix, int iy, float sx,
-                        float sy, const Spec& L, unsigned long long* nonfinite) {
+// the tile's pixel range and to the film.  filt(i) reads entry i of the 16x16
+// filter table.
+template <class Filter>
+__device__ void filmAddT(float* __restrict__ film, const PassParams& P, int ix, int iy, float sx,
+                         float sy, const Spec& L, unsigned long long* nonfinite, Filter filt) {
   bool bad = false;
 #pragma unroll
   for (int i = 0; i < 16; i++) bad = bad || isnan(L.v[i]) || isinf(L.v[i]);
@@ -970,7 +997,7 @@ __device__ void filmAdd(float* __restrict__ film, const PassParams& P, int ix, i
     for (int x = x0; x <= x1; x++) {
       float fx = fabsf(((float)x - dx) * ifw * 16.0f);
       int ixf = min((int)floorf(fx), 15);
-      float w = c_filter[iyf * 16 + ixf];
+      float w = filt(iyf * 16 + ixf);
       float* px = film + 4 * ((size_t)y * P.width + x);
       atomicAdd(px, w);
       atomicAdd(px + 1, smx * w);

@@ -13,6 +13,8 @@
 // primitive whose reference-arithmetic t lies on a box face is never pruned
 // (the quantised wide layout also widens each child box by one quantum).
 #pragma once
+#include <type_traits>
+
 #include "bvh.h"
 #include "dmath.cuh"
 #include "dshape.cuh"
@@ -105,13 +107,24 @@ __device__ __forceinline__ float qbyte(uint32_t word, uint32_t sel) {
 // child boxes and pushes the hit ones in the octant order of the ray, so the
 // nearest is taken next.  All votes use the full warp mask: every lane runs
 // every iteration of the uniform loops and does work only when it has some.
+// With an `accel_of` functor (ray index -> const DevAccel*) every lane walks
+// the scene of its own ray (batches of jobs over several scenes, which must
+// share the node layout); otherwise all rays walk A.
 constexpr int kSentinel = INT32_MIN;
 
-template <bool ANY, bool WIDE, bool COUNT, class LoadRay, class Emit>
+template <bool ANY, bool WIDE, bool COUNT, class LoadRay, class Emit,
+          class AccelOf = std::nullptr_t>
 __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n,
                                                     unsigned long long* __restrict__ next_ray,
                                                     LoadRay load, Emit emit,
-                                                    TraversalCounts* cnt = nullptr) {
+                                                    TraversalCounts* cnt = nullptr,
+                                                    AccelOf accel_of = nullptr) {
+  constexpr bool PER_LANE = !std::is_same<AccelOf, std::nullptr_t>::value;
+  const float4* l_nodes = nullptr;
+  const uint4* l_nodes8 = nullptr;
+  const float4* l_slots = nullptr;
+  const DShape* l_shapes = nullptr;
+#define TW_ACC(field) (PER_LANE ? l_##field : A.field)
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -151,7 +164,16 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
             best_prim = -1;
             bb1 = bb2 = 0.0f;
             sp = 0;
-            cur = WIDE ? A.root8 : A.root_ref;
+            if constexpr (PER_LANE) {
+              const DevAccel* la = accel_of(rid);
+              l_nodes = la->nodes;
+              l_nodes8 = la->nodes8;
+              l_slots = la->slots;
+              l_shapes = la->shapes;
+              cur = WIDE ? la->root8 : la->root_ref;
+            } else {
+              cur = WIDE ? A.root8 : A.root_ref;
+            }
             leaf = kSentinel;
           }
         } else {
@@ -167,7 +189,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
       if (work) {
         if (COUNT) cnt->nodes++;
         if (WIDE) {
-          const uint4* nd = A.nodes8 + 5 * (size_t)cur;
+          const uint4* nd = TW_ACC(nodes8) + 5 * (size_t)cur;
           uint4 w0 = __ldg(nd), w1 = __ldg(nd + 1), w2 = __ldg(nd + 2), w3 = __ldg(nd + 3),
                 w4 = __ldg(nd + 4);
           // child box slab distances: t = q * (scale / d) + (p - o) / d
@@ -216,7 +238,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
           }
           cur = first != kSentinel ? first : (sp > 0 ? stack[--sp] : kSentinel);
         } else {
-          const float4* nd = A.nodes + 4 * (size_t)cur;
+          const float4* nd = TW_ACC(nodes) + 4 * (size_t)cur;
           float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2);
           float4 refs = __ldg(nd + 3);
           float n0, f0, n1, f1;
@@ -257,7 +279,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
         leaf = kSentinel;
         for (;;) {
           if (COUNT) cnt->slots++;
-          const float4* sl = A.slots + 3 * (size_t)slot;
+          const float4* sl = TW_ACC(slots) + 3 * (size_t)slot;
           float4 s0 = __ldg(sl), s1 = __ldg(sl + 1), s2 = __ldg(sl + 2);
           int flags = __float_as_int(s2.z);
           int prim = __float_as_int(s2.y);
@@ -266,7 +288,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
           if (!(flags & SLOT_SHAPE)) {
             hit = triTest(s0, s1, s2, r, best_t, t, b1, b2);
           } else {
-            const DShape& sh = A.shapes[__float_as_int(s0.x)];
+            const DShape& sh = TW_ACC(shapes)[__float_as_int(s0.x)];
             Ray ro = transRay(sh.w2o, Ray{r.o, r.d, r.tmin, ANY ? r.tmax : best_t});
             if (ANY) {
               hit = shapeIntersects(sh, ro);
@@ -299,6 +321,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
       rid = -1;
     }
   }
+#undef TW_ACC
 }
 
 }  // namespace bgpu

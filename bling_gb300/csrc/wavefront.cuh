@@ -1,0 +1,379 @@
+// Wavefront building blocks shared by the per-pass integrator (integrator.cu)
+// and the batched job engine (batch.cu): the SoA path slots, queue appends,
+// camera rays, and the two halves of one path vertex (nextVertex,
+// Integrator/Path.hs:49-87) around its deferred shadow and MIS rays.
+//
+// Paths live in slots (throughput and radiance as 16-band spectra,
+// band-major) and never move; queues of slot indices carry the live paths from
+// stage to stage.  Arithmetic keeps the reference's operation order
+// (-fmad=false); random numbers come from the counter-based generator shared
+// with the CPU oracle, keyed by (seed, pass, pixel, sample index), so a path's
+// result does not depend on the slot or the launch that carries it.
+#pragma once
+#include "integrator_device.cuh"
+
+namespace bgpu {
+
+enum : int { VF_SHADOW = 1, VF_MIS = 2, VF_CONT = 4 };
+
+struct Slots {
+  size_t cap;
+  float* T;          // 16 x cap
+  float* L;          // 16 x cap
+  float* ray;        // 7 x cap: o, d, tmin (sign bit of tmin: the previous bounce was specular)
+  float* hit_t;      // cap
+  int32_t* hit_prim; // cap
+  float* hit_b;      // 2 x cap
+  // the current vertex, deferred until its shadow and MIS rays are traced
+  float* intl;       // 16 x cap: emission seen on a specular path
+  float* ls;         // 16 x cap: light-sample term before visibility
+  float* bsf;        // 16 x cap: MIS BSDF sample throughput
+  float* fc;         // 16 x cap: continuation BSDF sample throughput
+  float* bsw;        // cap: MIS weight of the BSDF sample
+  float* invpc;      // cap: 1 / continuation probability
+  int32_t* vflags;   // cap: VF_* | light index << 8
+  float* sray;       // 8 x cap: shadow ray o, d, tmin, tmax
+  int32_t* svis;     // cap: shadow ray unoccluded
+  float* mray;       // 7 x cap: MIS ray o, d, tmin
+  float* mhit_t;     // cap
+  int32_t* mhit_prim;// cap
+  float* mhit_b;     // 2 x cap
+};
+
+struct Queues {
+  int32_t* live[2];  // paths to trace this bounce / next bounce
+  int32_t* shadow;
+  int32_t* mis;
+  int32_t* resolve;
+};
+
+// counters (unsigned long long): queue sizes and statistics
+enum : int {
+  C_LIVE0 = 0, C_LIVE1 = 1, C_CLOSEST = 2, C_ANY = 3, C_NONFINITE = 4, C_NEXT_TRACE = 5,
+  C_SHADOW = 6, C_MIS = 7, C_RESOLVE = 8, C_NEXT_SHADOW = 9, C_NEXT_MIS = 10, C_DEGENERATE = 11,
+  C_COUNT = 16
+};
+
+constexpr size_t kSlotWords = 16 * 6 + 7 + 4 + 3 + 8 + 1 + 7 + 4;  // per slot, 4-byte words
+constexpr size_t kQueueWords = 5;
+constexpr size_t kCounterBytes = 256;
+
+// carves the slot arrays (kSlotWords per slot) from w, advancing it
+inline void carveSlots(float*& w, size_t cap, Slots& st) {
+  auto take = [&](size_t words) {
+    float* p = w;
+    w += words * cap;
+    return p;
+  };
+  st.cap = cap;
+  st.T = take(16);
+  st.L = take(16);
+  st.ray = take(7);
+  st.hit_t = take(1);
+  st.hit_prim = (int32_t*)take(1);
+  st.hit_b = take(2);
+  st.intl = take(16);
+  st.ls = take(16);
+  st.bsf = take(16);
+  st.fc = take(16);
+  st.bsw = take(1);
+  st.invpc = take(1);
+  st.vflags = (int32_t*)take(1);
+  st.sray = take(8);
+  st.svis = (int32_t*)take(1);
+  st.mray = take(7);
+  st.mhit_t = take(1);
+  st.mhit_prim = (int32_t*)take(1);
+  st.mhit_b = take(2);
+}
+
+// sample index g of a pass -> pixel and sample number (pixel-major, like the
+// tile loop of prender, Rendering.hs:127-140)
+__device__ __forceinline__ void decodeSample(const PassParams& P, uint64_t g, int& ix, int& iy,
+                                             uint32_t& n) {
+  uint64_t pix = g / (uint64_t)P.spp;
+  n = (uint32_t)(g % (uint64_t)P.spp);
+  ix = P.x0 + (int)(pix % (uint64_t)P.nx);
+  iy = P.y0 + (int)(pix / (uint64_t)P.nx);
+}
+__device__ __forceinline__ Sampler mkSampler(const PassParams& P, int ix, int iy, uint32_t n) {
+  Sampler s;
+  s.key = pixelKey(P.seed, P.pass, ix, iy);
+  s.n = n;
+  s.nu = P.nu;
+  s.nv = P.nv;
+  s.n1d = P.n1d;
+  s.n2d = P.n2d;
+  return s;
+}
+__device__ __forceinline__ void pixelSample(const PassParams& P, const Sampler& s, int ix, int iy,
+                                            float& sx, float& sy, float& lu, float& lv) {
+  float ox, oy;
+  strat2D(s, s.n, DIM_PIX_U, DIM_PIX_V, ox, oy);
+  uint32_t N = (uint32_t)P.spp;
+  uint32_t lp = permute(s.n, N, randU32(s.key, 0xffffffffu, DIM_LENS_PERM));
+  strat2D(s, lp, DIM_LENS_U, DIM_LENS_V, lu, lv);
+  sx = (float)ix + ox;
+  sy = (float)iy + oy;
+}
+
+__device__ __forceinline__ Spec loadBands(const float* base, size_t cap, int s) {
+  Spec v;
+#pragma unroll
+  for (int b = 0; b < 16; b++) v.v[b] = base[b * cap + s];
+  return v;
+}
+__device__ __forceinline__ void storeBands(float* base, size_t cap, int s, const Spec& v) {
+#pragma unroll
+  for (int b = 0; b < 16; b++) base[b * cap + s] = v.v[b];
+}
+__device__ __forceinline__ void storeRay(float* base, size_t cap, int s, const Ray& r, bool tmax) {
+  base[s] = r.o.x;
+  base[cap + s] = r.o.y;
+  base[2 * cap + s] = r.o.z;
+  base[3 * cap + s] = r.d.x;
+  base[4 * cap + s] = r.d.y;
+  base[5 * cap + s] = r.d.z;
+  base[6 * cap + s] = r.tmin;
+  if (tmax) base[7 * cap + s] = r.tmax;
+}
+__device__ __forceinline__ Ray loadRay7(const float* base, size_t cap, int s) {
+  return Ray{V3{base[s], base[cap + s], base[2 * cap + s]},
+             V3{base[3 * cap + s], base[4 * cap + s], base[5 * cap + s]}, fabsf(base[6 * cap + s]),
+             INFINITY};
+}
+__device__ __forceinline__ Ray loadShadowRay(const Slots& st, int s) {
+  size_t c = st.cap;
+  return Ray{V3{st.sray[s], st.sray[c + s], st.sray[2 * c + s]},
+             V3{st.sray[3 * c + s], st.sray[4 * c + s], st.sray[5 * c + s]}, st.sray[6 * c + s],
+             st.sray[7 * c + s]};
+}
+
+// warp-aggregated append (every lane of the warp calls it)
+__device__ __forceinline__ void queueAppend(bool live, int slot, int32_t* __restrict__ queue,
+                                            unsigned long long* count) {
+  const unsigned mask = 0xffffffffu;
+  __syncwarp();
+  unsigned ballot = __ballot_sync(mask, live);
+  if (!ballot) return;
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(ballot) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(ballot));
+  base = __shfl_sync(mask, base, leader);
+  if (live) queue[base + __popc(ballot & ((1u << lane) - 1))] = slot;
+}
+
+// intLe (Primitive.hs:68-76) + lEmit (Light.hs:85-96)
+__device__ __forceinline__ Spec intLe(const DevShading& S, const HitGeom& g, V3 wo) {
+  if (g.light_id < 0) return sConst(0);
+  return dot(g.n, wo) > 0 ? sLoad(S.shape_emission + 16 * g.shape) : sConst(0);
+}
+
+// camera ray of sample g (fireRay, Camera.hs:146-164)
+__device__ __forceinline__ Ray cameraRay(const PassParams& P, const bling_camera_desc& cam,
+                                         uint64_t g) {
+  int ix, iy;
+  uint32_t n;
+  decodeSample(P, g, ix, iy, n);
+  Sampler s = mkSampler(P, ix, iy, n);
+  float sx, sy, lu, lv;
+  pixelSample(P, s, ix, iy, sx, sy, lu, lv);
+  V3 pCamera = transPoint(cam.r2c, V3{sx, sy, 0});
+  Ray ray{V3{0, 0, 0}, normalize(pCamera), 0, INFINITY};
+  if (cam.lens_radius > 0) {
+    float u, v;
+    concentricSampleDisk(lu, lv, u, v);
+    V3 ro{u * cam.lens_radius, v * cam.lens_radius, 0};
+    V3 pFocus = rayAt(ray, cam.focal_distance / ray.d.z);
+    ray = Ray{ro, normalize(pFocus - ro), 0, INFINITY};
+  }
+  return transRay(cam.c2w, ray);
+}
+
+// the film splat of sample g (the raster position is recomputed from the sampler)
+template <class Filter>
+__device__ __forceinline__ void splatSample(float* film, const PassParams& P, uint64_t g,
+                                            const Spec& L, unsigned long long* nonfinite,
+                                            Filter filt) {
+  int ix, iy;
+  uint32_t sn;
+  decodeSample(P, g, ix, iy, sn);
+  Sampler smp = mkSampler(P, ix, iy, sn);
+  float sx, sy, lu, lv;
+  pixelSample(P, smp, ix, iy, sx, sy, lu, lv);
+  filmAddT(film, P, ix, iy, sx, sy, L, nonfinite, filt);
+}
+
+// the pass constants of render parameters (imageWindow', Image.hs:170-176;
+// Path.hs:34-36), integrator.cu
+int integrator_pass_params(const bling_render_params& p, uint64_t pass, int fw, int fh,
+                           PassParams& P, std::string& err);
+
+struct VertexOut {
+  bool shadow, mis, resolve;
+};
+
+// First half of one vertex of the path in slot s at bounce `depth`
+// (Path.hs:49-87): emission on specular paths, the BSDF, one light sample
+// and one BSDF sample for MIS (sampleOneLight/estimateDirect,
+// Scene.hs:184-241), Russian roulette and the continuation sample.  Stores
+// the deferred terms in the slot and says which rays to trace; a path that
+// ends here is handed to finish(L).
+template <class Finish>
+__device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevShading& S,
+                                                 const PassParams& P, const Slots& st, int s,
+                                                 uint64_t g, int depth,
+                                                 unsigned long long* counters, Finish finish) {
+  VertexOut out{false, false, false};
+  int ix, iy;
+  uint32_t sn;
+  decodeSample(P, g, ix, iy, sn);
+  Sampler smp = mkSampler(P, ix, iy, sn);
+  size_t c = st.cap;
+  Ray ray = loadRay7(st.ray, c, s);
+  bool specular = depth == 0 || signbit(st.ray[6 * c + s]);
+  int prim = st.hit_prim[s];
+  if (prim == kDegenerateRay) {
+    // a NaN ray: the reference's sample ends NaN and is dropped by the film
+    atomicAdd(counters + C_DEGENERATE, 1ull);
+    finish(sConst(NAN));
+    return out;
+  }
+  if (prim < 0 || depth == P.max_depth) {
+    Spec Lr = loadBands(st.L, c, s);
+    if (prim < 0 && specular) {  // nothing hit after a specular bounce: l + t * sum le
+      Spec sum = sConst(0);
+      for (int k = 0; k < S.n_lights; k++) sum = sum + lightLe(S.lights[k], ray.d);
+      Lr = Lr + loadBands(st.T, c, s) * sum;
+    }
+    finish(Lr);
+    return out;
+  }
+  float thit = st.hit_t[s], b1 = st.hit_b[2 * s], b2 = st.hit_b[2 * s + 1];
+  float lNumU = rnd1(smp, 1 + 4 * depth);
+  float ld1, ld2;
+  rnd2(smp, 1 + 3 * depth, ld1, ld2);
+  float lBsdfCompU = rnd1(smp, 2 + 4 * depth);
+  float lb1, lb2;
+  rnd2(smp, 2 + 3 * depth, lb1, lb2);
+  HitGeom gm = hitGeometry(A, S, ray, prim, thit, b1, b2);
+  V3 rd = ray.d;
+  storeBands(st.intl, c, s, specular ? intLe(S, gm, rd) : sConst(0));
+  V3 wo = -rd;
+  Bsdf bsdf = materialBsdf(S.materials, gm.material, gm.n, gm.sp, gm.sn, gm.sdpdu);
+  V3 nn = bsdf.cs.n, p = bsdf.p;
+  float eps = gm.eps;
+  int flags = 0;
+  int lc = S.n_lights;
+  int ln = 0;
+  if (lc > 0) {
+    // sampleOneLight (Scene.hs:233-241) -> estimateDirect (Scene.hs:218-222)
+    if (lc > 1) ln = min((int)floorf(lNumU * (float)lc), lc - 1);
+    const DLight& l = S.lights[ln];
+    // sampleLightMis (Scene.hs:184-192), visibility deferred
+    LightSample smpl = lightSample(A, S, l, p, eps, nn, ld1, ld2);
+    if (!(smpl.pdf == 0 || isBlack(smpl.li))) {
+      Spec f = evalBsdf(bsdf, wo, smpl.wi);
+      if (!isBlack(f)) {
+        Spec lsv;
+        if (smpl.delta) {
+          lsv = sScale(f * smpl.li, 1.0f / smpl.pdf);
+        } else {
+          float w = powerHeuristic(smpl.pdf, bsdfPdf(bsdf, wo, smpl.wi));
+          lsv = sScale(f * smpl.li, w / smpl.pdf);
+        }
+        storeBands(st.ls, c, s, lsv);
+        Ray sr = smpl.ray;
+        storeRay(st.sray, c, s, sr, true);
+        flags |= VF_SHADOW;
+      }
+    }
+    // sampleBsdfMis (Scene.hs:194-205), the hit deferred
+    BsdfSample bm = sampleBsdf(bsdf, wo, lBsdfCompU, lb1, lb2);
+    if (!(bm.pdf == 0 || isBlack(bm.f))) {
+      storeBands(st.bsf, c, s, bm.f);
+      st.bsw[s] = powerHeuristic(bm.pdf, lightPdf(A, l, p, bm.wi));
+      storeRay(st.mray, c, s, Ray{p, bm.wi, eps, INFINITY}, false);
+      flags |= VF_MIS;
+    }
+  }
+  // Russian roulette and the continuation (Path.hs:68-87)
+  Spec T = loadBands(st.T, c, s);
+  float pc = depth <= P.rr_depth ? 1.0f : hmin(0.75f, sY(T));
+  float x = rnd1(smp, 3 + 4 * depth);
+  if (!(x > pc)) {
+    float uc = rnd1(smp, 0 + 4 * depth);
+    float ud1, ud2;
+    rnd2(smp, 0 + 3 * depth, ud1, ud2);
+    BsdfSample bc = sampleBsdf(bsdf, wo, uc, ud1, ud2);
+    if (!(bc.pdf == 0 || isBlack(bc.f))) {
+      storeBands(st.fc, c, s, bc.f);
+      st.invpc[s] = 1.0f / pc;
+      bool spec2 = (bc.type & T_SPEC) != 0;
+      storeRay(st.ray, c, s, Ray{p, bc.wi, spec2 ? -eps : eps, INFINITY}, false);
+      flags |= VF_CONT;
+    }
+  }
+  st.vflags[s] = flags | (ln << 8);
+  out.shadow = (flags & VF_SHADOW) != 0;
+  out.mis = (flags & VF_MIS) != 0;
+  out.resolve = true;
+  return out;
+}
+
+// Second half of the vertex (Path.hs:60-87): adds the vertex's radiance once
+// its shadow and MIS rays are traced and computes the new throughput.
+// Returns true when the path continues, with its throughput and radiance in
+// Tn and Ln (the caller stores them); a path that ends is handed to finish(L).
+template <class Finish>
+__device__ __forceinline__ bool resolveVertex(const DevAccel& A, const DevShading& S,
+                                              const Slots& st, int s,
+                                              unsigned long long* counters, Finish finish,
+                                              Spec& Tn, Spec& Ln) {
+  size_t c = st.cap;
+  int vf = st.vflags[s];
+  int lc = S.n_lights;
+  Spec lsv = sConst(0), bsv = sConst(0);
+  if ((vf & VF_SHADOW) && st.svis[s]) lsv = loadBands(st.ls, c, s);
+  if (vf & VF_MIS) {
+    const DLight& l = S.lights[vf >> 8];
+    Ray mr = loadRay7(st.mray, c, s);
+    int mp = st.mhit_prim[s];
+    bool use = false;
+    Spec lr;
+    if (mp == kDegenerateRay) {
+      atomicAdd(counters + C_DEGENERATE, 1ull);
+      lr = sConst(NAN);  // a NaN ray poisons the sample, which the film then drops
+      use = true;
+    } else if (mp >= 0) {
+      if (l.kind == DLIGHT_AREA) {
+        int2 info = __ldg(S.prim_info + mp);
+        if (info.x < 0 && ~info.x == l.shape) {  // Eq Light: the same area light
+          HitGeom gm =
+              hitGeometry(A, S, mr, mp, st.mhit_t[s], st.mhit_b[2 * s], st.mhit_b[2 * s + 1]);
+          lr = intLe(S, gm, -mr.d);
+          use = true;
+        }
+      }
+    } else {
+      lr = lightLe(l, mr.d);
+      use = true;
+    }
+    if (use) bsv = sScale(loadBands(st.bsf, c, s) * lr, st.bsw[s]);
+  }
+  Spec ed = lsv + bsv;  // estimateDirect = ls + bs (Scene.hs:218)
+  Spec direct = lc == 1 ? ed : (lc > 1 ? sScale(ed, (float)lc) : sConst(0));
+  Spec lHere = loadBands(st.intl, c, s) + direct;
+  Spec T = loadBands(st.T, c, s);
+  Spec Lr = loadBands(st.L, c, s) + T * lHere;
+  if (vf & VF_CONT) {
+    Tn = sScale(loadBands(st.fc, c, s) * T, st.invpc[s]);
+    Ln = Lr;
+    return true;
+  }
+  finish(Lr);
+  return false;
+}
+
+}  // namespace bgpu

@@ -65,6 +65,7 @@ class Scene:
     lights: list = field(default_factory=list)
     prim_order: list | None = None
     camera: abi.CameraDesc | None = None
+    view: tuple | None = None  # (camera-to-world look-at transform, fov) for camera_for()
 
     # --- builders -------------------------------------------------------
     def add_material(self, kind, kd=None, ks=None, kt=None, eta=None, k=None, sigma=0.0,
@@ -98,6 +99,19 @@ class Scene:
         c.r2c_inv[:] = r2c.inv.tolist()
         c.lens_radius, c.focal_distance = lens_radius, focal_distance
         self.camera = c
+
+    def camera_for(self, width: int, height: int) -> abi.CameraDesc:
+        """The scene's pinhole view built for another image size
+        (mkPerspectiveCamera takes the image size, Camera.hs:108-147)."""
+        look, fov = self.view
+        c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, fov, width, height)
+        c = abi.CameraDesc()
+        c.c2w[:] = c2w.m.tolist()
+        c.c2w_inv[:] = c2w.inv.tolist()
+        c.r2c[:] = r2c.m.tolist()
+        c.r2c_inv[:] = r2c.inv.tolist()
+        c.lens_radius, c.focal_distance = 0.0, 1.0
+        return c
 
     @property
     def n_triangles(self) -> int:
@@ -211,9 +225,10 @@ def cornell_room(width=256, height=256, fov=40.0) -> Scene:
     short = s.add_shape(abi.SHAPE_BOX, (-0.15, 0.0, -0.15, 0.15, 0.3, 0.15),
                         xf.rotate_y(-18) @ xf.translate(0.67, 0.0, 0.33), white)
     s.prim_order = [m_grey, m_red, m_green, ~q, ~tall, ~short]
-    c2w = xf.look_at((0.5, 0.5, -1.4), (0.5, 0.5, 0.5), (0, 1, 0))
-    c2w, r2c = xf.perspective_camera(c2w, 0.0, 1.0, fov, width, height)
+    look = xf.look_at((0.5, 0.5, -1.4), (0.5, 0.5, 0.5), (0, 1, 0))
+    c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, fov, width, height)
     s.set_camera(c2w, r2c)
+    s.view = (look, fov)
     return s
 
 
@@ -440,9 +455,10 @@ def heightfield_scene(ns=2048, n_spheres=4096, seed=3, width=1920, height=1080, 
     s.lights = [S_light(abi.LIGHT_DIRECTIONAL, rgb_to_spectrum((2.6, 2.4, 2.1), illuminant=True),
                         tuple(float(v) for v in sd)),
                 Light(abi.LIGHT_INFINITE, env=env, w2l=xf.rotate_x(90))]
-    c2w = xf.look_at((0.0, 3.0, -8.0), (0.0, 0.0, 0.5), (0, 1, 0))
-    c2w, r2c = xf.perspective_camera(c2w, 0.0, 1.0, fov, width, height)
+    look = xf.look_at((0.0, 3.0, -8.0), (0.0, 0.0, 0.5), (0, 1, 0))
+    c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, fov, width, height)
     s.set_camera(c2w, r2c)
+    s.view = (look, fov)
     return s
 
 
@@ -453,3 +469,153 @@ def S_light(kind, spectrum, vec):
 def heightfield_params(width=1920, height=1080, spp_side=8, max_depth=8, rr_depth=3, seed=1):
     return render_params(width, height, (spp_side, spp_side), max_depth=max_depth, sample_depth=3,
                          rr_depth=rr_depth, filter_kind=abi.FILTER_BOX, seed=seed)
+
+
+# ---------------------------------------------------------------- batched instances
+def _material_mix(s: Scene, rng, n):
+    """n materials drawn like the heightfield workload's objects: 40% matte,
+    30% plastic (roughness ~U(0.05, 0.5)), 20% metal (roughness
+    ~U(0.01, 0.3)), 10% glass (IOR 1.5)."""
+    kinds = rng.choice(4, size=n, p=[0.4, 0.3, 0.2, 0.1])
+    cols = rng.uniform(0.1, 0.9, (n, 3))
+    out = []
+    for k in range(n):
+        kind = int(kinds[k])
+        if kind == 0:
+            m = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum(tuple(cols[k])))
+        elif kind == 1:
+            m = s.add_material(abi.MAT_PLASTIC, kd=rgb_to_spectrum(tuple(cols[k])),
+                               ks=constant(0.5), roughness=float(rng.uniform(0.05, 0.5)))
+        elif kind == 2:
+            m = s.add_material(abi.MAT_METAL, eta=constant(1.2), k=constant(7.0),
+                               roughness=float(rng.uniform(0.01, 0.3)))
+        else:
+            m = s.add_material(abi.MAT_GLASS, ks=constant(1.0), kt=constant(1.0), ior=1.5)
+        out.append(m)
+    return out
+
+
+def soup_spheres_scene(n_tris, n_spheres=256, seed=1, width=256, height=256, fov=45.0,
+                       env_size=(256, 128)) -> Scene:
+    """A seeded random triangle soup in [-1,1]^3 plus spheres, for the batched
+    workload.  Triangle edges ~U(0.5, 1.5) x 0.0275 x sqrt(2^20 / n_tris)
+    (capped at 0.3), so soups of every size are about as dense as the
+    1M-triangle ray-cast soup; the soup is split into 8 meshes whose
+    materials, and each sphere's (radius ~U(0.02, 0.1)), follow the
+    heightfield workload's mix; a procedural sky and a sun light it."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    s = Scene()
+    scale_e = min(0.3, 0.0275 * np.sqrt((1 << 20) / max(1, n_tris)))
+    c = rng.uniform(-1, 1, size=(n_tris, 3))
+    e1 = _unit_vectors(rng, n_tris) * (rng.uniform(0.5, 1.5, size=(n_tris, 1)) * scale_e)
+    e2 = _unit_vectors(rng, n_tris) * (rng.uniform(0.5, 1.5, size=(n_tris, 1)) * scale_e)
+    verts = np.empty((n_tris, 3, 3), dtype=np.float32)
+    verts[:, 0] = c
+    verts[:, 1] = c + e1
+    verts[:, 2] = c + e2
+    n_mesh = 8
+    mats = _material_mix(s, rng, n_mesh + n_spheres)
+    order = []
+    bounds = np.linspace(0, n_tris, n_mesh + 1).astype(np.int64)
+    for k in range(n_mesh):
+        part = verts[bounds[k]:bounds[k + 1]].reshape(-1, 3)
+        if len(part):
+            order.append(s.add_mesh(part, np.arange(len(part), dtype=np.int32), mats[k]))
+    pos = rng.uniform(-1, 1, (n_spheres, 3))
+    rad = rng.uniform(0.02, 0.1, n_spheres)
+    for k in range(n_spheres):
+        sh = s.add_shape(abi.SHAPE_SPHERE, (float(rad[k]),),
+                         xf.translate(*(float(v) for v in pos[k])), mats[n_mesh + k])
+        order.insert(0, ~sh)
+    s.prim_order = order
+    sun = (0.4, 0.7, 0.3)
+    sd = np.asarray(sun) / np.linalg.norm(sun)
+    s.lights = [S_light(abi.LIGHT_DIRECTIONAL, rgb_to_spectrum((2.6, 2.4, 2.1), illuminant=True),
+                        tuple(float(v) for v in sd)),
+                Light(abi.LIGHT_INFINITE, env=sky_env(env_size[0], env_size[1], sun),
+                      w2l=xf.rotate_x(90))]
+    look = xf.look_at((0.0, 0.6, -3.2), (0.0, 0.0, 0.0), (0, 1, 0))
+    c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, fov, width, height)
+    s.set_camera(c2w, r2c)
+    s.view = (look, fov)
+    return s
+
+
+@dataclass
+class BatchInstance:
+    scene: Scene
+    params: object  # abi.RenderParams
+    n_tris: int
+
+
+def batch_instances(n=64, seed=11, tri_range=(10_000, 2_000_000), side_range=(128, 1024),
+                    strata_range=(2, 16), depth_range=(3, 10), n_spheres=256):
+    """The batched workload: n scene instances, each a seeded soup plus
+    spheres with a triangle count log-uniform in tri_range, a square image
+    whose side is uniform in side_range, spp = sx * sy with sx, sy uniform in
+    strata_range (4 ... 256 spp), and a max depth uniform in depth_range."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(n):
+        nt = int(round(np.exp(rng.uniform(np.log(tri_range[0]), np.log(tri_range[1])))))
+        side = int(rng.integers(side_range[0], side_range[1] + 1))
+        sx = int(rng.integers(strata_range[0], strata_range[1] + 1))
+        sy = int(rng.integers(strata_range[0], strata_range[1] + 1))
+        depth = int(rng.integers(depth_range[0], depth_range[1] + 1))
+        sc = soup_spheres_scene(nt, n_spheres=n_spheres, seed=seed * 1000 + k, width=side,
+                                height=side)
+        p = render_params(side, side, (sx, sy), max_depth=depth, sample_depth=3, rr_depth=3,
+                          filter_kind=abi.FILTER_BOX, seed=seed * 1000 + k)
+        out.append(BatchInstance(sc, p, nt))
+    return out
+
+
+# ---------------------------------------------------------------- serving workload
+SERVING_TRIANGLES = (100_000, 200_000, 300_000, 500_000, 700_000, 1_000_000, 1_200_000, 2_000_000)
+
+
+def serving_scenes(seed=31, triangles=SERVING_TRIANGLES, n_spheres=512):
+    """Resident scenes of the serving workload (6M triangles in all): even
+    entries a heightfield of about that many triangles plus spheres, odd
+    entries a soup plus spheres, materials and lighting as in the heightfield
+    workload."""
+    out = []
+    for k, nt in enumerate(triangles):
+        if k % 2 == 0:
+            ns = int(round(np.sqrt(nt / 2))) + 1
+            out.append(heightfield_scene(ns=ns, n_spheres=n_spheres, seed=seed + k, width=256,
+                                         height=256, env_size=(256, 128)))
+        else:
+            out.append(soup_spheres_scene(nt, n_spheres=n_spheres, seed=seed + k, width=256,
+                                          height=256))
+    return out
+
+
+@dataclass
+class ServingJob:
+    arrival: float  # seconds after the first arrival
+    scene: int
+    params: object  # abi.RenderParams
+    pass_index: int
+
+
+def serving_jobs(n=64, rate=200.0, n_scenes=8, seed=41, side_range=(128, 1024),
+                 spp_range=(16, 512), max_depth=8):
+    """n jobs arriving as a Poisson process of `rate` per second, each on a
+    uniformly chosen scene, with a square image whose side is log-uniform in
+    side_range and spp log-uniform in spp_range (stratified sx x sy, sx the
+    rounded square root)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    out = []
+    for k in range(n):
+        if k:
+            t += float(rng.exponential(1.0 / rate))
+        side = int(round(np.exp(rng.uniform(np.log(side_range[0]), np.log(side_range[1])))))
+        spp = float(np.exp(rng.uniform(np.log(spp_range[0]), np.log(spp_range[1]))))
+        sx = max(1, int(round(np.sqrt(spp))))
+        sy = max(1, int(round(spp / sx)))
+        p = render_params(side, side, (sx, sy), max_depth=max_depth, sample_depth=3, rr_depth=3,
+                          filter_kind=abi.FILTER_BOX, seed=int(rng.integers(1, 1 << 30)))
+        out.append(ServingJob(t, int(rng.integers(0, n_scenes)), p, k))
+    return out

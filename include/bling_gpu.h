@@ -245,6 +245,19 @@ int bling_trace_counts(bling_scene* scene, const float* rays, size_t n, uint64_t
 
 /* ---- films and passes ---- */
 int bling_film_create(bling_ctx* ctx, int32_t width, int32_t height, bling_film** out);
+/* BLING_FILM_FP64: compensated accumulation for long renders (thousands of
+ * samples per pixel).  Samples are added to an FP32 film by the kernels as
+ * usual; after every bling_render_pass the pass's FP32 sums are added into
+ * FP64 totals and the FP32 film is zeroed, so FP32 only ever sums one pass.
+ * bling_film_read returns the totals rounded once to float;
+ * bling_film_read_f64 returns them as doubles.  Batched jobs write the FP32
+ * part; bling_film_fold folds it (reads fold too).  The reference film is
+ * FP32 (Image.hs:39-82): its sums stay within its rounding. */
+#define BLING_FILM_FP64 1u
+int bling_film_create_ex(bling_ctx* ctx, int32_t width, int32_t height, uint32_t flags,
+                         bling_film** out);
+int bling_film_fold(bling_film* film);
+int bling_film_read_f64(bling_film* film, double* host_wxyz);
 void bling_film_destroy(bling_film* film);
 int bling_film_clear(bling_film* film);
 /* copies the (weight, X, Y, Z) film, width*height*4 floats (Image.hs:64-82) */
@@ -258,6 +271,12 @@ int bling_film_resolve(bling_film* film, float* host_rgb);
  * the film.  `pass` selects the random stream (seed, pass). */
 int bling_render_pass(bling_scene* scene, bling_film* film, const bling_render_params* params,
                       uint64_t pass);
+/* The same pass through another camera (NULL: the scene's), for an image
+ * size the scene's camera was not built for (the reference builds the camera
+ * for the image size, Camera.hs:108-147). */
+int bling_render_pass_camera(bling_scene* scene, bling_film* film,
+                             const bling_render_params* params, const bling_camera_desc* camera,
+                             uint64_t pass);
 
 int bling_scene_stats(bling_scene* scene, bling_stats* out);
 
@@ -284,6 +303,118 @@ int bling_scene_stats(bling_scene* scene, bling_stats* out);
  *  - Counters, statistics and errors are as for bling_render_pass. */
 int bling_render_pass_noalloc(bling_scene* scene, const bling_render_params* params, uint64_t pass,
                               float* d_film_wxyz);
+
+/* ---- batched jobs: one persistent wavefront over many render jobs ----
+ * No counterpart in the reference, whose renderer runs one job at a time
+ * (Renderer.render, Rendering.hs:77-78).  A job is one bling_render_pass of a
+ * scene into a film; a batch keeps a fixed pool of path slots that started
+ * paths never leave until they end, and hands free slots the next samples of
+ * the submitted jobs in submission order (path regeneration), so the ray
+ * queues stay full across jobs of different scenes, sizes, sample counts and
+ * depths.  A job's film gets the same samples, with the same random numbers,
+ * as bling_render_pass(scene, film, params, pass) would add, up to the order
+ * of the float additions into the film.
+ *
+ *  - Scenes and films must belong to the batch's context, and all scenes of a
+ *    batch must share the BVH layout (BLING_FLAG_WIDE_BVH); they must outlive
+ *    the batch's use of them.  A film must not be read, cleared or rendered
+ *    by other calls while a job writes it.
+ *  - bling_batch_submit only enqueues; bling_batch_step runs `iterations`
+ *    wavefront iterations (each advances every live path by one bounce and
+ *    starts new paths in free slots) and synchronises; bling_batch_run steps
+ *    until every submitted job is complete.
+ *  - Jobs may be submitted between steps while others are in flight
+ *    (continuous batching).  The job table holds max_jobs incomplete jobs;
+ *    a submit beyond that returns BLING_ERR_STATE. */
+typedef struct bling_batch bling_batch;
+
+#define BLING_BATCH_PLAIN_LAUNCHES 0 /* each iteration's kernels launched one by one */
+#define BLING_BATCH_GRAPH 1          /* each iteration replayed from one CUDA graph */
+#define BLING_BATCH_DEVICE_LOOP 2    /* a conditional (while) graph runs up to
+                                        iters_per_launch iterations per launch and
+                                        stops early when no work is left */
+
+typedef struct bling_batch_opts {
+  int64_t slots;            /* path slots, the capacity of every queue; 0 = 2^21 */
+  int32_t block_size;       /* threads per block, 64 or 128; 0 = 128 */
+  int32_t max_jobs;         /* job table entries, a power of two; 0 = 1024 */
+  int32_t sort_rays;        /* 1: bin each iteration's bounce rays by scene, direction
+                               octant and origin cell (Morton order) before tracing */
+  int32_t graph_mode;       /* BLING_BATCH_* ; default (0 given) is plain launches */
+  int32_t iters_per_launch; /* BLING_BATCH_DEVICE_LOOP only; 0 = 16 */
+  int32_t reserved;
+} bling_batch_opts;
+
+typedef struct bling_batch_stats {
+  uint64_t rays_closest, rays_any, path_samples, nonfinite_drops, degenerate_rays;
+  uint64_t iterations, samples_submitted, samples_started;
+  int64_t jobs_submitted, jobs_done, jobs_active;
+  uint64_t device_bytes;
+} bling_batch_stats;
+
+int bling_batch_create(bling_ctx* ctx, const bling_batch_opts* opts, bling_batch** out);
+void bling_batch_destroy(bling_batch* batch);
+/* camera: NULL renders through the scene's camera; a job at another image
+ * size than the scene's camera was made for passes its own camera (the
+ * reference builds the camera for the image size, Camera.hs:108-147) */
+int bling_batch_submit(bling_batch* batch, bling_scene* scene, bling_film* film,
+                       const bling_render_params* params, const bling_camera_desc* camera,
+                       uint64_t pass, int64_t* job_id);
+int bling_batch_step(bling_batch* batch, int32_t iterations);
+int bling_batch_run(bling_batch* batch);
+/* samples finished and submitted of a job; done == total once it is complete */
+int bling_batch_job_status(bling_batch* batch, int64_t job_id, uint64_t* samples_done,
+                           uint64_t* samples_total);
+int bling_batch_stats_get(bling_batch* batch, bling_batch_stats* out);
+
+/* ---- render server: continuous batching of render jobs ----
+ * No counterpart in the reference.  Scenes stay resident (their BVHs in
+ * device memory); callers on any thread submit jobs, each one pass of a
+ * scene at its own size, sample count, depth and camera.  A worker thread
+ * admits jobs in arrival order while the device memory budget -- the
+ * batch's path state plus 16 bytes per pixel of every admitted job's film --
+ * and the job table allow, merges their samples into one shared wavefront
+ * (a bling_batch) and runs it `iters_per_step` iterations at a time; jobs
+ * arriving meanwhile join at the next step.  A finished film is copied to
+ * the host and its device memory released; bling_server_wait hands it over.
+ * Each job's film is the one bling_render_pass would produce for it, up to
+ * the order of the float additions.  Scenes must outlive their jobs.  The
+ * server uses the context's stream of the moment it was created. */
+typedef struct bling_server bling_server;
+
+typedef struct bling_server_opts {
+  bling_batch_opts batch;    /* the shared wavefront; graph_mode 0 selects BLING_BATCH_GRAPH */
+  uint64_t hbm_budget_bytes; /* path state + films of admitted jobs; 0 = 40 GiB */
+  int32_t iters_per_step;    /* wavefront iterations between admission rounds; 0 = 4 */
+  int32_t reserved;
+} bling_server_opts;
+
+typedef struct bling_job_times {
+  double submitted, admitted, finished; /* seconds since the server was created */
+  uint64_t samples;                     /* path samples of the job */
+} bling_job_times;
+
+typedef struct bling_server_stats {
+  int64_t jobs_submitted, jobs_admitted, jobs_done, jobs_failed, jobs_running, jobs_pending;
+  uint64_t samples_done, rays_closest, rays_any, iterations;
+  uint64_t budget_bytes, bytes_in_use, peak_bytes_in_use;
+} bling_server_stats;
+
+int bling_server_create(bling_ctx* ctx, const bling_server_opts* opts, bling_server** out);
+/* finishes the admitted jobs; pending ones fail with BLING_ERR_STATE */
+void bling_server_destroy(bling_server* server);
+/* thread-safe; camera NULL = the scene's camera.  A job whose film alone
+ * exceeds the budget is refused with BLING_ERR_BOUNDS. */
+int bling_server_submit(bling_server* server, bling_scene* scene, const bling_render_params* params,
+                        const bling_camera_desc* camera, uint64_t pass, int64_t* ticket);
+/* blocks until the job is done (timeout_ms < 0: no limit; BLING_ERR_TIMEOUT
+ * otherwise), copies its (w, X, Y, Z) film to host_wxyz (width*height*4
+ * floats, may be NULL) and its timestamps to times (may be NULL), and
+ * forgets the ticket.  A failed job returns its error code. */
+int bling_server_wait(bling_server* server, int64_t ticket, int32_t timeout_ms, float* host_wxyz,
+                      bling_job_times* times);
+int bling_server_stats_get(bling_server* server, bling_server_stats* out);
+const char* bling_server_last_error(bling_server* server);
 
 /* ---- host helpers for building scenes (no GPU needed) ---- */
 /* Builds the BVH of n primitive boxes (lo/hi: 3n floats each) on the host and
