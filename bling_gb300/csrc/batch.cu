@@ -58,6 +58,7 @@ struct BatchCtl {
   unsigned long long c[C_COUNT];   // C_LIVE0 + b: paths in buffer b; queue sizes, statistics
   int cur;                         // the buffer traced this iteration
   int pad2;
+  unsigned cls[32];                // shading-class counts [0, 16) and cursors [16, 32)
 };
 
 // the per-path state that moves between the two buffers
@@ -81,9 +82,11 @@ struct BatchQueues {
   int32_t* mis;
   int32_t* resolve;
   uint32_t* keys;      // bin key per path
+  int32_t* order;      // positions of the current buffer in shading-class order
+  int32_t* cls;        // shading class per position
   unsigned int* bins;  // kBins counters / offsets
 };
-constexpr size_t kQueueWordsB = 4;
+constexpr size_t kQueueWordsB = 6;
 
 // vertex temporaries (everything of Slots but T, L and ray), single-buffered
 constexpr size_t kTempWords = kSlotWords - 16 - 16 - 7;
@@ -155,6 +158,7 @@ __global__ void k_iter_begin(BatchCtl* ctl, unsigned long long cap) {
   ctl->c[C_RESOLVE] = 0;
   ctl->c[C_NEXT_SHADOW] = 0;
   ctl->c[C_NEXT_MIS] = 0;
+  for (int k = 0; k < 32; k++) ctl->cls[k] = 0;
 }
 
 // the job owning sample g: the last of jobs [lo, hi) whose first sample is <= g
@@ -210,24 +214,32 @@ __global__ void __launch_bounds__(128) k_bin_count(BatchCtl* ctl,
   const int cur = ctl->cur;
   const unsigned long long n = ctl->c[C_LIVE0 + cur];
   const PathState& S = ps.b[cur];
-  for (unsigned long long q = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
-       q += (unsigned long long)gridDim.x * blockDim.x) {
-    int sc = S.scene[q];
-    const BatchSceneDev& B = scenes[sc];
-    uint32_t cell = 0, oct = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  const unsigned long long nround = (n + stride - 1) / stride * stride;
+  const int lane = threadIdx.x & 31;
+  for (unsigned long long q = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+       q < nround; q += stride) {
+    uint32_t key = 0xffffffffu;
+    if (q < n) {
+      int sc = S.scene[q];
+      const BatchSceneDev& B = scenes[sc];
+      uint32_t cell = 0, oct = 0;
 #pragma unroll
-    for (int a = 0; a < 3; a++) {
-      float o = S.ray[a * cap + q], d = S.ray[(3 + a) * cap + q];
-      float ext = B.hi[a] - B.lo[a];
-      float u = ext > 0 ? (o - B.lo[a]) / ext : 0.0f;
-      int v = (int)(u * 8.0f);
-      v = v < 0 ? 0 : (v > 7 ? 7 : v);  // NaN -> 0
-      cell |= spread3((uint32_t)v) << a;
-      oct |= (signbit(d) ? 1u : 0u) << a;
+      for (int a = 0; a < 3; a++) {
+        float o = S.ray[a * cap + q], d = S.ray[(3 + a) * cap + q];
+        float ext = B.hi[a] - B.lo[a];
+        float u = ext > 0 ? (o - B.lo[a]) / ext : 0.0f;
+        int v = (int)(u * 8.0f);
+        v = v < 0 ? 0 : (v > 7 ? 7 : v);  // NaN -> 0
+        cell |= spread3((uint32_t)v) << a;
+        oct |= (signbit(d) ? 1u : 0u) << a;
+      }
+      key = ((uint32_t)(sc & 63) << 10) | (oct << 7) | (cell >> 2);
+      Q.keys[q] = key;
     }
-    uint32_t key = ((uint32_t)(sc & 63) << 10) | (oct << 7) | (cell >> 2);
-    Q.keys[q] = key;
-    atomicAdd(Q.bins + key, 1u);
+    // one atomic per distinct key in the warp
+    unsigned grp = __match_any_sync(0xffffffffu, key);
+    if (key != 0xffffffffu && lane == __ffs(grp) - 1) atomicAdd(Q.bins + key, (unsigned)__popc(grp));
   }
 }
 
@@ -260,10 +272,20 @@ __global__ void __launch_bounds__(128) k_bin_scatter(BatchCtl* ctl, PathStates p
   const unsigned long long n = ctl->c[C_LIVE0 + cur];
   const PathState& from = ps.b[cur];
   const PathState& to = ps.b[1 - cur];
-  for (unsigned long long q = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
-       q += (unsigned long long)gridDim.x * blockDim.x) {
-    unsigned int p = atomicAdd(Q.bins + Q.keys[q], 1u);
-    moveState(from, (int)q, to, (int)p, cap);
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  const unsigned long long nround = (n + stride - 1) / stride * stride;
+  const int lane = threadIdx.x & 31;
+  for (unsigned long long q = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+       q < nround; q += stride) {
+    uint32_t key = q < n ? Q.keys[q] : 0xffffffffu;
+    // one atomic per distinct key in the warp; lanes take consecutive positions
+    unsigned grp = __match_any_sync(0xffffffffu, key);
+    int leader = __ffs(grp) - 1;
+    unsigned base = 0;
+    if (key != 0xffffffffu && lane == leader) base = atomicAdd(Q.bins + key, (unsigned)__popc(grp));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (key != 0xffffffffu)
+      moveState(from, (int)q, to, (int)(base + __popc(grp & ((1u << lane) - 1))), cap);
   }
 }
 
@@ -337,6 +359,40 @@ __global__ void __launch_bounds__(128) k_btrace_mis(BatchCtl* ctl,
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ctl->c + C_CLOSEST, (unsigned long long)n);
 }
 
+// shading class of every path of the current buffer (after its closest hit)
+__global__ void __launch_bounds__(128) k_bclass_count(BatchCtl* ctl,
+                                                      const BatchSceneDev* __restrict__ scenes,
+                                                      Slots tmp, PathStates ps, BatchQueues Q) {
+  const int cur = ctl->cur;
+  const PathState& S = ps.b[cur];
+  int64_t n = (int64_t)ctl->c[C_LIVE0 + cur];
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t nround = (n + stride - 1) / stride * stride;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
+    int c = -1;
+    if (q < n) {
+      const BatchSceneDev& SC = scenes[S.scene[q]];
+      c = shadeClass(SC.A, SC.S, tmp.hit_prim[q]);
+      Q.cls[q] = c;
+    }
+    classCount(c, ctl->cls);
+  }
+}
+
+// the positions of the current buffer in shading-class order
+__global__ void __launch_bounds__(128) k_bclass_scatter(BatchCtl* ctl, BatchQueues Q) {
+  __shared__ unsigned off[kShadeClasses];
+  classOffsets(ctl->cls, off);
+  int64_t n = (int64_t)ctl->c[C_LIVE0 + ctl->cur];
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t nround = (n + stride - 1) / stride * stride;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
+    int c = q < n ? Q.cls[q] : -1;
+    int p = classSlot(c, off, ctl->cls + 16);
+    if (c >= 0) Q.order[p] = (int32_t)q;
+  }
+}
+
 // a warp's finished paths: their jobs' sample counts go up (one atomic per
 // job present in the warp)
 __device__ __forceinline__ void pathsDone(bool fin, int job, BatchCtl* ctl,
@@ -349,7 +405,7 @@ __device__ __forceinline__ void pathsDone(bool fin, int job, BatchCtl* ctl,
   if (b && lane == 0) atomicAdd(&ctl->finished, (unsigned long long)__popc(b));
 }
 
-__global__ void __launch_bounds__(128) k_bshade(BatchCtl* ctl, const BatchJobDev* __restrict__ jobs,
+__global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJobDev* __restrict__ jobs,
                                                 const BatchSceneDev* __restrict__ scenes,
                                                 Slots tmp, PathStates ps, BatchQueues Q,
                                                 unsigned long long* __restrict__ job_done) {
@@ -360,11 +416,13 @@ __global__ void __launch_bounds__(128) k_bshade(BatchCtl* ctl, const BatchJobDev
   int64_t n = (int64_t)c[C_LIVE0 + cur];
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += stride) {
     VertexOut o{false, false, false};
     bool fin = false;
     int job = -1;
-    if (q < n) {
+    int q = 0;
+    if (i < n) {
+      q = Q.order[i];  // shading-class order
       job = S.job[q];
       const BatchJobDev& J = jobs[job];
       const BatchSceneDev& SC = scenes[S.scene[q]];
@@ -383,7 +441,7 @@ __global__ void __launch_bounds__(128) k_bshade(BatchCtl* ctl, const BatchJobDev
 
 // the vertex's radiance; continuing paths move to the next free position of
 // the other buffer, finished ones are splatted into their job's film
-__global__ void __launch_bounds__(128) k_bresolve(BatchCtl* ctl,
+__global__ void __launch_bounds__(128, 3) k_bresolve(BatchCtl* ctl,
                                                   const BatchJobDev* __restrict__ jobs,
                                                   const BatchSceneDev* __restrict__ scenes,
                                                   Slots tmp, PathStates ps, BatchQueues Q,
@@ -523,6 +581,8 @@ cudaError_t enqueueIterationT(BatchEngine* b, int use_cond, unsigned long long m
     k_bin_flip<<<1, 32, 0, s>>>(b->d_ctl);
   }
   k_btrace<WIDE><<<b->g_trace, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps);
+  k_bclass_count<<<b->g_bin, 128, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
+  k_bclass_scatter<<<b->g_bin, 128, 0, s>>>(b->d_ctl, b->q);
   k_bshade<<<b->g_shade, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps, b->q,
                                      b->d_job_done);
   k_btrace_shadow<WIDE><<<b->g_shadow, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
@@ -686,6 +746,8 @@ int batch_create(int device, cudaStream_t stream, const BatchConfig& cfg, BatchE
   b->q.mis = (int32_t*)take(1);
   b->q.resolve = (int32_t*)take(1);
   b->q.keys = (uint32_t*)take(1);
+  b->q.order = (int32_t*)take(1);
+  b->q.cls = (int32_t*)take(1);
   b->q.bins = (unsigned int*)w;
   BRET(cudaMalloc(&b->d_ctl, sizeof(BatchCtl)));
   BRET(cudaMalloc(&b->d_jobs, sizeof(BatchJobDev) * cfg.max_jobs));

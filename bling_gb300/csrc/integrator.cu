@@ -48,6 +48,12 @@ static void carve(unsigned char* base, size_t cap, Slots& st, Queues& q,
   q.shadow = qw + 2 * cap;
   q.mis = qw + 3 * cap;
   q.resolve = qw + 4 * cap;
+  q.sorted = qw + 5 * cap;
+  q.cls = qw + 6 * cap;
+}
+
+__device__ __forceinline__ unsigned* classCounts(unsigned long long* counters) {
+  return (unsigned*)counters + kClassCountsAt;
 }
 
 // the pass's filter table, in constant memory
@@ -80,6 +86,44 @@ __global__ void k_bounce_reset(unsigned long long* counters, int next_live) {
   if (t == 4) counters[C_RESOLVE] = 0;
   if (t == 5) counters[C_NEXT_SHADOW] = 0;
   if (t == 6) counters[C_NEXT_MIS] = 0;
+  if (t < 32) classCounts(counters)[t] = 0;  // class counts [0, 16) and cursors [16, 32)
+}
+
+// shading class of every live path (after its closest hit)
+__global__ void __launch_bounds__(128) k_class_count(DevAccel A, DevShading S, Slots st,
+                                                     const int32_t* __restrict__ queue,
+                                                     const unsigned long long* __restrict__ qcount,
+                                                     int32_t* __restrict__ cls,
+                                                     unsigned long long* __restrict__ counters) {
+  int64_t n = (int64_t)*qcount;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t nround = (n + stride - 1) / stride * stride;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
+    int c = -1;
+    if (q < n) {
+      c = shadeClass(A, S, st.hit_prim[queue[q]]);
+      cls[q] = c;
+    }
+    classCount(c, classCounts(counters));
+  }
+}
+
+// the live queue in shading-class order
+__global__ void __launch_bounds__(128) k_class_scatter(const int32_t* __restrict__ queue,
+                                                       const unsigned long long* __restrict__ qcount,
+                                                       const int32_t* __restrict__ cls,
+                                                       int32_t* __restrict__ sorted,
+                                                       unsigned long long* __restrict__ counters) {
+  __shared__ unsigned off[kShadeClasses];
+  classOffsets(classCounts(counters), off);
+  int64_t n = (int64_t)*qcount;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t nround = (n + stride - 1) / stride * stride;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
+    int c = q < n ? cls[q] : -1;
+    int p = classSlot(c, off, classCounts(counters) + 16);
+    if (c >= 0) sorted[p] = queue[q];
+  }
 }
 
 // closest hit of the live paths' rays (scIntersect)
@@ -134,12 +178,12 @@ __global__ void __launch_bounds__(128) k_trace_mis(DevAccel A, Slots st,
 }
 
 // one vertex of every live path, up to its shadow and MIS rays (Path.hs:49-87)
-__global__ void __launch_bounds__(128) k_shade(DevAccel A, DevShading S, PassParams P, Slots st,
+__global__ void __launch_bounds__(128, 3) k_shade(DevAccel A, DevShading S, PassParams P, Slots st,
                                                Queues Q, int depth, int live_in,
                                                float* __restrict__ film,
                                                unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[live_in];
-  const int32_t* __restrict__ qin = Q.live[live_in];
+  const int32_t* __restrict__ qin = Q.sorted;  // the live paths in shading-class order
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;  // whole warps stay together for the appends
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
@@ -238,6 +282,10 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
       k_trace<true><<<gt, block, 0, stream>>>(A, st, Q.live[in], counters + C_LIVE0 + in, counters);
     else
       k_trace<false><<<gt, block, 0, stream>>>(A, st, Q.live[in], counters + C_LIVE0 + in, counters);
+    k_class_count<<<G.raygen, block, 0, stream>>>(A, S, st, Q.live[in], counters + C_LIVE0 + in,
+                                                   Q.cls, counters);
+    k_class_scatter<<<G.raygen, block, 0, stream>>>(Q.live[in], counters + C_LIVE0 + in, Q.cls,
+                                                     Q.sorted, counters);
     k_shade<<<std::min(G.shade, cap_blocks), block, 0, stream>>>(A, S, P, st, Q, depth,
                                                                   C_LIVE0 + in, d_film, counters);
     if (A.wide) {

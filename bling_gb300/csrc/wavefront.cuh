@@ -45,6 +45,8 @@ struct Queues {
   int32_t* shadow;
   int32_t* mis;
   int32_t* resolve;
+  int32_t* sorted;   // the live paths in shading-class order
+  int32_t* cls;      // shading class per live queue entry
 };
 
 // counters (unsigned long long): queue sizes and statistics
@@ -55,8 +57,11 @@ enum : int {
 };
 
 constexpr size_t kSlotWords = 16 * 6 + 7 + 4 + 3 + 8 + 1 + 7 + 4;  // per slot, 4-byte words
-constexpr size_t kQueueWords = 5;
+constexpr size_t kQueueWords = 7;
+// counters: C_COUNT 8-byte counters, then the shading-class counts and
+// cursors (kShadeClasses 4-byte entries each, 16 reserved)
 constexpr size_t kCounterBytes = 256;
+constexpr int kClassCountsAt = C_COUNT * 2;  // in 4-byte words
 
 // carves the slot arrays (kSlotWords per slot) from w, advancing it
 inline void carveSlots(float*& w, size_t cap, Slots& st) {
@@ -162,6 +167,59 @@ __device__ __forceinline__ void queueAppend(bool live, int slot, int32_t* __rest
   if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(ballot));
   base = __shfl_sync(mask, base, leader);
   if (live) queue[base + __popc(ballot & ((1u << lane) - 1))] = slot;
+}
+
+// ---- shading classes.  Before shading, the live paths of a bounce are
+// reordered by what their vertex runs: 0 for a miss or a degenerate ray (the
+// path ends), else 1 + the hit material's kind + 4 for an analytic shape
+// (triangles and shapes build their geometry differently).  Lanes of a warp
+// then run one BSDF's and one geometry's code instead of all of them in turn.
+// The order within a class is the queue's order, up to the interleaving of
+// warps.
+constexpr int kShadeClasses = 9;
+
+__device__ __forceinline__ int shadeClass(const DevAccel& A, const DevShading& S, int prim) {
+  if (prim < 0) return 0;
+  int2 info = __ldg(S.prim_info + prim);
+  int mi, shape = 0;
+  if (info.x >= 0) {
+    mi = S.meshes[info.x].material;
+  } else {
+    mi = A.shapes[~info.x].material;
+    shape = 1;
+  }
+  return 1 + (S.materials[mi].kind & 3) + 4 * shape;
+}
+
+// counts a warp's entries per class (one atomic per class present); every
+// lane of the warp calls it, c < 0 for lanes without an entry
+__device__ __forceinline__ void classCount(int c, unsigned* __restrict__ counts) {
+  unsigned grp = __match_any_sync(0xffffffffu, c);
+  if (c >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(counts + c, (unsigned)__popc(grp));
+}
+
+// the entry's position in the class-sorted order: the class's offset (off,
+// exclusive prefix of the counts) plus its rank; every lane calls it
+__device__ __forceinline__ int classSlot(int c, const unsigned* off, unsigned* __restrict__ cursor) {
+  const int lane = threadIdx.x & 31;
+  unsigned grp = __match_any_sync(0xffffffffu, c);
+  int leader = __ffs(grp) - 1;
+  unsigned base = 0;
+  if (c >= 0 && lane == leader) base = atomicAdd(cursor + c, (unsigned)__popc(grp));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  return c >= 0 ? (int)(off[c] + base + __popc(grp & ((1u << lane) - 1))) : -1;
+}
+
+// exclusive prefix of the class counts into shared memory (block-wide)
+__device__ __forceinline__ void classOffsets(const unsigned* __restrict__ counts, unsigned* off) {
+  if (threadIdx.x == 0) {
+    unsigned run = 0;
+    for (int c = 0; c < kShadeClasses; c++) {
+      off[c] = run;
+      run += counts[c];
+    }
+  }
+  __syncthreads();
 }
 
 // intLe (Primitive.hs:68-76) + lEmit (Light.hs:85-96)

@@ -570,6 +570,25 @@ def batch_instances(n=64, seed=11, tri_range=(10_000, 2_000_000), side_range=(12
     return out
 
 
+# ---------------------------------------------------------------- white furnace
+def furnace_scene(rho=0.5, width=32, height=32, le=1.0) -> Scene:
+    """A Lambertian sphere of albedo rho (radius 1 at the origin) under a
+    uniform environment of radiance le: light leaving the sphere is exactly
+    rho * le, because every reflected ray of a convex object escapes to the
+    environment; background pixels see le."""
+    s = Scene()
+    m = s.add_material(abi.MAT_MATTE, kd=constant(rho))
+    sh = s.add_shape(abi.SHAPE_SPHERE, (1.0,), xf.identity(), m)
+    s.prim_order = [~sh]
+    env = np.full((8, 16, 16), le, np.float32)
+    s.lights = [Light(abi.LIGHT_INFINITE, env=env, w2l=xf.identity())]
+    look = xf.look_at((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), (0, 1, 0))
+    c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, 40.0, width, height)
+    s.set_camera(c2w, r2c)
+    s.view = (look, 40.0)
+    return s
+
+
 # ---------------------------------------------------------------- serving workload
 SERVING_TRIANGLES = (100_000, 200_000, 300_000, 500_000, 700_000, 1_000_000, 1_200_000, 2_000_000)
 

@@ -275,3 +275,27 @@ def test_cornell_oracle_render_is_deterministic_and_finite():
     assert (f1[..., 0] > 0).all()
     y = f1[..., 2] / f1[..., 0]
     assert 0.05 < y.mean() < 2.0
+
+
+def _furnace_ratio(film):
+    """mean Y of the sphere's pixels over the mean Y of the background pixels"""
+    w = film[..., 0]
+    y = film[..., 2] / np.where(w > 0, w, 1)
+    h, wd = y.shape
+    yy, xx = np.mgrid[0:h, 0:wd]
+    r = np.hypot(xx + 0.5 - wd / 2, yy + 0.5 - h / 2)
+    inner = r < 0.25 * wd   # well inside the sphere's disc (radius ~0.39 of the width)
+    outer = r > 0.48 * wd   # background corners
+    return y[inner].mean() / y[outer].mean(), y[outer].mean()
+
+
+def test_white_furnace_oracle():
+    """A Lambertian sphere of albedo 0.5 under a uniform environment reflects
+    exactly 0.5 of it (direct light only: reflected rays of a convex object
+    escape, and a diffuse bounce adds no environment radiance afterwards)."""
+    sc = S.furnace_scene(0.5, 24, 24)
+    p = S.render_params(24, 24, (8, 8), max_depth=3, sample_depth=3, rr_depth=7)
+    film, _ = OracleScene(sc).render_pass(p, 0)
+    ratio, bg = _furnace_ratio(film)
+    assert abs(ratio - 0.5) < 0.01, ratio
+    assert abs(bg - spectrum_to_xyz(constant(1.0))[1]) < 1e-5

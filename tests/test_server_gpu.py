@@ -86,7 +86,9 @@ def test_jobs_arriving_under_load_render_as_alone(gpu_ctx):
                           for j, (_, o) in enumerate(results) if j != k)
     assert st["jobs_done"] == len(jobs) and st["jobs_failed"] == 0
     assert st["samples_done"] == sum(r[1]["samples"] for r in results)
-    assert overlapped > 0  # jobs shared the device
+    spans = [(round(r[1]["submitted"], 4), round(r[1]["admitted"], 4), round(r[1]["finished"], 4))
+             for r in results]
+    assert overlapped > 0, (spans, st)  # jobs shared the device
 
 
 def test_admission_keeps_films_within_the_budget(gpu_ctx):
