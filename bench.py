@@ -44,6 +44,28 @@ N_ANY = N_RAYS // 2
 CPU_SAMPLE_RAYS = 1 << 20
 
 
+def l2_read_peak(device: int):
+    """L2 read bandwidth measured on this GPU by the project's probe kernel
+    (libbling_probe.so: 16-byte ld.global.cg over a 64 MB working set that
+    stays in L2, 20 repeats, 2 blocks of 512 threads per SM); best of 3."""
+    import ctypes as C
+    lib = ROOT / "bling_gb300" / "libbling_probe.so"
+    if not lib.exists():
+        return None
+    L = C.CDLL(str(lib))
+    L.bling_probe_l2_read_gbs.restype = C.c_double
+    L.bling_probe_l2_read_gbs.argtypes = [C.c_int, C.c_size_t, C.c_int, C.c_int,
+                                          C.POINTER(C.c_float), C.POINTER(C.c_size_t)]
+    best, ms, ws = -1.0, C.c_float(), C.c_size_t()
+    for _ in range(3):
+        best = max(best, L.bling_probe_l2_read_gbs(device, 64 << 20, 20, 2, C.byref(ms),
+                                                   C.byref(ws)))
+    if best <= 0:
+        return None
+    return {"gbs": round(best, 1), "working_set_bytes": ws.value, "repeats": 20,
+            "how": "ld.global.cg.v4 over a 64 MB L2-resident working set, best of 3"}
+
+
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -579,6 +601,9 @@ def run_ours(args):
     closest_s = float(np.mean(closest_ms)) / 1e3
     achieved = bytes_per_ray * N_RAYS / closest_s / 1e9
     prof = profile_traffic()
+    l2 = l2_read_peak(local)
+    if l2:
+        l2["traversal_frac"] = round(achieved / l2["gbs"], 4)
 
     if rank == 0:
         cpu = None
@@ -602,7 +627,8 @@ def run_ours(args):
                          "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
                          "nodes_per_ray": round(counts["nodes_per_ray"], 3),
                          "slots_per_ray": round(counts["slots_per_ray"], 3),
-                         "kernel_ms": round(closest_s * 1e3, 4)},
+                         "kernel_ms": round(closest_s * 1e3, 4),
+                         "l2_read_peak": l2},
             "cpu_baseline": cpu,
             "gpu_launches": 2 * args.steps,
             "clocks": clk.summary(),

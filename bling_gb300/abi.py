@@ -26,6 +26,8 @@ MAT_MATTE, MAT_PLASTIC, MAT_METAL, MAT_GLASS = 0, 1, 2, 3
 SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_DISK, SHAPE_CYLINDER = 0, 1, 2, 3, 4
 LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE = 0, 1, 2
 FILTER_BOX, FILTER_GAUSS, FILTER_MITCHELL, FILTER_SINC, FILTER_TRIANGLE = 0, 1, 2, 3, 4
+SAMPLER_STRATIFIED, SAMPLER_RANDOM = 0, 1
+ABI_VERSION = 2  # BLING_ABI_VERSION of include/bling_gpu.h
 
 
 class Opts(C.Structure):
@@ -74,7 +76,8 @@ class RenderParams(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("strata_x", C.c_int32),
                 ("strata_y", C.c_int32), ("max_depth", C.c_int32), ("sample_depth", C.c_int32),
                 ("rr_depth", C.c_int32), ("filter_kind", C.c_int32),
-                ("filter_params", C.c_float * 4), ("seed", C.c_uint64)]
+                ("filter_params", C.c_float * 4), ("seed", C.c_uint64),
+                ("sampler_kind", C.c_int32), ("reserved", C.c_int32)]
 
 
 class Stats(C.Structure):

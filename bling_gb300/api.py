@@ -45,6 +45,9 @@ def lib():
     L = C.CDLL(str(_LIB_PATH))
     P, vp = C.POINTER, C.c_void_p
     L.bling_abi_version.restype = C.c_int
+    if L.bling_abi_version() != abi.ABI_VERSION:
+        raise BlingUnavailable(-3, f"{_LIB_PATH.name} has ABI version {L.bling_abi_version()}, "
+                               f"the bindings expect {abi.ABI_VERSION}: rebuild it")
     L.bling_ctx_create.argtypes = [P(vp), P(abi.Opts)]
     L.bling_ctx_destroy.argtypes = [vp]
     L.bling_last_error.argtypes = [vp]
@@ -119,6 +122,7 @@ class Context:
         o = abi.Opts()
         o.device, o.block_size, o.bvh_leaf_size = device, block_size, bvh_leaf_size
         o.flags = abi.FLAG_WIDE_BVH if wide_bvh else 0
+        self.wide_bvh = wide_bvh
         self.h = C.c_void_p()
         self._children = weakref.WeakSet()  # scenes and films, closed before the context
         rc = L.bling_ctx_create(C.byref(self.h), C.byref(o))

@@ -19,11 +19,13 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libbling_gpu.so"
+PROBE_LIB = PKG / "libbling_probe.so"  # measurement only: the L2 bandwidth probe
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SRCS = ["api.cu", "kernels_trace.cu", "integrator.cu", "scene_upload.cu", "batch.cu",
            "server.cu"]
 CPP_SRCS = ["bvh.cpp"]
+PROBE_SRCS = ["l2probe.cu"]
 HEADERS = ["dmath.cuh", "dshape.cuh", "trace.cuh", "internal.h", "integrator.h", "bvh.h",
            "spectrum_tables.h", "integrator_device.cuh", "filter_host.h"]
 
@@ -63,10 +65,21 @@ def _compile(src: Path, obj: Path, verbose_ptxas: bool):
     return r.stderr
 
 
+def _link(lib: Path, objs, changed: bool):
+    if changed or not lib.exists() or any(o.stat().st_mtime > lib.stat().st_mtime for o in objs):
+        tmp = lib.with_suffix(f".{os.getpid()}.tmp.so")
+        cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs),
+               "-Xcompiler", "-pthread"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+        os.replace(tmp, lib)
+
+
 def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     BUILD.mkdir(exist_ok=True)
     jobs = []
-    for name in CU_SRCS + CPP_SRCS:
+    for name in CU_SRCS + CPP_SRCS + PROBE_SRCS:
         src = CSRC / name
         obj = BUILD / (name + ".o")
         if force or verbose_ptxas or _stale(obj, src):
@@ -75,15 +88,8 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     if jobs:
         with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
             logs = list(ex.map(lambda j: _compile(j[0], j[1], verbose_ptxas), jobs))
-    objs = [BUILD / (n + ".o") for n in CU_SRCS + CPP_SRCS]
-    if jobs or not LIB.exists() or any(o.stat().st_mtime > LIB.stat().st_mtime for o in objs):
-        tmp = LIB.with_suffix(f".{os.getpid()}.tmp.so")
-        cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs),
-               "-Xcompiler", "-pthread"]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB)
+    _link(LIB, [BUILD / (n + ".o") for n in CU_SRCS + CPP_SRCS], bool(jobs))
+    _link(PROBE_LIB, [BUILD / (n + ".o") for n in PROBE_SRCS], bool(jobs))
     if verbose_ptxas:
         for log in logs:
             print(log)

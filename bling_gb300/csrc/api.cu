@@ -132,22 +132,40 @@ void shape_world_bounds(const bling_shape_desc& s, float lo[3], float hi[3]) {
   }
 }
 
-// sampler/integrator/filter parameters of a pass (the checks of bling_render_pass)
-int check_params(bling_ctx* c, const bling_render_params* p) {
-  if (p->width <= 0 || p->height <= 0)
-    return set_err(c, BLING_ERR_INVALID_ARG, "invalid image size %dx%d", p->width, p->height);
+}  // namespace
+
+// sampler/integrator/filter parameters of a pass (the checks of
+// bling_render_pass); touches no shared state, so any thread may call it
+int bgpu::validate_render_params(const bling_render_params* p, std::string& err) {
+  char buf[160];
+  auto fail = [&](const char* msg) {
+    err = msg;
+    return BLING_ERR_INVALID_ARG;
+  };
+  if (p->width <= 0 || p->height <= 0) {
+    snprintf(buf, sizeof buf, "invalid image size %dx%d", p->width, p->height);
+    return fail(buf);
+  }
   if (p->strata_x <= 0 || p->strata_y <= 0 || p->max_depth < 0 || p->sample_depth < 0 ||
       p->strata_x * p->strata_y > 4096)
-    return set_err(c, BLING_ERR_INVALID_ARG, "invalid sampler/integrator parameters");
-  if (p->filter_kind < BLING_FILTER_BOX || p->filter_kind > BLING_FILTER_TRIANGLE)
-    return set_err(c, BLING_ERR_INVALID_ARG, "unknown filter kind %d", p->filter_kind);
+    return fail("invalid sampler/integrator parameters");
+  if (p->filter_kind < BLING_FILTER_BOX || p->filter_kind > BLING_FILTER_TRIANGLE) {
+    snprintf(buf, sizeof buf, "unknown filter kind %d", p->filter_kind);
+    return fail(buf);
+  }
+  if (p->sampler_kind != BLING_SAMPLER_STRATIFIED && p->sampler_kind != BLING_SAMPLER_RANDOM) {
+    snprintf(buf, sizeof buf, "unknown sampler kind %d", p->sampler_kind);
+    return fail(buf);
+  }
+  if (p->reserved != 0) return fail("bling_render_params.reserved must be 0");
   return BLING_OK;
 }
 
-}  // namespace
-
 int bgpu::check_render_params(bling_ctx* c, const bling_render_params* p) {
-  return check_params(c, p);
+  std::string err;
+  int rc = validate_render_params(p, err);
+  if (rc != BLING_OK) return set_err(c, rc, "%s", err.c_str());
+  return BLING_OK;
 }
 
 // acc += pass; pass = 0 (the FP64 accumulator of a BLING_FILM_FP64 film)
@@ -683,11 +701,8 @@ int bling_render_pass_camera(bling_scene* s, bling_film* f, const bling_render_p
   if (p->width != f->width || p->height != f->height)
     return set_err(c, BLING_ERR_INVALID_ARG, "render size %dx%d does not match film %dx%d", p->width,
                    p->height, f->width, f->height);
-  if (p->strata_x <= 0 || p->strata_y <= 0 || p->max_depth < 0 || p->sample_depth < 0 ||
-      p->strata_x * p->strata_y > 4096)
-    return set_err(c, BLING_ERR_INVALID_ARG, "invalid sampler/integrator parameters");
-  if (p->filter_kind < BLING_FILTER_BOX || p->filter_kind > BLING_FILTER_TRIANGLE)
-    return set_err(c, BLING_ERR_INVALID_ARG, "unknown filter kind %d", p->filter_kind);
+  int prc = check_render_params(c, p);
+  if (prc) return prc;
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
   PassResult res{};
@@ -718,13 +733,8 @@ int bling_render_pass_noalloc(bling_scene* s, const bling_render_params* p, uint
                               float* d_film) {
   if (!s || !p || !d_film) return BLING_ERR_INVALID_ARG;
   bling_ctx* c = s->ctx;
-  if (p->width <= 0 || p->height <= 0)
-    return set_err(c, BLING_ERR_INVALID_ARG, "invalid image size %dx%d", p->width, p->height);
-  if (p->strata_x <= 0 || p->strata_y <= 0 || p->max_depth < 0 || p->sample_depth < 0 ||
-      p->strata_x * p->strata_y > 4096)
-    return set_err(c, BLING_ERR_INVALID_ARG, "invalid sampler/integrator parameters");
-  if (p->filter_kind < BLING_FILTER_BOX || p->filter_kind > BLING_FILTER_TRIANGLE)
-    return set_err(c, BLING_ERR_INVALID_ARG, "unknown filter kind %d", p->filter_kind);
+  int prc = check_render_params(c, p);
+  if (prc) return prc;
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
   PassResult res{};
@@ -789,7 +799,7 @@ int bling_batch_submit(bling_batch* b, bling_scene* s, bling_film* f, const blin
   if (p->width != f->width || p->height != f->height)
     return set_err(c, BLING_ERR_INVALID_ARG, "render size %dx%d does not match film %dx%d", p->width,
                    p->height, f->width, f->height);
-  int rc = check_params(c, p);
+  int rc = check_render_params(c, p);
   if (rc) return rc;
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));

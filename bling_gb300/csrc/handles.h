@@ -58,4 +58,6 @@ namespace bgpu {
 // the checks bling_render_pass applies to a job's parameters; sets the
 // context's message and returns a BLING_ERR_* on failure (api.cu)
 int check_render_params(bling_ctx* c, const bling_render_params* p);
+// the same checks without a context: the message goes to err
+int validate_render_params(const bling_render_params* p, std::string& err);
 }  // namespace bgpu

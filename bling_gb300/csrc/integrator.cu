@@ -333,8 +333,11 @@ int integrator_pass_params(const bling_render_params& p, uint64_t pass, int fw, 
   P.nu = p.strata_x;
   P.nv = p.strata_y;
   P.spp = p.strata_x * p.strata_y;
-  P.n1d = 4 * p.sample_depth;
-  P.n2d = 3 * p.sample_depth;
+  P.random = p.sampler_kind == BLING_SAMPLER_RANDOM ? 1 : 0;
+  // stratified dimensions (Path.hs:34-36); the Random sampler has none, its
+  // rnd'/rnd2D' always draw fresh uniforms (Sampling.hs:203-221)
+  P.n1d = P.random ? 0 : 4 * p.sample_depth;
+  P.n2d = P.random ? 0 : 3 * p.sample_depth;
   P.max_depth = p.max_depth;
   P.rr_depth = p.rr_depth;
   P.width = fw;

@@ -222,6 +222,7 @@ struct PassParams {
   int max_depth, rr_depth;
   int width, height;
   float fw, fh;
+  int random;  // Random sampler (Sampling.hs:101-110): no strata, fresh uniforms
   uint64_t chunk_base;
 };
 

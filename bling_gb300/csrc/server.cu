@@ -280,14 +280,10 @@ int bling_server_submit(bling_server* S, bling_scene* s, const bling_render_para
     S->err = "scene belongs to another context";
     return BLING_ERR_INVALID_ARG;
   }
-  // the context lock and the server lock are never held together
-  int prc;
+  // validation touches no shared state: a submission never waits for the
+  // worker, which holds the context lock while the device runs a step
   std::string perr;
-  {
-    std::lock_guard<std::mutex> g(S->ctx->mu);
-    prc = check_render_params(S->ctx, p);
-    if (prc) perr = S->ctx->err;
-  }
+  int prc = validate_render_params(p, perr);
   if (prc) {
     std::lock_guard<std::mutex> lk(S->mu);
     S->err = perr;

@@ -49,16 +49,41 @@ __device__ __forceinline__ bool triTest(const float4 s0, const float4 s1, const 
   return true;
 }
 
+// min/max that return NaN when either operand is NaN (PTX min.NaN/max.NaN)
+__device__ __forceinline__ float fminNaN(float a, float b) {
+  float r;
+  asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float fmaxNaN(float a, float b) {
+  float r;
+  asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+  return r;
+}
+
+// Widens a box's entry/exit distances by kBoxSlack (relative).  An infinite
+// bound stays infinite: n - |n| * s alone would turn +inf into inf - inf =
+// NaN and let a missed box pass.
+__device__ __forceinline__ float widenNear(float n) { return fminf(n, n - fabsf(n) * kBoxSlack); }
+__device__ __forceinline__ float widenFar(float f) { return fmaxf(f, f + fabsf(f) * kBoxSlack); }
+
+// Slab interval of a box.  A ray with a zero direction component (inv = +-inf)
+// is inside that slab for all t when the origin lies strictly between its
+// planes (-inf, +inf), outside for all t when it lies beyond them (+-inf on
+// both planes).  An origin exactly on a plane gives 0 * inf = NaN: the
+// NaN-propagating min/max carry it into the box's interval, and the hit test
+// below (fmaxf/fminf drop NaN) then counts the box as hit, which keeps the
+// traversal conservative for rays that run along a box face.
 __device__ __forceinline__ void boxInterval(float lox, float hix, float loy, float hiy, float loz,
                                             float hiz, const V3& o, const V3& inv, float& tn,
                                             float& tf) {
   float x0 = (lox - o.x) * inv.x, x1 = (hix - o.x) * inv.x;
   float y0 = (loy - o.y) * inv.y, y1 = (hiy - o.y) * inv.y;
   float z0 = (loz - o.z) * inv.z, z1 = (hiz - o.z) * inv.z;
-  float n = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
-  float f = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
-  tn = n - fabsf(n) * kBoxSlack;
-  tf = f + fabsf(f) * kBoxSlack;
+  float n = fmaxNaN(fmaxNaN(fminNaN(x0, x1), fminNaN(y0, y1)), fminNaN(z0, z1));
+  float f = fminNaN(fminNaN(fmaxNaN(x0, x1), fmaxNaN(y0, y1)), fmaxNaN(z0, z1));
+  tn = widenNear(n);
+  tf = widenFar(f);
 }
 
 // work counters of a traversal (the instrumented variant only; the
@@ -216,10 +241,11 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
             float tfx = fmaf(qbyte(i < 4 ? fx0 : fx1, sel), sx, bx);
             float tfy = fmaf(qbyte(i < 4 ? fy0 : fy1, sel), sy, by);
             float tfz = fmaf(qbyte(i < 4 ? fz0 : fz1, sel), sz, bz);
-            float tn = fmaxf(fmaxf(tnx, tny), tnz);
-            float tf = fminf(fminf(tfx, tfy), tfz);
-            tn = tn - fabsf(tn) * kBoxSlack;
-            tf = tf + fabsf(tf) * kBoxSlack;
+            // one plane per axis and side, so a NaN (0 * inf: a zero
+            // direction component) is dropped across axes, which ignores
+            // that axis: conservative
+            float tn = widenNear(fmaxf(fmaxf(tnx, tny), tnz));
+            float tf = widenFar(fminf(fminf(tfx, tfy), tfz));
             uint32_t meta = ((i < 4 ? w1.z : w1.w) >> (8 * (i & 3))) & 0xffu;
             bool h = meta != 0xffu && fmaxf(tn, r.tmin) <= fminf(tf, best_t);
             hits |= (h ? 1u : 0u) << i;

@@ -111,13 +111,23 @@ __device__ __forceinline__ Sampler mkSampler(const PassParams& P, int ix, int iy
   s.n2d = P.n2d;
   return s;
 }
+// the camera sample (runSample, Sampling.hs:101-132): stratified pixel
+// positions and shuffled stratified lens positions, or for the Random sampler
+// four independent uniforms
 __device__ __forceinline__ void pixelSample(const PassParams& P, const Sampler& s, int ix, int iy,
                                             float& sx, float& sy, float& lu, float& lv) {
   float ox, oy;
-  strat2D(s, s.n, DIM_PIX_U, DIM_PIX_V, ox, oy);
-  uint32_t N = (uint32_t)P.spp;
-  uint32_t lp = permute(s.n, N, randU32(s.key, 0xffffffffu, DIM_LENS_PERM));
-  strat2D(s, lp, DIM_LENS_U, DIM_LENS_V, lu, lv);
+  if (P.random) {
+    ox = randF(s.key, s.n, DIM_PIX_U);
+    oy = randF(s.key, s.n, DIM_PIX_V);
+    lu = randF(s.key, s.n, DIM_LENS_U);
+    lv = randF(s.key, s.n, DIM_LENS_V);
+  } else {
+    strat2D(s, s.n, DIM_PIX_U, DIM_PIX_V, ox, oy);
+    uint32_t N = (uint32_t)P.spp;
+    uint32_t lp = permute(s.n, N, randU32(s.key, 0xffffffffu, DIM_LENS_PERM));
+    strat2D(s, lp, DIM_LENS_U, DIM_LENS_V, lu, lv);
+  }
   sx = (float)ix + ox;
   sy = (float)iy + oy;
 }

@@ -176,9 +176,14 @@ class Scene:
 
 
 def render_params(width, height, strata=(4, 4), max_depth=5, sample_depth=3, rr_depth=7,
-                  filter_kind=abi.FILTER_BOX, filter_params=(0, 0, 0, 0), seed=1):
+                  filter_kind=abi.FILTER_BOX, filter_params=(0, 0, 0, 0), seed=1,
+                  sampler=abi.SAMPLER_STRATIFIED):
+    """Sampler renderer + path integrator parameters.  `strata` is (nu, nv) of
+    `Stratified nu nv`; with sampler=SAMPLER_RANDOM, `mkRandomSampler spp` is
+    strata=(spp, 1)."""
     p = abi.RenderParams()
     p.width, p.height = width, height
+    p.sampler_kind = sampler
     p.strata_x, p.strata_y = strata
     p.max_depth, p.sample_depth, p.rr_depth = max_depth, sample_depth, rr_depth
     p.filter_kind = filter_kind

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define BLING_ABI_VERSION 1
+#define BLING_ABI_VERSION 2
 
 #define BLING_OK 0
 #define BLING_ERR_INVALID_ARG (-1)
@@ -172,8 +172,16 @@ enum {
   BLING_FILTER_TRIANGLE = 4  /* params: w, h */
 };
 
-/* One render job: `SamplerRenderer (Stratified nu nv) (mkPathIntegrator md sd)`
- * (Rendering.hs:96-103, Sampling.hs:112-132, Path.hs:30-39). */
+/* Samplers (Sampling.hs:85-132). */
+enum {
+  BLING_SAMPLER_STRATIFIED = 0, /* Stratified nu nv: jittered strata, shuffled dimensions */
+  BLING_SAMPLER_RANDOM = 1      /* Random spp: independent uniforms for every dimension */
+};
+
+/* One render job: `SamplerRenderer sampler (mkPathIntegrator md sd)`
+ * (Rendering.hs:96-103, Sampling.hs:101-132, Path.hs:30-39).  With
+ * BLING_SAMPLER_RANDOM, `mkRandomSampler spp` is strata_x = spp, strata_y = 1:
+ * strata_x * strata_y samples per pixel per pass, none of them stratified. */
 typedef struct bling_render_params {
   int32_t width, height;
   int32_t strata_x, strata_y; /* stratified nu x nv samples per pixel per pass */
@@ -183,6 +191,8 @@ typedef struct bling_render_params {
   int32_t filter_kind;
   float filter_params[4];
   uint64_t seed;
+  int32_t sampler_kind;       /* BLING_SAMPLER_*; 0 = stratified */
+  int32_t reserved;           /* must be 0 */
 } bling_render_params;
 
 typedef struct bling_stats {

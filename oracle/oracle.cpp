@@ -2115,19 +2115,30 @@ static Sampler mkSampler(const bling_render_params* p, uint64_t pass, int px, in
   s.n = (uint32_t)n;
   s.nu = p->strata_x;
   s.nv = p->strata_y;
-  s.n1d = 4 * p->sample_depth;  // Path.hs:34-36
-  s.n2d = 3 * p->sample_depth;
+  // stratified dimensions (Path.hs:34-36); none for the Random sampler, whose
+  // rnd'/rnd2D' always draw fresh uniforms (Sampling.hs:203-221)
+  bool random = p->sampler_kind == BLING_SAMPLER_RANDOM;
+  s.n1d = random ? 0 : 4 * p->sample_depth;
+  s.n2d = random ? 0 : 3 * p->sample_depth;
   return s;
 }
 
 static Spec traceSample(const orc_scene* S, const bling_render_params* p, const Sampler& smp,
                         int px, int py, float& sx, float& sy, Counters& C) {
-  float ox, oy;
-  strat2D(smp, smp.n, DIM_PIX_U, DIM_PIX_V, ox, oy);  // pixel samples are not shuffled
-  uint32_t N = (uint32_t)(p->strata_x * p->strata_y);
-  uint32_t lp = permute(smp.n, N, randU32(smp.key, 0xffffffffu, DIM_LENS_PERM));
-  float lu, lv;
-  strat2D(smp, lp, DIM_LENS_U, DIM_LENS_V, lu, lv);  // lens samples are shuffled
+  float ox, oy, lu, lv;
+  if (p->sampler_kind == BLING_SAMPLER_RANDOM) {
+    // runSample (Random spp): ox, oy, then the lens pair, all uniform
+    // (Sampling.hs:101-110)
+    ox = randF(smp.key, smp.n, DIM_PIX_U);
+    oy = randF(smp.key, smp.n, DIM_PIX_V);
+    lu = randF(smp.key, smp.n, DIM_LENS_U);
+    lv = randF(smp.key, smp.n, DIM_LENS_V);
+  } else {
+    strat2D(smp, smp.n, DIM_PIX_U, DIM_PIX_V, ox, oy);  // pixel samples are not shuffled
+    uint32_t N = (uint32_t)(p->strata_x * p->strata_y);
+    uint32_t lp = permute(smp.n, N, randU32(smp.key, 0xffffffffu, DIM_LENS_PERM));
+    strat2D(smp, lp, DIM_LENS_U, DIM_LENS_V, lu, lv);  // lens samples are shuffled
+  }
   sx = (float)px + ox;
   sy = (float)py + oy;
   Ray r = cameraRay(S, sx, sy, lu, lv);

@@ -299,3 +299,40 @@ def test_white_furnace_oracle():
     ratio, bg = _furnace_ratio(film)
     assert abs(ratio - 0.5) < 0.01, ratio
     assert abs(bg - spectrum_to_xyz(constant(1.0))[1]) < 1e-5
+
+
+def _occupied_strata(o, params, px, py, side):
+    """how many of the side x side pixel strata the pixel's samples fall in"""
+    cells = set()
+    for n in range(side * side):
+        _, ras, _ = o.sample_li(params, 0, px, py, n)
+        fx, fy = ras[0] - px, ras[1] - py
+        assert 0.0 <= fx < 1.0 and 0.0 <= fy < 1.0
+        cells.add((int(fx * side), int(fy * side)))
+    return len(cells)
+
+
+def test_random_sampler_is_not_stratified():
+    """Stratified 8x8 puts one sample in each of the pixel's 64 strata;
+    Random 64 (runSample (Random spp), Sampling.hs:101-110) draws the positions
+    independently, which leaves strata empty (all 64 filled has probability
+    64!/64^64)."""
+    sc = S.cornell_room(8, 8)
+    o = OracleScene(sc)
+    strat = S.render_params(8, 8, (8, 8), max_depth=1)
+    rand = S.render_params(8, 8, (64, 1), max_depth=1, sampler=abi.SAMPLER_RANDOM)
+    for px, py in [(0, 0), (3, 5), (7, 7)]:
+        assert _occupied_strata(o, strat, px, py, 8) == 64
+        assert _occupied_strata(o, rand, px, py, 8) < 60
+
+
+def test_random_sampler_converges_to_the_stratified_image():
+    sc = S.cornell_room(16, 16)
+    o = OracleScene(sc)
+    fs, _ = o.render_pass(S.render_params(16, 16, (8, 8), max_depth=5, rr_depth=3), 0)
+    fr, st = o.render_pass(S.render_params(16, 16, (64, 1), max_depth=5, rr_depth=3,
+                                           sampler=abi.SAMPLER_RANDOM), 0)
+    assert st["path_samples"] == 18 * 18 * 64
+    assert np.array_equal(fs[..., 0], fr[..., 0])  # box filter: 64 samples per pixel on both
+    ys, yr = fs[..., 2].sum() / fs[..., 0].sum(), fr[..., 2].sum() / fr[..., 0].sum()
+    assert abs(yr - ys) < 0.03 * ys, (yr, ys)

@@ -179,6 +179,31 @@ def test_statistical_parity_independent_streams(gpu_ctx):
     assert abs(np.mean(z)) < 0.2  # no bias
 
 
+@pytest.mark.parametrize("strata", [(16, 8), (32, 16)])
+def test_many_strata_per_pixel_vs_oracle(gpu_ctx, strata):
+    """hundreds of stratified samples per pixel and pass (the sampler's
+    permutations over large strata counts).  Depth 1 (camera ray and direct
+    lighting at the first vertex): with deeper paths, a last-bit difference
+    of sinf/cosf sends about one path in a few hundred elsewhere, and with
+    hundreds of samples per pixel most pixels hold one such path."""
+    sc = S.cornell_room(24, 24)
+    p = S.render_params(24, 24, strata, max_depth=1, sample_depth=3, rr_depth=3, seed=5)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p, passes=2)
+    _compare(fg, fo, exact_weights=True)
+    assert st_g["path_samples"] == st_o[0]["path_samples"] * 2
+
+
+def test_random_sampler_vs_oracle(gpu_ctx):
+    """runSample (Random spp) (Sampling.hs:101-110): unstratified camera
+    samples and fresh uniforms in every dimension, on both sides"""
+    sc = S.cornell_room(48, 48)
+    p = S.render_params(48, 48, (8, 1), max_depth=5, sample_depth=3, rr_depth=3, seed=3,
+                        sampler=abi.SAMPLER_RANDOM)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p)
+    _compare(fg, fo, exact_weights=True)
+    assert st_g["path_samples"] == st_o[0]["path_samples"] == 50 * 50 * 8
+
+
 def test_passes_accumulate(gpu_ctx):
     sc = S.cornell_room(32, 32)
     p = S.cornell_params(32, 32, spp_side=2)

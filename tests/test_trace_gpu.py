@@ -70,6 +70,65 @@ def test_1m_soup_vs_oracle_bvh(ctx):
     _check_closest(g, o, sub, brute=True)
 
 
+def _grid_scene(n=96, seed=4):
+    """an n x n-cell height grid on integer x and z coordinates: its BVH boxes
+    have faces on the integer planes"""
+    rng = np.random.default_rng(seed)
+    xs, zs = np.meshgrid(np.arange(n + 1, dtype=np.float32), np.arange(n + 1, dtype=np.float32))
+    ys = rng.uniform(0.0, 0.5, xs.shape).astype(np.float32)
+    v = np.stack([xs.ravel(), ys.ravel(), zs.ravel()], 1)
+    idx = []
+    for j in range(n):
+        for i in range(n):
+            a = j * (n + 1) + i
+            idx += [a, a + 1, a + n + 2, a, a + n + 2, a + n + 1]
+    sc = S.Scene()
+    m = sc.add_material(abi.MAT_MATTE, kd=constant(0.5))
+    sc.add_mesh(v, idx, m)
+    sc.prim_order = [0]
+    return sc
+
+
+def _axis_plane_rays(n, count, seed, zero_axis):
+    """rays whose direction has an exact zero (+0.0 or -0.0) on zero_axis and
+    whose origin lies on an integer plane of that axis"""
+    rng = np.random.default_rng(seed)
+    o = np.stack([rng.integers(0, n + 1, count), np.full(count, 3.0),
+                  rng.integers(0, n + 1, count)], 0).astype(np.float32)
+    o[2 - zero_axis] += rng.uniform(0, 1, count).astype(np.float32)  # the other horizontal axis
+    d = np.stack([rng.uniform(-1, 1, count), rng.uniform(-1, -0.05, count),
+                  rng.uniform(-1, 1, count)], 0).astype(np.float32)
+    d[zero_axis] = np.where(rng.uniform(size=count) < 0.5, np.float32(0.0), np.float32(-0.0))
+    d /= np.linalg.norm(d, axis=0)
+    d[zero_axis] = np.where(rng.uniform(size=count) < 0.5, np.float32(0.0), np.float32(-0.0))
+    rays = np.concatenate([o, d, np.zeros((1, count), np.float32),
+                           np.full((1, count), np.inf, np.float32)]).astype(np.float32)
+    return np.ascontiguousarray(rays)
+
+
+@pytest.mark.parametrize("zero_axis", [0, 2])
+def test_zero_direction_component_on_box_faces(ctx, zero_axis):
+    """rays with a zero direction component that run along BVH box faces (0 *
+    inf in the slab test): same answers as brute force, and no more traversal
+    work than rays tilted off the plane (binary layout; the 8-wide layout
+    ignores the zero axis in the box test, which is conservative but visits
+    more nodes)"""
+    n = 96
+    sc = _grid_scene(n)
+    g, o = ctx.scene(sc), OracleScene(sc)
+    rays = _axis_plane_rays(n, 4096, 8 + zero_axis, zero_axis)
+    t, p = _check_closest(g, o, rays)
+    assert (p >= 0).mean() > 0.5
+    ra = rays.copy()
+    ra[7] = np.where(p >= 0, t, 5.0)  # any hit up to the closest hit
+    assert np.array_equal(g.any(ra), o.any(ra, brute=True))
+    if not ctx.wide_bvh:
+        tilted = rays.copy()
+        tilted[3 + zero_axis] = 1e-3
+        c0, c1 = g.traversal_counts(rays), g.traversal_counts(tilted)
+        assert c0["nodes_per_ray"] <= 3 * c1["nodes_per_ray"], (c0, c1)
+
+
 def test_full_size_closest_is_closest(gpu_ctx):
     """16M rays over the 1M soup: any-hit with tmax just below the reported
     closest t finds nothing, with tmax = t finds the hit."""
