@@ -136,12 +136,13 @@ def test_wait_timeout_and_errors(gpu_ctx):
 def test_submit_does_not_wait_for_the_running_step(gpu_ctx):
     """A job submitted while a long step runs on the device is queued at
     once: submission takes no lock that the worker holds during a step."""
-    sc = S.heightfield_scene(ns=257, n_spheres=64, width=128, height=128, env_size=(64, 32))
+    sc = S.heightfield_scene(ns=257, n_spheres=64, width=256, height=256, env_size=(64, 32))
     g = gpu_ctx.scene(sc)
     srv = Server(gpu_ctx, slots=1 << 20, iters_per_step=64)
-    big = srv.submit(g, S.heightfield_params(128, 128, spp_side=16, max_depth=8), 0)
-    time.sleep(0.05)  # the worker is inside a step by now
-    small = S.heightfield_params(128, 128, spp_side=1, max_depth=3)
+    # 17M path samples: far longer than the submissions below
+    big = srv.submit(g, S.heightfield_params(256, 256, spp_side=16, max_depth=8), 0)
+    time.sleep(0.02)  # the worker is inside a step by now
+    small = S.heightfield_params(256, 256, spp_side=1, max_depth=3)
     t0 = time.perf_counter()
     tickets = [srv.submit(g, small, k) for k in range(8)]
     dt = time.perf_counter() - t0
