@@ -12,6 +12,7 @@ needs it raises :class:`BlingUnavailable`; nothing falls back to the CPU.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import weakref
 from dataclasses import dataclass
@@ -23,6 +24,19 @@ from . import abi
 
 _LIB_PATH = Path(__file__).resolve().parent / "libbling_gpu.so"
 _lib = None
+_live_contexts = weakref.WeakSet()
+
+
+@atexit.register
+def _close_all():
+    """Closes every live context (its scenes, films, batches and servers
+    first) while the interpreter and the CUDA runtime are still intact: at
+    interpreter teardown, objects are finalized in no fixed order."""
+    for ctx in list(_live_contexts):
+        try:
+            ctx.close()
+        except Exception:  # noqa: BLE001 - best effort at exit
+            pass
 
 
 class BlingError(RuntimeError):
@@ -126,6 +140,7 @@ class Context:
         self.h = C.c_void_p()
         self._children = weakref.WeakSet()  # scenes and films, closed before the context
         rc = L.bling_ctx_create(C.byref(self.h), C.byref(o))
+        _live_contexts.add(self)
         if rc != 0:
             msg = L.bling_last_error(self.h).decode() if self.h else "context creation failed"
             if self.h:
@@ -173,7 +188,8 @@ class GpuScene:
 
     def close(self):
         if getattr(self, "h", None):
-            lib().bling_scene_destroy(self.h)
+            if getattr(self.ctx, "h", None):  # a destroyed context took its objects' handles with it
+                lib().bling_scene_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -258,7 +274,8 @@ class Film:
 
     def close(self):
         if getattr(self, "h", None):
-            lib().bling_film_destroy(self.h)
+            if getattr(self.ctx, "h", None):  # a destroyed context took its objects' handles with it
+                lib().bling_film_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -300,7 +317,8 @@ class Batch:
 
     def close(self):
         if getattr(self, "h", None):
-            lib().bling_batch_destroy(self.h)
+            if getattr(self.ctx, "h", None):  # a destroyed context took its objects' handles with it
+                lib().bling_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -363,7 +381,8 @@ class Server:
 
     def close(self):
         if getattr(self, "h", None):
-            lib().bling_server_destroy(self.h)
+            if getattr(self.ctx, "h", None):  # a destroyed context took its objects' handles with it
+                lib().bling_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

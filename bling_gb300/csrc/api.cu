@@ -61,6 +61,97 @@ int ensure_scratch(bling_ctx* c, size_t bytes) {
   return BLING_OK;
 }
 
+// ---- host-buffer ray queries, chunked so that copies overlap traversal
+//
+// The rays (SoA, 8 floats per ray) are copied in, traced and their results
+// copied out chunk by chunk through kPipeBuffers staging buffers: while the
+// kernel traces chunk k on the context's stream, chunk k+1 is copied in on
+// one copy stream and chunk k-1's results are copied out on another.
+constexpr int kPipeBuffers = 3;
+constexpr size_t kPipeChunk = size_t(1) << 21;  // rays per chunk
+
+struct QueryOut {
+  void* host;
+  size_t bytes_per_ray;
+};
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+int ensure_pipeline(bling_ctx* c) {
+  if (c->copy_in) return BLING_OK;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming);
+  for (int b = 0; b < kPipeBuffers && e == cudaSuccess; b++) {
+    e = cudaEventCreateWithFlags(&c->ev_in[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_run[b], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_out[b], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess)
+    return set_err(c, BLING_ERR_CUDA, "copy stream creation: %s", cudaGetErrorString(e));
+  return BLING_OK;
+}
+
+void destroy_pipeline(bling_ctx* c) {
+  if (c->copy_in) cudaStreamDestroy(c->copy_in);
+  if (c->copy_out) cudaStreamDestroy(c->copy_out);
+  if (c->ev_start) cudaEventDestroy(c->ev_start);
+  for (int b = 0; b < kPipeBuffers; b++) {
+    if (c->ev_in[b]) cudaEventDestroy(c->ev_in[b]);
+    if (c->ev_run[b]) cudaEventDestroy(c->ev_run[b]);
+    if (c->ev_out[b]) cudaEventDestroy(c->ev_out[b]);
+  }
+  c->copy_in = c->copy_out = nullptr;
+}
+
+// launch(d_rays, count, d_outs) enqueues the query kernel of one chunk on
+// c->stream; outs[j] receives bytes_per_ray bytes per ray.  Called with c->mu
+// held; returns once every result is in host memory.
+template <class Launch>
+int pipelined_query(bling_ctx* c, const float* rays, size_t n, const QueryOut* outs, int n_outs,
+                    Launch launch) {
+  const size_t chunk = std::min(n, kPipeChunk);
+  size_t slot = align256(32 * chunk);
+  for (int j = 0; j < n_outs; j++) slot += align256(outs[j].bytes_per_ray * chunk);
+  int rc = ensure_scratch(c, kPipeBuffers * slot);
+  if (rc) return rc;
+  rc = ensure_pipeline(c);
+  if (rc) return rc;
+  // the copy streams start after the work already queued on the context's stream
+  CK(c, cudaEventRecord(c->ev_start, c->stream));
+  CK(c, cudaStreamWaitEvent(c->copy_in, c->ev_start, 0));
+  for (size_t i = 0, k = 0; i < n; i += chunk, k++) {
+    const int b = (int)(k % kPipeBuffers);
+    const size_t cn = std::min(chunk, n - i);
+    char* base = (char*)c->d_scratch + b * slot;
+    float* d_r = (float*)base;
+    void* d_out[4] = {nullptr, nullptr, nullptr, nullptr};
+    size_t off = align256(32 * chunk);
+    for (int j = 0; j < n_outs; j++) {
+      d_out[j] = base + off;
+      off += align256(outs[j].bytes_per_ray * chunk);
+    }
+    // the buffer's previous results must be out before new rays come in
+    if (k >= (size_t)kPipeBuffers) CK(c, cudaStreamWaitEvent(c->copy_in, c->ev_out[b], 0));
+    // the chunk's slice of each of the 8 ray rows (o, d, tmin, tmax)
+    for (int row = 0; row < 8; row++)
+      CK(c, cudaMemcpyAsync(d_r + row * cn, rays + row * n + i, cn * sizeof(float),
+                            cudaMemcpyHostToDevice, c->copy_in));
+    CK(c, cudaEventRecord(c->ev_in[b], c->copy_in));
+    CK(c, cudaStreamWaitEvent(c->stream, c->ev_in[b], 0));
+    CK(c, launch(d_r, (int64_t)cn, d_out));
+    CK(c, cudaEventRecord(c->ev_run[b], c->stream));
+    CK(c, cudaStreamWaitEvent(c->copy_out, c->ev_run[b], 0));
+    for (int j = 0; j < n_outs; j++)
+      CK(c, cudaMemcpyAsync((char*)outs[j].host + i * outs[j].bytes_per_ray, d_out[j],
+                            cn * outs[j].bytes_per_ray, cudaMemcpyDeviceToHost, c->copy_out));
+    CK(c, cudaEventRecord(c->ev_out[b], c->copy_out));
+  }
+  // the last copy-out follows the last kernel, which follows every earlier one
+  CK(c, cudaStreamSynchronize(c->copy_out));
+  return BLING_OK;
+}
+
 template <class T>
 int upload(bling_ctx* c, std::vector<void*>& owned, const T* host, size_t count, T** out) {
   *out = nullptr;
@@ -234,6 +325,8 @@ void bling_ctx_destroy(bling_ctx* c) {
       cudaStreamSynchronize(c->own_stream);
       cudaStreamDestroy(c->own_stream);
     }
+    if (c->copy_out) cudaStreamSynchronize(c->copy_out);
+    destroy_pipeline(c);
     if (c->d_scratch) cudaFree(c->d_scratch);
     if (c->d_counter) cudaFree(c->d_counter);
     integrator_workspace_free(c->ws);
@@ -494,20 +587,15 @@ int bling_trace_closest(bling_scene* s, const float* rays, size_t n, float* t, i
   bling_ctx* c = s->ctx;
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
-  size_t rb = 8 * n * sizeof(float), tb = n * 4, pb = n * 4, bb = b1b2 ? 8 * n : 0;
-  int rc = ensure_scratch(c, rb + tb + pb + bb);
+  QueryOut outs[3] = {{t, 4}, {prim, 4}, {b1b2, 8}};
+  int rc = pipelined_query(c, rays, n, outs, b1b2 ? 3 : 2,
+                           [&](const float* d_r, int64_t cn, void** d_out) {
+                             return launch_trace_closest(s->accel, d_r, cn, (float*)d_out[0],
+                                                         (int32_t*)d_out[1],
+                                                         b1b2 ? (float*)d_out[2] : nullptr,
+                                                         c->d_counter, c->stream);
+                           });
   if (rc) return rc;
-  char* base = (char*)c->d_scratch;
-  float* d_r = (float*)base;
-  float* d_t = (float*)(base + rb);
-  int32_t* d_p = (int32_t*)(base + rb + tb);
-  float* d_b = b1b2 ? (float*)(base + rb + tb + pb) : nullptr;
-  CK(c, cudaMemcpyAsync(d_r, rays, rb, cudaMemcpyHostToDevice, c->stream));
-  CK(c, launch_trace_closest(s->accel, d_r, (int64_t)n, d_t, d_p, d_b, c->d_counter, c->stream));
-  CK(c, cudaMemcpyAsync(t, d_t, tb, cudaMemcpyDeviceToHost, c->stream));
-  CK(c, cudaMemcpyAsync(prim, d_p, pb, cudaMemcpyDeviceToHost, c->stream));
-  if (b1b2) CK(c, cudaMemcpyAsync(b1b2, d_b, bb, cudaMemcpyDeviceToHost, c->stream));
-  CK(c, cudaStreamSynchronize(c->stream));
   s->stats.rays_closest += n;
   return BLING_OK;
 }
@@ -518,15 +606,13 @@ int bling_trace_any(bling_scene* s, const float* rays, size_t n, uint8_t* hit) {
   bling_ctx* c = s->ctx;
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
-  size_t rb = 8 * n * sizeof(float);
-  int rc = ensure_scratch(c, rb + n);
+  QueryOut outs[1] = {{hit, 1}};
+  int rc = pipelined_query(c, rays, n, outs, 1,
+                           [&](const float* d_r, int64_t cn, void** d_out) {
+                             return launch_trace_any(s->accel, d_r, cn, (uint8_t*)d_out[0],
+                                                     c->d_counter, c->stream);
+                           });
   if (rc) return rc;
-  float* d_r = (float*)c->d_scratch;
-  uint8_t* d_h = (uint8_t*)c->d_scratch + rb;
-  CK(c, cudaMemcpyAsync(d_r, rays, rb, cudaMemcpyHostToDevice, c->stream));
-  CK(c, launch_trace_any(s->accel, d_r, (int64_t)n, d_h, c->d_counter, c->stream));
-  CK(c, cudaMemcpyAsync(hit, d_h, n, cudaMemcpyDeviceToHost, c->stream));
-  CK(c, cudaStreamSynchronize(c->stream));
   s->stats.rays_any += n;
   return BLING_OK;
 }

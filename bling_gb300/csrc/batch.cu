@@ -64,14 +64,14 @@ struct BatchCtl {
 // the per-path state that moves between the two buffers
 struct PathState {
   unsigned long long* gidx;  // job-relative sample index
-  float* T;                  // 16 x cap
-  float* L;                  // 16 x cap
-  float* ray;                // 7 x cap (sign of tmin: the previous bounce was specular)
+  float* T;                  // 16 per path
+  float* L;                  // 16 per path
+  float* ray;                // 8 per path (sign of tmin: the previous bounce was specular)
   int32_t* job;              // job table index
   int32_t* scene;            // scene table index
   int32_t* depth;            // bounce of the path's current vertex
 };
-constexpr size_t kStateWords = 2 + 16 + 16 + 7 + 3;
+constexpr size_t kStateWords = 2 + 16 + 16 + 8 + 3;
 
 struct PathStates {
   PathState b[2];
@@ -89,7 +89,7 @@ struct BatchQueues {
 constexpr size_t kQueueWordsB = 6;
 
 // vertex temporaries (everything of Slots but T, L and ray), single-buffered
-constexpr size_t kTempWords = kSlotWords - 16 - 16 - 7;
+constexpr size_t kTempWords = kSlotWords - 16 - 16 - 8;
 
 struct JobFilter {
   const float* t;
@@ -121,15 +121,11 @@ __device__ __forceinline__ long long queueSlot(bool live, unsigned long long* co
 }
 
 __device__ __forceinline__ void moveState(const PathState& from, int q, const PathState& to,
-                                          int p, size_t cap) {
+                                          int p) {
   to.gidx[p] = from.gidx[q];
-#pragma unroll
-  for (int b = 0; b < 16; b++) {
-    to.T[b * cap + p] = from.T[b * cap + q];
-    to.L[b * cap + p] = from.L[b * cap + q];
-  }
-#pragma unroll
-  for (int k = 0; k < 7; k++) to.ray[k * cap + p] = from.ray[k * cap + q];
+  storeBands(to.T, p, loadBands(from.T, q));
+  storeBands(to.L, p, loadBands(from.L, q));
+  copyRay(from.ray, q, to.ray, p);
   to.job[p] = from.job[q];
   to.scene[p] = from.scene[q];
   to.depth[p] = from.depth[q];
@@ -193,9 +189,9 @@ __global__ void __launch_bounds__(128) k_regen(BatchCtl* ctl, const BatchJobDev*
     S.depth[q] = 0;
     S.gidx[q] = local;
     Ray ray = cameraRay(J.P, J.cam, local);
-    storeRay(S.ray, cap, q, ray, false);
-    storeBands(S.T, cap, q, sConst(1.0f));
-    storeBands(S.L, cap, q, sConst(0.0f));
+    storeRay(S.ray, q, ray);
+    storeBands(S.T, q, sConst(1.0f));
+    storeBands(S.L, q, sConst(0.0f));
   }
 }
 
@@ -226,7 +222,7 @@ __global__ void __launch_bounds__(128) k_bin_count(BatchCtl* ctl,
       uint32_t cell = 0, oct = 0;
 #pragma unroll
       for (int a = 0; a < 3; a++) {
-        float o = S.ray[a * cap + q], d = S.ray[(3 + a) * cap + q];
+        float o = S.ray[8 * (size_t)q + a], d = S.ray[8 * (size_t)q + 3 + a];
         float ext = B.hi[a] - B.lo[a];
         float u = ext > 0 ? (o - B.lo[a]) / ext : 0.0f;
         int v = (int)(u * 8.0f);
@@ -285,7 +281,7 @@ __global__ void __launch_bounds__(128) k_bin_scatter(BatchCtl* ctl, PathStates p
     if (key != 0xffffffffu && lane == leader) base = atomicAdd(Q.bins + key, (unsigned)__popc(grp));
     base = __shfl_sync(0xffffffffu, base, leader);
     if (key != 0xffffffffu)
-      moveState(from, (int)q, to, (int)(base + __popc(grp & ((1u << lane) - 1))), cap);
+      moveState(from, (int)q, to, (int)(base + __popc(grp & ((1u << lane) - 1))));
   }
 }
 
@@ -309,12 +305,9 @@ __global__ void __launch_bounds__(128) k_btrace(BatchCtl* ctl,
   int64_t n = (int64_t)ctl->c[C_LIVE0 + cur];
   traceWarpPersistent<false, WIDE, false>(
       scenes[0].A, n, ctl->c + C_NEXT_TRACE,
-      [&](int64_t q) { return loadRay7(S.ray, cap, (int)q); },
+      [&](int64_t q) { return loadRay7(S.ray, (int)q); },
       [&](int64_t q, const RayQueryResult& res) {
-        tmp.hit_t[q] = res.t;
-        tmp.hit_prim[q] = res.hit ? res.prim : -1;
-        tmp.hit_b[2 * q] = res.b1;
-        tmp.hit_b[2 * q + 1] = res.b2;
+        tmp.hit[q] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
       },
       nullptr, [&](int64_t q) { return &scenes[S.scene[q]].A; });
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ctl->c + C_CLOSEST, (unsigned long long)n);
@@ -347,13 +340,10 @@ __global__ void __launch_bounds__(128) k_btrace_mis(BatchCtl* ctl,
   const int32_t* __restrict__ queue = Q.mis;
   traceWarpPersistent<false, WIDE, false>(
       scenes[0].A, n, ctl->c + C_NEXT_MIS,
-      [&](int64_t q) { return loadRay7(tmp.mray, tmp.cap, queue[q]); },
+      [&](int64_t q) { return loadRay7(tmp.mray, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         int s = queue[q];
-        tmp.mhit_t[s] = res.t;
-        tmp.mhit_prim[s] = res.hit ? res.prim : -1;
-        tmp.mhit_b[2 * s] = res.b1;
-        tmp.mhit_b[2 * s + 1] = res.b2;
+        tmp.mhit[s] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
       },
       nullptr, [&](int64_t q) { return &scenes[S.scene[queue[q]]].A; });
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ctl->c + C_CLOSEST, (unsigned long long)n);
@@ -372,7 +362,7 @@ __global__ void __launch_bounds__(128) k_bclass_count(BatchCtl* ctl,
     int c = -1;
     if (q < n) {
       const BatchSceneDev& SC = scenes[S.scene[q]];
-      c = shadeClass(SC.A, SC.S, tmp.hit_prim[q]);
+      c = shadeClass(SC.A, SC.S, hitPrim(tmp.hit, q));
       Q.cls[q] = c;
     }
     classCount(c, ctl->cls);
@@ -475,10 +465,9 @@ __global__ void __launch_bounds__(128, 3) k_bresolve(BatchCtl* ctl,
     }
     long long p = queueSlot(cont, c + C_LIVE0 + nxt);
     if (cont) {
-      storeBands(D.T, cap, (int)p, Tn);
-      storeBands(D.L, cap, (int)p, Ln);
-#pragma unroll
-      for (int k = 0; k < 7; k++) D.ray[k * cap + p] = S.ray[k * cap + q];
+      storeBands(D.T, (int)p, Tn);
+      storeBands(D.L, (int)p, Ln);
+      copyRay(S.ray, q, D.ray, (int)p);
       D.gidx[p] = S.gidx[q];
       D.job[p] = job;
       D.scene[p] = S.scene[q];
@@ -695,7 +684,9 @@ int batch_create(int device, cudaStream_t stream, const BatchConfig& cfg, BatchE
   b->device = device;
   b->stream = stream;
   b->cfg = cfg;
-  b->cap = cfg.slots;
+  // a multiple of 64 paths keeps every per-path array 16-byte aligned (the
+  // records are read with 16-byte vector loads)
+  b->cap = (cfg.slots + 63) / 64 * 64;
   b->job_mask = (unsigned)cfg.max_jobs - 1;
   b->jobs.resize(cfg.max_jobs);
   b->done_buf.resize(cfg.max_jobs);
@@ -718,7 +709,7 @@ int batch_create(int device, cudaStream_t stream, const BatchConfig& cfg, BatchE
     PathState& p = b->ps.b[k];
     p.T = take(16);
     p.L = take(16);
-    p.ray = take(7);
+    p.ray = take(8);
     p.job = (int32_t*)take(1);
     p.scene = (int32_t*)take(1);
     p.depth = (int32_t*)take(1);
@@ -726,9 +717,7 @@ int batch_create(int device, cudaStream_t stream, const BatchConfig& cfg, BatchE
   Slots& t = b->tmp;
   t.cap = cap;
   t.T = t.L = t.ray = nullptr;  // per buffer (viewOf)
-  t.hit_t = take(1);
-  t.hit_prim = (int32_t*)take(1);
-  t.hit_b = take(2);
+  t.hit = reinterpret_cast<float4*>(take(4));
   t.intl = take(16);
   t.ls = take(16);
   t.bsf = take(16);
@@ -738,10 +727,8 @@ int batch_create(int device, cudaStream_t stream, const BatchConfig& cfg, BatchE
   t.vflags = (int32_t*)take(1);
   t.sray = take(8);
   t.svis = (int32_t*)take(1);
-  t.mray = take(7);
-  t.mhit_t = take(1);
-  t.mhit_prim = (int32_t*)take(1);
-  t.mhit_b = take(2);
+  t.mray = take(8);
+  t.mhit = reinterpret_cast<float4*>(take(4));
   b->q.shadow = (int32_t*)take(1);
   b->q.mis = (int32_t*)take(1);
   b->q.resolve = (int32_t*)take(1);

@@ -23,6 +23,12 @@ struct bling_ctx {
   size_t scratch_bytes = 0;
   // next-ray counter of the persistent traversal kernels (calls are serialised)
   unsigned long long* d_counter = nullptr;
+  // copy streams and events of the chunked host-buffer queries (made on first use)
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t ev_start = nullptr;
+  cudaEvent_t ev_in[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_run[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t ev_out[3] = {nullptr, nullptr, nullptr};
   bgpu::IntegratorWorkspace ws;
 };
 

@@ -68,9 +68,9 @@ __global__ void k_raygen(PassParams P, bling_camera_desc cam, Slots st, int64_t 
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
        i += (int64_t)gridDim.x * blockDim.x) {
     Ray ray = cameraRay(P, cam, P.chunk_base + (uint64_t)i);
-    storeRay(st.ray, st.cap, (int)i, ray, false);
-    storeBands(st.T, st.cap, (int)i, sConst(1.0f));
-    storeBands(st.L, st.cap, (int)i, sConst(0.0f));
+    storeRay(st.ray, (int)i, ray);
+    storeBands(st.T, (int)i, sConst(1.0f));
+    storeBands(st.L, (int)i, sConst(0.0f));
     queue[i] = (int32_t)i;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) counters[C_LIVE0] = (unsigned long long)count;
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(128) k_class_count(DevAccel A, DevShading S, S
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
     int c = -1;
     if (q < n) {
-      c = shadeClass(A, S, st.hit_prim[queue[q]]);
+      c = shadeClass(A, S, hitPrim(st.hit, queue[q]));
       cls[q] = c;
     }
     classCount(c, classCounts(counters));
@@ -133,13 +133,10 @@ __global__ void __launch_bounds__(128) k_trace(DevAccel A, Slots st, const int32
                                                unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)*qcount;
   traceWarpPersistent<false, WIDE, false>(
-      A, n, counters + C_NEXT_TRACE, [&](int64_t q) { return loadRay7(st.ray, st.cap, queue[q]); },
+      A, n, counters + C_NEXT_TRACE, [&](int64_t q) { return loadRay7(st.ray, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         int s = queue[q];
-        st.hit_t[s] = res.t;
-        st.hit_prim[s] = res.hit ? res.prim : -1;
-        st.hit_b[2 * s] = res.b1;
-        st.hit_b[2 * s + 1] = res.b2;
+        st.hit[s] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
       });
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_CLOSEST, (unsigned long long)n);
 }
@@ -166,13 +163,10 @@ __global__ void __launch_bounds__(128) k_trace_mis(DevAccel A, Slots st,
                                                    unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_MIS];
   traceWarpPersistent<false, WIDE, false>(
-      A, n, counters + C_NEXT_MIS, [&](int64_t q) { return loadRay7(st.mray, st.cap, queue[q]); },
+      A, n, counters + C_NEXT_MIS, [&](int64_t q) { return loadRay7(st.mray, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         int s = queue[q];
-        st.mhit_t[s] = res.t;
-        st.mhit_prim[s] = res.hit ? res.prim : -1;
-        st.mhit_b[2 * s] = res.b1;
-        st.mhit_b[2 * s + 1] = res.b2;
+        st.mhit[s] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
       });
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_CLOSEST, (unsigned long long)n);
 }
@@ -221,8 +215,8 @@ __global__ void __launch_bounds__(128) k_resolve(DevAccel A, DevShading S, PassP
           [&](const Spec& L) { splatSample(film, P, g, L, counters + C_NONFINITE, PassFilter{}); },
           Tn, Ln);
       if (cont) {
-        storeBands(st.T, st.cap, s, Tn);
-        storeBands(st.L, st.cap, s, Ln);
+        storeBands(st.T, s, Tn);
+        storeBands(st.L, s, Ln);
       }
     }
     queueAppend(cont, s, Q.live[live_out], counters + live_out);
@@ -385,7 +379,10 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
   filterTableHost(p.filter_kind, p.filter_params, P.fw, P.fh, tbl);
   RET_CUDA(cudaMemcpyToSymbolAsync(c_filter, tbl, sizeof tbl, 0, cudaMemcpyHostToDevice, stream));
   size_t cap = (size_t)std::min<uint64_t>(total, uint64_t(1) << 22);
-  rc = ensureWorkspace(ws, std::max<size_t>(cap, 1024), err);
+  // a multiple of 64 paths keeps every per-path array 16-byte aligned (the
+  // records are read with 16-byte vector loads)
+  cap = (std::max<size_t>(cap, 1024) + 63) / 64 * 64;
+  rc = ensureWorkspace(ws, cap, err);
   if (rc) return rc;
   Slots st;
   Queues Q;

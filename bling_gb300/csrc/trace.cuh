@@ -113,6 +113,15 @@ __device__ __forceinline__ bool degenerateRay(const Ray& r) {
          isnan(r.d.z) || isnan(r.tmin) || isnan(r.tmax);
 }
 
+// 32 bytes of read-only global memory, 32-byte aligned, in one 256-bit load
+// (ld.global.nc.v8, sm_100 and later): half the load instructions of four
+// 16-byte loads for a 64-byte node
+__device__ __forceinline__ void ldg256(const float4* p, float4& a, float4& b) {
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+
 // u8 -> float without a conversion instruction: 0x4B0000bb is 2^23 + bb
 __device__ __forceinline__ float qbyte(uint32_t word, uint32_t sel) {
   return __uint_as_float(__byte_perm(word, 0x4B000000u, sel)) - 8388608.0f;
@@ -264,9 +273,10 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
           }
           cur = first != kSentinel ? first : (sp > 0 ? stack[--sp] : kSentinel);
         } else {
-          const float4* nd = TW_ACC(nodes) + 4 * (size_t)cur;
-          float4 a = __ldg(nd), b = __ldg(nd + 1), c = __ldg(nd + 2);
-          float4 refs = __ldg(nd + 3);
+          const float4* nd = TW_ACC(nodes) + 4 * (size_t)cur;  // 64-byte aligned
+          float4 a, b, c, refs;
+          ldg256(nd, a, b);
+          ldg256(nd + 2, c, refs);
           float n0, f0, n1, f1;
           boxInterval(a.x, a.y, a.z, a.w, c.x, c.y, r.o, inv, n0, f0);
           boxInterval(b.x, b.y, b.z, b.w, c.z, c.w, r.o, inv, n1, f1);

@@ -18,26 +18,22 @@ enum : int { VF_SHADOW = 1, VF_MIS = 2, VF_CONT = 4 };
 
 struct Slots {
   size_t cap;
-  float* T;          // 16 x cap
-  float* L;          // 16 x cap
-  float* ray;        // 7 x cap: o, d, tmin (sign bit of tmin: the previous bounce was specular)
-  float* hit_t;      // cap
-  int32_t* hit_prim; // cap
-  float* hit_b;      // 2 x cap
+  float* T;          // 16 per path
+  float* L;          // 16 per path
+  float* ray;        // 8 per path: o, d, tmin (sign bit: the previous bounce was specular), tmax
+  float4* hit;       // per path: t, primitive ID (int bits; -1 none), b1, b2
   // the current vertex, deferred until its shadow and MIS rays are traced
-  float* intl;       // 16 x cap: emission seen on a specular path
-  float* ls;         // 16 x cap: light-sample term before visibility
-  float* bsf;        // 16 x cap: MIS BSDF sample throughput
-  float* fc;         // 16 x cap: continuation BSDF sample throughput
+  float* intl;       // 16 per path: emission seen on a specular path
+  float* ls;         // 16 per path: light-sample term before visibility
+  float* bsf;        // 16 per path: MIS BSDF sample throughput
+  float* fc;         // 16 per path: continuation BSDF sample throughput
   float* bsw;        // cap: MIS weight of the BSDF sample
   float* invpc;      // cap: 1 / continuation probability
   int32_t* vflags;   // cap: VF_* | light index << 8
-  float* sray;       // 8 x cap: shadow ray o, d, tmin, tmax
+  float* sray;       // 8 per path: shadow ray o, d, tmin, tmax
   int32_t* svis;     // cap: shadow ray unoccluded
-  float* mray;       // 7 x cap: MIS ray o, d, tmin
-  float* mhit_t;     // cap
-  int32_t* mhit_prim;// cap
-  float* mhit_b;     // 2 x cap
+  float* mray;       // 8 per path: MIS ray o, d, tmin, tmax
+  float4* mhit;      // per path: the MIS ray's hit, as hit
 };
 
 struct Queues {
@@ -56,7 +52,7 @@ enum : int {
   C_COUNT = 16
 };
 
-constexpr size_t kSlotWords = 16 * 6 + 7 + 4 + 3 + 8 + 1 + 7 + 4;  // per slot, 4-byte words
+constexpr size_t kSlotWords = 16 * 6 + 8 + 4 + 3 + 8 + 1 + 8 + 4;  // per slot, 4-byte words
 constexpr size_t kQueueWords = 7;
 // counters: C_COUNT 8-byte counters, then the shading-class counts and
 // cursors (kShadeClasses 4-byte entries each, 16 reserved)
@@ -73,10 +69,8 @@ inline void carveSlots(float*& w, size_t cap, Slots& st) {
   st.cap = cap;
   st.T = take(16);
   st.L = take(16);
-  st.ray = take(7);
-  st.hit_t = take(1);
-  st.hit_prim = (int32_t*)take(1);
-  st.hit_b = take(2);
+  st.ray = take(8);
+  st.hit = reinterpret_cast<float4*>(take(4));
   st.intl = take(16);
   st.ls = take(16);
   st.bsf = take(16);
@@ -86,10 +80,8 @@ inline void carveSlots(float*& w, size_t cap, Slots& st) {
   st.vflags = (int32_t*)take(1);
   st.sray = take(8);
   st.svis = (int32_t*)take(1);
-  st.mray = take(7);
-  st.mhit_t = take(1);
-  st.mhit_prim = (int32_t*)take(1);
-  st.mhit_b = take(2);
+  st.mray = take(8);
+  st.mhit = reinterpret_cast<float4*>(take(4));
 }
 
 // sample index g of a pass -> pixel and sample number (pixel-major, like the
@@ -132,36 +124,62 @@ __device__ __forceinline__ void pixelSample(const PassParams& P, const Sampler& 
   sy = (float)iy + oy;
 }
 
-__device__ __forceinline__ Spec loadBands(const float* base, size_t cap, int s) {
+// Per-path records.  A bounce visits its paths in shading-class order, so
+// the lanes of a warp touch scattered paths: spectra are stored per path
+// (16 consecutive floats, 64 bytes) and rays as 8 floats (o, d, tmin, tmax),
+// so that a lane's loads fill whole 32-byte sectors instead of one float
+// per sector.
+__device__ __forceinline__ Spec loadBands(const float* base, int s) {
+  const float4* p = reinterpret_cast<const float4*>(base + 16 * (size_t)s);
   Spec v;
 #pragma unroll
-  for (int b = 0; b < 16; b++) v.v[b] = base[b * cap + s];
+  for (int k = 0; k < 4; k++) {
+    float4 q = p[k];
+    v.v[4 * k] = q.x;
+    v.v[4 * k + 1] = q.y;
+    v.v[4 * k + 2] = q.z;
+    v.v[4 * k + 3] = q.w;
+  }
   return v;
 }
-__device__ __forceinline__ void storeBands(float* base, size_t cap, int s, const Spec& v) {
+__device__ __forceinline__ void storeBands(float* base, int s, const Spec& v) {
+  float4* p = reinterpret_cast<float4*>(base + 16 * (size_t)s);
 #pragma unroll
-  for (int b = 0; b < 16; b++) base[b * cap + s] = v.v[b];
+  for (int k = 0; k < 4; k++)
+    p[k] = make_float4(v.v[4 * k], v.v[4 * k + 1], v.v[4 * k + 2], v.v[4 * k + 3]);
 }
-__device__ __forceinline__ void storeRay(float* base, size_t cap, int s, const Ray& r, bool tmax) {
-  base[s] = r.o.x;
-  base[cap + s] = r.o.y;
-  base[2 * cap + s] = r.o.z;
-  base[3 * cap + s] = r.d.x;
-  base[4 * cap + s] = r.d.y;
-  base[5 * cap + s] = r.d.z;
-  base[6 * cap + s] = r.tmin;
-  if (tmax) base[7 * cap + s] = r.tmax;
+// a ray record: the sign bit of tmin may carry a flag (loadRay7 drops it)
+__device__ __forceinline__ void storeRay(float* base, int s, const Ray& r) {
+  float4* p = reinterpret_cast<float4*>(base + 8 * (size_t)s);
+  p[0] = make_float4(r.o.x, r.o.y, r.o.z, r.d.x);
+  p[1] = make_float4(r.d.y, r.d.z, r.tmin, r.tmax);
 }
-__device__ __forceinline__ Ray loadRay7(const float* base, size_t cap, int s) {
-  return Ray{V3{base[s], base[cap + s], base[2 * cap + s]},
-             V3{base[3 * cap + s], base[4 * cap + s], base[5 * cap + s]}, fabsf(base[6 * cap + s]),
-             INFINITY};
+__device__ __forceinline__ void copyRay(const float* from, int q, float* to, int p) {
+  const float4* a = reinterpret_cast<const float4*>(from + 8 * (size_t)q);
+  float4* b = reinterpret_cast<float4*>(to + 8 * (size_t)p);
+  b[0] = a[0];
+  b[1] = a[1];
+}
+// a hit record: t, the primitive ID as int bits (-1: no hit), barycentrics
+__device__ __forceinline__ float4 hitRecord(bool hit, float t, int prim, float b1, float b2) {
+  return make_float4(t, __int_as_float(hit ? prim : -1), b1, b2);
+}
+__device__ __forceinline__ int hitPrim(const float4* rec, int s) {
+  return __float_as_int(reinterpret_cast<const float*>(rec + s)[1]);
+}
+__device__ __forceinline__ float rayTminBits(const float* base, int s) {
+  return base[8 * (size_t)s + 6];
+}
+// a closest-hit ray (tmax = infinity, tmin without its flag)
+__device__ __forceinline__ Ray loadRay7(const float* base, int s) {
+  const float4* p = reinterpret_cast<const float4*>(base + 8 * (size_t)s);
+  float4 a = p[0], b = p[1];
+  return Ray{V3{a.x, a.y, a.z}, V3{a.w, b.x, b.y}, fabsf(b.z), INFINITY};
 }
 __device__ __forceinline__ Ray loadShadowRay(const Slots& st, int s) {
-  size_t c = st.cap;
-  return Ray{V3{st.sray[s], st.sray[c + s], st.sray[2 * c + s]},
-             V3{st.sray[3 * c + s], st.sray[4 * c + s], st.sray[5 * c + s]}, st.sray[6 * c + s],
-             st.sray[7 * c + s]};
+  const float4* p = reinterpret_cast<const float4*>(st.sray + 8 * (size_t)s);
+  float4 a = p[0], b = p[1];
+  return Ray{V3{a.x, a.y, a.z}, V3{a.w, b.x, b.y}, b.z, b.w};
 }
 
 // warp-aggregated append (every lane of the warp calls it)
@@ -299,9 +317,10 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
   decodeSample(P, g, ix, iy, sn);
   Sampler smp = mkSampler(P, ix, iy, sn);
   size_t c = st.cap;
-  Ray ray = loadRay7(st.ray, c, s);
-  bool specular = depth == 0 || signbit(st.ray[6 * c + s]);
-  int prim = st.hit_prim[s];
+  Ray ray = loadRay7(st.ray, s);
+  bool specular = depth == 0 || signbit(rayTminBits(st.ray, s));
+  const float4 hit = st.hit[s];
+  int prim = __float_as_int(hit.y);
   if (prim == kDegenerateRay) {
     // a NaN ray: the reference's sample ends NaN and is dropped by the film
     atomicAdd(counters + C_DEGENERATE, 1ull);
@@ -309,16 +328,16 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
     return out;
   }
   if (prim < 0 || depth == P.max_depth) {
-    Spec Lr = loadBands(st.L, c, s);
+    Spec Lr = loadBands(st.L, s);
     if (prim < 0 && specular) {  // nothing hit after a specular bounce: l + t * sum le
       Spec sum = sConst(0);
       for (int k = 0; k < S.n_lights; k++) sum = sum + lightLe(S.lights[k], ray.d);
-      Lr = Lr + loadBands(st.T, c, s) * sum;
+      Lr = Lr + loadBands(st.T, s) * sum;
     }
     finish(Lr);
     return out;
   }
-  float thit = st.hit_t[s], b1 = st.hit_b[2 * s], b2 = st.hit_b[2 * s + 1];
+  float thit = hit.x, b1 = hit.z, b2 = hit.w;
   float lNumU = rnd1(smp, 1 + 4 * depth);
   float ld1, ld2;
   rnd2(smp, 1 + 3 * depth, ld1, ld2);
@@ -327,7 +346,7 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
   rnd2(smp, 2 + 3 * depth, lb1, lb2);
   HitGeom gm = hitGeometry(A, S, ray, prim, thit, b1, b2);
   V3 rd = ray.d;
-  storeBands(st.intl, c, s, specular ? intLe(S, gm, rd) : sConst(0));
+  storeBands(st.intl, s, specular ? intLe(S, gm, rd) : sConst(0));
   V3 wo = -rd;
   Bsdf bsdf = materialBsdf(S.materials, gm.material, gm.n, gm.sp, gm.sn, gm.sdpdu);
   V3 nn = bsdf.cs.n, p = bsdf.p;
@@ -351,23 +370,23 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
           float w = powerHeuristic(smpl.pdf, bsdfPdf(bsdf, wo, smpl.wi));
           lsv = sScale(f * smpl.li, w / smpl.pdf);
         }
-        storeBands(st.ls, c, s, lsv);
+        storeBands(st.ls, s, lsv);
         Ray sr = smpl.ray;
-        storeRay(st.sray, c, s, sr, true);
+        storeRay(st.sray, s, sr);
         flags |= VF_SHADOW;
       }
     }
     // sampleBsdfMis (Scene.hs:194-205), the hit deferred
     BsdfSample bm = sampleBsdf(bsdf, wo, lBsdfCompU, lb1, lb2);
     if (!(bm.pdf == 0 || isBlack(bm.f))) {
-      storeBands(st.bsf, c, s, bm.f);
+      storeBands(st.bsf, s, bm.f);
       st.bsw[s] = powerHeuristic(bm.pdf, lightPdf(A, l, p, bm.wi));
-      storeRay(st.mray, c, s, Ray{p, bm.wi, eps, INFINITY}, false);
+      storeRay(st.mray, s, Ray{p, bm.wi, eps, INFINITY});
       flags |= VF_MIS;
     }
   }
   // Russian roulette and the continuation (Path.hs:68-87)
-  Spec T = loadBands(st.T, c, s);
+  Spec T = loadBands(st.T, s);
   float pc = depth <= P.rr_depth ? 1.0f : hmin(0.75f, sY(T));
   float x = rnd1(smp, 3 + 4 * depth);
   if (!(x > pc)) {
@@ -376,10 +395,10 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
     rnd2(smp, 0 + 3 * depth, ud1, ud2);
     BsdfSample bc = sampleBsdf(bsdf, wo, uc, ud1, ud2);
     if (!(bc.pdf == 0 || isBlack(bc.f))) {
-      storeBands(st.fc, c, s, bc.f);
+      storeBands(st.fc, s, bc.f);
       st.invpc[s] = 1.0f / pc;
       bool spec2 = (bc.type & T_SPEC) != 0;
-      storeRay(st.ray, c, s, Ray{p, bc.wi, spec2 ? -eps : eps, INFINITY}, false);
+      storeRay(st.ray, s, Ray{p, bc.wi, spec2 ? -eps : eps, INFINITY});
       flags |= VF_CONT;
     }
   }
@@ -403,11 +422,12 @@ __device__ __forceinline__ bool resolveVertex(const DevAccel& A, const DevShadin
   int vf = st.vflags[s];
   int lc = S.n_lights;
   Spec lsv = sConst(0), bsv = sConst(0);
-  if ((vf & VF_SHADOW) && st.svis[s]) lsv = loadBands(st.ls, c, s);
+  if ((vf & VF_SHADOW) && st.svis[s]) lsv = loadBands(st.ls, s);
   if (vf & VF_MIS) {
     const DLight& l = S.lights[vf >> 8];
-    Ray mr = loadRay7(st.mray, c, s);
-    int mp = st.mhit_prim[s];
+    Ray mr = loadRay7(st.mray, s);
+    const float4 mh = st.mhit[s];
+    int mp = __float_as_int(mh.y);
     bool use = false;
     Spec lr;
     if (mp == kDegenerateRay) {
@@ -419,7 +439,7 @@ __device__ __forceinline__ bool resolveVertex(const DevAccel& A, const DevShadin
         int2 info = __ldg(S.prim_info + mp);
         if (info.x < 0 && ~info.x == l.shape) {  // Eq Light: the same area light
           HitGeom gm =
-              hitGeometry(A, S, mr, mp, st.mhit_t[s], st.mhit_b[2 * s], st.mhit_b[2 * s + 1]);
+              hitGeometry(A, S, mr, mp, mh.x, mh.z, mh.w);
           lr = intLe(S, gm, -mr.d);
           use = true;
         }
@@ -428,15 +448,15 @@ __device__ __forceinline__ bool resolveVertex(const DevAccel& A, const DevShadin
       lr = lightLe(l, mr.d);
       use = true;
     }
-    if (use) bsv = sScale(loadBands(st.bsf, c, s) * lr, st.bsw[s]);
+    if (use) bsv = sScale(loadBands(st.bsf, s) * lr, st.bsw[s]);
   }
   Spec ed = lsv + bsv;  // estimateDirect = ls + bs (Scene.hs:218)
   Spec direct = lc == 1 ? ed : (lc > 1 ? sScale(ed, (float)lc) : sConst(0));
-  Spec lHere = loadBands(st.intl, c, s) + direct;
-  Spec T = loadBands(st.T, c, s);
-  Spec Lr = loadBands(st.L, c, s) + T * lHere;
+  Spec lHere = loadBands(st.intl, s) + direct;
+  Spec T = loadBands(st.T, s);
+  Spec Lr = loadBands(st.L, s) + T * lHere;
   if (vf & VF_CONT) {
-    Tn = sScale(loadBands(st.fc, c, s) * T, st.invpc[s]);
+    Tn = sScale(loadBands(st.fc, s) * T, st.invpc[s]);
     Ln = Lr;
     return true;
   }

@@ -129,6 +129,35 @@ def test_zero_direction_component_on_box_faces(ctx, zero_axis):
         assert c0["nodes_per_ray"] <= 3 * c1["nodes_per_ray"], (c0, c1)
 
 
+def test_host_buffer_chunks_equal_device_buffer_queries(gpu_ctx):
+    """the host-buffer calls copy, trace and copy back in chunks of 2^21 rays
+    on three streams; a ragged count over several chunks gives exactly the
+    device-buffer answers"""
+    import torch
+    soup = S.triangle_soup(1 << 18, seed=9)
+    g = gpu_ctx.scene(soup)
+    n = (1 << 22) + 12345
+    rays = S.soup_rays(n, seed=10)
+    t, p, b = g.closest(rays)
+    dev = torch.device("cuda", 0)
+    d_r = torch.from_numpy(rays).to(dev)
+    d_t = torch.empty(n, dtype=torch.float32, device=dev)
+    d_p = torch.empty(n, dtype=torch.int32, device=dev)
+    d_b = torch.empty(2 * n, dtype=torch.float32, device=dev)
+    g.closest_device(d_r, d_t, d_p, d_b)
+    torch.cuda.synchronize()
+    assert np.array_equal(p, d_p.cpu().numpy())
+    assert np.array_equal(_bits(t), _bits(d_t.cpu().numpy()))
+    assert np.array_equal(_bits(b.ravel()), _bits(d_b.cpu().numpy()))
+    ra = S.soup_rays(n, seed=11, any_hit=True)
+    h = g.any(ra)
+    d_h = torch.empty(n, dtype=torch.uint8, device=dev)
+    g.any_device(torch.from_numpy(ra).to(dev), d_h)
+    torch.cuda.synchronize()
+    assert np.array_equal(h, d_h.cpu().numpy())
+    assert 0.05 < h.mean() < 0.999
+
+
 def test_full_size_closest_is_closest(gpu_ctx):
     """16M rays over the 1M soup: any-hit with tmax just below the reported
     closest t finds nothing, with tmax = t finds the hit."""
