@@ -1,0 +1,662 @@
+"""Reader for bling's ``.bling`` scene files: the flat scene record a bling
+front end hands to the GPU path integrator.
+
+Mirrors the reference's parser (``src/lib/Graphics/Bling/IO/*.hs``): the same
+objects, blocks and keywords, the same parser state and its defaults
+(``RenderJob.hs:24-33``), and the same order of primitives and lights, so a
+file renders through :class:`~bling_gb300.api.GpuPathRenderer` with the
+primitive IDs and light list ``mkScene`` would build (``Scene.hs:160-166``).
+Numbers are rounded to binary32 once, as GHC's ``read :: Float`` does, and
+transforms, spectra and meshes are built with the binary32 restatements of
+``Transform.hs`` and ``Spectrum.hs`` (``transform.py``, ``spectrum.py``).
+
+The subset is what the GPU path renders:
+
+* objects: ``filter``, ``imageSize``, ``renderer``, ``transform``,
+  ``newTransform``, ``camera``, ``light``, ``material``, ``emission``,
+  ``prim``;
+* primitives: ``mesh`` and ``shape`` (box, cylinder, disk, quad, sphere);
+* materials: matte, plastic, metal, glass, with ``constant`` textures;
+* lights: directional, point, and infinite with a ``constant`` map;
+* spectra: ``rgbR``/``rgbI`` (decimal or ``%rrggbb``), ``spd { l v, ... }``,
+  ``temp``;
+* the sampler renderer (``stratified``/``random``) with the ``path``
+  integrator.
+
+Anything else raises :class:`Unsupported` naming the construct; a file whose
+renderer is not the path integrator parses, and :attr:`Job.renderer` names
+the renderer it asked for.
+"""
+from __future__ import annotations
+
+import math
+import re
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+from . import transform as xf
+from .gen_spectrum_tables import BANDS, LAMBDA_END, LAMBDA_START, f32_of_decimal, lerp
+from .scene import Light, Scene, render_params
+from .spectrum import constant, rgb_to_spectrum
+
+F = np.float32
+
+
+class BlingFileError(ValueError):
+    """A syntax error in a .bling file."""
+
+
+class Unsupported(BlingFileError):
+    """A construct the reference parses but the GPU path does not render."""
+
+
+@dataclass
+class Job:
+    """A parsed render job: the scene, the image size and the renderer."""
+    scene: Scene
+    width: int
+    height: int
+    filter_kind: int
+    filter_params: tuple
+    renderer: str                      # "path", or the reference renderer the file selects
+    sampler_kind: int = abi.SAMPLER_STRATIFIED
+    strata: tuple = (2, 2)             # (nu, nv), or (spp, 1) for the random sampler
+    max_depth: int = 7                 # mkPathIntegrator 7 3 (IntegratorParser.hs)
+    sample_depth: int = 3
+
+    def params(self, seed: int = 1, rr_depth: int = 7) -> abi.RenderParams:
+        """bling_render_params of the job's sampler renderer and path
+        integrator (Russian roulette after depth 7 as in Path.hs:68)."""
+        return render_params(self.width, self.height, self.strata, max_depth=self.max_depth,
+                             sample_depth=self.sample_depth, rr_depth=rr_depth,
+                             filter_kind=self.filter_kind, filter_params=self.filter_params,
+                             seed=seed, sampler=self.sampler_kind)
+
+
+# ---------------------------------------------------------------- tokens
+# ws = spaces and '#' comments (ParserCore.hs:111-119); words are alphaNum
+# runs (pString); numbers are [+-]digits[.digits] (flt')
+_TOKEN = re.compile(r"""
+    (?P<ws>\s+|\#[^\n]*)
+  | (?P<str>"(?:[^"\\\r\n]|\\[^\r\n])*")
+  | (?P<hex>%[0-9A-Fa-f]{2}(?:\s*[0-9A-Fa-f]{2}){2})
+  | (?P<num>[+-]?\d+(?:\.\d*)?(?![A-Za-z]))
+  | (?P<word>[A-Za-z0-9]+)
+  | (?P<sym>[{},])
+""", re.X)
+
+
+class _Tokens:
+    def __init__(self, text: str):
+        self.toks = []
+        pos = 0
+        line = 1
+        while pos < len(text):
+            m = _TOKEN.match(text, pos)
+            if not m:
+                raise BlingFileError(f"line {line}: unexpected character {text[pos]!r}")
+            kind = m.lastgroup
+            if kind != "ws":
+                self.toks.append((kind, m.group(kind), line))
+            line += m.group(0).count("\n")
+            pos = m.end()
+        self.i = 0
+
+    def peek(self):
+        return self.toks[self.i] if self.i < len(self.toks) else (None, None, -1)
+
+    def next(self):
+        t = self.peek()
+        if t[0] is None:
+            raise BlingFileError("unexpected end of file")
+        self.i += 1
+        return t
+
+    def error(self, msg):
+        return BlingFileError(f"line {self.peek()[2]}: {msg}")
+
+    def word(self) -> str:
+        kind, val, line = self.next()
+        if kind not in ("word", "num"):
+            raise BlingFileError(f"line {line}: expected a name, got {val!r}")
+        return val
+
+    def expect(self, what: str):
+        kind, val, line = self.next()
+        if val != what:
+            raise BlingFileError(f"line {line}: expected {what!r}, got {val!r}")
+
+    def flt(self) -> np.float32:
+        kind, val, line = self.next()
+        if kind != "num":
+            raise BlingFileError(f"line {line}: expected a number, got {val!r}")
+        return f32_of_decimal(val if "." not in val or not val.endswith(".") else val + "0")
+
+    def integ(self) -> int:
+        kind, val, line = self.next()
+        if kind != "num" or not val.isdigit():
+            raise BlingFileError(f"line {line}: expected a non-negative integer, got {val!r}")
+        return int(val)
+
+    def vec(self):
+        return [self.flt(), self.flt(), self.flt()]
+
+    def named_flt(self, name):
+        self.expect(name)
+        return self.flt()
+
+    def named_int(self, name):
+        self.expect(name)
+        return self.integ()
+
+    def named_vec(self, name):
+        self.expect(name)
+        return self.vec()
+
+    def at(self, val) -> bool:
+        return self.peek()[1] == val
+
+    def block(self, body):
+        """pBlock: '{' body '}'"""
+        self.expect("{")
+        r = body()
+        self.expect("}")
+        return r
+
+    def named_block(self, name, body):
+        self.expect(name)
+        return self.block(body)
+
+
+# ---------------------------------------------------------------- binary32 helpers
+def _ghc_min(a, b):
+    return a if a <= b else b
+
+
+def _ghc_max(a, b):
+    return b if a <= b else a
+
+
+def _clamp(v, lo, hi):
+    """clamp (Math.hs:78-87)"""
+    return lo if v < lo else (hi if v > hi else v)
+
+
+def trans_point(t: xf.Transform, p):
+    """transPoint (Transform.hs:246-256): left-to-right binary32 sums; the
+    homogeneous divide only when w != 1."""
+    m = t.m
+    x, y, z = F(p[0]), F(p[1]), F(p[2])
+
+    def row(r):
+        return ((m[4 * r] * x + m[4 * r + 1] * y) + m[4 * r + 2] * z) + m[4 * r + 3]
+    xp, yp, zp, wp = row(0), row(1), row(2), row(3)
+    if wp == F(1):
+        return [xp, yp, zp]
+    return [xp / wp, yp / wp, zp / wp]
+
+
+def _avg_irregular_spd(ls, vs, l0, l1):
+    """avgSpd (IrregularSpd ls vs) l0 l1 (Spectrum.hs:307-314)"""
+    if l1 <= ls[0]:
+        return vs[0]
+    if l0 >= ls[-1]:
+        return vs[-1]
+
+    def find(lim, default):
+        for k, l in enumerate(ls):
+            if l >= lim:
+                return k
+        return default
+    i0 = find(l0, 0)
+    i1 = find(l1, len(vs) - 1)
+    sl = vs[i0:i1 + 1]
+    acc = F(0)
+    for v in sl:
+        acc = acc + v
+    return acc / F(len(sl))
+
+
+def spectrum_from_spd(pairs) -> np.ndarray:
+    """fromSpd (mkSpd pairs) (Spectrum.hs:199-208, 329-335): the pairs sorted
+    by wavelength (a stable sort, as sortBy), each band the plain average of
+    the samples from the first at or above its lower edge to the first at or
+    above its upper edge."""
+    if not pairs:
+        raise BlingFileError("empty SPD")
+    srt = sorted(pairs, key=lambda p: p[0])
+    ls = [F(l) for l, _ in srt]
+    vs = [F(v) for _, v in srt]
+    out = []
+    for i in range(BANDS):
+        l0 = lerp(F(i) / F(BANDS), LAMBDA_START, LAMBDA_END)
+        l1 = lerp(F(i + 1) / F(BANDS), LAMBDA_START, LAMBDA_END)
+        out.append(_avg_irregular_spd(ls, vs, l0, l1))
+    return np.asarray(out, np.float32)
+
+
+def _planck(temp, w):
+    """planck (Spectrum.hs:491-493) in binary32; w'^^(-5) = recip of GHC's
+    (^) by squaring, ((w'*w')*(w'*w'))*w'."""
+    w1 = F(w) * F(1e-9)
+    w2 = w1 * w1
+    p5 = (w2 * w2) * w1
+    num = F(0.4e-9) * (F(3.74183e-16) * (F(1) / p5))
+    return num / (F(math.exp(float(F(1.4388e-2) / (w1 * F(temp))))) - F(1))
+
+
+def spectrum_blackbody(temp) -> np.ndarray:
+    """sBlackBody (Spectrum.hs:480-483): fromSpd of an SpdFunc, each band the
+    mean of the function at the band's two edges (avgSpd, :316).  The
+    exponential is evaluated in double and rounded once, a stand-in for GHC's
+    expf."""
+    out = []
+    for i in range(BANDS):
+        l0 = lerp(F(i) / F(BANDS), LAMBDA_START, LAMBDA_END)
+        l1 = lerp(F(i + 1) / F(BANDS), LAMBDA_START, LAMBDA_END)
+        out.append((_planck(temp, l0) + _planck(temp, l1)) * F(0.5))
+    return np.asarray(out, np.float32)
+
+
+# ---------------------------------------------------------------- the parser
+class _State:
+    """PState with the reference's start values (RenderJob.hs:24-33)."""
+
+    def __init__(self, base: Path):
+        self.res = (640, 480)
+        self.renderer = "path"
+        self.sampler = (abi.SAMPLER_STRATIFIED, (2, 2))
+        self.depths = (7, 3)
+        self.filter = (abi.FILTER_BOX, (0.0, 0.0, 0.0, 0.0))
+        # defaultCamera 640 480 (CameraParser.hs): fixed at 640 x 480
+        self.camera = (xf.translate(0, 0, -5), F(0), F(1), F(90), 640, 480)
+        self.transform = xf.identity()
+        self.material = None  # defaultMaterial, created on first use
+        self.emit = None
+        self.lights = []      # newest first
+        self.blocks = []      # primitive blocks, newest first: ("mesh", i) / ("shape", i)
+        self.base = base
+
+
+class _Parser:
+    def __init__(self, text: str, base: Path):
+        self.t = _Tokens(text)
+        self.s = _State(base)
+        self.scene = Scene()
+
+    # -- state ---------------------------------------------------------
+    def _material(self) -> int:
+        if self.s.material is None:  # mkMatte (rgbR 0.9 0.9 0.9) 0 (MaterialParser.hs)
+            self.s.material = self.scene.add_material(
+                abi.MAT_MATTE, kd=rgb_to_spectrum((F(0.9), F(0.9), F(0.9))), sigma=0.0)
+        return self.s.material
+
+    # -- job -----------------------------------------------------------
+    def job(self) -> Job:
+        t = self.t
+        while t.peek()[0] is not None:
+            name = t.word()
+            handler = {
+                "filter": self.p_filter, "prim": self.p_prim, "imageSize": self.p_size,
+                "renderer": self.p_renderer, "transform": self.p_global_trans,
+                "newTransform": self.p_new_transform, "camera": self.p_camera,
+                "light": self.p_light, "material": self.p_material,
+                "emission": self.p_emission,
+            }.get(name)
+            if handler is None:
+                raise t.error(f"unknown object type {name}")
+            handler()
+        sc = self.scene
+        self._material()  # a file without prims still has the default material
+        sc.prim_order = [v if k == "mesh" else ~v for k, v in self.s.blocks]
+        sc.lights = list(self.s.lights)
+        c2w, lr, fd, fov, sx, sy = self.s.camera
+        cc2w, r2c = xf.perspective_camera(c2w, lr, fd, fov, sx, sy)
+        sc.set_camera(cc2w, r2c, float(lr), float(fd))
+        sc.view = (c2w, fov)
+        (kind, strata), (md, sd) = self.s.sampler, self.s.depths
+        fk, fp = self.s.filter
+        return Job(sc, self.s.res[0], self.s.res[1], fk, fp, self.s.renderer, kind, strata, md, sd)
+
+    def p_size(self):
+        self.s.res = (self.t.integ(), self.t.integ())
+
+    def p_filter(self):
+        t = self.t
+        name = t.word()
+        if name == "box":
+            self.s.filter = (abi.FILTER_BOX, (0.0, 0.0, 0.0, 0.0))
+        elif name == "gauss":
+            self.s.filter = (abi.FILTER_GAUSS, (t.flt(), t.flt(), t.flt(), 0.0))
+        elif name == "sinc":
+            self.s.filter = (abi.FILTER_SINC, (t.flt(), t.flt(), t.flt(), 0.0))
+        elif name == "triangle":
+            self.s.filter = (abi.FILTER_TRIANGLE, (t.flt(), t.flt(), 0.0, 0.0))
+        elif name == "mitchell":
+            self.s.filter = (abi.FILTER_MITCHELL, (t.flt(), t.flt(), t.flt(), t.flt()))
+        else:
+            raise t.error(f'unknown pixel filter function "{name}"')
+
+    # -- renderer (RendererParser.hs, IntegratorParser.hs) --------------
+    def p_renderer(self):
+        t = self.t
+
+        def body():
+            name = t.word()
+            if name != "sampler":
+                self._skip_to_block_end()
+                self.s.renderer = name
+                return
+            sampler, depths = t.named_block("sampled", self._sampled)
+            self.s.sampler = sampler
+            if depths is None:
+                return
+            self.s.depths = depths
+            self.s.renderer = "path"
+        t.block(body)
+
+    def _sampled(self):
+        t = self.t
+
+        def sampler():
+            kind = t.word()
+            if kind == "stratified":
+                return (abi.SAMPLER_STRATIFIED, (t.integ(), t.integ()))
+            if kind == "random":
+                return (abi.SAMPLER_RANDOM, (t.integ(), 1))
+            raise t.error(f"unknown sampler type {kind}")
+        smp = t.named_block("sampler", sampler)
+
+        def integrator():
+            kind = t.word()
+            if kind == "path":
+                return (t.named_int("maxDepth"), t.named_int("sampleDepth"))
+            self._skip_to_block_end()
+            self.s.renderer = f"sampler/{kind}"
+            return None
+        depths = t.named_block("integrator", integrator)
+        return smp, depths
+
+    def _skip_to_block_end(self):
+        """consumes tokens up to (not including) the '}' closing the current block"""
+        depth = 0
+        while True:
+            kind, val, _ = self.t.peek()
+            if val is None:
+                raise self.t.error("unterminated block")
+            if val == "}" and depth == 0:
+                return
+            self.t.next()
+            depth += {"{": 1, "}": -1}.get(val, 0)
+
+    # -- transforms (TransformParser.hs) --------------------------------
+    def p_transform(self) -> xf.Transform:
+        t = self.t
+
+        def body():
+            ts = []
+            while not t.at("}"):
+                name = t.word()
+                if name == "rotateX":
+                    ts.append(xf.rotate_x(t.flt()))
+                elif name == "rotateY":
+                    ts.append(xf.rotate_y(t.flt()))
+                elif name == "rotateZ":
+                    ts.append(xf.rotate_z(t.flt()))
+                elif name == "scale":
+                    ts.append(xf.scale(*t.vec()))
+                elif name == "translate":
+                    ts.append(xf.translate(*t.vec()))
+                elif name == "matrix":
+                    ts.append(t.block(self._matrix))
+                elif name == "lookAt":
+                    ts.append(t.block(lambda: xf.look_at(t.named_vec("pos"), t.named_vec("look"),
+                                                         t.named_vec("up"))))
+                else:
+                    raise t.error(f"unknown transform {name}")
+            # mconcat = foldr (<>) mempty
+            acc = xf.identity()
+            for tr in reversed(ts):
+                acc = xf.concat(tr, acc)
+            return acc
+        return t.block(body)
+
+    def _matrix(self):
+        t = self.t
+        rows = []
+        for _ in range(4):
+            t.expect("m")
+            rows.append([t.flt() for _ in range(4)])
+        m = np.asarray(rows, np.float32).reshape(16)
+        return xf.Transform(m, xf.invert(m))
+
+    def p_global_trans(self):
+        self.s.transform = xf.concat(self.p_transform(), self.s.transform)
+
+    def p_new_transform(self):
+        self.s.transform = xf.identity()
+        self.p_global_trans()
+
+    # -- camera (CameraParser.hs) ---------------------------------------
+    def p_camera(self):
+        t = self.t
+
+        def body():
+            kind = t.word()
+            if kind != "perspective":
+                raise Unsupported(f"camera {kind}: the GPU path renders perspective cameras")
+            fov = t.named_flt("fov")
+            lr = t.named_flt("lensRadius")
+            fd = t.named_flt("focalDistance")
+            sx, sy = self.s.res
+            self.s.camera = (self.s.transform, lr, fd, fov, sx, sy)
+        t.block(body)
+
+    # -- spectra (ParserCore.hs:151-190) --------------------------------
+    def p_spectrum(self) -> np.ndarray:
+        t = self.t
+        kind = t.word()
+        if kind in ("rgbR", "rgbI"):
+            rgb = self._rgb()
+            return rgb_to_spectrum(rgb, illuminant=(kind == "rgbI"))
+        if kind == "spd":
+            def body():
+                pairs = [(t.flt(), t.flt())]
+                while t.at(","):
+                    t.next()
+                    pairs.append((t.flt(), t.flt()))
+                return pairs
+            return spectrum_from_spd(t.block(body))
+        if kind == "temp":
+            return spectrum_blackbody(t.flt())
+        raise t.error(f"unknown spectrum type {kind}")
+
+    def _rgb(self):
+        kind, val, line = self.t.peek()
+        if kind == "hex":
+            self.t.next()
+            digits = val[1:].replace(" ", "").replace("\t", "").replace("\n", "")
+            return tuple(F(int(digits[k:k + 2], 16)) / F(255) for k in (0, 2, 4))
+        return (self.t.flt(), self.t.flt(), self.t.flt())
+
+    # -- materials (MaterialParser.hs) ----------------------------------
+    def _spectrum_texture(self, name) -> np.ndarray:
+        t = self.t
+
+        def body():
+            kind = t.word()
+            if kind != "constant":
+                raise Unsupported(f"texture {kind} ({name}): the GPU path renders constant "
+                                  "textures")
+            return self.p_spectrum()
+        return t.named_block(name, body)
+
+    def _scalar_texture(self, name) -> np.float32:
+        t = self.t
+
+        def body():
+            kind = t.word()
+            if kind != "constant":
+                raise Unsupported(f"texture {kind} ({name}): the GPU path renders constant "
+                                  "textures")
+            return t.flt()
+        return t.named_block(name, body)
+
+    def p_material(self):
+        self.s.material = self.t.block(self._material_body)
+
+    def _material_body(self) -> int:
+        t = self.t
+        kind = t.word()
+        sc = self.scene
+        if kind == "matte":
+            kd = self._spectrum_texture("kd")
+            sig = self._scalar_texture("sigma")
+            return sc.add_material(abi.MAT_MATTE, kd=kd, sigma=float(sig))
+        if kind == "plastic":
+            kd = self._spectrum_texture("kd")
+            ks = self._spectrum_texture("ks")
+            rough = self._scalar_texture("rough")
+            return sc.add_material(abi.MAT_PLASTIC, kd=kd, ks=ks, roughness=float(rough))
+        if kind == "metal":
+            eta = self._spectrum_texture("eta")
+            k = self._spectrum_texture("k")
+            rough = self._scalar_texture("rough")
+            return sc.add_material(abi.MAT_METAL, eta=eta, k=k, roughness=float(rough))
+        if kind == "glass":
+            ior = self._scalar_texture("ior")
+            kr = self._spectrum_texture("kr")
+            kt = self._spectrum_texture("kt")
+            return sc.add_material(abi.MAT_GLASS, ks=kr, kt=kt, ior=float(ior))
+        if kind in ("blackbody", "bumpMap", "shinyMetal", "substrate", "transMatte", "mirror"):
+            raise Unsupported(f"material {kind}: the GPU path renders matte, plastic, metal "
+                              "and glass")
+        raise t.error(f"unknown material type {kind}")
+
+    def p_emission(self):
+        t = self.t
+
+        def body():
+            if t.at("none"):
+                t.next()
+                return None
+            return self.p_spectrum()
+        self.s.emit = t.block(body)
+
+    # -- lights (LightParser.hs) ----------------------------------------
+    def p_light(self):
+        t = self.t
+
+        def body():
+            kind = t.word()
+            if kind == "directional":
+                t.expect("intensity")
+                s = self.p_spectrum()
+                n = xf.normalize(t.named_vec("normal"))
+                return Light(abi.LIGHT_DIRECTIONAL, s, vec=tuple(float(x) for x in n))
+            if kind == "point":
+                t.expect("intensity")
+                s = self.p_spectrum()
+                p = t.named_vec("position")
+                return Light(abi.LIGHT_POINT, s, vec=tuple(float(x) for x in p))
+            if kind == "infinite":
+                w2l = self.p_transform()
+                t.expect("l")
+                env = t.block(self._env_map)
+                return Light(abi.LIGHT_INFINITE, env=env, w2l=w2l)
+            raise t.error(f"unknown light type {kind}")
+        self.s.lights.insert(0, t.block(body))
+
+    def _env_map(self):
+        t = self.t
+        kind = t.word()
+        if kind == "constant":  # constSpectrumMap2d: a 1 x 1 map (Texture.hs:131-132)
+            return self.p_spectrum().reshape(1, 1, BANDS)
+        if kind in ("file", "sunSky", "rgbeFile"):
+            raise Unsupported(f"environment map {kind}: the GPU path takes constant maps from "
+                              ".bling files (image maps through bling_light_desc.env)")
+        raise t.error(f"unknown map type {kind}")
+
+    # -- primitives (PrimitiveParser.hs) --------------------------------
+    def p_prim(self):
+        self.t.block(self._prim_body)
+
+    def _prim_body(self):
+        t = self.t
+        kind = t.word()
+        if kind == "mesh":
+            self._mesh()
+        elif kind == "shape":
+            self._shape()
+        elif kind in ("bezier", "heightMap", "julia", "mandelbulb", "waveFront"):
+            raise Unsupported(f"primitive {kind}: the GPU path renders meshes and shapes")
+        else:
+            raise t.error(f"unknown primitive type {kind}")
+
+    def _mesh(self):
+        """pMesh + mkTriangleMesh: vertices moved to world space with
+        transPoint at build (TriangleMesh.hs:58), faces fanned (triangulate)."""
+        t = self.t
+        vc = t.named_int("vertexCount")
+        fc = t.named_int("faceCount")
+        verts = []
+        for _ in range(vc):
+            t.expect("v")
+            verts.append(trans_point(self.s.transform, t.vec()))
+        idx = []
+        for _ in range(fc):
+            t.expect("f")
+            face = [t.integ()]
+            while t.peek()[0] == "num":
+                face.append(t.integ())
+            for k in range(1, len(face) - 1):
+                idx += [face[0], face[k], face[k + 1]]
+        v = np.asarray(verts, np.float32).reshape(-1, 3)
+        m = self.scene.add_mesh(v, np.asarray(idx, np.int32), self._material())
+        self.s.blocks.insert(0, ("mesh", m))
+
+    def _shape(self):
+        t = self.t
+
+        def body():
+            kind = t.word()
+            if kind == "box":  # mkBox (Shape.hs:41-44)
+                a, b = t.named_vec("pmin"), t.named_vec("pmax")
+                lo = [_ghc_min(a[k], b[k]) for k in range(3)]
+                hi = [_ghc_max(a[k], b[k]) for k in range(3)]
+                return abi.SHAPE_BOX, tuple(lo + hi)
+            if kind == "cylinder":  # mkCylinder (Shape.hs:47-56)
+                r = t.named_flt("radius")
+                z0, z1 = t.named_flt("zmin"), t.named_flt("zmax")
+                pm = xf.radians(_clamp(t.named_flt("phiMax"), F(0), F(360)))
+                return abi.SHAPE_CYLINDER, (r, _ghc_min(z0, z1), _ghc_max(z0, z1), pm)
+            if kind == "disk":  # mkDisk (Shape.hs:59-68)
+                h = t.named_flt("height")
+                r0, r1 = t.named_flt("radius"), t.named_flt("innerRadius")
+                pm = xf.radians(_clamp(t.named_flt("phiMax"), F(0), F(360)))
+                return abi.SHAPE_DISK, (h, _ghc_max(r0, r1), _ghc_min(r0, r1), pm)
+            if kind == "quad":
+                return abi.SHAPE_QUAD, (t.flt(), t.flt())
+            if kind == "sphere":
+                return abi.SHAPE_SPHERE, (t.named_flt("radius"),)
+            raise t.error(f"unknown shape type {kind}")
+        kind, params = t.block(body)
+        # mkGeom (transform s) False (material s) (emit s) shp sid
+        sh = self.scene.add_shape(kind, tuple(float(p) for p in params), self.s.transform,
+                                  self._material(), emission=self.s.emit)
+        self.s.blocks.insert(0, ("shape", sh))
+
+
+def parse(text: str, base_path: str | Path = ".") -> Job:
+    """Parses .bling source text (parseJob, RenderJob.hs:36-48)."""
+    return _Parser(text, Path(base_path)).job()
+
+
+def load(path: str | Path) -> Job:
+    """Reads and parses a .bling file; relative resources resolve against its
+    directory."""
+    p = Path(path)
+    return parse(p.read_text(), p.parent)

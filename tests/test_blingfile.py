@@ -1,0 +1,197 @@
+"""The .bling reader (bling_gb300/blingfile.py) against the reference's
+parser semantics (src/lib/Graphics/Bling/IO/*.hs): parser-state defaults,
+newest-first primitive and light order, transforms applied to mesh vertices
+with binary32 transPoint, face fans, shape constructors, materials, spectra,
+renderer selection; plus an oracle render of a parsed scene.  The GPU parity
+of a parsed scene is in test_render_gpu.py."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from bling_gb300 import abi
+from bling_gb300 import blingfile as B
+from bling_gb300 import transform as xf
+from bling_gb300.spectrum import constant, rgb_to_spectrum
+from oracle.oracle import OracleScene
+
+F = np.float32
+
+SCENE = """
+# a small room in .bling syntax
+filter mitchell 2 2 0.333333 0.333333
+renderer { sampler sampled { sampler { stratified 3 2 } integrator { path maxDepth 6 sampleDepth 2 } } }
+imageSize 48 32
+
+transform { lookAt { pos 0 1 -4 look 0 0.5 0 up 0 1 0 } }
+camera { perspective fov 45 lensRadius 0 focalDistance 10 }
+newTransform { }
+
+material { matte kd { constant rgbR 0.6 0.6 0.6 } sigma { constant 0 } }
+prim { mesh vertexCount 4 faceCount 1
+   v -2 0 -2  v 2 0 -2  v 2 0 2  v -2 0 2
+   f 0 3 2 1 }
+
+material { plastic kd { constant rgbR %20 40 c0 } ks { constant spd { 400 0.3, 700 0.5, 550 0.4 } }
+           rough { constant 0.1 } }
+transform { translate -0.7 0.4 0 }
+prim { shape { sphere radius 0.4 } }
+
+material { glass ior { constant 1.5 } kr { constant rgbR 1 1 1 } kt { constant rgbR 1 1 1 } }
+newTransform { rotateY 30 translate 0.7 0.3 0.2 }
+prim { shape { box pmin 0.3 0.3 0.3 pmax -0.3 -0.3 -0.3 } }
+
+material { metal eta { constant rgbR 0.2 0.2 0.2 } k { constant rgbR 3.9 3.9 3.9 } rough { constant 0.05 } }
+newTransform { rotateX 90 translate 0 0.01 1 }
+prim { shape { disk height 0 radius 0.3 innerRadius 0.5 phiMax 400 } }
+
+emission { rgbI 6 6 6 }
+newTransform { rotateX -90 translate 0 2 0 }
+prim { shape { quad 0.5 0.5 } }
+emission { none }
+
+light { directional intensity rgbI 1 0.9 0.8 normal 0.3 1 -0.4 }
+light { infinite { rotateX -90 } l { constant rgbI 0.2 0.25 0.3 } }
+"""
+
+
+@pytest.fixture(scope="module")
+def job():
+    return B.parse(SCENE)
+
+
+def test_parser_state_and_renderer(job):
+    assert (job.width, job.height) == (48, 32)
+    assert job.renderer == "path"
+    assert job.sampler_kind == abi.SAMPLER_STRATIFIED and job.strata == (3, 2)
+    assert (job.max_depth, job.sample_depth) == (6, 2)
+    assert job.filter_kind == abi.FILTER_MITCHELL
+    assert job.filter_params[0] == F(2) and job.filter_params[2] == B.f32_of_decimal("0.333333")
+    p = job.params(seed=9)
+    assert (p.width, p.height, p.strata_x, p.strata_y, p.max_depth, p.sample_depth, p.rr_depth,
+            p.seed) == (48, 32, 3, 2, 6, 2, 7, 9)
+
+
+def test_defaults_of_an_empty_file():
+    j = B.parse("# nothing\n")
+    assert (j.width, j.height, j.renderer, j.strata, j.max_depth, j.sample_depth) == \
+        (640, 480, "path", (2, 2), 7, 3)
+    assert j.filter_kind == abi.FILTER_BOX
+    # defaultCamera: translate (0 0 -5), fov 90, built for 640 x 480
+    c2w, r2c = xf.perspective_camera(xf.translate(0, 0, -5), 0, 1, 90, 640, 480)
+    assert np.array_equal(np.asarray(j.scene.camera.c2w, F), c2w.m)
+    assert np.array_equal(np.asarray(j.scene.camera.r2c, F), r2c.m)
+
+
+def test_primitives_and_lights_newest_first(job):
+    sc = job.scene
+    # prim blocks are prepended (RenderJob.hs:52): quad, disk, box, sphere, mesh
+    kinds = [sc.shapes[~v].kind if v < 0 else "mesh" for v in sc.prim_order]
+    assert kinds == [abi.SHAPE_QUAD, abi.SHAPE_DISK, abi.SHAPE_BOX, abi.SHAPE_SPHERE, "mesh"]
+    # lights are prepended too: infinite, then directional
+    assert [l.kind for l in sc.lights] == [abi.LIGHT_INFINITE, abi.LIGHT_DIRECTIONAL]
+    assert sc.lights[0].env.shape == (1, 1, 16)
+    assert np.array_equal(sc.lights[0].env[0, 0], rgb_to_spectrum((F(0.2), F(0.25), F(0.3)), True))
+    assert np.array_equal(sc.lights[0].w2l.m, xf.rotate_x(-90).m)
+    d = sc.lights[1].vec
+    assert np.array_equal(np.asarray(d, F), np.asarray(xf.normalize([F(0.3), F(1), F(-0.4)]), F))
+    # only the quad emits
+    em = [s.emission is not None for s in sc.shapes]
+    assert em == [False, False, False, True]
+    assert np.array_equal(sc.shapes[3].emission, rgb_to_spectrum((F(6), F(6), F(6)), True))
+
+
+def test_mesh_vertices_and_face_fan(job):
+    m = job.scene.meshes[0]
+    assert m.indices.tolist() == [0, 3, 2, 0, 2, 1]  # triangulate: fan of f 0 3 2 1
+    # newTransform { } before the mesh: identity, vertices unchanged
+    assert m.vertices.tolist()[1] == [2.0, 0.0, -2.0]
+
+
+def test_shape_transforms_and_constructors(job):
+    sc = job.scene
+    sphere, box, disk, quad = sc.shapes
+    # "transform" composes onto the current transform: t <> current
+    assert np.array_equal(sphere.o2w.m, xf.concat(xf.translate(F(-0.7), F(0.4), F(0)),
+                                                  xf.identity()).m)
+    # mkBox: per-axis min and max of the two corners
+    assert box.params == tuple(float(F(x)) for x in [-0.3, -0.3, -0.3, 0.3, 0.3, 0.3])
+    t = xf.concat(xf.rotate_y(F(30)), xf.concat(xf.translate(F(0.7), F(0.3), F(0.2)), xf.identity()))
+    assert np.array_equal(box.o2w.m, t.m)
+    # mkDisk: outer = max, inner = min, phiMax clamped to 360 degrees, in radians
+    assert disk.params[1] == 0.5 and disk.params[2] == float(F(0.3))
+    assert disk.params[3] == float(xf.radians(F(360)))
+    assert quad.params == (0.5, 0.5)
+
+
+def test_materials(job):
+    mats = job.scene.materials
+    kinds = [m.kind for m in mats]
+    assert kinds == [abi.MAT_MATTE, abi.MAT_PLASTIC, abi.MAT_GLASS, abi.MAT_METAL]
+    plastic = mats[1]
+    assert np.array_equal(np.asarray(plastic.kd, F),
+                          rgb_to_spectrum((F(0x20) / F(255), F(0x40) / F(255), F(0xc0) / F(255))))
+    assert plastic.roughness == float(F(0.1))
+    ks = np.asarray(plastic.ks, F)
+    # pairs sorted by wavelength (400, 550, 700); band 0 ([400, 418.75]) averages
+    # the samples from the first at or above 400 to the first at or above
+    # 418.75 (avgSpd of an IrregularSpd); the last band takes the 700 sample
+    assert ks[0] == (F(0.3) + F(0.4)) / F(2) and ks[-1] == F(0.5)
+    glass = mats[2]
+    assert glass.ior == 1.5 and np.array_equal(np.asarray(glass.kt, F), rgb_to_spectrum((1, 1, 1)))
+
+
+def test_constant_spd_gives_a_flat_spectrum():
+    s = B.spectrum_from_spd([(380.0, 0.25), (500.0, 0.25), (720.0, 0.25)])
+    assert np.array_equal(s, constant(0.25))
+
+
+def test_other_renderers_parse_and_are_named():
+    j = B.parse("renderer { sppm photonCount 20000 maxDepth 10 radius 10 alpha 0.9 }")
+    assert j.renderer == "sppm"
+    j = B.parse("renderer { sampler sampled { sampler { random 16 } "
+                "integrator { directLighting maxDepth 3 } } }")
+    assert j.renderer == "sampler/directLighting" and j.strata == (16, 1)
+    assert j.sampler_kind == abi.SAMPLER_RANDOM
+
+
+@pytest.mark.parametrize("src,what", [
+    ("material { mirror kr { constant rgbR 1 1 1 } }", "mirror"),
+    ("material { matte kd { checker 1 1 1 tex1 { constant rgbR 1 1 1 } "
+     "tex2 { constant rgbR 0 0 0 } } sigma { constant 0 } }", "checker"),
+    ("prim { julia c 0 0 0 0 epsilon 0.1 iterations 4 }", "julia"),
+    ("light { infinite { } l { sunSky east 0 0 1 sunDir 0 1 0 turbidity 2 } }", "sunSky"),
+])
+def test_unsupported_constructs_are_named(src, what):
+    with pytest.raises(B.Unsupported, match=what):
+        B.parse(src)
+
+
+def test_syntax_errors_carry_the_line():
+    with pytest.raises(B.BlingFileError, match="line 3"):
+        B.parse("imageSize 8 8\n\nmaterial { plaster }\n")
+
+
+def test_parsed_scene_renders_on_the_oracle(job):
+    p = job.params()
+    film, st = OracleScene(job.scene).render_pass(p, 0)
+    assert np.isfinite(film).all()
+    # the filter-padded extent (imageWindow', Image.hs:170-176): 53 x 37 pixels, 6 spp
+    assert st["path_samples"] == 53 * 37 * 6
+    assert film[..., 2].sum() > 0
+
+
+REF_EXAMPLES = Path("/root/reference/examples")
+
+
+@pytest.mark.skipif(not REF_EXAMPLES.exists(), reason="reference examples not present")
+def test_reference_cornell_box_example_parses():
+    j = B.load(REF_EXAMPLES / "cornell-box.bling")
+    assert (j.width, j.height) == (480, 480)
+    assert j.renderer == "sppm"  # the file's last renderer block
+    assert j.scene.n_triangles == 30 and len(j.scene.shapes) == 1
+    assert j.scene.shapes[0].emission is not None  # the ceiling light quad
+    film, _ = OracleScene(j.scene).render_pass(
+        B.Job(j.scene, 24, 24, abi.FILTER_BOX, (0, 0, 0, 0), "path", strata=(1, 1),
+              max_depth=3).params(), 0)
+    assert np.isfinite(film).all()

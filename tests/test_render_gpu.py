@@ -204,6 +204,18 @@ def test_random_sampler_vs_oracle(gpu_ctx):
     assert st_g["path_samples"] == st_o[0]["path_samples"] == 50 * 50 * 8
 
 
+def test_parsed_bling_scene_vs_oracle(gpu_ctx):
+    """a scene read from .bling text (mesh, four materials, area, directional
+    and infinite lights, Mitchell filter) renders on the GPU as on the oracle"""
+    from bling_gb300 import blingfile
+    from test_blingfile import SCENE
+    job = blingfile.parse(SCENE)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, job.scene, job.params(seed=4))
+    _compare(fg, fo, rel=2e-3, frac=0.9)
+    assert st_g["path_samples"] == st_o[0]["path_samples"]
+    assert st_g["nonfinite_drops"] == 0
+
+
 def test_passes_accumulate(gpu_ctx):
     sc = S.cornell_room(32, 32)
     p = S.cornell_params(32, 32, spp_side=2)
