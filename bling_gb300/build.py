@@ -26,8 +26,6 @@ CU_SRCS = ["api.cu", "kernels_trace.cu", "integrator.cu", "scene_upload.cu", "ba
            "server.cu"]
 CPP_SRCS = ["bvh.cpp"]
 PROBE_SRCS = ["l2probe.cu"]
-HEADERS = ["dmath.cuh", "dshape.cuh", "trace.cuh", "internal.h", "integrator.h", "bvh.h",
-           "spectrum_tables.h", "integrator_device.cuh", "filter_host.h"]
 
 
 def nvcc() -> str:
@@ -38,8 +36,10 @@ def nvcc() -> str:
 
 
 def _deps():
-    out = [CSRC / h for h in HEADERS] + [PKG.parent / "include" / "bling_gpu.h", Path(__file__)]
-    return out
+    """Every header of csrc/ (any source may include any of them), the public
+    header and this recipe."""
+    headers = sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh"))
+    return headers + [PKG.parent / "include" / "bling_gpu.h", Path(__file__)]
 
 
 def _stale(obj: Path, src: Path) -> bool:

@@ -40,6 +40,7 @@ struct BatchJobDev {
   int32_t scene;
   int32_t pad;
   unsigned long long start, total;  // the job's samples in the engine's sample sequence
+  unsigned long long offset;        // sample index (in the pass) of the job's first sample
   float filter[256];
 };
 
@@ -183,7 +184,7 @@ __global__ void __launch_bounds__(128) k_regen(BatchCtl* ctl, const BatchJobDev*
     unsigned long long g = base + i;
     int j = findJob(jobs, job_mask, lo, hi, g);
     const BatchJobDev& J = jobs[j];
-    unsigned long long local = g - J.start;
+    unsigned long long local = g - J.start + J.offset;
     S.job[q] = j;
     S.scene[q] = J.scene;
     S.depth[q] = 0;
@@ -296,7 +297,7 @@ __global__ void k_bin_flip(BatchCtl* ctl) {
 
 // closest hits of the current buffer's rays, each lane in its ray's scene
 template <bool WIDE>
-__global__ void __launch_bounds__(128) k_btrace(BatchCtl* ctl,
+__global__ void __launch_bounds__(128, 10) k_btrace(BatchCtl* ctl,
                                                 const BatchSceneDev* __restrict__ scenes,
                                                 Slots tmp, PathStates ps) {
   const int cur = ctl->cur;
@@ -314,7 +315,7 @@ __global__ void __launch_bounds__(128) k_btrace(BatchCtl* ctl,
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(128) k_btrace_shadow(BatchCtl* ctl,
+__global__ void __launch_bounds__(128, 10) k_btrace_shadow(BatchCtl* ctl,
                                                        const BatchSceneDev* __restrict__ scenes,
                                                        Slots tmp, PathStates ps, BatchQueues Q) {
   const PathState& S = ps.b[ctl->cur];
@@ -332,7 +333,7 @@ __global__ void __launch_bounds__(128) k_btrace_shadow(BatchCtl* ctl,
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(128) k_btrace_mis(BatchCtl* ctl,
+__global__ void __launch_bounds__(128, 10) k_btrace_mis(BatchCtl* ctl,
                                                     const BatchSceneDev* __restrict__ scenes,
                                                     Slots tmp, PathStates ps, BatchQueues Q) {
   const PathState& S = ps.b[ctl->cur];
@@ -395,7 +396,7 @@ __device__ __forceinline__ void pathsDone(bool fin, int job, BatchCtl* ctl,
   if (b && lane == 0) atomicAdd(&ctl->finished, (unsigned long long)__popc(b));
 }
 
-__global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJobDev* __restrict__ jobs,
+__global__ void __launch_bounds__(128, 4) k_bshade(BatchCtl* ctl, const BatchJobDev* __restrict__ jobs,
                                                 const BatchSceneDev* __restrict__ scenes,
                                                 Slots tmp, PathStates ps, BatchQueues Q,
                                                 unsigned long long* __restrict__ job_done) {
@@ -799,7 +800,7 @@ int batch_scene(BatchEngine* b, uint64_t key, const DevAccel& A, const DevShadin
 
 int batch_submit(BatchEngine* b, int scene, const bling_camera_desc& cam, float* d_film, int fw,
                  int fh, const bling_render_params& p, uint64_t pass, int64_t& job_id,
-                 std::string& err) {
+                 std::string& err, uint64_t first, uint64_t count) {
   if (scene < 0 || scene >= (int)b->scene_keys.size()) {
     err = "unknown batch scene";
     return BLING_ERR_INVALID_ARG;
@@ -817,6 +818,14 @@ int batch_submit(BatchEngine* b, int scene, const bling_camera_desc& cam, float*
     err = "job sample count out of range";
     return BLING_ERR_INVALID_ARG;
   }
+  // a slice [first, first + count) of the pass's samples (count 0: the rest)
+  if (first >= total || count > total - first) {
+    err = "sample range outside the pass";
+    return BLING_ERR_INVALID_ARG;
+  }
+  if (count == 0) count = total - first;
+  h.offset = first;
+  total = count;
   filterTableHost(p.filter_kind, p.filter_params, h.P.fw, h.P.fh, h.filter);
   h.cam = cam;
   h.film = d_film;

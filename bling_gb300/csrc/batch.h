@@ -55,9 +55,12 @@ void batch_destroy(BatchEngine* b);
 // within a process) and returns its table index
 int batch_scene(BatchEngine* b, uint64_t key, const DevAccel& A, const DevShading& S,
                 const float lo[3], const float hi[3], int& index, std::string& err);
+// submits samples [first, first + count) of one pass (count 0: all from
+// first on); the samples keep their pass indices, so slices of one pass
+// submitted as separate jobs render the film the whole pass renders
 int batch_submit(BatchEngine* b, int scene, const bling_camera_desc& cam, float* d_film, int fw,
                  int fh, const bling_render_params& p, uint64_t pass, int64_t& job_id,
-                 std::string& err);
+                 std::string& err, uint64_t first = 0, uint64_t count = 0);
 // runs `iterations` wavefront iterations (fewer if all work is done) and
 // updates the jobs' progress
 int batch_step(BatchEngine* b, int iterations, std::string& err);

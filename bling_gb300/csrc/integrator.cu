@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(128) k_class_scatter(const int32_t* __restrict
 
 // closest hit of the live paths' rays (scIntersect)
 template <bool WIDE>
-__global__ void __launch_bounds__(128) k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
+__global__ void __launch_bounds__(128, 10) k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
                                                const unsigned long long* __restrict__ qcount,
                                                unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)*qcount;
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(128) k_trace(DevAccel A, Slots st, const int32
 
 // occlusion of the shadow rays (occluded, Scene.hs:168-170)
 template <bool WIDE>
-__global__ void __launch_bounds__(128) k_trace_shadow(DevAccel A, Slots st,
+__global__ void __launch_bounds__(128, 10) k_trace_shadow(DevAccel A, Slots st,
                                                       const int32_t* __restrict__ queue,
                                                       unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_SHADOW];
@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(DevAccel A, Slots st,
 
 // closest hit of the BSDF-sampled MIS rays
 template <bool WIDE>
-__global__ void __launch_bounds__(128) k_trace_mis(DevAccel A, Slots st,
+__global__ void __launch_bounds__(128, 10) k_trace_mis(DevAccel A, Slots st,
                                                    const int32_t* __restrict__ queue,
                                                    unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_MIS];
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(128) k_trace_mis(DevAccel A, Slots st,
 }
 
 // one vertex of every live path, up to its shadow and MIS rays (Path.hs:49-87)
-__global__ void __launch_bounds__(128, 3) k_shade(DevAccel A, DevShading S, PassParams P, Slots st,
+__global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, PassParams P, Slots st,
                                                Queues Q, int depth, int live_in,
                                                float* __restrict__ film,
                                                unsigned long long* __restrict__ counters) {

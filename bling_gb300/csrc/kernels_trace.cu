@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(kTraceBlock)
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kTraceBlock)
+__global__ void __launch_bounds__(kTraceBlock, 10)
     k_trace_any(DevAccel A, const float* __restrict__ rays, int64_t n,
                 uint8_t* __restrict__ out_hit, unsigned long long* __restrict__ next_ray) {
   traceWarpPersistent<true, WIDE, false>(

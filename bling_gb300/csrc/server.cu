@@ -40,7 +40,9 @@ struct ServerJob {
   int rc = BLING_OK;
   std::string err;
   float* d_film = nullptr;
-  int64_t batch_id = -1;
+  int scene_idx = -1;          // the scene's batch table index
+  uint64_t sent = 0;           // samples of the pass handed to the batch, in slices
+  std::vector<int64_t> slices; // batch job ids of the slices
   std::vector<float> result;  // (w, X, Y, Z) per pixel once done
   double t_submit = 0, t_admit = 0, t_done = 0;
 };
@@ -55,6 +57,8 @@ struct bling_server {
   uint64_t in_use = 0;      // base_bytes + films of admitted jobs
   int iters_per_step = 4;
   int max_jobs = 1024;
+  uint64_t slice = 1 << 20;    // samples per slice handed to the batch
+  uint64_t backlog = 1 << 21;  // submitted but unstarted samples kept queued
   std::chrono::steady_clock::time_point t0;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
@@ -89,7 +93,22 @@ void failJob(ServerJob* j, int rc, const std::string& msg) {
   j->err = msg;
 }
 
-// one admission round and one step of the batch; called without S->mu held
+// the job with the fewest samples left to hand out, or null
+ServerJob* shortestUnsent(const std::vector<ServerJob*>& running) {
+  ServerJob* best = nullptr;
+  for (ServerJob* j : running) {
+    if (j->state != J_RUNNING || j->sent >= j->samples) continue;
+    if (!best || j->samples - j->sent < best->samples - best->sent) best = j;
+  }
+  return best;
+}
+
+// one admission round and one step of the batch; called without S->mu held.
+// Admitted jobs get a film and their scene's batch index; their samples go
+// to the batch in slices of at most S->slice, shortest remaining job first,
+// while fewer than S->backlog submitted samples wait for a free path slot.
+// A job that arrives while a long one runs therefore starts within about
+// one backlog of samples, and its work shares the wavefront with the rest.
 void serveRound(bling_server* S, std::vector<ServerJob*>& admit, std::vector<ServerJob*>& running,
                 std::vector<ServerJob*>& finished) {
   bling_ctx* c = S->ctx;
@@ -106,14 +125,10 @@ void serveRound(bling_server* S, std::vector<ServerJob*>& admit, std::vector<Ser
       continue;
     }
     e = cudaMemsetAsync(j->d_film, 0, j->bytes, c->stream);
-    int idx = 0;
     int rc = e == cudaSuccess ? BLING_OK : BLING_ERR_CUDA;
     if (rc == BLING_OK)
       rc = batch_scene(S->eng, j->scene->serial, j->scene->accel, j->scene->shading, j->scene->lo,
-                       j->scene->hi, idx, err);
-    if (rc == BLING_OK)
-      rc = batch_submit(S->eng, idx, j->camera, j->d_film, j->params.width, j->params.height,
-                        j->params, j->pass, j->batch_id, err);
+                       j->scene->hi, j->scene_idx, err);
     if (rc != BLING_OK) {
       cudaFree(j->d_film);
       j->d_film = nullptr;
@@ -125,6 +140,28 @@ void serveRound(bling_server* S, std::vector<ServerJob*>& admit, std::vector<Ser
     running.push_back(j);
   }
   if (running.empty()) return;
+  BatchStats bs;
+  batch_stats(S->eng, bs);
+  uint64_t queued = bs.samples_submitted - bs.samples_started;
+  while (queued < S->backlog) {
+    ServerJob* j = shortestUnsent(running);
+    if (!j) break;
+    uint64_t n = std::min<uint64_t>(S->slice, j->samples - j->sent);
+    int64_t id = -1;
+    int rc = batch_submit(S->eng, j->scene_idx, j->camera, j->d_film, j->params.width,
+                          j->params.height, j->params, j->pass, id, err, j->sent, n);
+    if (rc == BLING_ERR_STATE) break;  // job table full until slices complete
+    if (rc != BLING_OK) {
+      // no further slices; the job fails once its slices in flight are done
+      j->rc = rc;
+      j->err = err;
+      j->sent = j->samples;
+      continue;
+    }
+    j->slices.push_back(id);
+    j->sent += n;
+    queued += n;
+  }
   int rc = batch_step(S->eng, S->iters_per_step, err);
   if (rc != BLING_OK) {
     for (ServerJob* j : running) {
@@ -138,21 +175,29 @@ void serveRound(bling_server* S, std::vector<ServerJob*>& admit, std::vector<Ser
   }
   std::vector<ServerJob*> still;
   for (ServerJob* j : running) {
-    uint64_t d = 0, t = 0;
-    batch_job_status(S->eng, j->batch_id, d, t, err);
-    if (d < t) {
+    bool done = j->sent >= j->samples;
+    for (size_t k = 0; done && k < j->slices.size(); k++) {
+      uint64_t d = 0, t = 0;
+      batch_job_status(S->eng, j->slices[k], d, t, err);
+      done = d >= t;
+    }
+    if (!done) {
       still.push_back(j);
       continue;
     }
-    j->result.resize(j->bytes / sizeof(float));
-    cudaError_t e = cudaMemcpy(j->result.data(), j->d_film, j->bytes, cudaMemcpyDeviceToHost);
+    if (j->rc != BLING_OK) {
+      failJob(j, j->rc, j->err);
+    } else {
+      j->result.resize(j->bytes / sizeof(float));
+      cudaError_t e = cudaMemcpy(j->result.data(), j->d_film, j->bytes, cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess)
+        failJob(j, BLING_ERR_CUDA, std::string("film copy: ") + cudaGetErrorString(e));
+      else
+        j->state = J_DONE;
+    }
     cudaFree(j->d_film);
     j->d_film = nullptr;
     j->t_done = S->now();
-    if (e != cudaSuccess)
-      failJob(j, BLING_ERR_CUDA, std::string("film copy: ") + cudaGetErrorString(e));
-    else
-      j->state = J_DONE;
     finished.push_back(j);
   }
   running.swap(still);
@@ -165,6 +210,9 @@ void workerLoop(bling_server* S) {
     if (S->stop && S->running.empty()) break;
     std::vector<ServerJob*> admit;
     if (!S->stop) {
+      // smallest jobs first (ties in arrival order)
+      std::stable_sort(S->pending.begin(), S->pending.end(),
+                       [](const ServerJob* a, const ServerJob* b) { return a->samples < b->samples; });
       while (!S->pending.empty()) {
         ServerJob* j = S->pending.front();
         if (S->in_use + j->bytes > S->budget) break;
@@ -226,6 +274,10 @@ int bling_server_create(bling_ctx* c, const bling_server_opts* o, bling_server**
     if (o->iters_per_step > 0) S->iters_per_step = o->iters_per_step;
   }
   S->max_jobs = cfg.max_jobs;
+  // slices of half the path slots, and one slot pool's worth of samples
+  // queued ahead of the wavefront
+  S->slice = std::max<uint64_t>(uint64_t(1) << 12, (uint64_t)cfg.slots / 2);
+  S->backlog = std::max<uint64_t>(S->slice, (uint64_t)cfg.slots);
   {
     std::lock_guard<std::mutex> g(c->mu);
     if (!c->stream) {

@@ -151,3 +151,30 @@ def test_submit_does_not_wait_for_the_running_step(gpu_ctx):
     srv.close()
     assert dt < 0.02, dt
     assert all(r[1]["submitted"] < res_big[1]["finished"] for r in res)
+
+
+def test_short_job_overtakes_a_long_one():
+    """Samples go to the wavefront in slices, shortest remaining job first:
+    a short job submitted while a long one runs finishes long before it, and
+    both films are the ones their jobs render alone."""
+    from bling_gb300.api import Context
+    ctx = Context(device=0)
+    try:
+        sc = S.heightfield_scene(ns=257, n_spheres=64, width=256, height=256, env_size=(64, 32))
+        g = ctx.scene(sc)
+        srv = Server(ctx, slots=1 << 20, iters_per_step=8)
+        long_p = S.heightfield_params(256, 256, spp_side=16, max_depth=8)  # 17M samples
+        short_p = S.heightfield_params(96, 96, spp_side=2, max_depth=4)
+        t_long = srv.submit(g, long_p, 0)
+        time.sleep(0.02)
+        t_short = srv.submit(g, short_p, 1)
+        f_short, times_short = srv.wait(t_short)
+        f_long, times_long = srv.wait(t_long)
+        srv.close()
+        assert times_short["finished"] < times_long["finished"]
+        assert (times_short["finished"] - times_short["submitted"]) < \
+            0.5 * (times_long["finished"] - times_long["submitted"])
+        _same(f_short, _alone(ctx, sc, short_p, 1))
+        _same(f_long, _alone(ctx, sc, long_p, 0))
+    finally:
+        ctx.close()
