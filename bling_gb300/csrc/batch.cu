@@ -297,7 +297,7 @@ __global__ void k_bin_flip(BatchCtl* ctl) {
 
 // closest hits of the current buffer's rays, each lane in its ray's scene
 template <bool WIDE>
-__global__ void __launch_bounds__(128, 10) k_btrace(BatchCtl* ctl,
+__global__ void __launch_bounds__(128) k_btrace(BatchCtl* ctl,
                                                 const BatchSceneDev* __restrict__ scenes,
                                                 Slots tmp, PathStates ps) {
   const int cur = ctl->cur;
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(128, 10) k_btrace(BatchCtl* ctl,
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(128, 10) k_btrace_shadow(BatchCtl* ctl,
+__global__ void __launch_bounds__(128) k_btrace_shadow(BatchCtl* ctl,
                                                        const BatchSceneDev* __restrict__ scenes,
                                                        Slots tmp, PathStates ps, BatchQueues Q) {
   const PathState& S = ps.b[ctl->cur];
@@ -333,7 +333,7 @@ __global__ void __launch_bounds__(128, 10) k_btrace_shadow(BatchCtl* ctl,
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(128, 10) k_btrace_mis(BatchCtl* ctl,
+__global__ void __launch_bounds__(128) k_btrace_mis(BatchCtl* ctl,
                                                     const BatchSceneDev* __restrict__ scenes,
                                                     Slots tmp, PathStates ps, BatchQueues Q) {
   const PathState& S = ps.b[ctl->cur];
@@ -396,7 +396,7 @@ __device__ __forceinline__ void pathsDone(bool fin, int job, BatchCtl* ctl,
   if (b && lane == 0) atomicAdd(&ctl->finished, (unsigned long long)__popc(b));
 }
 
-__global__ void __launch_bounds__(128, 4) k_bshade(BatchCtl* ctl, const BatchJobDev* __restrict__ jobs,
+__global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJobDev* __restrict__ jobs,
                                                 const BatchSceneDev* __restrict__ scenes,
                                                 Slots tmp, PathStates ps, BatchQueues Q,
                                                 unsigned long long* __restrict__ job_done) {

@@ -274,10 +274,10 @@ int bling_server_create(bling_ctx* c, const bling_server_opts* o, bling_server**
     if (o->iters_per_step > 0) S->iters_per_step = o->iters_per_step;
   }
   S->max_jobs = cfg.max_jobs;
-  // slices of half the path slots, and one slot pool's worth of samples
-  // queued ahead of the wavefront
+  // slices of half the path slots; queued ahead of the wavefront, enough
+  // samples to refill every slot in each iteration of a step
   S->slice = std::max<uint64_t>(uint64_t(1) << 12, (uint64_t)cfg.slots / 2);
-  S->backlog = std::max<uint64_t>(S->slice, (uint64_t)cfg.slots);
+  S->backlog = std::max<uint64_t>(S->slice, (uint64_t)cfg.slots * (uint64_t)S->iters_per_step);
   {
     std::lock_guard<std::mutex> g(c->mu);
     if (!c->stream) {

@@ -160,14 +160,14 @@ def test_short_job_overtakes_a_long_one():
     from bling_gb300.api import Context
     ctx = Context(device=0)
     try:
-        sc = S.heightfield_scene(ns=257, n_spheres=64, width=256, height=256, env_size=(64, 32))
+        sc = S.heightfield_scene(ns=257, n_spheres=64, width=512, height=512, env_size=(64, 32))
         g = ctx.scene(sc)
         srv = Server(ctx, slots=1 << 20, iters_per_step=8)
-        long_p = S.heightfield_params(256, 256, spp_side=16, max_depth=8)  # 17M samples
+        long_p = S.heightfield_params(512, 512, spp_side=16, max_depth=8)  # 67M samples
         short_p = S.heightfield_params(96, 96, spp_side=2, max_depth=4)
-        t_long = srv.submit(g, long_p, 0)
-        time.sleep(0.02)
-        t_short = srv.submit(g, short_p, 1)
+        t_long = srv.submit(g, long_p, 0, camera=sc.camera_for(512, 512))
+        time.sleep(0.01)
+        t_short = srv.submit(g, short_p, 1, camera=sc.camera_for(96, 96))
         f_short, times_short = srv.wait(t_short)
         f_long, times_long = srv.wait(t_long)
         srv.close()
