@@ -409,19 +409,34 @@ def measure_serving(args):
     Reported: p50/p99 latency (arrival to film on the host) and path
     samples/s over the run, next to the same jobs run alone one after the
     other through bling_render_pass (latency of that FIFO from the same
-    arrivals, each job's service time measured)."""
-    import threading
+    arrivals, each job's service time measured).
 
-    import torch
-
+    A second line, `small_jobs`, runs the same comparison for preview-sized
+    traffic on the same scenes: 256 jobs at 2000/s, sides log-uniform in
+    [64, 128], 1-16 spp."""
     from bling_gb300 import scene as S
-    from bling_gb300.api import Context, Server
+    from bling_gb300.api import Context
     ctx = Context(device=0)
     t0 = time.perf_counter()
     scenes = S.serving_scenes()
     gs = [ctx.scene(s) for s in scenes]
     build_s = time.perf_counter() - t0
-    jobs = S.serving_jobs(n=args.serving_jobs)
+    out = _serve(args, ctx, scenes, gs, S.serving_jobs(n=args.serving_jobs), 200)
+    out["scene_build_s"] = round(build_s, 2)
+    out["small_jobs"] = _serve(args, ctx, scenes, gs,
+                               S.serving_jobs(n=256, rate=2000.0, seed=43, side_range=(64, 128),
+                                              spp_range=(1, 16)), 2000)
+    ctx.close()
+    return out
+
+
+def _serve(args, ctx, scenes, gs, jobs, rate):
+    import threading
+
+    import torch
+
+    from bling_gb300 import scene as S
+    from bling_gb300.api import Server
     cams = [scenes[j.scene].camera_for(j.params.width, j.params.height) for j in jobs]
     samples = [_extent_samples(j.params) for j in jobs]
     # plain: each job alone, in arrival order
@@ -468,11 +483,10 @@ def measure_serving(args):
     tot = sum(samples)
     plain_span = max(j.arrival for j in jobs) + 0.0
     plain_make = max(plain_lat[k] + jobs[k].arrival for k in range(len(jobs)))
-    ctx.close()
     return {
         "scenes": len(scenes), "triangles": sum(s.n_triangles for s in scenes) +
-        sum(len(s.shapes) for s in scenes), "scene_build_s": round(build_s, 2),
-        "jobs": len(jobs), "arrival_rate_per_s": 200, "arrivals_span_s": round(plain_span, 3),
+        sum(len(s.shapes) for s in scenes),
+        "jobs": len(jobs), "arrival_rate_per_s": rate, "arrivals_span_s": round(plain_span, 3),
         "path_samples": tot,
         "served": {"p50_latency_s": round(_pct(lat, 50), 4), "p99_latency_s": round(_pct(lat, 99), 4),
                    "makespan_s": round(last - first, 3),
