@@ -669,6 +669,7 @@ int batch_create(int device, cudaStream_t stream, const BatchConfig& cfg, BatchE
     err = "batch slots must be in [1024, 2^27]";
     return BLING_ERR_INVALID_ARG;
   }
+  static_assert(128 <= kMaxTraceBlock, "batch blocks must fit the traversal's shared stack");
   if (cfg.block != 64 && cfg.block != 128) {
     err = "batch block size must be 64 or 128";
     return BLING_ERR_INVALID_ARG;

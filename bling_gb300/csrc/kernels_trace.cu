@@ -15,6 +15,7 @@ __device__ __forceinline__ Ray loadRay(const float* __restrict__ rays, int64_t n
 }
 
 constexpr int kTraceBlock = 128;
+static_assert(kTraceBlock <= kMaxTraceBlock, "the traversal's shared stack holds kMaxTraceBlock lanes");
 
 template <bool WIDE>
 __global__ void __launch_bounds__(kTraceBlock)

@@ -216,6 +216,22 @@ def test_parsed_bling_scene_vs_oracle(gpu_ctx):
     assert st_g["nonfinite_drops"] == 0
 
 
+def test_film_resolve_and_png(gpu_ctx, tmp_path):
+    """bling_film_resolve (getPixel + xyzToRgb on the read film) equals the
+    host restatement, and the 8-bit image round-trips through a PNG"""
+    from bling_gb300 import image
+    sc = S.cornell_room(40, 30)
+    g = gpu_ctx.scene(sc)
+    film = gpu_ctx.film(40, 30)
+    g.render_pass(film, S.cornell_params(40, 30, spp_side=2), 0)
+    rgb = film.resolve()
+    assert np.array_equal(rgb, image.resolve(film.read()))
+    img = image.to_rgb8(rgb)
+    image.write_png(tmp_path / "cornell.png", img)
+    assert np.array_equal(image.read_png(tmp_path / "cornell.png"), img)
+    assert img.mean() > 10
+
+
 def test_passes_accumulate(gpu_ctx):
     sc = S.cornell_room(32, 32)
     p = S.cornell_params(32, 32, spp_side=2)
