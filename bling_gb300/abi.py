@@ -22,7 +22,7 @@ BLING_ERR_STATE = -6
 
 FLAG_WIDE_BVH = 1
 
-MAT_MATTE, MAT_PLASTIC, MAT_METAL, MAT_GLASS = 0, 1, 2, 3
+MAT_MATTE, MAT_PLASTIC, MAT_METAL, MAT_GLASS, MAT_MIRROR = 0, 1, 2, 3, 4
 SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_DISK, SHAPE_CYLINDER = 0, 1, 2, 3, 4
 LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE = 0, 1, 2
 FILTER_BOX, FILTER_GAUSS, FILTER_MITCHELL, FILTER_SINC, FILTER_TRIANGLE = 0, 1, 2, 3, 4

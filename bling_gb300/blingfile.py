@@ -16,7 +16,7 @@ The subset is what the GPU path renders:
   ``newTransform``, ``camera``, ``light``, ``material``, ``emission``,
   ``prim``;
 * primitives: ``mesh`` and ``shape`` (box, cylinder, disk, quad, sphere);
-* materials: matte, plastic, metal, glass, with ``constant`` textures;
+* materials: matte, plastic, metal, glass, mirror, with ``constant`` textures;
 * lights: directional, point, and infinite with a ``constant`` map;
 * spectra: ``rgbR``/``rgbI`` (decimal or ``%rrggbb``), ``spd { l v, ... }``,
   ``temp``;
@@ -531,9 +531,12 @@ class _Parser:
             kr = self._spectrum_texture("kr")
             kt = self._spectrum_texture("kt")
             return sc.add_material(abi.MAT_GLASS, ks=kr, kt=kt, ior=float(ior))
-        if kind in ("blackbody", "bumpMap", "shinyMetal", "substrate", "transMatte", "mirror"):
-            raise Unsupported(f"material {kind}: the GPU path renders matte, plastic, metal "
-                              "and glass")
+        if kind == "mirror":
+            kr = self._spectrum_texture("kr")
+            return sc.add_material(abi.MAT_MIRROR, ks=kr)
+        if kind in ("blackbody", "bumpMap", "shinyMetal", "substrate", "transMatte"):
+            raise Unsupported(f"material {kind}: the GPU path renders matte, plastic, metal, "
+                              "glass and mirror")
         raise t.error(f"unknown material type {kind}")
 
     def p_emission(self):

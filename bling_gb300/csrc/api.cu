@@ -356,6 +356,12 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   // ---- validate (mkTriangleMesh checks, TriangleMesh.hs:48-55)
   if (d->n_meshes < 0 || d->n_shapes < 0 || d->n_materials < 0 || d->n_lights < 0)
     return set_err(c, BLING_ERR_INVALID_ARG, "negative counts");
+  if (d->n_materials > 0 && !d->materials)
+    return set_err(c, BLING_ERR_INVALID_ARG, "null material array");
+  for (int i = 0; i < d->n_materials; i++)
+    if (d->materials[i].kind < BLING_MAT_MATTE || d->materials[i].kind > BLING_MAT_MIRROR)
+      return set_err(c, BLING_ERR_INVALID_ARG, "material %d: unknown kind %d", i,
+                     d->materials[i].kind);
   for (int i = 0; i < d->n_meshes; i++) {
     const bling_mesh_desc& m = d->meshes[i];
     if (m.n_indices % 3 != 0)

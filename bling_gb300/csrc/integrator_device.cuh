@@ -562,6 +562,14 @@ static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ 
     x.eta = m.eta;
     x.k = m.k;
     b.c[b.n++] = x;
+  } else if (kind == BLING_MAT_MIRROR) {
+    // mirrorMaterial: specRefl frNoOp (sClamp 0 1 kr) (Material.hs:68-72)
+    x.kind = BX_SPEC_REFL;
+    x.type = T_REFL | T_SPEC;
+    x.r = m.ks;
+    x.clampR = true;
+    x.fr = FR_NOOP;
+    b.c[b.n++] = x;
   } else {
     x.kind = BX_SPEC_REFL;
     x.type = T_REFL | T_SPEC;

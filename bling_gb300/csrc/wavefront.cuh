@@ -199,12 +199,14 @@ __device__ __forceinline__ void queueAppend(bool live, int slot, int32_t* __rest
 
 // ---- shading classes.  Before shading, the live paths of a bounce are
 // reordered by what their vertex runs: 0 for a miss or a degenerate ray (the
-// path ends), else 1 + the hit material's kind + 4 for an analytic shape
+// path ends), else 1 + the hit material's kind + kMaterialKinds for an analytic shape
 // (triangles and shapes build their geometry differently).  Lanes of a warp
 // then run one BSDF's and one geometry's code instead of all of them in turn.
 // The order within a class is the queue's order, up to the interleaving of
 // warps.
-constexpr int kShadeClasses = 9;
+constexpr int kMaterialKinds = 5;  // BLING_MAT_MATTE .. BLING_MAT_MIRROR
+constexpr int kShadeClasses = 1 + 2 * kMaterialKinds;
+static_assert(kShadeClasses <= 16, "class counts and cursors hold 16 entries each");
 
 __device__ __forceinline__ int shadeClass(const DevAccel& A, const DevShading& S, int prim) {
   if (prim < 0) return 0;
@@ -216,7 +218,7 @@ __device__ __forceinline__ int shadeClass(const DevAccel& A, const DevShading& S
     mi = A.shapes[~info.x].material;
     shape = 1;
   }
-  return 1 + (S.materials[mi].kind & 3) + 4 * shape;
+  return 1 + S.materials[mi].kind + kMaterialKinds * shape;
 }
 
 // counts a warp's entries per class (one atomic per class present); every

@@ -70,7 +70,8 @@ enum {
   BLING_MAT_MATTE = 0,   /* mkMatte kd sigma            (Material.hs:228-237) */
   BLING_MAT_PLASTIC = 1, /* mkPlastic kd ks roughness   (Material.hs:272-282) */
   BLING_MAT_METAL = 2,   /* mkMetal eta k roughness     (Material.hs:285-292) */
-  BLING_MAT_GLASS = 3    /* glassMaterial ior kr kt     (Material.hs:252-262) */
+  BLING_MAT_GLASS = 3,   /* glassMaterial ior kr kt     (Material.hs:252-262) */
+  BLING_MAT_MIRROR = 4   /* mirrorMaterial kr: kr in ks (Material.hs:68-72) */
 };
 
 typedef struct bling_material {
@@ -79,7 +80,7 @@ typedef struct bling_material {
   float roughness; /* plastic/metal: Blinn exponent is 1/roughness */
   float ior;       /* glass */
   float kd[BLING_BANDS];  /* matte/plastic diffuse */
-  float ks[BLING_BANDS];  /* plastic specular, glass reflection */
+  float ks[BLING_BANDS];  /* plastic specular, glass and mirror reflection */
   float kt[BLING_BANDS];  /* glass transmission */
   float eta[BLING_BANDS]; /* metal */
   float k[BLING_BANDS];   /* metal */

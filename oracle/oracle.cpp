@@ -1306,6 +1306,14 @@ static Bsdf materialBsdf(const Material& m, const DG& dgg, const DG& dgs) {
       add(x);
       break;
     }
+    case BLING_MAT_MIRROR: {  // mirrorMaterial: specRefl frNoOp (sClamp 0 1 kr)
+      x.kind = BX_SPEC_REFL;
+      x.type = T_REFL | T_SPEC;
+      x.r = sClamp(0, 1, m.ks);
+      x.fr.kind = FR_NOOP;
+      add(x);
+      break;
+    }
     default: {  // glass
       x.kind = BX_SPEC_REFL;
       x.type = T_REFL | T_SPEC;

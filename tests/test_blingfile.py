@@ -156,7 +156,8 @@ def test_other_renderers_parse_and_are_named():
 
 
 @pytest.mark.parametrize("src,what", [
-    ("material { mirror kr { constant rgbR 1 1 1 } }", "mirror"),
+    ("material { shinyMetal kr { constant rgbR 1 1 1 } ks { constant rgbR 1 1 1 } "
+     "rough { constant 0.1 } }", "shinyMetal"),
     ("material { matte kd { checker 1 1 1 tex1 { constant rgbR 1 1 1 } "
      "tex2 { constant rgbR 0 0 0 } } sigma { constant 0 } }", "checker"),
     ("prim { julia c 0 0 0 0 epsilon 0.1 iterations 4 }", "julia"),

@@ -216,6 +216,21 @@ def test_parsed_bling_scene_vs_oracle(gpu_ctx):
     assert st_g["nonfinite_drops"] == 0
 
 
+def test_mirror_material_vs_oracle(gpu_ctx):
+    """mirrorMaterial (specRefl frNoOp kr, Material.hs:68-72): a mirror sphere
+    and a mirror quad over a matte floor under a sky and a sun"""
+    sc = _materials_scene()
+    mirror = sc.add_material(abi.MAT_MIRROR, ks=rgb_to_spectrum((0.9, 0.8, 0.7)))
+    sc.shapes[1].material = mirror  # the metal sphere becomes a mirror
+    q = sc.add_shape(abi.SHAPE_QUAD, (0.6, 0.4), xf.rotate_y(20) @ xf.translate(0.0, 0.5, 1.2),
+                     mirror)
+    sc.prim_order = sc.prim_order + [~q]
+    p = S.render_params(64, 64, (3, 3), max_depth=6, sample_depth=2, rr_depth=2, seed=7)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p)
+    _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
+    assert st_g["nonfinite_drops"] == 0
+
+
 def test_film_resolve_and_png(gpu_ctx, tmp_path):
     """bling_film_resolve (getPixel + xyzToRgb on the read film) equals the
     host restatement, and the 8-bit image round-trips through a PNG"""
