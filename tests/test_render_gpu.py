@@ -231,6 +231,38 @@ def test_mirror_material_vs_oracle(gpu_ctx):
     assert st_g["nonfinite_drops"] == 0
 
 
+def test_lights_and_thin_lens_vs_oracle(gpu_ctx):
+    """a point light, disk, cylinder and box area lights (shape sampling of
+    each kind, Shape.hs:333-409), and a thin-lens camera (lens samples,
+    concentricSampleDisk, Camera.hs:146-164)"""
+    s = S.Scene()
+    grey = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.6, 0.6, 0.6)))
+    plastic = s.add_material(abi.MAT_PLASTIC, kd=rgb_to_spectrum((0.3, 0.5, 0.2)),
+                             ks=constant(0.3), roughness=0.2)
+    v = np.array([[-4, 0, -4], [4, 0, -4], [4, 0, 4], [-4, 0, 4]], np.float32)
+    s.add_mesh(v, [0, 1, 2, 0, 2, 3], grey)
+    order = [0]
+    order.append(~s.add_shape(abi.SHAPE_SPHERE, (0.5,), xf.translate(0.6, 0.5, 0.4), plastic))
+    em = rgb_to_spectrum((4, 3.5, 3), illuminant=True)
+    order.append(~s.add_shape(abi.SHAPE_DISK, (0.0, 0.4, 0.1, 2 * np.pi),
+                              xf.rotate_x(90) @ xf.translate(-1.0, 2.0, 0.0), grey, emission=em))
+    order.append(~s.add_shape(abi.SHAPE_CYLINDER, (0.08, -0.5, 0.5, 2 * np.pi),
+                              xf.rotate_x(90) @ xf.translate(1.5, 0.6, -0.5), grey, emission=em))
+    order.append(~s.add_shape(abi.SHAPE_BOX, (-0.1, -0.1, -0.1, 0.1, 0.1, 0.1),
+                              xf.translate(-0.6, 0.15, -0.6), grey, emission=em))
+    s.prim_order = order
+    s.lights = [S.Light(abi.LIGHT_POINT, rgb_to_spectrum((2, 2, 2), illuminant=True),
+                        vec=(0.0, 2.5, -1.0))]
+    look = xf.look_at((0, 1.6, -4), (0, 0.4, 0), (0, 1, 0))
+    c2w, r2c = xf.perspective_camera(look, 0.08, 4.0, 45.0, 64, 48)
+    s.set_camera(c2w, r2c, lens_radius=0.08, focal_distance=4.0)
+    p = S.render_params(64, 48, (3, 3), max_depth=5, sample_depth=3, rr_depth=3, seed=11)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, s, p)
+    _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
+    assert st_g["nonfinite_drops"] == 0
+    assert fg[..., 2].sum() > 0
+
+
 def test_film_resolve_and_png(gpu_ctx, tmp_path):
     """bling_film_resolve (getPixel + xyzToRgb on the read film) equals the
     host restatement, and the 8-bit image round-trips through a PNG"""
