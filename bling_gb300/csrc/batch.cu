@@ -350,37 +350,54 @@ __global__ void __launch_bounds__(128) k_btrace_mis(BatchCtl* ctl,
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ctl->c + C_CLOSEST, (unsigned long long)n);
 }
 
-// shading class of every path of the current buffer (after its closest hit)
+// Shading order of the current buffer: paths sorted by (job, shading class).
+// Shading reads each path's job parameters and scene tables through the job
+// and scene tables; grouping a job's paths keeps those loads uniform across a
+// warp, and the class keeps its lanes on one BSDF's code.  The key is
+// (job table index mod 4096) x 16 + class in the kBins counters: one
+// counting pass, the scan of k_bin_scan, and a scatter of positions.  Order
+// within a key is arbitrary; it only changes which warp shades a path.
+__device__ __forceinline__ uint32_t shadeKey(int job, int cls) {
+  return ((uint32_t)(job & 4095) << 4) | (uint32_t)cls;
+}
+
 __global__ void __launch_bounds__(128) k_bclass_count(BatchCtl* ctl,
                                                       const BatchSceneDev* __restrict__ scenes,
                                                       Slots tmp, PathStates ps, BatchQueues Q) {
+  static_assert(kShadeClasses <= 16 && (4096u << 4) <= (unsigned)kBins, "shade keys fit the bins");
   const int cur = ctl->cur;
   const PathState& S = ps.b[cur];
   int64_t n = (int64_t)ctl->c[C_LIVE0 + cur];
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;
+  const int lane = threadIdx.x & 31;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
-    int c = -1;
+    uint32_t key = 0xffffffffu;
     if (q < n) {
       const BatchSceneDev& SC = scenes[S.scene[q]];
-      c = shadeClass(SC.A, SC.S, hitPrim(tmp.hit, q));
-      Q.cls[q] = c;
+      key = shadeKey(S.job[q], shadeClass(SC.A, SC.S, hitPrim(tmp.hit, q)));
+      Q.keys[q] = key;
     }
-    classCount(c, ctl->cls);
+    // one atomic per distinct key in the warp
+    unsigned grp = __match_any_sync(0xffffffffu, key);
+    if (key != 0xffffffffu && lane == __ffs(grp) - 1) atomicAdd(Q.bins + key, (unsigned)__popc(grp));
   }
 }
 
-// the positions of the current buffer in shading-class order
+// the positions of the current buffer in (job, class) order
 __global__ void __launch_bounds__(128) k_bclass_scatter(BatchCtl* ctl, BatchQueues Q) {
-  __shared__ unsigned off[kShadeClasses];
-  classOffsets(ctl->cls, off);
   int64_t n = (int64_t)ctl->c[C_LIVE0 + ctl->cur];
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;
+  const int lane = threadIdx.x & 31;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
-    int c = q < n ? Q.cls[q] : -1;
-    int p = classSlot(c, off, ctl->cls + 16);
-    if (c >= 0) Q.order[p] = (int32_t)q;
+    uint32_t key = q < n ? Q.keys[q] : 0xffffffffu;
+    unsigned grp = __match_any_sync(0xffffffffu, key);
+    int leader = __ffs(grp) - 1;
+    unsigned base = 0;
+    if (key != 0xffffffffu && lane == leader) base = atomicAdd(Q.bins + key, (unsigned)__popc(grp));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (key != 0xffffffffu) Q.order[base + __popc(grp & ((1u << lane) - 1))] = (int32_t)q;
   }
 }
 
@@ -571,7 +588,9 @@ cudaError_t enqueueIterationT(BatchEngine* b, int use_cond, unsigned long long m
     k_bin_flip<<<1, 32, 0, s>>>(b->d_ctl);
   }
   k_btrace<WIDE><<<b->g_trace, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps);
+  cudaMemsetAsync(b->q.bins, 0, sizeof(unsigned int) * kBins, s);
   k_bclass_count<<<b->g_bin, 128, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
+  k_bin_scan<<<1, 1024, 0, s>>>(b->q.bins);
   k_bclass_scatter<<<b->g_bin, 128, 0, s>>>(b->d_ctl, b->q);
   k_bshade<<<b->g_shade, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps, b->q,
                                      b->d_job_done);
