@@ -681,6 +681,53 @@ def profile_traffic():
     return None
 
 
+def run_batch_profile(args):
+    """Plain per-job passes against one batch over the same jobs, for
+    profiling: `--batch-profile N` instances of the batched workload (seed 5),
+    the batch with 4M slots and one CUDA graph per iteration (no autotuning).
+    `--batch-profile-mode` picks "plain", "batched" or "both"."""
+    import torch
+
+    from bling_gb300 import build as gb
+    gb.build()
+    from bling_gb300 import scene as S
+    from bling_gb300.api import Batch, Context
+    from bling_gb300.autotune import extent_samples
+    inst = S.batch_instances(n=args.batch_profile, seed=5)
+    ctx = Context(device=0)
+    gs = [ctx.scene(i.scene) for i in inst]
+    params = [i.params for i in inst]
+    films = [ctx.film(p.width, p.height) for p in params]
+    samples = sum(extent_samples(p) for p in params)
+    out = {"workload": f"batched workload, {len(inst)} instances (seed 5)", "path_samples": samples,
+           "triangles": sum(i.n_tris for i in inst)}
+    if args.batch_profile_mode in ("plain", "both"):
+        gs[0].render_pass(films[0], params[0], 0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for g, p, f in zip(gs, params, films):
+            g.render_pass(f, p, 1)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out["plain"] = {"s": round(dt, 3), "path_samples_per_s": round(samples / dt, 1)}
+    if args.batch_profile_mode in ("batched", "both"):
+        b = Batch(ctx, slots=1 << 22, graph_mode=1)
+        b.submit(gs[0], films[0], params[0], 0)
+        b.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for g, p, f in zip(gs, params, films):
+            b.submit(g, f, p, 1)
+        b.run()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out["batched"] = {"s": round(dt, 3), "path_samples_per_s": round(samples / dt, 1),
+                          "iterations": b.stats()["iterations"]}
+        b.close()
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
 def main():
     global N_RAYS, N_ANY
     ap = argparse.ArgumentParser()
@@ -703,6 +750,10 @@ def main():
                     help="wavefront iterations between admission rounds")
     ap.add_argument("--render-size", type=int, nargs=3, metavar=("W", "H", "STRATA"),
                     help="only render the large-mesh workload at W x H, STRATA^2 spp (profiling)")
+    ap.add_argument("--batch-profile", type=int, default=0, metavar="N",
+                    help="only time plain passes against one batch over N batched-workload "
+                         "instances (profiling)")
+    ap.add_argument("--batch-profile-mode", default="both", choices=["plain", "batched", "both"])
     ap.add_argument("--rays", type=int, default=N_RAYS,
                     help="closest-hit rays per step (any-hit: half); smaller for profiling")
     args = ap.parse_args()
@@ -711,6 +762,8 @@ def main():
         args.warmup = 3
     if args.render_size:
         run_render_profile(args)
+    elif args.batch_profile:
+        run_batch_profile(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

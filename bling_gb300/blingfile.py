@@ -16,7 +16,8 @@ The subset is what the GPU path renders:
   ``newTransform``, ``camera``, ``light``, ``material``, ``emission``,
   ``prim``;
 * primitives: ``mesh`` and ``shape`` (box, cylinder, disk, quad, sphere);
-* materials: matte, plastic, metal, glass, mirror, with ``constant`` textures;
+* materials: matte, plastic, metal, glass, mirror, shinyMetal, transMatte,
+  with ``constant`` textures;
 * lights: directional, point, and infinite with a ``constant`` map;
 * spectra: ``rgbR``/``rgbI`` (decimal or ``%rrggbb``), ``spd { l v, ... }``,
   ``temp``;
@@ -534,9 +535,19 @@ class _Parser:
         if kind == "mirror":
             kr = self._spectrum_texture("kr")
             return sc.add_material(abi.MAT_MIRROR, ks=kr)
-        if kind in ("blackbody", "bumpMap", "shinyMetal", "substrate", "transMatte"):
+        if kind == "shinyMetal":
+            kr = self._spectrum_texture("kr")
+            ks = self._spectrum_texture("ks")
+            rough = self._scalar_texture("rough")
+            return sc.add_material(abi.MAT_SHINY_METAL, kd=kr, ks=ks, roughness=float(rough))
+        if kind == "transMatte":
+            kr = self._spectrum_texture("kr")
+            kt = self._spectrum_texture("kt")
+            ks = self._scalar_texture("ks")
+            return sc.add_material(abi.MAT_TRANS_MATTE, kd=kr, kt=kt, sigma=float(ks))
+        if kind in ("blackbody", "bumpMap", "substrate"):
             raise Unsupported(f"material {kind}: the GPU path renders matte, plastic, metal, "
-                              "glass and mirror")
+                              "glass, mirror, shinyMetal and transMatte")
         raise t.error(f"unknown material type {kind}")
 
     def p_emission(self):

@@ -1,5 +1,7 @@
 // Wavefront path integrator: host-side interface (integrator.cu).
 #pragma once
+#include <cmath>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -13,6 +15,41 @@ struct DMaterial {
   float sigma, rough, ior;
   float kd[16], ks[16], kt[16], eta[16], k[16];
 };
+
+// Spectra a material derives from its constant parameters, once at upload
+// (the reference derives them per hit from constant textures: same values).
+//  * shiny metal (Material.hs:98-109): eta/k <- frApproxEta/frApproxK of ks
+//    for the microfacet lobe, kd/kt <- frApproxEta/frApproxK of kr (given in
+//    kd) for the specular lobe (Fresnel.hs:72-78);
+//  * translucent matte (Material.hs:43-53): kd <- r = sClamp 0 1 kr,
+//    kt <- t = sClamp 0 1 kt * (white - r).
+// Haskell's clamp, min and max order (max lo (min hi x)) is kept.
+inline float ghcClamp(float x, float lo, float hi) {
+  float m = hi <= x ? hi : x;  // min hi x
+  return lo <= m ? m : lo;     // max lo m
+}
+inline void deriveMaterialSpectra(DMaterial& m) {
+  if (m.kind == BLING_MAT_SHINY_METAL) {
+    float kr[16];
+    memcpy(kr, m.kd, sizeof kr);
+    for (int i = 0; i < 16; i++) {
+      float rs = sqrtf(ghcClamp(m.ks[i], 0.0f, 0.999f));
+      float refl = ghcClamp(m.ks[i], 0.0f, 0.999f);
+      m.eta[i] = (1.0f + rs) / (1.0f - rs);
+      m.k[i] = sqrtf(refl / (1.0f - refl)) * 2.0f;
+      float rr = sqrtf(ghcClamp(kr[i], 0.0f, 0.999f));
+      float reflr = ghcClamp(kr[i], 0.0f, 0.999f);
+      m.kd[i] = (1.0f + rr) / (1.0f - rr);
+      m.kt[i] = sqrtf(reflr / (1.0f - reflr)) * 2.0f;
+    }
+  } else if (m.kind == BLING_MAT_TRANS_MATTE) {
+    for (int i = 0; i < 16; i++) {
+      float r = ghcClamp(m.kd[i], 0.0f, 1.0f);
+      m.kt[i] = ghcClamp(m.kt[i], 0.0f, 1.0f) * (1.0f - r);
+      m.kd[i] = r;
+    }
+  }
+}
 
 struct DMesh {
   const float* verts;   // 3 per vertex (world space)

@@ -318,7 +318,9 @@ struct BxDF {
   const float* eta;
   const float* k;
   bool clampR;     // glass: sClamp' of the colour
+  bool btdf;       // brdfToBtdf (Reflection.hs:188-195): wi in the other hemisphere
 };
+__device__ __forceinline__ V3 otherHemisphere(V3 w) { return V3{w.x, w.y, -w.z}; }
 __device__ __forceinline__ Spec bxR(const BxDF& b) {
   if (!b.r) return sConst(1.0f);
   Spec s = sLoad(b.r);
@@ -403,6 +405,7 @@ __device__ __forceinline__ float orenNayarScale(const BxDF& b, V3 wo, V3 wi) {
 #define BLING_OUTLINE
 
 static __device__ BLING_OUTLINE Spec bxEval(const BxDF& b, V3 wo, V3 wi) {
+  if (b.btdf) wi = otherHemisphere(wi);
   switch (b.kind) {
     case BX_LAMBERT: return sScale(bxR(b), kInvPi * absCosTheta(wo));
     case BX_OREN: return sScale(sScale(bxR(b), orenNayarScale(b, wo, wi)), kInvPi * absCosTheta(wo));
@@ -420,7 +423,8 @@ static __device__ BLING_OUTLINE Spec bxEval(const BxDF& b, V3 wo, V3 wi) {
     default: return sConst(0);
   }
 }
-static __device__ BLING_OUTLINE float bxPdf(const BxDF& b, V3 wo, V3 wi) {
+// the BRDF's pdf (a BTDF's sample calls its BRDF's sample, Reflection.hs:192-193)
+static __device__ BLING_OUTLINE float bxPdfBrdf(const BxDF& b, V3 wo, V3 wi) {
   switch (b.kind) {
     case BX_LAMBERT:
     case BX_OREN: return sameHemisphere(wo, wi) ? kInvPi * absCosTheta(wi) : 0.0f;
@@ -434,14 +438,22 @@ static __device__ BLING_OUTLINE float bxPdf(const BxDF& b, V3 wo, V3 wi) {
     default: return 0;
   }
 }
+static __device__ BLING_OUTLINE float bxPdf(const BxDF& b, V3 wo, V3 wi) {
+  return bxPdfBrdf(b, wo, b.btdf ? otherHemisphere(wi) : wi);
+}
+static __device__ BLING_OUTLINE void bxSampleBrdf(const BxDF& b, V3 wo, float u1, float u2, Spec& f, V3& wi, float& pdf);
 static __device__ BLING_OUTLINE void bxSample(const BxDF& b, V3 wo, float u1, float u2, Spec& f, V3& wi, float& pdf) {
+  bxSampleBrdf(b, wo, u1, u2, f, wi, pdf);
+  if (b.btdf) wi = otherHemisphere(wi);
+}
+static __device__ BLING_OUTLINE void bxSampleBrdf(const BxDF& b, V3 wo, float u1, float u2, Spec& f, V3& wi, float& pdf) {
   switch (b.kind) {
     case BX_LAMBERT:
     case BX_OREN: {
       wi = toSameHemisphere(wo, cosineSampleHemisphere(u1, u2));
       if (sameHemisphere(wo, wi)) {
         f = b.kind == BX_LAMBERT ? bxR(b) : sScale(bxR(b), orenNayarScale(b, wo, wi));
-        pdf = bxPdf(b, wo, wi);
+        pdf = bxPdfBrdf(b, wo, wi);
       } else {
         f = sConst(0);
         pdf = 0;
@@ -524,6 +536,7 @@ static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ 
   x.fr = FR_NOOP;
   x.eta = x.k = nullptr;
   x.clampR = false;
+  x.btdf = false;
   int kind = m.kind;
   float sigma = m.sigma, rough = m.rough, ior = m.ior;
   if (kind == BLING_MAT_MATTE) {
@@ -562,6 +575,45 @@ static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ 
     x.eta = m.eta;
     x.k = m.k;
     b.c[b.n++] = x;
+  } else if (kind == BLING_MAT_SHINY_METAL) {
+    // mkShinyMetal (Material.hs:98-109): a Blinn microfacet lobe and a
+    // specular one, both white, with conductor Fresnel terms approximated
+    // from ks and kr (derived at upload into eta/k and kd/kt)
+    x.kind = BX_MICRO;
+    x.type = T_REFL | T_GLOSSY;
+    x.e = fixExponent(1.0f / rough);
+    x.fr = FR_COND;
+    x.eta = m.eta;
+    x.k = m.k;
+    b.c[b.n++] = x;
+    BxDF y = x;
+    y.kind = BX_SPEC_REFL;
+    y.type = T_REFL | T_SPEC;
+    y.e = 0;
+    y.eta = m.kd;
+    y.k = m.kt;
+    b.c[b.n++] = y;
+  } else if (kind == BLING_MAT_TRANS_MATTE) {
+    // translucentMatte (Material.hs:43-53): Lambertian or Oren-Nayar
+    // reflection of r and the same lobe of t turned into a BTDF (r and t
+    // derived at upload into kd and kt)
+    x.type = T_REFL | T_DIFF;
+    x.r = m.kd;
+    if (sigma == 0) {
+      x.kind = BX_LAMBERT;
+    } else {
+      x.kind = BX_OREN;
+      float s = hclamp(sigma, 0, 1);
+      float sig2 = s * s;
+      x.A = 1.0f - (sig2 / (2.0f * (sig2 + 0.33f)));
+      x.B = 0.45f * sig2 / (sig2 + 0.09f);
+    }
+    b.c[b.n++] = x;
+    BxDF y = x;
+    y.type = T_TRANS | T_DIFF;
+    y.r = m.kt;
+    y.btdf = true;
+    b.c[b.n++] = y;
   } else if (kind == BLING_MAT_MIRROR) {
     // mirrorMaterial: specRefl frNoOp (sClamp 0 1 kr) (Material.hs:68-72)
     x.kind = BX_SPEC_REFL;

@@ -78,6 +78,7 @@ int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
     memcpy(o.kt, m.kt, 64);
     memcpy(o.eta, m.eta, 64);
     memcpy(o.k, m.k, 64);
+    deriveMaterialSpectra(o);
   }
   void* dm;
   if ((rc = up(mats.data(), mats.size() * sizeof(DMaterial), &dm))) return rc;

@@ -204,7 +204,7 @@ __device__ __forceinline__ void queueAppend(bool live, int slot, int32_t* __rest
 // then run one BSDF's and one geometry's code instead of all of them in turn.
 // The order within a class is the queue's order, up to the interleaving of
 // warps.
-constexpr int kMaterialKinds = 5;  // BLING_MAT_MATTE .. BLING_MAT_MIRROR
+constexpr int kMaterialKinds = 7;  // BLING_MAT_MATTE .. BLING_MAT_TRANS_MATTE
 constexpr int kShadeClasses = 1 + 2 * kMaterialKinds;
 static_assert(kShadeClasses <= 16, "class counts and cursors hold 16 entries each");
 

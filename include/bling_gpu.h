@@ -71,7 +71,9 @@ enum {
   BLING_MAT_PLASTIC = 1, /* mkPlastic kd ks roughness   (Material.hs:272-282) */
   BLING_MAT_METAL = 2,   /* mkMetal eta k roughness     (Material.hs:285-292) */
   BLING_MAT_GLASS = 3,   /* glassMaterial ior kr kt     (Material.hs:252-262) */
-  BLING_MAT_MIRROR = 4   /* mirrorMaterial kr: kr in ks (Material.hs:68-72) */
+  BLING_MAT_MIRROR = 4,  /* mirrorMaterial kr: kr in ks (Material.hs:68-72) */
+  BLING_MAT_SHINY_METAL = 5, /* mkShinyMetal kr ks rough: kr in kd (Material.hs:98-109) */
+  BLING_MAT_TRANS_MATTE = 6  /* translucentMatte kr kt ks: kr in kd, ks in sigma (Material.hs:43-53) */
 };
 
 typedef struct bling_material {

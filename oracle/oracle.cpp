@@ -550,7 +550,9 @@ struct BxDF {
   float ei, et;     // specular transmission
   float e;          // Blinn exponent
   Fresnel fr;
+  bool btdf;        // brdfToBtdf (Reflection.hs:188-195)
 };
+static inline V otherHemisphere(V w) { return V{w.x, w.y, -w.z}; }
 
 struct Material {
   int kind;
@@ -1135,8 +1137,9 @@ static Spec orenNayar(const BxDF& b, V wo, V wi) {
   return sScale(b.r, b.A + b.B * maxcos * sina * tanb);
 }
 
-// bxdfEval b wo wi
+// bxdfEval b wo wi; a BTDF evaluates its BRDF at the mirrored wi
 static Spec bxEval(const BxDF& b, V wo, V wi) {
+  if (b.btdf) wi = otherHemisphere(wi);
   switch (b.kind) {
     case BX_LAMBERT: return sScale(b.r, INV_PI * absCosTheta(wo));  // Diffuse.hs:26
     case BX_OREN: return sScale(orenNayar(b, wo, wi), INV_PI * absCosTheta(wo));
@@ -1154,8 +1157,8 @@ static Spec bxEval(const BxDF& b, V wo, V wi) {
     default: return BLACK;  // specular: e _ _ = black
   }
 }
-// bxdfPdf b wo wi
-static float bxPdf(const BxDF& b, V wo, V wi) {
+// bxdfPdf of the BRDF itself
+static float bxPdfBrdf(const BxDF& b, V wo, V wi) {
   switch (b.kind) {
     case BX_LAMBERT:
     case BX_OREN: return sameHemisphere(wo, wi) ? INV_PI * absCosTheta(wi) : 0.0f;  // cosPdf
@@ -1169,14 +1172,23 @@ static float bxPdf(const BxDF& b, V wo, V wi) {
     default: return 0;
   }
 }
-// bxdfSample b False wo u -> (f, wi, pdf)
+// bxdfPdf b wo wi
+static float bxPdf(const BxDF& b, V wo, V wi) {
+  return bxPdfBrdf(b, wo, b.btdf ? otherHemisphere(wi) : wi);
+}
+static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf);
+// bxdfSample b False wo u -> (f, wi, pdf); a BTDF mirrors its BRDF's sample
 static void bxSample(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf) {
+  bxSampleBrdf(b, wo, u1, u2, f, wi, pdf);
+  if (b.btdf) wi = otherHemisphere(wi);
+}
+static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf) {
   switch (b.kind) {
     case BX_LAMBERT: {  // cosSample (Diffuse.hs:14-22)
       wi = toSameHemisphere(wo, cosineSampleHemisphere(u1, u2));
       if (sameHemisphere(wo, wi)) {
         f = b.r;
-        pdf = bxPdf(b, wo, wi);
+        pdf = bxPdfBrdf(b, wo, wi);
       } else {
         f = BLACK;
         wi = wo;
@@ -1188,7 +1200,7 @@ static void bxSample(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, fl
       wi = toSameHemisphere(wo, cosineSampleHemisphere(u1, u2));
       if (sameHemisphere(wo, wi)) {
         f = orenNayar(b, wo, wi);
-        pdf = bxPdf(b, wo, wi);
+        pdf = bxPdfBrdf(b, wo, wi);
       } else {
         f = BLACK;
         pdf = 0;
@@ -1253,6 +1265,21 @@ struct Bsdf {  // Reflection.hs:201-218
 };
 
 // mkBsdf' with the material's BxDFs (Material.hs:228-292)
+// frApproxEta / frApproxK (Fresnel.hs:72-78), on sClamp 0 0.999 of the colour
+static Spec frApproxEta(const Spec& r) {
+  Spec c = sClamp(0.0f, 0.999f, r), o;
+  for (int i = 0; i < 16; i++) {
+    float rs = std::sqrt(c.v[i]);
+    o.v[i] = (1.0f + rs) / (1.0f - rs);
+  }
+  return o;
+}
+static Spec frApproxK(const Spec& r) {
+  Spec c = sClamp(0.0f, 0.999f, r), o;
+  for (int i = 0; i < 16; i++) o.v[i] = std::sqrt(c.v[i] / (1.0f - c.v[i])) * 2.0f;
+  return o;
+}
+
 static Bsdf materialBsdf(const Material& m, const DG& dgg, const DG& dgs) {
   Bsdf b;
   b.n = 0;
@@ -1304,6 +1331,47 @@ static Bsdf materialBsdf(const Material& m, const DG& dgg, const DG& dgs) {
       x.fr.eta = m.eta;
       x.fr.k = m.k;
       add(x);
+      break;
+    }
+    case BLING_MAT_SHINY_METAL: {  // mkShinyMetal kr ks rough (Material.hs:98-109)
+      x.kind = BX_MICRO;
+      x.type = T_REFL | T_GLOSSY;
+      x.r = WHITE;
+      x.e = fixExponent(1.0f / m.rough);
+      x.fr.kind = FR_COND;
+      x.fr.eta = frApproxEta(m.ks);
+      x.fr.k = frApproxK(m.ks);
+      add(x);
+      BxDF y{};
+      y.kind = BX_SPEC_REFL;
+      y.type = T_REFL | T_SPEC;
+      y.r = WHITE;
+      y.fr.kind = FR_COND;
+      y.fr.eta = frApproxEta(m.kd);  // kr
+      y.fr.k = frApproxK(m.kd);
+      add(y);
+      break;
+    }
+    case BLING_MAT_TRANS_MATTE: {  // translucentMatte kr kt ks (Material.hs:43-53)
+      Spec r = sClamp(0, 1, m.kd);
+      Spec t = sClamp(0, 1, m.kt) * (WHITE - r);
+      x.type = T_REFL | T_DIFF;
+      x.r = r;
+      if (m.sigma == 0) {
+        x.kind = BX_LAMBERT;
+      } else {
+        x.kind = BX_OREN;
+        float sg = clampf(m.sigma, 0, 1);
+        float sig2 = sg * sg;
+        x.A = 1.0f - (sig2 / (2.0f * (sig2 + 0.33f)));
+        x.B = 0.45f * sig2 / (sig2 + 0.09f);
+      }
+      add(x);
+      BxDF y = x;
+      y.type = T_TRANS | T_DIFF;
+      y.r = t;
+      y.btdf = true;
+      add(y);
       break;
     }
     case BLING_MAT_MIRROR: {  // mirrorMaterial: specRefl frNoOp (sClamp 0 1 kr)

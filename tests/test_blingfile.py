@@ -141,6 +141,18 @@ def test_materials(job):
     assert glass.ior == 1.5 and np.array_equal(np.asarray(glass.kt, F), rgb_to_spectrum((1, 1, 1)))
 
 
+def test_shiny_metal_and_translucent_matte():
+    j = B.parse("material { shinyMetal kr { constant rgbR 0.9 0.8 0.5 } ks { constant rgbR 0.3 0.3 0.3 } "
+                "rough { constant 0.2 } } prim { shape { sphere radius 1 } } "
+                "material { transMatte kr { constant rgbR 0.4 0.4 0.4 } kt { constant rgbR 0.5 0.5 0.5 } "
+                "ks { constant 0.3 } } prim { shape { sphere radius 1 } }")
+    shiny, trans = j.scene.materials
+    assert shiny.kind == abi.MAT_SHINY_METAL and shiny.roughness == float(F(0.2))
+    assert np.array_equal(np.asarray(shiny.kd, F), rgb_to_spectrum((F(0.9), F(0.8), F(0.5))))
+    assert trans.kind == abi.MAT_TRANS_MATTE and trans.sigma == float(F(0.3))
+    assert np.array_equal(np.asarray(trans.kt, F), rgb_to_spectrum((F(0.5), F(0.5), F(0.5))))
+
+
 def test_constant_spd_gives_a_flat_spectrum():
     s = B.spectrum_from_spd([(380.0, 0.25), (500.0, 0.25), (720.0, 0.25)])
     assert np.array_equal(s, constant(0.25))
@@ -156,8 +168,9 @@ def test_other_renderers_parse_and_are_named():
 
 
 @pytest.mark.parametrize("src,what", [
-    ("material { shinyMetal kr { constant rgbR 1 1 1 } ks { constant rgbR 1 1 1 } "
-     "rough { constant 0.1 } }", "shinyMetal"),
+    ("material { substrate kd { constant rgbR 1 1 1 } ks { constant rgbR 1 1 1 } "
+     "ka { constant rgbR 0 0 0 } urough { constant 0.1 } vrough { constant 0.1 } "
+     "depth { constant 0 } }", "substrate"),
     ("material { matte kd { checker 1 1 1 tex1 { constant rgbR 1 1 1 } "
      "tex2 { constant rgbR 0 0 0 } } sigma { constant 0 } }", "checker"),
     ("prim { julia c 0 0 0 0 epsilon 0.1 iterations 4 }", "julia"),

@@ -231,6 +231,28 @@ def test_mirror_material_vs_oracle(gpu_ctx):
     assert st_g["nonfinite_drops"] == 0
 
 
+def test_shiny_metal_and_translucent_matte_vs_oracle(gpu_ctx):
+    """mkShinyMetal (conductor Fresnel approximated from the colours) and
+    translucentMatte (a diffuse BRDF and the same lobe as a BTDF, light seen
+    through a thin translucent quad)"""
+    sc = _materials_scene()
+    shiny = sc.add_material(abi.MAT_SHINY_METAL, kd=rgb_to_spectrum((0.95, 0.8, 0.4)),
+                            ks=rgb_to_spectrum((0.5, 0.45, 0.3)), roughness=0.1)
+    trans = sc.add_material(abi.MAT_TRANS_MATTE, kd=rgb_to_spectrum((0.3, 0.4, 0.3)),
+                            kt=rgb_to_spectrum((0.7, 0.6, 0.5)), sigma=0.2)
+    trans_l = sc.add_material(abi.MAT_TRANS_MATTE, kd=rgb_to_spectrum((0.5, 0.5, 0.5)),
+                              kt=rgb_to_spectrum((0.9, 0.9, 0.9)))
+    sc.shapes[1].material = shiny   # the metal sphere
+    sc.shapes[0].material = trans   # the plastic sphere
+    q = sc.add_shape(abi.SHAPE_QUAD, (0.8, 0.8), xf.rotate_x(-90) @ xf.translate(0.0, 1.6, -1.0),
+                     trans_l)  # a translucent ceiling panel under the sphere light
+    sc.prim_order = sc.prim_order + [~q]
+    p = S.render_params(64, 64, (3, 3), max_depth=6, sample_depth=2, rr_depth=2, seed=13)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p)
+    _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
+    assert st_g["nonfinite_drops"] == 0
+
+
 def test_lights_and_thin_lens_vs_oracle(gpu_ctx):
     """a point light, disk, cylinder and box area lights (shape sampling of
     each kind, Shape.hs:333-409), and a thin-lens camera (lens samples,
