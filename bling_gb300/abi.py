@@ -28,7 +28,7 @@ SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_DISK, SHAPE_CYLINDER = 0, 1, 2, 3, 4
 LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE = 0, 1, 2
 FILTER_BOX, FILTER_GAUSS, FILTER_MITCHELL, FILTER_SINC, FILTER_TRIANGLE = 0, 1, 2, 3, 4
 SAMPLER_STRATIFIED, SAMPLER_RANDOM = 0, 1
-ABI_VERSION = 2  # BLING_ABI_VERSION of include/bling_gpu.h
+ABI_VERSION = 3  # BLING_ABI_VERSION of include/bling_gpu.h
 
 
 class Opts(C.Structure):
@@ -62,7 +62,8 @@ class LightDesc(C.Structure):
 
 class CameraDesc(C.Structure):
     _fields_ = [("c2w", M16), ("c2w_inv", M16), ("r2c", M16), ("r2c_inv", M16),
-                ("lens_radius", C.c_float), ("focal_distance", C.c_float)]
+                ("lens_radius", C.c_float), ("focal_distance", C.c_float),
+                ("w2r", M16), ("pixel_area", C.c_float), ("reserved", C.c_float)]
 
 
 class SceneDesc(C.Structure):

@@ -315,9 +315,7 @@ class _Parser:
         sc.prim_order = [v if k == "mesh" else ~v for k, v in self.s.blocks]
         sc.lights = list(self.s.lights)
         c2w, lr, fd, fov, sx, sy = self.s.camera
-        cc2w, r2c = xf.perspective_camera(c2w, lr, fd, fov, sx, sy)
-        sc.set_camera(cc2w, r2c, float(lr), float(fd))
-        sc.view = (c2w, fov)
+        sc.set_perspective(c2w, float(lr), float(fd), fov, sx, sy)
         (kind, strata), (md, sd) = self.s.sampler, self.s.depths
         fk, fp = self.s.filter
         return Job(sc, self.s.res[0], self.s.res[1], fk, fp, self.s.renderer, kind, strata, md, sd)

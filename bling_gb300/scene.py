@@ -91,27 +91,24 @@ class Scene:
                                  None if emission is None else np.asarray(emission, np.float32)))
         return len(self.shapes) - 1
 
-    def set_camera(self, c2w: xf.Transform, r2c: xf.Transform, lens_radius=0.0, focal_distance=1.0):
-        c = abi.CameraDesc()
-        c.c2w[:] = c2w.m.tolist()
-        c.c2w_inv[:] = c2w.inv.tolist()
-        c.r2c[:] = r2c.m.tolist()
-        c.r2c_inv[:] = r2c.inv.tolist()
-        c.lens_radius, c.focal_distance = lens_radius, focal_distance
-        self.camera = c
+    def set_camera(self, c2w: xf.Transform, r2c: xf.Transform, lens_radius=0.0, focal_distance=1.0,
+                   w2r: xf.Transform | None = None, pixel_area=0.0):
+        self.camera = camera_desc(c2w, r2c, lens_radius, focal_distance, w2r, pixel_area)
+
+    def set_perspective(self, look: xf.Transform, lens_radius, focal_distance, fov, width, height):
+        """mkPerspectiveCamera look lr fd fov w h, with the world-to-raster
+        transform and pixel area of sampleCam; remembered for camera_for()."""
+        c2w, r2c, w2r, ap = xf.perspective_camera(look, lens_radius, focal_distance, fov, width,
+                                                  height, full=True)
+        self.camera = camera_desc(c2w, r2c, lens_radius, focal_distance, w2r, ap)
+        self.view = (look, fov)
 
     def camera_for(self, width: int, height: int) -> abi.CameraDesc:
         """The scene's pinhole view built for another image size
         (mkPerspectiveCamera takes the image size, Camera.hs:108-147)."""
         look, fov = self.view
-        c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, fov, width, height)
-        c = abi.CameraDesc()
-        c.c2w[:] = c2w.m.tolist()
-        c.c2w_inv[:] = c2w.inv.tolist()
-        c.r2c[:] = r2c.m.tolist()
-        c.r2c_inv[:] = r2c.inv.tolist()
-        c.lens_radius, c.focal_distance = 0.0, 1.0
-        return c
+        c2w, r2c, w2r, ap = xf.perspective_camera(look, 0.0, 1.0, fov, width, height, full=True)
+        return camera_desc(c2w, r2c, 0.0, 1.0, w2r, ap)
 
     @property
     def n_triangles(self) -> int:
@@ -175,6 +172,20 @@ class Scene:
         return sd, keep
 
 
+def camera_desc(c2w: xf.Transform, r2c: xf.Transform, lens_radius=0.0, focal_distance=1.0,
+                w2r: xf.Transform | None = None, pixel_area=0.0) -> abi.CameraDesc:
+    c = abi.CameraDesc()
+    c.c2w[:] = c2w.m.tolist()
+    c.c2w_inv[:] = c2w.inv.tolist()
+    c.r2c[:] = r2c.m.tolist()
+    c.r2c_inv[:] = r2c.inv.tolist()
+    c.lens_radius, c.focal_distance = lens_radius, focal_distance
+    if w2r is not None:
+        c.w2r[:] = w2r.m.tolist()
+        c.pixel_area = float(pixel_area)
+    return c
+
+
 def render_params(width, height, strata=(4, 4), max_depth=5, sample_depth=3, rr_depth=7,
                   filter_kind=abi.FILTER_BOX, filter_params=(0, 0, 0, 0), seed=1,
                   sampler=abi.SAMPLER_STRATIFIED):
@@ -231,9 +242,7 @@ def cornell_room(width=256, height=256, fov=40.0) -> Scene:
                         xf.rotate_y(-18) @ xf.translate(0.67, 0.0, 0.33), white)
     s.prim_order = [m_grey, m_red, m_green, ~q, ~tall, ~short]
     look = xf.look_at((0.5, 0.5, -1.4), (0.5, 0.5, 0.5), (0, 1, 0))
-    c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, fov, width, height)
-    s.set_camera(c2w, r2c)
-    s.view = (look, fov)
+    s.set_perspective(look, 0.0, 1.0, fov, width, height)
     return s
 
 
@@ -461,9 +470,7 @@ def heightfield_scene(ns=2048, n_spheres=4096, seed=3, width=1920, height=1080, 
                         tuple(float(v) for v in sd)),
                 Light(abi.LIGHT_INFINITE, env=env, w2l=xf.rotate_x(90))]
     look = xf.look_at((0.0, 3.0, -8.0), (0.0, 0.0, 0.5), (0, 1, 0))
-    c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, fov, width, height)
-    s.set_camera(c2w, r2c)
-    s.view = (look, fov)
+    s.set_perspective(look, 0.0, 1.0, fov, width, height)
     return s
 
 
@@ -540,9 +547,7 @@ def soup_spheres_scene(n_tris, n_spheres=256, seed=1, width=256, height=256, fov
                 Light(abi.LIGHT_INFINITE, env=sky_env(env_size[0], env_size[1], sun),
                       w2l=xf.rotate_x(90))]
     look = xf.look_at((0.0, 0.6, -3.2), (0.0, 0.0, 0.0), (0, 1, 0))
-    c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, fov, width, height)
-    s.set_camera(c2w, r2c)
-    s.view = (look, fov)
+    s.set_perspective(look, 0.0, 1.0, fov, width, height)
     return s
 
 
@@ -588,9 +593,7 @@ def furnace_scene(rho=0.5, width=32, height=32, le=1.0) -> Scene:
     env = np.full((8, 16, 16), le, np.float32)
     s.lights = [Light(abi.LIGHT_INFINITE, env=env, w2l=xf.identity())]
     look = xf.look_at((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), (0, 1, 0))
-    c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, 40.0, width, height)
-    s.set_camera(c2w, r2c)
-    s.view = (look, 40.0)
+    s.set_perspective(look, 0.0, 1.0, 40.0, width, height)
     return s
 
 

@@ -209,9 +209,11 @@ def perspective(fov, n, f) -> Transform:
     return concat(scale(i_tan, i_tan, 1), Transform(m, invert(m)))
 
 
-def perspective_camera(c2w: Transform, lens_radius, focal_distance, fov, sx, sy):
-    """mkPerspectiveCamera / mkProjective (Camera.hs:204-243): returns the
-    (c2w, r2c) transforms the camera uses to fire rays."""
+def perspective_camera(c2w: Transform, lens_radius, focal_distance, fov, sx, sy, full=False):
+    """mkPerspectiveCamera / mkProjective (Camera.hs:108-147): returns the
+    (c2w, r2c) transforms the camera uses to fire rays; with full=True also
+    the world-to-raster transform and the pixel area that sampleCam uses
+    (w2r = (inverse c2w <> p) <> s2r, ap = pw * ph)."""
     p = perspective(fov, F(1e-2), F(1000))
     sx, sy = F(sx), F(sy)
     aspect = sx / sy
@@ -224,4 +226,10 @@ def perspective_camera(c2w: Transform, lens_radius, focal_distance, fov, sx, sy)
     t = translate(-s0, -s3, 0)
     s2r = concat(t, concat(st2, st1))  # t <> st2 <> st1, (<>) is infixr
     r2c = concat(s2r.inverse(), p.inverse())
-    return c2w, r2c
+    if not full:
+        return c2w, r2c
+    w2r = concat(concat(c2w.inverse(), p), s2r)
+    fl = tanf(radians(fov) / F(2))
+    pw = fl * (s1 - s0) / sx
+    ph = fl * (s3 - s2) / sy
+    return c2w, r2c, w2r, F(pw * ph)

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define BLING_ABI_VERSION 2
+#define BLING_ABI_VERSION 3
 
 #define BLING_OK 0
 #define BLING_ERR_INVALID_ARG (-1)
@@ -139,12 +139,18 @@ typedef struct bling_light_desc {
   float l2w[16];               /* infinite: light-to-world */
 } bling_light_desc;
 
-/* A projective camera (Camera.hs:120-127, mkProjective Camera.hs:204-229). */
+/* A projective camera (ProjectiveCamera, Camera.hs:23-31; mkProjective,
+ * Camera.hs:108-135).  w2r and pixel_area are what sampleCam uses
+ * (Camera.hs:95-100): the light tracer needs them, path tracing does not
+ * (zero them when no light tracing is done). */
 typedef struct bling_camera_desc {
   float c2w[16], c2w_inv[16];
   float r2c[16], r2c_inv[16];
   float lens_radius;
   float focal_distance;
+  float w2r[16];    /* world to raster: (inverse c2w <> p) <> s2r */
+  float pixel_area; /* pw * ph at the focal length tan (fov / 2) */
+  float reserved;
 } bling_camera_desc;
 
 /* The scene.  Primitive IDs follow the list handed to mkKdTree

@@ -43,11 +43,14 @@ def test_library_exports_every_declared_symbol(so):
 def test_abi_version(so):
     from bling_gb300 import abi
     so.bling_abi_version.restype = C.c_int
-    assert so.bling_abi_version() == abi.ABI_VERSION == 2
+    assert so.bling_abi_version() == abi.ABI_VERSION == 3
     hdr = (ROOT / "include" / "bling_gpu.h").read_text()
     assert f"#define BLING_ABI_VERSION {abi.ABI_VERSION}" in hdr
     # bling_render_params: 8 int32, 4 float, uint64 seed, int32 sampler_kind, int32 reserved
     assert C.sizeof(abi.RenderParams) == 64
+    # bling_camera_desc: c2w, c2w_inv, r2c, r2c_inv, lens radius, focal distance, w2r,
+    # pixel area, reserved
+    assert C.sizeof(abi.CameraDesc) == 4 * (16 * 5 + 4)
 
 
 def test_host_spectrum_helpers_match_oracle(so):
