@@ -88,7 +88,13 @@ class Stats(C.Structure):
                 ("degenerate_rays", C.c_uint64),
                 ("bvh_build_ms", C.c_double), ("last_pass_ms", C.c_double),
                 ("bvh_nodes", C.c_uint64), ("bvh_leaf_prims", C.c_uint64),
-                ("device_bytes", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("light_splats", C.c_uint64)]
+
+
+class LightParams(C.Structure):
+    """bling_light_params: photons per pass, seed, depth limit (0: none)."""
+    _fields_ = [("photons", C.c_int64), ("seed", C.c_uint64), ("max_depth", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 BATCH_PLAIN_LAUNCHES, BATCH_GRAPH, BATCH_DEVICE_LOOP = 0, 1, 2

@@ -91,6 +91,11 @@ def lib():
     L.bling_render_pass_camera.argtypes = [vp, vp, P(abi.RenderParams), P(abi.CameraDesc),
                                            C.c_uint64]
     L.bling_render_pass_camera.restype = C.c_int
+    L.bling_light_pass.argtypes = [vp, vp, P(abi.LightParams), C.c_uint64]
+    L.bling_film_read_splats.argtypes = [vp, P(C.c_float)]
+    L.bling_film_resolve_splats.argtypes = [vp, C.c_float, P(C.c_float)]
+    for fn in ("bling_light_pass", "bling_film_read_splats", "bling_film_resolve_splats"):
+        getattr(L, fn).restype = C.c_int
     L.bling_rgb_to_spectrum.argtypes = [C.c_int32, C.c_float, C.c_float, C.c_float, P(C.c_float)]
     L.bling_spectrum_to_xyz.argtypes = [P(C.c_float), P(C.c_float)]
     L.bling_batch_create.argtypes = [vp, P(abi.BatchOpts), P(vp)]
@@ -252,6 +257,14 @@ class GpuScene:
             self.ctx.check(lib().bling_render_pass_camera(self.h, film.h, C.byref(params),
                                                           C.byref(camera), pass_index))
 
+    def light_pass(self, film: "Film", photons: int, seed: int = 0, pass_index: int = 0,
+                   max_depth: int = 0):
+        """one light-tracer pass of `photons` photons into the film's splat
+        image (LightTracer.hs:37-110); max_depth 0: no limit"""
+        p = abi.LightParams()
+        p.photons, p.seed, p.max_depth = photons, seed, max_depth
+        self.ctx.check(lib().bling_light_pass(self.h, film.h, C.byref(p), pass_index))
+
 
 class Film:
     """A (weight, X, Y, Z) film resident on the device (Image.hs:64-82)."""
@@ -295,6 +308,18 @@ class Film:
     def resolve(self) -> np.ndarray:
         out = np.empty((self.height, self.width, 3), np.float32)
         self.ctx.check(lib().bling_film_resolve(self.h, _fp(out)))
+        return out
+
+    def read_splats(self) -> np.ndarray:
+        """the (height, width, 3) XYZ splat image of light passes"""
+        out = np.empty((self.height, self.width, 3), np.float32)
+        self.ctx.check(lib().bling_film_read_splats(self.h, _fp(out)))
+        return out
+
+    def resolve_splats(self, splat_weight: float) -> np.ndarray:
+        """getPixel with splat weight (Image.hs:302-315) to linear sRGB"""
+        out = np.empty((self.height, self.width, 3), np.float32)
+        self.ctx.check(lib().bling_film_resolve_splats(self.h, splat_weight, _fp(out)))
         return out
 
 

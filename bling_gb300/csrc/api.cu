@@ -330,6 +330,7 @@ void bling_ctx_destroy(bling_ctx* c) {
     if (c->d_scratch) cudaFree(c->d_scratch);
     if (c->d_counter) cudaFree(c->d_counter);
     integrator_workspace_free(c->ws);
+    light_workspace_free(c->lt_ws);
   }
   delete c;
 }
@@ -693,6 +694,7 @@ void bling_film_destroy(bling_film* f) {
     cudaStreamSynchronize(f->ctx->stream);
     cudaFree(f->d_film);
     cudaFree(f->d_acc);
+    cudaFree(f->d_splat);
   }
   delete f;
 }
@@ -728,6 +730,8 @@ int bling_film_clear(bling_film* f) {
   CK(c, cudaMemsetAsync(f->d_film, 0, (size_t)f->width * f->height * 16, c->stream));
   if (f->d_acc)
     CK(c, cudaMemsetAsync(f->d_acc, 0, (size_t)f->width * f->height * 32, c->stream));
+  if (f->d_splat)
+    CK(c, cudaMemsetAsync(f->d_splat, 0, (size_t)f->width * f->height * 12, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
   return BLING_OK;
 }
@@ -778,6 +782,102 @@ int bling_film_resolve(bling_film* f, float* host_rgb) {
     host_rgb[3 * i + 1] = gg;
     host_rgb[3 * i + 2] = b;
   }
+  return BLING_OK;
+}
+
+int bling_film_read_splats(bling_film* f, float* host_xyz) {
+  if (!f || !host_xyz) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = f->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  size_t n = (size_t)f->width * f->height * 3;
+  if (!f->d_splat) {  // no light pass yet: the reference's zeroed splat image
+    std::fill(host_xyz, host_xyz + n, 0.0f);
+    return BLING_OK;
+  }
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaMemcpyAsync(host_xyz, f->d_splat, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return BLING_OK;
+}
+
+int bling_film_resolve_splats(bling_film* f, float splat_weight, float* host_rgb) {
+  if (!f || !host_rgb) return BLING_ERR_INVALID_ARG;
+  size_t np = (size_t)f->width * f->height;
+  std::vector<float> px(4 * np), sp(3 * np);
+  int rc = bling_film_read(f, px.data());
+  if (!rc) rc = bling_film_read_splats(f, sp.data());
+  if (rc) return rc;
+  // getPixel (Image.hs:302-315), xyzToRgb (Spectrum.hs:162-168)
+  float sw = splat_weight;
+  for (size_t i = 0; i < np; i++) {
+    float w = px[4 * i], x = px[4 * i + 1], y = px[4 * i + 2], z = px[4 * i + 3];
+    float sx = sp[3 * i], sy = sp[3 * i + 1], sz = sp[3 * i + 2];
+    if (w == 0) {
+      x = sw * sx;
+      y = sw * sy;
+      z = sw * sz;
+    } else {
+      float wi = 1.0f / w;
+      x = sw * sx + x * wi;
+      y = sw * sy + y * wi;
+      z = sw * sz + z * wi;
+    }
+    host_rgb[3 * i] = 3.240479f * x - 1.537150f * y - 0.498535f * z;
+    host_rgb[3 * i + 1] = (-0.969256f) * x + 1.875991f * y + 0.041556f * z;
+    host_rgb[3 * i + 2] = 0.055648f * x - 0.204043f * y + 1.057311f * z;
+  }
+  return BLING_OK;
+}
+
+// ---------------------------------------------------------------- light tracer
+int bling_light_pass(bling_scene* s, bling_film* f, const bling_light_params* p, uint64_t pass) {
+  if (!s || !f || !p) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = s->ctx;
+  if (f->ctx != c) return set_err(c, BLING_ERR_INVALID_ARG, "film and scene belong to different contexts");
+  if (p->photons < 0 || p->max_depth < 0)
+    return set_err(c, BLING_ERR_INVALID_ARG, "photons and max_depth must be >= 0");
+  const bling_camera_desc& cam = s->shading.camera;
+  if (!(cam.pixel_area > 0))
+    return set_err(c, BLING_ERR_INVALID_ARG,
+                   "the scene's camera has no world-to-raster transform and pixel area");
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  auto t0 = std::chrono::steady_clock::now();
+  size_t sbytes = (size_t)f->width * f->height * 3 * sizeof(float);
+  if (!f->d_splat) {
+    cudaError_t e = cudaMalloc(&f->d_splat, sbytes);
+    if (e != cudaSuccess) {
+      f->d_splat = nullptr;
+      return set_err(c, e == cudaErrorMemoryAllocation ? BLING_ERR_OOM : BLING_ERR_CUDA,
+                     "splat image allocation: %s", cudaGetErrorString(e));
+    }
+    CK(c, cudaMemsetAsync(f->d_splat, 0, sbytes, c->stream));
+  }
+  LightPassArgs a;
+  a.seed = p->seed;
+  a.pass = pass;
+  a.photons = p->photons;
+  a.width = f->width;
+  a.height = f->height;
+  a.max_depth = p->max_depth;
+  // boundingSphere (AABB.hs:53-66) of the primitives' world bounds
+  float lo[3] = {s->lo[0], s->lo[1], s->lo[2]}, hi[3] = {s->hi[0], s->hi[1], s->hi[2]};
+  float d2 = 0;
+  for (int k = 0; k < 3; k++) a.wc[k] = lo[k] + (hi[k] - lo[k]) * 0.5f;
+  float e0 = hi[0] - a.wc[0], e1 = hi[1] - a.wc[1], e2 = hi[2] - a.wc[2];
+  d2 = e0 * e0 + e1 * e1 + e2 * e2;
+  a.wr = sqrtf(d2);
+  LightPassResult res{};
+  int rc = light_pass(c->stream, s->accel, s->shading, a, f->d_splat, c->lt_ws, res, c->err);
+  if (rc) return rc;
+  auto t1 = std::chrono::steady_clock::now();
+  s->stats.last_pass_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  s->stats.rays_closest += res.rays_closest;
+  s->stats.rays_any += res.rays_any;
+  s->stats.path_samples += res.photons;
+  s->stats.nonfinite_drops += res.nonfinite;
+  s->stats.degenerate_rays += res.degenerate;
+  s->stats.light_splats += res.splats;
   return BLING_OK;
 }
 

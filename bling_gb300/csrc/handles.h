@@ -10,6 +10,7 @@
 #include "batch.h"
 #include "integrator.h"
 #include "internal.h"
+#include "lighttrace.h"
 
 struct bling_ctx {
   int device = 0;
@@ -30,6 +31,7 @@ struct bling_ctx {
   cudaEvent_t ev_run[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t ev_out[3] = {nullptr, nullptr, nullptr};
   bgpu::IntegratorWorkspace ws;
+  bgpu::LightWorkspace lt_ws;  // photon slots of the light tracer (made on first use)
 };
 
 struct bling_scene {
@@ -53,6 +55,7 @@ struct bling_film {
   int32_t width = 0, height = 0;
   float* d_film = nullptr;  // width*height*4: the samples added since the last fold
   double* d_acc = nullptr;  // BLING_FILM_FP64: width*height*4 totals of the folded passes
+  float* d_splat = nullptr; // width*height*3 XYZ splats of light passes (made on first use)
 };
 
 struct bling_batch {

@@ -441,11 +441,16 @@ static __device__ BLING_OUTLINE float bxPdfBrdf(const BxDF& b, V3 wo, V3 wi) {
 static __device__ BLING_OUTLINE float bxPdf(const BxDF& b, V3 wo, V3 wi) {
   return bxPdfBrdf(b, wo, b.btdf ? otherHemisphere(wi) : wi);
 }
+// bxdfSample b Adj wo u (Diffuse.hs:14-49, Specular.hs:12-58,
+// Microfacet.hs:42-54); Adj = the adjoint transport of light paths
+template <bool Adj>
 static __device__ BLING_OUTLINE void bxSampleBrdf(const BxDF& b, V3 wo, float u1, float u2, Spec& f, V3& wi, float& pdf);
+template <bool Adj = false>
 static __device__ BLING_OUTLINE void bxSample(const BxDF& b, V3 wo, float u1, float u2, Spec& f, V3& wi, float& pdf) {
-  bxSampleBrdf(b, wo, u1, u2, f, wi, pdf);
+  bxSampleBrdf<Adj>(b, wo, u1, u2, f, wi, pdf);
   if (b.btdf) wi = otherHemisphere(wi);
 }
+template <bool Adj>
 static __device__ BLING_OUTLINE void bxSampleBrdf(const BxDF& b, V3 wo, float u1, float u2, Spec& f, V3& wi, float& pdf) {
   switch (b.kind) {
     case BX_LAMBERT:
@@ -453,6 +458,7 @@ static __device__ BLING_OUTLINE void bxSampleBrdf(const BxDF& b, V3 wo, float u1
       wi = toSameHemisphere(wo, cosineSampleHemisphere(u1, u2));
       if (sameHemisphere(wo, wi)) {
         f = b.kind == BX_LAMBERT ? bxR(b) : sScale(bxR(b), orenNayarScale(b, wo, wi));
+        if (Adj) f = sScale(f, fabsf(cosTheta(wo) / cosTheta(wi)));
         pdf = bxPdfBrdf(b, wo, wi);
       } else {
         f = sConst(0);
@@ -481,10 +487,11 @@ static __device__ BLING_OUTLINE void bxSampleBrdf(const BxDF& b, V3 wo, float u1
       float c = sqrtf(hmax(0.0f, 1.0f - sint2));
       float cost = entering ? -c : c;
       wi = V3{eta * (-wo.x), eta * (-wo.y), cost};
-      float fr = frDielScalar(ei, et, cost);
+      float fr = frDielScalar(ei, et, Adj ? cosTheta(wo) : cost);
       Spec t = bxR(b);
+      float sc = Adj ? fabsf(cosTheta(wo) / cost) : eta2;
 #pragma unroll
-      for (int i = 0; i < 16; i++) f.v[i] = ((1.0f - fr) * t.v[i]) * eta2;
+      for (int i = 0; i < 16; i++) f.v[i] = ((1.0f - fr) * t.v[i]) * sc;
       pdf = 1;
       return;
     }
@@ -501,7 +508,7 @@ static __device__ BLING_OUTLINE void bxSampleBrdf(const BxDF& b, V3 wo, float u1
       float costH = dot(wo, wh);
       float fact = d * fabsf(costH) / p * mfG(wo, wi, wh);
       if (sameHemisphere(wo, wi)) {
-        f = sScale(rTimesFresnel(b, costH), fact / absCosTheta(wi));
+        f = sScale(rTimesFresnel(b, costH), fact / absCosTheta(Adj ? wo : wi));
         pdf = p / (4.0f * fabsf(costH));
       } else {
         f = sConst(0);
@@ -651,7 +658,8 @@ struct BsdfSample {
   V3 wi;
 };
 
-// sampleBsdf'' False bxdfAll (Reflection.hs:278-316)
+// sampleBsdf'' Adj bxdfAll (Reflection.hs:278-316); Adj = sampleAdjBsdf
+template <bool Adj = false>
 static __device__ BLING_OUTLINE BsdfSample sampleBsdf(const Bsdf& b, V3 woW, float uComp, float u1, float u2) {
   BsdfSample out;
   out.type = T_REFL | T_DIFF;
@@ -668,7 +676,7 @@ static __device__ BLING_OUTLINE BsdfSample sampleBsdf(const Bsdf& b, V3 woW, flo
   Spec fSample;
   V3 wi;
   float pdfp;
-  bxSample(bx, wo, u1, u2, fSample, wi, pdfp);
+  bxSample<Adj>(bx, wo, u1, u2, fSample, wi, pdfp);
   V3 wiW = localToWorld(b.cs, wi);
   float sideTest = dot(wiW, b.ng) / dot(woW, b.ng);
   if (pdfp == 0 || sideTest == 0) return out;
@@ -677,14 +685,16 @@ static __device__ BLING_OUTLINE BsdfSample sampleBsdf(const Bsdf& b, V3 woW, flo
   if (!ok) return out;
   out.type = bx.type;
   out.wi = wiW;
+  // fAdj: the adjoint's correction for shading normals
+  const float adjScale = fabsf(sideTest);
   if (bx.type & T_SPEC) {
     out.pdf = pdfp * invCnt;
-    out.f = sScale(fSample, cntf);
+    out.f = sScale(Adj ? sScale(fSample, adjScale) : fSample, cntf);
     return out;
   }
   if (cntm == 1) {
     out.pdf = pdfp;
-    out.f = fSample;
+    out.f = Adj ? sScale(fSample, adjScale) : fSample;
     return out;
   }
   float others = 0.0f;
@@ -695,13 +705,15 @@ static __device__ BLING_OUTLINE BsdfSample sampleBsdf(const Bsdf& b, V3 woW, flo
   for (int i = 0; i < cntm; i++) {
     if (i == sNum) continue;
     bool ok2 = wantTrans ? (b.c[i].type & T_TRANS) != 0 : (b.c[i].type & T_REFL) != 0;
-    if (ok2) fOthers = fOthers + bxEval(b.c[i], wi, wo);
+    if (ok2) fOthers = fOthers + (Adj ? bxEval(b.c[i], wo, wi) : bxEval(b.c[i], wi, wo));
   }
   out.pdf = pdf;
   out.f = sScale(sScale(fSample, pdfp) + fOthers, 1.0f / pdf);
+  if (Adj) out.f = sScale(out.f, adjScale);
   return out;
 }
-// evalBsdf False (Reflection.hs:318-332)
+// evalBsdf Adj (Reflection.hs:318-332)
+template <bool Adj = false>
 static __device__ BLING_OUTLINE Spec evalBsdf(const Bsdf& b, V3 woW, V3 wiW) {
   float cosWo = dot(woW, b.ng);
   float sideTest = dot(wiW, b.ng) / cosWo;
@@ -712,9 +724,9 @@ static __device__ BLING_OUTLINE Spec evalBsdf(const Bsdf& b, V3 woW, V3 wiW) {
   Spec f = sConst(0);
   for (int i = 0; i < b.n; i++) {
     bool ok = wantTrans ? (b.c[i].type & T_TRANS) != 0 : (b.c[i].type & T_REFL) != 0;
-    if (ok) f = f + bxEval(b.c[i], wi, wo);
+    if (ok) f = f + (Adj ? bxEval(b.c[i], wo, wi) : bxEval(b.c[i], wi, wo));
   }
-  return f;
+  return Adj ? sScale(f, fabsf(sideTest)) : f;  // shading-normal correction of the adjoint
 }
 // bsdfPdf (Reflection.hs:251-257)
 static __device__ BLING_OUTLINE float bsdfPdf(const Bsdf& b, V3 woW, V3 wiW) {

@@ -28,15 +28,23 @@ import numpy as np
 F = np.float32
 
 
-def resolve(film: np.ndarray) -> np.ndarray:
+def resolve(film: np.ndarray, splats: np.ndarray | None = None,
+            splat_weight: float = 0.0) -> np.ndarray:
     """(h, w, 4) film (weight, X, Y, Z) -> (h, w, 3) linear RGB, float32:
-    getPixel with splat weight 0 (Image.hs:302-315) and xyzToRgb
-    (Spectrum.hs:162-168), in the reference's binary32 order."""
+    getPixel (Image.hs:302-315) and xyzToRgb (Spectrum.hs:162-168), in the
+    reference's binary32 order.  splats: the (h, w, 3) XYZ splat image of
+    light passes, added with splat_weight (1 / (passes * photons per pass)
+    for the light tracer, LightTracer.hs:44)."""
     from .spectrum import xyz_to_rgb
     f = np.asarray(film, np.float32)
     w = f[..., 0]
     inv = np.where(w != 0, F(1) / np.where(w != 0, w, F(1)), F(0)).astype(np.float32)
-    r, g, b = xyz_to_rgb(f[..., 1] * inv, f[..., 2] * inv, f[..., 3] * inv)
+    x, y, z = f[..., 1] * inv, f[..., 2] * inv, f[..., 3] * inv
+    if splats is not None:
+        sw = F(splat_weight)
+        sp = np.asarray(splats, np.float32)
+        x, y, z = sw * sp[..., 0] + x, sw * sp[..., 1] + y, sw * sp[..., 2] + z
+    r, g, b = xyz_to_rgb(x, y, z)
     return np.stack([r, g, b], -1).astype(np.float32)
 
 

@@ -215,6 +215,7 @@ typedef struct bling_stats {
   uint64_t bvh_nodes;
   uint64_t bvh_leaf_prims;
   uint64_t device_bytes;
+  uint64_t light_splats;    /* camera connections of light passes added to the splat image */
 } bling_stats;
 
 /* ---- context ---- */
@@ -298,6 +299,30 @@ int bling_render_pass_camera(bling_scene* scene, bling_film* film,
                              uint64_t pass);
 
 int bling_scene_stats(bling_scene* scene, bling_stats* out);
+
+/* ---- light tracer ----
+ * replaces the reference's LightTracer renderer (Renderer/LightTracer.hs:
+ * 20-110): photons leave the lights (sampleLightRay, Scene.hs:121-135), bounce
+ * by adjoint BSDF sampling and connect every vertex to the camera
+ * (connectCam, sampleCam: Camera.hs:90-100); unoccluded connections are added
+ * to the film's splat image (splatSample, Image.hs:201-221).  The scene's
+ * camera must carry w2r and pixel_area (mkProjective, Camera.hs:108-147). */
+typedef struct bling_light_params {
+  int64_t photons;   /* photons per pass (mkLightTracer ppp) */
+  uint64_t seed;     /* with the pass index, selects the random stream */
+  int32_t max_depth; /* vertices per photon; 0 = until Russian roulette ends it (the reference) */
+  int32_t reserved;
+} bling_light_params;
+int bling_light_pass(bling_scene* scene, bling_film* film, const bling_light_params* params,
+                     uint64_t pass);
+/* copies the splat image, width*height*3 floats (X, Y, Z); zeros before the
+ * first light pass.  bling_film_clear clears it too. */
+int bling_film_read_splats(bling_film* film, float* host_xyz);
+/* getPixel with splat weight sw (Image.hs:302-315): the film's weighted mean
+ * plus sw times the splats, to linear sRGB floats, width*height*3.  After n
+ * light passes of ppp photons the reference's sw is 1 / (n * ppp)
+ * (LightTracer.hs:44). */
+int bling_film_resolve_splats(bling_film* film, float splat_weight, float* host_rgb);
 
 /* One render pass, like bling_render_pass, that allocates no device memory.
  * No counterpart in the reference: it serves callers that cannot call

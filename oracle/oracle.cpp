@@ -1176,18 +1176,22 @@ static float bxPdfBrdf(const BxDF& b, V wo, V wi) {
 static float bxPdf(const BxDF& b, V wo, V wi) {
   return bxPdfBrdf(b, wo, b.btdf ? otherHemisphere(wi) : wi);
 }
-static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf);
-// bxdfSample b False wo u -> (f, wi, pdf); a BTDF mirrors its BRDF's sample
-static void bxSample(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf) {
-  bxSampleBrdf(b, wo, u1, u2, f, wi, pdf);
+static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf,
+                         bool adj);
+// bxdfSample b adj wo u -> (f, wi, pdf); a BTDF mirrors its BRDF's sample
+// (Reflection.hs:188-195).  adj: the adjoint (light-to-camera) transport
+static void bxSample(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf,
+                     bool adj = false) {
+  bxSampleBrdf(b, wo, u1, u2, f, wi, pdf, adj);
   if (b.btdf) wi = otherHemisphere(wi);
 }
-static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf) {
+static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi, float& pdf,
+                         bool adj) {
   switch (b.kind) {
     case BX_LAMBERT: {  // cosSample (Diffuse.hs:14-22)
       wi = toSameHemisphere(wo, cosineSampleHemisphere(u1, u2));
       if (sameHemisphere(wo, wi)) {
-        f = b.r;
+        f = adj ? sScale(b.r, fabsf(cosTheta(wo) / cosTheta(wi))) : b.r;
         pdf = bxPdfBrdf(b, wo, wi);
       } else {
         f = BLACK;
@@ -1196,10 +1200,11 @@ static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi
       }
       return;
     }
-    case BX_OREN: {  // Diffuse.hs:38-42
+    case BX_OREN: {  // Diffuse.hs:38-49
       wi = toSameHemisphere(wo, cosineSampleHemisphere(u1, u2));
       if (sameHemisphere(wo, wi)) {
-        f = orenNayar(b, wo, wi);
+        f = adj ? sScale(orenNayar(b, wo, wi), fabsf(cosTheta(wo) / cosTheta(wi)))
+                : orenNayar(b, wo, wi);
         pdf = bxPdfBrdf(b, wo, wi);
       } else {
         f = BLACK;
@@ -1213,7 +1218,7 @@ static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi
       pdf = 1;
       return;
     }
-    case BX_SPEC_TRANS: {  // sampleSpecTrans (Specular.hs:100-124), adj = False
+    case BX_SPEC_TRANS: {  // sampleSpecTrans (Specular.hs:35-58)
       bool entering = cosTheta(wo) > 0;
       float ei = entering ? b.ei : b.et, et = entering ? b.et : b.ei;
       float sini2 = sinTheta2(wo);
@@ -1229,8 +1234,8 @@ static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi
       float c = sqrtf(hmax(0.0f, 1.0f - sint2));
       float cost = entering ? -c : c;
       wi = V{eta * (-wo.x), eta * (-wo.y), cost};
-      Spec fr = sConst(frDielScalar(ei, et, cost));
-      f = sScale((WHITE - fr) * b.r, eta2);
+      Spec fr = sConst(frDielScalar(ei, et, adj ? cosTheta(wo) : cost));
+      f = adj ? sScale((WHITE - fr) * b.r, fabsf(cosTheta(wo) / cost)) : sScale((WHITE - fr) * b.r, eta2);
       pdf = 1;
       return;
     }
@@ -1244,7 +1249,7 @@ static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi
       float fact = d * fabsf(costH) / p * mfG(wo, wi, wh);
       Spec fp = b.r * frEval(b.fr, costH);
       if (sameHemisphere(wo, wi)) {
-        f = sScale(fp, fact / absCosTheta(wi));
+        f = sScale(fp, fact / absCosTheta(adj ? wo : wi));
         pdf = p / (4.0f * fabsf(costH));
       } else {
         f = BLACK;
@@ -1410,8 +1415,10 @@ struct BsdfSample {
   V wi;
 };
 
-// sampleBsdf'' False bxdfAll (Reflection.hs:278-316)
-static BsdfSample sampleBsdf(const Bsdf& b, V woW, float uComp, float u1, float u2) {
+// sampleBsdf'' adj bxdfAll (Reflection.hs:278-316); adj = True is
+// sampleAdjBsdf (Reflection.hs:272-273)
+static BsdfSample sampleBsdf(const Bsdf& b, V woW, float uComp, float u1, float u2,
+                             bool adj = false) {
   BsdfSample empty{T_REFL | T_DIFF, 0, BLACK, V{0, 1, 0}};
   if (b.n == 0) return empty;
   V wo = worldToLocal(b.cs, woW);
@@ -1423,27 +1430,30 @@ static BsdfSample sampleBsdf(const Bsdf& b, V woW, float uComp, float u1, float 
   Spec fSample;
   V wi;
   float pdfp;
-  bxSample(bx, wo, u1, u2, fSample, wi, pdfp);
+  bxSample(bx, wo, u1, u2, fSample, wi, pdfp, adj);
   V wiW = localToWorld(b.cs, wi);
   float sideTest = dot(wiW, b.ng) / dot(woW, b.ng);
   if (pdfp == 0 || sideTest == 0) return empty;
   bool wantTrans = sideTest < 0;
   auto flt = [&](const BxDF& x) { return wantTrans ? (x.type & T_TRANS) != 0 : (x.type & T_REFL) != 0; };
   if (!flt(bx)) return empty;
-  if (bx.type & T_SPEC) return BsdfSample{bx.type, pdfp * invCnt, sScale(fSample, cntf), wiW};
-  if (cntm == 1) return BsdfSample{bx.type, pdfp, fSample, wiW};
+  // fAdj: the adjoint's correction for shading normals
+  auto fAdj = [&](const Spec& ff) { return adj ? sScale(ff, fabsf(sideTest)) : ff; };
+  if (bx.type & T_SPEC) return BsdfSample{bx.type, pdfp * invCnt, sScale(fAdj(fSample), cntf), wiW};
+  if (cntm == 1) return BsdfSample{bx.type, pdfp, fAdj(fSample), wiW};
   float others = 0.0f;
   for (int i = 0; i < cntm; i++)
     if (i != sNum) others = others + bxPdf(b.c[i], wo, wi);
   float pdf = (pdfp + others) * invCnt;
   Spec fOthers = BLACK;
   for (int i = 0; i < cntm; i++)
-    if (i != sNum && flt(b.c[i])) fOthers = fOthers + bxEval(b.c[i], wi, wo);  // flip
+    if (i != sNum && flt(b.c[i]))
+      fOthers = fOthers + (adj ? bxEval(b.c[i], wo, wi) : bxEval(b.c[i], wi, wo));  // flip unless adj
   Spec fSum = sScale(sScale(fSample, pdfp) + fOthers, 1.0f / pdf);
-  return BsdfSample{bx.type, pdf, fSum, wiW};
+  return BsdfSample{bx.type, pdf, fAdj(fSum), wiW};
 }
-// evalBsdf False (Reflection.hs:318-332)
-static Spec evalBsdf(const Bsdf& b, V woW, V wiW) {
+// evalBsdf adj (Reflection.hs:318-332)
+static Spec evalBsdf(const Bsdf& b, V woW, V wiW, bool adj = false) {
   float cosWo = dot(woW, b.ng);
   float sideTest = dot(wiW, b.ng) / cosWo;
   if (sideTest == 0) return BLACK;
@@ -1454,9 +1464,9 @@ static Spec evalBsdf(const Bsdf& b, V woW, V wiW) {
   for (int i = 0; i < b.n; i++) {
     const BxDF& x = b.c[i];
     bool ok = wantTrans ? (x.type & T_TRANS) != 0 : (x.type & T_REFL) != 0;
-    if (ok) f = f + bxEval(x, wi, wo);  // flip (bxdfEval b) wo wi
+    if (ok) f = f + (adj ? bxEval(x, wo, wi) : bxEval(x, wi, wo));  // flip (bxdfEval b) unless adj
   }
-  return f;
+  return adj ? sScale(f, fabsf(sideTest)) : f;  // shading-normal correction of the adjoint
 }
 // bsdfPdf (Reflection.hs:251-257)
 static float bsdfPdf(const Bsdf& b, V woW, V wiW) {
@@ -1779,6 +1789,180 @@ static Spec pathLi(const orc_scene& S, const Sampler& smp, Ray ray, int md, int 
     ray = Ray{p, bs.wi, eps, INF};
     C.closest++;
     hit = sceneIntersect(S, ray, it);
+  }
+}
+
+// ---------------------------------------------------------------- light tracer
+// Renderer/LightTracer.hs.  A photon's random numbers come from the shared
+// generator keyed by (seed, pass, photon): dimension 0 picks the light, 1-2
+// the point on it, 3-4 the direction (oneRay, LightTracer.hs:46-55); vertex d
+// draws 5+4d (BSDF component), 6+4d and 7+4d (direction) and 8+4d (Russian
+// roulette) (nextVertex, LightTracer.hs:81-110).
+static inline uint64_t photonKey(uint64_t seed, uint64_t pass, uint64_t photon) {
+  return pixelKey(seed, pass, -0x4c54, (int)(uint32_t)(photon >> 32));
+}
+
+// sample' (Light.hs:166-213): the emitted radiance, the ray leaving the
+// light, the normal there and the pdf; (wc, wr) is the bounding sphere of the
+// scene (boundingSphere, AABB.hs:62-66)
+static void lightEmit(const orc_scene& S, const Light& l, V wc, float wr, float uo1, float uo2,
+                      float ud1, float ud2, Spec& r, Ray& ray, V& ns, float& pd) {
+  if (l.kind == LIGHT_AREA) {
+    const Shape& s = S.shapes[l.shape];
+    V orgp, nsp;
+    sampleShapeP(s, uo1, uo2, orgp, nsp);  // sampleShape'
+    V org = transPoint(s.o2w.m, orgp);
+    ns = normalize(transNormal(s.o2w.i, nsp));
+    V wi = localToWorld(coordinateSystem(ns), cosineSampleHemisphere(ud1, ud2));
+    pd = INV_PI * (1.0f / shapeArea(s)) * absDot(ns, wi);  // shapePdf' = 1 / area
+    ray = Ray{org, wi, 1e-3f, INF};
+    r = s.emission;
+    return;
+  }
+  if (l.kind == BLING_LIGHT_DIRECTIONAL) {
+    LC c = coordinateSystem(l.vec);  // coordinateSystem''
+    float d1, d2;
+    concentricSampleDisk(uo1, uo2, d1, d2);
+    V pdisk = wc + sv(wr, sv(d1, c.s) + sv(d2, c.t));
+    ns = -l.vec;
+    ray = Ray{pdisk + sv(wr, l.vec), ns, 0, INF};
+    pd = 1.0f / (PI * wr * wr);
+    r = l.spec;
+    return;
+  }
+  if (l.kind == BLING_LIGHT_POINT) {
+    V d = uniformSampleSphere(ud1, ud2);
+    ray = Ray{l.vec, d, 0, INF};
+    pd = 1.0f / (2.0f * PI);  // uniformSpherePdf (Montecarlo.hs:188-190)
+    ns = d;
+    r = l.spec;
+    return;
+  }
+  // infinite: sampleContinuous2D over the map, then a disk across the scene
+  float v, pdf1, u, pdf0;
+  int im, iu;
+  sampleContinuous1D(l.mfunc, l.mcdf, l.mint, ud2, v, pdf1, im);
+  sampleContinuous1D(l.cfunc[im], l.ccdf[im], l.cint[im], ud1, u, pdf0, iu);
+  float mapPdf = pdf0 * pdf1;
+  if (mapPdf == 0) {  // emptySample'
+    r = BLACK;
+    ray = Ray{V{0, 0, 0}, V{0, 1, 0}, 0, 0};
+    ns = V{0, 1, 0};
+    pd = 0;
+    return;
+  }
+  r = envLookup(l, u, v);
+  float phi = u * 2.0f * PI, theta = v * PI;  // cartToSph
+  V d = transVector(l.w2l.i, sphericalDirection(sinf(theta), cosf(theta), phi));
+  LC c = coordinateSystem(-d);
+  float d1, d2;
+  concentricSampleDisk(uo1, uo2, d1, d2);
+  V pDisk = wc + sv(wr, sv(d1, c.s) + sv(d2, c.t));
+  ray = Ray{pDisk + sv(wr, d), -d, 0, INF};
+  float sint = sinf(theta);
+  float pdDir = mapPdf / (2.0f * PI * PI * sint);
+  float pdArea = 1.0f / (PI * wr * wr);
+  pd = sint == 0 ? 0.0f : pdDir * pdArea;
+  ns = d;
+}
+
+// sampleCam of the projective camera (Camera.hs:90-100): the raster
+// position of world point p, the lens centre and the pdf
+static void sampleCam(const bling_camera_desc& cam, V p, float& px, float& py, V& pLens,
+                      float& cPdf) {
+  V pRas = transPoint(cam.w2r, p);
+  pLens = transPoint(cam.c2w, V{0, 0, 0});
+  float cost = fabsf(normalize(transPoint(cam.r2c, pRas)).z);
+  float cost3 = cost * cost * cost;
+  cPdf = cam.pixel_area * cost3;
+  px = pRas.x;
+  py = pRas.y;
+}
+
+struct SplatImg {  // the splat part of MImage (Image.hs:64-71), origin (0, 0)
+  int w, h;
+  float* xyz;
+  uint64_t splats = 0, nonfinite = 0;
+};
+
+// connectCam (LightTracer.hs:57-71) with splatSample (Image.hs:201-221).  A
+// splat outside the image is dropped before its visibility is asked (the
+// reference asks first; the image is the same).
+static void connectCam(const orc_scene& S, SplatImg& img, const Spec& li, const Bsdf& bsdf, V wi,
+                       float eps, Counters& C) {
+  float px, py, cPdf;
+  V pCam;
+  V p = bsdf.p;
+  sampleCam(S.cam, p, px, py, pCam, cPdf);
+  V dCam = pCam - p;
+  V we = normalize(dCam);
+  Spec f = evalBsdf(bsdf, wi, we, true);
+  if (isBlack(f) || cPdf == 0) return;
+  float dCam2 = sqLen(dCam);
+  Spec lr = sScale(li * f, 1.0f / (cPdf * dCam2));
+  if (!(px >= 0.0f && px < (float)img.w && py >= 0.0f && py < (float)img.h)) return;
+  C.any++;
+  if (occluded(S, Ray{p, we, eps, sqrtf(dCam2)})) return;
+  if (sNaN(lr) || sInf(lr)) {
+    img.nonfinite++;
+    return;
+  }
+  int ix = (int)floorf(px), iy = (int)floorf(py);
+  float x, y, z;
+  spectrumToXYZ(lr, x, y, z);
+  float* o = img.xyz + 3 * ((size_t)iy * img.w + ix);
+  o[0] = o[0] + x;
+  o[1] = o[1] + y;
+  o[2] = o[2] + z;
+  img.splats++;
+}
+
+// oneRay + nextVertex (LightTracer.hs:46-110) for photon g, iterated;
+// max_depth > 0 stops a photon after that many vertices
+static void tracePhoton(const orc_scene& S, uint64_t seed, uint64_t pass, uint64_t g, V wc,
+                        float wr, int max_depth, SplatImg& img, Counters& C) {
+  uint64_t key = photonKey(seed, pass, g);
+  uint32_t n = (uint32_t)g;
+  int lc = (int)S.lights.size();
+  if (lc == 0) return;  // sampleLightRay of no lights: pdf 0
+  float ul = randF(key, n, 0);
+  float uo1 = randF(key, n, 1), uo2 = randF(key, n, 2);
+  float ud1 = randF(key, n, 3), ud2 = randF(key, n, 4);
+  int ln = lc == 1 ? 0 : std::min((int)floorf(ul * (float)lc), lc - 1);
+  Spec le;
+  Ray ray;
+  V nl;
+  float pdf;
+  lightEmit(S, S.lights[ln], wc, wr, uo1, uo2, ud1, ud2, le, ray, nl, pdf);
+  if (lc != 1) pdf = pdf / (float)lc;  // sampleLightRay (Scene.hs:121-135)
+  V wo = normalize(ray.d);
+  Spec li = sScale(le, absDot(nl, wo) / pdf);
+  if (!(pdf > 0 && !isBlack(li))) return;
+  V wi = -wo;
+  Isect it;
+  C.closest++;
+  bool hit = sceneIntersect(S, ray, it);
+  for (int depth = 0;; depth++) {
+    if (!hit || isBlack(li)) return;
+    uint32_t dim = 5 + 4 * (uint32_t)depth;
+    float ubc = randF(key, n, dim), ubd1 = randF(key, n, dim + 1), ubd2 = randF(key, n, dim + 2);
+    float pcont = depth > 3 ? 0.8f : 1.0f;
+    const Prim& pr = S.prims[it.prim];
+    int mat = pr.is_shape ? S.shapes[pr.index].material : S.meshes[pr.index].material;
+    DG dgs = shadingGeometry(S, pr, it.dg);
+    Bsdf bsdf = materialBsdf(S.mats[mat], it.dg, dgs);
+    V p = bsdf.p;
+    BsdfSample bs = sampleBsdf(bsdf, wi, ubc, ubd1, ubd2, true);  // sampleAdjBsdf
+    Spec li2 = sScale(li * bs.f, 1.0f / pcont);
+    connectCam(S, img, li, bsdf, wi, it.eps, C);
+    if (isBlack(bs.f) || bs.pdf == 0) return;
+    if (randF(key, n, dim + 3) > pcont) return;
+    if (max_depth > 0 && depth + 1 >= max_depth) return;
+    ray = Ray{p, bs.wi, it.eps, INF};
+    C.closest++;
+    hit = sceneIntersect(S, ray, it);
+    wi = -bs.wi;
+    li = li2;
   }
 }
 
@@ -2411,6 +2595,61 @@ void orc_camera_perspective(const float c2w[32], float lr, float fd, float fov, 
   memcpy(out->r2c_inv, r2c + 16, 64);
   out->lens_radius = lr;
   out->focal_distance = fd;
+  // w2r = w2s <> s2r with w2s = inverse c2w <> p; ap = pw * ph
+  float c2wi[32], w2s[32], w2r[32];
+  memcpy(c2wi, c2w + 16, 64);
+  memcpy(c2wi + 16, c2w, 64);
+  orc_xf_concat(c2wi, p, w2s);
+  orc_xf_concat(w2s, s2r, w2r);
+  memcpy(out->w2r, w2r, 64);
+  float fl = tanf(radians(fov) / 2.0f);
+  float pw = fl * (s1 - s0) / sx;
+  float ph = fl * (s3 - s2) / sy;
+  out->pixel_area = pw * ph;
+  out->reserved = 0;
+}
+
+int orc_light_pass(const orc_scene* S, int32_t width, int32_t height, uint64_t seed, uint64_t pass,
+                   int32_t max_depth, int64_t first, int64_t count, float* splat_xyz, int nth,
+                   uint64_t stats[4]) {
+  if (width <= 0 || height <= 0 || count < 0 || first < 0) return BLING_ERR_INVALID_ARG;
+  // worldBounds of the scene's primitives (Primitive/KdTree.hs:111) and its
+  // bounding sphere (AABB.hs:53-66)
+  V lo{INF, INF, INF}, hi{-INF, -INF, -INF};
+  for (size_t i = 0; i < S->prims.size(); i++) {
+    AabbF b = primBounds(*S, (int)i);
+    lo = V{hmin(lo.x, b.lo.x), hmin(lo.y, b.lo.y), hmin(lo.z, b.lo.z)};
+    hi = V{hmax(hi.x, b.hi.x), hmax(hi.y, b.hi.y), hmax(hi.z, b.hi.z)};
+  }
+  V wc = lo + (hi - lo) * V{0.5f, 0.5f, 0.5f};
+  float wr = len(hi - wc);
+  int T = nthreadsOf(nth);
+  if ((int64_t)T > count) T = (int)std::max<int64_t>(1, count);
+  std::vector<std::vector<float>> imgs(T);
+  std::vector<Counters> cs(T);
+  std::vector<uint64_t> sp(T), nf(T);
+  std::vector<std::thread> th;
+  for (int t = 0; t < T; t++) {
+    th.emplace_back([&, t] {
+      imgs[t].assign((size_t)width * height * 3, 0.0f);
+      SplatImg img{width, height, imgs[t].data()};
+      int64_t b = first + count * t / T, e = first + count * (t + 1) / T;
+      for (int64_t g = b; g < e; g++) tracePhoton(*S, seed, pass, (uint64_t)g, wc, wr, max_depth, img, cs[t]);
+      sp[t] = img.splats;
+      nf[t] = img.nonfinite;
+    });
+  }
+  for (auto& x : th) x.join();
+  uint64_t st[4] = {0, 0, 0, 0};
+  for (int t = 0; t < T; t++) {
+    for (size_t k = 0; k < imgs[t].size(); k++) splat_xyz[k] = splat_xyz[k] + imgs[t][k];
+    st[0] += cs[t].closest;
+    st[1] += cs[t].any;
+    st[2] += sp[t];
+    st[3] += nf[t];
+  }
+  if (stats) memcpy(stats, st, sizeof st);
+  return BLING_OK;
 }
 
 }  // extern "C"

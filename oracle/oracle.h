@@ -45,6 +45,16 @@ int orc_render_pass(const orc_scene* s, const bling_render_params* p, uint64_t p
 int orc_sample_li(const orc_scene* s, const bling_render_params* p, uint64_t pass, int px,
                   int py, int n, float* out_xyz, float* out_raster, float* out_spectrum);
 
+/* Photons [first, first + count) of one light-tracer pass (oneRay/nextVertex,
+ * Renderer/LightTracer.hs:46-110) splatted into splat_xyz (width*height*3
+ * floats, accumulated in place; splatSample, Image.hs:201-221) through the
+ * scene's camera (sampleCam, Camera.hs:90-100).  max_depth > 0 ends a photon
+ * after that many vertices (the reference has no limit).  stats: closest and
+ * any-hit queries, splats added, non-finite splats dropped. */
+int orc_light_pass(const orc_scene* s, int32_t width, int32_t height, uint64_t seed, uint64_t pass,
+                   int32_t max_depth, int64_t first, int64_t count, float* splat_xyz, int nthreads,
+                   uint64_t stats[4]);
+
 /* restated helpers, for known-answer tests */
 void orc_rgb_to_spectrum(int illum, float r, float g, float b, float out[16]);
 void orc_spectrum_to_xyz(const float s[16], float xyz[3]);

@@ -38,6 +38,9 @@ def lib():
         L.orc_render_pass.argtypes = [C.c_void_p, P(abi.RenderParams), C.c_uint64, P(C.c_float),
                                       C.c_int, C.c_int, C.c_int, P(C.c_uint64), P(C.c_uint64),
                                       P(C.c_uint64)]
+        L.orc_light_pass.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64,
+                                     C.c_int32, C.c_int64, C.c_int64, P(C.c_float), C.c_int,
+                                     P(C.c_uint64)]
         L.orc_sample_li.argtypes = [C.c_void_p, P(abi.RenderParams), C.c_uint64, C.c_int, C.c_int,
                                     C.c_int, P(C.c_float), P(C.c_float), P(C.c_float)]
         L.orc_rgb_to_spectrum.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, P(C.c_float)]
@@ -111,6 +114,21 @@ class OracleScene:
         if rc != 0:
             raise ValueError(f"orc_render_pass failed: {rc}")
         return film, {"path_samples": ps.value, "rays_closest": rc_.value, "rays_any": ra.value}
+
+    def light_pass(self, width, height, photons, seed=0, pass_index=0, max_depth=0, splats=None,
+                   first=0, count=None, nthreads=0):
+        """Photons [first, first + count) of a light-tracer pass into an
+        (height, width, 3) XYZ splat image; returns (splats, stats)."""
+        if splats is None:
+            splats = np.zeros((height, width, 3), np.float32)
+        count = photons - first if count is None else count
+        st = (C.c_uint64 * 4)()
+        rc = lib().orc_light_pass(self.h, width, height, seed, pass_index, max_depth, first, count,
+                                  fp(splats), nthreads, st)
+        if rc != 0:
+            raise ValueError(f"orc_light_pass failed: {rc}")
+        return splats, {"rays_closest": st[0], "rays_any": st[1], "splats": st[2],
+                        "nonfinite": st[3]}
 
     def sample_li(self, params, pass_index, px, py, n):
         xyz = np.zeros(3, np.float32)

@@ -1,0 +1,179 @@
+"""Parity of the GPU light tracer (bling_light_pass) with the CPU oracle.
+
+The oracle and the GPU draw the same random numbers per photon, so photon
+paths coincide until a transcendental function (sinf/cosf/powf, not correctly
+rounded on either side) perturbs a direction in the last bit; the splat image
+is summed with atomics on the GPU (another order of float additions).  The
+tests check per-pixel XYZ within 1e-3 relative for most pixels (2e-3 with
+glossy and specular paths), image means within 0.5%, query and splat counts
+within 1%, and that the light tracer converges to the path tracer's image.
+"""
+import numpy as np
+import pytest
+
+from bling_gb300 import abi, image
+from bling_gb300 import scene as S
+from bling_gb300 import transform as xf
+from bling_gb300.spectrum import constant, rgb_to_spectrum
+from oracle.oracle import OracleScene
+
+pytestmark = pytest.mark.gpu
+
+
+def _both(gpu_ctx, sc, w, h, photons, seed=1, passes=1, max_depth=0):
+    g = gpu_ctx.scene(sc)
+    film = gpu_ctx.film(w, h)
+    o = OracleScene(sc)
+    so = None
+    sts = []
+    for k in range(passes):
+        g.light_pass(film, photons, seed=seed, pass_index=k, max_depth=max_depth)
+        so, st = o.light_pass(w, h, photons, seed=seed, pass_index=k, max_depth=max_depth,
+                              splats=so)
+        sts.append(st)
+    return film, g, so, sts
+
+
+def _compare(sg, so, rel=1e-3, frac=0.97):
+    scale = np.abs(so).mean() + 1e-12
+    err = np.abs(sg - so) / (np.abs(so) + 1e-3 * scale)
+    close = (err <= rel).all(-1)
+    assert close.mean() >= frac, f"only {close.mean():.4f} of pixels within {rel}"
+    m_g, m_o = sg.mean(axis=(0, 1)), so.mean(axis=(0, 1))
+    assert np.all(np.abs(m_g - m_o) <= 5e-3 * np.abs(m_o) + 1e-9), (m_g, m_o)
+
+
+def _counts_close(stats_g, st_o, photons):
+    assert stats_g["path_samples"] == photons
+    assert abs(stats_g["rays_closest"] - st_o["rays_closest"]) <= 0.01 * st_o["rays_closest"]
+    assert abs(stats_g["rays_any"] - st_o["rays_any"]) <= 0.01 * st_o["rays_any"] + 2
+    assert abs(stats_g["light_splats"] - st_o["splats"]) <= 0.01 * st_o["splats"] + 2
+    assert stats_g["nonfinite_drops"] == st_o["nonfinite"] == 0
+
+
+def test_cornell_room_light_pass_vs_oracle(gpu_ctx):
+    sc = S.cornell_room(48, 48)
+    film, g, so, st = _both(gpu_ctx, sc, 48, 48, 200_000, seed=7)
+    sg = film.read_splats()
+    _compare(sg, so)
+    _counts_close(g.stats(), st[0], 200_000)
+    # the film's camera-sample part is untouched
+    assert not film.read().any()
+
+
+def _lights_materials_scene(w=64, h=48):
+    """every material kind on spheres and a translucent panel over a matte
+    floor, lit by sphere, disk, cylinder and box area lights, a point light,
+    a directional light and an environment map"""
+    s = S.Scene()
+    floor = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.6, 0.6, 0.6)), sigma=0.3)
+    mats = [
+        s.add_material(abi.MAT_PLASTIC, kd=rgb_to_spectrum((0.2, 0.3, 0.7)), ks=constant(0.4),
+                       roughness=0.1),
+        s.add_material(abi.MAT_METAL, eta=constant(0.2), k=constant(3.9), roughness=0.05),
+        s.add_material(abi.MAT_GLASS, ks=constant(1.0), kt=constant(1.0), ior=1.5),
+        s.add_material(abi.MAT_MIRROR, ks=rgb_to_spectrum((0.9, 0.9, 0.8))),
+        s.add_material(abi.MAT_SHINY_METAL, kd=rgb_to_spectrum((0.95, 0.8, 0.4)),
+                       ks=rgb_to_spectrum((0.5, 0.45, 0.3)), roughness=0.1),
+        s.add_material(abi.MAT_TRANS_MATTE, kd=rgb_to_spectrum((0.3, 0.4, 0.3)),
+                       kt=rgb_to_spectrum((0.7, 0.6, 0.5)), sigma=0.2),
+        s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.7, 0.3, 0.2))),
+    ]
+    v = np.array([[-4, 0, -4], [4, 0, -4], [4, 0, 4], [-4, 0, 4]], np.float32)
+    s.add_mesh(v, [0, 1, 2, 0, 2, 3], floor)
+    order = [0]
+    for k, m in enumerate(mats):
+        x = -2.1 + 0.7 * k
+        order.append(~s.add_shape(abi.SHAPE_SPHERE, (0.3,), xf.translate(x, 0.3, 0.2), m))
+    em = rgb_to_spectrum((4, 3.5, 3), illuminant=True)
+    order.append(~s.add_shape(abi.SHAPE_SPHERE, (0.25,), xf.translate(0, 2.4, -0.8), floor,
+                              emission=em))
+    order.append(~s.add_shape(abi.SHAPE_DISK, (0.0, 0.4, 0.1, 2 * np.pi),
+                              xf.rotate_x(90) @ xf.translate(-1.5, 2.0, 0.0), floor, emission=em))
+    order.append(~s.add_shape(abi.SHAPE_CYLINDER, (0.08, -0.5, 0.5, 2 * np.pi),
+                              xf.rotate_x(90) @ xf.translate(1.8, 0.6, -0.8), floor, emission=em))
+    order.append(~s.add_shape(abi.SHAPE_BOX, (-0.1, -0.1, -0.1, 0.1, 0.1, 0.1),
+                              xf.translate(-0.6, 0.15, -0.9), floor, emission=em))
+    trans = s.add_material(abi.MAT_TRANS_MATTE, kd=rgb_to_spectrum((0.5, 0.5, 0.5)),
+                           kt=rgb_to_spectrum((0.9, 0.9, 0.9)))
+    order.append(~s.add_shape(abi.SHAPE_QUAD, (0.8, 0.8),
+                              xf.rotate_x(-90) @ xf.translate(0.0, 1.6, -0.8), trans))
+    s.prim_order = order
+    sun = S.Light(abi.LIGHT_DIRECTIONAL, rgb_to_spectrum((1.5, 1.4, 1.2), illuminant=True),
+                  vec=tuple(np.array([0.3, 0.8, -0.5]) / np.linalg.norm([0.3, 0.8, -0.5])))
+    env = np.zeros((16, 32, 16), np.float32)
+    for y in range(16):
+        env[y] = rgb_to_spectrum((0.2 + 0.02 * y, 0.3, 0.5 - 0.02 * y), illuminant=True)
+    sky = S.Light(abi.LIGHT_INFINITE, env=env, w2l=xf.rotate_x(-90))
+    point = S.Light(abi.LIGHT_POINT, rgb_to_spectrum((2, 2, 2), illuminant=True),
+                    vec=(0.5, 2.2, -1.5))
+    s.lights = [sun, sky, point]
+    look = xf.look_at((0, 1.6, -4.5), (0, 0.4, 0), (0, 1, 0))
+    s.set_perspective(look, 0.0, 1.0, 45.0, w, h)
+    return s
+
+
+def test_every_light_and_material_vs_oracle(gpu_ctx):
+    sc = _lights_materials_scene()
+    film, g, so, st = _both(gpu_ctx, sc, 64, 48, 300_000, seed=3)
+    sg = film.read_splats()
+    _compare(sg, so, rel=2e-3, frac=0.9)
+    _counts_close(g.stats(), st[0], 300_000)
+
+
+def test_passes_accumulate_and_clear(gpu_ctx):
+    sc = S.cornell_room(32, 32)
+    film, g, so, st = _both(gpu_ctx, sc, 32, 32, 50_000, seed=2, passes=3)
+    _compare(film.read_splats(), so)
+    film.clear()
+    assert not film.read_splats().any()
+    fresh = gpu_ctx.film(32, 32)
+    assert not fresh.read_splats().any()  # before any light pass
+
+
+def test_max_depth_one_is_direct_connections_only(gpu_ctx):
+    sc = S.cornell_room(32, 32)
+    film, g, so, st = _both(gpu_ctx, sc, 32, 32, 100_000, seed=4, max_depth=1)
+    _compare(film.read_splats(), so)
+    # one closest-hit query per emitted photon, none after its first vertex
+    assert g.stats()["rays_closest"] == st[0]["rays_closest"] <= 100_000
+
+
+def test_resolve_splats_matches_host(gpu_ctx):
+    sc = S.cornell_room(32, 32)
+    g = gpu_ctx.scene(sc)
+    film = gpu_ctx.film(32, 32)
+    g.render_pass(film, S.cornell_params(32, 32, spp_side=2), 0)
+    g.light_pass(film, 40_000, seed=1)
+    sw = 1.0 / 40_000
+    got = film.resolve_splats(sw)
+    want = image.resolve(film.read(), film.read_splats(), sw)
+    assert np.allclose(got, want, rtol=1e-6, atol=1e-7)
+
+
+def test_light_tracer_converges_to_the_path_tracer(gpu_ctx):
+    W = H = 48
+    sc = S.cornell_room(W, H)
+    g = gpu_ctx.scene(sc)
+    pt_film = gpu_ctx.film(W, H)
+    g.render_pass(pt_film, S.cornell_params(W, H, spp_side=24, max_depth=40, rr_depth=3), 0)
+    pt = pt_film.resolve()
+    lt_film = gpu_ctx.film(W, H)
+    n = 4_000_000
+    for k in range(4):
+        g.light_pass(lt_film, n, seed=11, pass_index=k)
+    lt = lt_film.resolve_splats(1.0 / (4 * n))
+    for sl in (np.s_[18:30, 18:30], np.s_[38:46, 12:36], np.s_[12:24, 12:36], np.s_[16:32, 2:8]):
+        a, b = pt[sl].mean((0, 1)), lt[sl].mean((0, 1))
+        assert np.all(np.abs(a - b) <= 0.04 * np.abs(a) + 1e-3), (sl, a, b)
+
+
+def test_camera_without_world_to_raster_is_refused(gpu_ctx):
+    sc = S.cornell_room(16, 16)
+    look = xf.look_at((0.5, 0.5, -1.4), (0.5, 0.5, 0.5), (0, 1, 0))
+    c2w, r2c = xf.perspective_camera(look, 0.0, 1.0, 40.0, 16, 16)
+    sc.set_camera(c2w, r2c)  # no w2r / pixel area
+    g = gpu_ctx.scene(sc)
+    film = gpu_ctx.film(16, 16)
+    with pytest.raises(Exception, match="world-to-raster"):
+        g.light_pass(film, 1000)
