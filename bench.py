@@ -311,6 +311,68 @@ def measure_render(ctx, stream, args):
     return out
 
 
+def measure_light(ctx, stream, args):
+    """The light tracer on the Cornell room (secondary line): photons/s and
+    Mrays/s (emission, continuation and camera-connection queries, counted on
+    the device) per pass of `--light-photons` photons, CUDA events on the
+    stream; the oracle's light tracer on a bounded photon sample beside it."""
+    import torch
+
+    from bling_gb300 import scene as S
+    W = H = 256
+    n = args.light_photons
+    sc = S.cornell_room(W, H)
+    g = ctx.scene(sc)
+    film = ctx.film(W, H)
+    g.light_pass(film, n, seed=1, pass_index=0)  # warm-up pass
+    s0 = g.stats()
+    times = []
+    passes = 3
+    for k in range(passes):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record(stream)
+        g.light_pass(film, n, seed=1, pass_index=k + 1)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        times.append(ev[0].elapsed_time(ev[1]) / 1e3)
+    s1 = g.stats()
+    tot = sum(times)
+    rays = (s1["rays_closest"] - s0["rays_closest"]) + (s1["rays_any"] - s0["rays_any"])
+    out = {"workload": f"cornell_{W}x{H}_{n}_photons_per_pass",
+           "photons_per_s": round(passes * n / tot, 1), "mrays_per_s": round(rays / tot / 1e6, 2),
+           "ms_per_pass": round(tot / passes * 1e3, 3), "passes": passes,
+           "rays_per_photon": round(rays / (passes * n), 3),
+           "splats_per_photon": round((s1["light_splats"] - s0["light_splats"]) / (passes * n), 3),
+           "nonfinite_drops": s1["nonfinite_drops"]}
+    if not args.no_cpu_baseline:
+        from oracle.oracle import OracleScene
+        o = OracleScene(sc)
+        m = 400_000
+        t0 = time.perf_counter()
+        o.light_pass(W, H, m, seed=1, pass_index=1)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(m / dt, 1), "unit": "photons/s",
+                               "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"{m} photons of one pass, all host threads"}
+    del g, film
+    return out
+
+
+def run_light_profile(args):
+    """Only light passes of the Cornell room (for an ncu launch list)."""
+    from bling_gb300.api import Context
+    from bling_gb300 import scene as S
+    ctx = Context(device=0)
+    g = ctx.scene(S.cornell_room(256, 256))
+    film = ctx.film(256, 256)
+    for k in range(args.warmup + args.steps):
+        g.light_pass(film, args.light_photons, seed=1, pass_index=k)
+    st = g.stats()
+    print(json.dumps({"light_profile": True, "photons": args.light_photons,
+                      "passes": args.warmup + args.steps, "rays_closest": st["rays_closest"],
+                      "rays_any": st["rays_any"], "splats": st["light_splats"]}))
+
+
 def _extent_samples(p):
     from bling_gb300.autotune import extent_samples
     return extent_samples(p)
@@ -601,6 +663,9 @@ def run_ours(args):
     render = None
     if not args.no_render and rank == 0:
         render = measure_render(ctx, stream, args)
+    light = None
+    if not args.no_light and rank == 0:
+        light = measure_light(ctx, stream, args)
     batched = served = None
     if not args.no_batch and rank == 0:
         batched = measure_batched(args)
@@ -652,6 +717,7 @@ def run_ours(args):
             "bvh_build_ms": round(st["bvh_build_ms"], 1),
             "bvh_nodes": st["bvh_nodes"],
             "path_integrator": render,
+            "light_tracer": light,
             "batched_wavefront": batched,
             "serving": served,
         }
@@ -742,6 +808,10 @@ def main():
     ap.add_argument("--no-render", action="store_true", help="skip the path-integrator workloads")
     ap.add_argument("--no-heightfield", action="store_true")
     ap.add_argument("--wide-bvh", action="store_true", help="8-wide quantised BVH layout")
+    ap.add_argument("--no-light", action="store_true", help="skip the light-tracer workload")
+    ap.add_argument("--light-photons", type=int, default=1 << 22)
+    ap.add_argument("--light-profile", action="store_true",
+                    help="only run light passes of the Cornell room (profiling)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched workload")
     ap.add_argument("--batch-instances", type=int, default=64)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
@@ -760,7 +830,9 @@ def main():
     N_RAYS, N_ANY = args.rays, args.rays // 2
     if args.warmup < 3:
         args.warmup = 3
-    if args.render_size:
+    if args.light_profile:
+        run_light_profile(args)
+    elif args.render_size:
         run_render_profile(args)
     elif args.batch_profile:
         run_batch_profile(args)

@@ -67,6 +67,7 @@ class Job:
     strata: tuple = (2, 2)             # (nu, nv), or (spp, 1) for the random sampler
     max_depth: int = 7                 # mkPathIntegrator 7 3 (IntegratorParser.hs)
     sample_depth: int = 3
+    photons_per_pass: int = 0          # renderer { light passPhotons N } (RendererParser.hs:28-30)
 
     def params(self, seed: int = 1, rr_depth: int = 7) -> abi.RenderParams:
         """bling_render_params of the job's sampler renderer and path
@@ -269,6 +270,7 @@ class _State:
     def __init__(self, base: Path):
         self.res = (640, 480)
         self.renderer = "path"
+        self.photons = 0  # photons per pass of the light tracer
         self.sampler = (abi.SAMPLER_STRATIFIED, (2, 2))
         self.depths = (7, 3)
         self.filter = (abi.FILTER_BOX, (0.0, 0.0, 0.0, 0.0))
@@ -318,7 +320,8 @@ class _Parser:
         sc.set_perspective(c2w, float(lr), float(fd), fov, sx, sy)
         (kind, strata), (md, sd) = self.s.sampler, self.s.depths
         fk, fp = self.s.filter
-        return Job(sc, self.s.res[0], self.s.res[1], fk, fp, self.s.renderer, kind, strata, md, sd)
+        return Job(sc, self.s.res[0], self.s.res[1], fk, fp, self.s.renderer, kind, strata, md, sd,
+                   self.s.photons)
 
     def p_size(self):
         self.s.res = (self.t.integ(), self.t.integ())
@@ -345,6 +348,10 @@ class _Parser:
 
         def body():
             name = t.word()
+            if name == "light":  # mkLightTracer ppp, run by bling_light_pass
+                self.s.photons = t.named_int("passPhotons")
+                self.s.renderer = "light"
+                return
             if name != "sampler":
                 self._skip_to_block_end()
                 self.s.renderer = name

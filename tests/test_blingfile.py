@@ -161,6 +161,8 @@ def test_constant_spd_gives_a_flat_spectrum():
 def test_other_renderers_parse_and_are_named():
     j = B.parse("renderer { sppm photonCount 20000 maxDepth 10 radius 10 alpha 0.9 }")
     assert j.renderer == "sppm"
+    j = B.parse("renderer { light passPhotons 50000 }")
+    assert j.renderer == "light" and j.photons_per_pass == 50000
     j = B.parse("renderer { sampler sampled { sampler { random 16 } "
                 "integrator { directLighting maxDepth 3 } } }")
     assert j.renderer == "sampler/directLighting" and j.strata == (16, 1)
