@@ -91,6 +91,22 @@ class Stats(C.Structure):
                 ("device_bytes", C.c_uint64), ("light_splats", C.c_uint64)]
 
 
+class SppmParams(C.Structure):
+    """bling_sppm_params: mkSPPM n md r alpha, the pixel filter, the seed."""
+    _fields_ = [("photons", C.c_int64), ("max_depth", C.c_int32), ("radius", C.c_float),
+                ("alpha", C.c_float), ("filter_kind", C.c_int32), ("filter_params", C.c_float * 4),
+                ("seed", C.c_uint64)]
+
+
+def sppm_params(photons, max_depth=5, radius=0.05, alpha=0.7, filter_kind=FILTER_BOX,
+                filter_params=(0.0, 0.0, 0.0, 0.0), seed=1) -> SppmParams:
+    p = SppmParams()
+    p.photons, p.max_depth, p.radius, p.alpha = photons, max_depth, radius, alpha
+    p.filter_kind, p.seed = filter_kind, seed
+    p.filter_params[:] = list(filter_params)
+    return p
+
+
 class LightParams(C.Structure):
     """bling_light_params: photons per pass, seed, depth limit (0: none)."""
     _fields_ = [("photons", C.c_int64), ("seed", C.c_uint64), ("max_depth", C.c_int32),

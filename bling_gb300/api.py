@@ -94,7 +94,10 @@ def lib():
     L.bling_light_pass.argtypes = [vp, vp, P(abi.LightParams), C.c_uint64]
     L.bling_film_read_splats.argtypes = [vp, P(C.c_float)]
     L.bling_film_resolve_splats.argtypes = [vp, C.c_float, P(C.c_float)]
-    for fn in ("bling_light_pass", "bling_film_read_splats", "bling_film_resolve_splats"):
+    L.bling_sppm_pass.argtypes = [vp, vp, P(abi.SppmParams), C.c_uint64]
+    L.bling_film_read_sppm_radii.argtypes = [vp, P(C.c_float), C.c_int64, P(C.c_int64)]
+    for fn in ("bling_light_pass", "bling_film_read_splats", "bling_film_resolve_splats",
+               "bling_sppm_pass", "bling_film_read_sppm_radii"):
         getattr(L, fn).restype = C.c_int
     L.bling_rgb_to_spectrum.argtypes = [C.c_int32, C.c_float, C.c_float, C.c_float, P(C.c_float)]
     L.bling_spectrum_to_xyz.argtypes = [P(C.c_float), P(C.c_float)]
@@ -265,6 +268,11 @@ class GpuScene:
         p.photons, p.seed, p.max_depth = photons, seed, max_depth
         self.ctx.check(lib().bling_light_pass(self.h, film.h, C.byref(p), pass_index))
 
+    def sppm_pass(self, film: "Film", params, pass_index: int = 0):
+        """one SPPM pass (SPPM.hs:392-480): camera samples into the film,
+        photon splats into its splat image; params: abi.SppmParams"""
+        self.ctx.check(lib().bling_sppm_pass(self.h, film.h, C.byref(params), pass_index))
+
 
 class Film:
     """A (weight, X, Y, Z) film resident on the device (Image.hs:64-82)."""
@@ -314,6 +322,16 @@ class Film:
         """the (height, width, 3) XYZ splat image of light passes"""
         out = np.empty((self.height, self.width, 3), np.float32)
         self.ctx.check(lib().bling_film_read_splats(self.h, _fp(out)))
+        return out
+
+    def read_sppm_radii(self) -> np.ndarray:
+        """the squared SPPM radii of the sample extent's pixels (empty before
+        the first SPPM pass)"""
+        n = C.c_int64()
+        self.ctx.check(lib().bling_film_read_sppm_radii(self.h, None, 0, C.byref(n)))
+        out = np.empty(n.value, np.float32)
+        if n.value:
+            self.ctx.check(lib().bling_film_read_sppm_radii(self.h, _fp(out), n.value, C.byref(n)))
         return out
 
     def resolve_splats(self, splat_weight: float) -> np.ndarray:

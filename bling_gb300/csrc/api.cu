@@ -331,6 +331,7 @@ void bling_ctx_destroy(bling_ctx* c) {
     if (c->d_counter) cudaFree(c->d_counter);
     integrator_workspace_free(c->ws);
     light_workspace_free(c->lt_ws);
+    sppm_workspace_free(c->sp_ws);
   }
   delete c;
 }
@@ -695,6 +696,7 @@ void bling_film_destroy(bling_film* f) {
     cudaFree(f->d_film);
     cudaFree(f->d_acc);
     cudaFree(f->d_splat);
+    cudaFree(f->d_sppm);
   }
   delete f;
 }
@@ -733,6 +735,9 @@ int bling_film_clear(bling_film* f) {
   if (f->d_splat)
     CK(c, cudaMemsetAsync(f->d_splat, 0, (size_t)f->width * f->height * 12, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  cudaFree(f->d_sppm);  // the next SPPM pass starts from the initial radius again
+  f->d_sppm = nullptr;
+  f->sppm_pixels = 0;
   return BLING_OK;
 }
 
@@ -829,6 +834,115 @@ int bling_film_resolve_splats(bling_film* f, float splat_weight, float* host_rgb
   return BLING_OK;
 }
 
+// ---------------------------------------------------------------- SPPM
+namespace {
+// the film's splat image, made on first use
+int ensure_splats(bling_ctx* c, bling_film* f) {
+  if (f->d_splat) return BLING_OK;
+  size_t sbytes = (size_t)f->width * f->height * 3 * sizeof(float);
+  cudaError_t e = cudaMalloc(&f->d_splat, sbytes);
+  if (e != cudaSuccess) {
+    f->d_splat = nullptr;
+    return set_err(c, e == cudaErrorMemoryAllocation ? BLING_ERR_OOM : BLING_ERR_CUDA,
+                   "splat image allocation: %s", cudaGetErrorString(e));
+  }
+  CK(c, cudaMemsetAsync(f->d_splat, 0, sbytes, c->stream));
+  return BLING_OK;
+}
+// boundingSphere (AABB.hs:53-66) of the primitives' world bounds
+void scene_sphere(const bling_scene* s, float wc[3], float& wr) {
+  for (int k = 0; k < 3; k++) wc[k] = s->lo[k] + (s->hi[k] - s->lo[k]) * 0.5f;
+  float e0 = s->hi[0] - wc[0], e1 = s->hi[1] - wc[1], e2 = s->hi[2] - wc[2];
+  wr = sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
+}
+}  // namespace
+
+int bling_sppm_pass(bling_scene* s, bling_film* f, const bling_sppm_params* p, uint64_t pass) {
+  if (!s || !f || !p) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = s->ctx;
+  if (f->ctx != c) return set_err(c, BLING_ERR_INVALID_ARG, "film and scene belong to different contexts");
+  if (p->photons < 0 || p->max_depth < 1 || p->max_depth > 24)
+    return set_err(c, BLING_ERR_INVALID_ARG, "photons must be >= 0 and max_depth in 1..24");
+  if (!(p->radius > 0) || !(p->alpha > 0 && p->alpha < 1))
+    return set_err(c, BLING_ERR_INVALID_ARG, "radius must be > 0 and alpha in (0, 1)");
+  SppmArgs a;
+  memset(&a, 0, sizeof a);
+  a.seed = p->seed;
+  a.pass = pass;
+  a.photons = p->photons;
+  a.max_depth = p->max_depth;
+  a.alpha = p->alpha;
+  a.rp.width = f->width;
+  a.rp.height = f->height;
+  a.rp.strata_x = a.rp.strata_y = 1;  // mkRandomSampler 1 (SPPM.hs:150)
+  a.rp.max_depth = p->max_depth;
+  a.rp.rr_depth = 7;
+  a.rp.filter_kind = p->filter_kind;
+  memcpy(a.rp.filter_params, p->filter_params, sizeof a.rp.filter_params);
+  a.rp.seed = p->seed;
+  a.rp.sampler_kind = BLING_SAMPLER_RANDOM;
+  int prc = check_render_params(c, &a.rp);
+  if (prc) return prc;
+  scene_sphere(s, a.wc, a.wr);
+  std::lock_guard<std::mutex> g(c->mu);
+  CK(c, cudaSetDevice(c->device));
+  auto t0 = std::chrono::steady_clock::now();
+  int rc = ensure_splats(c, f);
+  if (rc) return rc;
+  int64_t np = 0;
+  rc = sppm_extent_pixels(a.rp, np, c->err);
+  if (rc) return rc;
+  if (!f->d_sppm || f->sppm_pixels != np) {  // first pass: every radius^2 = r * r, N = M = 0
+    cudaFree(f->d_sppm);
+    f->d_sppm = nullptr;
+    f->sppm_pixels = 0;
+    cudaError_t e = cudaMalloc(&f->d_sppm, (size_t)np * 12);
+    if (e != cudaSuccess) {
+      f->d_sppm = nullptr;
+      return set_err(c, e == cudaErrorMemoryAllocation ? BLING_ERR_OOM : BLING_ERR_CUDA,
+                     "SPPM statistics allocation: %s", cudaGetErrorString(e));
+    }
+    std::vector<float> r2(np, p->radius * p->radius);
+    CK(c, cudaMemcpyAsync(f->d_sppm, r2.data(), (size_t)np * 4, cudaMemcpyHostToDevice, c->stream));
+    CK(c, cudaMemsetAsync((char*)f->d_sppm + (size_t)np * 4, 0, (size_t)np * 8, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    f->sppm_pixels = np;
+  }
+  SppmPixelStats px{(float*)f->d_sppm, (float*)f->d_sppm + np, (uint32_t*)((float*)f->d_sppm + 2 * np),
+                    np};
+  SppmResult res{};
+  rc = sppm_pass(c->stream, s->accel, s->shading, a, f->d_film, f->d_splat, px, c->sp_ws, res,
+                 c->err);
+  if (rc) return rc;
+  if (f->d_acc) {  // the camera samples' FP32 sums into the FP64 totals
+    CK(c, film_fold(f, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  s->stats.last_pass_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  s->stats.rays_closest += res.rays_closest;
+  s->stats.path_samples += res.camera_samples + res.photons;
+  s->stats.nonfinite_drops += res.nonfinite;
+  s->stats.degenerate_rays += res.degenerate;
+  s->stats.light_splats += res.splats;
+  return BLING_OK;
+}
+
+int bling_film_read_sppm_radii(bling_film* f, float* r2, int64_t capacity, int64_t* count) {
+  if (!f || !count) return BLING_ERR_INVALID_ARG;
+  bling_ctx* c = f->ctx;
+  std::lock_guard<std::mutex> g(c->mu);
+  *count = f->d_sppm ? f->sppm_pixels : 0;
+  if (!f->d_sppm) return BLING_OK;
+  if (!r2 || capacity < f->sppm_pixels)
+    return set_err(c, BLING_ERR_BOUNDS, "radius buffer holds %lld of %lld pixels",
+                   (long long)capacity, (long long)f->sppm_pixels);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaMemcpyAsync(r2, f->d_sppm, (size_t)f->sppm_pixels * 4, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return BLING_OK;
+}
+
 // ---------------------------------------------------------------- light tracer
 int bling_light_pass(bling_scene* s, bling_film* f, const bling_light_params* p, uint64_t pass) {
   if (!s || !f || !p) return BLING_ERR_INVALID_ARG;
@@ -843,16 +957,8 @@ int bling_light_pass(bling_scene* s, bling_film* f, const bling_light_params* p,
   std::lock_guard<std::mutex> g(c->mu);
   CK(c, cudaSetDevice(c->device));
   auto t0 = std::chrono::steady_clock::now();
-  size_t sbytes = (size_t)f->width * f->height * 3 * sizeof(float);
-  if (!f->d_splat) {
-    cudaError_t e = cudaMalloc(&f->d_splat, sbytes);
-    if (e != cudaSuccess) {
-      f->d_splat = nullptr;
-      return set_err(c, e == cudaErrorMemoryAllocation ? BLING_ERR_OOM : BLING_ERR_CUDA,
-                     "splat image allocation: %s", cudaGetErrorString(e));
-    }
-    CK(c, cudaMemsetAsync(f->d_splat, 0, sbytes, c->stream));
-  }
+  int src = ensure_splats(c, f);
+  if (src) return src;
   LightPassArgs a;
   a.seed = p->seed;
   a.pass = pass;
@@ -860,13 +966,7 @@ int bling_light_pass(bling_scene* s, bling_film* f, const bling_light_params* p,
   a.width = f->width;
   a.height = f->height;
   a.max_depth = p->max_depth;
-  // boundingSphere (AABB.hs:53-66) of the primitives' world bounds
-  float lo[3] = {s->lo[0], s->lo[1], s->lo[2]}, hi[3] = {s->hi[0], s->hi[1], s->hi[2]};
-  float d2 = 0;
-  for (int k = 0; k < 3; k++) a.wc[k] = lo[k] + (hi[k] - lo[k]) * 0.5f;
-  float e0 = hi[0] - a.wc[0], e1 = hi[1] - a.wc[1], e2 = hi[2] - a.wc[2];
-  d2 = e0 * e0 + e1 * e1 + e2 * e2;
-  a.wr = sqrtf(d2);
+  scene_sphere(s, a.wc, a.wr);
   LightPassResult res{};
   int rc = light_pass(c->stream, s->accel, s->shading, a, f->d_splat, c->lt_ws, res, c->err);
   if (rc) return rc;

@@ -11,6 +11,7 @@
 #include "integrator.h"
 #include "internal.h"
 #include "lighttrace.h"
+#include "sppm.h"
 
 struct bling_ctx {
   int device = 0;
@@ -32,6 +33,7 @@ struct bling_ctx {
   cudaEvent_t ev_out[3] = {nullptr, nullptr, nullptr};
   bgpu::IntegratorWorkspace ws;
   bgpu::LightWorkspace lt_ws;  // photon slots of the light tracer (made on first use)
+  bgpu::SppmWorkspace sp_ws;   // hit points, hash and photon slots of SPPM (made on first use)
 };
 
 struct bling_scene {
@@ -56,6 +58,9 @@ struct bling_film {
   float* d_film = nullptr;  // width*height*4: the samples added since the last fold
   double* d_acc = nullptr;  // BLING_FILM_FP64: width*height*4 totals of the folded passes
   float* d_splat = nullptr; // width*height*3 XYZ splats of light passes (made on first use)
+  // SPPM pixel statistics of the sample extent: r2, N (floats), M (uint32), made by the first pass
+  void* d_sppm = nullptr;
+  int64_t sppm_pixels = 0;
 };
 
 struct bling_batch {

@@ -712,6 +712,67 @@ static __device__ BLING_OUTLINE BsdfSample sampleBsdf(const Bsdf& b, V3 woW, flo
   if (Adj) out.f = sScale(out.f, adjScale);
   return out;
 }
+// bsdfHasNonSpecular (Reflection.hs:246-249)
+__device__ __forceinline__ bool bsdfHasNonSpecular(const Bsdf& b) {
+  for (int i = 0; i < b.n; i++)
+    if (!(b.c[i].type & T_SPEC)) return true;
+  return false;
+}
+// sampleBsdf'' False flags (Reflection.hs:278-316) over the BxDFs whose type
+// lies within `flags` (bxdfMatches, Reflection.hs:119-121, 185-186)
+static __device__ BsdfSample sampleBsdfFlags(const Bsdf& b, V3 woW, int flags, float uComp,
+                                             float u1, float u2) {
+  BsdfSample out;
+  out.type = T_REFL | T_DIFF;
+  out.pdf = 0;
+  out.f = sConst(0);
+  out.wi = V3{0, 1, 0};
+  int idx[2], cntm = 0;
+  for (int i = 0; i < b.n; i++)
+    if ((b.c[i].type & flags) == b.c[i].type) idx[cntm++] = i;
+  if (cntm == 0) return out;
+  V3 wo = worldToLocal(b.cs, woW);
+  float cntf = (float)cntm;
+  float invCnt = 1.0f / cntf;
+  int sNum = max(0, min(cntm - 1, (int)floorf(uComp * cntf)));
+  const BxDF& bx = b.c[idx[sNum]];
+  Spec fSample;
+  V3 wi;
+  float pdfp;
+  bxSample<false>(bx, wo, u1, u2, fSample, wi, pdfp);
+  V3 wiW = localToWorld(b.cs, wi);
+  float sideTest = dot(wiW, b.ng) / dot(woW, b.ng);
+  if (pdfp == 0 || sideTest == 0) return out;
+  bool wantTrans = sideTest < 0;
+  bool ok = wantTrans ? (bx.type & T_TRANS) != 0 : (bx.type & T_REFL) != 0;
+  if (!ok) return out;
+  out.type = bx.type;
+  out.wi = wiW;
+  if (bx.type & T_SPEC) {
+    out.pdf = pdfp * invCnt;
+    out.f = sScale(fSample, cntf);
+    return out;
+  }
+  if (cntm == 1) {
+    out.pdf = pdfp;
+    out.f = fSample;
+    return out;
+  }
+  float others = 0.0f;
+  for (int j = 0; j < cntm; j++)
+    if (j != sNum) others = others + bxPdf(b.c[idx[j]], wo, wi);
+  float pdf = (pdfp + others) * invCnt;
+  Spec fOthers = sConst(0);
+  for (int j = 0; j < cntm; j++) {
+    if (j == sNum) continue;
+    const BxDF& o = b.c[idx[j]];
+    bool ok2 = wantTrans ? (o.type & T_TRANS) != 0 : (o.type & T_REFL) != 0;
+    if (ok2) fOthers = fOthers + bxEval(o, wi, wo);
+  }
+  out.pdf = pdf;
+  out.f = sScale(sScale(fSample, pdfp) + fOthers, 1.0f / pdf);
+  return out;
+}
 // evalBsdf Adj (Reflection.hs:318-332)
 template <bool Adj = false>
 static __device__ BLING_OUTLINE Spec evalBsdf(const Bsdf& b, V3 woW, V3 wiW) {

@@ -215,7 +215,7 @@ typedef struct bling_stats {
   uint64_t bvh_nodes;
   uint64_t bvh_leaf_prims;
   uint64_t device_bytes;
-  uint64_t light_splats;    /* camera connections of light passes added to the splat image */
+  uint64_t light_splats;    /* splats of light and SPPM passes added to the splat image */
 } bling_stats;
 
 /* ---- context ---- */
@@ -299,6 +299,33 @@ int bling_render_pass_camera(bling_scene* scene, bling_film* film,
                              uint64_t pass);
 
 int bling_scene_stats(bling_scene* scene, bling_stats* out);
+
+/* ---- stochastic progressive photon mapping ----
+ * replaces the reference's SPPM renderer (Renderer/SPPM.hs:392-480).  One
+ * pass: one Random-sampler camera sample per pixel of the sample extent
+ * records hit points at non-specular surfaces (following specular
+ * reflection and transmission both) and adds the emission it sees to the
+ * film; a spatial hash over the hit points; ceil(sqrt photons)^2 photons
+ * splat hpF * f * li / (|wi.ng| r^2 pi) into the splat image for every hit
+ * point within its radius; each pixel's radius shrinks by alpha
+ * (statsUpdate).  The film keeps the per-pixel radii between passes
+ * (bling_film_clear resets them).  After n passes the reference's splat
+ * weight is 1 / (n * ceil(sqrt photons)^2) (SPPM.hs:418). */
+typedef struct bling_sppm_params {
+  int64_t photons;        /* photons per pass (mkSPPM n) */
+  int32_t max_depth;      /* camera path vertices (mkSPPM md), 1..24 */
+  float radius;           /* initial search radius (mkSPPM r) */
+  float alpha;            /* radius reduction (mkSPPM alpha), in (0, 1) */
+  int32_t filter_kind;    /* the job's pixel filter, for the camera samples */
+  float filter_params[4];
+  uint64_t seed;
+} bling_sppm_params;
+int bling_sppm_pass(bling_scene* scene, bling_film* film, const bling_sppm_params* params,
+                    uint64_t pass);
+/* copies the per-pixel squared radii of the sample extent (row-major over
+ * imageWindow', Image.hs:170-176) into r2 (capacity floats); *count gets the
+ * number of pixels, 0 before the first SPPM pass */
+int bling_film_read_sppm_radii(bling_film* film, float* r2, int64_t capacity, int64_t* count);
 
 /* ---- light tracer ----
  * replaces the reference's LightTracer renderer (Renderer/LightTracer.hs:

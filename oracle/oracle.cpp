@@ -1792,6 +1792,15 @@ static Spec pathLi(const orc_scene& S, const Sampler& smp, Ray ray, int md, int 
   }
 }
 
+// hash (SPPM.hs:291-293) and the bucket of a cell: abs (hash) `rem` cnt, clamped
+static long long cellBucketOf(long long x, long long y, long long z, long long cnt) {
+  long long h = (long long)((unsigned long long)x * 73856093ull ^ (unsigned long long)y * 19349663ull ^
+                            (unsigned long long)z * 83492791ull);
+  h = h < 0 ? -h : h;
+  long long r = h % cnt;
+  return r < 0 ? 0 : (r > cnt - 1 ? cnt - 1 : r);
+}
+
 // ---------------------------------------------------------------- light tracer
 // Renderer/LightTracer.hs.  A photon's random numbers come from the shared
 // generator keyed by (seed, pass, photon): dimension 0 picks the light, 1-2
@@ -2418,11 +2427,18 @@ int orc_sample_li(const orc_scene* s, const bling_render_params* p, uint64_t pas
   return BLING_OK;
 }
 
-int orc_render_pass(const orc_scene* S, const bling_render_params* p, uint64_t pass, float* film,
-                    int row_begin, int row_end, int nth, uint64_t* path_samples,
-                    uint64_t* rays_closest, uint64_t* rays_any) {
-  if (p->strata_x <= 0 || p->strata_y <= 0 || p->width <= 0 || p->height <= 0)
-    return BLING_ERR_INVALID_ARG;
+}  // extern "C"
+
+// prender's tiles (Rendering.hs:111-150): every pixel of the sample extent
+// gets its samples, each added to its tile's image (mkImageTile, addSample),
+// and the tiles are added to the film in order (addTile).  sampleFn(smp, ix,
+// iy, tile, sx, sy, C) returns one sample's radiance.
+template <class SampleFn>
+static int renderTiles(const orc_scene* S, const bling_render_params* p, uint64_t pass, float* film,
+                       int row_begin, int row_end, int nth, int ntiles_hint, SampleFn sampleFn,
+                       uint64_t* path_samples, uint64_t* rays_closest, uint64_t* rays_any) {
+  (void)S;
+  (void)ntiles_hint;
   int x0, x1, y0, y1;
   sampleExtent(p, x0, x1, y0, y1);
   float fw, fh;
@@ -2456,20 +2472,19 @@ int orc_render_pass(const orc_scene* S, const bling_render_params* p, uint64_t p
     th[ti] = h;
     tox[ti] = px0;
     toy[ti] = py0;
-    if (w <= 0 || h <= 0) return;
-    timgs[ti].assign((size_t)w * h * 4, 0.0f);
-    FilmImg img{w, h, px0, py0, timgs[ti].data()};
     Counters C;
     uint64_t ps = 0;
+    if (w > 0 && h > 0) timgs[ti].assign((size_t)w * h * 4, 0.0f);
+    FilmImg img{w, h, px0, py0, timgs[ti].data()};
     for (int iy = T.ys; iy <= T.ye; iy++) {
       if (iy < rb || iy >= re) continue;
       for (int ix = T.xs; ix <= T.xe; ix++)
         for (int n = 0; n < nsp; n++) {
           Sampler smp = mkSampler(p, pass, ix, iy, n);
           float sx, sy;
-          Spec L = traceSample(S, p, smp, ix, iy, sx, sy, C);
+          Spec L = sampleFn(smp, ix, iy, ti, sx, sy, C);
           ps++;
-          addSample(img, tblv, fw, fh, sx, sy, L);  // NaN/Inf samples are skipped
+          if (w > 0 && h > 0) addSample(img, tblv, fw, fh, sx, sy, L);  // NaN/Inf samples are skipped
         }
     }
     nps += ps;
@@ -2491,6 +2506,335 @@ int orc_render_pass(const orc_scene* S, const bling_render_params* p, uint64_t p
   if (path_samples) *path_samples = nps;
   if (rays_closest) *rays_closest = ncl;
   if (rays_any) *rays_any = nany;
+  return BLING_OK;
+}
+
+static size_t extentTiles(const bling_render_params* p) {
+  int x0, x1, y0, y1;
+  sampleExtent(p, x0, x1, y0, y1);
+  return (size_t)((x1 - x0) / 16 + 1) * (size_t)((y1 - y0) / 16 + 1);
+}
+
+extern "C" {
+
+int orc_render_pass(const orc_scene* S, const bling_render_params* p, uint64_t pass, float* film,
+                    int row_begin, int row_end, int nth, uint64_t* path_samples,
+                    uint64_t* rays_closest, uint64_t* rays_any) {
+  if (p->strata_x <= 0 || p->strata_y <= 0 || p->width <= 0 || p->height <= 0)
+    return BLING_ERR_INVALID_ARG;
+  return renderTiles(
+      S, p, pass, film, row_begin, row_end, nth, 0,
+      [&](const Sampler& smp, int ix, int iy, size_t, float& sx, float& sy, Counters& C) {
+        return traceSample(S, p, smp, ix, iy, sx, sy, C);
+      },
+      path_samples, rays_closest, rays_any);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- SPPM
+// Renderer/SPPM.hs.  The camera pass's random numbers: the Random sampler's
+// pixel and lens dimensions keyed by (seed, 2 pass, pixel), then 3 per node
+// of the sample's specular tree, by heap index (root 1, children 2k, 2k+1).
+// The photon pass: a stratified sampler with ceil(sqrt n)^2 samples over one
+// pixel keyed by (seed, 2 pass + 1, 0, 0), 7 stratified 1D and 5 2D
+// dimensions (SPPM.hs:471-474).
+static const uint32_t DIM_CAM_TREE = 3u << 20;
+
+// bsdfHasNonSpecular (Reflection.hs:246-249)
+static bool bsdfHasNonSpecular(const Bsdf& b) {
+  for (int i = 0; i < b.n; i++)
+    if (!(b.c[i].type & T_SPEC)) return true;
+  return false;
+}
+
+// sampleBsdf'' False flags (Reflection.hs:278-316) over the BxDFs whose type
+// lies within flags (bxdfMatches)
+static BsdfSample sampleBsdfFlags(const Bsdf& b, V woW, int flags, float uComp, float u1, float u2) {
+  BsdfSample empty{T_REFL | T_DIFF, 0, BLACK, V{0, 1, 0}};
+  int idx[2], cntm = 0;
+  for (int i = 0; i < b.n; i++)
+    if ((b.c[i].type & flags) == b.c[i].type) idx[cntm++] = i;
+  if (cntm == 0) return empty;
+  V wo = worldToLocal(b.cs, woW);
+  float cntf = (float)cntm;
+  float invCnt = 1.0f / cntf;
+  int sNum = std::max(0, std::min(cntm - 1, (int)floorf(uComp * cntf)));
+  const BxDF& bx = b.c[idx[sNum]];
+  Spec fSample;
+  V wi;
+  float pdfp;
+  bxSample(bx, wo, u1, u2, fSample, wi, pdfp);
+  V wiW = localToWorld(b.cs, wi);
+  float sideTest = dot(wiW, b.ng) / dot(woW, b.ng);
+  if (pdfp == 0 || sideTest == 0) return empty;
+  bool wantTrans = sideTest < 0;
+  auto flt = [&](const BxDF& x) { return wantTrans ? (x.type & T_TRANS) != 0 : (x.type & T_REFL) != 0; };
+  if (!flt(bx)) return empty;
+  if (bx.type & T_SPEC) return BsdfSample{bx.type, pdfp * invCnt, sScale(fSample, cntf), wiW};
+  if (cntm == 1) return BsdfSample{bx.type, pdfp, fSample, wiW};
+  float others = 0.0f;
+  for (int j = 0; j < cntm; j++)
+    if (j != sNum) others = others + bxPdf(b.c[idx[j]], wo, wi);
+  float pdf = (pdfp + others) * invCnt;
+  Spec fOthers = BLACK;
+  for (int j = 0; j < cntm; j++)
+    if (j != sNum && flt(b.c[idx[j]])) fOthers = fOthers + bxEval(b.c[idx[j]], wi, wo);
+  return BsdfSample{bx.type, pdf, sScale(sScale(fSample, pdfp) + fOthers, 1.0f / pdf), wiW};
+}
+
+struct HitPoint {  // HitPoint (SPPM.hs:58-64)
+  Bsdf bsdf;
+  float px, py, r2;
+  V w;
+  Spec F;
+};
+
+struct PixelStats {  // PixelStats (SPPM.hs:226-238) over the sample extent
+  int x0, x1, y0, y1;
+  float* r2;
+  float* n;
+  uint32_t* m;
+  int64_t count;
+  // sIdx (SPPM.hs:248-253); positions outside the arrays give -1
+  int64_t idx(float px, float py) const {
+    int w = x1 - x0, h = y1 - y0;
+    int ix = std::min(w, (int)px), iy = std::min(h, (int)py);  // truncate
+    int64_t i = (int64_t)w * (iy - y0) + (ix - x0);
+    return (i >= 0 && i < count) ? i : -1;
+  }
+};
+
+struct CamTree {
+  const orc_scene* S;
+  const PixelStats* st;
+  uint64_t key;
+  uint32_t n;
+  int md;
+  float sx, sy;
+  std::vector<HitPoint>* hps;
+  Counters* C;
+
+  // traceCam (SPPM.hs:101-131) of the node with heap index k
+  Spec trace(const Ray& ray, int depth, const Spec& t, uint32_t k) {
+    if (depth == md) return BLACK;
+    Isect it;
+    C->closest++;
+    if (!sceneIntersect(*S, ray, it)) {
+      Spec esc = BLACK;  // escaped (SPPM.hs:74-75)
+      for (const Light& l : S->lights) esc = esc + lightLe(l, ray);
+      return BLACK + t * esc;
+    }
+    V wo = -ray.d;
+    const Prim& pr = S->prims[it.prim];
+    int mat = pr.is_shape ? S->shapes[pr.index].material : S->meshes[pr.index].material;
+    DG dgs = shadingGeometry(*S, pr, it.dg);
+    Bsdf bsdf = materialBsdf(S->mats[mat], it.dg, dgs);
+    Spec ls = t * intLe(*S, it, ray.d);
+    if (bsdfHasNonSpecular(bsdf)) {
+      int64_t si = st->idx(sx, sy);
+      hps->push_back(HitPoint{bsdf, sx, sy, si >= 0 ? st->r2[si] : 0.0f, wo, t});
+    }
+    Spec lr = follow(T_REFL, it, bsdf, wo, t, depth, k);
+    Spec lt = follow(T_TRANS, it, bsdf, wo, t, depth, k);
+    return BLACK + lr + lt + ls;
+  }
+  // followCam (SPPM.hs:83-99)
+  Spec follow(int prop, const Isect& it, const Bsdf& bsdf, V wo, const Spec& t, int depth,
+              uint32_t k) {
+    uint32_t k2 = 2 * k + (prop == T_TRANS ? 1u : 0u);
+    uint32_t dim = DIM_CAM_TREE + 3 * k2;
+    float uc = randF(key, n, dim), u1 = randF(key, n, dim + 1), u2 = randF(key, n, dim + 2);
+    BsdfSample bs = sampleBsdfFlags(bsdf, wo, prop | T_SPEC, uc, u1, u2);
+    if (bs.pdf == 0 || isBlack(bs.f)) return BLACK;
+    return trace(Ray{bsdf.p, bs.wi, it.eps, INF}, depth + 1, bs.f * t, k2);
+  }
+};
+
+extern "C" {
+
+int orc_sppm_pass(const orc_scene* S, const bling_sppm_params* sp, int32_t width, int32_t height,
+                  uint64_t pass, float* film, float* splat_xyz, float* r2, float* nacc, uint32_t* m,
+                  int64_t stat_count, int nth, uint64_t stats[4]) {
+  if (width <= 0 || height <= 0 || sp->max_depth < 1 || sp->max_depth > 24) return BLING_ERR_INVALID_ARG;
+  bling_render_params rp;
+  memset(&rp, 0, sizeof rp);
+  rp.width = width;
+  rp.height = height;
+  rp.strata_x = rp.strata_y = 1;  // mkRandomSampler 1 (SPPM.hs:150)
+  rp.max_depth = sp->max_depth;
+  rp.rr_depth = 7;
+  rp.filter_kind = sp->filter_kind;
+  memcpy(rp.filter_params, sp->filter_params, sizeof rp.filter_params);
+  rp.seed = sp->seed;
+  rp.sampler_kind = BLING_SAMPLER_RANDOM;
+  PixelStats st;
+  sampleExtent(&rp, st.x0, st.x1, st.y0, st.y1);
+  st.count = (int64_t)(st.x1 - st.x0 + 1) * (st.y1 - st.y0 + 1);
+  if (stat_count != st.count) return BLING_ERR_BOUNDS;
+  st.r2 = r2;
+  st.n = nacc;
+  st.m = m;
+  // ---- camera pass: hit points per tile, in tile order (mkHitPoints, SPPM.hs:136-164)
+  std::vector<std::vector<HitPoint>> tile_hps(extentTiles(&rp));
+  uint64_t ncam = 0, ncl = 0, nany = 0;
+  int rc = renderTiles(
+      S, &rp, 2 * pass, film, 0, 0, nth, 0,
+      [&](const Sampler& smp, int ix, int iy, size_t tile, float& sx, float& sy, Counters& C) {
+        float ox = randF(smp.key, smp.n, DIM_PIX_U), oy = randF(smp.key, smp.n, DIM_PIX_V);
+        float lu = randF(smp.key, smp.n, DIM_LENS_U), lv = randF(smp.key, smp.n, DIM_LENS_V);
+        sx = (float)ix + ox;
+        sy = (float)iy + oy;
+        Ray ray = cameraRay(S, sx, sy, lu, lv);
+        CamTree tr{S, &st, smp.key, smp.n, sp->max_depth, sx, sy, &tile_hps[tile], &C};
+        return tr.trace(ray, 0, WHITE, 1);
+      },
+      &ncam, &ncl, &nany);
+  if (rc) return rc;
+  std::vector<HitPoint> hps;
+  for (auto& t : tile_hps) hps.insert(hps.end(), t.begin(), t.end());
+  uint64_t st_out[4] = {ncl, 0, 0, 0};
+  // ---- spatial hash (mkHash, SPPM.hs:283-323); the buckets hold hit-point indices
+  int sn = std::max(1, (int)ceilf(sqrtf((float)sp->photons)));
+  int64_t nphot = (int64_t)sn * sn;
+  long long cnt = (long long)hps.size();
+  if (cnt > 0 && !S->lights.empty()) {
+    float r2m = 0;
+    for (const HitPoint& h : hps) r2m = hmax(h.r2, r2m);
+    float r = sqrtf(r2m);
+    V lo{INF, INF, INF};
+    for (const HitPoint& h : hps) {
+      V a = h.bsdf.p - V{r, r, r};
+      lo = V{hmin(lo.x, a.x), hmin(lo.y, a.y), hmin(lo.z, a.z)};
+    }
+    float invSize = 1.0f / (2.0f * r);
+    std::vector<std::vector<int>> buckets((size_t)cnt);
+    for (long long i = 0; i < cnt; i++) {
+      const HitPoint& h = hps[i];
+      if (h.r2 == 0) continue;
+      float rp = sqrtf(h.r2);
+      V p = h.bsdf.p;
+      float f0[3] = {invSize * fabsf((p.x - rp) - lo.x), invSize * fabsf((p.y - rp) - lo.y),
+                     invSize * fabsf((p.z - rp) - lo.z)};
+      float f1[3] = {invSize * fabsf((p.x + rp) - lo.x), invSize * fabsf((p.y + rp) - lo.y),
+                     invSize * fabsf((p.z + rp) - lo.z)};
+      if (!(std::max(f1[0], std::max(f1[1], f1[2])) < 9.2e18f &&
+            std::max(f0[0], std::max(f0[1], f0[2])) < 9.2e18f))
+        continue;
+      for (long long x = (long long)f0[0]; x <= (long long)f1[0]; x++)
+        for (long long y = (long long)f0[1]; y <= (long long)f1[1]; y++)
+          for (long long z = (long long)f0[2]; z <= (long long)f1[2]; z++)
+            buckets[(size_t)cellBucketOf(x, y, z, cnt)].push_back((int)i);
+    }
+    // ---- photon pass (tracePhoton/followPhoton, SPPM.hs:172-224)
+    uint64_t key = pixelKey(sp->seed, 2 * pass + 1, 0, 0);
+    V wlo{INF, INF, INF}, whi{-INF, -INF, -INF};
+    for (size_t i = 0; i < S->prims.size(); i++) {
+      AabbF b = primBounds(*S, (int)i);
+      wlo = V{hmin(wlo.x, b.lo.x), hmin(wlo.y, b.lo.y), hmin(wlo.z, b.lo.z)};
+      whi = V{hmax(whi.x, b.hi.x), hmax(whi.y, b.hi.y), hmax(whi.z, b.hi.z)};
+    }
+    V wc = wlo + (whi - wlo) * V{0.5f, 0.5f, 0.5f};
+    float wr = len(whi - wc);
+    int T = nthreadsOf(nth);
+    if ((int64_t)T > nphot) T = (int)std::max<int64_t>(1, nphot);
+    std::vector<std::vector<float>> imgs(T);
+    std::vector<std::vector<uint32_t>> ms(T);
+    std::vector<uint64_t> ncls(T), nspl(T), nnf(T);
+    std::vector<std::thread> th;
+    int lc = (int)S->lights.size();
+    for (int t = 0; t < T; t++) {
+      th.emplace_back([&, t] {
+        imgs[t].assign((size_t)width * height * 3, 0.0f);
+        ms[t].assign((size_t)st.count, 0u);
+        int64_t b = nphot * t / T, e = nphot * (t + 1) / T;
+        for (int64_t j = b; j < e; j++) {
+          Sampler smp{key, (uint32_t)j, sn, sn, 7, 5};
+          float ul = rnd1(smp, 0), uo1, uo2, ud1, ud2;
+          rnd2(smp, 0, uo1, uo2);
+          rnd2(smp, 1, ud1, ud2);
+          int ln = lc == 1 ? 0 : std::min((int)floorf(ul * (float)lc), lc - 1);
+          Spec le;
+          Ray ray;
+          V nl;
+          float pdf;
+          lightEmit(*S, S->lights[ln], wc, wr, uo1, uo2, ud1, ud2, le, ray, nl, pdf);
+          if (lc != 1) pdf = pdf / (float)lc;
+          Spec li = sScale(le, absDot(nl, -ray.d) / pdf);
+          if (!(pdf > 0 && !isBlack(li))) continue;
+          for (int d = 0;; d++) {
+            Isect it;
+            ncls[t]++;
+            if (!sceneIntersect(*S, ray, it)) break;
+            V wi = -ray.d;
+            const Prim& pr = S->prims[it.prim];
+            int mat = pr.is_shape ? S->shapes[pr.index].material : S->meshes[pr.index].material;
+            DG dgs = shadingGeometry(*S, pr, it.dg);
+            Bsdf bsdf = materialBsdf(S->mats[mat], it.dg, dgs);
+            V p = bsdf.p;
+            if (bsdfHasNonSpecular(bsdf)) {  // hashLookup (SPPM.hs:295-302)
+              float cx = fabsf((p.x - lo.x) * invSize), cy = fabsf((p.y - lo.y) * invSize),
+                    cz = fabsf((p.z - lo.z) * invSize);
+              if (cx < 9.2e18f && cy < 9.2e18f && cz < 9.2e18f) {
+                long long bi = cellBucketOf((long long)cx, (long long)cy, (long long)cz, cnt);
+                for (int hi : buckets[(size_t)bi]) {
+                  const HitPoint& h = hps[hi];
+                  if (!(sqLen(h.bsdf.p - p) <= h.r2)) continue;
+                  Spec f = evalBsdf(h.bsdf, h.w, wi);
+                  Spec l = sScale(h.F * f * li, 1.0f / (absDot(wi, bsdf.ng) * h.r2 * PI));
+                  if (h.px >= 0.0f && h.px < (float)width && h.py >= 0.0f && h.py < (float)height) {
+                    if (sNaN(l) || sInf(l)) {
+                      nnf[t]++;
+                    } else {
+                      float x, y, z;
+                      spectrumToXYZ(l, x, y, z);
+                      float* o = imgs[t].data() + 3 * ((size_t)floorf(h.py) * width + (size_t)floorf(h.px));
+                      o[0] = o[0] + x;
+                      o[1] = o[1] + y;
+                      o[2] = o[2] + z;
+                      nspl[t]++;
+                    }
+                  }
+                  int64_t si = st.idx(h.px, h.py);
+                  if (si >= 0) ms[t][si]++;
+                }
+              }
+            }
+            float ubc = rnd1(smp, 1 + d * 2), u1, u2;
+            rnd2(smp, 2 + d, u1, u2);
+            BsdfSample bs = sampleBsdf(bsdf, wi, ubc, u1, u2, true);
+            float pcont = d > 7 ? 0.8f : 1.0f;
+            Spec li2 = sScale(bs.f * li, 1.0f / pcont);
+            if (bs.pdf == 0 || isBlack(li2)) break;
+            if (rnd1(smp, 2 + d * 2) > pcont) break;
+            ray = Ray{p, bs.wi, it.eps, INF};
+            li = li2;
+          }
+        }
+      });
+    }
+    for (auto& x : th) x.join();
+    for (int t = 0; t < T; t++) {
+      for (size_t k = 0; k < imgs[t].size(); k++) splat_xyz[k] = splat_xyz[k] + imgs[t][k];
+      for (int64_t k = 0; k < st.count; k++) m[k] += ms[t][k];
+      st_out[0] += ncls[t];
+      st_out[2] += nspl[t];
+      st_out[3] += nnf[t];
+    }
+  }
+  st_out[1] = (uint64_t)hps.size();
+  // ---- statsUpdate (SPPM.hs:258-279)
+  float a = sp->alpha;
+  for (int64_t i = 0; i < st.count; i++) {
+    uint32_t mm = m[i];
+    if (mm == 0) continue;
+    float n2 = nacc[i] + a * (float)mm;
+    float ratio = n2 / (nacc[i] + (float)mm);
+    r2[i] = r2[i] * ratio;
+    nacc[i] = n2;
+    m[i] = 0;
+  }
+  if (stats) memcpy(stats, st_out, sizeof st_out);
   return BLING_OK;
 }
 

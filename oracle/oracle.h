@@ -55,6 +55,15 @@ int orc_light_pass(const orc_scene* s, int32_t width, int32_t height, uint64_t s
                    int32_t max_depth, int64_t first, int64_t count, float* splat_xyz, int nthreads,
                    uint64_t stats[4]);
 
+/* One SPPM pass (Renderer/SPPM.hs:392-480): camera samples of the Random
+ * sampler added to film (w,X,Y,Z), hit points, spatial hash, photon splats
+ * into splat_xyz and the per-pixel statistics r2/n/m (stat_count entries over
+ * the sample extent, updated in place).  stats: closest-hit queries, hit
+ * points, splats, non-finite splats dropped. */
+int orc_sppm_pass(const orc_scene* s, const bling_sppm_params* params, int32_t width, int32_t height,
+                  uint64_t pass, float* film_wxyz, float* splat_xyz, float* r2, float* n, uint32_t* m,
+                  int64_t stat_count, int nthreads, uint64_t stats[4]);
+
 /* restated helpers, for known-answer tests */
 void orc_rgb_to_spectrum(int illum, float r, float g, float b, float out[16]);
 void orc_spectrum_to_xyz(const float s[16], float xyz[3]);

@@ -41,6 +41,10 @@ def lib():
         L.orc_light_pass.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64,
                                      C.c_int32, C.c_int64, C.c_int64, P(C.c_float), C.c_int,
                                      P(C.c_uint64)]
+        L.orc_sppm_pass.argtypes = [C.c_void_p, P(abi.SppmParams), C.c_int32, C.c_int32,
+                                    C.c_uint64, P(C.c_float), P(C.c_float), P(C.c_float),
+                                    P(C.c_float), P(C.c_uint32), C.c_int64, C.c_int,
+                                    P(C.c_uint64)]
         L.orc_sample_li.argtypes = [C.c_void_p, P(abi.RenderParams), C.c_uint64, C.c_int, C.c_int,
                                     C.c_int, P(C.c_float), P(C.c_float), P(C.c_float)]
         L.orc_rgb_to_spectrum.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, P(C.c_float)]
@@ -130,12 +134,55 @@ class OracleScene:
         return splats, {"rays_closest": st[0], "rays_any": st[1], "splats": st[2],
                         "nonfinite": st[3]}
 
+    def sppm_state(self, params, width, height):
+        """fresh per-pixel SPPM statistics: radius^2 = r^2, N = 0, M = 0 over
+        the sample extent (imageWindow')"""
+        from bling_gb300.scene import render_params
+        rp = render_params(width, height, (1, 1), filter_kind=params.filter_kind,
+                           filter_params=tuple(params.filter_params))
+        x0, x1, y0, y1 = _extent(rp)
+        n = (x1 - x0 + 1) * (y1 - y0 + 1)
+        return {"r2": np.full(n, np.float32(params.radius) * np.float32(params.radius), np.float32),
+                "n": np.zeros(n, np.float32), "m": np.zeros(n, np.uint32)}
+
+    def sppm_pass(self, params, width, height, pass_index=0, film=None, splats=None, state=None,
+                  nthreads=0):
+        """one SPPM pass; returns (film, splats, state, stats)"""
+        if film is None:
+            film = np.zeros((height, width, 4), np.float32)
+        if splats is None:
+            splats = np.zeros((height, width, 3), np.float32)
+        if state is None:
+            state = self.sppm_state(params, width, height)
+        st = (C.c_uint64 * 4)()
+        rc = lib().orc_sppm_pass(self.h, C.byref(params), width, height, pass_index, fp(film),
+                                 fp(splats), fp(state["r2"]), fp(state["n"]),
+                                 state["m"].ctypes.data_as(C.POINTER(C.c_uint32)),
+                                 len(state["r2"]), nthreads, st)
+        if rc != 0:
+            raise ValueError(f"orc_sppm_pass failed: {rc}")
+        return film, splats, state, {"rays_closest": st[0], "hitpoints": st[1], "splats": st[2],
+                                     "nonfinite": st[3]}
+
     def sample_li(self, params, pass_index, px, py, n):
         xyz = np.zeros(3, np.float32)
         ras = np.zeros(2, np.float32)
         spec = np.zeros(16, np.float32)
         lib().orc_sample_li(self.h, C.byref(params), pass_index, px, py, n, fp(xyz), fp(ras), fp(spec))
         return xyz, ras, spec
+
+
+def _extent(p):
+    """imageWindow' (Image.hs:170-176) of render parameters"""
+    import math
+    if p.filter_kind == abi.FILTER_BOX:
+        fw = fh = 0.5
+    else:
+        fw, fh = float(np.float32(p.filter_params[0])), float(np.float32(p.filter_params[1]))
+    return (math.floor(np.float32(0.5) - np.float32(fw)),
+            math.floor(np.float32(0.5) + np.float32(p.width) + np.float32(fw)),
+            math.floor(np.float32(0.5) - np.float32(fh)),
+            math.floor(np.float32(0.5) + np.float32(p.height) + np.float32(fh)))
 
 
 def resolve(film):
