@@ -165,10 +165,16 @@ __global__ void k_sp_reset(unsigned long long* counters, int next) {
   if (threadIdx.x == 1) counters[S_NEXT_TRACE] = 0;
 }
 
+// a queue's node count: appends past the capacity were dropped (and counted
+// as an overflow, after which the chunk runs again)
+__device__ __forceinline__ int64_t nodeCount(const unsigned long long* counters, int q, size_t cap) {
+  return (int64_t)min(counters[S_NODES0 + q], (unsigned long long)cap);
+}
+
 template <bool WIDE>
-__global__ void __launch_bounds__(128, 10) k_sp_camtrace(DevAccel A, CamNodes nb, int in,
+__global__ void __launch_bounds__(128, 10) k_sp_camtrace(DevAccel A, CamNodes nb, int in, size_t cap,
                                                          unsigned long long* __restrict__ counters) {
-  int64_t n = (int64_t)counters[S_NODES0 + in];
+  int64_t n = nodeCount(counters, in, cap);
   traceWarpPersistent<false, WIDE, false>(
       A, n, counters + S_NEXT_TRACE, [&](int64_t q) { return loadRay7(nb.ray, (int)q); },
       [&](int64_t q, const RayQueryResult& res) {
@@ -184,7 +190,7 @@ __global__ void __launch_bounds__(128, 4) k_sp_camshade(DevAccel A, DevShading S
                                                         unsigned long long* __restrict__ counters) {
   const CamNodes& ni = cs.nb[in];
   const CamNodes& no = cs.nb[1 - in];
-  int64_t n = (int64_t)counters[S_NODES0 + in];
+  int64_t n = nodeCount(counters, in, cs.NC);
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
@@ -715,9 +721,11 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
       k_sp_reset<<<1, 32, 0, stream>>>(counters, S_NODES0 + (1 - in));
       unsigned nb = (unsigned)std::max<size_t>(1, (ws.cam_nodes + block - 1) / block);
       if (wide)
-        k_sp_camtrace<true><<<std::min(g_trace, nb), block, 0, stream>>>(A, cs.nb[in], in, counters);
+        k_sp_camtrace<true><<<std::min(g_trace, nb), block, 0, stream>>>(A, cs.nb[in], in, cs.NC,
+                                                                          counters);
       else
-        k_sp_camtrace<false><<<std::min(g_trace, nb), block, 0, stream>>>(A, cs.nb[in], in, counters);
+        k_sp_camtrace<false><<<std::min(g_trace, nb), block, 0, stream>>>(A, cs.nb[in], in, cs.NC,
+                                                                           counters);
       k_sp_camshade<<<std::min(g_shade, nb), block, 0, stream>>>(A, S, P, cs, hp, px.r2, px.count, in, d,
                                                                a.max_depth, counters);
       RET_CUDA(cudaGetLastError());
