@@ -933,8 +933,8 @@ int bling_film_read_sppm_radii(bling_film* f, float* r2, int64_t capacity, int64
   bling_ctx* c = f->ctx;
   std::lock_guard<std::mutex> g(c->mu);
   *count = f->d_sppm ? f->sppm_pixels : 0;
-  if (!f->d_sppm) return BLING_OK;
-  if (!r2 || capacity < f->sppm_pixels)
+  if (!f->d_sppm || !r2) return BLING_OK;  // r2 = NULL asks for the count
+  if (capacity < f->sppm_pixels)
     return set_err(c, BLING_ERR_BOUNDS, "radius buffer holds %lld of %lld pixels",
                    (long long)capacity, (long long)f->sppm_pixels);
   CK(c, cudaSetDevice(c->device));

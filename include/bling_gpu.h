@@ -324,7 +324,8 @@ int bling_sppm_pass(bling_scene* scene, bling_film* film, const bling_sppm_param
                     uint64_t pass);
 /* copies the per-pixel squared radii of the sample extent (row-major over
  * imageWindow', Image.hs:170-176) into r2 (capacity floats); *count gets the
- * number of pixels, 0 before the first SPPM pass */
+ * number of pixels, 0 before the first SPPM pass.  r2 = NULL only asks for
+ * the count. */
 int bling_film_read_sppm_radii(bling_film* film, float* r2, int64_t capacity, int64_t* count);
 
 /* ---- light tracer ----
