@@ -358,6 +358,73 @@ def measure_light(ctx, stream, args):
     return out
 
 
+def measure_sppm(ctx, stream, args):
+    """SPPM on the Cornell room (secondary line): one pass = a camera pass
+    (one sample per pixel, specular trees to depth 5), the hit-point hash and
+    `--sppm-photons` photons; passes/s, photons/s and Mrays/s, CUDA events on
+    the stream; the oracle on one bounded pass beside it."""
+    import torch
+
+    from bling_gb300 import abi
+    from bling_gb300 import scene as S
+    W = H = 256
+    n = args.sppm_photons
+    sc = S.cornell_room(W, H)
+    sp = abi.sppm_params(n, max_depth=5, radius=0.01, alpha=0.7, seed=1)
+    g = ctx.scene(sc)
+    film = ctx.film(W, H)
+    g.sppm_pass(film, sp, 0)  # warm-up pass
+    s0 = g.stats()
+    times = []
+    passes = 3
+    for k in range(passes):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record(stream)
+        g.sppm_pass(film, sp, k + 1)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+        times.append(ev[0].elapsed_time(ev[1]) / 1e3)
+    s1 = g.stats()
+    tot = sum(times)
+    sn = int(np.ceil(np.sqrt(np.float32(n))))
+    rays = s1["rays_closest"] - s0["rays_closest"]
+    out = {"workload": f"cornell_{W}x{H}_{sn * sn}_photons_depth5_r0.01",
+           "passes_per_s": round(passes / tot, 2), "ms_per_pass": round(tot / passes * 1e3, 3),
+           "photons_per_s": round(passes * sn * sn / tot, 1), "mrays_per_s": round(rays / tot / 1e6, 2),
+           "splats_per_photon": round((s1["light_splats"] - s0["light_splats"]) / (passes * sn * sn), 3),
+           "passes": passes, "nonfinite_drops": s1["nonfinite_drops"]}
+    if not args.no_cpu_baseline:
+        from oracle.oracle import OracleScene
+        o = OracleScene(sc)
+        m = 250_000
+        spc = abi.sppm_params(m, max_depth=5, radius=0.01, alpha=0.7, seed=1)
+        t0 = time.perf_counter()
+        o.sppm_pass(spc, W, H, 0)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(m / dt, 1), "unit": "photons/s",
+                               "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": f"one pass with {m} photons (camera pass included), all host threads"}
+    del g, film
+    return out
+
+
+def run_sppm_profile(args):
+    """Only SPPM passes of the Cornell room (for an ncu launch list)."""
+    from bling_gb300 import abi
+    from bling_gb300 import scene as S
+    from bling_gb300.api import Context
+    ctx = Context(device=0)
+    g = ctx.scene(S.cornell_room(256, 256))
+    film = ctx.film(256, 256)
+    sp = abi.sppm_params(args.sppm_photons, max_depth=5, radius=0.01, alpha=0.7, seed=1)
+    for k in range(args.warmup + args.steps):
+        g.sppm_pass(film, sp, k)
+    st = g.stats()
+    print(json.dumps({"sppm_profile": True, "photons": args.sppm_photons,
+                      "passes": args.warmup + args.steps, "rays_closest": st["rays_closest"],
+                      "splats": st["light_splats"]}))
+
+
 def run_light_profile(args):
     """Only light passes of the Cornell room (for an ncu launch list)."""
     from bling_gb300.api import Context
@@ -663,9 +730,11 @@ def run_ours(args):
     render = None
     if not args.no_render and rank == 0:
         render = measure_render(ctx, stream, args)
-    light = None
+    light = sppm = None
     if not args.no_light and rank == 0:
         light = measure_light(ctx, stream, args)
+    if not args.no_sppm and rank == 0:
+        sppm = measure_sppm(ctx, stream, args)
     batched = served = None
     if not args.no_batch and rank == 0:
         batched = measure_batched(args)
@@ -718,6 +787,7 @@ def run_ours(args):
             "bvh_nodes": st["bvh_nodes"],
             "path_integrator": render,
             "light_tracer": light,
+            "sppm": sppm,
             "batched_wavefront": batched,
             "serving": served,
         }
@@ -812,6 +882,10 @@ def main():
     ap.add_argument("--light-photons", type=int, default=1 << 22)
     ap.add_argument("--light-profile", action="store_true",
                     help="only run light passes of the Cornell room (profiling)")
+    ap.add_argument("--no-sppm", action="store_true", help="skip the SPPM workload")
+    ap.add_argument("--sppm-photons", type=int, default=1 << 20)
+    ap.add_argument("--sppm-profile", action="store_true",
+                    help="only run SPPM passes of the Cornell room (profiling)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched workload")
     ap.add_argument("--batch-instances", type=int, default=64)
     ap.add_argument("--no-serving", action="store_true", help="skip the serving workload")
@@ -832,6 +906,8 @@ def main():
         args.warmup = 3
     if args.light_profile:
         run_light_profile(args)
+    elif args.sppm_profile:
+        run_sppm_profile(args)
     elif args.render_size:
         run_render_profile(args)
     elif args.batch_profile:
