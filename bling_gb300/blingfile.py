@@ -68,6 +68,13 @@ class Job:
     max_depth: int = 7                 # mkPathIntegrator 7 3 (IntegratorParser.hs)
     sample_depth: int = 3
     photons_per_pass: int = 0          # renderer { light passPhotons N } (RendererParser.hs:28-30)
+    sppm: tuple | None = None          # (photonCount, maxDepth, radius, alpha) (RendererParser.hs:40-45)
+
+    def sppm_params(self, seed: int = 1) -> abi.SppmParams:
+        """bling_sppm_params of a `renderer { sppm ... }` job (mkSPPM n md r alpha)"""
+        n, md, r, a = self.sppm
+        return abi.sppm_params(n, md, r, a, filter_kind=self.filter_kind,
+                               filter_params=self.filter_params, seed=seed)
 
     def params(self, seed: int = 1, rr_depth: int = 7) -> abi.RenderParams:
         """bling_render_params of the job's sampler renderer and path
@@ -271,6 +278,7 @@ class _State:
         self.res = (640, 480)
         self.renderer = "path"
         self.photons = 0  # photons per pass of the light tracer
+        self.sppm = None  # mkSPPM arguments
         self.sampler = (abi.SAMPLER_STRATIFIED, (2, 2))
         self.depths = (7, 3)
         self.filter = (abi.FILTER_BOX, (0.0, 0.0, 0.0, 0.0))
@@ -321,7 +329,7 @@ class _Parser:
         (kind, strata), (md, sd) = self.s.sampler, self.s.depths
         fk, fp = self.s.filter
         return Job(sc, self.s.res[0], self.s.res[1], fk, fp, self.s.renderer, kind, strata, md, sd,
-                   self.s.photons)
+                   self.s.photons, self.s.sppm)
 
     def p_size(self):
         self.s.res = (self.t.integ(), self.t.integ())
@@ -351,6 +359,13 @@ class _Parser:
             if name == "light":  # mkLightTracer ppp, run by bling_light_pass
                 self.s.photons = t.named_int("passPhotons")
                 self.s.renderer = "light"
+                return
+            if name == "sppm":  # mkSPPM n md r alpha, run by bling_sppm_pass
+                n, md = t.named_int("photonCount"), t.named_int("maxDepth")
+                r = t.named_flt("radius")
+                a = t.named_flt("alpha") if t.at("alpha") else F(0.8)
+                self.s.sppm = (n, md, r, a)
+                self.s.renderer = "sppm"
                 return
             if name != "sampler":
                 self._skip_to_block_end()

@@ -160,7 +160,10 @@ def test_constant_spd_gives_a_flat_spectrum():
 
 def test_other_renderers_parse_and_are_named():
     j = B.parse("renderer { sppm photonCount 20000 maxDepth 10 radius 10 alpha 0.9 }")
-    assert j.renderer == "sppm"
+    assert j.renderer == "sppm" and j.sppm == (20000, 10, F(10), B.f32_of_decimal("0.9"))
+    sp = j.sppm_params(seed=3)
+    assert (sp.photons, sp.max_depth, sp.seed) == (20000, 10, 3) and sp.alpha == F(0.9)
+    assert B.parse("renderer { sppm photonCount 5 maxDepth 2 radius 1 }").sppm[3] == F(0.8)
     j = B.parse("renderer { light passPhotons 50000 }")
     assert j.renderer == "light" and j.photons_per_pass == 50000
     j = B.parse("renderer { sampler sampled { sampler { random 16 } "
