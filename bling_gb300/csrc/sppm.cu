@@ -82,10 +82,14 @@ struct SpHash {
   const int32_t* entries;
 };
 struct SpPhotons {
-  float* li;  // 16 per photon
+  float* li[2];   // 16 per photon: the power at this vertex / at the next (by depth parity)
   float* ray;
   float4* hit;
+  float4* gpos;   // this vertex's hit: position, bucket (int bits; -1: no lookup)
+  float4* gwi;    // this vertex's wi, |wi . ng|
+  uint32_t* cnt;  // per live entry: hit points found (then the pair offsets; total at [cap])
   int32_t* live[2];
+  uint32_t* sums;
 };
 struct PhotonParams {
   uint64_t seed, pass;  // the photon pass's sampler key: (seed, 2 pass + 1, pixel 0 0)
@@ -433,7 +437,7 @@ __global__ void __launch_bounds__(128) k_sp_emit(DevAccel A, DevShading S, Photo
       Spec li = sScale(le, absDot(nl, wi) / pdf);
       live = pdf > 0 && !isBlack(li);
       if (live) {
-        storeBands(ph.li, (int)i, li);
+        storeBands(ph.li[0], (int)i, li);
         storeRay(ph.ray, (int)i, ray);
       }
     }
@@ -459,20 +463,35 @@ __global__ void __launch_bounds__(128, 10) k_sp_ptrace(DevAccel A, SpPhotons ph,
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + S_CLOSEST, (unsigned long long)n);
 }
 
-// followPhoton (SPPM.hs:187-224) at photon vertex `depth`
-__global__ void __launch_bounds__(128, 4) k_sp_photon(DevAccel A, DevShading S, PassParams P,
-                                                      PhotonParams Q, SpPhotons ph, SpHp hp,
-                                                      SpHash hs, float* __restrict__ splat,
-                                                      uint32_t* __restrict__ m, int64_t stat_count,
-                                                      int in, int depth,
+// the hit points of bucket b within their radius of p (hashLookup/treeLookup,
+// SPPM.hs:295-302, 360-373), visited in bucket order
+template <class Visit>
+__device__ __forceinline__ void bucketScan(const SpHash& hs, const SpHp& hp, long long b, V3 p,
+                                           Visit visit) {
+  for (uint32_t e = hs.off[b]; e < hs.off[b + 1]; e++) {
+    int h = hs.entries[e];
+    float4 hpp = hp.p[h];
+    if (sqLen(V3{hpp.x, hpp.y, hpp.z} - p) <= hpp.w) visit(h);
+  }
+}
+
+// followPhoton (SPPM.hs:187-224) at photon vertex `depth`: the hit, the
+// number of hit points its lookup finds (their splats follow in k_sp_splat)
+// and the continuation
+__global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, PhotonParams Q,
+                                                      SpPhotons ph, SpHp hp, SpHash hs, int in,
+                                                      int depth,
                                                       unsigned long long* __restrict__ counters) {
   const int32_t* __restrict__ qin = ph.live[in];
+  const float* __restrict__ li_in = ph.li[depth & 1];
+  float* __restrict__ li_out = ph.li[(depth + 1) & 1];
   int64_t n = (int64_t)counters[S_PLIVE0 + in];
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
     bool cont = false;
     int s = 0;
+    uint32_t found = 0;
     if (q < n) {
       s = qin[q];
       float4 hit = ph.hit[s];
@@ -480,58 +499,24 @@ __global__ void __launch_bounds__(128, 4) k_sp_photon(DevAccel A, DevShading S, 
       if (prim == kDegenerateRay) {
         atomicAdd(counters + S_DEGENERATE, 1ull);
       } else if (prim >= 0) {
-        Spec li = loadBands(ph.li, s);
+        Spec li = loadBands(li_in, s);
         Ray ray = loadRay7(ph.ray, s);
         V3 wi = -ray.d;
         HitGeom hg = hitGeometry(A, S, ray, prim, hit.x, hit.z, hit.w);
         Bsdf bsdf = materialBsdf(S.materials, hg.material, hg.n, hg.sp, hg.sn, hg.sdpdu);
         V3 p = bsdf.p;
-        if (bsdfHasNonSpecular(bsdf)) {
+        long long b = -1;
+        if (bsdfHasNonSpecular(bsdf) && hs.cnt > 0) {
           // hashLookup (SPPM.hs:295-302): the bucket of p's cell
           float cx = fabsf((p.x - hs.lo.x) * hs.scale), cy = fabsf((p.y - hs.lo.y) * hs.scale),
                 cz = fabsf((p.z - hs.lo.z) * hs.scale);
           if (cx < 9.2e18f && cy < 9.2e18f && cz < 9.2e18f) {
-            long long b = cellBucket((long long)cx, (long long)cy, (long long)cz, hs.cnt);
-            float cosg = absDot(wi, bsdf.ng);
-            for (uint32_t e = hs.off[b]; e < hs.off[b + 1]; e++) {
-              int h = hs.entries[e];
-              float4 hpp = hp.p[h];
-              V3 hpos{hpp.x, hpp.y, hpp.z};
-              float r2 = hpp.w;
-              if (!(sqLen(hpos - p) <= r2)) continue;
-              float4 pix = hp.pix[h], w4 = hp.w[h], ng4 = hp.ng[h], sn4 = hp.sn[h], sd4 = hp.sd[h];
-              Bsdf hb = materialBsdf(S.materials, __float_as_int(pix.z), V3{ng4.x, ng4.y, ng4.z},
-                                     hpos, V3{sn4.x, sn4.y, sn4.z}, V3{sd4.x, sd4.y, sd4.z});
-              Spec f = evalBsdf<false>(hb, V3{w4.x, w4.y, w4.z}, wi);
-              Spec l = sScale(loadBands(hp.F, h) * f * li, 1.0f / (cosg * r2 * kPi));
-              // splatSample (Image.hs:201-221) at the hit point's pixel
-              float px = pix.x, py = pix.y;
-              if (px >= 0.0f && px < (float)P.width && py >= 0.0f && py < (float)P.height) {
-                bool bad = false;
-#pragma unroll
-                for (int i = 0; i < 16; i++) bad = bad || isnan(l.v[i]) || isinf(l.v[i]);
-                if (bad) {
-                  atomicAdd(counters + S_NONFINITE, 1ull);
-                } else {
-                  float x = 0, y = 0, z = 0;
-#pragma unroll
-                  for (int i = 0; i < 16; i++) {
-                    x = x + c_cieX[i] * l.v[i];
-                    y = y + c_cieY[i] * l.v[i];
-                    z = z + c_cieZ[i] * l.v[i];
-                  }
-                  float* o = splat + 3 * ((size_t)floorf(py) * P.width + (size_t)floorf(px));
-                  atomicAdd(o, x / c_cieYSum);
-                  atomicAdd(o + 1, y / c_cieYSum);
-                  atomicAdd(o + 2, z / c_cieYSum);
-                  atomicAdd(counters + S_SPLATS, 1ull);
-                }
-              }
-              int64_t si = statIndex(P, px, py);
-              if (si >= 0 && si < stat_count) atomicAdd(m + si, 1u);
-            }
+            b = cellBucket((long long)cx, (long long)cy, (long long)cz, hs.cnt);
+            bucketScan(hs, hp, b, p, [&](int) { found++; });
           }
         }
+        ph.gpos[s] = make_float4(p.x, p.y, p.z, __int_as_float(found ? (int)b : -1));
+        ph.gwi[s] = make_float4(wi.x, wi.y, wi.z, absDot(wi, bsdf.ng));
         Sampler smp{pixelKey(Q.seed, Q.pass, 0, 0), (uint32_t)(Q.chunk_base + (uint64_t)s), Q.sn,
                     Q.sn, 7, 5};
         float ubc = rnd1(smp, 1 + depth * 2), u1, u2;
@@ -540,14 +525,115 @@ __global__ void __launch_bounds__(128, 4) k_sp_photon(DevAccel A, DevShading S, 
         float pcont = depth > 7 ? 0.8f : 1.0f;
         Spec li2 = sScale(bs.f * li, 1.0f / pcont);
         if (!(bs.pdf == 0 || isBlack(li2)) && !(rnd1(smp, 2 + depth * 2) > pcont)) {
-          storeBands(ph.li, s, li2);
+          storeBands(li_out, s, li2);
           storeRay(ph.ray, s, Ray{p, bs.wi, hg.eps, INFINITY});
           cont = true;
         }
       }
+      ph.cnt[q] = found;
     }
     queueAppend(cont, s, ph.live[1 - in], counters + S_PLIVE0 + (1 - in));
   }
+}
+
+// the (photon, hit point) pairs of this vertex, at the prefix offsets of
+// the counts (a photon's pairs in bucket order)
+__global__ void __launch_bounds__(128) k_sp_fill(SpPhotons ph, SpHp hp, SpHash hs, int in,
+                                                 const uint32_t* __restrict__ off,
+                                                 int2* __restrict__ pairs,
+                                                 const unsigned long long* __restrict__ counters) {
+  const int32_t* __restrict__ qin = ph.live[in];
+  int64_t n = (int64_t)counters[S_PLIVE0 + in];
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    int s = qin[q];
+    float4 gp = ph.gpos[s];
+    int b = __float_as_int(gp.w);
+    if (b < 0) continue;
+    uint32_t k = off[q];
+    bucketScan(hs, hp, b, V3{gp.x, gp.y, gp.z}, [&](int h) { pairs[k++] = make_int2(s, h); });
+  }
+}
+
+// one thread per pair: the splat hpF * f * li / (|wi.ng| r^2 pi) at the hit
+// point's pixel (splatSample, Image.hs:201-221) and the photon count there
+__global__ void __launch_bounds__(128) k_sp_splat(DevShading S, PassParams P, SpPhotons ph, SpHp hp,
+                                                  int depth, const int2* __restrict__ pairs,
+                                                  const uint32_t* __restrict__ total,
+                                                  float* __restrict__ splat, uint32_t* __restrict__ m,
+                                                  int64_t stat_count,
+                                                  unsigned long long* __restrict__ counters) {
+  const float* __restrict__ li_in = ph.li[depth & 1];
+  int64_t T = (int64_t)*total;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    int2 pr = pairs[i];
+    int s = pr.x, h = pr.y;
+    float4 gw = ph.gwi[s];
+    V3 wi{gw.x, gw.y, gw.z};
+    float4 hpp = hp.p[h], pix = hp.pix[h], w4 = hp.w[h], ng4 = hp.ng[h], sn4 = hp.sn[h], sd4 = hp.sd[h];
+    float r2 = hpp.w;
+    Bsdf hb = materialBsdf(S.materials, __float_as_int(pix.z), V3{ng4.x, ng4.y, ng4.z},
+                           V3{hpp.x, hpp.y, hpp.z}, V3{sn4.x, sn4.y, sn4.z}, V3{sd4.x, sd4.y, sd4.z});
+    Spec f = evalBsdf<false>(hb, V3{w4.x, w4.y, w4.z}, wi);
+    Spec l = sScale(loadBands(hp.F, h) * f * loadBands(li_in, s), 1.0f / (gw.w * r2 * kPi));
+    float px = pix.x, py = pix.y;
+    if (px >= 0.0f && px < (float)P.width && py >= 0.0f && py < (float)P.height) {
+      bool bad = false;
+#pragma unroll
+      for (int k = 0; k < 16; k++) bad = bad || isnan(l.v[k]) || isinf(l.v[k]);
+      if (bad) {
+        atomicAdd(counters + S_NONFINITE, 1ull);
+      } else {
+        float x = 0, y = 0, z = 0;
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+          x = x + c_cieX[k] * l.v[k];
+          y = y + c_cieY[k] * l.v[k];
+          z = z + c_cieZ[k] * l.v[k];
+        }
+        float* o = splat + 3 * ((size_t)floorf(py) * P.width + (size_t)floorf(px));
+        atomicAdd(o, x / c_cieYSum);
+        atomicAdd(o + 1, y / c_cieYSum);
+        atomicAdd(o + 2, z / c_cieYSum);
+        atomicAdd(counters + S_SPLATS, 1ull);
+      }
+    }
+    int64_t si = statIndex(P, px, py);
+    if (si >= 0 && si < stat_count) atomicAdd(m + si, 1u);
+  }
+}
+
+// exclusive scan of the live entries' counts (n read on the device), the
+// total at out[cap]
+__global__ void __launch_bounds__(1024) k_scan_live(const uint32_t* __restrict__ in,
+                                                    uint32_t* __restrict__ out,
+                                                    const unsigned long long* __restrict__ nptr,
+                                                    uint32_t* __restrict__ sums) {
+  __shared__ uint32_t part[1024];
+  int64_t n = (int64_t)*nptr;
+  int t = threadIdx.x;
+  int64_t i = (int64_t)blockIdx.x * 1024 + t;
+  uint32_t v = i < n ? in[i] : 0u;
+  part[t] = v;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    uint32_t a = t >= o ? part[t - o] : 0u;
+    __syncthreads();
+    part[t] += a;
+    __syncthreads();
+  }
+  if (i < n) out[i] = part[t] - v;
+  if (t == 1023) sums[blockIdx.x] = part[t];
+}
+__global__ void __launch_bounds__(1024) k_scan_live_add(uint32_t* __restrict__ out,
+                                                        const unsigned long long* __restrict__ nptr,
+                                                        const uint32_t* __restrict__ sums, int64_t nb,
+                                                        uint32_t* __restrict__ total) {
+  int64_t n = (int64_t)*nptr;
+  int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) out[i] += sums[blockIdx.x];
+  if (i == 0) *total = sums[nb];
 }
 
 // statsUpdate (SPPM.hs:258-279)
@@ -620,18 +706,30 @@ size_t hpBytes(size_t H) { return H * (6 * 16 + 64); }
 SpPhotons carvePhotons(void* base, size_t cap) {
   SpPhotons p;
   float* w = (float*)base;
-  p.li = w;
+  p.li[0] = w;
+  w += 16 * cap;
+  p.li[1] = w;
   w += 16 * cap;
   p.ray = w;
   w += 8 * cap;
   p.hit = (float4*)w;
   w += 4 * cap;
+  p.gpos = (float4*)w;
+  w += 4 * cap;
+  p.gwi = (float4*)w;
+  w += 4 * cap;
+  p.cnt = (uint32_t*)w;
+  w += cap + 64;  // counts, then the total at [cap]
   p.live[0] = (int32_t*)w;
   w += cap;
   p.live[1] = (int32_t*)w;
+  w += cap;
+  p.sums = (uint32_t*)w;  // block sums of the count scan: cap / 1024 + 1 entries
   return p;
 }
-size_t photonBytes(size_t cap) { return 4 * cap * (16 + 8 + 4 + 2); }
+size_t photonBytes(size_t cap) {
+  return 4 * (cap * (16 + 16 + 8 + 4 + 4 + 4 + 1 + 2) + 64 + cap / 1024 + 64);
+}
 
 size_t round64(size_t n) { return (std::max<size_t>(n, 64) + 63) / 64 * 64; }
 
@@ -652,6 +750,7 @@ void sppm_workspace_free(SppmWorkspace& ws) {
   cudaFree(ws.buckets);
   cudaFree(ws.entries);
   cudaFree(ws.photons);
+  cudaFree(ws.pairs);
   cudaFree(ws.counters);
   ws = SppmWorkspace{};
 }
@@ -848,7 +947,11 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
     Q.wr = a.wr;
     unsigned g_pt = wide ? residentGrid(k_sp_ptrace<true>, sms, block)
                          : residentGrid(k_sp_ptrace<false>, sms, block);
-    unsigned g_ph = residentGrid(k_sp_photon, sms, block);
+    unsigned g_vx = residentGrid(k_sp_vertex, sms, block);
+    unsigned g_sp = residentGrid(k_sp_splat, sms, block);
+    const size_t cap_n = ws.photon_cap;
+    const unsigned nb = (unsigned)((cap_n + 1023) / 1024);
+    uint32_t* total = ph.cnt + cap_n;
     for (int64_t base = 0; base < nphot; base += (int64_t)ws.photon_cap) {
       int64_t count = std::min<int64_t>((int64_t)ws.photon_cap, nphot - base);
       Q.chunk_base = (uint64_t)base;
@@ -863,16 +966,36 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
           k_sp_ptrace<true><<<std::min(g_pt, cap_blocks), block, 0, stream>>>(A, ph, in, counters);
         else
           k_sp_ptrace<false><<<std::min(g_pt, cap_blocks), block, 0, stream>>>(A, ph, in, counters);
-        k_sp_photon<<<std::min(g_ph, cap_blocks), block, 0, stream>>>(
-            A, S, P, Q, ph, hp, hs, d_splat, px.m, px.count, in, depth, counters);
+        k_sp_vertex<<<std::min(g_vx, cap_blocks), block, 0, stream>>>(A, S, Q, ph, hp, hs, in, depth,
+                                                                     counters);
+        // the pairs' offsets: a prefix sum of the live entries' counts, in place
+        k_scan_live<<<nb, 1024, 0, stream>>>(ph.cnt, ph.cnt, counters + S_PLIVE0 + in, ph.sums);
+        k_scan_sums<<<1, 1024, 0, stream>>>(ph.sums, (int64_t)nb);
+        k_scan_live_add<<<nb, 1024, 0, stream>>>(ph.cnt, counters + S_PLIVE0 + in, ph.sums,
+                                                 (int64_t)nb, total);
         RET_CUDA(cudaGetLastError());
-        if (depth >= 7 && (depth & 3) == 3) {
-          unsigned long long live = 0;
-          RET_CUDA(cudaMemcpyAsync(&live, counters + S_PLIVE0 + (1 - in), sizeof live,
-                                   cudaMemcpyDeviceToHost, stream));
-          RET_CUDA(cudaStreamSynchronize(stream));
-          if (live == 0) break;
+        uint32_t tp = 0;
+        unsigned long long live = 0;
+        RET_CUDA(cudaMemcpyAsync(&tp, total, sizeof tp, cudaMemcpyDeviceToHost, stream));
+        RET_CUDA(cudaMemcpyAsync(&live, counters + S_PLIVE0 + (1 - in), sizeof live,
+                                 cudaMemcpyDeviceToHost, stream));
+        RET_CUDA(cudaStreamSynchronize(stream));
+        if (tp > 0) {
+          if (ws.pair_cap < tp) {
+            size_t have = ws.pairs ? 8 * ws.pair_cap : 0;
+            size_t want = std::max<size_t>(2 * (size_t)tp, cap_n);
+            RET_CUDA(growTo(ws.pairs, have, 8 * want));
+            ws.pair_cap = want;
+          }
+          int2* pairs = (int2*)ws.pairs;
+          k_sp_fill<<<std::min(g_wide, cap_blocks), block, 0, stream>>>(ph, hp, hs, in, ph.cnt, pairs,
+                                                                         counters);
+          unsigned gsp = std::min<unsigned>(g_sp, (unsigned)((tp + block - 1) / block));
+          k_sp_splat<<<gsp, block, 0, stream>>>(S, P, ph, hp, depth, pairs, total, d_splat, px.m,
+                                                px.count, counters);
+          RET_CUDA(cudaGetLastError());
         }
+        if (live == 0) break;
       }
     }
   }
