@@ -531,6 +531,8 @@ __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, 
         }
       }
       ph.cnt[q] = found;
+      // no hit point found (or no hit at all): the fill pass skips the entry
+      if (!found) ph.gpos[s] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
     }
     queueAppend(cont, s, ph.live[1 - in], counters + S_PLIVE0 + (1 - in));
   }
