@@ -79,7 +79,8 @@ struct SpHash {
   float scale;       // 1 / cell size
   long long cnt;     // buckets
   const uint32_t* off;  // cnt + 1 offsets into entries
-  const int32_t* entries;
+  const int32_t* entries;  // hit-point index per entry
+  const float4* epos;      // the entry's hit point: position, radius^2 (a copy, read in bucket order)
 };
 struct SpPhotons {
   float* li[2];   // 16 per photon: the power at this vertex / at the next (by depth parity)
@@ -329,7 +330,8 @@ template <bool FILL>
 __global__ void __launch_bounds__(128) k_sp_cells(SpHp hp, int64_t nh, V3 lo, float invSize,
                                                   long long cnt, uint32_t* __restrict__ counts,
                                                   const uint32_t* __restrict__ off,
-                                                  int32_t* __restrict__ entries) {
+                                                  int32_t* __restrict__ entries,
+                                                  float4* __restrict__ epos) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nh;
        i += (int64_t)gridDim.x * blockDim.x) {
     float4 p = hp.p[i];
@@ -350,7 +352,10 @@ __global__ void __launch_bounds__(128) k_sp_cells(SpHp hp, int64_t nh, V3 lo, fl
         for (long long z = z0; z <= z1; z++) {
           long long b = cellBucket(x, y, z, cnt);
           unsigned pos = atomicAdd(counts + b, 1u);
-          if (FILL) entries[off[b] + pos] = (int32_t)i;
+          if (FILL) {
+            entries[off[b] + pos] = (int32_t)i;
+            epos[off[b] + pos] = p;
+          }
         }
   }
 }
@@ -469,9 +474,8 @@ template <class Visit>
 __device__ __forceinline__ void bucketScan(const SpHash& hs, const SpHp& hp, long long b, V3 p,
                                            Visit visit) {
   for (uint32_t e = hs.off[b]; e < hs.off[b + 1]; e++) {
-    int h = hs.entries[e];
-    float4 hpp = hp.p[h];
-    if (sqLen(V3{hpp.x, hpp.y, hpp.z} - p) <= hpp.w) visit(h);
+    float4 hpp = hs.epos[e];
+    if (sqLen(V3{hpp.x, hpp.y, hpp.z} - p) <= hpp.w) visit(hs.entries[e]);
   }
 }
 
@@ -907,7 +911,7 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
     RET_CUDA(cudaMemsetAsync(counts, 0, 4 * ((size_t)cnt + 1), stream));
     unsigned gc = std::min<unsigned>(g_wide, (unsigned)((nh + block - 1) / block));
     k_sp_cells<false><<<gc, block, 0, stream>>>(hp, (int64_t)nh, lo, invSize, cnt, counts, nullptr,
-                                                nullptr);
+                                                nullptr, nullptr);
     k_scan_blocks<<<(unsigned)nblk, 1024, 0, stream>>>(counts, off, cnt, sums);
     k_scan_sums<<<1, 1024, 0, stream>>>(sums, (int64_t)nblk);
     k_scan_add<<<(unsigned)nblk, 1024, 0, stream>>>(off, cnt, sums);
@@ -915,18 +919,19 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
     uint32_t E = 0;
     RET_CUDA(cudaMemcpyAsync(&E, off + cnt, 4, cudaMemcpyDeviceToHost, stream));
     RET_CUDA(cudaStreamSynchronize(stream));
-    if (ws.entry_cap < (size_t)E + 1) {
-      void* e = ws.entries;
-      size_t have = ws.entries ? 4 * ws.entry_cap : 0;
-      RET_CUDA(growTo(e, have, 4 * ((size_t)E + 1)));
-      ws.entries = (int32_t*)e;
-      ws.entry_cap = (size_t)E + 1;
+    if (ws.entry_cap < (size_t)E + 1) {  // E + 1 positions (float4), then E + 1 indices
+      size_t want = round64((size_t)E + 1);
+      size_t have = ws.entries ? 20 * ws.entry_cap : 0;
+      RET_CUDA(growTo(ws.entries, have, 20 * want));
+      ws.entry_cap = want;
     }
+    float4* epos = (float4*)ws.entries;
+    int32_t* eidx = (int32_t*)(epos + ws.entry_cap);
     RET_CUDA(cudaMemsetAsync(counts, 0, 4 * ((size_t)cnt + 1), stream));
     k_sp_cells<true><<<gc, block, 0, stream>>>(hp, (int64_t)nh, lo, invSize, cnt, counts, off,
-                                               ws.entries);
+                                               eidx, epos);
     RET_CUDA(cudaGetLastError());
-    hs = SpHash{lo, invSize, cnt, off, ws.entries};
+    hs = SpHash{lo, invSize, cnt, off, eidx, epos};
   }
 
   // ---- 3. photon pass
@@ -952,17 +957,19 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
     unsigned g_vx = residentGrid(k_sp_vertex, sms, block);
     unsigned g_sp = residentGrid(k_sp_splat, sms, block);
     const size_t cap_n = ws.photon_cap;
-    const unsigned nb = (unsigned)((cap_n + 1023) / 1024);
     uint32_t* total = ph.cnt + cap_n;
     for (int64_t base = 0; base < nphot; base += (int64_t)ws.photon_cap) {
       int64_t count = std::min<int64_t>((int64_t)ws.photon_cap, nphot - base);
       Q.chunk_base = (uint64_t)base;
-      unsigned cap_blocks = (unsigned)std::max<int64_t>(1, (count + block - 1) / block);
+      unsigned emit_blocks = (unsigned)std::max<int64_t>(1, (count + block - 1) / block);
       k_sp_preset<<<1, 32, 0, stream>>>(counters, S_PLIVE0);
-      k_sp_emit<<<std::min(g_wide, cap_blocks), block, 0, stream>>>(A, S, Q, ph, count, counters);
+      k_sp_emit<<<std::min(g_wide, emit_blocks), block, 0, stream>>>(A, S, Q, ph, count, counters);
       RET_CUDA(cudaGetLastError());
+      int64_t n_cur = count;  // an upper bound of the live photons, exact after the first bounce
       for (int depth = 0;; depth++) {
         int in = depth & 1;
+        unsigned cap_blocks = (unsigned)std::max<int64_t>(1, (n_cur + block - 1) / block);
+        unsigned nb = (unsigned)std::max<int64_t>(1, (n_cur + 1023) / 1024);
         k_sp_preset<<<1, 32, 0, stream>>>(counters, S_PLIVE0 + (1 - in));
         if (wide)
           k_sp_ptrace<true><<<std::min(g_pt, cap_blocks), block, 0, stream>>>(A, ph, in, counters);
@@ -998,6 +1005,7 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
           RET_CUDA(cudaGetLastError());
         }
         if (live == 0) break;
+        n_cur = (int64_t)live;
       }
     }
   }

@@ -39,7 +39,7 @@ struct SppmWorkspace {
   size_t hp_cap = 0;
   void* buckets = nullptr;  // bucket counts, offsets, cursors, block sums
   size_t bucket_cap = 0;
-  int32_t* entries = nullptr;
+  void* entries = nullptr;  // bucket entries: positions (float4), then hit-point indices
   size_t entry_cap = 0;
   void* photons = nullptr;  // photon slots
   size_t photon_cap = 0;
