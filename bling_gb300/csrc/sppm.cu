@@ -468,17 +468,6 @@ __global__ void __launch_bounds__(128, 10) k_sp_ptrace(DevAccel A, SpPhotons ph,
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + S_CLOSEST, (unsigned long long)n);
 }
 
-// the hit points of bucket b within their radius of p (hashLookup/treeLookup,
-// SPPM.hs:295-302, 360-373), visited in bucket order
-template <class Visit>
-__device__ __forceinline__ void bucketScan(const SpHash& hs, const SpHp& hp, long long b, V3 p,
-                                           Visit visit) {
-  for (uint32_t e = hs.off[b]; e < hs.off[b + 1]; e++) {
-    float4 hpp = hs.epos[e];
-    if (sqLen(V3{hpp.x, hpp.y, hpp.z} - p) <= hpp.w) visit(hs.entries[e]);
-  }
-}
-
 // followPhoton (SPPM.hs:187-224) at photon vertex `depth`: the hit, the
 // number of hit points its lookup finds (their splats follow in k_sp_splat)
 // and the continuation
@@ -493,9 +482,8 @@ __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, 
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
-    bool cont = false;
+    bool cont = false, looked = false;
     int s = 0;
-    uint32_t found = 0;
     if (q < n) {
       s = qin[q];
       float4 hit = ph.hit[s];
@@ -511,15 +499,14 @@ __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, 
         V3 p = bsdf.p;
         long long b = -1;
         if (bsdfHasNonSpecular(bsdf) && hs.cnt > 0) {
-          // hashLookup (SPPM.hs:295-302): the bucket of p's cell
+          // hashLookup (SPPM.hs:295-302): the bucket of p's cell, scanned by k_sp_count
           float cx = fabsf((p.x - hs.lo.x) * hs.scale), cy = fabsf((p.y - hs.lo.y) * hs.scale),
                 cz = fabsf((p.z - hs.lo.z) * hs.scale);
-          if (cx < 9.2e18f && cy < 9.2e18f && cz < 9.2e18f) {
+          if (cx < 9.2e18f && cy < 9.2e18f && cz < 9.2e18f)
             b = cellBucket((long long)cx, (long long)cy, (long long)cz, hs.cnt);
-            bucketScan(hs, hp, b, p, [&](int) { found++; });
-          }
         }
-        ph.gpos[s] = make_float4(p.x, p.y, p.z, __int_as_float(found ? (int)b : -1));
+        ph.gpos[s] = make_float4(p.x, p.y, p.z, __int_as_float((int)b));
+        looked = true;
         ph.gwi[s] = make_float4(wi.x, wi.y, wi.z, absDot(wi, bsdf.ng));
         Sampler smp{pixelKey(Q.seed, Q.pass, 0, 0), (uint32_t)(Q.chunk_base + (uint64_t)s), Q.sn,
                     Q.sn, 7, 5};
@@ -534,30 +521,49 @@ __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, 
           cont = true;
         }
       }
-      ph.cnt[q] = found;
-      // no hit point found (or no hit at all): the fill pass skips the entry
-      if (!found) ph.gpos[s] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
+      // no hit at all: the count and fill passes skip the entry
+      if (!looked) ph.gpos[s] = make_float4(0.0f, 0.0f, 0.0f, __int_as_float(-1));
     }
     queueAppend(cont, s, ph.live[1 - in], counters + S_PLIVE0 + (1 - in));
   }
 }
 
-// the (photon, hit point) pairs of this vertex, at the prefix offsets of
-// the counts (a photon's pairs in bucket order)
-__global__ void __launch_bounds__(128) k_sp_fill(SpPhotons ph, SpHp hp, SpHash hs, int in,
-                                                 const uint32_t* __restrict__ off,
-                                                 int2* __restrict__ pairs,
-                                                 const unsigned long long* __restrict__ counters) {
+// one warp per live photon: the hit points of its bucket within their radius
+// (hashLookup/treeLookup, SPPM.hs:295-302, 360-373), 32 entries at a time.
+// COUNT = true stores their number; false writes the (photon, hit point)
+// pairs, in bucket order, from the photon's prefix offset.
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_sp_gather(SpPhotons ph, SpHash hs, int in,
+                                                   uint32_t* __restrict__ cnt_off,
+                                                   int2* __restrict__ pairs,
+                                                   const unsigned long long* __restrict__ counters) {
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
   const int32_t* __restrict__ qin = ph.live[in];
   int64_t n = (int64_t)counters[S_PLIVE0 + in];
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
-       q += (int64_t)gridDim.x * blockDim.x) {
+  int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t q = warp; q < n; q += nwarps) {
     int s = qin[q];
     float4 gp = ph.gpos[s];
     int b = __float_as_int(gp.w);
-    if (b < 0) continue;
-    uint32_t k = off[q];
-    bucketScan(hs, hp, b, V3{gp.x, gp.y, gp.z}, [&](int h) { pairs[k++] = make_int2(s, h); });
+    uint32_t run = COUNT ? 0u : cnt_off[q];
+    if (b >= 0) {
+      V3 p{gp.x, gp.y, gp.z};
+      uint32_t lo = hs.off[b], hi = hs.off[b + 1];
+      for (uint32_t e0 = lo; e0 < hi; e0 += 32) {
+        uint32_t e = e0 + lane;
+        bool hitp = false;
+        if (e < hi) {
+          float4 hpp = hs.epos[e];
+          hitp = sqLen(V3{hpp.x, hpp.y, hpp.z} - p) <= hpp.w;
+        }
+        unsigned m = __ballot_sync(full, hitp);
+        if (!COUNT && hitp) pairs[run + __popc(m & ((1u << lane) - 1))] = make_int2(s, hs.entries[e]);
+        run += __popc(m);
+      }
+    }
+    if (COUNT && lane == 0) cnt_off[q] = run;
   }
 }
 
@@ -977,6 +983,9 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
           k_sp_ptrace<false><<<std::min(g_pt, cap_blocks), block, 0, stream>>>(A, ph, in, counters);
         k_sp_vertex<<<std::min(g_vx, cap_blocks), block, 0, stream>>>(A, S, Q, ph, hp, hs, in, depth,
                                                                      counters);
+        unsigned warp_blocks = (unsigned)std::max<int64_t>(1, (n_cur + 3) / 4);  // 4 warps a block
+        k_sp_gather<true><<<std::min(g_wide * 2, warp_blocks), block, 0, stream>>>(ph, hs, in, ph.cnt,
+                                                                                nullptr, counters);
         // the pairs' offsets: a prefix sum of the live entries' counts, in place
         k_scan_live<<<nb, 1024, 0, stream>>>(ph.cnt, ph.cnt, counters + S_PLIVE0 + in, ph.sums);
         k_scan_sums<<<1, 1024, 0, stream>>>(ph.sums, (int64_t)nb);
@@ -997,8 +1006,8 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
             ws.pair_cap = want;
           }
           int2* pairs = (int2*)ws.pairs;
-          k_sp_fill<<<std::min(g_wide, cap_blocks), block, 0, stream>>>(ph, hp, hs, in, ph.cnt, pairs,
-                                                                         counters);
+          k_sp_gather<false><<<std::min(g_wide * 2, warp_blocks), block, 0, stream>>>(ph, hs, in, ph.cnt,
+                                                                                   pairs, counters);
           unsigned gsp = std::min<unsigned>(g_sp, (unsigned)((tp + block - 1) / block));
           k_sp_splat<<<gsp, block, 0, stream>>>(S, P, ph, hp, depth, pairs, total, d_splat, px.m,
                                                 px.count, counters);
