@@ -88,9 +88,7 @@ struct SpPhotons {
   float4* hit;
   float4* gpos;   // this vertex's hit: position, bucket (int bits; -1: no lookup)
   float4* gwi;    // this vertex's wi, |wi . ng|
-  uint32_t* cnt;  // per live entry: hit points found (then the pair offsets; total at [cap])
   int32_t* live[2];
-  uint32_t* sums;
 };
 struct PhotonParams {
   uint64_t seed, pass;  // the photon pass's sampler key: (seed, 2 pass + 1, pixel 0 0)
@@ -528,124 +526,103 @@ __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, 
   }
 }
 
-// one warp per live photon: the hit points of its bucket within their radius
-// (hashLookup/treeLookup, SPPM.hs:295-302, 360-373), 32 entries at a time.
-// COUNT = true stores their number; false writes the (photon, hit point)
-// pairs, in bucket order, from the photon's prefix offset.
-template <bool COUNT>
-__global__ void __launch_bounds__(128) k_sp_gather(SpPhotons ph, SpHash hs, int in,
-                                                   uint32_t* __restrict__ cnt_off,
-                                                   int2* __restrict__ pairs,
-                                                   const unsigned long long* __restrict__ counters) {
+// the splat of one (photon, hit point) pair: hpF * f * li / (|wi.ng| r^2 pi)
+// at the hit point's pixel (splatSample, Image.hs:201-221), and the photon
+// count of that pixel
+__device__ __forceinline__ void splatPair(const DevShading& S, const PassParams& P,
+                                          const SpPhotons& ph, const SpHp& hp, const float* li_in,
+                                          int s, int h, float* __restrict__ splat,
+                                          uint32_t* __restrict__ m, int64_t stat_count,
+                                          unsigned long long* __restrict__ counters) {
+  float4 gw = ph.gwi[s];
+  V3 wi{gw.x, gw.y, gw.z};
+  float4 hpp = hp.p[h], pix = hp.pix[h], w4 = hp.w[h], ng4 = hp.ng[h], sn4 = hp.sn[h], sd4 = hp.sd[h];
+  float r2 = hpp.w;
+  Bsdf hb = materialBsdf(S.materials, __float_as_int(pix.z), V3{ng4.x, ng4.y, ng4.z},
+                         V3{hpp.x, hpp.y, hpp.z}, V3{sn4.x, sn4.y, sn4.z}, V3{sd4.x, sd4.y, sd4.z});
+  Spec f = evalBsdf<false>(hb, V3{w4.x, w4.y, w4.z}, wi);
+  Spec l = sScale(loadBands(hp.F, h) * f * loadBands(li_in, s), 1.0f / (gw.w * r2 * kPi));
+  float px = pix.x, py = pix.y;
+  if (px >= 0.0f && px < (float)P.width && py >= 0.0f && py < (float)P.height) {
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < 16; k++) bad = bad || isnan(l.v[k]) || isinf(l.v[k]);
+    if (bad) {
+      atomicAdd(counters + S_NONFINITE, 1ull);
+    } else {
+      float x = 0, y = 0, z = 0;
+#pragma unroll
+      for (int k = 0; k < 16; k++) {
+        x = x + c_cieX[k] * l.v[k];
+        y = y + c_cieY[k] * l.v[k];
+        z = z + c_cieZ[k] * l.v[k];
+      }
+      float* o = splat + 3 * ((size_t)floorf(py) * P.width + (size_t)floorf(px));
+      atomicAdd(o, x / c_cieYSum);
+      atomicAdd(o + 1, y / c_cieYSum);
+      atomicAdd(o + 2, z / c_cieYSum);
+      atomicAdd(counters + S_SPLATS, 1ull);
+    }
+  }
+  int64_t si = statIndex(P, px, py);
+  if (si >= 0 && si < stat_count) atomicAdd(m + si, 1u);
+}
+
+// hashLookup/treeLookup (SPPM.hs:295-302, 360-373) with the splats: one warp
+// per live photon scans the photon's bucket 32 entries at a time; the hit
+// points within their radius go to the warp's queue in shared memory, and
+// every 32 queued pairs are splatted by the whole warp (one pair per lane).
+constexpr int kGatherBlock = 128;
+__global__ void __launch_bounds__(kGatherBlock) k_sp_gather(DevShading S, PassParams P, SpPhotons ph,
+                                                            SpHp hp, SpHash hs, int in, int depth,
+                                                            float* __restrict__ splat,
+                                                            uint32_t* __restrict__ m,
+                                                            int64_t stat_count,
+                                                            unsigned long long* __restrict__ counters) {
+  __shared__ int2 queue[kGatherBlock / 32][64];
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  int2* wq = queue[threadIdx.x >> 5];
   const int32_t* __restrict__ qin = ph.live[in];
+  const float* __restrict__ li_in = ph.li[depth & 1];
   int64_t n = (int64_t)counters[S_PLIVE0 + in];
   int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  int qn = 0;  // queued pairs (the same in every lane)
   for (int64_t q = warp; q < n; q += nwarps) {
     int s = qin[q];
     float4 gp = ph.gpos[s];
     int b = __float_as_int(gp.w);
-    uint32_t run = COUNT ? 0u : cnt_off[q];
-    if (b >= 0) {
-      V3 p{gp.x, gp.y, gp.z};
-      uint32_t lo = hs.off[b], hi = hs.off[b + 1];
-      for (uint32_t e0 = lo; e0 < hi; e0 += 32) {
-        uint32_t e = e0 + lane;
-        bool hitp = false;
-        if (e < hi) {
-          float4 hpp = hs.epos[e];
-          hitp = sqLen(V3{hpp.x, hpp.y, hpp.z} - p) <= hpp.w;
-        }
-        unsigned m = __ballot_sync(full, hitp);
-        if (!COUNT && hitp) pairs[run + __popc(m & ((1u << lane) - 1))] = make_int2(s, hs.entries[e]);
-        run += __popc(m);
+    if (b < 0) continue;
+    V3 p{gp.x, gp.y, gp.z};
+    uint32_t lo = hs.off[b], hi = hs.off[b + 1];
+    for (uint32_t e0 = lo; e0 < hi; e0 += 32) {
+      uint32_t e = e0 + lane;
+      bool found = false;
+      if (e < hi) {
+        float4 hpp = hs.epos[e];
+        found = sqLen(V3{hpp.x, hpp.y, hpp.z} - p) <= hpp.w;
+      }
+      unsigned mk = __ballot_sync(full, found);
+      if (found) wq[qn + __popc(mk & ((1u << lane) - 1))] = make_int2(s, hs.entries[e]);
+      qn += __popc(mk);
+      __syncwarp();
+      if (qn >= 32) {  // a full warp of splats, then the rest to the front of the queue
+        int2 pr = wq[lane];
+        splatPair(S, P, ph, hp, li_in, pr.x, pr.y, splat, m, stat_count, counters);
+        __syncwarp();
+        int2 rest = lane + 32 < qn ? wq[lane + 32] : make_int2(0, 0);
+        __syncwarp();
+        if (lane + 32 < qn) wq[lane] = rest;
+        qn -= 32;
+        __syncwarp();
       }
     }
-    if (COUNT && lane == 0) cnt_off[q] = run;
   }
-}
-
-// one thread per pair: the splat hpF * f * li / (|wi.ng| r^2 pi) at the hit
-// point's pixel (splatSample, Image.hs:201-221) and the photon count there
-__global__ void __launch_bounds__(128) k_sp_splat(DevShading S, PassParams P, SpPhotons ph, SpHp hp,
-                                                  int depth, const int2* __restrict__ pairs,
-                                                  const uint32_t* __restrict__ total,
-                                                  float* __restrict__ splat, uint32_t* __restrict__ m,
-                                                  int64_t stat_count,
-                                                  unsigned long long* __restrict__ counters) {
-  const float* __restrict__ li_in = ph.li[depth & 1];
-  int64_t T = (int64_t)*total;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < T;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    int2 pr = pairs[i];
-    int s = pr.x, h = pr.y;
-    float4 gw = ph.gwi[s];
-    V3 wi{gw.x, gw.y, gw.z};
-    float4 hpp = hp.p[h], pix = hp.pix[h], w4 = hp.w[h], ng4 = hp.ng[h], sn4 = hp.sn[h], sd4 = hp.sd[h];
-    float r2 = hpp.w;
-    Bsdf hb = materialBsdf(S.materials, __float_as_int(pix.z), V3{ng4.x, ng4.y, ng4.z},
-                           V3{hpp.x, hpp.y, hpp.z}, V3{sn4.x, sn4.y, sn4.z}, V3{sd4.x, sd4.y, sd4.z});
-    Spec f = evalBsdf<false>(hb, V3{w4.x, w4.y, w4.z}, wi);
-    Spec l = sScale(loadBands(hp.F, h) * f * loadBands(li_in, s), 1.0f / (gw.w * r2 * kPi));
-    float px = pix.x, py = pix.y;
-    if (px >= 0.0f && px < (float)P.width && py >= 0.0f && py < (float)P.height) {
-      bool bad = false;
-#pragma unroll
-      for (int k = 0; k < 16; k++) bad = bad || isnan(l.v[k]) || isinf(l.v[k]);
-      if (bad) {
-        atomicAdd(counters + S_NONFINITE, 1ull);
-      } else {
-        float x = 0, y = 0, z = 0;
-#pragma unroll
-        for (int k = 0; k < 16; k++) {
-          x = x + c_cieX[k] * l.v[k];
-          y = y + c_cieY[k] * l.v[k];
-          z = z + c_cieZ[k] * l.v[k];
-        }
-        float* o = splat + 3 * ((size_t)floorf(py) * P.width + (size_t)floorf(px));
-        atomicAdd(o, x / c_cieYSum);
-        atomicAdd(o + 1, y / c_cieYSum);
-        atomicAdd(o + 2, z / c_cieYSum);
-        atomicAdd(counters + S_SPLATS, 1ull);
-      }
-    }
-    int64_t si = statIndex(P, px, py);
-    if (si >= 0 && si < stat_count) atomicAdd(m + si, 1u);
+  if (lane < qn) {
+    int2 pr = wq[lane];
+    splatPair(S, P, ph, hp, li_in, pr.x, pr.y, splat, m, stat_count, counters);
   }
-}
-
-// exclusive scan of the live entries' counts (n read on the device), the
-// total at out[cap]
-__global__ void __launch_bounds__(1024) k_scan_live(const uint32_t* __restrict__ in,
-                                                    uint32_t* __restrict__ out,
-                                                    const unsigned long long* __restrict__ nptr,
-                                                    uint32_t* __restrict__ sums) {
-  __shared__ uint32_t part[1024];
-  int64_t n = (int64_t)*nptr;
-  int t = threadIdx.x;
-  int64_t i = (int64_t)blockIdx.x * 1024 + t;
-  uint32_t v = i < n ? in[i] : 0u;
-  part[t] = v;
-  __syncthreads();
-  for (int o = 1; o < 1024; o <<= 1) {
-    uint32_t a = t >= o ? part[t - o] : 0u;
-    __syncthreads();
-    part[t] += a;
-    __syncthreads();
-  }
-  if (i < n) out[i] = part[t] - v;
-  if (t == 1023) sums[blockIdx.x] = part[t];
-}
-__global__ void __launch_bounds__(1024) k_scan_live_add(uint32_t* __restrict__ out,
-                                                        const unsigned long long* __restrict__ nptr,
-                                                        const uint32_t* __restrict__ sums, int64_t nb,
-                                                        uint32_t* __restrict__ total) {
-  int64_t n = (int64_t)*nptr;
-  int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
-  if (i < n) out[i] += sums[blockIdx.x];
-  if (i == 0) *total = sums[nb];
 }
 
 // statsUpdate (SPPM.hs:258-279)
@@ -730,18 +707,12 @@ SpPhotons carvePhotons(void* base, size_t cap) {
   w += 4 * cap;
   p.gwi = (float4*)w;
   w += 4 * cap;
-  p.cnt = (uint32_t*)w;
-  w += cap + 64;  // counts, then the total at [cap]
   p.live[0] = (int32_t*)w;
   w += cap;
   p.live[1] = (int32_t*)w;
-  w += cap;
-  p.sums = (uint32_t*)w;  // block sums of the count scan: cap / 1024 + 1 entries
   return p;
 }
-size_t photonBytes(size_t cap) {
-  return 4 * (cap * (16 + 16 + 8 + 4 + 4 + 4 + 1 + 2) + 64 + cap / 1024 + 64);
-}
+size_t photonBytes(size_t cap) { return 4 * cap * (16 + 16 + 8 + 4 + 4 + 4 + 2); }
 
 size_t round64(size_t n) { return (std::max<size_t>(n, 64) + 63) / 64 * 64; }
 
@@ -762,7 +733,6 @@ void sppm_workspace_free(SppmWorkspace& ws) {
   cudaFree(ws.buckets);
   cudaFree(ws.entries);
   cudaFree(ws.photons);
-  cudaFree(ws.pairs);
   cudaFree(ws.counters);
   ws = SppmWorkspace{};
 }
@@ -961,9 +931,6 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
     unsigned g_pt = wide ? residentGrid(k_sp_ptrace<true>, sms, block)
                          : residentGrid(k_sp_ptrace<false>, sms, block);
     unsigned g_vx = residentGrid(k_sp_vertex, sms, block);
-    unsigned g_sp = residentGrid(k_sp_splat, sms, block);
-    const size_t cap_n = ws.photon_cap;
-    uint32_t* total = ph.cnt + cap_n;
     for (int64_t base = 0; base < nphot; base += (int64_t)ws.photon_cap) {
       int64_t count = std::min<int64_t>((int64_t)ws.photon_cap, nphot - base);
       Q.chunk_base = (uint64_t)base;
@@ -975,7 +942,6 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
       for (int depth = 0;; depth++) {
         int in = depth & 1;
         unsigned cap_blocks = (unsigned)std::max<int64_t>(1, (n_cur + block - 1) / block);
-        unsigned nb = (unsigned)std::max<int64_t>(1, (n_cur + 1023) / 1024);
         k_sp_preset<<<1, 32, 0, stream>>>(counters, S_PLIVE0 + (1 - in));
         if (wide)
           k_sp_ptrace<true><<<std::min(g_pt, cap_blocks), block, 0, stream>>>(A, ph, in, counters);
@@ -984,34 +950,14 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
         k_sp_vertex<<<std::min(g_vx, cap_blocks), block, 0, stream>>>(A, S, Q, ph, hp, hs, in, depth,
                                                                      counters);
         unsigned warp_blocks = (unsigned)std::max<int64_t>(1, (n_cur + 3) / 4);  // 4 warps a block
-        k_sp_gather<true><<<std::min(g_wide * 2, warp_blocks), block, 0, stream>>>(ph, hs, in, ph.cnt,
-                                                                                nullptr, counters);
-        // the pairs' offsets: a prefix sum of the live entries' counts, in place
-        k_scan_live<<<nb, 1024, 0, stream>>>(ph.cnt, ph.cnt, counters + S_PLIVE0 + in, ph.sums);
-        k_scan_sums<<<1, 1024, 0, stream>>>(ph.sums, (int64_t)nb);
-        k_scan_live_add<<<nb, 1024, 0, stream>>>(ph.cnt, counters + S_PLIVE0 + in, ph.sums,
-                                                 (int64_t)nb, total);
+        k_sp_gather<<<std::min(g_wide * 2, warp_blocks), kGatherBlock, 0, stream>>>(
+            S, P, ph, hp, hs, in, depth, d_splat, px.m, px.count, counters);
         RET_CUDA(cudaGetLastError());
-        uint32_t tp = 0;
-        unsigned long long live = 0;
-        RET_CUDA(cudaMemcpyAsync(&tp, total, sizeof tp, cudaMemcpyDeviceToHost, stream));
-        RET_CUDA(cudaMemcpyAsync(&live, counters + S_PLIVE0 + (1 - in), sizeof live,
-                                 cudaMemcpyDeviceToHost, stream));
-        RET_CUDA(cudaStreamSynchronize(stream));
-        if (tp > 0) {
-          if (ws.pair_cap < tp) {
-            size_t have = ws.pairs ? 8 * ws.pair_cap : 0;
-            size_t want = std::max<size_t>(2 * (size_t)tp, cap_n);
-            RET_CUDA(growTo(ws.pairs, have, 8 * want));
-            ws.pair_cap = want;
-          }
-          int2* pairs = (int2*)ws.pairs;
-          k_sp_gather<false><<<std::min(g_wide * 2, warp_blocks), block, 0, stream>>>(ph, hs, in, ph.cnt,
-                                                                                   pairs, counters);
-          unsigned gsp = std::min<unsigned>(g_sp, (unsigned)((tp + block - 1) / block));
-          k_sp_splat<<<gsp, block, 0, stream>>>(S, P, ph, hp, depth, pairs, total, d_splat, px.m,
-                                                px.count, counters);
-          RET_CUDA(cudaGetLastError());
+        unsigned long long live = (unsigned long long)n_cur;
+        if (depth >= 3 && (depth & 3) == 3) {  // the live count, every fourth bounce
+          RET_CUDA(cudaMemcpyAsync(&live, counters + S_PLIVE0 + (1 - in), sizeof live,
+                                   cudaMemcpyDeviceToHost, stream));
+          RET_CUDA(cudaStreamSynchronize(stream));
         }
         if (live == 0) break;
         n_cur = (int64_t)live;

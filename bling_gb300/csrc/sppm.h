@@ -43,8 +43,6 @@ struct SppmWorkspace {
   size_t entry_cap = 0;
   void* photons = nullptr;  // photon slots
   size_t photon_cap = 0;
-  void* pairs = nullptr;    // (photon, hit point) pairs of one photon vertex
-  size_t pair_cap = 0;
   unsigned long long* counters = nullptr;
 };
 
