@@ -24,6 +24,7 @@ FLAG_WIDE_BVH = 1
 
 MAT_MATTE, MAT_PLASTIC, MAT_METAL, MAT_GLASS, MAT_MIRROR = 0, 1, 2, 3, 4
 MAT_SHINY_METAL, MAT_TRANS_MATTE = 5, 6
+MAT_SUBSTRATE, MAT_BLACKBODY = 7, 8  # substrate: ka in kt, urough in roughness, vrough in sigma, depth in ior
 SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_DISK, SHAPE_CYLINDER = 0, 1, 2, 3, 4
 LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE = 0, 1, 2
 FILTER_BOX, FILTER_GAUSS, FILTER_MITCHELL, FILTER_SINC, FILTER_TRIANGLE = 0, 1, 2, 3, 4

@@ -565,9 +565,20 @@ class _Parser:
             kt = self._spectrum_texture("kt")
             ks = self._scalar_texture("ks")
             return sc.add_material(abi.MAT_TRANS_MATTE, kd=kr, kt=kt, sigma=float(ks))
-        if kind in ("blackbody", "bumpMap", "substrate"):
-            raise Unsupported(f"material {kind}: the GPU path renders matte, plastic, metal, "
-                              "glass, mirror, shinyMetal and transMatte")
+        if kind == "substrate":  # pSubstrateMaterial (MaterialParser.hs:50-58)
+            kd = self._spectrum_texture("kd")
+            ks = self._spectrum_texture("ks")
+            ka = self._spectrum_texture("ka")
+            ur = self._scalar_texture("urough")
+            vr = self._scalar_texture("vrough")
+            depth = self._scalar_texture("depth")
+            return sc.add_material(abi.MAT_SUBSTRATE, kd=kd, ks=ks, kt=ka, roughness=float(ur),
+                                   sigma=float(vr), ior=float(depth))
+        if kind == "blackbody":
+            return sc.add_material(abi.MAT_BLACKBODY)
+        if kind == "bumpMap":
+            raise Unsupported(f"material {kind}: the GPU path renders constant materials without "
+                              "bump maps")
         raise t.error(f"unknown material type {kind}")
 
     def p_emission(self):

@@ -48,6 +48,19 @@ inline void deriveMaterialSpectra(DMaterial& m) {
       m.kt[i] = ghcClamp(m.kt[i], 0.0f, 1.0f) * (1.0f - r);
       m.kd[i] = r;
     }
+  } else if (m.kind == BLING_MAT_SUBSTRATE) {
+    // mkSubstrate (Material.hs:111-127): rd, rs, ra = sClamp 0 1 of kd, ks,
+    // ka (in kt); mkAnisotropic (1 / u) (1 / v) with u, v = max 0 of the
+    // roughnesses; the exponents go to rough (ex) and sigma (ey)
+    for (int i = 0; i < 16; i++) {
+      m.kd[i] = ghcClamp(m.kd[i], 0.0f, 1.0f);
+      m.ks[i] = ghcClamp(m.ks[i], 0.0f, 1.0f);
+      m.kt[i] = ghcClamp(m.kt[i], 0.0f, 1.0f);
+    }
+    float u = 0.0f <= m.rough ? m.rough : 0.0f, v = 0.0f <= m.sigma ? m.sigma : 0.0f;
+    float ex = 1.0f / u, ey = 1.0f / v;
+    m.rough = (ex > 10000 || std::isnan(ex)) ? 10000.0f : ex;  // fixExponent (Microfacet.hs:199-201)
+    m.sigma = (ey > 10000 || std::isnan(ey)) ? 10000.0f : ey;
   }
 }
 

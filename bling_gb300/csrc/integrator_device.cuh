@@ -304,7 +304,7 @@ __device__ __forceinline__ V3 toSameHemisphere(V3 wo, V3 wi) {
   return wo.z < 0 ? V3{wi.x, wi.y, -wi.z} : wi;
 }
 
-enum { BX_LAMBERT, BX_OREN, BX_SPEC_REFL, BX_SPEC_TRANS, BX_MICRO };
+enum { BX_LAMBERT, BX_OREN, BX_SPEC_REFL, BX_SPEC_TRANS, BX_MICRO, BX_FBLEND };
 enum { T_REFL = 1, T_TRANS = 2, T_DIFF = 4, T_GLOSSY = 8, T_SPEC = 16 };
 enum { FR_NOOP, FR_DIEL, FR_COND };
 
@@ -397,6 +397,65 @@ __device__ __forceinline__ float orenNayarScale(const BxDF& b, V3 wo, V3 wi) {
   return b.A + b.B * maxcos * sina * tanb;
 }
 
+// the Anisotropic microfacet distribution (Microfacet.hs:136-192): ex, ey
+__device__ __forceinline__ float anisoPdf(float ex, float ey, V3 wh) {
+  float costh = absCosTheta(wh);
+  float e = (ex * wh.x * wh.x + ey * wh.y * wh.y) / hmax(0.0f, 1.0f - costh * costh);
+  return sqrtf((ex + 1.0f) * (ey + 1.0f)) * kInvTwoPi * powf(costh, e);
+}
+__device__ __forceinline__ float anisoD(float ex, float ey, V3 wh) {
+  float costh = absCosTheta(wh);
+  float d = 1.0f - costh * costh;
+  if (d == 0) return 0;
+  float e = (ex * wh.x * wh.x + ey * wh.y * wh.y) / d;
+  return sqrtf((ex + 2.0f) * (ey + 2.0f)) * kInvTwoPi * powf(costh, e);
+}
+__device__ __forceinline__ void anisoSample(float ex, float ey, float u1, float u2, V3& wh,
+                                            float& pdf) {
+  float phi, cost;
+  auto quad = [&](float up, int which) {
+    float p = ex == ey ? kPi * up * 0.5f : atanf(sqrtf((ex + 1.0f) / (ey + 1.0f)) * tanf(kPi * up * 0.5f));
+    float cp = cosf(p), sp = sinf(p);
+    cost = powf(u2, 1.0f / (ex * cp * cp + ey * sp * sp + 1.0f));
+    phi = which == 0 ? p : (which == 1 ? kPi - p : (which == 2 ? p + kPi : 2.0f * kPi - p));
+  };
+  if (u1 < 0.25f)
+    quad(4.0f * u1, 0);
+  else if (u1 < 0.5f)
+    quad(4.0f * (0.5f - u1), 1);
+  else if (u1 < 0.75f)
+    quad(4.0f * (u1 - 0.5f), 2);
+  else
+    quad(4.0f * (1.0f - u1), 3);
+  float sint = sqrtf(hmax(0.0f, 1.0f - cost * cost));
+  wh = V3{sint * cosf(phi), sint * sinf(phi), cost};
+  float ds = 1.0f - cost * cost;
+  float e = (ex * wh.x * wh.x + ey * wh.y * wh.y) / ds;
+  float f = kInvTwoPi * powf(cost, e);
+  pdf = sqrtf((ex + 1.0f) * (ey + 1.0f)) * f;
+}
+// FresnelBlend's e wo wi (Microfacet.hs:63-86): rd in r, rs in eta, ra in k,
+// the distribution's exponents in A and B, the coating depth in e
+__device__ __forceinline__ Spec fblendEval(const BxDF& b, V3 wo, V3 wi) {
+  float costi = absCosTheta(wi), costo = absCosTheta(wo);
+  Spec rd = sLoad(b.r), rs = sLoad(b.eta), ra = sLoad(b.k);
+  Spec a = sConst(1.0f);
+  if (b.e > 0) {
+    float x = -(b.e * (costi + costo) / (costi * costo));
+#pragma unroll
+    for (int i = 0; i < 16; i++) a.v[i] = expf(ra.v[i] * x);
+  }
+  float ds = ((costo * 28.0f / 23.0f) * kPi) * (1.0f - powf(1.0f - 0.5f * costi, 5.0f)) *
+             (1.0f - powf(1.0f - 0.5f * costo, 5.0f));
+  Spec diff = sScale(a * rd * (sConst(1.0f) - rs), ds);
+  V3 wh = normalize(wi + wo);
+  if (wh.z < 0) wh = -wh;
+  float costih = absDot(wi, wh);
+  Spec schlick = rs + sScale(sConst(1.0f) - rs, powf(1.0f - costih, 5.0f));
+  Spec spec = sScale(schlick, anisoD(b.A, b.B, wh) * costo / (4.0f * costih * hmax(costi, costo)));
+  return diff + spec;
+}
+
 // bxdfEval b wo wi
 // Inlining of the BSDF, geometry and light helpers below is left to the
 // compiler: keeping them out of line (__noinline__) measured 18% slower in
@@ -420,6 +479,7 @@ static __device__ BLING_OUTLINE Spec bxEval(const BxDF& b, V3 wo, V3 wi) {
       float x = blinnD(b.e, wh) * mfG(wo, wi, wh) / (4.0f * costi);
       return sScale(rTimesFresnel(b, costh), x);
     }
+    case BX_FBLEND: return fblendEval(b, wo, wi);
     default: return sConst(0);
   }
 }
@@ -434,6 +494,12 @@ static __device__ BLING_OUTLINE float bxPdfBrdf(const BxDF& b, V3 wo, V3 wi) {
       V3 wh = normalize(whp);
       if (cosTheta(wh) < 0) return 0;
       return blinnPdf(b.e, wh) / (4.0f * absDot(wo, wh));
+    }
+    case BX_FBLEND: {  // Microfacet.hs:104-108
+      if (!sameHemisphere(wo, wi)) return 0;
+      V3 wh = normalize(wi + wo);
+      if (wh.z < 0) wh = -wh;
+      return 0.5f * (absCosTheta(wi) * kInvPi + anisoPdf(b.A, b.B, wh) / (4.0f * absDot(wo, wh)));
     }
     default: return 0;
   }
@@ -471,6 +537,27 @@ static __device__ BLING_OUTLINE void bxSampleBrdf(const BxDF& b, V3 wo, float u1
       wi = V3{-wo.x, -wo.y, wo.z};
       pdf = 1;
       return;
+    case BX_FBLEND: {  // Microfacet.hs:88-102
+      V3 wh;
+      float pdfp;
+      if (u1 < 0.5f) {
+        wi = toSameHemisphere(wo, cosineSampleHemisphere(u1 * 2.0f, u2));
+        wh = normalize(wi + wo);
+        if (wh.z < 0) wh = -wh;
+        pdfp = anisoPdf(b.A, b.B, wh);
+      } else {
+        anisoSample(b.A, b.B, 2.0f * (u1 - 0.5f), u2, wh, pdfp);
+        wi = sv(2.0f * dot(wo, wh), wh) - wo;
+      }
+      if (pdfp == 0) {
+        f = sConst(0);
+        pdf = 0;
+        return;
+      }
+      pdf = 0.5f * (absCosTheta(wi) * kInvPi + pdfp / (4.0f * absDot(wo, wh)));
+      f = sScale(Adj ? fblendEval(b, wi, wo) : fblendEval(b, wo, wi), 1.0f / pdf);
+      return;
+    }
     case BX_SPEC_TRANS: {
       bool entering = cosTheta(wo) > 0;
       float ei = entering ? b.ei : b.et, et = entering ? b.et : b.ei;
@@ -621,6 +708,20 @@ static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ 
     y.r = m.kt;
     y.btdf = true;
     b.c[b.n++] = y;
+  } else if (kind == BLING_MAT_SUBSTRATE) {
+    // mkSubstrate (Material.hs:111-127): one FresnelBlend lobe; the clamped
+    // spectra and the anisotropic exponents are derived at upload
+    x.kind = BX_FBLEND;
+    x.type = T_REFL | T_GLOSSY;
+    x.r = m.kd;
+    x.eta = m.ks;
+    x.k = m.kt;
+    x.A = m.rough;
+    x.B = m.sigma;
+    x.e = m.ior;
+    b.c[b.n++] = x;
+  } else if (kind == BLING_MAT_BLACKBODY) {
+    // blackBodyMaterial (Reflection.hs:337-338): no BxDFs
   } else if (kind == BLING_MAT_MIRROR) {
     // mirrorMaterial: specRefl frNoOp (sClamp 0 1 kr) (Material.hs:68-72)
     x.kind = BX_SPEC_REFL;

@@ -204,7 +204,7 @@ __device__ __forceinline__ void queueAppend(bool live, int slot, int32_t* __rest
 // then run one BSDF's and one geometry's code instead of all of them in turn.
 // The order within a class is the queue's order, up to the interleaving of
 // warps.
-constexpr int kMaterialKinds = 7;  // BLING_MAT_MATTE .. BLING_MAT_TRANS_MATTE
+constexpr int kMaterialKinds = 7;  // BLING_MAT_MATTE .. BLING_MAT_TRANS_MATTE; substrate sorts with plastic
 constexpr int kShadeClasses = 1 + 2 * kMaterialKinds;
 static_assert(kShadeClasses <= 16, "class counts and cursors hold 16 entries each");
 
@@ -218,7 +218,10 @@ __device__ __forceinline__ int shadeClass(const DevAccel& A, const DevShading& S
     mi = A.shapes[~info.x].material;
     shape = 1;
   }
-  return 1 + S.materials[mi].kind + kMaterialKinds * shape;
+  int kind = S.materials[mi].kind;
+  if (kind == BLING_MAT_SUBSTRATE) kind = BLING_MAT_PLASTIC;  // both glossy, one class
+  if (kind == BLING_MAT_BLACKBODY) kind = BLING_MAT_MATTE;    // no BxDF: the path ends
+  return 1 + kind + kMaterialKinds * shape;
 }
 
 // counts a warp's entries per class (one atomic per class present); every

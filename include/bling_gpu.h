@@ -73,7 +73,10 @@ enum {
   BLING_MAT_GLASS = 3,   /* glassMaterial ior kr kt     (Material.hs:252-262) */
   BLING_MAT_MIRROR = 4,  /* mirrorMaterial kr: kr in ks (Material.hs:68-72) */
   BLING_MAT_SHINY_METAL = 5, /* mkShinyMetal kr ks rough: kr in kd (Material.hs:98-109) */
-  BLING_MAT_TRANS_MATTE = 6  /* translucentMatte kr kt ks: kr in kd, ks in sigma (Material.hs:43-53) */
+  BLING_MAT_TRANS_MATTE = 6, /* translucentMatte kr kt ks: kr in kd, ks in sigma (Material.hs:43-53) */
+  BLING_MAT_SUBSTRATE = 7,   /* mkSubstrate kd ks ka urough vrough depth: ka in kt, urough in
+                                roughness, vrough in sigma, depth in ior (Material.hs:111-127) */
+  BLING_MAT_BLACKBODY = 8    /* blackBodyMaterial: a BSDF without components (Reflection.hs:337-338) */
 };
 
 typedef struct bling_material {

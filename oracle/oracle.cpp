@@ -532,7 +532,7 @@ struct Mesh {
   int material;
 };
 
-enum BxKind { BX_LAMBERT, BX_OREN, BX_SPEC_REFL, BX_SPEC_TRANS, BX_MICRO };
+enum BxKind { BX_LAMBERT, BX_OREN, BX_SPEC_REFL, BX_SPEC_TRANS, BX_MICRO, BX_FBLEND };
 enum { T_REFL = 1, T_TRANS = 2, T_DIFF = 4, T_GLOSSY = 8, T_SPEC = 16 };
 enum FrKind { FR_NOOP, FR_DIEL, FR_COND };
 
@@ -551,6 +551,7 @@ struct BxDF {
   float e;          // Blinn exponent
   Fresnel fr;
   bool btdf;        // brdfToBtdf (Reflection.hs:188-195)
+  Spec rs, ra;      // FresnelBlend: specular, absorption (rd in r; ex, ey in A, B; depth in e)
 };
 static inline V otherHemisphere(V w) { return V{w.x, w.y, -w.z}; }
 
@@ -1138,6 +1139,65 @@ static Spec orenNayar(const BxDF& b, V wo, V wi) {
 }
 
 // bxdfEval b wo wi; a BTDF evaluates its BRDF at the mirrored wi
+// the Anisotropic distribution (Microfacet.hs:136-192)
+static float anisoPdf(float ex, float ey, V wh) {
+  float costh = absCosTheta(wh);
+  float e = (ex * wh.x * wh.x + ey * wh.y * wh.y) / hmax(0.0f, 1.0f - costh * costh);
+  return sqrtf((ex + 1.0f) * (ey + 1.0f)) * INV_TWO_PI * powf(costh, e);
+}
+static float anisoD(float ex, float ey, V wh) {
+  float costh = absCosTheta(wh);
+  float d = 1.0f - costh * costh;
+  if (d == 0) return 0;
+  float e = (ex * wh.x * wh.x + ey * wh.y * wh.y) / d;
+  return sqrtf((ex + 2.0f) * (ey + 2.0f)) * INV_TWO_PI * powf(costh, e);
+}
+static void anisoSample(float ex, float ey, float u1, float u2, V& wh, float& pdf) {
+  auto quad = [&](float up, float& p, float& c) {
+    p = ex == ey ? PI * up * 0.5f : atanf(sqrtf((ex + 1.0f) / (ey + 1.0f)) * tanf(PI * up * 0.5f));
+    float cp = cosf(p), sp = sinf(p);
+    c = powf(u2, 1.0f / (ex * cp * cp + ey * sp * sp + 1.0f));
+  };
+  float p, cost, phi;
+  if (u1 < 0.25f) {
+    quad(4.0f * u1, p, cost);
+    phi = p;
+  } else if (u1 < 0.5f) {
+    quad(4.0f * (0.5f - u1), p, cost);
+    phi = PI - p;
+  } else if (u1 < 0.75f) {
+    quad(4.0f * (u1 - 0.5f), p, cost);
+    phi = p + PI;
+  } else {
+    quad(4.0f * (1.0f - u1), p, cost);
+    phi = TWO_PI - p;
+  }
+  float sint = sqrtf(hmax(0.0f, 1.0f - cost * cost));
+  wh = V{sint * cosf(phi), sint * sinf(phi), cost};  // sphericalDirection
+  float ds = 1.0f - cost * cost;
+  float e = (ex * wh.x * wh.x + ey * wh.y * wh.y) / ds;
+  float f = INV_TWO_PI * powf(cost, e);
+  pdf = sqrtf((ex + 1.0f) * (ey + 1.0f)) * f;
+}
+// mkFresnelBlend's e wo wi (Microfacet.hs:63-86)
+static Spec fblendEval(const BxDF& b, V wo, V wi) {
+  float costi = absCosTheta(wi), costo = absCosTheta(wo);
+  Spec a = WHITE;
+  if (b.e > 0) {
+    float x = -(b.e * (costi + costo) / (costi * costo));
+    for (int i = 0; i < 16; i++) a.v[i] = expf(b.ra.v[i] * x);
+  }
+  float ds = ((costo * 28.0f / 23.0f) * PI) * (1.0f - powf(1.0f - 0.5f * costi, 5.0f)) *
+             (1.0f - powf(1.0f - 0.5f * costo, 5.0f));
+  Spec diff = sScale(a * b.r * (WHITE - b.rs), ds);
+  V wh = normalize(wi + wo);
+  if (wh.z < 0) wh = -wh;
+  float costih = absDot(wi, wh);
+  Spec schlick = b.rs + sScale(WHITE - b.rs, powf(1.0f - costih, 5.0f));
+  Spec spec = sScale(schlick, anisoD(b.A, b.B, wh) * costo / (4.0f * costih * hmax(costi, costo)));
+  return diff + spec;
+}
+
 static Spec bxEval(const BxDF& b, V wo, V wi) {
   if (b.btdf) wi = otherHemisphere(wi);
   switch (b.kind) {
@@ -1154,6 +1214,7 @@ static Spec bxEval(const BxDF& b, V wo, V wi) {
       float x = blinnD(b.e, wh) * mfG(wo, wi, wh) / (4.0f * costi);
       return sScale(b.r * frEval(b.fr, costh), x);
     }
+    case BX_FBLEND: return fblendEval(b, wo, wi);
     default: return BLACK;  // specular: e _ _ = black
   }
 }
@@ -1168,6 +1229,12 @@ static float bxPdfBrdf(const BxDF& b, V wo, V wi) {
       V wh = normalize(whp);
       if (cosTheta(wh) < 0) return 0;
       return blinnPdf(b.e, wh) / (4.0f * absDot(wo, wh));
+    }
+    case BX_FBLEND: {  // Microfacet.hs:104-108
+      if (!sameHemisphere(wo, wi)) return 0;
+      V wh = normalize(wi + wo);
+      if (wh.z < 0) wh = -wh;
+      return 0.5f * (absCosTheta(wi) * INV_PI + anisoPdf(b.A, b.B, wh) / (4.0f * absDot(wo, wh)));
     }
     default: return 0;
   }
@@ -1210,6 +1277,27 @@ static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi
         f = BLACK;
         pdf = 0;
       }
+      return;
+    }
+    case BX_FBLEND: {  // Microfacet.hs:88-102
+      V wh;
+      float pdfp;
+      if (u1 < 0.5f) {
+        wi = toSameHemisphere(wo, cosineSampleHemisphere(u1 * 2.0f, u2));
+        wh = normalize(wi + wo);
+        if (wh.z < 0) wh = -wh;
+        pdfp = anisoPdf(b.A, b.B, wh);
+      } else {
+        anisoSample(b.A, b.B, 2.0f * (u1 - 0.5f), u2, wh, pdfp);
+        wi = sv(2.0f * dot(wo, wh), wh) - wo;
+      }
+      if (pdfp == 0) {
+        f = BLACK;
+        pdf = 0;
+        return;
+      }
+      pdf = 0.5f * (absCosTheta(wi) * INV_PI + pdfp / (4.0f * absDot(wo, wh)));
+      f = sScale(adj ? fblendEval(b, wi, wo) : fblendEval(b, wo, wi), 1.0f / pdf);
       return;
     }
     case BX_SPEC_REFL: {  // Specular.hs:86-87
@@ -1355,6 +1443,21 @@ static Bsdf materialBsdf(const Material& m, const DG& dgg, const DG& dgs) {
       y.fr.eta = frApproxEta(m.kd);  // kr
       y.fr.k = frApproxK(m.kd);
       add(y);
+      break;
+    }
+    case BLING_MAT_BLACKBODY:  // blackBodyMaterial (Reflection.hs:337-338): no BxDFs
+      break;
+    case BLING_MAT_SUBSTRATE: {  // mkSubstrate kd ks ka u v depth (Material.hs:111-127)
+      x.kind = BX_FBLEND;
+      x.type = T_REFL | T_GLOSSY;
+      x.r = sClamp(0, 1, m.kd);
+      x.rs = sClamp(0, 1, m.ks);
+      x.ra = sClamp(0, 1, m.kt);  // ka
+      float u = hmax(0.0f, m.rough), v = hmax(0.0f, m.sigma);
+      x.A = fixExponent(1.0f / u);  // mkAnisotropic (1 / u) (1 / v)
+      x.B = fixExponent(1.0f / v);
+      x.e = m.ior;  // coating depth
+      add(x);
       break;
     }
     case BLING_MAT_TRANS_MATTE: {  // translucentMatte kr kt ks (Material.hs:43-53)

@@ -153,6 +153,17 @@ def test_shiny_metal_and_translucent_matte():
     assert np.array_equal(np.asarray(trans.kt, F), rgb_to_spectrum((F(0.5), F(0.5), F(0.5))))
 
 
+def test_substrate_and_blackbody():
+    j = B.parse("material { substrate kd { constant rgbR 0.5 0.4 0.3 } ks { constant rgbR 0.2 0.2 0.2 } "
+                "ka { constant rgbR 0.1 0.1 0.1 } urough { constant 0.05 } vrough { constant 0.2 } "
+                "depth { constant 0.5 } } prim { shape { sphere radius 1 } } "
+                "material { blackbody } prim { shape { sphere radius 1 } }")
+    sub, bb = j.scene.materials
+    assert sub.kind == abi.MAT_SUBSTRATE and bb.kind == abi.MAT_BLACKBODY
+    assert (sub.roughness, sub.sigma, sub.ior) == (float(F(0.05)), float(F(0.2)), float(F(0.5)))
+    assert np.array_equal(np.asarray(sub.kt, F), rgb_to_spectrum((F(0.1), F(0.1), F(0.1))))
+
+
 def test_constant_spd_gives_a_flat_spectrum():
     s = B.spectrum_from_spd([(380.0, 0.25), (500.0, 0.25), (720.0, 0.25)])
     assert np.array_equal(s, constant(0.25))
@@ -173,9 +184,8 @@ def test_other_renderers_parse_and_are_named():
 
 
 @pytest.mark.parametrize("src,what", [
-    ("material { substrate kd { constant rgbR 1 1 1 } ks { constant rgbR 1 1 1 } "
-     "ka { constant rgbR 0 0 0 } urough { constant 0.1 } vrough { constant 0.1 } "
-     "depth { constant 0 } }", "substrate"),
+    ("material { bumpMap { scale 0.1 tex { constant 1 } } material { matte kd { constant 1 } "
+     "sigma { constant 0 } } }", "bumpMap"),
     ("material { matte kd { checker 1 1 1 tex1 { constant rgbR 1 1 1 } "
      "tex2 { constant rgbR 0 0 0 } } sigma { constant 0 } }", "checker"),
     ("prim { julia c 0 0 0 0 epsilon 0.1 iterations 4 }", "julia"),

@@ -177,3 +177,16 @@ def test_camera_without_world_to_raster_is_refused(gpu_ctx):
     film = gpu_ctx.film(16, 16)
     with pytest.raises(Exception, match="world-to-raster"):
         g.light_pass(film, 1000)
+
+
+def test_substrate_light_pass_vs_oracle(gpu_ctx):
+    """adjoint sampling of the FresnelBlend lobe (e wi wo, Microfacet.hs:92)
+    and a blackbody sphere that ends photons"""
+    sc = _lights_materials_scene()
+    sub = sc.add_material(abi.MAT_SUBSTRATE, kd=rgb_to_spectrum((0.6, 0.3, 0.2)), ks=constant(0.2),
+                          kt=rgb_to_spectrum((0.2, 0.1, 0.1)), roughness=0.03, sigma=0.3, ior=0.2)
+    sc.shapes[0].material = sub
+    sc.shapes[6].material = sc.add_material(abi.MAT_BLACKBODY)
+    film, g, so, st = _both(gpu_ctx, sc, 64, 48, 300_000, seed=8)
+    _compare(film.read_splats(), so, rel=2e-3, frac=0.9)
+    _counts_close(g.stats(), st[0], 300_000)

@@ -307,3 +307,23 @@ def test_passes_accumulate(gpu_ctx):
     fg, fo, st_g, _ = _render_both(gpu_ctx, sc, p, passes=3)
     _compare(fg, fo, exact_weights=True)
     assert st_g["path_samples"] == 3 * 34 * 34 * 4
+
+
+def test_substrate_and_blackbody_vs_oracle(gpu_ctx):
+    """mkSubstrate (FresnelBlend with the anisotropic microfacet distribution,
+    with and without a coating depth) and blackBodyMaterial (no BxDFs: paths
+    end there)"""
+    sc = _materials_scene()
+    sub = sc.add_material(abi.MAT_SUBSTRATE, kd=rgb_to_spectrum((0.6, 0.3, 0.2)), ks=constant(0.15),
+                          kt=constant(0.0), roughness=0.05, sigma=0.05, ior=0.0)
+    aniso = sc.add_material(abi.MAT_SUBSTRATE, kd=rgb_to_spectrum((0.2, 0.4, 0.6)),
+                            ks=constant(0.3), kt=rgb_to_spectrum((0.3, 0.1, 0.1)), roughness=0.02,
+                            sigma=0.4, ior=0.3)
+    black = sc.add_material(abi.MAT_BLACKBODY)
+    sc.shapes[0].material = sub     # the plastic sphere
+    sc.shapes[1].material = aniso   # the metal sphere
+    sc.shapes[3].material = black   # the matte sphere
+    p = S.render_params(64, 64, (3, 3), max_depth=6, sample_depth=2, rr_depth=2, seed=17)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p)
+    _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
+    assert st_g["nonfinite_drops"] == 0
