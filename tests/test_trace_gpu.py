@@ -288,7 +288,7 @@ def test_mesh_validation(gpu_ctx, bad):
 def test_unknown_material_kind_is_refused(gpu_ctx):
     s = S.Scene()
     m = s.add_material(abi.MAT_MATTE, kd=constant(0.5))
-    s.materials[m].kind = 7
+    s.materials[m].kind = 9
     s.add_shape(abi.SHAPE_SPHERE, (1.0,), xf.identity(), m)
     with pytest.raises(BlingError) as e:
         gpu_ctx.scene(s)
