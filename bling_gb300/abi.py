@@ -40,7 +40,11 @@ class Opts(C.Structure):
 class Material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("sigma", C.c_float), ("roughness", C.c_float),
                 ("ior", C.c_float), ("kd", F16), ("ks", F16), ("kt", F16), ("eta", F16),
-                ("k", F16)]
+                ("k", F16), ("kd_texture", C.c_int32), ("kd_tex_scale", C.c_float * 3),
+                ("kd2", F16)]
+
+
+TEX_CONSTANT, TEX_CHECKER = 0, 1
 
 
 class MeshDesc(C.Structure):

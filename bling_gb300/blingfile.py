@@ -504,16 +504,29 @@ class _Parser:
         return (self.t.flt(), self.t.flt(), self.t.flt())
 
     # -- materials (MaterialParser.hs) ----------------------------------
-    def _spectrum_texture(self, name) -> np.ndarray:
+    def _spectrum_texture(self, name, checker=False):
+        """a constant spectrum texture; with checker=True also `checker sx sy
+        sz tex1 {constant ..} tex2 {constant ..}` (checkerBoard,
+        MaterialParser.hs:209), returned as (tex1, ((sx, sy, sz), tex2))"""
         t = self.t
 
         def body():
             kind = t.word()
+            if kind == "checker" and checker:
+                scale = t.vec()
+                t1 = self._spectrum_texture("tex1")
+                t2 = self._spectrum_texture("tex2")
+                return (t1, (tuple(scale), t2))
             if kind != "constant":
                 raise Unsupported(f"texture {kind} ({name}): the GPU path renders constant "
-                                  "textures")
+                                  "textures and checkerboard diffuse colours")
             return self.p_spectrum()
         return t.named_block(name, body)
+
+    @staticmethod
+    def _kd(v):
+        """(kd, kd_checker) of a kd texture"""
+        return v if isinstance(v, tuple) else (v, None)
 
     def _scalar_texture(self, name) -> np.float32:
         t = self.t
@@ -534,14 +547,15 @@ class _Parser:
         kind = t.word()
         sc = self.scene
         if kind == "matte":
-            kd = self._spectrum_texture("kd")
+            kd, chk = self._kd(self._spectrum_texture("kd", checker=True))
             sig = self._scalar_texture("sigma")
-            return sc.add_material(abi.MAT_MATTE, kd=kd, sigma=float(sig))
+            return sc.add_material(abi.MAT_MATTE, kd=kd, sigma=float(sig), kd_checker=chk)
         if kind == "plastic":
-            kd = self._spectrum_texture("kd")
+            kd, chk = self._kd(self._spectrum_texture("kd", checker=True))
             ks = self._spectrum_texture("ks")
             rough = self._scalar_texture("rough")
-            return sc.add_material(abi.MAT_PLASTIC, kd=kd, ks=ks, roughness=float(rough))
+            return sc.add_material(abi.MAT_PLASTIC, kd=kd, ks=ks, roughness=float(rough),
+                                   kd_checker=chk)
         if kind == "metal":
             eta = self._spectrum_texture("eta")
             k = self._spectrum_texture("k")
@@ -566,14 +580,14 @@ class _Parser:
             ks = self._scalar_texture("ks")
             return sc.add_material(abi.MAT_TRANS_MATTE, kd=kr, kt=kt, sigma=float(ks))
         if kind == "substrate":  # pSubstrateMaterial (MaterialParser.hs:50-58)
-            kd = self._spectrum_texture("kd")
+            kd, chk = self._kd(self._spectrum_texture("kd", checker=True))
             ks = self._spectrum_texture("ks")
             ka = self._spectrum_texture("ka")
             ur = self._scalar_texture("urough")
             vr = self._scalar_texture("vrough")
             depth = self._scalar_texture("depth")
             return sc.add_material(abi.MAT_SUBSTRATE, kd=kd, ks=ks, kt=ka, roughness=float(ur),
-                                   sigma=float(vr), ior=float(depth))
+                                   sigma=float(vr), ior=float(depth), kd_checker=chk)
         if kind == "blackbody":
             return sc.add_material(abi.MAT_BLACKBODY)
         if kind == "bumpMap":

@@ -361,7 +361,11 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   if (d->n_materials > 0 && !d->materials)
     return set_err(c, BLING_ERR_INVALID_ARG, "null material array");
   for (int i = 0; i < d->n_materials; i++)
-    if (d->materials[i].kind < BLING_MAT_MATTE || d->materials[i].kind > BLING_MAT_BLACKBODY)
+    if (d->materials[i].kind < BLING_MAT_MATTE || d->materials[i].kind > BLING_MAT_BLACKBODY ||
+        (d->materials[i].kd_texture != BLING_TEX_CONSTANT &&
+         !(d->materials[i].kd_texture == BLING_TEX_CHECKER &&
+           (d->materials[i].kind == BLING_MAT_MATTE || d->materials[i].kind == BLING_MAT_PLASTIC ||
+            d->materials[i].kind == BLING_MAT_SUBSTRATE))))
       return set_err(c, BLING_ERR_INVALID_ARG, "material %d: unknown kind %d", i,
                      d->materials[i].kind);
   for (int i = 0; i < d->n_meshes; i++) {

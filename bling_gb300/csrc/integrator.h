@@ -14,6 +14,9 @@ struct DMaterial {
   int kind;
   float sigma, rough, ior;
   float kd[16], ks[16], kt[16], eta[16], k[16];
+  int kd_tex;           // BLING_TEX_*
+  float kd_scale[3];    // checkerBoard scale
+  float kd2[16];        // the checker's second spectrum
 };
 
 // Spectra a material derives from its constant parameters, once at upload
@@ -54,6 +57,7 @@ inline void deriveMaterialSpectra(DMaterial& m) {
     // roughnesses; the exponents go to rough (ex) and sigma (ey)
     for (int i = 0; i < 16; i++) {
       m.kd[i] = ghcClamp(m.kd[i], 0.0f, 1.0f);
+      m.kd2[i] = ghcClamp(m.kd2[i], 0.0f, 1.0f);
       m.ks[i] = ghcClamp(m.ks[i], 0.0f, 1.0f);
       m.kt[i] = ghcClamp(m.kt[i], 0.0f, 1.0f);
     }

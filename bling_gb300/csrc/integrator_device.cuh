@@ -633,9 +633,16 @@ static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ 
   x.btdf = false;
   int kind = m.kind;
   float sigma = m.sigma, rough = m.rough, ior = m.ior;
+  // the kd texture: checkerBoard (Texture.hs:209-219) at the shading point
+  const float* kd = m.kd;
+  if (m.kd_tex == BLING_TEX_CHECKER) {
+    long long c = (long long)floorf(dgs_p.x * m.kd_scale[0]) + (long long)floorf(dgs_p.y * m.kd_scale[1]) +
+                  (long long)floorf(dgs_p.z * m.kd_scale[2]);
+    if (c % 2 != 0) kd = m.kd2;  // Haskell's mod 2 is 0 for even sums of either sign
+  }
   if (kind == BLING_MAT_MATTE) {
     x.type = T_REFL | T_DIFF;
-    x.r = m.kd;
+    x.r = kd;
     if (sigma == 0) {
       x.kind = BX_LAMBERT;
     } else {
@@ -649,7 +656,7 @@ static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ 
   } else if (kind == BLING_MAT_PLASTIC) {
     x.kind = BX_LAMBERT;
     x.type = T_REFL | T_DIFF;
-    x.r = m.kd;
+    x.r = kd;
     b.c[b.n++] = x;
     BxDF y = x;
     y.kind = BX_MICRO;
@@ -713,7 +720,7 @@ static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ 
     // spectra and the anisotropic exponents are derived at upload
     x.kind = BX_FBLEND;
     x.type = T_REFL | T_GLOSSY;
-    x.r = m.kd;
+    x.r = kd;
     x.eta = m.ks;
     x.k = m.kt;
     x.A = m.rough;

@@ -69,12 +69,19 @@ class Scene:
 
     # --- builders -------------------------------------------------------
     def add_material(self, kind, kd=None, ks=None, kt=None, eta=None, k=None, sigma=0.0,
-                     roughness=0.0, ior=1.5) -> int:
+                     roughness=0.0, ior=1.5, kd_checker=None) -> int:
+        """kd_checker: (scale (sx, sy, sz), second spectrum) makes kd the
+        checkerBoard scale kd kd2 texture (Texture.hs:209-219)"""
         m = abi.Material()
         m.kind, m.sigma, m.roughness, m.ior = kind, sigma, roughness, ior
         for name, v in (("kd", kd), ("ks", ks), ("kt", kt), ("eta", eta), ("k", k)):
             arr = constant(0) if v is None else np.asarray(v, dtype=np.float32)
             getattr(m, name)[:] = arr.tolist()
+        if kd_checker is not None:
+            scale, kd2 = kd_checker
+            m.kd_texture = abi.TEX_CHECKER
+            m.kd_tex_scale[:] = [float(np.float32(x)) for x in scale]
+            m.kd2[:] = np.asarray(kd2, np.float32).tolist()
         self.materials.append(m)
         return len(self.materials) - 1
 

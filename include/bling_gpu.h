@@ -89,7 +89,15 @@ typedef struct bling_material {
   float kt[BLING_BANDS];  /* glass transmission */
   float eta[BLING_BANDS]; /* metal */
   float k[BLING_BANDS];   /* metal */
+  /* the texture of kd (matte, plastic, substrate): BLING_TEX_CONSTANT, or
+   * BLING_TEX_CHECKER = checkerBoard kd_tex_scale kd kd2 (Texture.hs:209-219):
+   * kd where floor (x sx) + floor (y sy) + floor (z sz) of the shading point
+   * is even, kd2 where it is odd */
+  int32_t kd_texture;
+  float kd_tex_scale[3];
+  float kd2[BLING_BANDS];
 } bling_material;
+enum { BLING_TEX_CONSTANT = 0, BLING_TEX_CHECKER = 1 };
 
 /* A triangle mesh (mkTriangleMesh, Primitive/TriangleMesh.hs:39-60).
  * Vertices and normals are already in world space (the reference applies

@@ -559,6 +559,9 @@ struct Material {
   int kind;
   float sigma, rough, ior;
   Spec kd, ks, kt, eta, k;
+  int kd_tex;
+  float kd_scale[3];
+  Spec kd2;
 };
 
 struct Prim {
@@ -1373,7 +1376,14 @@ static Spec frApproxK(const Spec& r) {
   return o;
 }
 
-static Bsdf materialBsdf(const Material& m, const DG& dgg, const DG& dgs) {
+static Bsdf materialBsdf(const Material& m0, const DG& dgg, const DG& dgs) {
+  // the kd texture: checkerBoard (Texture.hs:209-219) at the shading point
+  Material m = m0;
+  if (m.kd_tex == BLING_TEX_CHECKER) {
+    long long c = (long long)floorf(dgs.p.x * m.kd_scale[0]) + (long long)floorf(dgs.p.y * m.kd_scale[1]) +
+                  (long long)floorf(dgs.p.z * m.kd_scale[2]);
+    if (((c % 2) + 2) % 2 == 1) m.kd = m.kd2;
+  }
   Bsdf b;
   b.n = 0;
   V nn = dgs.n, sn = normalize(dgs.dpdu);
@@ -2292,6 +2302,9 @@ int orc_scene_create(const bling_scene_desc* d, orc_scene** out) {
     memcpy(m.kt.v, bm.kt, 64);
     memcpy(m.eta.v, bm.eta, 64);
     memcpy(m.k.v, bm.k, 64);
+    m.kd_tex = bm.kd_texture;
+    memcpy(m.kd_scale, bm.kd_tex_scale, 12);
+    memcpy(m.kd2.v, bm.kd2, 64);
     S->mats.push_back(m);
   }
   for (int i = 0; i < d->n_meshes; i++) {

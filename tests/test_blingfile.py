@@ -164,6 +164,15 @@ def test_substrate_and_blackbody():
     assert np.array_equal(np.asarray(sub.kt, F), rgb_to_spectrum((F(0.1), F(0.1), F(0.1))))
 
 
+def test_checkerboard_diffuse_colour():
+    j = B.parse("material { matte kd { checker 2 2 2 tex1 { constant rgbR 0.8 0.8 0.8 } "
+                "tex2 { constant rgbR 0.1 0.1 0.1 } } sigma { constant 0 } } "
+                "prim { shape { sphere radius 1 } }")
+    m = j.scene.materials[0]
+    assert m.kd_texture == abi.TEX_CHECKER and list(m.kd_tex_scale) == [2.0, 2.0, 2.0]
+    assert np.array_equal(np.asarray(m.kd2, F), rgb_to_spectrum((F(0.1), F(0.1), F(0.1))))
+
+
 def test_constant_spd_gives_a_flat_spectrum():
     s = B.spectrum_from_spd([(380.0, 0.25), (500.0, 0.25), (720.0, 0.25)])
     assert np.array_equal(s, constant(0.25))
@@ -186,8 +195,9 @@ def test_other_renderers_parse_and_are_named():
 @pytest.mark.parametrize("src,what", [
     ("material { bumpMap { scale 0.1 tex { constant 1 } } material { matte kd { constant 1 } "
      "sigma { constant 0 } } }", "bumpMap"),
-    ("material { matte kd { checker 1 1 1 tex1 { constant rgbR 1 1 1 } "
-     "tex2 { constant rgbR 0 0 0 } } sigma { constant 0 } }", "checker"),
+    ("material { metal eta { checker 1 1 1 tex1 { constant rgbR 1 1 1 } "
+     "tex2 { constant rgbR 0 0 0 } } k { constant rgbR 1 1 1 } rough { constant 0.1 } }",
+     "checker"),
     ("prim { julia c 0 0 0 0 epsilon 0.1 iterations 4 }", "julia"),
     ("light { infinite { } l { sunSky east 0 0 1 sunDir 0 1 0 turbidity 2 } }", "sunSky"),
 ])

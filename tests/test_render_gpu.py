@@ -327,3 +327,33 @@ def test_substrate_and_blackbody_vs_oracle(gpu_ctx):
     fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p)
     _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
     assert st_g["nonfinite_drops"] == 0
+
+
+def test_checkerboard_diffuse_colour_vs_oracle(gpu_ctx):
+    """checkerBoard kd textures (Texture.hs:209-219) on a matte floor, a
+    plastic sphere and a substrate sphere: the colour follows the parity of
+    floor(x sx) + floor(y sy) + floor(z sz) at the shading point"""
+    sc = _materials_scene()
+    floor = sc.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.8, 0.8, 0.8)), sigma=0.3,
+                            kd_checker=((2.0, 2.0, 2.0), rgb_to_spectrum((0.1, 0.2, 0.1))))
+    plastic = sc.add_material(abi.MAT_PLASTIC, kd=rgb_to_spectrum((0.7, 0.2, 0.2)), ks=constant(0.3),
+                              roughness=0.1,
+                              kd_checker=((8.0, 8.0, 8.0), rgb_to_spectrum((0.2, 0.2, 0.7))))
+    sub = sc.add_material(abi.MAT_SUBSTRATE, kd=rgb_to_spectrum((0.6, 0.5, 0.2)), ks=constant(0.1),
+                          kt=constant(0.0), roughness=0.1, sigma=0.1, ior=0.0,
+                          kd_checker=((5.0, 0.0, 5.0), rgb_to_spectrum((0.1, 0.1, 0.1))))
+    sc.meshes[0].material = floor
+    sc.shapes[0].material = plastic
+    sc.shapes[3].material = sub
+    p = S.render_params(64, 64, (3, 3), max_depth=5, sample_depth=2, rr_depth=2, seed=23)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p)
+    _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
+
+
+def test_textured_kd_of_other_materials_is_refused(gpu_ctx):
+    s = S.Scene()
+    m = s.add_material(abi.MAT_METAL, eta=constant(0.2), k=constant(3.9), roughness=0.1,
+                       kd_checker=((1.0, 1.0, 1.0), constant(0.5)))
+    s.add_shape(abi.SHAPE_SPHERE, (1.0,), xf.identity(), m)
+    with pytest.raises(Exception):
+        gpu_ctx.scene(s)
