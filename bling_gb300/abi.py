@@ -40,11 +40,11 @@ class Opts(C.Structure):
 class Material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("sigma", C.c_float), ("roughness", C.c_float),
                 ("ior", C.c_float), ("kd", F16), ("ks", F16), ("kt", F16), ("eta", F16),
-                ("k", F16), ("kd_texture", C.c_int32), ("kd_tex_scale", C.c_float * 3),
+                ("k", F16), ("kd_texture", C.c_int32), ("kd_tex_params", C.c_float * 9),
                 ("kd2", F16)]
 
 
-TEX_CONSTANT, TEX_CHECKER = 0, 1
+TEX_CONSTANT, TEX_CHECKER, TEX_GRAPH_PAPER = 0, 1, 2
 
 
 class MeshDesc(C.Structure):

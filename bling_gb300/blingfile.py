@@ -516,7 +516,19 @@ class _Parser:
                 scale = t.vec()
                 t1 = self._spectrum_texture("tex1")
                 t2 = self._spectrum_texture("tex2")
-                return (t1, (tuple(scale), t2))
+                return (t1, ("checker", (tuple(scale), t2)))
+            if kind == "graphPaper" and checker:  # MaterialParser.hs:220-224
+                lw = t.flt()
+
+                def mapping():
+                    mk = t.word()
+                    if mk != "planar":
+                        raise Unsupported(f"texture mapping {mk}: graph paper takes planar mappings")
+                    return (t.vec(), t.vec(), (t.flt(), t.flt()))
+                vu, vv, off = t.named_block("map", mapping)
+                t1 = self._spectrum_texture("tex1")
+                t2 = self._spectrum_texture("tex2")
+                return (t1, ("graph", (lw, vu, vv, off, t2)))
             if kind != "constant":
                 raise Unsupported(f"texture {kind} ({name}): the GPU path renders constant "
                                   "textures and checkerboard diffuse colours")
@@ -525,8 +537,11 @@ class _Parser:
 
     @staticmethod
     def _kd(v):
-        """(kd, kd_checker) of a kd texture"""
-        return v if isinstance(v, tuple) else (v, None)
+        """(kd, texture keyword arguments of add_material) of a kd texture"""
+        if not isinstance(v, tuple):
+            return v, {}
+        kd, (kind, args) = v
+        return kd, ({"kd_checker": args} if kind == "checker" else {"kd_graph": args})
 
     def _scalar_texture(self, name) -> np.float32:
         t = self.t
@@ -549,13 +564,12 @@ class _Parser:
         if kind == "matte":
             kd, chk = self._kd(self._spectrum_texture("kd", checker=True))
             sig = self._scalar_texture("sigma")
-            return sc.add_material(abi.MAT_MATTE, kd=kd, sigma=float(sig), kd_checker=chk)
+            return sc.add_material(abi.MAT_MATTE, kd=kd, sigma=float(sig), **chk)
         if kind == "plastic":
             kd, chk = self._kd(self._spectrum_texture("kd", checker=True))
             ks = self._spectrum_texture("ks")
             rough = self._scalar_texture("rough")
-            return sc.add_material(abi.MAT_PLASTIC, kd=kd, ks=ks, roughness=float(rough),
-                                   kd_checker=chk)
+            return sc.add_material(abi.MAT_PLASTIC, kd=kd, ks=ks, roughness=float(rough), **chk)
         if kind == "metal":
             eta = self._spectrum_texture("eta")
             k = self._spectrum_texture("k")
@@ -587,7 +601,7 @@ class _Parser:
             vr = self._scalar_texture("vrough")
             depth = self._scalar_texture("depth")
             return sc.add_material(abi.MAT_SUBSTRATE, kd=kd, ks=ks, kt=ka, roughness=float(ur),
-                                   sigma=float(vr), ior=float(depth), kd_checker=chk)
+                                   sigma=float(vr), ior=float(depth), **chk)
         if kind == "blackbody":
             return sc.add_material(abi.MAT_BLACKBODY)
         if kind == "bumpMap":

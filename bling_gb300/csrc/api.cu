@@ -363,7 +363,8 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   for (int i = 0; i < d->n_materials; i++)
     if (d->materials[i].kind < BLING_MAT_MATTE || d->materials[i].kind > BLING_MAT_BLACKBODY ||
         (d->materials[i].kd_texture != BLING_TEX_CONSTANT &&
-         !(d->materials[i].kd_texture == BLING_TEX_CHECKER &&
+         !((d->materials[i].kd_texture == BLING_TEX_CHECKER ||
+            d->materials[i].kd_texture == BLING_TEX_GRAPH_PAPER) &&
            (d->materials[i].kind == BLING_MAT_MATTE || d->materials[i].kind == BLING_MAT_PLASTIC ||
             d->materials[i].kind == BLING_MAT_SUBSTRATE))))
       return set_err(c, BLING_ERR_INVALID_ARG, "material %d: unknown kind %d", i,

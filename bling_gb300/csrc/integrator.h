@@ -15,8 +15,8 @@ struct DMaterial {
   float sigma, rough, ior;
   float kd[16], ks[16], kt[16], eta[16], k[16];
   int kd_tex;           // BLING_TEX_*
-  float kd_scale[3];    // checkerBoard scale
-  float kd2[16];        // the checker's second spectrum
+  float kd_par[9];      // the texture's parameters (bling_material.kd_tex_params)
+  float kd2[16];        // the texture's second spectrum
 };
 
 // Spectra a material derives from its constant parameters, once at upload

@@ -633,12 +633,18 @@ static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ 
   x.btdf = false;
   int kind = m.kind;
   float sigma = m.sigma, rough = m.rough, ior = m.ior;
-  // the kd texture: checkerBoard (Texture.hs:209-219) at the shading point
+  // the kd texture at the shading point
   const float* kd = m.kd;
-  if (m.kd_tex == BLING_TEX_CHECKER) {
-    long long c = (long long)floorf(dgs_p.x * m.kd_scale[0]) + (long long)floorf(dgs_p.y * m.kd_scale[1]) +
-                  (long long)floorf(dgs_p.z * m.kd_scale[2]);
+  if (m.kd_tex == BLING_TEX_CHECKER) {  // checkerBoard (Texture.hs:209-219)
+    long long c = (long long)floorf(dgs_p.x * m.kd_par[0]) + (long long)floorf(dgs_p.y * m.kd_par[1]) +
+                  (long long)floorf(dgs_p.z * m.kd_par[2]);
     if (c % 2 != 0) kd = m.kd2;  // Haskell's mod 2 is 0 for even sums of either sign
+  } else if (m.kd_tex == BLING_TEX_GRAPH_PAPER) {  // graphPaper + planarMapping (Texture.hs:172-207)
+    const float* q = m.kd_par;
+    float u = dot(dgs_p, V3{q[1], q[2], q[3]}) + q[7], v = dot(dgs_p, V3{q[4], q[5], q[6]}) + q[8];
+    float xf = fabsf(u - truncf(u)), zf = fabsf(v - truncf(v));  // properFraction
+    float lo = q[0] / 2.0f, hi = 1.0f - lo;
+    if (xf < lo || zf < lo || xf > hi || zf > hi) kd = m.kd2;
   }
   if (kind == BLING_MAT_MATTE) {
     x.type = T_REFL | T_DIFF;

@@ -79,7 +79,7 @@ int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
     memcpy(o.eta, m.eta, 64);
     memcpy(o.k, m.k, 64);
     o.kd_tex = m.kd_texture;
-    memcpy(o.kd_scale, m.kd_tex_scale, 12);
+    memcpy(o.kd_par, m.kd_tex_params, 36);
     memcpy(o.kd2, m.kd2, 64);
     deriveMaterialSpectra(o);
   }

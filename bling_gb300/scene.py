@@ -69,9 +69,11 @@ class Scene:
 
     # --- builders -------------------------------------------------------
     def add_material(self, kind, kd=None, ks=None, kt=None, eta=None, k=None, sigma=0.0,
-                     roughness=0.0, ior=1.5, kd_checker=None) -> int:
+                     roughness=0.0, ior=1.5, kd_checker=None, kd_graph=None) -> int:
         """kd_checker: (scale (sx, sy, sz), second spectrum) makes kd the
-        checkerBoard scale kd kd2 texture (Texture.hs:209-219)"""
+        checkerBoard scale kd kd2 texture (Texture.hs:209-219); kd_graph:
+        (lw, vu, vv, (ou, ov), line spectrum) makes it graphPaper lw
+        (planarMapping (vu, vv) (ou, ov)) kd lines (Texture.hs:172-207)"""
         m = abi.Material()
         m.kind, m.sigma, m.roughness, m.ior = kind, sigma, roughness, ior
         for name, v in (("kd", kd), ("ks", ks), ("kt", kt), ("eta", eta), ("k", k)):
@@ -80,8 +82,13 @@ class Scene:
         if kd_checker is not None:
             scale, kd2 = kd_checker
             m.kd_texture = abi.TEX_CHECKER
-            m.kd_tex_scale[:] = [float(np.float32(x)) for x in scale]
+            m.kd_tex_params[:3] = [float(np.float32(x)) for x in scale]
             m.kd2[:] = np.asarray(kd2, np.float32).tolist()
+        if kd_graph is not None:
+            lw, vu, vv, (ou, ov), lines = kd_graph
+            m.kd_texture = abi.TEX_GRAPH_PAPER
+            m.kd_tex_params[:] = [float(np.float32(x)) for x in [lw, *vu, *vv, ou, ov]]
+            m.kd2[:] = np.asarray(lines, np.float32).tolist()
         self.materials.append(m)
         return len(self.materials) - 1
 

@@ -89,15 +89,21 @@ typedef struct bling_material {
   float kt[BLING_BANDS];  /* glass transmission */
   float eta[BLING_BANDS]; /* metal */
   float k[BLING_BANDS];   /* metal */
-  /* the texture of kd (matte, plastic, substrate): BLING_TEX_CONSTANT, or
-   * BLING_TEX_CHECKER = checkerBoard kd_tex_scale kd kd2 (Texture.hs:209-219):
-   * kd where floor (x sx) + floor (y sy) + floor (z sz) of the shading point
-   * is even, kd2 where it is odd */
+  /* the texture of kd (matte, plastic, substrate), picked per hit from the
+   * shading point p:
+   *  - BLING_TEX_CONSTANT: kd;
+   *  - BLING_TEX_CHECKER, checkerBoard (sx sy sz) kd kd2 (Texture.hs:209-219),
+   *    params sx sy sz: kd where floor (x sx) + floor (y sy) + floor (z sz)
+   *    is even, kd2 where it is odd;
+   *  - BLING_TEX_GRAPH_PAPER, graphPaper lw (planarMapping (vu, vv) (ou, ov))
+   *    kd kd2 (Texture.hs:172-207), params lw vu vv ou ov: with u = p.vu + ou,
+   *    v = p.vv + ov, kd2 (the lines) where the fraction of |u| or |v| is
+   *    below lw/2 or above 1 - lw/2, kd (the paper) elsewhere */
   int32_t kd_texture;
-  float kd_tex_scale[3];
+  float kd_tex_params[9];
   float kd2[BLING_BANDS];
 } bling_material;
-enum { BLING_TEX_CONSTANT = 0, BLING_TEX_CHECKER = 1 };
+enum { BLING_TEX_CONSTANT = 0, BLING_TEX_CHECKER = 1, BLING_TEX_GRAPH_PAPER = 2 };
 
 /* A triangle mesh (mkTriangleMesh, Primitive/TriangleMesh.hs:39-60).
  * Vertices and normals are already in world space (the reference applies

@@ -560,7 +560,7 @@ struct Material {
   float sigma, rough, ior;
   Spec kd, ks, kt, eta, k;
   int kd_tex;
-  float kd_scale[3];
+  float kd_par[9];
   Spec kd2;
 };
 
@@ -1377,12 +1377,18 @@ static Spec frApproxK(const Spec& r) {
 }
 
 static Bsdf materialBsdf(const Material& m0, const DG& dgg, const DG& dgs) {
-  // the kd texture: checkerBoard (Texture.hs:209-219) at the shading point
+  // the kd texture at the shading point
   Material m = m0;
-  if (m.kd_tex == BLING_TEX_CHECKER) {
-    long long c = (long long)floorf(dgs.p.x * m.kd_scale[0]) + (long long)floorf(dgs.p.y * m.kd_scale[1]) +
-                  (long long)floorf(dgs.p.z * m.kd_scale[2]);
+  if (m.kd_tex == BLING_TEX_CHECKER) {  // checkerBoard (Texture.hs:209-219)
+    long long c = (long long)floorf(dgs.p.x * m.kd_par[0]) + (long long)floorf(dgs.p.y * m.kd_par[1]) +
+                  (long long)floorf(dgs.p.z * m.kd_par[2]);
     if (((c % 2) + 2) % 2 == 1) m.kd = m.kd2;
+  } else if (m.kd_tex == BLING_TEX_GRAPH_PAPER) {  // graphPaper + planarMapping (Texture.hs:172-207)
+    const float* q = m.kd_par;
+    float u = dot(dgs.p, V{q[1], q[2], q[3]}) + q[7], v = dot(dgs.p, V{q[4], q[5], q[6]}) + q[8];
+    float xf = fabsf(u - truncf(u)), zf = fabsf(v - truncf(v));  // properFraction
+    float lo = q[0] / 2.0f, hi = 1.0f - lo;
+    if (xf < lo || zf < lo || xf > hi || zf > hi) m.kd = m.kd2;
   }
   Bsdf b;
   b.n = 0;
@@ -2303,7 +2309,7 @@ int orc_scene_create(const bling_scene_desc* d, orc_scene** out) {
     memcpy(m.eta.v, bm.eta, 64);
     memcpy(m.k.v, bm.k, 64);
     m.kd_tex = bm.kd_texture;
-    memcpy(m.kd_scale, bm.kd_tex_scale, 12);
+    memcpy(m.kd_par, bm.kd_tex_params, 36);
     memcpy(m.kd2.v, bm.kd2, 64);
     S->mats.push_back(m);
   }

@@ -169,7 +169,13 @@ def test_checkerboard_diffuse_colour():
                 "tex2 { constant rgbR 0.1 0.1 0.1 } } sigma { constant 0 } } "
                 "prim { shape { sphere radius 1 } }")
     m = j.scene.materials[0]
-    assert m.kd_texture == abi.TEX_CHECKER and list(m.kd_tex_scale) == [2.0, 2.0, 2.0]
+    assert m.kd_texture == abi.TEX_CHECKER and list(m.kd_tex_params)[:3] == [2.0, 2.0, 2.0]
+    j = B.parse("material { plastic kd { graphPaper 0.1 map { planar 1 0 0 0 0 1 0.5 0.25 } "
+                "tex1 { constant rgbR 0.9 0.9 0.9 } tex2 { constant rgbR 0.1 0.1 0.4 } } "
+                "ks { constant rgbR 0.2 0.2 0.2 } rough { constant 0.1 } }")
+    g = j.scene.materials[0]
+    assert g.kd_texture == abi.TEX_GRAPH_PAPER
+    assert list(g.kd_tex_params) == [float(F(0.1)), 1, 0, 0, 0, 0, 1, 0.5, 0.25]
     assert np.array_equal(np.asarray(m.kd2, F), rgb_to_spectrum((F(0.1), F(0.1), F(0.1))))
 
 

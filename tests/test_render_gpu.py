@@ -357,3 +357,21 @@ def test_textured_kd_of_other_materials_is_refused(gpu_ctx):
     s.add_shape(abi.SHAPE_SPHERE, (1.0,), xf.identity(), m)
     with pytest.raises(Exception):
         gpu_ctx.scene(s)
+
+
+def test_graph_paper_diffuse_colour_vs_oracle(gpu_ctx):
+    """graphPaper with a planar mapping (Texture.hs:172-207) on the matte
+    floor and a plastic sphere"""
+    sc = _materials_scene()
+    floor = sc.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.9, 0.9, 0.85)),
+                            kd_graph=(0.08, (2.0, 0.0, 0.0), (0.0, 0.0, 2.0), (0.25, 0.5),
+                                      rgb_to_spectrum((0.1, 0.1, 0.5))))
+    plastic = sc.add_material(abi.MAT_PLASTIC, kd=rgb_to_spectrum((0.7, 0.6, 0.2)), ks=constant(0.3),
+                              roughness=0.1,
+                              kd_graph=(0.2, (0.0, 6.0, 0.0), (6.0, 0.0, 0.0), (0.0, 0.0),
+                                        rgb_to_spectrum((0.1, 0.1, 0.1))))
+    sc.meshes[0].material = floor
+    sc.shapes[0].material = plastic
+    p = S.render_params(64, 64, (3, 3), max_depth=5, sample_depth=2, rr_depth=2, seed=29)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p)
+    _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
