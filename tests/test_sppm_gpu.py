@@ -142,3 +142,30 @@ def test_invalid_parameters_are_refused(gpu_ctx):
         args.update(kw)
         with pytest.raises(Exception):
             g.sppm_pass(film, abi.sppm_params(**args), 0)
+
+
+def test_edge_cases_no_lights_no_hit_points(gpu_ctx):
+    """a scene without lights: the light tracer and SPPM add nothing; a view
+    of empty space: SPPM records no hit points and skips its photon pass;
+    zero photons: ceil(sqrt 0) = 0 is raised to one photon (SPPM.hs:464-466)"""
+    s = S.Scene()
+    m = s.add_material(abi.MAT_MATTE, kd=constant(0.5))
+    s.add_shape(abi.SHAPE_SPHERE, (1.0,), xf.identity(), m)
+    s.set_perspective(xf.look_at((0, 0, -4), (0, 0, 0), (0, 1, 0)), 0.0, 1.0, 40.0, 16, 16)
+    g = gpu_ctx.scene(s)
+    film = gpu_ctx.film(16, 16)
+    g.light_pass(film, 10_000)
+    g.sppm_pass(film, abi.sppm_params(10_000, max_depth=3, radius=0.05, alpha=0.7), 0)
+    assert not film.read_splats().any()
+    o = OracleScene(s)
+    _, spl, _, st = o.sppm_pass(abi.sppm_params(10_000, max_depth=3, radius=0.05, alpha=0.7), 16, 16)
+    assert not spl.any() and st["splats"] == 0
+    # looking away from everything: no hit points
+    s.lights = [S.Light(abi.LIGHT_POINT, constant(1.0), vec=(0.0, 3.0, 0.0))]
+    s.set_perspective(xf.look_at((0, 0, -4), (0, 0, -8), (0, 1, 0)), 0.0, 1.0, 40.0, 16, 16)
+    g2 = gpu_ctx.scene(s)
+    f2 = gpu_ctx.film(16, 16)
+    g2.sppm_pass(f2, abi.sppm_params(0, max_depth=3, radius=0.05, alpha=0.7), 0)
+    assert not f2.read_splats().any() and not f2.read()[..., 1:].any()
+    st2 = g2.stats()
+    assert st2["path_samples"] == 18 * 18 + 1  # camera samples + one photon (not traced)
