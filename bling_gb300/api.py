@@ -477,6 +477,60 @@ class PassDone:
     splat_weight: float = 1.0
 
 
+class GpuLightTracer:
+    """``mkLightTracer ppp`` as a bling ``Renderer`` (LightTracer.hs:37-44):
+    pass n adds ppp photons to the film's splat image and reports the splat
+    weight 1 / (n ppp).  max_depth 0 keeps the reference's unbounded paths."""
+
+    def __init__(self, photons_per_pass: int, ctx: Context | None = None, seed: int = 0,
+                 max_depth: int = 0):
+        self.ctx = ctx or Context()
+        self.ppp, self.seed, self.max_depth = photons_per_pass, seed, max_depth
+
+    def render(self, job: RenderJob, report) -> Film:
+        p = job.params
+        gscene = job.scene if isinstance(job.scene, GpuScene) else self.ctx.scene(job.scene)
+        film = self.ctx.film(p.width, p.height)
+        report("Started")
+        n = 1
+        while True:
+            gscene.light_pass(film, self.ppp, seed=self.seed, pass_index=n, max_depth=self.max_depth)
+            if not report(PassDone(n, film, 1.0 / (n * self.ppp))):
+                break
+            n += 1
+        return film
+
+
+class GpuSPPM:
+    """``mkSPPM n md r alpha`` as a bling ``Renderer`` (SPPM.hs:462-480): pass
+    n adds camera samples to the film and ceil(sqrt n)^2 photons' splats to
+    its splat image, shrinks the radii, and reports the splat weight
+    1 / (n sn^2).  The job's pixel filter applies to the camera samples."""
+
+    def __init__(self, photons: int, max_depth: int, radius: float, alpha: float = 0.8,
+                 ctx: Context | None = None, seed: int = 1):
+        self.ctx = ctx or Context()
+        self.photons, self.max_depth, self.radius, self.alpha, self.seed = (photons, max_depth,
+                                                                            radius, alpha, seed)
+
+    def render(self, job: RenderJob, report) -> Film:
+        p = job.params
+        gscene = job.scene if isinstance(job.scene, GpuScene) else self.ctx.scene(job.scene)
+        film = self.ctx.film(p.width, p.height)
+        sp = abi.sppm_params(self.photons, self.max_depth, self.radius, self.alpha,
+                             filter_kind=p.filter_kind, filter_params=tuple(p.filter_params),
+                             seed=self.seed)
+        sn = max(1, int(np.ceil(np.sqrt(np.float32(self.photons)))))
+        report("Started")
+        n = 1
+        while True:
+            gscene.sppm_pass(film, sp, n - 1)
+            if not report(PassDone(n, film, 1.0 / (n * sn * sn))):
+                break
+            n += 1
+        return film
+
+
 class GpuPathRenderer:
     """The GPU path integrator as a bling ``Renderer`` (Rendering.hs:77-78)."""
 

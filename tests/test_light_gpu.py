@@ -190,3 +190,24 @@ def test_substrate_light_pass_vs_oracle(gpu_ctx):
     film, g, so, st = _both(gpu_ctx, sc, 64, 48, 300_000, seed=8)
     _compare(film.read_splats(), so, rel=2e-3, frac=0.9)
     _counts_close(g.stats(), st[0], 300_000)
+
+
+def test_renderer_interfaces_report_the_reference_splat_weights(gpu_ctx):
+    """GpuLightTracer and GpuSPPM as bling Renderers: PassDone n with splat
+    weight 1 / (n ppp) (LightTracer.hs:44) and 1 / (n sn^2) (SPPM.hs:418)"""
+    from bling_gb300.api import GpuLightTracer, GpuSPPM, PassDone, RenderJob
+    sc = S.cornell_room(24, 24)
+    job = RenderJob(gpu_ctx.scene(sc), S.cornell_params(24, 24))
+    for r, w in ((GpuLightTracer(5000, ctx=gpu_ctx), lambda n: 1.0 / (n * 5000)),
+                 (GpuSPPM(5000, 3, 0.03, ctx=gpu_ctx), lambda n: 1.0 / (n * 71 * 71))):
+        seen = []
+
+        def report(ev):
+            if isinstance(ev, PassDone):
+                seen.append(ev)
+                return ev.pass_num < 3
+            return True
+        film = r.render(job, report)
+        assert [e.pass_num for e in seen] == [1, 2, 3]
+        assert all(abs(e.splat_weight - w(e.pass_num)) < 1e-12 for e in seen)
+        assert film.read_splats().sum() > 0
