@@ -224,7 +224,8 @@ typedef struct bling_render_params {
 typedef struct bling_stats {
   uint64_t rays_closest;    /* closest-hit queries (camera, continuation, BSDF-MIS) */
   uint64_t rays_any;        /* any-hit queries (shadow) */
-  uint64_t path_samples;    /* completed camera paths */
+  uint64_t path_samples;    /* completed camera paths; light passes add their photons, SPPM
+                               passes their camera samples and photons */
   uint64_t nonfinite_drops; /* NaN/Inf samples skipped by the film (Image.hs:253-256) */
   uint64_t degenerate_rays; /* rays with a NaN component, answered without traversal */
   double bvh_build_ms;
