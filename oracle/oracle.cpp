@@ -1378,17 +1378,18 @@ static Spec frApproxK(const Spec& r) {
 
 static Bsdf materialBsdf(const Material& m0, const DG& dgg, const DG& dgs) {
   // the kd texture at the shading point
-  Material m = m0;
+  const Material& m = m0;
+  const Spec* kdp = &m.kd;  // the textured diffuse colour of matte, plastic, substrate
   if (m.kd_tex == BLING_TEX_CHECKER) {  // checkerBoard (Texture.hs:209-219)
     long long c = (long long)floorf(dgs.p.x * m.kd_par[0]) + (long long)floorf(dgs.p.y * m.kd_par[1]) +
                   (long long)floorf(dgs.p.z * m.kd_par[2]);
-    if (((c % 2) + 2) % 2 == 1) m.kd = m.kd2;
+    if (((c % 2) + 2) % 2 == 1) kdp = &m.kd2;
   } else if (m.kd_tex == BLING_TEX_GRAPH_PAPER) {  // graphPaper + planarMapping (Texture.hs:172-207)
     const float* q = m.kd_par;
     float u = dot(dgs.p, V{q[1], q[2], q[3]}) + q[7], v = dot(dgs.p, V{q[4], q[5], q[6]}) + q[8];
     float xf = fabsf(u - truncf(u)), zf = fabsf(v - truncf(v));  // properFraction
     float lo = q[0] / 2.0f, hi = 1.0f - lo;
-    if (xf < lo || zf < lo || xf > hi || zf > hi) m.kd = m.kd2;
+    if (xf < lo || zf < lo || xf > hi || zf > hi) kdp = &m.kd2;
   }
   Bsdf b;
   b.n = 0;
@@ -1403,11 +1404,11 @@ static Bsdf materialBsdf(const Material& m0, const DG& dgg, const DG& dgs) {
       if (m.sigma == 0) {
         x.kind = BX_LAMBERT;
         x.type = T_REFL | T_DIFF;
-        x.r = m.kd;
+        x.r = *kdp;
       } else {
         x.kind = BX_OREN;
         x.type = T_REFL | T_DIFF;
-        x.r = m.kd;
+        x.r = *kdp;
         float s = clampf(m.sigma, 0, 1);
         float sig2 = s * s;
         x.A = 1.0f - (sig2 / (2.0f * (sig2 + 0.33f)));
@@ -1418,7 +1419,7 @@ static Bsdf materialBsdf(const Material& m0, const DG& dgg, const DG& dgs) {
     case BLING_MAT_PLASTIC: {
       x.kind = BX_LAMBERT;
       x.type = T_REFL | T_DIFF;
-      x.r = m.kd;
+      x.r = *kdp;
       add(x);
       BxDF y{};
       y.kind = BX_MICRO;
@@ -1466,7 +1467,7 @@ static Bsdf materialBsdf(const Material& m0, const DG& dgg, const DG& dgs) {
     case BLING_MAT_SUBSTRATE: {  // mkSubstrate kd ks ka u v depth (Material.hs:111-127)
       x.kind = BX_FBLEND;
       x.type = T_REFL | T_GLOSSY;
-      x.r = sClamp(0, 1, m.kd);
+      x.r = sClamp(0, 1, *kdp);
       x.rs = sClamp(0, 1, m.ks);
       x.ra = sClamp(0, 1, m.kt);  // ka
       float u = hmax(0.0f, m.rough), v = hmax(0.0f, m.sigma);
