@@ -288,7 +288,7 @@ int light_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, cons
   res = LightPassResult{};
   if (a.photons <= 0) return BLING_OK;
   // a multiple of 64 photons keeps every per-photon array 16-byte aligned
-  size_t cap = (size_t)std::min<int64_t>(a.photons, int64_t(1) << 20);
+  size_t cap = (size_t)std::min<int64_t>(a.photons, int64_t(1) << 22);
   cap = (std::max<size_t>(cap, 1024) + 63) / 64 * 64;
   if (ws.capacity < cap || !ws.buffer) {
     light_workspace_free(ws);
