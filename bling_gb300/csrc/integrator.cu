@@ -378,7 +378,7 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
   float tbl[256];
   filterTableHost(p.filter_kind, p.filter_params, P.fw, P.fh, tbl);
   RET_CUDA(cudaMemcpyToSymbolAsync(c_filter, tbl, sizeof tbl, 0, cudaMemcpyHostToDevice, stream));
-  size_t cap = (size_t)std::min<uint64_t>(total, uint64_t(1) << 22);
+  size_t cap = (size_t)std::min<uint64_t>(total, uint64_t(1) << 24);
   // a multiple of 64 paths keeps every per-path array 16-byte aligned (the
   // records are read with 16-byte vector loads)
   cap = (std::max<size_t>(cap, 1024) + 63) / 64 * 64;
