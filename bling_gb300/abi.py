@@ -124,7 +124,7 @@ BATCH_PLAIN_LAUNCHES, BATCH_GRAPH, BATCH_DEVICE_LOOP = 0, 1, 2
 class BatchOpts(C.Structure):
     _fields_ = [("slots", C.c_int64), ("block_size", C.c_int32), ("max_jobs", C.c_int32),
                 ("sort_rays", C.c_int32), ("graph_mode", C.c_int32),
-                ("iters_per_launch", C.c_int32), ("reserved", C.c_int32)]
+                ("iters_per_launch", C.c_int32), ("max_run_iterations", C.c_int32)]
 
 
 class BatchStats(C.Structure):

@@ -117,8 +117,9 @@ def lib():
     L.bling_server_stats_get.argtypes = [vp, P(abi.ServerStats)]
     L.bling_server_last_error.argtypes = [vp]
     L.bling_server_last_error.restype = C.c_char_p
+    L.bling_server_debug_fail_step.argtypes = [vp, C.c_int32]
     for fn in ("bling_server_create", "bling_server_submit", "bling_server_wait",
-               "bling_server_stats_get"):
+               "bling_server_stats_get", "bling_server_debug_fail_step"):
         getattr(L, fn).restype = C.c_int
     for fn in ("bling_ctx_create", "bling_ctx_set_stream", "bling_scene_create", "bling_scene_stats",
                "bling_trace_closest", "bling_trace_any", "bling_trace_closest_device",
@@ -349,11 +350,12 @@ class Batch:
 
     def __init__(self, ctx: Context, slots: int = 0, block_size: int = 0, max_jobs: int = 0,
                  sort_rays: bool = False, graph_mode: int = abi.BATCH_GRAPH,
-                 iters_per_launch: int = 0):
+                 iters_per_launch: int = 0, max_run_iterations: int = 0):
         self.ctx = ctx
         o = abi.BatchOpts()
         o.slots, o.block_size, o.max_jobs = slots, block_size, max_jobs
         o.sort_rays, o.graph_mode, o.iters_per_launch = int(sort_rays), graph_mode, iters_per_launch
+        o.max_run_iterations = max_run_iterations
         self.h = C.c_void_p()
         ctx.check(lib().bling_batch_create(ctx.h, C.byref(o), C.byref(self.h)))
         ctx._children.add(self)
@@ -421,6 +423,11 @@ class Server:
     def _check(self, rc):
         if rc != 0:
             raise BlingError(rc, lib().bling_server_last_error(self.h).decode())
+
+    def debug_fail_step(self, after_steps: int):
+        """Test hook: the wavefront step after `after_steps` more steps fails
+        on the host (``bling_server_debug_fail_step``); -1 disarms."""
+        self._check(lib().bling_server_debug_fail_step(self.h, after_steps))
 
     def close(self):
         if getattr(self, "h", None):

@@ -1064,6 +1064,9 @@ int bling_batch_create(bling_ctx* c, const bling_batch_opts* o, bling_batch** ou
     cfg.sort_rays = o->sort_rays != 0;
     cfg.graph_mode = o->graph_mode;
     if (o->iters_per_launch) cfg.iters_per_launch = o->iters_per_launch;
+    if (o->max_run_iterations < 0)
+      return set_err(c, BLING_ERR_INVALID_ARG, "max_run_iterations must be >= 0");
+    cfg.max_run_iterations = o->max_run_iterations;
   } else {
     cfg.graph_mode = BLING_BATCH_PLAIN_LAUNCHES;
   }

@@ -509,6 +509,15 @@ __global__ void k_iter_end(BatchCtl* ctl, cudaGraphConditionalHandle handle, int
   }
 }
 
+// drops the paths in flight and stops sample generation at `end` (batch_cancel)
+__global__ void k_cancel(BatchCtl* ctl, unsigned long long end) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  ctl->next_sample = end;
+  ctl->regen_count = 0;
+  ctl->c[C_LIVE0] = 0;
+  ctl->c[C_LIVE0 + 1] = 0;
+}
+
 // ------------------------------------------------------------------ host side
 struct BatchEngine {
   int device = 0;
@@ -923,17 +932,40 @@ int batch_run(BatchEngine* b, std::string& err) {
   // logic error from looping forever
   const int per = b->cfg.graph_mode == 2 ? std::max(1, b->cfg.iters_per_launch) * 4 : 8;
   const unsigned long long limit =
-      ((b->end_sample / (unsigned long long)b->cap) + 2) * 4096ull + 1000000ull;
+      b->cfg.max_run_iterations > 0
+          ? (unsigned long long)b->cfg.max_run_iterations
+          : ((b->end_sample / (unsigned long long)b->cap) + 2) * 4096ull + 1000000ull;
   unsigned long long spent = 0;
   while (b->job_lo < b->job_hi) {
-    int rc = batch_step(b, per, err);
-    if (rc) return rc;
-    spent += (unsigned long long)per;
-    if (spent > limit) {
-      err = "batch did not finish within its iteration bound";
+    if (spent >= limit) {
+      char buf[128];
+      snprintf(buf, sizeof buf, "batch did not finish within its bound of %llu iterations",
+               limit);
+      err = buf;
       return BLING_ERR_TIMEOUT;
     }
+    int n = (int)std::min<unsigned long long>((unsigned long long)per, limit - spent);
+    int rc = batch_step(b, n, err);
+    if (rc) return rc;
+    spent += (unsigned long long)n;
   }
+  return BLING_OK;
+}
+
+int batch_cancel(BatchEngine* b, std::string& err) {
+  BRET(cudaStreamSynchronize(b->stream));
+  k_cancel<<<1, 32, 0, b->stream>>>(b->d_ctl, b->end_sample);
+  BRET(cudaGetLastError());
+  if (b->job_lo != b->job_hi) {
+    b->stats.jobs_done += (int64_t)(b->job_hi - b->job_lo);
+    b->job_lo = b->job_hi;
+  }
+  b->ctl_dirty = true;
+  int rc = syncHostCtl(b, err);
+  if (rc) return rc;
+  BRET(cudaStreamSynchronize(b->stream));
+  b->stats.samples_started = b->end_sample;
+  b->stats.jobs_active = 0;
   return BLING_OK;
 }
 

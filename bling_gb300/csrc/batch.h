@@ -37,6 +37,7 @@ struct BatchConfig {
   int graph_mode = 1;        // 0 plain launches, 1 a CUDA graph per iteration,
                              // 2 a conditional (while) graph running many iterations
   int iters_per_launch = 16; // iterations per graph launch in mode 2
+  int64_t max_run_iterations = 0;  // batch_run's bound on iterations; 0 = derived from the work
 };
 
 struct BatchStats {
@@ -64,8 +65,16 @@ int batch_submit(BatchEngine* b, int scene, const bling_camera_desc& cam, float*
 // runs `iterations` wavefront iterations (fewer if all work is done) and
 // updates the jobs' progress
 int batch_step(BatchEngine* b, int iterations, std::string& err);
-// steps until every submitted job is complete
+// steps until every submitted job is complete; BLING_ERR_TIMEOUT once more
+// than the iteration bound (cfg.max_run_iterations, or one derived from the
+// submitted work) has run; the jobs stay in flight and a later step or run
+// continues them
 int batch_run(BatchEngine* b, std::string& err);
+// drops every incomplete job and every path in flight (after a failed step,
+// before the caller releases the jobs' films): waits for the stream, stops
+// sample generation at the samples submitted so far and empties the live
+// queues.  Dropped jobs read as retired.  Later submits run normally.
+int batch_cancel(BatchEngine* b, std::string& err);
 int batch_job_status(BatchEngine* b, int64_t job_id, uint64_t& done, uint64_t& total,
                      std::string& err);
 void batch_stats(BatchEngine* b, BatchStats& out);

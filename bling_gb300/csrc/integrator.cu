@@ -27,6 +27,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "filter_host.h"
@@ -34,13 +35,20 @@
 
 namespace bgpu {
 
-// lays slots, queues and counters out in one buffer of slotBytes(cap) bytes
-static size_t slotBytes(size_t cap) { return kCounterBytes + (kSlotWords + kQueueWords) * 4 * cap; }
+// the pass's 16x16 filter table sits between the counters and the slots
+constexpr size_t kFilterBytes = 256 * sizeof(float);
+
+// lays counters, the filter table, slots and queues out in one buffer of
+// slotBytes(cap) bytes
+static size_t slotBytes(size_t cap) {
+  return kCounterBytes + kFilterBytes + (kSlotWords + kQueueWords) * 4 * cap;
+}
 
 static void carve(unsigned char* base, size_t cap, Slots& st, Queues& q,
-                  unsigned long long*& counters) {
+                  unsigned long long*& counters, float*& filter) {
   counters = (unsigned long long*)base;
-  float* w = (float*)(base + kCounterBytes);
+  filter = (float*)(base + kCounterBytes);
+  float* w = (float*)(base + kCounterBytes + kFilterBytes);
   carveSlots(w, cap, st);
   int32_t* qw = (int32_t*)w;
   q.live[0] = qw;
@@ -55,11 +63,6 @@ static void carve(unsigned char* base, size_t cap, Slots& st, Queues& q,
 __device__ __forceinline__ unsigned* classCounts(unsigned long long* counters) {
   return (unsigned*)counters + kClassCountsAt;
 }
-
-// the pass's filter table, in constant memory
-struct PassFilter {
-  __device__ __forceinline__ float operator()(int i) const { return c_filter[i]; }
-};
 
 // ------------------------------------------------------------------ kernels
 // camera rays (fireRay, Camera.hs:146-164) for samples [chunk_base, chunk_base + count)
@@ -174,7 +177,7 @@ __global__ void __launch_bounds__(128, 10) k_trace_mis(DevAccel A, Slots st,
 // one vertex of every live path, up to its shadow and MIS rays (Path.hs:49-87)
 __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, PassParams P, Slots st,
                                                Queues Q, int depth, int live_in,
-                                               float* __restrict__ film,
+                                               float* __restrict__ film, const float* filter,
                                                unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[live_in];
   const int32_t* __restrict__ qin = Q.sorted;  // the live paths in shading-class order
@@ -187,7 +190,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, Pass
       s = qin[q];
       uint64_t g = P.chunk_base + (uint64_t)s;  // slots never move
       o = shadeVertex(A, S, P, st, s, g, depth, counters, [&](const Spec& L) {
-        splatSample(film, P, g, L, counters + C_NONFINITE, PassFilter{});
+        splatSample(film, P, g, L, counters + C_NONFINITE, TableFilter{filter});
       });
     }
     queueAppend(o.shadow, s, Q.shadow, counters + C_SHADOW);
@@ -199,6 +202,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, Pass
 // the vertex's radiance and the continuation (Path.hs:60-87)
 __global__ void __launch_bounds__(128) k_resolve(DevAccel A, DevShading S, PassParams P, Slots st,
                                                  Queues Q, int live_out, float* __restrict__ film,
+                                                 const float* filter,
                                                  unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_RESOLVE];
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -212,7 +216,9 @@ __global__ void __launch_bounds__(128) k_resolve(DevAccel A, DevShading S, PassP
       Spec Tn, Ln;
       cont = resolveVertex(
           A, S, st, s, counters,
-          [&](const Spec& L) { splatSample(film, P, g, L, counters + C_NONFINITE, PassFilter{}); },
+          [&](const Spec& L) {
+            splatSample(film, P, g, L, counters + C_NONFINITE, TableFilter{filter});
+          },
           Tn, Ln);
       if (cont) {
         storeBands(st.T, s, Tn);
@@ -238,8 +244,10 @@ struct Grids {
 };
 Grids g_grids[64];
 bool g_grids_ready[64] = {false};
+std::mutex g_grids_mu;  // callers on any thread
 
 Grids grids(int device, int sms) {
+  std::lock_guard<std::mutex> lk(g_grids_mu);
   if (device >= 0 && device < 64 && g_grids_ready[device]) return g_grids[device];
   Grids g;
   // both layouts' kernels use the same registers within a few; take the smaller grid
@@ -260,7 +268,7 @@ Grids grids(int device, int sms) {
 // the bounces of one chunk of path samples
 cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S, PassParams P,
                      Slots st, Queues Q, unsigned long long* counters, int64_t count, int max_depth,
-                     float* d_film, const Grids& G) {
+                     float* d_film, const float* d_filter, const Grids& G) {
   const int block = 128;
   unsigned g_ray = (unsigned)std::min<int64_t>((count + block - 1) / block, (int64_t)G.raygen);
   k_raygen<<<g_ray, block, 0, stream>>>(P, S.camera, st, count, Q.live[0], counters);
@@ -281,7 +289,8 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
     k_class_scatter<<<G.raygen, block, 0, stream>>>(Q.live[in], counters + C_LIVE0 + in, Q.cls,
                                                      Q.sorted, counters);
     k_shade<<<std::min(G.shade, cap_blocks), block, 0, stream>>>(A, S, P, st, Q, depth,
-                                                                  C_LIVE0 + in, d_film, counters);
+                                                                  C_LIVE0 + in, d_film, d_filter,
+                                                                  counters);
     if (A.wide) {
       k_trace_shadow<true><<<gs, block, 0, stream>>>(A, st, Q.shadow, counters);
       k_trace_mis<true><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);
@@ -291,7 +300,7 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
     }
     k_resolve<<<std::min(G.resolve, cap_blocks), block, 0, stream>>>(A, S, P, st, Q,
                                                                       C_LIVE0 + (1 - in), d_film,
-                                                                      counters);
+                                                                      d_filter, counters);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -353,12 +362,35 @@ void integrator_workspace_free(IntegratorWorkspace& ws) {
   ws = IntegratorWorkspace{};
 }
 
+// A workspace of at least `cap` path slots, or, when the device has no room
+// for that many, the largest of cap/2, cap/4, ... down to kMinWorkspaceSlots
+// (the pass runs in more chunks then).  A workspace already holding at least
+// the floor is kept when a larger one does not fit.
+constexpr size_t kMinWorkspaceSlots = size_t(1) << 20;
+
 static int ensureWorkspace(IntegratorWorkspace& ws, size_t cap, std::string& err) {
   if (ws.capacity >= cap && ws.buffer) return BLING_OK;
-  integrator_workspace_free(ws);
-  RET_CUDA(cudaMalloc(&ws.buffer, slotBytes(cap)));
-  ws.capacity = cap;
-  return BLING_OK;
+  const size_t floor_slots = std::min(cap, kMinWorkspaceSlots);
+  for (size_t c = cap;; c = std::max(floor_slots, (c / 2 + 63) / 64 * 64)) {
+    if (ws.buffer && ws.capacity >= c) return BLING_OK;  // the one we have is as large
+    void* buf = nullptr;
+    cudaError_t e = cudaMalloc(&buf, slotBytes(c));
+    if (e == cudaSuccess) {
+      integrator_workspace_free(ws);
+      ws.buffer = buf;
+      ws.capacity = c;
+      return BLING_OK;
+    }
+    if (e != cudaErrorMemoryAllocation) RET_CUDA(e);
+    (void)cudaGetLastError();  // clear the allocation error before trying smaller
+    if (c == floor_slots) break;
+  }
+  if (ws.buffer && ws.capacity >= floor_slots) return BLING_OK;
+  char buf[160];
+  snprintf(buf, sizeof buf, "no device memory for a path workspace of %zu slots (%zu bytes)",
+           floor_slots, slotBytes(floor_slots));
+  err = buf;
+  return BLING_ERR_OOM;
 }
 
 int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S,
@@ -375,9 +407,6 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
     err = "too many samples in one pass";
     return BLING_ERR_INVALID_ARG;
   }
-  float tbl[256];
-  filterTableHost(p.filter_kind, p.filter_params, P.fw, P.fh, tbl);
-  RET_CUDA(cudaMemcpyToSymbolAsync(c_filter, tbl, sizeof tbl, 0, cudaMemcpyHostToDevice, stream));
   size_t cap = (size_t)std::min<uint64_t>(total, uint64_t(1) << 24);
   // a multiple of 64 paths keeps every per-path array 16-byte aligned (the
   // records are read with 16-byte vector loads)
@@ -387,7 +416,11 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
   Slots st;
   Queues Q;
   unsigned long long* counters;
-  carve((unsigned char*)ws.buffer, ws.capacity, st, Q, counters);
+  float* d_filter;
+  carve((unsigned char*)ws.buffer, ws.capacity, st, Q, counters, d_filter);
+  float tbl[256];
+  filterTableHost(p.filter_kind, p.filter_params, P.fw, P.fh, tbl);
+  RET_CUDA(cudaMemcpyAsync(d_filter, tbl, sizeof tbl, cudaMemcpyHostToDevice, stream));
   RET_CUDA(cudaMemsetAsync(counters, 0, C_COUNT * sizeof(unsigned long long), stream));
   int sms = 0;
   RET_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
@@ -395,7 +428,7 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
   for (uint64_t base = 0; base < total; base += ws.capacity) {
     int64_t count = (int64_t)std::min<uint64_t>(ws.capacity, total - base);
     P.chunk_base = base;
-    RET_CUDA(runChunk(stream, A, S, P, st, Q, counters, count, p.max_depth, d_film, G));
+    RET_CUDA(runChunk(stream, A, S, P, st, Q, counters, count, p.max_depth, d_film, d_filter, G));
   }
   unsigned long long cnt[C_COUNT];
   RET_CUDA(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, stream));
@@ -410,19 +443,22 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
 
 // ------------------------------------------------------------------ no-allocation pass
 // Path state for bling_render_pass_noalloc, in one file-scope device array:
-// the wavefront of one pass of at most kNoAllocSlots path samples (slots,
-// queues and counters, laid out by carve()).  Every GPU that loads the library
-// holds it (about 35 MiB) until the process exits.  All calls share the array;
-// the counters are cleared at the start of every call and the path state is
-// written before it is read.  Two calls whose work overlaps on the GPU
-// (different streams or contexts on one device) race on it.
+// the wavefront of one pass of at most kNoAllocSlots path samples (counters,
+// filter table, slots and queues, laid out by carve()).  Every GPU that loads
+// the library holds it (about 35 MiB) until the process exits.  All calls
+// share the array; the counters and the filter table are written at the
+// start of every call and the path state is written before it is read.  Two
+// calls whose work overlaps on the GPU (different streams or contexts on one
+// device) race on it.
 constexpr size_t kNoAllocSlots = size_t(1) << 16;
-constexpr size_t kNoAllocBytes = kCounterBytes + (kSlotWords + kQueueWords) * 4 * kNoAllocSlots;
+constexpr size_t kNoAllocBytes =
+    kCounterBytes + kFilterBytes + (kSlotWords + kQueueWords) * 4 * kNoAllocSlots;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
 constexpr int kMaxDevices = 64;
 unsigned char* g_noalloc_ptr[kMaxDevices] = {nullptr};
+std::mutex g_noalloc_mu;  // guards the per-device address table
 }  // namespace
 
 size_t integrator_noalloc_max_samples() { return kNoAllocSlots; }
@@ -438,14 +474,38 @@ int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const
   }
   // set-up, once per device with that device current: the host-side name of
   // a __device__ array is not a device address, so fetch the address
-  if (!g_noalloc_ptr[device]) {
-    void* ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr) {
-      err = std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e);
-      return BLING_ERR_CUDA;
+  unsigned char* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+      void* ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess || !ptr) {
+        err = std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e);
+        return BLING_ERR_CUDA;
+      }
+      g_noalloc_ptr[device] = (unsigned char*)ptr;
     }
-    g_noalloc_ptr[device] = (unsigned char*)ptr;
+    scratch = g_noalloc_ptr[device];
+  }
+  // the film must be device memory of this device: a host pointer would fault
+  // in the kernels
+  {
+    cudaPointerAttributes pa;
+    cudaError_t e = cudaPointerGetAttributes(&pa, d_film);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      err = std::string("film pointer: ") + cudaGetErrorString(e);
+      return BLING_ERR_INVALID_ARG;
+    }
+    if (pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged) {
+      err = "the film must be device memory (cudaMalloc or managed), not a host pointer";
+      return BLING_ERR_INVALID_ARG;
+    }
+    if (pa.device != device) {
+      err = "the film lives on another device than the scene";
+      return BLING_ERR_INVALID_ARG;
+    }
   }
   RET_CUDA(loadCieConstants(device));
   PassParams P;
@@ -461,19 +521,21 @@ int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const
     err = buf;
     return BLING_ERR_BOUNDS;
   }
-  float tbl[256];
-  filterTableHost(p.filter_kind, p.filter_params, P.fw, P.fh, tbl);
-  RET_CUDA(cudaMemcpyToSymbolAsync(c_filter, tbl, sizeof tbl, 0, cudaMemcpyHostToDevice, stream));
   Slots st;
   Queues Q;
   unsigned long long* counters;
-  carve(g_noalloc_ptr[device], kNoAllocSlots, st, Q, counters);
+  float* d_filter;
+  carve(scratch, kNoAllocSlots, st, Q, counters, d_filter);
+  float tbl[256];
+  filterTableHost(p.filter_kind, p.filter_params, P.fw, P.fh, tbl);
+  RET_CUDA(cudaMemcpyAsync(d_filter, tbl, sizeof tbl, cudaMemcpyHostToDevice, stream));
   RET_CUDA(cudaMemsetAsync(counters, 0, C_COUNT * sizeof(unsigned long long), stream));
   int sms = 0;
   RET_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   Grids G = grids(device, sms);
   P.chunk_base = 0;
-  RET_CUDA(runChunk(stream, A, S, P, st, Q, counters, (int64_t)total, p.max_depth, d_film, G));
+  RET_CUDA(runChunk(stream, A, S, P, st, Q, counters, (int64_t)total, p.max_depth, d_film, d_filter,
+                    G));
   unsigned long long cnt[C_COUNT];
   RET_CUDA(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, stream));
   RET_CUDA(cudaStreamSynchronize(stream));

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <vector>
+#include <mutex>
 
 #include "dmath.cuh"
 #include "dshape.cuh"
@@ -75,9 +76,12 @@ __device__ __forceinline__ Spec sClamp01(const Spec& a) {
 static __constant__ float c_cieX[16], c_cieY[16], c_cieZ[16];
 static __constant__ float c_cieYSum;
 
-// fills this translation unit's CIE tables on the current device (once per device)
+// fills this translation unit's CIE tables on the current device (once per
+// device; callers on several threads serialise on a mutex)
 static cudaError_t loadCieConstants(int device) {
+  static std::mutex mu;
   static bool ready[64] = {false};
+  std::lock_guard<std::mutex> g(mu);
   if (device >= 0 && device < 64 && ready[device]) return cudaSuccess;
   auto bits = [](uint32_t b) {
     float f;
@@ -1207,7 +1211,12 @@ static __device__ BLING_OUTLINE float lightPdf(const DevAccel& A, const DLight& 
 }
 
 // ------------------------------------------------------------------ film
-static __constant__ float c_filter[256];
+// the pass's 16x16 filter table in device memory (the caller's workspace), so
+// passes of different contexts on one device never share it
+struct TableFilter {
+  const float* t;
+  __device__ __forceinline__ float operator()(int i) const { return __ldg(t + i); }
+};
 
 // addSample (Image.hs:250-299) into the tile image of the sample's tile
 // (mkImageTile/addTile, Image.hs:108-120,178-199): the footprint is clipped to

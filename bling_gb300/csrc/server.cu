@@ -57,6 +57,7 @@ struct bling_server {
   uint64_t in_use = 0;      // base_bytes + films of admitted jobs
   int iters_per_step = 4;
   int max_jobs = 1024;
+  int64_t fail_after = -1;  // test hook: the step after this many more steps fails (-1: none)
   uint64_t slice = 1 << 20;    // samples per slice handed to the batch
   uint64_t backlog = 1 << 21;  // submitted but unstarted samples kept queued
   std::chrono::steady_clock::time_point t0;
@@ -162,8 +163,25 @@ void serveRound(bling_server* S, std::vector<ServerJob*>& admit, std::vector<Ser
     j->sent += n;
     queued += n;
   }
-  int rc = batch_step(S->eng, S->iters_per_step, err);
+  int rc;
+  bool inject = false;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->fail_after == 0) inject = true;
+    if (S->fail_after >= 0) S->fail_after -= 1;
+  }
+  if (inject) {
+    rc = BLING_ERR_CUDA;
+    err = "injected step failure (bling_server_debug_fail_step)";
+  } else {
+    rc = batch_step(S->eng, S->iters_per_step, err);
+  }
   if (rc != BLING_OK) {
+    // the engine's job table and paths in flight still point at the running
+    // jobs' films: drop them before the films are released, so that no later
+    // step writes into freed (and possibly reused) memory
+    std::string cerr;
+    if (batch_cancel(S->eng, cerr) != BLING_OK) err += "; cancelling the batch: " + cerr;
     for (ServerJob* j : running) {
       failJob(j, rc, err);
       if (j->d_film) cudaFree(j->d_film);
@@ -270,6 +288,7 @@ int bling_server_create(bling_ctx* c, const bling_server_opts* o, bling_server**
     cfg.sort_rays = b.sort_rays != 0;
     if (b.graph_mode) cfg.graph_mode = b.graph_mode;
     if (b.iters_per_launch) cfg.iters_per_launch = b.iters_per_launch;
+    cfg.max_run_iterations = b.max_run_iterations > 0 ? b.max_run_iterations : 0;
     if (o->hbm_budget_bytes) budget = o->hbm_budget_bytes;
     if (o->iters_per_step > 0) S->iters_per_step = o->iters_per_step;
   }
@@ -413,6 +432,13 @@ int bling_server_stats_get(bling_server* S, bling_server_stats* out) {
   out->rays_closest = bs.rays_closest;
   out->rays_any = bs.rays_any;
   out->iterations = bs.iterations;
+  return BLING_OK;
+}
+
+int bling_server_debug_fail_step(bling_server* S, int32_t after_steps) {
+  if (!S || after_steps < -1) return BLING_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->fail_after = after_steps;
   return BLING_OK;
 }
 

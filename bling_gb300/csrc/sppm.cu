@@ -44,6 +44,9 @@ namespace {
 enum : int {
   S_NODES0 = 0, S_NODES1 = 1, S_NEXT_TRACE = 2, S_CLOSEST = 3, S_HP = 4, S_NODE_OVF = 5,
   S_NONFINITE = 6, S_DEGENERATE = 7, S_PLIVE0 = 8, S_PLIVE1 = 9, S_SPLATS = 10,
+  // S_CLOSEST, S_NONFINITE, S_DEGENERATE as they were before the camera chunk
+  // being run, restored when the chunk runs again with larger buffers
+  S_SAVED_CLOSEST = 11, S_SAVED_NONFINITE = 12, S_SAVED_DEGENERATE = 13,
   S_COUNT = 16
 };
 // 32-bit words after the 8-byte counters: r2 max (float bits), ordered p min/max
@@ -144,10 +147,6 @@ inline float fromOrdered(uint32_t o) {
   memcpy(&f, &b, 4);
   return f;
 }
-
-struct SppmFilter {
-  __device__ __forceinline__ float operator()(int i) const { return c_filter[i]; }
-};
 
 // ------------------------------------------------------------------ camera pass
 __global__ void __launch_bounds__(128) k_sp_camgen(PassParams P, bling_camera_desc cam, SpCam cs,
@@ -282,12 +281,12 @@ __global__ void __launch_bounds__(128, 4) k_sp_camshade(DevAccel A, DevShading S
 
 // addSample of every camera sample's gathered emission (SPPM.hs:152-156)
 __global__ void __launch_bounds__(128) k_sp_camfilm(PassParams P, SpCam cs, int64_t count,
-                                                    float* __restrict__ film,
+                                                    float* __restrict__ film, const float* filter,
                                                     unsigned long long* counters) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
        i += (int64_t)gridDim.x * blockDim.x)
     splatSample(film, P, P.chunk_base + (uint64_t)i, loadBands(cs.Ls, (int)i),
-                counters + S_NONFINITE, SppmFilter{});
+                counters + S_NONFINITE, TableFilter{filter});
 }
 
 // ------------------------------------------------------------------ spatial hash
@@ -755,12 +754,19 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
   PassParams P;
   int rc = integrator_pass_params(a.rp, 2 * a.pass, a.rp.width, a.rp.height, P, err);
   if (rc) return rc;
+  // counters, then the pass's 16x16 filter table
+  if (!ws.counters) RET_CUDA(cudaMalloc(&ws.counters, kSpCounterBytes + 256 * sizeof(float)));
+  unsigned long long* counters = ws.counters;
+  float* d_filter = (float*)((unsigned char*)ws.counters + kSpCounterBytes);
   float tbl[256];
   filterTableHost(a.rp.filter_kind, a.rp.filter_params, P.fw, P.fh, tbl);
-  RET_CUDA(cudaMemcpyToSymbolAsync(c_filter, tbl, sizeof tbl, 0, cudaMemcpyHostToDevice, stream));
-  if (!ws.counters) RET_CUDA(cudaMalloc(&ws.counters, kSpCounterBytes));
-  unsigned long long* counters = ws.counters;
+  RET_CUDA(cudaMemcpyAsync(d_filter, tbl, sizeof tbl, cudaMemcpyHostToDevice, stream));
   RET_CUDA(cudaMemsetAsync(counters, 0, kSpCounterBytes, stream));
+  // device-side copies of three statistics counters around a camera chunk
+  auto copyCounter = [&](int to, int from) {
+    return cudaMemcpyAsync(counters + to, counters + from, sizeof(unsigned long long),
+                           cudaMemcpyDeviceToDevice, stream);
+  };
   int sms = 0;
   RET_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   const int block = 128;
@@ -796,6 +802,9 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
     unsigned cap_blocks = (unsigned)std::max<int64_t>(1, (count + block - 1) / block);
     RET_CUDA(cudaMemcpyAsync(counters + S_HP, &nh, sizeof nh, cudaMemcpyHostToDevice, stream));
     RET_CUDA(cudaMemsetAsync(counters + S_NODE_OVF, 0, sizeof(unsigned long long), stream));
+    RET_CUDA(copyCounter(S_SAVED_CLOSEST, S_CLOSEST));
+    RET_CUDA(copyCounter(S_SAVED_NONFINITE, S_NONFINITE));
+    RET_CUDA(copyCounter(S_SAVED_DEGENERATE, S_DEGENERATE));
     k_sp_camgen<<<std::min(g_wide, cap_blocks), block, 0, stream>>>(P, S.camera, cs, count, counters);
     for (int d = 0; d < a.max_depth; d++) {
       int in = d & 1;
@@ -823,6 +832,9 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
       size_t have = camBytes(ws.cam_samples, ws.cam_nodes);
       RET_CUDA(growTo(ws.cam, have, camBytes(ws.cam_samples, NC2)));
       ws.cam_nodes = NC2;
+      RET_CUDA(copyCounter(S_CLOSEST, S_SAVED_CLOSEST));  // the rerun counts afresh
+      RET_CUDA(copyCounter(S_NONFINITE, S_SAVED_NONFINITE));
+      RET_CUDA(copyCounter(S_DEGENERATE, S_SAVED_DEGENERATE));
       continue;  // run the chunk again
     }
     if (c2[S_HP] > ws.hp_cap) {  // more hit points than the buffer holds: grow, keep the earlier ones
@@ -844,9 +856,13 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
       cudaFree(ws.hp);
       ws.hp = nbuf;
       ws.hp_cap = H2;
+      RET_CUDA(copyCounter(S_CLOSEST, S_SAVED_CLOSEST));  // the rerun counts afresh
+      RET_CUDA(copyCounter(S_NONFINITE, S_SAVED_NONFINITE));
+      RET_CUDA(copyCounter(S_DEGENERATE, S_SAVED_DEGENERATE));
       continue;  // run the chunk again
     }
-    k_sp_camfilm<<<std::min(g_wide, cap_blocks), block, 0, stream>>>(P, cs, count, d_film, counters);
+    k_sp_camfilm<<<std::min(g_wide, cap_blocks), block, 0, stream>>>(P, cs, count, d_film, d_filter,
+                                                                       counters);
     RET_CUDA(cudaGetLastError());
     nh = c2[S_HP];
     base += count;

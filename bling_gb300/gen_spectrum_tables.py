@@ -118,8 +118,10 @@ def hexf(x: np.float32) -> str:
 
 
 def main(argv):
-    src_path = Path(argv[1]) if len(argv) > 1 else Path(
-        "/root/reference/src/lib/Graphics/Bling/Spectrum.hs")
+    if len(argv) < 2:
+        raise SystemExit("usage: gen_spectrum_tables.py <bling's src/lib/Graphics/Bling/Spectrum.hs>"
+                         " [output header]")
+    src_path = Path(argv[1])
     out_path = Path(argv[2]) if len(argv) > 2 else Path(__file__).with_name("csrc") / "spectrum_tables.h"
     src = src_path.read_text()
 

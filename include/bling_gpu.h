@@ -380,6 +380,8 @@ int bling_film_resolve_splats(bling_film* film, float splat_weight, float* host_
  *
  *  - The film is the caller's device buffer `d_film_wxyz`, width*height*4
  *    floats (w, X, Y, Z), accumulated in place (zero it before the first pass).
+ *    It must be device (or managed) memory of the scene's device: anything
+ *    else is refused with BLING_ERR_INVALID_ARG before any launch.
  *  - The path state lives in a static device array inside the library,
  *    reserved in every process that loads it on every GPU it runs on (about
  *    35 MiB), so one call renders at most 65536 path samples: sample-extent
@@ -432,7 +434,9 @@ typedef struct bling_batch_opts {
                                octant and origin cell (Morton order) before tracing */
   int32_t graph_mode;       /* BLING_BATCH_* ; default (0 given) is plain launches */
   int32_t iters_per_launch; /* BLING_BATCH_DEVICE_LOOP only; 0 = 16 */
-  int32_t reserved;
+  int32_t max_run_iterations; /* bling_batch_run returns BLING_ERR_TIMEOUT after this many
+                                 iterations with jobs still incomplete (they stay in flight);
+                                 0 = a bound derived from the submitted work */
 } bling_batch_opts;
 
 typedef struct bling_batch_stats {
@@ -505,6 +509,12 @@ int bling_server_wait(bling_server* server, int64_t ticket, int32_t timeout_ms, 
                       bling_job_times* times);
 int bling_server_stats_get(bling_server* server, bling_server_stats* out);
 const char* bling_server_last_error(bling_server* server);
+/* Test hook (no counterpart in the reference): after `after_steps` more
+ * wavefront steps, the next step fails on the host with BLING_ERR_CUDA
+ * without launching anything, as a failed launch would; -1 disarms.  The
+ * running jobs fail, the batch drops their work before their films are
+ * released, and later jobs render normally. */
+int bling_server_debug_fail_step(bling_server* server, int32_t after_steps);
 
 /* ---- host helpers for building scenes (no GPU needed) ---- */
 /* Builds the BVH of n primitive boxes (lo/hi: 3n floats each) on the host and

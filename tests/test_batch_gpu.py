@@ -159,3 +159,26 @@ def test_job_table_capacity_and_validation(gpu_ctx):
     with pytest.raises(BlingError):
         Batch(gpu_ctx, max_jobs=3)
     b.close()
+
+
+def test_run_returns_timeout_at_its_iteration_bound_and_continues_later(gpu_ctx):
+    """bling_batch_run stops with BLING_ERR_TIMEOUT once max_run_iterations
+    iterations ran with work left; the job stays in flight, and stepping on
+    completes it with the film the job renders alone."""
+    sc = S.cornell_room(48, 48)
+    g = gpu_ctx.scene(sc)
+    p = S.cornell_params(48, 48, spp_side=4, max_depth=5, rr_depth=3, seed=21)
+    b = Batch(gpu_ctx, slots=4096, max_run_iterations=3)
+    film = gpu_ctx.film(48, 48)
+    job = b.submit(g, film, p, 0)
+    with pytest.raises(BlingError) as e:
+        b.run()
+    assert e.value.code == abi.BLING_ERR_TIMEOUT
+    done, total = b.status(job)
+    assert 0 < total and done < total
+    assert b.stats()["iterations"] == 3
+    while not b.done(job):
+        b.step(8)
+    ref, _ = _alone(gpu_ctx, g, p, 0)
+    _same(film.read(), ref)
+    b.close()

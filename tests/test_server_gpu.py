@@ -178,3 +178,29 @@ def test_short_job_overtakes_a_long_one():
         _same(f_long, _alone(ctx, sc, long_p, 0))
     finally:
         ctx.close()
+
+
+def test_failed_step_drops_the_running_jobs_and_later_jobs_render_as_alone(gpu_ctx):
+    """A step that fails (injected on the host after one good step, so paths
+    of the running job are in flight) fails the running job; the batch drops
+    that job's work before its film is released, and a job submitted
+    afterwards -- whose film may reuse the released memory -- renders exactly
+    as it does alone."""
+    sc = S.cornell_room(64, 64)
+    g = gpu_ctx.scene(sc)
+    srv = Server(gpu_ctx, slots=8192, iters_per_step=2)
+    srv.debug_fail_step(1)
+    p_first = S.cornell_params(64, 64, spp_side=4, max_depth=5, rr_depth=3, seed=11)
+    t = srv.submit(g, p_first, 0)
+    with pytest.raises(BlingError) as e:
+        srv.wait(t)
+    assert e.value.code == abi.BLING_ERR_CUDA
+    assert "injected" in str(e.value)
+    p_next = S.cornell_params(64, 64, spp_side=2, max_depth=5, rr_depth=3, seed=12)
+    tickets = [srv.submit(g, p_next, k) for k in range(2)]
+    res = [srv.wait(tk) for tk in tickets]
+    st = srv.stats()
+    srv.close()
+    assert st["jobs_failed"] == 1 and st["jobs_done"] == 2
+    for k, (film, _) in enumerate(res):
+        _same(film, _alone(gpu_ctx, sc, p_next, k))

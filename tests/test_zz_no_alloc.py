@@ -10,7 +10,9 @@ samples per call).
 
 Checked here through the C ABI: two calls in a row agree with the allocating
 entry point (bling_render_pass) on the same film-sized job, within the render
-tests' tolerance, and a pass over the limit is refused with a clear error.
+tests' tolerance, and with the CPU oracle within the parity bar of the render
+tests; a pass over the limit and a film that is host memory are refused with a
+clear error before anything runs on the device.
 This file is collected last, so a run that stops at the first failure has
 already run every other test.
 """
@@ -23,6 +25,7 @@ import torch
 from bling_gb300 import abi
 from bling_gb300 import scene as S
 from bling_gb300.api import lib
+from oracle.oracle import OracleScene
 
 pytestmark = pytest.mark.gpu
 
@@ -56,6 +59,33 @@ def test_noalloc_pass_matches_render_pass_twice(gpu_ctx):
         # same kernels, same random numbers: only the order of atomic adds differs
         assert np.allclose(out[..., 1:], ref[..., 1:], rtol=1e-5, atol=1e-6)
         assert out[..., 2].mean() > 0
+    # the two passes against the oracle's: weights exact (box filter), XYZ
+    # within 1e-3 relative for >= 97% of pixels, image means within 0.5%
+    o = OracleScene(sc)
+    fo, _ = o.render_pass(params, 0)
+    fo, _ = o.render_pass(params, 1, fo)
+    out = d_film.cpu().numpy()
+    assert np.array_equal(out[..., 0], fo[..., 0])
+    scale = np.abs(fo[..., 1:]).mean() + 1e-12
+    err = np.abs(out[..., 1:] - fo[..., 1:]) / (np.abs(fo[..., 1:]) + 1e-3 * scale)
+    assert (err <= 1e-3).all(-1).mean() >= 0.97
+    m_g, m_o = out[..., 1:].mean(axis=(0, 1)), fo[..., 1:].mean(axis=(0, 1))
+    assert np.all(np.abs(m_g - m_o) <= 5e-3 * np.abs(m_o))
+
+
+def test_noalloc_pass_refuses_a_host_film(gpu_ctx):
+    """A film in host memory is refused on the host (the pointer's memory
+    type is checked before any launch), so no kernel ever sees it."""
+    L = _bind()
+    w = h = 16
+    sc = S.cornell_room(w, h)
+    params = S.cornell_params(w, h, spp_side=1)
+    g = gpu_ctx.scene(sc)
+    host = np.zeros((h, w, 4), np.float32)
+    rc = L.bling_render_pass_noalloc(g.h, C.byref(params), 0, C.c_void_p(host.ctypes.data))
+    assert rc == abi.BLING_ERR_INVALID_ARG
+    assert "device memory" in L.bling_last_error(gpu_ctx.h).decode()
+    assert not host.any()
 
 
 def test_noalloc_pass_refuses_oversized_passes(gpu_ctx):
