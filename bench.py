@@ -15,9 +15,12 @@ Metric: Mrays/s over all traversal queries (closest + any).
           of the rays and D2H copy of (t, prim) / hit flags inside the timed
           region
   cpu_baseline / --impl reference
-          the CPU oracle (a C++ restatement of the reference's Haskell
-          intersection code; the Haskell reference cannot be built here) on a
-          bounded sample of the same rays, all host cores
+          the reference's algorithm on the host cores: the CPU oracle's
+          restatement of its kd-tree (exact-event SAH build and front-to-back
+          traversal, Primitive/KdTree.hs) and intersection code, on a bounded
+          sample of the same rays, all host cores (the Haskell reference has
+          no toolchain here); kd-tree build time and node/leaf counts beside
+          it
 
 Multi-GPU: the path does not shard -- `--gpus N` runs N independent replicas
 (one per rank, torchrun), `value` = all ranks' rays / the slowest rank's time.
@@ -154,25 +157,41 @@ def barrier(world: int):
         dist.barrier()
 
 
-def cpu_oracle_rate(soup, rays_np, ra_np, n_sample: int):
-    """Mrays/s of the CPU oracle (closest + any over a bounded sample)."""
+def kd_oracle(scene):
+    """The CPU oracle of a scene with the reference's kd-tree built: returns
+    (oracle, {"build_s", kd-tree statistics})."""
     from oracle.oracle import OracleScene
-    o = OracleScene(soup)
+    o = OracleScene(scene)
+    t0 = time.perf_counter()
+    st = o.kdtree()
+    info = {"build_s": round(time.perf_counter() - t0, 3)}
+    info.update(st)
+    o.use_kdtree(True)
+    return o, info
+
+
+def cpu_oracle_rate(soup, rays_np, ra_np, n_sample: int):
+    """Mrays/s of the reference's kd-tree traversal on the host cores (closest
+    + any over a bounded sample)."""
+    o, kd = kd_oracle(soup)
     nc = n_sample
     na = n_sample // 2
     rc = np.ascontiguousarray(rays_np[:, :nc])
     rr = np.ascontiguousarray(ra_np[:, :na])
     t0 = time.perf_counter()
-    o.closest(rc)
-    o.any(rr)
+    o.closest_kd(rc)
+    o.any_kd(rr)
     dt = time.perf_counter() - t0
     cores = os.cpu_count() or 1
-    return (nc + na) / dt / 1e6, cores, dt, f"{nc} closest + {na} any-hit rays of the same workload"
+    return ((nc + na) / dt / 1e6, cores, dt,
+            f"{nc} closest + {na} any-hit rays of the same workload through the kd-tree", kd)
 
 
 def run_reference(args):
-    """--impl reference: the reference's algorithm on the host cores (the CPU
-    oracle restatement; the Haskell reference has no toolchain here)."""
+    """--impl reference: the reference's algorithm on the host cores -- the
+    CPU oracle's restatement of its kd-tree build and traversal
+    (Primitive/KdTree.hs:81-246) and of its intersection code; the Haskell
+    reference has no toolchain here."""
     world, rank, _ = dist_env()
     if world > 1 and rank != 0:
         return
@@ -182,19 +201,23 @@ def run_reference(args):
     soup = S.triangle_soup(N_TRIS, seed=1)
     rays = S.soup_rays(N_RAYS if args.full_rays else (args.cpu_rays * 2), seed=2)
     ra = S.soup_rays(N_RAYS if args.full_rays else (args.cpu_rays * 2), seed=3, any_hit=True)
-    from oracle.oracle import OracleScene
-    o = OracleScene(soup)
+    o, kd = kd_oracle(soup)
     n = args.cpu_rays
     rc = np.ascontiguousarray(rays[:, :n])
     rr = np.ascontiguousarray(ra[:, :n // 2])
     for _ in range(args.warmup):
-        o.closest(rc[:, : max(1, n // 16)])
+        o.closest_kd(rc[:, : max(1, n // 16)])
     times = []
+    visits = None
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        o.closest(rc)
-        o.any(rr)
+        _, _, _, cc = o.closest_kd(rc)
+        _, ca = o.any_kd(rr)
         times.append(time.perf_counter() - t0)
+        visits = {"closest_nodes_per_ray": round(cc["nodes"] / n, 2),
+                  "closest_prims_per_ray": round(cc["prims"] / n, 2),
+                  "any_nodes_per_ray": round(ca["nodes"] / max(1, n // 2), 2),
+                  "any_prims_per_ray": round(ca["prims"] / max(1, n // 2), 2)}
     dt = float(np.mean(times))
     val = (n + n // 2) / dt / 1e6
     cores = os.cpu_count() or 1
@@ -205,10 +228,13 @@ def run_reference(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(args, world),
         "cpu_baseline": {"value": round(val, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
-                         "sample": f"{n} closest + {n // 2} any-hit rays per step (of 16M + 8M)"},
+                         "sample": f"{n} closest + {n // 2} any-hit rays per step (of 16M + 8M) "
+                                   "through the kd-tree"},
         "e2e": {"value": round(val, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "note": "reference is Haskell (GHC absent); its algorithm runs as the C++ oracle restatement",
+        "kdtree": dict(kd, **(visits or {})),
+        "note": "reference is Haskell (GHC absent); its kd-tree and intersection code run as the "
+                "C++ oracle restatement (oracle/kdtree.h, oracle/oracle.cpp)",
     }
     print(json.dumps(line), flush=True)
 
@@ -259,24 +285,43 @@ def measure_e2e(ctx, g, rays, ra, flush, args, world, dev):
             "d2h_bytes_per_step": N_RAYS * 8 + N_ANY * 1}
 
 
+def _cpu_render_rate(sc, p, bands):
+    """path samples/s of the oracle's path integrator through the reference's
+    kd-tree, all host threads, over `bands` = [(row_begin, row_end), ...] of
+    the sample extent; returns (cpu_baseline dict without "sample", kd info)"""
+    o, kd = kd_oracle(sc)
+    samples, dt = 0, 0.0
+    for rb, re_ in bands:
+        t0 = time.perf_counter()
+        _, st = o.render_pass(p, 0, rows=(rb, re_))
+        dt += time.perf_counter() - t0
+        samples += st["path_samples"]
+    return {"value": round(samples / dt, 1), "unit": "path samples/s",
+            "cores": os.cpu_count() or 1, "kind": "port"}, kd
+
+
 def measure_render(ctx, stream, args):
     """The path integrator on the two render workloads (secondary lines):
     path samples/s and Mrays/s (camera, continuation, BSDF-MIS and shadow
-    queries, counted on the device) per pass, CUDA events on the stream."""
+    queries, counted on the device) per pass, CUDA events on the stream.  The
+    large-mesh workload accumulates into an FP64-compensated film, as its
+    configuration asks.  Beside each: the oracle's path integrator through the
+    reference's kd-tree on the host cores (the whole Cornell image; 8 bands
+    of 2 rows spread over the heightfield image)."""
     import torch
 
     from bling_gb300 import scene as S
     out = {}
     cases = [("cornell_256x256_16spp_depth5", S.cornell_room(256, 256),
-              S.cornell_params(256, 256, spp_side=4, max_depth=5, rr_depth=3), 10)]
+              S.cornell_params(256, 256, spp_side=4, max_depth=5, rr_depth=3), 10, False)]
     if not args.no_heightfield:
         cases.append(("heightfield_8.4Mtri_4096spheres_1920x1080_64spp_depth8",
-                      S.heightfield_scene(), S.heightfield_params(1920, 1080, spp_side=8), 2))
-    for name, sc, p, passes in cases:
+                      S.heightfield_scene(), S.heightfield_params(1920, 1080, spp_side=8), 2, True))
+    for name, sc, p, passes, fp64 in cases:
         t0 = time.perf_counter()
         g = ctx.scene(sc)
         build_s = time.perf_counter() - t0
-        film = ctx.film(p.width, p.height)
+        film = ctx.film(p.width, p.height, fp64=fp64)
         g.render_pass(film, p, 0)  # warm-up pass
         s0 = g.stats()
         times = []
@@ -296,17 +341,21 @@ def measure_render(ctx, stream, args):
             "ms_per_pass": round(tot / passes * 1e3, 3), "passes": passes,
             "rays_per_path": round(rays / max(1, s1["path_samples"] - s0["path_samples"]), 3),
             "scene_build_s": round(build_s, 3), "bvh_build_ms": round(s1["bvh_build_ms"], 1),
-            "nonfinite_drops": s1["nonfinite_drops"]}
-        if name.startswith("cornell") and not args.no_cpu_baseline:
-            from oracle.oracle import OracleScene
-            o = OracleScene(sc)
-            t0 = time.perf_counter()
-            _, st = o.render_pass(p, 0, rows=(0, 48))
-            dt = time.perf_counter() - t0
-            out[name]["cpu_baseline"] = {
-                "value": round(st["path_samples"] / dt, 1), "unit": "path samples/s",
-                "cores": os.cpu_count() or 1, "kind": "port",
-                "sample": "rows 0-47 of the 258 x 258 sample extent, 16 spp, one pass"}
+            "nonfinite_drops": s1["nonfinite_drops"],
+            "film": "fp64-compensated" if fp64 else "fp32"}
+        if not args.no_cpu_baseline:
+            ny = p.height + 2  # box filter: the sample extent is one pixel wider on each side
+            if name.startswith("cornell"):
+                bands, what = [(0, ny)], f"the whole {p.width + 2} x {ny} sample extent"
+            else:
+                bands = [(int(k * ny / 8) + ny // 16, int(k * ny / 8) + ny // 16 + 2)
+                         for k in range(8)]
+                what = (f"8 bands of 2 rows spread over the {p.width + 2} x {ny} sample extent "
+                        f"(rows {', '.join(str(b[0]) for b in bands)})")
+            cpu, kd = _cpu_render_rate(sc, p, bands)
+            cpu["sample"] = f"{what}, {p.strata_x * p.strata_y} spp, one pass, kd-tree"
+            out[name]["cpu_baseline"] = cpu
+            out[name]["cpu_kdtree"] = kd
         del g, film
     return out
 
@@ -345,15 +394,14 @@ def measure_light(ctx, stream, args):
            "splats_per_photon": round((s1["light_splats"] - s0["light_splats"]) / (passes * n), 3),
            "nonfinite_drops": s1["nonfinite_drops"]}
     if not args.no_cpu_baseline:
-        from oracle.oracle import OracleScene
-        o = OracleScene(sc)
+        o, _ = kd_oracle(sc)
         m = 400_000
         t0 = time.perf_counter()
         o.light_pass(W, H, m, seed=1, pass_index=1)
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": round(m / dt, 1), "unit": "photons/s",
                                "cores": os.cpu_count() or 1, "kind": "port",
-                               "sample": f"{m} photons of one pass, all host threads"}
+                               "sample": f"{m} photons of one pass, all host threads, kd-tree"}
     del g, film
     return out
 
@@ -394,8 +442,7 @@ def measure_sppm(ctx, stream, args):
            "splats_per_photon": round((s1["light_splats"] - s0["light_splats"]) / (passes * sn * sn), 3),
            "passes": passes, "nonfinite_drops": s1["nonfinite_drops"]}
     if not args.no_cpu_baseline:
-        from oracle.oracle import OracleScene
-        o = OracleScene(sc)
+        o, _ = kd_oracle(sc)
         m = 250_000
         spc = abi.sppm_params(m, max_depth=5, radius=0.01, alpha=0.7, seed=1)
         t0 = time.perf_counter()
@@ -403,7 +450,8 @@ def measure_sppm(ctx, stream, args):
         dt = time.perf_counter() - t0
         out["cpu_baseline"] = {"value": round(m / dt, 1), "unit": "photons/s",
                                "cores": os.cpu_count() or 1, "kind": "port",
-                               "sample": f"one pass with {m} photons (camera pass included), all host threads"}
+                               "sample": f"one pass with {m} photons (camera pass included), "
+                                         "all host threads, kd-tree"}
     del g, film
     return out
 
@@ -741,24 +789,48 @@ def run_ours(args):
     if not args.no_serving and rank == 0:
         served = measure_serving(args)
 
-    # ---- roofline of the dominant kernel (closest hit)
+    # ---- roofline of the dominant kernel (closest hit).  Traversal reads the
+    # BVH and the leaf slots out of L2 (the 1M soup's ~100 MB working set
+    # stays resident), so the bound is the L2 read bandwidth, measured in this
+    # run by the probe kernel.  Algorithmic bytes per ray: 32 (ray) + 8 (t,
+    # primitive) + 32 per box test + 48 per leaf slot tested; a visit of a
+    # binary node tests its two children's boxes (64 B of node), a visit of
+    # an 8-wide node reads its 80 B node once.
     hbm_peak, peak_kind = peaks()
     counts = traversal_counts(g, rays)
-    node_bytes = 80 if args.wide_bvh else 64
-    bytes_per_ray = 32 + 8 + node_bytes * counts["nodes_per_ray"] + 48 * counts["slots_per_ray"]
+    box_tests = (80.0 / 32.0 if args.wide_bvh else 2.0) * counts["nodes_per_ray"]
+    bytes_per_ray = 32 + 8 + 32 * box_tests + 48 * counts["slots_per_ray"]
     closest_s = float(np.mean(closest_ms)) / 1e3
     achieved = bytes_per_ray * N_RAYS / closest_s / 1e9
     prof = profile_traffic()
     l2 = l2_read_peak(local)
     if l2:
-        l2["traversal_frac"] = round(achieved / l2["gbs"], 4)
+        roof = {"bound": "l2", "achieved": round(achieved, 1), "peak": l2["gbs"], "unit": "GB/s",
+                "frac": round(achieved / l2["gbs"], 4),
+                "peak_source": "measured in this run: " + l2["how"]}
+    else:
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(achieved / hbm_peak, 4), "peak_source": peak_kind}
+    roof.update({
+        "traffic": prof.get("dram_bytes_per_launch") if prof else None,
+        "traffic_source": (prof.get("captured") if prof else None),
+        "kernel": "k_trace_closest", "bvh_layout": "wide8" if args.wide_bvh else "binary",
+        "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
+        "bytes_per_ray_formula": "32 ray + 8 result + 32 x box tests + 48 x leaf slots",
+        "node_visits_per_ray": round(counts["nodes_per_ray"], 3),
+        "box_tests_per_ray": round(box_tests, 3),
+        "slots_per_ray": round(counts["slots_per_ray"], 3),
+        "rays_per_launch": N_RAYS,
+        "kernel_ms": round(closest_s * 1e3, 4),
+        "hbm_peak": hbm_peak, "hbm_peak_source": peak_kind,
+        "frac_of_hbm": round(achieved / hbm_peak, 4)})
 
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
-            rate, cores, dt, sample = cpu_oracle_rate(soup, rays, ra, args.cpu_rays)
+            rate, cores, dt, sample, kd = cpu_oracle_rate(soup, rays, ra, args.cpu_rays)
             cpu = {"value": round(rate, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
-                   "sample": sample}
+                   "sample": sample, "kdtree": kd}
         line = {
             "metric": "Mrays/s", "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -766,17 +838,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_config(args, world),
             "e2e": e2e,
-            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak,
-                         "unit": "GB/s", "frac": round(achieved / hbm_peak, 4),
-                         "traffic": prof.get("dram_bytes_per_launch") if prof else None,
-                         "peak_source": peak_kind,
-                         "kernel": "k_trace_closest",
-                         "bvh_layout": "wide8" if args.wide_bvh else "binary",
-                         "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
-                         "nodes_per_ray": round(counts["nodes_per_ray"], 3),
-                         "slots_per_ray": round(counts["slots_per_ray"], 3),
-                         "kernel_ms": round(closest_s * 1e3, 4),
-                         "l2_read_peak": l2},
+            "roofline": roof,
             "cpu_baseline": cpu,
             "gpu_launches": 2 * args.steps,
             "clocks": clk.summary(),

@@ -15,7 +15,7 @@ from pathlib import Path
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_build" / "liboracle.so"
 SRCS = [HERE / "oracle.cpp"]
-DEPS = SRCS + [HERE / "oracle.h", HERE / "oracle_math.h",
+DEPS = SRCS + [HERE / "oracle.h", HERE / "oracle_math.h", HERE / "kdtree.h",
                HERE.parent / "include" / "bling_gpu.h",
                HERE.parent / "bling_gb300" / "csrc" / "spectrum_tables.h"]
 FLAGS = ["-O3", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "../bling_gb300/csrc/spectrum_tables.h"
+#include "kdtree.h"
 #include "oracle_math.h"
 
 using namespace orc;
@@ -610,6 +611,11 @@ struct orc_scene {
   // oracle BVH
   std::vector<BvhNode> nodes;
   std::vector<int> order;
+  // the reference's kd-tree (kdtree.h), built on request; `use_kd` makes it
+  // the accelerator of scIntersect/occluded in the renderers
+  kd::Tree kd;
+  bool kd_built = false;
+  bool use_kd = false;
 };
 
 namespace {
@@ -930,6 +936,58 @@ static bool anyBvh(const orc_scene& S, const Ray& r) {
   return false;
 }
 
+// ---- the reference's kd-tree (kdtree.h) over the primitives' world bounds
+struct KdRay {
+  float o[3], d[3], tmin, tmax;
+};
+static inline KdRay kdRayOf(const Ray& r) {
+  return KdRay{{r.o.x, r.o.y, r.o.z}, {r.d.x, r.d.y, r.d.z}, r.tmin, r.tmax};
+}
+
+// kdTreePrimitive's intersect (KdTree.hs:240-242): the root interval, then
+// traverse with `nearest'` in the leaves
+static bool closestKd(const orc_scene& S, const Ray& r0, Hit& h, kd::Counts& c) {
+  KdRay r = kdRayOf(r0);
+  float tn, tf;
+  if (!kd::rootInterval(S.kd.bounds, r.o, r.d, r.tmin, r.tmax, tn, tf)) return false;
+  const float inv[3] = {1.0f / r.d[0], 1.0f / r.d[1], 1.0f / r.d[2]};
+  bool any = false;
+  auto hit = [&](int p, KdRay& kr) {
+    Ray q = r0;
+    q.tmax = kr.tmax;
+    float t, b1, b2;
+    if (primHitT(S, p, q, t, b1, b2)) {  // near: rayMax := intDist
+      kr.tmax = t;
+      h.t = t;
+      h.prim = p;
+      h.b1 = b1;
+      h.b2 = b2;
+      any = true;
+    }
+  };
+  kd::closest(S.kd, 0, r, inv, tn, tf, hit, c);
+  return any;
+}
+// kdTreePrimitive's intersects (KdTree.hs:244-246)
+static bool anyKd(const orc_scene& S, const Ray& r0, kd::Counts& c) {
+  KdRay r = kdRayOf(r0);
+  float tn, tf;
+  if (!kd::rootInterval(S.kd.bounds, r.o, r.d, r.tmin, r.tmax, tn, tf)) return false;
+  const float inv[3] = {1.0f / r.d[0], 1.0f / r.d[1], 1.0f / r.d[2]};
+  auto hit = [&](int p, const KdRay&) { return primHitAny(S, p, r0); };
+  return kd::any(S.kd, 0, r, inv, tn, tf, hit, c);
+}
+
+static void buildKd(orc_scene& S, int nth) {
+  std::vector<kd::Box> boxes(S.prims.size());
+  for (size_t i = 0; i < S.prims.size(); i++) {
+    AabbF b = primBounds(S, (int)i);  // worldBounds of the primitive
+    boxes[i] = kd::Box{{b.lo.x, b.lo.y, b.lo.z}, {b.hi.x, b.hi.y, b.hi.z}};
+  }
+  kd::build(S.kd, boxes, nth);
+  S.kd_built = true;
+}
+
 struct Isect {
   float t, eps;
   int prim;
@@ -938,7 +996,8 @@ struct Isect {
 // scIntersect returning the full Intersection (Primitive.hs:57-65, Geometry.hs:33-36)
 static bool sceneIntersect(const orc_scene& S, const Ray& r, Isect& it) {
   Hit h;
-  if (!closestBvh(S, r, h)) return false;
+  kd::Counts kc;
+  if (!(S.use_kd ? closestKd(S, r, h, kc) : closestBvh(S, r, h))) return false;
   const Prim& pr = S.prims[h.prim];
   it.t = h.t;
   it.prim = h.prim;
@@ -955,7 +1014,13 @@ static bool sceneIntersect(const orc_scene& S, const Ray& r, Isect& it) {
   }
   return true;
 }
-static bool occluded(const orc_scene& S, const Ray& r) { return anyBvh(S, r); }
+static bool occluded(const orc_scene& S, const Ray& r) {
+  if (S.use_kd) {
+    kd::Counts kc;
+    return anyKd(S, r, kc);
+  }
+  return anyBvh(S, r);
+}
 
 // ---------------------------------------------------------------- Monte Carlo
 // concentricSampleDisk (Montecarlo.hs:389-406)
@@ -2474,6 +2539,78 @@ void orc_trace_closest_bvh(const orc_scene* s, const float* rays, size_t n, floa
 }
 void orc_trace_any_bvh(const orc_scene* s, const float* rays, size_t n, uint8_t* hit, int nth) {
   parallelFor(n, nth, [&](size_t i) { hit[i] = anyBvh(*s, rayOf(rays, n, i)) ? 1 : 0; });
+}
+
+int orc_kdtree_build(orc_scene* s, int nth, int64_t* stats) {
+  if (!s) return BLING_ERR_INVALID_ARG;
+  if (!s->kd_built) buildKd(*s, nth > 0 ? nth : nthreadsOf(1 << 30));
+  if (stats) {
+    const kd::Stats& k = s->kd.stats;
+    int64_t v[8] = {k.interiors, k.leaves, k.empty_leaves, k.leaf_refs,
+                    k.max_leaf,  k.max_depth, k.depth_sum, s->kd.depth_limit};
+    memcpy(stats, v, sizeof v);
+  }
+  return BLING_OK;
+}
+
+int orc_scene_use_kdtree(orc_scene* s, int on, int nth) {
+  if (!s) return BLING_ERR_INVALID_ARG;
+  if (on && !s->kd_built) orc_kdtree_build(s, nth, nullptr);
+  s->use_kd = on != 0;
+  return BLING_OK;
+}
+
+int orc_trace_closest_kd(orc_scene* s, const float* rays, size_t n, float* t, int32_t* prim,
+                         float* b1b2, int nth, uint64_t* counts) {
+  if (!s) return BLING_ERR_INVALID_ARG;
+  if (!s->kd_built) orc_kdtree_build(s, nth, nullptr);
+  std::atomic<uint64_t> nodes{0}, prims{0};
+  parallelFor(n, nth, [&](size_t i) {
+    Hit h;
+    kd::Counts c;
+    Ray r = rayOf(rays, n, i);
+    if (closestKd(*s, r, h, c)) {
+      t[i] = h.t;
+      prim[i] = h.prim;
+      if (b1b2) {
+        b1b2[2 * i] = h.b1;
+        b1b2[2 * i + 1] = h.b2;
+      }
+    } else {
+      t[i] = INF;
+      prim[i] = -1;
+      if (b1b2) b1b2[2 * i] = b1b2[2 * i + 1] = 0;
+    }
+    if (counts) {
+      nodes.fetch_add((uint64_t)c.nodes, std::memory_order_relaxed);
+      prims.fetch_add((uint64_t)c.prims, std::memory_order_relaxed);
+    }
+  });
+  if (counts) {
+    counts[0] = nodes.load();
+    counts[1] = prims.load();
+  }
+  return BLING_OK;
+}
+
+int orc_trace_any_kd(orc_scene* s, const float* rays, size_t n, uint8_t* hit, int nth,
+                     uint64_t* counts) {
+  if (!s) return BLING_ERR_INVALID_ARG;
+  if (!s->kd_built) orc_kdtree_build(s, nth, nullptr);
+  std::atomic<uint64_t> nodes{0}, prims{0};
+  parallelFor(n, nth, [&](size_t i) {
+    kd::Counts c;
+    hit[i] = anyKd(*s, rayOf(rays, n, i), c) ? 1 : 0;
+    if (counts) {
+      nodes.fetch_add((uint64_t)c.nodes, std::memory_order_relaxed);
+      prims.fetch_add((uint64_t)c.prims, std::memory_order_relaxed);
+    }
+  });
+  if (counts) {
+    counts[0] = nodes.load();
+    counts[1] = prims.load();
+  }
+  return BLING_OK;
 }
 
 // sample extent (imageWindow', Image.hs:170-176)

@@ -31,6 +31,24 @@ void orc_trace_closest_bvh(const orc_scene* s, const float* rays, size_t n, floa
 void orc_trace_any_bvh(const orc_scene* s, const float* rays, size_t n, uint8_t* hit,
                        int nthreads);
 
+/* The reference's kd-tree (Primitive/KdTree.hs:81-246, restated in
+ * kdtree.h) over the primitives' world bounds, built once per scene.
+ * stats (8 entries): interior nodes, leaves, empty leaves, primitive
+ * references in leaves, largest leaf, deepest leaf, sum of leaf depths, the
+ * depth limit round(8 + 3 ln N). */
+int orc_kdtree_build(orc_scene* s, int nthreads, int64_t* stats);
+/* closest / any hit through the kd-tree with the reference's traversal
+ * order (traverse / traverse', KdTree.hs:209-246); counts (2 entries, may be
+ * NULL): nodes visited, primitive tests */
+int orc_trace_closest_kd(orc_scene* s, const float* rays, size_t n, float* t, int32_t* prim,
+                         float* b1b2, int nthreads, uint64_t* counts);
+int orc_trace_any_kd(orc_scene* s, const float* rays, size_t n, uint8_t* hit, int nthreads,
+                     uint64_t* counts);
+/* on != 0: the renderers (orc_render_pass, orc_light_pass, orc_sppm_pass)
+ * trace through the kd-tree instead of the oracle's BVH (built first if
+ * needed) */
+int orc_scene_use_kdtree(orc_scene* s, int on, int nthreads);
+
 /* Full render pass over the film-padded sample extent, film (w,X,Y,Z)
  * accumulated in place (width*height*4 floats).  Restates prender/tile
  * (Rendering.hs:111-150) with the path integrator (Path.hs).  Only the rows

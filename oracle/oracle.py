@@ -35,6 +35,12 @@ def lib():
                                        P(C.c_int32), P(C.c_float), C.c_int]
         for fn in ("orc_trace_any_brute", "orc_trace_any_bvh"):
             getattr(L, fn).argtypes = [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_uint8), C.c_int]
+        L.orc_kdtree_build.argtypes = [C.c_void_p, C.c_int, P(C.c_int64)]
+        L.orc_trace_closest_kd.argtypes = [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_float),
+                                           P(C.c_int32), P(C.c_float), C.c_int, P(C.c_uint64)]
+        L.orc_trace_any_kd.argtypes = [C.c_void_p, P(C.c_float), C.c_size_t, P(C.c_uint8),
+                                       C.c_int, P(C.c_uint64)]
+        L.orc_scene_use_kdtree.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.orc_render_pass.argtypes = [C.c_void_p, P(abi.RenderParams), C.c_uint64, P(C.c_float),
                                       C.c_int, C.c_int, C.c_int, P(C.c_uint64), P(C.c_uint64),
                                       P(C.c_uint64)]
@@ -107,6 +113,41 @@ class OracleScene:
         fn = lib().orc_trace_any_brute if brute else lib().orc_trace_any_bvh
         fn(self.h, fp(rays), n, hit.ctypes.data_as(C.POINTER(C.c_uint8)), nthreads)
         return hit
+
+    KD_STATS = ("interiors", "leaves", "empty_leaves", "leaf_refs", "max_leaf", "max_depth",
+                "depth_sum", "depth_limit")
+
+    def kdtree(self, nthreads=0) -> dict:
+        """Builds the reference's kd-tree (once) and returns its statistics."""
+        st = (C.c_int64 * 8)()
+        lib().orc_kdtree_build(self.h, nthreads, st)
+        return dict(zip(self.KD_STATS, list(st)))
+
+    def closest_kd(self, rays, nthreads=0):
+        """closest hits through the kd-tree in the reference's traversal
+        order; returns (t, prim, b1b2, {"nodes": .., "prims": ..})"""
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[1]
+        t = np.empty(n, np.float32)
+        prim = np.empty(n, np.int32)
+        b = np.empty(2 * n, np.float32)
+        cnt = (C.c_uint64 * 2)()
+        lib().orc_trace_closest_kd(self.h, fp(rays), n, fp(t),
+                                   prim.ctypes.data_as(C.POINTER(C.c_int32)), fp(b), nthreads, cnt)
+        return t, prim, b.reshape(n, 2), {"nodes": cnt[0], "prims": cnt[1]}
+
+    def any_kd(self, rays, nthreads=0):
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        n = rays.shape[1]
+        hit = np.empty(n, np.uint8)
+        cnt = (C.c_uint64 * 2)()
+        lib().orc_trace_any_kd(self.h, fp(rays), n, hit.ctypes.data_as(C.POINTER(C.c_uint8)),
+                               nthreads, cnt)
+        return hit, {"nodes": cnt[0], "prims": cnt[1]}
+
+    def use_kdtree(self, on=True, nthreads=0):
+        """the renderers trace through the kd-tree (True) or the oracle's BVH"""
+        lib().orc_scene_use_kdtree(self.h, int(bool(on)), nthreads)
 
     def render_pass(self, params, pass_index=0, film=None, rows=None, nthreads=0):
         if film is None:
