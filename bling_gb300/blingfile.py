@@ -69,6 +69,15 @@ class Job:
     sample_depth: int = 3
     photons_per_pass: int = 0          # renderer { light passPhotons N } (RendererParser.hs:28-30)
     sppm: tuple | None = None          # (photonCount, maxDepth, radius, alpha) (RendererParser.hs:40-45)
+    camera_view: tuple | None = None   # (camera-to-world, lens radius, focal distance, fov)
+
+    def camera_for(self, width: int, height: int) -> abi.CameraDesc:
+        """the file's camera built for another image size (mkPerspectiveCamera
+        takes the image size, Camera.hs:108-147), e.g. for a reduced render"""
+        from .scene import camera_desc
+        c2w, lr, fd, fov = self.camera_view
+        c2w_, r2c, w2r, ap = xf.perspective_camera(c2w, lr, fd, fov, width, height, full=True)
+        return camera_desc(c2w_, r2c, lr, fd, w2r, ap)
 
     def sppm_params(self, seed: int = 1) -> abi.SppmParams:
         """bling_sppm_params of a `renderer { sppm ... }` job (mkSPPM n md r alpha)"""
@@ -329,7 +338,7 @@ class _Parser:
         (kind, strata), (md, sd) = self.s.sampler, self.s.depths
         fk, fp = self.s.filter
         return Job(sc, self.s.res[0], self.s.res[1], fk, fp, self.s.renderer, kind, strata, md, sd,
-                   self.s.photons, self.s.sppm)
+                   self.s.photons, self.s.sppm, (c2w, float(lr), float(fd), fov))
 
     def p_size(self):
         self.s.res = (self.t.integ(), self.t.integ())

@@ -4,6 +4,7 @@ newest-first primitive and light order, transforms applied to mesh vertices
 with binary32 transPoint, face fans, shape constructors, materials, spectra,
 renderer selection; plus an oracle render of a parsed scene.  The GPU parity
 of a parsed scene is in test_render_gpu.py."""
+import sys
 from pathlib import Path
 
 import numpy as np
@@ -226,12 +227,15 @@ def test_parsed_scene_renders_on_the_oracle(job):
     assert film[..., 2].sum() > 0
 
 
-REF_EXAMPLES = Path("/root/reference/examples")
+def _examples_dir():
+    sys.path.insert(0, str(Path(__file__).resolve().parent / "golden"))
+    import make_example_scenes
+    return make_example_scenes.source_dir()
 
 
-@pytest.mark.skipif(not REF_EXAMPLES.exists(), reason="reference examples not present")
+@pytest.mark.skipif(_examples_dir() is None, reason="bling's examples directory not present")
 def test_reference_cornell_box_example_parses():
-    j = B.load(REF_EXAMPLES / "cornell-box.bling")
+    j = B.load(_examples_dir() / "cornell-box.bling")
     assert (j.width, j.height) == (480, 480)
     assert j.renderer == "sppm"  # the file's last renderer block
     assert j.scene.n_triangles == 30 and len(j.scene.shapes) == 1
