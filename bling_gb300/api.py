@@ -270,7 +270,7 @@ class GpuScene:
         self.ctx.check(lib().bling_light_pass(self.h, film.h, C.byref(p), pass_index))
 
     def sppm_pass(self, film: "Film", params, pass_index: int = 0):
-        """one SPPM pass (SPPM.hs:392-480): camera samples into the film,
+        """one SPPM pass (SPPM.hs:410-480): camera samples into the film,
         photon splats into its splat image; params: abi.SppmParams"""
         self.ctx.check(lib().bling_sppm_pass(self.h, film.h, C.byref(params), pass_index))
 
@@ -509,7 +509,7 @@ class GpuLightTracer:
 
 
 class GpuSPPM:
-    """``mkSPPM n md r alpha`` as a bling ``Renderer`` (SPPM.hs:462-480): pass
+    """``mkSPPM n md r alpha`` as a bling ``Renderer`` (SPPM.hs:466-480): pass
     n adds camera samples to the film and ceil(sqrt n)^2 photons' splats to
     its splat image, shrinks the radii, and reports the splat weight
     1 / (n sn^2).  The job's pixel filter applies to the camera samples."""

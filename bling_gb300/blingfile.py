@@ -5,7 +5,7 @@ Mirrors the reference's parser (``src/lib/Graphics/Bling/IO/*.hs``): the same
 objects, blocks and keywords, the same parser state and its defaults
 (``RenderJob.hs:24-33``), and the same order of primitives and lights, so a
 file renders through :class:`~bling_gb300.api.GpuPathRenderer` with the
-primitive IDs and light list ``mkScene`` would build (``Scene.hs:160-166``).
+primitive IDs and light list ``mkScene`` would build (``Scene.hs:37-43``).
 Numbers are rounded to binary32 once, as GHC's ``read :: Float`` does, and
 transforms, spectra and meshes are built with the binary32 restatements of
 ``Transform.hs`` and ``Spectrum.hs`` (``transform.py``, ``spectrum.py``).

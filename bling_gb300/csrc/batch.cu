@@ -172,7 +172,7 @@ __device__ __forceinline__ int findJob(const BatchJobDev* __restrict__ jobs, uns
   return (int)(lo & mask);
 }
 
-// camera rays of the samples started this iteration (fireRay, Camera.hs:146-164)
+// camera rays of the samples started this iteration (fireRay, Camera.hs:49-68)
 __global__ void __launch_bounds__(128) k_regen(BatchCtl* ctl, const BatchJobDev* __restrict__ jobs,
                                                unsigned job_mask, PathStates ps, size_t cap) {
   const unsigned long long n = ctl->regen_count, base = ctl->regen_base;

@@ -11,7 +11,7 @@
 //   k_trace         closest hit of the bounce rays (scIntersect)
 //   k_shade         emission on specular paths, the BSDF, one light sample and
 //                   one BSDF sample for MIS (sampleOneLight/estimateDirect,
-//                   Scene.hs:184-241), Russian roulette and the continuation
+//                   Scene.hs:61-118), Russian roulette and the continuation
 //                   sample; queues the shadow ray, the MIS ray and the vertex
 //   k_trace_shadow  any hit of the shadow rays (occluded)
 //   k_trace_mis     closest hit of the MIS rays
@@ -65,7 +65,7 @@ __device__ __forceinline__ unsigned* classCounts(unsigned long long* counters) {
 }
 
 // ------------------------------------------------------------------ kernels
-// camera rays (fireRay, Camera.hs:146-164) for samples [chunk_base, chunk_base + count)
+// camera rays (fireRay, Camera.hs:49-68) for samples [chunk_base, chunk_base + count)
 __global__ void k_raygen(PassParams P, bling_camera_desc cam, Slots st, int64_t count,
                          int32_t* __restrict__ queue, unsigned long long* counters) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(128, 10) k_trace(DevAccel A, Slots st, const i
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_CLOSEST, (unsigned long long)n);
 }
 
-// occlusion of the shadow rays (occluded, Scene.hs:168-170)
+// occlusion of the shadow rays (occluded, Scene.hs:45-47)
 template <bool WIDE>
 __global__ void __launch_bounds__(128, 10) k_trace_shadow(DevAccel A, Slots st,
                                                       const int32_t* __restrict__ queue,

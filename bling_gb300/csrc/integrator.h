@@ -63,7 +63,7 @@ inline void deriveMaterialSpectra(DMaterial& m) {
     }
     float u = 0.0f <= m.rough ? m.rough : 0.0f, v = 0.0f <= m.sigma ? m.sigma : 0.0f;
     float ex = 1.0f / u, ey = 1.0f / v;
-    m.rough = (ex > 10000 || std::isnan(ex)) ? 10000.0f : ex;  // fixExponent (Microfacet.hs:199-201)
+    m.rough = (ex > 10000 || std::isnan(ex)) ? 10000.0f : ex;  // fixExponent (Microfacet.hs:126-128)
     m.sigma = (ey > 10000 || std::isnan(ey)) ? 10000.0f : ey;
   }
 }

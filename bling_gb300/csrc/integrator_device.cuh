@@ -231,7 +231,7 @@ struct PassParams {
 };
 
 // ------------------------------------------------------------------ Monte Carlo
-// concentricSampleDisk (Montecarlo.hs:389-406)
+// concentricSampleDisk (Montecarlo.hs:160-179)
 __device__ __forceinline__ void concentricSampleDisk(float u1, float u2, float& ox, float& oy) {
   float sx = u1 * 2.0f - 1.0f, sy = u2 * 2.0f - 1.0f;
   if (sx == 0 && sy == 0) {
@@ -331,7 +331,7 @@ __device__ __forceinline__ Spec bxR(const BxDF& b) {
   return b.clampR ? sClamp01(s) : s;
 }
 
-// frDielectric (Fresnel.hs:146-180), one value for all bands
+// frDielectric (Fresnel.hs:21-56), one value for all bands
 __device__ __forceinline__ float frDielScalar(float etai, float etat, float cosi) {
   float c = hmax(0.0f, 1.0f - cosi * cosi);
   float costp = cosi > 0 ? c / (etat * etat) : c * (etat * etat);
@@ -352,7 +352,7 @@ __device__ __forceinline__ Spec rTimesFresnel(const BxDF& b, float cosi) {
     float f = frDielScalar(b.ei, b.et, cosi);
     return r * sConst(f);
   }
-  // frConductor (Fresnel.hs:183-195)
+  // frConductor (Fresnel.hs:58-70)
   float acosi = fabsf(cosi);
   Spec out;
 #pragma unroll
@@ -618,7 +618,7 @@ struct Bsdf {
   V3 p, ng;
 };
 
-// mkBsdf' with the material's BxDFs (Material.hs:228-292)
+// mkBsdf' with the material's BxDFs (Material.hs:32-127)
 static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ mats, int mi, V3 dgg_n, V3 dgs_p,
                              V3 dgs_n, V3 dgs_dpdu) {
   const DMaterial& m = mats[mi];
@@ -1095,7 +1095,7 @@ __device__ __forceinline__ const float* envTexel(const DLight& l, float u, float
   y = max(0, min(l.env_h - 1, y));
   return l.env + 16 * ((size_t)y * l.env_w + x);
 }
-// upperBound + sampleContinuous1D (Montecarlo.hs:282-301); findIndex (>= u)
+// upperBound + sampleContinuous1D (Montecarlo.hs:53-73); findIndex (>= u)
 // on a non-decreasing CDF is its lower bound
 static __device__ void sampleContinuous1D(const float* func, const float* cdf, int n, float fi, float u,
                                    float& x, float& pdf, int& off) {
@@ -1157,7 +1157,7 @@ static __device__ BLING_OUTLINE LightSample lightSample(const DevAccel& A, const
     ls.delta = true;
     return ls;
   }
-  // infinite (Light.hs:130-141), sampleContinuous2D (Montecarlo.hs:319-322)
+  // infinite (Light.hs:130-141), sampleContinuous2D (Montecarlo.hs:90-93)
   float v, pdf1, u, pdf0;
   int im, iu;
   sampleContinuous1D(l.cond_int, l.marg_cdf, l.env_h, l.marg_int, u2, v, pdf1, im);

@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(128, 4) k_lt_vertex(DevAccel A, DevShading S, 
   }
 }
 
-// occluded (Scene.hs:168-170) for the camera connections; the visible ones
+// occluded (Scene.hs:45-47) for the camera connections; the visible ones
 // are splatted
 template <bool WIDE>
 __global__ void __launch_bounds__(128, 10) k_lt_shadow(DevAccel A, LtSlots st,

@@ -1,8 +1,8 @@
 // Upload of the shading data the path integrator needs: materials, meshes
 // (vertices, indices, normals, uvs), per-primitive owners, shape emission and
-// the light list in the reference's order (mkScene, Scene.hs:160-166), with
+// the light list in the reference's order (mkScene, Scene.hs:37-43), with
 // the environment map's importance distribution (mkInfiniteAreaLight,
-// Light.hs:72-82; mkDist2D, Montecarlo.hs:309-317).
+// Light.hs:72-82; mkDist2D, Montecarlo.hs:79-88).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -27,7 +27,7 @@ float sYHost(const float* s) {
   for (int i = 0; i < 16; i++) acc = acc + s[i] * fbits(BLING_CIE_Y_BITS[i]);
   return acc / fbits(BLING_CIE_Y_SUM_BITS);
 }
-// mkDist1D (Montecarlo.hs:269-277)
+// mkDist1D (Montecarlo.hs:40-48)
 void mkDist1D(const float* func, int n, float* cdf, float& fi) {
   std::vector<float> i(n + 1);
   i[0] = 0;
@@ -147,7 +147,7 @@ int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
       if ((rc = up(l.env, (size_t)w * h * 64, &p))) return rc;
       o.env = (const float*)p;
       // mkInfiniteAreaLight's Dist2D over sY of each texel (Light.hs:76-82,
-      // Montecarlo.hs:309-317)
+      // Montecarlo.hs:79-88)
       std::vector<float> func((size_t)w * h), cdf((size_t)h * (w + 1)), cint(h), mcdf(h + 1);
       for (int v = 0; v < h; v++) {
         for (int u = 0; u < w; u++) {

@@ -1,8 +1,8 @@
 // Stochastic progressive photon mapping on the GPU.
 //
-// One pass of the reference's SPPM renderer (Renderer/SPPM.hs:392-480):
+// One pass of the reference's SPPM renderer (Renderer/SPPM.hs:410-480):
 //
-// 1. Camera pass (mkHitPoints, traceCam/followCam, SPPM.hs:79-164): one
+// 1. Camera pass (mkHitPoints, traceCam/followCam, SPPM.hs:77-164): one
 //    Random-sampler camera sample per pixel of the sample extent.  At every
 //    hit the path records a hit point if the BSDF has a non-specular part,
 //    then follows BOTH its specular reflection and its specular transmission
@@ -11,19 +11,19 @@
 //    (addSample).  The branching paths are a wavefront of nodes, each with
 //    its sample and its position in the sample's binary tree (heap index);
 //    the tree position keys the node's random numbers.
-// 2. Spatial hash (mkHash, SPPM.hs:283-323): cells of twice the largest
+// 2. Spatial hash (mkHash, SPPM.hs:297-353): cells of twice the largest
 //    radius over the hit points' bounds, one bucket per hit point, every hit
 //    point entered in the buckets of the cells its sphere's box covers, with
 //    the reference's cell hash.  A bucket is scanned linearly instead of
 //    through the reference's per-bucket kd-tree: both visit the bucket's hit
 //    points within their radius.
-// 3. Photon pass (tracePhoton/followPhoton, SPPM.hs:172-224): ceil(sqrt n)^2
+// 3. Photon pass (tracePhoton/followPhoton, SPPM.hs:170-243): ceil(sqrt n)^2
 //    photons with stratified sampler dimensions; at every non-specular hit the
 //    hit points of the hit's bucket within their radius get
 //    hpF * f * li / (|wi.ng| r^2 pi) splatted at their pixel and a photon
 //    counted; the photon continues by adjoint BSDF sampling, with Russian
 //    roulette (0.8) after its eighth vertex.
-// 4. Radius update (statsUpdate, SPPM.hs:258-279).
+// 4. Radius update (statsUpdate, SPPM.hs:272-295).
 //
 // The reference seeds its generators from system entropy; here the camera
 // pass keys the shared counter-based generator by (seed, 2 pass, pixel) and
@@ -101,14 +101,14 @@ struct PhotonParams {
   float wr;
 };
 
-// sIdx (SPPM.hs:248-253): a raster position's entry in the pixel statistics
+// sIdx (SPPM.hs:264-274): a raster position's entry in the pixel statistics
 __device__ __forceinline__ int64_t statIndex(const PassParams& P, float px, float py) {
   int w = P.x1 - P.x0, h = P.y1 - P.y0;
   int ix = min(w, (int)px), iy = min(h, (int)py);  // truncate
   return (int64_t)w * (iy - P.y0) + (ix - P.x0);
 }
 
-// hash (SPPM.hs:291-293) and the bucket of a cell
+// hash (SPPM.hs:303-305) and the bucket of a cell
 __host__ __device__ __forceinline__ long long cellBucket(long long x, long long y, long long z,
                                                          long long cnt) {
   long long h = (long long)((unsigned long long)x * 73856093ull ^ (unsigned long long)y * 19349663ull ^
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(128, 10) k_sp_camtrace(DevAccel A, CamNodes nb
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + S_CLOSEST, (unsigned long long)n);
 }
 
-// traceCam / followCam (SPPM.hs:79-135) for the nodes at tree depth `depth`
+// traceCam / followCam (SPPM.hs:77-131) for the nodes at tree depth `depth`
 __global__ void __launch_bounds__(128, 4) k_sp_camshade(DevAccel A, DevShading S, PassParams P,
                                                         SpCam cs, SpHp hp, const float* __restrict__ r2s,
                                                         int64_t stat_count, int in, int depth, int md,
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(128, 4) k_sp_camshade(DevAccel A, DevShading S
   }
 }
 
-// addSample of every camera sample's gathered emission (SPPM.hs:152-156)
+// addSample of every camera sample's gathered emission (SPPM.hs:150-154)
 __global__ void __launch_bounds__(128) k_sp_camfilm(PassParams P, SpCam cs, int64_t count,
                                                     float* __restrict__ film, const float* filter,
                                                     unsigned long long* counters) {
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(256) k_sp_bounds(SpHp hp, int64_t nh,
   }
 }
 
-// the cells a hit point's box covers (mkHash, SPPM.hs:306-319); FILL = false
+// the cells a hit point's box covers (mkHash, SPPM.hs:324-353); FILL = false
 // counts them per bucket, true enters the hit point
 template <bool FILL>
 __global__ void __launch_bounds__(128) k_sp_cells(SpHp hp, int64_t nh, V3 lo, float invSize,
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(1024) k_scan_add(uint32_t* __restrict__ out, i
 }
 
 // ------------------------------------------------------------------ photon pass
-// tracePhoton (SPPM.hs:172-185): photons [chunk_base, chunk_base + count)
+// tracePhoton (SPPM.hs:181-193): photons [chunk_base, chunk_base + count)
 __global__ void __launch_bounds__(128) k_sp_emit(DevAccel A, DevShading S, PhotonParams Q,
                                                  SpPhotons ph, int64_t count,
                                                  unsigned long long* counters) {
@@ -465,7 +465,7 @@ __global__ void __launch_bounds__(128, 10) k_sp_ptrace(DevAccel A, SpPhotons ph,
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + S_CLOSEST, (unsigned long long)n);
 }
 
-// followPhoton (SPPM.hs:187-224) at photon vertex `depth`: the hit, the
+// followPhoton (SPPM.hs:195-243) at photon vertex `depth`: the hit, the
 // number of hit points its lookup finds (their splats follow in k_sp_splat)
 // and the continuation
 __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, PhotonParams Q,
@@ -496,7 +496,7 @@ __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, 
         V3 p = bsdf.p;
         long long b = -1;
         if (bsdfHasNonSpecular(bsdf) && hs.cnt > 0) {
-          // hashLookup (SPPM.hs:295-302): the bucket of p's cell, scanned by k_sp_count
+          // hashLookup (SPPM.hs:307-314): the bucket of p's cell, scanned by k_sp_count
           float cx = fabsf((p.x - hs.lo.x) * hs.scale), cy = fabsf((p.y - hs.lo.y) * hs.scale),
                 cz = fabsf((p.z - hs.lo.z) * hs.scale);
           if (cx < 9.2e18f && cy < 9.2e18f && cz < 9.2e18f)
@@ -567,7 +567,7 @@ __device__ __forceinline__ void splatPair(const DevShading& S, const PassParams&
   if (si >= 0 && si < stat_count) atomicAdd(m + si, 1u);
 }
 
-// hashLookup/treeLookup (SPPM.hs:295-302, 360-373) with the splats: one warp
+// hashLookup/treeLookup (SPPM.hs:307-314, 391-408) with the splats: one warp
 // per live photon scans the photon's bucket 32 entries at a time; the hit
 // points within their radius go to the warp's queue in shared memory, and
 // every 32 queued pairs are splatted by the whole warp (one pair per lane).
@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(kGatherBlock) k_sp_gather(DevShading S, PassPa
   }
 }
 
-// statsUpdate (SPPM.hs:258-279)
+// statsUpdate (SPPM.hs:272-295)
 __global__ void __launch_bounds__(256) k_sp_stats(SppmPixelStats st, float alpha) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < st.count;
        i += (int64_t)gridDim.x * blockDim.x) {

@@ -22,7 +22,7 @@ struct SppmResult {
   uint64_t rays_closest, camera_samples, hitpoints, photons, splats, nonfinite, degenerate;
 };
 
-// per-pixel statistics of the sample extent (PixelStats, SPPM.hs:226-238):
+// per-pixel statistics of the sample extent (PixelStats, SPPM.hs:245-262):
 // radius^2, accumulated photon count N, photons of the current pass M
 struct SppmPixelStats {
   float* r2;

@@ -261,7 +261,7 @@ __device__ __forceinline__ Spec intLe(const DevShading& S, const HitGeom& g, V3 
   return dot(g.n, wo) > 0 ? sLoad(S.shape_emission + 16 * g.shape) : sConst(0);
 }
 
-// camera ray of sample g (fireRay, Camera.hs:146-164)
+// camera ray of sample g (fireRay, Camera.hs:49-68)
 __device__ __forceinline__ Ray cameraRay(const PassParams& P, const bling_camera_desc& cam,
                                          uint64_t g) {
   int ix, iy;
@@ -308,7 +308,7 @@ struct VertexOut {
 // First half of one vertex of the path in slot s at bounce `depth`
 // (Path.hs:49-87): emission on specular paths, the BSDF, one light sample
 // and one BSDF sample for MIS (sampleOneLight/estimateDirect,
-// Scene.hs:184-241), Russian roulette and the continuation sample.  Stores
+// Scene.hs:61-118), Russian roulette and the continuation sample.  Stores
 // the deferred terms in the slot and says which rays to trace; a path that
 // ends here is handed to finish(L).
 template <class Finish>
@@ -360,10 +360,10 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
   int lc = S.n_lights;
   int ln = 0;
   if (lc > 0) {
-    // sampleOneLight (Scene.hs:233-241) -> estimateDirect (Scene.hs:218-222)
+    // sampleOneLight (Scene.hs:109-118) -> estimateDirect (Scene.hs:84-99)
     if (lc > 1) ln = min((int)floorf(lNumU * (float)lc), lc - 1);
     const DLight& l = S.lights[ln];
-    // sampleLightMis (Scene.hs:184-192), visibility deferred
+    // sampleLightMis (Scene.hs:61-69), visibility deferred
     LightSample smpl = lightSample(A, S, l, p, eps, nn, ld1, ld2);
     if (!(smpl.pdf == 0 || isBlack(smpl.li))) {
       Spec f = evalBsdf(bsdf, wo, smpl.wi);
@@ -381,7 +381,7 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
         flags |= VF_SHADOW;
       }
     }
-    // sampleBsdfMis (Scene.hs:194-205), the hit deferred
+    // sampleBsdfMis (Scene.hs:71-82), the hit deferred
     BsdfSample bm = sampleBsdf(bsdf, wo, lBsdfCompU, lb1, lb2);
     if (!(bm.pdf == 0 || isBlack(bm.f))) {
       storeBands(st.bsf, s, bm.f);
@@ -455,7 +455,7 @@ __device__ __forceinline__ bool resolveVertex(const DevAccel& A, const DevShadin
     }
     if (use) bsv = sScale(loadBands(st.bsf, s) * lr, st.bsw[s]);
   }
-  Spec ed = lsv + bsv;  // estimateDirect = ls + bs (Scene.hs:218)
+  Spec ed = lsv + bsv;  // estimateDirect = ls + bs (Scene.hs:95)
   Spec direct = lc == 1 ? ed : (lc > 1 ? sScale(ed, (float)lc) : sConst(0));
   Spec lHere = loadBands(st.intl, s) + direct;
   Spec T = loadBands(st.T, s);

@@ -67,10 +67,10 @@ typedef struct bling_opts {
 
 /* Materials (src/lib/Graphics/Bling/Material.hs). Textures are constant. */
 enum {
-  BLING_MAT_MATTE = 0,   /* mkMatte kd sigma            (Material.hs:228-237) */
-  BLING_MAT_PLASTIC = 1, /* mkPlastic kd ks roughness   (Material.hs:272-282) */
-  BLING_MAT_METAL = 2,   /* mkMetal eta k roughness     (Material.hs:285-292) */
-  BLING_MAT_GLASS = 3,   /* glassMaterial ior kr kt     (Material.hs:252-262) */
+  BLING_MAT_MATTE = 0,   /* mkMatte kd sigma            (Material.hs:32-41) */
+  BLING_MAT_PLASTIC = 1, /* mkPlastic kd ks roughness   (Material.hs:76-87) */
+  BLING_MAT_METAL = 2,   /* mkMetal eta k roughness     (Material.hs:89-96) */
+  BLING_MAT_GLASS = 3,   /* glassMaterial ior kr kt     (Material.hs:56-66) */
   BLING_MAT_MIRROR = 4,  /* mirrorMaterial kr: kr in ks (Material.hs:68-72) */
   BLING_MAT_SHINY_METAL = 5, /* mkShinyMetal kr ks rough: kr in kd (Material.hs:98-109) */
   BLING_MAT_TRANS_MATTE = 6, /* translucentMatte kr kt ks: kr in kd, ks in sigma (Material.hs:43-53) */
@@ -171,11 +171,11 @@ typedef struct bling_camera_desc {
 } bling_camera_desc;
 
 /* The scene.  Primitive IDs follow the list handed to mkKdTree
- * (Scene.hs:160-166): `prim_order` lists the meshes (v >= 0 -> mesh v, which
+ * (Scene.hs:37-43): `prim_order` lists the meshes (v >= 0 -> mesh v, which
  * expands to its triangles in index order) and shapes (v < 0 -> shape ~v) in
  * that order; NULL means all meshes, then all shapes.  Lights follow
  * `mkScene`: the non-geometric lights, then the emissive shapes in primitive
- * order (Scene.hs:162,165). */
+ * order (Scene.hs:39,42). */
 typedef struct bling_scene_desc {
   const bling_mesh_desc* meshes;
   int32_t n_meshes;
@@ -248,13 +248,13 @@ int bling_ctx_set_stream(bling_ctx* ctx, void* stream);
 int bling_abi_version(void);
 
 /* ---- scenes: copies the host arrays, builds and uploads the BVH ----
- * replaces mkScene/mkKdTree (Scene.hs:160-166, Primitive/KdTree.hs:107-112) */
+ * replaces mkScene/mkKdTree (Scene.hs:37-43, Primitive/KdTree.hs:107-112) */
 int bling_scene_create(bling_ctx* ctx, const bling_scene_desc* desc, bling_scene** out);
 void bling_scene_destroy(bling_scene* scene);
 
 /* ---- ray queries over host buffers (SoA rays: ox oy oz dx dy dz tmin tmax,
  *      each n floats, i.e. rays[k*n + i]) ----
- * bling_trace_closest replaces `scIntersect` (Scene.hs:172-174) on a batch:
+ * bling_trace_closest replaces `scIntersect` (Scene.hs:49-51) on a batch:
  * the nearest hit, ties to the larger primitive ID as the reference's
  * `nearest'` fold does (Primitive.hs:29-43, TriangleMesh.hs:166).
  * prim[i] = -1 on a miss.  b1b2 may be NULL (2n floats: the barycentrics
@@ -264,7 +264,7 @@ void bling_scene_destroy(bling_scene* scene);
  * such rays as occluded, as triangleIntersects does for NaN. */
 int bling_trace_closest(bling_scene* scene, const float* rays, size_t n, float* t,
                         int32_t* prim, float* b1b2);
-/* replaces `occluded` (Scene.hs:168-170): hit[i] = 1 when any primitive is hit
+/* replaces `occluded` (Scene.hs:45-47): hit[i] = 1 when any primitive is hit
  * within [tmin, tmax]. */
 int bling_trace_any(bling_scene* scene, const float* rays, size_t n, uint8_t* hit);
 
@@ -319,7 +319,7 @@ int bling_render_pass_camera(bling_scene* scene, bling_film* film,
 int bling_scene_stats(bling_scene* scene, bling_stats* out);
 
 /* ---- stochastic progressive photon mapping ----
- * replaces the reference's SPPM renderer (Renderer/SPPM.hs:392-480).  One
+ * replaces the reference's SPPM renderer (Renderer/SPPM.hs:410-480).  One
  * pass: one Random-sampler camera sample per pixel of the sample extent
  * records hit points at non-specular surfaces (following specular
  * reflection and transmission both) and adds the emission it sees to the
@@ -328,7 +328,7 @@ int bling_scene_stats(bling_scene* scene, bling_stats* out);
  * point within its radius; each pixel's radius shrinks by alpha
  * (statsUpdate).  The film keeps the per-pixel radii between passes
  * (bling_film_clear resets them).  After n passes the reference's splat
- * weight is 1 / (n * ceil(sqrt photons)^2) (SPPM.hs:418). */
+ * weight is 1 / (n * ceil(sqrt photons)^2) (SPPM.hs:460). */
 typedef struct bling_sppm_params {
   int64_t photons;        /* photons per pass (mkSPPM n) */
   int32_t max_depth;      /* camera path vertices (mkSPPM md), 1..24 */

@@ -582,7 +582,7 @@ struct Light {
   std::vector<Spec> env;
   int w, h;
   Xf w2l;
-  // Dist2D (Montecarlo.hs:303-333)
+  // Dist2D (Montecarlo.hs:75-106)
   std::vector<std::vector<float>> cfunc, ccdf;
   std::vector<float> cint;
   std::vector<float> mfunc, mcdf;
@@ -1023,7 +1023,7 @@ static bool occluded(const orc_scene& S, const Ray& r) {
 }
 
 // ---------------------------------------------------------------- Monte Carlo
-// concentricSampleDisk (Montecarlo.hs:389-406)
+// concentricSampleDisk (Montecarlo.hs:160-179)
 static void concentricSampleDisk(float u1, float u2, float& ox, float& oy) {
   float sx = u1 * 2.0f - 1.0f, sy = u2 * 2.0f - 1.0f;
   if (sx == 0 && sy == 0) {
@@ -1056,20 +1056,20 @@ static void concentricSampleDisk(float u1, float u2, float& ox, float& oy) {
   ox = r * cosf(theta);
   oy = r * sinf(theta);
 }
-// cosineSampleHemisphere (Montecarlo.hs:375-378)
+// cosineSampleHemisphere (Montecarlo.hs:146-149)
 static V cosineSampleHemisphere(float u1, float u2) {
   float x, y;
   concentricSampleDisk(u1, u2, x, y);
   return V{x, y, sqrtf(hmax(0.0f, 1.0f - x * x - y * y))};
 }
-// uniformSampleSphere (Montecarlo.hs:410-415)
+// uniformSampleSphere (Montecarlo.hs:181-186)
 static V uniformSampleSphere(float u1, float u2) {
   float u = u1 * 2.0f - 1.0f;
   float s = sqrtf(1.0f - (u * u));
   float omega = u2 * 2.0f * PI;
   return V{s * cosf(omega), s * sinf(omega), u};
 }
-// uniformConePdf / uniformSampleCone (Montecarlo.hs:356-373)
+// uniformConePdf / uniformSampleCone (Montecarlo.hs:127-144)
 static float uniformConePdf(float cosThetaMax) {
   if (cosThetaMax >= 1) return 0;
   return 1.0f / (TWO_PI * (1.0f - cosThetaMax));
@@ -1082,12 +1082,12 @@ static V uniformSampleCone(const LC& c, float cosThetaMax, float u1, float u2) {
   return V{c.s.x * a, c.s.y * a, c.s.z * a} + V{c.t.x * b, c.t.y * b, c.t.z * b} +
          V{c.n.x * cosTheta, c.n.y * cosTheta, c.n.z * cosTheta};
 }
-// powerHeuristic (Montecarlo.hs:342-345)
+// powerHeuristic (Montecarlo.hs:113-116)
 static float powerHeuristic(float fPdf, float gPdf) {
   float f = 1.0f * fPdf, g = 1.0f * gPdf;
   return (f * f) / (f * f + g * g);
 }
-// Dist1D (Montecarlo.hs:263-301)
+// Dist1D (Montecarlo.hs:34-73)
 static void mkDist1D(const std::vector<float>& func, std::vector<float>& cdf, float& fi) {
   int n = (int)func.size();
   std::vector<float> i(n + 1);
@@ -1133,7 +1133,7 @@ static inline float sinPhi(V v) {
 static inline bool sameHemisphere(V a, V b) { return a.z * b.z > 0; }
 static inline V toSameHemisphere(V wo, V wi) { return wo.z < 0 ? V{wi.x, wi.y, -wi.z} : wi; }
 
-// Fresnel (Fresnel.hs:146-195)
+// Fresnel (Fresnel.hs:13-70)
 static float frDielScalar(float etai, float etat, float cosi) {
   float c = hmax(0.0f, 1.0f - cosi * cosi);
   float costp = cosi > 0 ? c / (etat * etat) : c * (etat * etat);
@@ -1368,7 +1368,7 @@ static void bxSampleBrdf(const BxDF& b, V wo, float u1, float u2, Spec& f, V& wi
       f = sScale(adj ? fblendEval(b, wi, wo) : fblendEval(b, wo, wi), 1.0f / pdf);
       return;
     }
-    case BX_SPEC_REFL: {  // Specular.hs:86-87
+    case BX_SPEC_REFL: {  // Specular.hs:11-20
       f = b.r * frEval(b.fr, cosTheta(wo));
       wi = V{-wo.x, -wo.y, wo.z};
       pdf = 1;
@@ -1425,7 +1425,7 @@ struct Bsdf {  // Reflection.hs:201-218
   V ng;
 };
 
-// mkBsdf' with the material's BxDFs (Material.hs:228-292)
+// mkBsdf' with the material's BxDFs (Material.hs:32-127)
 // frApproxEta / frApproxK (Fresnel.hs:72-78), on sClamp 0 0.999 of the colour
 static Spec frApproxEta(const Spec& r) {
   Spec c = sClamp(0.0f, 0.999f, r), o;
@@ -1838,7 +1838,7 @@ static float lightPdf(const orc_scene& S, const Light& l, V p, V wi) {
   float sint = sinf(theta);
   if (sint == 0) return 0;
   float u = phi / (2.0f * PI), v = theta / PI;
-  // pdfDist2D (Montecarlo.hs:324-333)
+  // pdfDist2D (Montecarlo.hs:95-106)
   int nu = (int)l.cfunc[0].size(), nv = (int)l.mfunc.size();
   int iu = std::max(0, std::min(nu - 1, (int)floorf(u * (float)nu)));
   int iv = std::max(0, std::min(nv - 1, (int)floorf(v * (float)nv)));
@@ -1870,7 +1870,7 @@ static int intLightId(const orc_scene& S, const Isect& it) {
   return s.emissive ? s.light_id : -1;
 }
 
-// estimateDirect = sampleLightMis + sampleBsdfMis (Scene.hs:184-222)
+// estimateDirect = sampleLightMis + sampleBsdfMis (Scene.hs:61-99)
 static Spec estimateDirect(const orc_scene& S, int li, V p, float eps, V n, V wo, const Bsdf& bsdf,
                            float ld1, float ld2, float ubc, float ubd1, float ubd2, Counters& C) {
   const Light& l = S.lights[li];
@@ -1949,7 +1949,7 @@ static Spec pathLi(const orc_scene& S, const Sampler& smp, Ray ray, int md, int 
     V n = bsdf.cs.n;
     V p = bsdf.p;
     float eps = it.eps;
-    // sampleOneLight (Scene.hs:233-241)
+    // sampleOneLight (Scene.hs:109-118)
     Spec direct = BLACK;
     int lc = (int)S.lights.size();
     if (lc == 1) {
@@ -1977,7 +1977,7 @@ static Spec pathLi(const orc_scene& S, const Sampler& smp, Ray ray, int md, int 
   }
 }
 
-// hash (SPPM.hs:291-293) and the bucket of a cell: abs (hash) `rem` cnt, clamped
+// hash (SPPM.hs:303-305) and the bucket of a cell: abs (hash) `rem` cnt, clamped
 static long long cellBucketOf(long long x, long long y, long long z, long long cnt) {
   long long h = (long long)((unsigned long long)x * 73856093ull ^ (unsigned long long)y * 19349663ull ^
                             (unsigned long long)z * 83492791ull);
@@ -2417,7 +2417,7 @@ int orc_scene_create(const bling_scene_desc* d, orc_scene** out) {
     s.light_id = -1;
     S->shapes.push_back(s);
   }
-  // user lights first (Scene.hs:162)
+  // user lights first (Scene.hs:39)
   for (int i = 0; i < d->n_lights; i++) {
     const bling_light_desc& ld = d->lights[i];
     Light l;
@@ -2476,7 +2476,7 @@ int orc_scene_create(const bling_scene_desc* d, orc_scene** out) {
       p.index = ~v;
       S->prims.push_back(p);
       Shape& s = S->shapes[~v];
-      if (s.emissive) {  // geometric lights in primitive order (Scene.hs:165)
+      if (s.emissive) {  // geometric lights in primitive order (Scene.hs:42)
         Light l;
         l.kind = LIGHT_AREA;
         l.shape = ~v;
@@ -2623,7 +2623,7 @@ static void sampleExtent(const bling_render_params* p, int& x0, int& x1, int& y0
   y1 = (int)floorf(0.5f + (float)p->height + fh);
 }
 
-// camera ray of one sample (fireRay, Camera.hs:146-164)
+// camera ray of one sample (fireRay, Camera.hs:49-68)
 static Ray cameraRay(const orc_scene* S, float ix, float iy, float lu, float lv) {
   const bling_camera_desc& c = S->cam;
   V pCamera = transPoint(c.r2c, V{ix, iy, 0});
@@ -2843,20 +2843,20 @@ static BsdfSample sampleBsdfFlags(const Bsdf& b, V woW, int flags, float uComp, 
   return BsdfSample{bx.type, pdf, sScale(sScale(fSample, pdfp) + fOthers, 1.0f / pdf), wiW};
 }
 
-struct HitPoint {  // HitPoint (SPPM.hs:58-64)
+struct HitPoint {  // HitPoint (SPPM.hs:56-63)
   Bsdf bsdf;
   float px, py, r2;
   V w;
   Spec F;
 };
 
-struct PixelStats {  // PixelStats (SPPM.hs:226-238) over the sample extent
+struct PixelStats {  // PixelStats (SPPM.hs:245-262) over the sample extent
   int x0, x1, y0, y1;
   float* r2;
   float* n;
   uint32_t* m;
   int64_t count;
-  // sIdx (SPPM.hs:248-253); positions outside the arrays give -1
+  // sIdx (SPPM.hs:264-274); positions outside the arrays give -1
   int64_t idx(float px, float py) const {
     int w = x1 - x0, h = y1 - y0;
     int ix = std::min(w, (int)px), iy = std::min(h, (int)py);  // truncate
@@ -2875,7 +2875,7 @@ struct CamTree {
   std::vector<HitPoint>* hps;
   Counters* C;
 
-  // traceCam (SPPM.hs:101-131) of the node with heap index k
+  // traceCam (SPPM.hs:105-131) of the node with heap index k
   Spec trace(const Ray& ray, int depth, const Spec& t, uint32_t k) {
     if (depth == md) return BLACK;
     Isect it;
@@ -2899,7 +2899,7 @@ struct CamTree {
     Spec lt = follow(T_TRANS, it, bsdf, wo, t, depth, k);
     return BLACK + lr + lt + ls;
   }
-  // followCam (SPPM.hs:83-99)
+  // followCam (SPPM.hs:89-104)
   Spec follow(int prop, const Isect& it, const Bsdf& bsdf, V wo, const Spec& t, int depth,
               uint32_t k) {
     uint32_t k2 = 2 * k + (prop == T_TRANS ? 1u : 0u);
@@ -2935,7 +2935,7 @@ int orc_sppm_pass(const orc_scene* S, const bling_sppm_params* sp, int32_t width
   st.r2 = r2;
   st.n = nacc;
   st.m = m;
-  // ---- camera pass: hit points per tile, in tile order (mkHitPoints, SPPM.hs:136-164)
+  // ---- camera pass: hit points per tile, in tile order (mkHitPoints, SPPM.hs:133-164)
   std::vector<std::vector<HitPoint>> tile_hps(extentTiles(&rp));
   uint64_t ncam = 0, ncl = 0, nany = 0;
   int rc = renderTiles(
@@ -2954,7 +2954,7 @@ int orc_sppm_pass(const orc_scene* S, const bling_sppm_params* sp, int32_t width
   std::vector<HitPoint> hps;
   for (auto& t : tile_hps) hps.insert(hps.end(), t.begin(), t.end());
   uint64_t st_out[4] = {ncl, 0, 0, 0};
-  // ---- spatial hash (mkHash, SPPM.hs:283-323); the buckets hold hit-point indices
+  // ---- spatial hash (mkHash, SPPM.hs:297-353); the buckets hold hit-point indices
   int sn = std::max(1, (int)ceilf(sqrtf((float)sp->photons)));
   int64_t nphot = (int64_t)sn * sn;
   long long cnt = (long long)hps.size();
@@ -2986,7 +2986,7 @@ int orc_sppm_pass(const orc_scene* S, const bling_sppm_params* sp, int32_t width
           for (long long z = (long long)f0[2]; z <= (long long)f1[2]; z++)
             buckets[(size_t)cellBucketOf(x, y, z, cnt)].push_back((int)i);
     }
-    // ---- photon pass (tracePhoton/followPhoton, SPPM.hs:172-224)
+    // ---- photon pass (tracePhoton/followPhoton, SPPM.hs:170-243)
     uint64_t key = pixelKey(sp->seed, 2 * pass + 1, 0, 0);
     V wlo{INF, INF, INF}, whi{-INF, -INF, -INF};
     for (size_t i = 0; i < S->prims.size(); i++) {
@@ -3032,7 +3032,7 @@ int orc_sppm_pass(const orc_scene* S, const bling_sppm_params* sp, int32_t width
             DG dgs = shadingGeometry(*S, pr, it.dg);
             Bsdf bsdf = materialBsdf(S->mats[mat], it.dg, dgs);
             V p = bsdf.p;
-            if (bsdfHasNonSpecular(bsdf)) {  // hashLookup (SPPM.hs:295-302)
+            if (bsdfHasNonSpecular(bsdf)) {  // hashLookup (SPPM.hs:307-314)
               float cx = fabsf((p.x - lo.x) * invSize), cy = fabsf((p.y - lo.y) * invSize),
                     cz = fabsf((p.z - lo.z) * invSize);
               if (cx < 9.2e18f && cy < 9.2e18f && cz < 9.2e18f) {
@@ -3083,7 +3083,7 @@ int orc_sppm_pass(const orc_scene* S, const bling_sppm_params* sp, int32_t width
     }
   }
   st_out[1] = (uint64_t)hps.size();
-  // ---- statsUpdate (SPPM.hs:258-279)
+  // ---- statsUpdate (SPPM.hs:272-295)
   float a = sp->alpha;
   for (int64_t i = 0; i < st.count; i++) {
     uint32_t mm = m[i];

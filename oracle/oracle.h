@@ -73,7 +73,7 @@ int orc_light_pass(const orc_scene* s, int32_t width, int32_t height, uint64_t s
                    int32_t max_depth, int64_t first, int64_t count, float* splat_xyz, int nthreads,
                    uint64_t stats[4]);
 
-/* One SPPM pass (Renderer/SPPM.hs:392-480): camera samples of the Random
+/* One SPPM pass (Renderer/SPPM.hs:410-480): camera samples of the Random
  * sampler added to film (w,X,Y,Z), hit points, spatial hash, photon splats
  * into splat_xyz and the per-pixel statistics r2/n/m (stat_count entries over
  * the sample extent, updated in place).  stats: closest-hit queries, hit
@@ -99,7 +99,7 @@ void orc_xf_rotate(int axis, float deg, float out[32]);
 void orc_xf_look_at(const float pos[3], const float look[3], const float up[3], float out[32]);
 void orc_xf_perspective(float fov, float n, float f, float out[32]);
 void orc_xf_concat(const float a[32], const float b[32], float out[32]);
-/* mkPerspectiveCamera c2w lr fd fov sx sy (Camera.hs:232-243) */
+/* mkPerspectiveCamera c2w lr fd fov sx sy (Camera.hs:136-148) */
 void orc_camera_perspective(const float c2w[32], float lens_radius, float focal_distance,
                             float fov, float sx, float sy, bling_camera_desc* out);
 

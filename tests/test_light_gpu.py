@@ -194,7 +194,7 @@ def test_substrate_light_pass_vs_oracle(gpu_ctx):
 
 def test_renderer_interfaces_report_the_reference_splat_weights(gpu_ctx):
     """GpuLightTracer and GpuSPPM as bling Renderers: PassDone n with splat
-    weight 1 / (n ppp) (LightTracer.hs:44) and 1 / (n sn^2) (SPPM.hs:418)"""
+    weight 1 / (n ppp) (LightTracer.hs:44) and 1 / (n sn^2) (SPPM.hs:460)"""
     from bling_gb300.api import GpuLightTracer, GpuSPPM, PassDone, RenderJob
     sc = S.cornell_room(24, 24)
     job = RenderJob(gpu_ctx.scene(sc), S.cornell_params(24, 24))

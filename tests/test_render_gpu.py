@@ -256,7 +256,7 @@ def test_shiny_metal_and_translucent_matte_vs_oracle(gpu_ctx):
 def test_lights_and_thin_lens_vs_oracle(gpu_ctx):
     """a point light, disk, cylinder and box area lights (shape sampling of
     each kind, Shape.hs:333-409), and a thin-lens camera (lens samples,
-    concentricSampleDisk, Camera.hs:146-164)"""
+    concentricSampleDisk, Camera.hs:49-68)"""
     s = S.Scene()
     grey = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.6, 0.6, 0.6)))
     plastic = s.add_material(abi.MAT_PLASTIC, kd=rgb_to_spectrum((0.3, 0.5, 0.2)),

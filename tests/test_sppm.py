@@ -4,7 +4,7 @@
   the reference's splat weight) agrees with a path-traced one where the
   camera sees lit surfaces, within the noise and the photon-mapping blur;
 * the per-pixel radii shrink by the alpha rule where photons arrived
-  (statsUpdate, SPPM.hs:258-279) and stay where none did;
+  (statsUpdate, SPPM.hs:272-295) and stay where none did;
 * the camera pass follows specular reflection and transmission both: a
   glass sphere in front of a wall yields hit points through the glass
   only when the camera paths may bounce.

@@ -147,7 +147,7 @@ def test_invalid_parameters_are_refused(gpu_ctx):
 def test_edge_cases_no_lights_no_hit_points(gpu_ctx):
     """a scene without lights: the light tracer and SPPM add nothing; a view
     of empty space: SPPM records no hit points and skips its photon pass;
-    zero photons: ceil(sqrt 0) = 0 is raised to one photon (SPPM.hs:464-466)"""
+    zero photons: ceil(sqrt 0) = 0 is raised to one photon (SPPM.hs:474)"""
     s = S.Scene()
     m = s.add_material(abi.MAT_MATTE, kd=constant(0.5))
     s.add_shape(abi.SHAPE_SPHERE, (1.0,), xf.identity(), m)
