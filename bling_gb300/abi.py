@@ -21,6 +21,7 @@ BLING_ERR_BOUNDS = -5
 BLING_ERR_STATE = -6
 
 FLAG_WIDE_BVH = 1
+FLAG_GPU_BVH = 2
 
 MAT_MATTE, MAT_PLASTIC, MAT_METAL, MAT_GLASS, MAT_MIRROR = 0, 1, 2, 3, 4
 MAT_SHINY_METAL, MAT_TRANS_MATTE = 5, 6
@@ -29,7 +30,7 @@ SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_DISK, SHAPE_CYLINDER = 0, 1, 2, 3, 4
 LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE = 0, 1, 2
 FILTER_BOX, FILTER_GAUSS, FILTER_MITCHELL, FILTER_SINC, FILTER_TRIANGLE = 0, 1, 2, 3, 4
 SAMPLER_STRATIFIED, SAMPLER_RANDOM = 0, 1
-ABI_VERSION = 3  # BLING_ABI_VERSION of include/bling_gpu.h
+ABI_VERSION = 4  # BLING_ABI_VERSION of include/bling_gpu.h
 
 
 class Opts(C.Structure):
@@ -93,7 +94,8 @@ class Stats(C.Structure):
                 ("degenerate_rays", C.c_uint64),
                 ("bvh_build_ms", C.c_double), ("last_pass_ms", C.c_double),
                 ("bvh_nodes", C.c_uint64), ("bvh_leaf_prims", C.c_uint64),
-                ("device_bytes", C.c_uint64), ("light_splats", C.c_uint64)]
+                ("device_bytes", C.c_uint64), ("light_splats", C.c_uint64),
+                ("scene_build_ms", C.c_double)]
 
 
 class SppmParams(C.Structure):

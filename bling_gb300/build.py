@@ -23,7 +23,7 @@ PROBE_LIB = PKG / "libbling_probe.so"  # measurement only: the L2 bandwidth prob
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SRCS = ["api.cu", "kernels_trace.cu", "integrator.cu", "scene_upload.cu", "batch.cu",
-           "server.cu", "lighttrace.cu", "sppm.cu"]
+           "server.cu", "lighttrace.cu", "sppm.cu", "bvh_gpu.cu"]
 CPP_SRCS = ["bvh.cpp"]
 PROBE_SRCS = ["l2probe.cu"]
 

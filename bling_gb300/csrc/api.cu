@@ -14,6 +14,7 @@
 #include "../../include/bling_gpu.h"
 #include "batch.h"
 #include "bvh.h"
+#include "bvh_gpu.h"
 #include "handles.h"
 #include "integrator.h"
 #include "internal.h"
@@ -289,6 +290,13 @@ int bling_ctx_create(bling_ctx** out, const bling_opts* opts) {
   std::unique_ptr<bling_ctx> c(new bling_ctx());
   if (opts) c->opts = *opts;
   c->device = c->opts.device;
+  if ((c->opts.flags & BLING_FLAG_WIDE_BVH) && (c->opts.flags & BLING_FLAG_GPU_BVH)) {
+    set_err(c.get(), BLING_ERR_INVALID_ARG,
+            "BLING_FLAG_GPU_BVH builds the binary layout; it cannot be combined with "
+            "BLING_FLAG_WIDE_BVH");
+    *out = c.release();
+    return BLING_ERR_INVALID_ARG;
+  }
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
   if (e != cudaSuccess || ndev <= 0) {
@@ -437,6 +445,7 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
       }
     }
   }
+  std::unique_ptr<bling_scene> S(new bling_scene());
   BvhBuildInput bi;
   bi.n = n_prims;
   bi.lo = lo.data();
@@ -444,18 +453,49 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   bi.max_leaf = c->opts.bvh_leaf_size > 0 ? c->opts.bvh_leaf_size : 4;
   bi.wide = (c->opts.flags & BLING_FLAG_WIDE_BVH) != 0;
   BvhBuildOutput bo;
-  if (build_bvh(bi, bo) != 0) return set_err(c, BLING_ERR_INVALID_ARG, "BVH build failed (depth bound)");
+  // ---- BVH on the GPU (BLING_FLAG_GPU_BVH): boxes up, tree built in place
+  GpuBvh gb;
+  bool gpu_built = false;
+  auto tb0 = std::chrono::steady_clock::now();  // the BVH construction alone
+  if ((c->opts.flags & BLING_FLAG_GPU_BVH) && !bi.wide) {
+    float *d_lo = nullptr, *d_hi = nullptr;
+    int rc0 = upload(c, S->owned, lo.data(), lo.size(), &d_lo);
+    if (!rc0) rc0 = upload(c, S->owned, hi.data(), hi.size(), &d_hi);
+    if (rc0) return rc0;
+    std::string berr;
+    int brc = build_bvh_gpu(c->stream, d_lo, d_hi, n_prims, gb, berr);
+    // the boxes were only needed for the build
+    S->owned.erase(std::remove_if(S->owned.begin(), S->owned.end(),
+                                  [&](void* p) { return p == d_lo || p == d_hi; }),
+                   S->owned.end());
+    cudaFree(d_lo);
+    cudaFree(d_hi);
+    if (brc) {
+      gb.release();
+      return set_err(c, brc == -2 ? BLING_ERR_OOM : BLING_ERR_CUDA, "%s", berr.c_str());
+    }
+    if (gb.depth < kBvhMaxDepth) {
+      gpu_built = true;
+    } else {
+      gb.release();  // deeper than the traversal stack holds: build on the host
+    }
+  }
+  if (!gpu_built && build_bvh(bi, bo) != 0)
+    return set_err(c, BLING_ERR_INVALID_ARG, "BVH build failed (depth bound)");
+  const double bvh_ms =
+      std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb0).count();
   // the wide layout when it was built (it is skipped for very deep trees)
-  const bool wide = bi.wide && bo.wide_depth >= 0;
+  const bool wide = !gpu_built && bi.wide && bo.wide_depth >= 0;
   const std::vector<int32_t>& slot_prim = wide ? bo.slot_prim8 : bo.slot_prim;
   const std::vector<uint8_t>& slot_last = wide ? bo.slot_last8 : bo.slot_last;
-  // ---- leaf slots
-  size_t n_slots = slot_prim.size();
+  // ---- leaf slots: in leaf order, or (GPU build) in primitive order, one per
+  // leaf, gathered into leaf order on the device
+  size_t n_slots = gpu_built ? (size_t)n_prims : slot_prim.size();
   std::vector<float> slots(12 * n_slots, 0.0f);
   for (size_t s = 0; s < n_slots; s++) {
-    int32_t prim = slot_prim[s];
+    int32_t prim = gpu_built ? (int32_t)s : slot_prim[s];
     float* o = &slots[12 * s];
-    int32_t flags = slot_last[s] ? SLOT_LAST : 0;
+    int32_t flags = (gpu_built || slot_last[s]) ? SLOT_LAST : 0;
     int32_t v = prim_owner[prim];
     if (v >= 0) {
       const bling_mesh_desc& m = d->meshes[v];
@@ -481,7 +521,6 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
     memcpy(&o[9], &prim, 4);
     memcpy(&o[10], &flags, 4);
   }
-  std::unique_ptr<bling_scene> S(new bling_scene());
   S->ctx = c;
   S->serial = ++g_scene_serial;
   for (int k = 0; k < 3; k++) {
@@ -494,14 +533,38 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
       S->hi[k] = std::max(S->hi[k], hi[3 * p + k]);
     }
   int rc;
-  if (wide) {
+  if (gpu_built) {
+    S->d_nodes = gb.nodes;  // owned by the scene from here on
+    if (gb.nodes) S->owned.push_back(gb.nodes);
+    gb.nodes = nullptr;
+    float4* d_src = nullptr;
+    if ((rc = upload(c, S->owned, (const float4*)slots.data(), slots.size() / 4, &d_src))) {
+      gb.release();
+      return rc;
+    }
+    float4* d_dst = nullptr;
+    cudaError_t e = cudaMalloc(&d_dst, slots.size() * sizeof(float));
+    if (e == cudaSuccess) {
+      S->owned.push_back(d_dst);
+      e = launch_gather_slots(d_src, gb.order, n_prims, d_dst, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    S->owned.erase(std::remove(S->owned.begin(), S->owned.end(), (void*)d_src), S->owned.end());
+    cudaFree(d_src);
+    gb.release();
+    if (e != cudaSuccess)
+      return set_err(c, e == cudaErrorMemoryAllocation ? BLING_ERR_OOM : BLING_ERR_CUDA,
+                     "leaf slots: %s", cudaGetErrorString(e));
+    S->d_slots = d_dst;
+  } else if (wide) {
     if ((rc = upload(c, S->owned, (const uint4*)bo.nodes8.data(), bo.nodes8.size() / 4, &S->d_nodes8)))
       return rc;
   } else {
     if ((rc = upload(c, S->owned, (const float4*)bo.nodes.data(), bo.nodes.size() / 4, &S->d_nodes)))
       return rc;
   }
-  if ((rc = upload(c, S->owned, (const float4*)slots.data(), slots.size() / 4, &S->d_slots)))
+  if (!gpu_built &&
+      (rc = upload(c, S->owned, (const float4*)slots.data(), slots.size() / 4, &S->d_slots)))
     return rc;
   // ---- shapes on the device
   std::vector<DShape> shapes(d->n_shapes);
@@ -527,12 +590,13 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   S->accel.nodes8 = S->d_nodes8;
   S->accel.slots = S->d_slots;
   S->accel.shapes = S->d_shapes;
-  S->accel.root_ref = bo.root_ref;
+  S->accel.root_ref = gpu_built ? gb.root_ref : bo.root_ref;
   S->accel.root8 = bo.root8;
   S->accel.wide = wide ? 1 : 0;
   S->accel.n_shapes = d->n_shapes;
   S->accel.n_prims = n_prims;
-  S->n_nodes = wide ? (int64_t)bo.nodes8.size() / 20 : (int64_t)bo.nodes.size() / 16;
+  S->n_nodes = gpu_built ? gb.n_nodes
+                         : (wide ? (int64_t)bo.nodes8.size() / 20 : (int64_t)bo.nodes.size() / 16);
   S->n_slots = (int64_t)n_slots;
   // ---- shading data for the path integrator
   if ((rc = integrator_upload_scene(c->stream, *d, order, prim_owner, prim_tri, shapes, shape_light,
@@ -540,11 +604,12 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
     return rc;
   CK(c, cudaStreamSynchronize(c->stream));
   auto t1 = std::chrono::steady_clock::now();
-  S->stats.bvh_build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+  S->stats.bvh_build_ms = bvh_ms;
+  S->stats.scene_build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   S->stats.bvh_nodes = (uint64_t)S->n_nodes;
   S->stats.bvh_leaf_prims = (uint64_t)n_slots;
-  size_t bytes = (wide ? bo.nodes8.size() : bo.nodes.size()) * 4 + slots.size() * 4 +
-                 shapes.size() * sizeof(DShape);
+  size_t bytes = (gpu_built ? (size_t)gb.n_nodes * 16 : (wide ? bo.nodes8.size() : bo.nodes.size())) * 4 +
+                 slots.size() * 4 + shapes.size() * sizeof(DShape);
   S->stats.device_bytes = bytes + S->shading.bytes;
   *out = S.release();
   return BLING_OK;
@@ -558,6 +623,7 @@ void bling_scene_destroy(bling_scene* s) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     for (void* p : s->owned) cudaFree(p);
+    s->owned.clear();
   }
   delete s;
 }

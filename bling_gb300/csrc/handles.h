@@ -50,6 +50,11 @@ struct bling_scene {
   int32_t root_ref = 0;
   float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // world bounds of all primitives
   uint64_t serial = 0;  // unique per process (batches key their scene tables on it)
+  // frees what a creation that failed part way had allocated (on the current
+  // device); bling_scene_destroy empties `owned` first
+  ~bling_scene() {
+    for (void* p : owned) cudaFree(p);
+  }
 };
 
 struct bling_film {

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define BLING_ABI_VERSION 3
+#define BLING_ABI_VERSION 4
 
 #define BLING_OK 0
 #define BLING_ERR_INVALID_ARG (-1)
@@ -54,6 +54,11 @@ typedef struct bling_film bling_film;
 
 /* bling_opts.flags */
 #define BLING_FLAG_WIDE_BVH 1u /* 8-wide quantised BVH layout instead of the binary one */
+#define BLING_FLAG_GPU_BVH 2u  /* build the BVH on the GPU (Morton order and PLOC
+                                  clustering, binary layout, one primitive per
+                                  leaf) instead of the host's binned SAH; not with
+                                  BLING_FLAG_WIDE_BVH.  A tree deeper than the
+                                  traversal's stack allows is rebuilt on the host. */
 
 typedef struct bling_opts {
   int32_t device;        /* CUDA device ordinal */
@@ -228,12 +233,13 @@ typedef struct bling_stats {
                                passes their camera samples and photons */
   uint64_t nonfinite_drops; /* NaN/Inf samples skipped by the film (Image.hs:253-256) */
   uint64_t degenerate_rays; /* rays with a NaN component, answered without traversal */
-  double bvh_build_ms;
+  double bvh_build_ms;       /* the BVH construction (host or GPU builder) */
   double last_pass_ms;
   uint64_t bvh_nodes;
   uint64_t bvh_leaf_prims;
   uint64_t device_bytes;
   uint64_t light_splats;    /* splats of light and SPPM passes added to the splat image */
+  double scene_build_ms;    /* all of bling_scene_create: checks, BVH, uploads */
 } bling_stats;
 
 /* ---- context ---- */

@@ -28,10 +28,23 @@ def wide_ctx():
     ctx.close()
 
 
-@pytest.fixture(params=["binary", "wide"])
+@pytest.fixture(scope="module")
+def gpu_built_ctx():
+    """A third context whose scenes build their BVH on the GPU."""
+    from bling_gb300.api import Context
+    ctx = Context(device=0, gpu_bvh=True)
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(params=["binary", "wide", "gpu-built"])
 def ctx(request, gpu_ctx):
-    """Both BVH layouts must give the oracle's answers."""
-    return gpu_ctx if request.param == "binary" else request.getfixturevalue("wide_ctx")
+    """Both BVH layouts, and the tree built on the GPU, must give the
+    oracle's answers: traversal is conservative, so the answer does not
+    depend on the tree."""
+    if request.param == "binary":
+        return gpu_ctx
+    return request.getfixturevalue("wide_ctx" if request.param == "wide" else "gpu_built_ctx")
 
 
 def _bits(a):
