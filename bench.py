@@ -749,7 +749,8 @@ def run_ours(args):
     from bling_gb300 import scene as S
     from bling_gb300.api import Context
 
-    ctx = Context(device=local, wide_bvh=args.wide_bvh)
+    ctx = Context(device=local, wide_bvh=args.wide_bvh, compact_bvh=args.compact_bvh,
+                  gpu_bvh=args.gpu_bvh)
     stream = torch.cuda.current_stream(dev)
     ctx.set_stream(stream.cuda_stream)
     soup = S.triangle_soup(N_TRIS, seed=1)
@@ -820,13 +821,14 @@ def run_ours(args):
     # BVH and the leaf slots out of L2 (the 1M soup's ~100 MB working set
     # stays resident), so the bound is the L2 read bandwidth, measured in this
     # run by the probe kernel.  Algorithmic bytes per ray: 32 (ray) + 8 (t,
-    # primitive) + 32 per box test + 48 per leaf slot tested; a visit of a
-    # binary node tests its two children's boxes (64 B of node), a visit of
-    # an 8-wide node reads its 80 B node once.
+    # primitive) + the node bytes of every visit + 48 per leaf slot tested.
     hbm_peak, peak_kind = peaks()
     counts = traversal_counts(g, rays)
-    box_tests = (80.0 / 32.0 if args.wide_bvh else 2.0) * counts["nodes_per_ray"]
-    bytes_per_ray = 32 + 8 + 32 * box_tests + 48 * counts["slots_per_ray"]
+    # a visit reads 64 B of a binary node (two child boxes of 32 B each), 80 B
+    # of an 8-wide node or 32 B of a compact node (two quantised boxes)
+    node_bytes = 80.0 if args.wide_bvh else (32.0 if args.compact_bvh else 64.0)
+    box_tests = (8.0 if args.wide_bvh else 2.0) * counts["nodes_per_ray"]
+    bytes_per_ray = 32 + 8 + node_bytes * counts["nodes_per_ray"] + 48 * counts["slots_per_ray"]
     closest_s = float(np.mean(closest_ms)) / 1e3
     achieved = bytes_per_ray * N_RAYS / closest_s / 1e9
     prof = profile_traffic()
@@ -841,9 +843,13 @@ def run_ours(args):
     roof.update({
         "traffic": prof.get("dram_bytes_per_launch") if prof else None,
         "traffic_source": (prof.get("captured") if prof else None),
-        "kernel": "k_trace_closest", "bvh_layout": "wide8" if args.wide_bvh else "binary",
+        "kernel": "k_trace_closest",
+        "bvh_layout": ("wide8" if args.wide_bvh else "compact32" if args.compact_bvh
+                       else "binary-gpu-built" if args.gpu_bvh else "binary"),
         "algorithmic_bytes_per_ray": round(bytes_per_ray, 1),
-        "bytes_per_ray_formula": "32 ray + 8 result + 32 x box tests + 48 x leaf slots",
+        "bytes_per_ray_formula": "32 ray + 8 result + node bytes x node visits + 48 x leaf slots "
+                                 "(binary: 64 B a visit = 32 B per box test)",
+        "node_bytes_per_visit": node_bytes,
         "node_visits_per_ray": round(counts["nodes_per_ray"], 3),
         "box_tests_per_ray": round(box_tests, 3),
         "slots_per_ray": round(counts["slots_per_ray"], 3),
@@ -967,6 +973,9 @@ def main():
     ap.add_argument("--no-render", action="store_true", help="skip the path-integrator workloads")
     ap.add_argument("--no-heightfield", action="store_true")
     ap.add_argument("--wide-bvh", action="store_true", help="8-wide quantised BVH layout")
+    ap.add_argument("--compact-bvh", action="store_true",
+                    help="32-byte quantised binary BVH nodes")
+    ap.add_argument("--gpu-bvh", action="store_true", help="build the BVH on the GPU")
     ap.add_argument("--no-light", action="store_true", help="skip the light-tracer workload")
     ap.add_argument("--light-photons", type=int, default=1 << 22)
     ap.add_argument("--light-profile", action="store_true",

@@ -290,12 +290,17 @@ int bling_ctx_create(bling_ctx** out, const bling_opts* opts) {
   std::unique_ptr<bling_ctx> c(new bling_ctx());
   if (opts) c->opts = *opts;
   c->device = c->opts.device;
-  if ((c->opts.flags & BLING_FLAG_WIDE_BVH) && (c->opts.flags & BLING_FLAG_GPU_BVH)) {
-    set_err(c.get(), BLING_ERR_INVALID_ARG,
-            "BLING_FLAG_GPU_BVH builds the binary layout; it cannot be combined with "
-            "BLING_FLAG_WIDE_BVH");
-    *out = c.release();
-    return BLING_ERR_INVALID_ARG;
+  {
+    const uint32_t f = c->opts.flags;
+    const int layouts = ((f & BLING_FLAG_WIDE_BVH) ? 1 : 0) + ((f & BLING_FLAG_GPU_BVH) ? 1 : 0) +
+                        ((f & BLING_FLAG_COMPACT_BVH) ? 1 : 0);
+    if (layouts > 1 || (f & ~(BLING_FLAG_WIDE_BVH | BLING_FLAG_GPU_BVH | BLING_FLAG_COMPACT_BVH))) {
+      set_err(c.get(), BLING_ERR_INVALID_ARG,
+              "bling_opts.flags: at most one of BLING_FLAG_WIDE_BVH, BLING_FLAG_GPU_BVH and "
+              "BLING_FLAG_COMPACT_BVH, and no unknown flags");
+      *out = c.release();
+      return BLING_ERR_INVALID_ARG;
+    }
   }
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
@@ -452,6 +457,7 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   bi.hi = hi.data();
   bi.max_leaf = c->opts.bvh_leaf_size > 0 ? c->opts.bvh_leaf_size : 4;
   bi.wide = (c->opts.flags & BLING_FLAG_WIDE_BVH) != 0;
+  bi.compact = (c->opts.flags & BLING_FLAG_COMPACT_BVH) != 0;
   BvhBuildOutput bo;
   // ---- BVH on the GPU (BLING_FLAG_GPU_BVH): boxes up, tree built in place
   GpuBvh gb;
@@ -486,8 +492,9 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
       std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb0).count();
   // the wide layout when it was built (it is skipped for very deep trees)
   const bool wide = !gpu_built && bi.wide && bo.wide_depth >= 0;
-  const std::vector<int32_t>& slot_prim = wide ? bo.slot_prim8 : bo.slot_prim;
-  const std::vector<uint8_t>& slot_last = wide ? bo.slot_last8 : bo.slot_last;
+  const bool compact = !gpu_built && !wide && bi.compact && bo.compact_ok;
+  const std::vector<int32_t>& slot_prim = wide ? bo.slot_prim8 : (compact ? bo.slot_primC : bo.slot_prim);
+  const std::vector<uint8_t>& slot_last = wide ? bo.slot_last8 : (compact ? bo.slot_lastC : bo.slot_last);
   // ---- leaf slots: in leaf order, or (GPU build) in primitive order, one per
   // leaf, gathered into leaf order on the device
   size_t n_slots = gpu_built ? (size_t)n_prims : slot_prim.size();
@@ -559,6 +566,10 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   } else if (wide) {
     if ((rc = upload(c, S->owned, (const uint4*)bo.nodes8.data(), bo.nodes8.size() / 4, &S->d_nodes8)))
       return rc;
+  } else if (compact) {
+    if ((rc = upload(c, S->owned, (const float4*)bo.nodesC.data(), bo.nodesC.size() / 4,
+                     &S->d_nodesC)))
+      return rc;
   } else {
     if ((rc = upload(c, S->owned, (const float4*)bo.nodes.data(), bo.nodes.size() / 4, &S->d_nodes)))
       return rc;
@@ -592,11 +603,15 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   S->accel.shapes = S->d_shapes;
   S->accel.root_ref = gpu_built ? gb.root_ref : bo.root_ref;
   S->accel.root8 = bo.root8;
-  S->accel.wide = wide ? 1 : 0;
+  S->accel.nodesC = S->d_nodesC;
+  S->accel.rootC = bo.rootC;
+  S->accel.wide = wide ? LAYOUT_WIDE : (compact ? LAYOUT_COMPACT : LAYOUT_BINARY);
   S->accel.n_shapes = d->n_shapes;
   S->accel.n_prims = n_prims;
   S->n_nodes = gpu_built ? gb.n_nodes
-                         : (wide ? (int64_t)bo.nodes8.size() / 20 : (int64_t)bo.nodes.size() / 16);
+                         : (wide ? (int64_t)bo.nodes8.size() / 20
+                                 : (compact ? (int64_t)bo.nodesC.size() / 8
+                                            : (int64_t)bo.nodes.size() / 16));
   S->n_slots = (int64_t)n_slots;
   // ---- shading data for the path integrator
   if ((rc = integrator_upload_scene(c->stream, *d, order, prim_owner, prim_tri, shapes, shape_light,
@@ -608,7 +623,9 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   S->stats.scene_build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   S->stats.bvh_nodes = (uint64_t)S->n_nodes;
   S->stats.bvh_leaf_prims = (uint64_t)n_slots;
-  size_t bytes = (gpu_built ? (size_t)gb.n_nodes * 16 : (wide ? bo.nodes8.size() : bo.nodes.size())) * 4 +
+  size_t bytes = (gpu_built ? (size_t)gb.n_nodes * 16
+                            : (wide ? bo.nodes8.size() : (compact ? bo.nodesC.size() : bo.nodes.size()))) *
+                     4 +
                  slots.size() * 4 + shapes.size() * sizeof(DShape);
   S->stats.device_bytes = bytes + S->shading.bytes;
   *out = S.release();
@@ -1229,8 +1246,10 @@ int bling_bvh_selftest(const float* lo, const float* hi, int64_t n, int32_t max_
   bi.hi = hi;
   bi.max_leaf = max_leaf > 0 ? max_leaf : 4;
   bi.wide = true;
+  bi.compact = true;
   BvhBuildOutput bo;
   if (build_bvh(bi, bo) != 0) return BLING_ERR_INVALID_ARG;
+  if (!bo.compact_ok) return -50;  // the 32-byte layout must exist for every tree
   stats[0] = (int64_t)bo.nodes.size() / 16;
   stats[1] = bo.wide_depth >= 0 ? (int64_t)bo.nodes8.size() / 20 : 0;
   stats[2] = bo.max_depth;

@@ -296,7 +296,7 @@ __global__ void k_bin_flip(BatchCtl* ctl) {
 }
 
 // closest hits of the current buffer's rays, each lane in its ray's scene
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128) k_btrace(BatchCtl* ctl,
                                                 const BatchSceneDev* __restrict__ scenes,
                                                 Slots tmp, PathStates ps) {
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(128) k_btrace(BatchCtl* ctl,
   const PathState& S = ps.b[cur];
   const size_t cap = tmp.cap;
   int64_t n = (int64_t)ctl->c[C_LIVE0 + cur];
-  traceWarpPersistent<false, WIDE, false>(
+  traceWarpPersistent<false, LAYOUT, false>(
       scenes[0].A, n, ctl->c + C_NEXT_TRACE,
       [&](int64_t q) { return loadRay7(S.ray, (int)q); },
       [&](int64_t q, const RayQueryResult& res) {
@@ -314,14 +314,14 @@ __global__ void __launch_bounds__(128) k_btrace(BatchCtl* ctl,
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ctl->c + C_CLOSEST, (unsigned long long)n);
 }
 
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128) k_btrace_shadow(BatchCtl* ctl,
                                                        const BatchSceneDev* __restrict__ scenes,
                                                        Slots tmp, PathStates ps, BatchQueues Q) {
   const PathState& S = ps.b[ctl->cur];
   int64_t n = (int64_t)ctl->c[C_SHADOW];
   const int32_t* __restrict__ queue = Q.shadow;
-  traceWarpPersistent<true, WIDE, false>(
+  traceWarpPersistent<true, LAYOUT, false>(
       scenes[0].A, n, ctl->c + C_NEXT_SHADOW,
       [&](int64_t q) { return loadShadowRay(tmp, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
@@ -332,14 +332,14 @@ __global__ void __launch_bounds__(128) k_btrace_shadow(BatchCtl* ctl,
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ctl->c + C_ANY, (unsigned long long)n);
 }
 
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128) k_btrace_mis(BatchCtl* ctl,
                                                     const BatchSceneDev* __restrict__ scenes,
                                                     Slots tmp, PathStates ps, BatchQueues Q) {
   const PathState& S = ps.b[ctl->cur];
   int64_t n = (int64_t)ctl->c[C_MIS];
   const int32_t* __restrict__ queue = Q.mis;
-  traceWarpPersistent<false, WIDE, false>(
+  traceWarpPersistent<false, LAYOUT, false>(
       scenes[0].A, n, ctl->c + C_NEXT_MIS,
       [&](int64_t q) { return loadRay7(tmp.mray, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
@@ -573,16 +573,16 @@ unsigned residentBlocks(K kernel, int block, int sms) {
   return (unsigned)(std::max(1, sms) * std::max(1, per_sm));
 }
 
-template <bool WIDE>
+template <int LAYOUT>
 void shapesFor(BatchEngine* b, int sms) {
   const int bl = b->cfg.block;
-  b->g_trace = residentBlocks(k_btrace<WIDE>, bl, sms);
-  b->g_shadow = residentBlocks(k_btrace_shadow<WIDE>, bl, sms);
-  b->g_mis = residentBlocks(k_btrace_mis<WIDE>, bl, sms);
+  b->g_trace = residentBlocks(k_btrace<LAYOUT>, bl, sms);
+  b->g_shadow = residentBlocks(k_btrace_shadow<LAYOUT>, bl, sms);
+  b->g_mis = residentBlocks(k_btrace_mis<LAYOUT>, bl, sms);
 }
 
 // one iteration's launches, in order, on b->stream
-template <bool WIDE>
+template <int LAYOUT>
 cudaError_t enqueueIterationT(BatchEngine* b, int use_cond, unsigned long long max_iters) {
   const int bl = b->cfg.block;
   const size_t cap = (size_t)b->cap;
@@ -596,15 +596,15 @@ cudaError_t enqueueIterationT(BatchEngine* b, int use_cond, unsigned long long m
     k_bin_scatter<<<b->g_bin, 128, 0, s>>>(b->d_ctl, b->ps, b->q, cap);
     k_bin_flip<<<1, 32, 0, s>>>(b->d_ctl);
   }
-  k_btrace<WIDE><<<b->g_trace, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps);
+  k_btrace<LAYOUT><<<b->g_trace, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps);
   cudaMemsetAsync(b->q.bins, 0, sizeof(unsigned int) * kBins, s);
   k_bclass_count<<<b->g_bin, 128, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
   k_bin_scan<<<1, 1024, 0, s>>>(b->q.bins);
   k_bclass_scatter<<<b->g_bin, 128, 0, s>>>(b->d_ctl, b->q);
   k_bshade<<<b->g_shade, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps, b->q,
                                      b->d_job_done);
-  k_btrace_shadow<WIDE><<<b->g_shadow, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
-  k_btrace_mis<WIDE><<<b->g_mis, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
+  k_btrace_shadow<LAYOUT><<<b->g_shadow, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
+  k_btrace_mis<LAYOUT><<<b->g_mis, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
   k_bresolve<<<b->g_resolve, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps, b->q,
                                          b->d_job_done);
   k_iter_end<<<1, 32, 0, s>>>(b->d_ctl, b->cond, use_cond, max_iters);
@@ -612,18 +612,16 @@ cudaError_t enqueueIterationT(BatchEngine* b, int use_cond, unsigned long long m
 }
 
 cudaError_t enqueueIteration(BatchEngine* b, int use_cond, unsigned long long max_iters) {
-  return b->wide == 1 ? enqueueIterationT<true>(b, use_cond, max_iters)
-                      : enqueueIterationT<false>(b, use_cond, max_iters);
+  return withLayout(b->wide, [&](auto L) {
+    return enqueueIterationT<decltype(L)::value>(b, use_cond, max_iters);
+  });
 }
 
 int launchShapes(BatchEngine* b, std::string& err) {
   int sms = 0;
   BRET(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
   const int bl = b->cfg.block;
-  if (b->wide == 1)
-    shapesFor<true>(b, sms);
-  else
-    shapesFor<false>(b, sms);
+  withLayout(b->wide, [&](auto L) { shapesFor<decltype(L)::value>(b, sms); });
   unsigned cap_blocks = (unsigned)std::max<int64_t>(1, (b->cap + bl - 1) / bl);
   b->g_shade = std::min(residentBlocks(k_bshade, bl, sms), cap_blocks);
   b->g_resolve = std::min(residentBlocks(k_bresolve, bl, sms), cap_blocks);
@@ -806,7 +804,7 @@ int batch_scene(BatchEngine* b, uint64_t key, const DevAccel& A, const DevShadin
     err = "batch scene table full";
     return BLING_ERR_BOUNDS;
   }
-  int wide = A.wide ? 1 : 0;
+  int wide = A.wide;
   if (b->wide >= 0 && b->wide != wide) {
     err = "all scenes of a batch must use the same BVH layout";
     return BLING_ERR_INVALID_ARG;

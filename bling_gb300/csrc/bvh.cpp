@@ -345,6 +345,101 @@ static bool build_wide(const Builder& B, BvhBuildOutput& out) {
   return out.wide_depth <= kWideStack / 7 - 1;
 }
 
+// ---- 32-byte quantised binary layout
+// quantises child box kb into the node frame (origin lo, scales 2^e[a]) with
+// one quantum of margin; false if the decoded box would not contain kb
+static bool quantise(const Box& nb, const int e[3], const Box& kb, uint8_t qlo[3],
+                     uint8_t qhi[3]) {
+  for (int a = 0; a < 3; a++) {
+    double lo = nb.lo[a], scale = std::ldexp(1.0, e[a]);
+    double ql = std::floor(((double)kb.lo[a] - lo) / scale) - 1;
+    double qh = std::ceil(((double)kb.hi[a] - lo) / scale) + 1;
+    ql = std::max(0.0, std::min(255.0, ql));
+    qh = std::max(0.0, std::min(255.0, qh));
+    if (lo + ql * scale > (double)kb.lo[a] || lo + qh * scale < (double)kb.hi[a]) return false;
+    qlo[a] = (uint8_t)ql;
+    qhi[a] = (uint8_t)qh;
+  }
+  return true;
+}
+
+static bool emit_compact(const Builder& B, int64_t bnode, BvhBuildOutput& out) {
+  const size_t me = out.nodesC.size() / 8;
+  out.nodesC.resize(out.nodesC.size() + 8, 0u);
+  const BNode& nd = B.nodes[bnode];
+  int64_t c[2] = {nd.left, nd.right};
+  bool leaf[2] = {B.nodes[c[0]].count > 0, B.nodes[c[1]].count > 0};
+  if (!leaf[0] && leaf[1]) {  // a leaf child goes first
+    std::swap(c[0], c[1]);
+    std::swap(leaf[0], leaf[1]);
+  }
+  auto add_leaf = [&](const BNode& k) {
+    for (int64_t i = 0; i < k.count; i++) {
+      out.slot_primC.push_back(B.refs[k.begin + i]);
+      out.slot_lastC.push_back(i + 1 == k.count ? 1 : 0);
+    }
+  };
+  uint32_t meta = (leaf[0] ? 1u : 0u) | (leaf[1] ? 2u : 0u);
+  uint32_t w7 = 0;
+  if (leaf[0]) {
+    const BNode& k0 = B.nodes[c[0]];
+    if (k0.count > 63) return false;
+    meta |= (uint32_t)k0.count << 2;
+    w7 = (uint32_t)out.slot_primC.size();
+    add_leaf(k0);
+    if (leaf[1]) add_leaf(B.nodes[c[1]]);
+  }
+  // the node frame: origin = the node's box minimum, 255 quanta cover the extent
+  const Box& nb = nd.box;
+  int e[3];
+  uint32_t ebits = 0;
+  for (int a = 0; a < 3; a++) {
+    double ext = (double)nb.hi[a] - nb.lo[a];
+    int ea = -100;
+    if (ext > 0) {
+      ea = (int)std::ceil(std::log2(ext * (1.0 + 1.0 / 1024.0) / 255.0));
+      while (std::ldexp(255.0, ea) < ext * (1.0 + 1.0 / 1024.0)) ea++;
+    }
+    e[a] = std::max(-126, std::min(127, ea));
+    ebits |= (uint32_t)(e[a] + 127) << (8 * a);
+  }
+  uint8_t q[12];
+  for (int k = 0; k < 2; k++)
+    if (!quantise(nb, e, B.nodes[c[k]].box, &q[6 * k], &q[6 * k + 3])) return false;
+  {
+    uint32_t* w = &out.nodesC[8 * me];
+    memcpy(&w[0], nb.lo, 12);
+    w[3] = ebits | (meta << 24);
+    memcpy(&w[4], q, 12);
+  }
+  if (!leaf[0]) {  // both inner: child 0 next, child 1 after child 0's subtree
+    if (!emit_compact(B, c[0], out)) return false;
+    w7 = (uint32_t)(out.nodesC.size() / 8);
+    if (!emit_compact(B, c[1], out)) return false;
+  } else if (!leaf[1]) {  // leaf child 0, inner child 1 next
+    if (!emit_compact(B, c[1], out)) return false;
+  }
+  out.nodesC[8 * me + 7] = w7;
+  return true;
+}
+
+static bool build_compact(const Builder& B, BvhBuildOutput& out) {
+  out.nodesC.clear();
+  out.slot_primC.clear();
+  out.slot_lastC.clear();
+  const BNode& root = B.nodes[0];
+  if (root.count > 0) {
+    out.rootC = ~(int32_t)0;
+    for (int64_t i = 0; i < root.count; i++) {
+      out.slot_primC.push_back(B.refs[root.begin + i]);
+      out.slot_lastC.push_back(i + 1 == root.count ? 1 : 0);
+    }
+    return true;
+  }
+  out.rootC = 0;
+  return emit_compact(B, 0, out);
+}
+
 }  // namespace
 
 int build_bvh(const BvhBuildInput& in, BvhBuildOutput& out) {
@@ -358,6 +453,12 @@ int build_bvh(const BvhBuildInput& in, BvhBuildOutput& out) {
     out.slot_prim8.clear();
     out.slot_last8.clear();
     out.wide_depth = -1;  // the wide layout is not available for this tree
+  }
+  out.compact_ok = in.compact && build_compact(B, out);
+  if (!out.compact_ok) {
+    out.nodesC.clear();
+    out.slot_primC.clear();
+    out.slot_lastC.clear();
   }
   out.nodes.clear();
   out.slot_prim.clear();
@@ -573,6 +674,43 @@ DBox validate_wide(Validator& V, const BvhBuildOutput& out, int32_t ref, int dep
   return un;
 }
 
+DBox validate_compact(Validator& V, const BvhBuildOutput& out, int32_t ref, int depth) {
+  if (ref < 0) return V.leaf(ref);
+  DBox un;
+  un.reset();
+  size_t n_nodes = out.nodesC.size() / 8;
+  if (depth > kBvhMaxDepth || (size_t)ref >= n_nodes) {
+    V.err = -40;
+    return un;
+  }
+  const uint32_t* w = &out.nodesC[8 * (size_t)ref];
+  float p[3];
+  memcpy(p, w, 12);
+  uint8_t q[12];
+  memcpy(q, &w[4], 12);
+  uint32_t meta = w[3] >> 24;
+  bool l0 = meta & 1u, l1 = meta & 2u;
+  if (!l0 && l1) {
+    V.err = -41;  // a leaf child must come first
+    return un;
+  }
+  int32_t refs[2];
+  refs[0] = l0 ? ~(int32_t)w[7] : ref + 1;
+  refs[1] = l1 ? ~(int32_t)(w[7] + (meta >> 2)) : (l0 ? ref + 1 : (int32_t)w[7]);
+  for (int c = 0; c < 2; c++) {
+    DBox cb = validate_compact(V, out, refs[c], depth + 1);
+    DBox dec;
+    for (int a = 0; a < 3; a++) {
+      double scale = std::ldexp(1.0, (int)((w[3] >> (8 * a)) & 0xff) - 127);
+      dec.lo[a] = (double)p[a] + q[6 * c + a] * scale;
+      dec.hi[a] = (double)p[a] + q[6 * c + 3 + a] * scale;
+    }
+    if (!dec.contains(cb)) V.err = -42;
+    un.grow(cb);
+  }
+  return un;
+}
+
 }  // namespace
 
 int validate_bvh(const BvhBuildInput& in, const BvhBuildOutput& out) {
@@ -592,6 +730,12 @@ int validate_bvh(const BvhBuildInput& in, const BvhBuildOutput& out) {
     V.leaf(out.root8);
     int rc = V.finish();
     if (rc) return rc - 100;
+  }
+  if (out.compact_ok) {
+    Validator V(in, out.slot_primC, out.slot_lastC);
+    validate_compact(V, out, out.rootC, 0);
+    int rc = V.finish();
+    if (rc) return rc - 200;
   }
   return 0;
 }

@@ -20,6 +20,7 @@ struct BvhBuildInput {
   int max_leaf = 4;             // primitives per leaf at most (when splittable)
   int threads = 0;              // 0: hardware concurrency
   bool wide = true;             // also produce the 8-wide quantised layout
+  bool compact = false;         // also produce the 32-byte quantised binary layout
 };
 
 struct BvhBuildOutput {
@@ -52,6 +53,26 @@ struct BvhBuildOutput {
   std::vector<uint8_t> slot_last8;
   int32_t root8 = 0;      // node 0, or a leaf ref when the whole scene is one leaf
   int wide_depth = 0;     // longest root-to-leaf path in wide nodes
+
+  // The binary tree in 32-byte quantised nodes (filled when
+  // BvhBuildInput::compact), one 256-bit load per visit.  8 words per node:
+  //   w0..w2  origin p.xyz (float): the node's box minimum
+  //   w3      biased exponents ex | ey << 8 | ez << 16 (scale 2^(e - 127)),
+  //           meta << 24: bit 0 child 0 is a leaf, bit 1 child 1 is a leaf,
+  //           bits 2..7 the slot count of a leaf child 0
+  //   w4..w6  child boxes q, bytes: c0 lo.xyz hi.xyz, c1 lo.xyz hi.xyz
+  //           (box = p + q * scale, rounded outward by one quantum)
+  //   w7      both children inner: child 1's node (child 0 is the next node);
+  //           otherwise the first slot of leaf child 0; a leaf child 1's
+  //           slots follow it, an inner child 1 is the next node
+  // Nodes are in depth-first order and a node with one leaf child keeps it
+  // as child 0, so one word locates both children.  The leaf slots follow
+  // their own order.
+  std::vector<uint32_t> nodesC;
+  std::vector<int32_t> slot_primC;
+  std::vector<uint8_t> slot_lastC;
+  int32_t rootC = 0;      // node 0, or a leaf ref when the whole scene is one leaf
+  bool compact_ok = false;
 };
 
 constexpr int kWideStack = 128;  // per-lane stack entries of the wide traversal

@@ -41,6 +41,7 @@ struct bling_scene {
   bgpu::DevAccel accel{};
   float4* d_nodes = nullptr;
   uint4* d_nodes8 = nullptr;
+  float4* d_nodesC = nullptr;
   float4* d_slots = nullptr;
   bgpu::DShape* d_shapes = nullptr;
   bgpu::DevShading shading{};

@@ -130,12 +130,12 @@ __global__ void __launch_bounds__(128) k_class_scatter(const int32_t* __restrict
 }
 
 // closest hit of the live paths' rays (scIntersect)
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
                                                const unsigned long long* __restrict__ qcount,
                                                unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)*qcount;
-  traceWarpPersistent<false, WIDE, false>(
+  traceWarpPersistent<false, LAYOUT, false>(
       A, n, counters + C_NEXT_TRACE, [&](int64_t q) { return loadRay7(st.ray, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         int s = queue[q];
@@ -145,12 +145,12 @@ __global__ void __launch_bounds__(128, 10) k_trace(DevAccel A, Slots st, const i
 }
 
 // occlusion of the shadow rays (occluded, Scene.hs:45-47)
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_trace_shadow(DevAccel A, Slots st,
                                                       const int32_t* __restrict__ queue,
                                                       unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_SHADOW];
-  traceWarpPersistent<true, WIDE, false>(
+  traceWarpPersistent<true, LAYOUT, false>(
       A, n, counters + C_NEXT_SHADOW, [&](int64_t q) { return loadShadowRay(st, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         st.svis[queue[q]] = res.hit ? 0 : 1;
@@ -160,12 +160,12 @@ __global__ void __launch_bounds__(128, 10) k_trace_shadow(DevAccel A, Slots st,
 }
 
 // closest hit of the BSDF-sampled MIS rays
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_trace_mis(DevAccel A, Slots st,
                                                    const int32_t* __restrict__ queue,
                                                    unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_MIS];
-  traceWarpPersistent<false, WIDE, false>(
+  traceWarpPersistent<false, LAYOUT, false>(
       A, n, counters + C_NEXT_MIS, [&](int64_t q) { return loadRay7(st.mray, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         int s = queue[q];
@@ -250,10 +250,14 @@ Grids grids(int device, int sms) {
   std::lock_guard<std::mutex> lk(g_grids_mu);
   if (device >= 0 && device < 64 && g_grids_ready[device]) return g_grids[device];
   Grids g;
-  // both layouts' kernels use the same registers within a few; take the smaller grid
-  g.trace = std::min(residentGrid(k_trace<true>, sms), residentGrid(k_trace<false>, sms));
-  g.shadow = std::min(residentGrid(k_trace_shadow<true>, sms), residentGrid(k_trace_shadow<false>, sms));
-  g.mis = std::min(residentGrid(k_trace_mis<true>, sms), residentGrid(k_trace_mis<false>, sms));
+  // the layouts' kernels use the same registers within a few; take the smallest grid
+  g.trace = std::min({residentGrid(k_trace<LAYOUT_BINARY>, sms), residentGrid(k_trace<LAYOUT_WIDE>, sms),
+                      residentGrid(k_trace<LAYOUT_COMPACT>, sms)});
+  g.shadow = std::min({residentGrid(k_trace_shadow<LAYOUT_BINARY>, sms),
+                       residentGrid(k_trace_shadow<LAYOUT_WIDE>, sms),
+                       residentGrid(k_trace_shadow<LAYOUT_COMPACT>, sms)});
+  g.mis = std::min({residentGrid(k_trace_mis<LAYOUT_BINARY>, sms), residentGrid(k_trace_mis<LAYOUT_WIDE>, sms),
+                    residentGrid(k_trace_mis<LAYOUT_COMPACT>, sms)});
   g.shade = residentGrid(k_shade, sms);
   g.resolve = residentGrid(k_resolve, sms);
   g.raygen = (unsigned)std::max(1, sms * 8);
@@ -280,10 +284,10 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
     k_bounce_reset<<<1, 32, 0, stream>>>(counters, C_LIVE0 + (1 - in));
     unsigned gt = std::min(G.trace, cap_blocks), gs = std::min(G.shadow, cap_blocks),
              gm = std::min(G.mis, cap_blocks);
-    if (A.wide)
-      k_trace<true><<<gt, block, 0, stream>>>(A, st, Q.live[in], counters + C_LIVE0 + in, counters);
-    else
-      k_trace<false><<<gt, block, 0, stream>>>(A, st, Q.live[in], counters + C_LIVE0 + in, counters);
+    withLayout(A.wide, [&](auto L) {
+      k_trace<decltype(L)::value><<<gt, block, 0, stream>>>(A, st, Q.live[in],
+                                                           counters + C_LIVE0 + in, counters);
+    });
     k_class_count<<<G.raygen, block, 0, stream>>>(A, S, st, Q.live[in], counters + C_LIVE0 + in,
                                                    Q.cls, counters);
     k_class_scatter<<<G.raygen, block, 0, stream>>>(Q.live[in], counters + C_LIVE0 + in, Q.cls,
@@ -291,13 +295,10 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
     k_shade<<<std::min(G.shade, cap_blocks), block, 0, stream>>>(A, S, P, st, Q, depth,
                                                                   C_LIVE0 + in, d_film, d_filter,
                                                                   counters);
-    if (A.wide) {
-      k_trace_shadow<true><<<gs, block, 0, stream>>>(A, st, Q.shadow, counters);
-      k_trace_mis<true><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);
-    } else {
-      k_trace_shadow<false><<<gs, block, 0, stream>>>(A, st, Q.shadow, counters);
-      k_trace_mis<false><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);
-    }
+    withLayout(A.wide, [&](auto L) {
+      k_trace_shadow<decltype(L)::value><<<gs, block, 0, stream>>>(A, st, Q.shadow, counters);
+      k_trace_mis<decltype(L)::value><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);
+    });
     k_resolve<<<std::min(G.resolve, cap_blocks), block, 0, stream>>>(A, S, P, st, Q,
                                                                       C_LIVE0 + (1 - in), d_film,
                                                                       d_filter, counters);

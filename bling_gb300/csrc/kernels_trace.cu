@@ -17,12 +17,12 @@ __device__ __forceinline__ Ray loadRay(const float* __restrict__ rays, int64_t n
 constexpr int kTraceBlock = 128;
 static_assert(kTraceBlock <= kMaxTraceBlock, "the traversal's shared stack holds kMaxTraceBlock lanes");
 
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_closest(DevAccel A, const float* __restrict__ rays, int64_t n,
                     float* __restrict__ out_t, int32_t* __restrict__ out_prim,
                     float* __restrict__ out_b, unsigned long long* __restrict__ next_ray) {
-  traceWarpPersistent<false, WIDE, false>(
+  traceWarpPersistent<false, LAYOUT, false>(
       A, n, next_ray, [&](int64_t i) { return loadRay(rays, n, i); },
       [&](int64_t i, const RayQueryResult& q) {
         out_t[i] = q.hit ? q.t : INFINITY;
@@ -34,22 +34,22 @@ __global__ void __launch_bounds__(kTraceBlock)
       });
 }
 
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(kTraceBlock, 10)
     k_trace_any(DevAccel A, const float* __restrict__ rays, int64_t n,
                 uint8_t* __restrict__ out_hit, unsigned long long* __restrict__ next_ray) {
-  traceWarpPersistent<true, WIDE, false>(
+  traceWarpPersistent<true, LAYOUT, false>(
       A, n, next_ray, [&](int64_t i) { return loadRay(rays, n, i); },
       [&](int64_t i, const RayQueryResult& q) { out_hit[i] = q.hit ? 1 : 0; });
 }
 
 // totals[0] nodes visited, totals[1] leaf slots tested, totals[2] the next-ray counter
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(kTraceBlock)
     k_trace_counts(DevAccel A, const float* __restrict__ rays, int64_t n,
                    unsigned long long* __restrict__ totals) {
   TraversalCounts c{0, 0};
-  traceWarpPersistent<false, WIDE, true>(
+  traceWarpPersistent<false, LAYOUT, true>(
       A, n, totals + 2, [&](int64_t i) { return loadRay(rays, n, i); },
       [&](int64_t, const RayQueryResult&) {}, &c);
   // warp reduction, one atomic per warp
@@ -80,13 +80,12 @@ cudaError_t launch_trace_counts(const DevAccel& A, const float* d_rays, int64_t 
   if (n <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d_totals, 0, 3 * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  if (A.wide)
-    k_trace_counts<true><<<persistentGrid(k_trace_counts<true>, n), kTraceBlock, 0, stream>>>(
+  return withLayout(A.wide, [&](auto L) {
+    constexpr int LY = decltype(L)::value;
+    k_trace_counts<LY><<<persistentGrid(k_trace_counts<LY>, n), kTraceBlock, 0, stream>>>(
         A, d_rays, n, d_totals);
-  else
-    k_trace_counts<false><<<persistentGrid(k_trace_counts<false>, n), kTraceBlock, 0, stream>>>(
-        A, d_rays, n, d_totals);
-  return cudaGetLastError();
+    return cudaGetLastError();
+  });
 }
 
 cudaError_t launch_trace_closest(const DevAccel& A, const float* d_rays, int64_t n, float* d_t,
@@ -95,13 +94,12 @@ cudaError_t launch_trace_closest(const DevAccel& A, const float* d_rays, int64_t
   if (n <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  if (A.wide)
-    k_trace_closest<true><<<persistentGrid(k_trace_closest<true>, n), kTraceBlock, 0, stream>>>(
+  return withLayout(A.wide, [&](auto L) {
+    constexpr int LY = decltype(L)::value;
+    k_trace_closest<LY><<<persistentGrid(k_trace_closest<LY>, n), kTraceBlock, 0, stream>>>(
         A, d_rays, n, d_t, d_prim, d_b1b2, d_counter);
-  else
-    k_trace_closest<false><<<persistentGrid(k_trace_closest<false>, n), kTraceBlock, 0, stream>>>(
-        A, d_rays, n, d_t, d_prim, d_b1b2, d_counter);
-  return cudaGetLastError();
+    return cudaGetLastError();
+  });
 }
 
 cudaError_t launch_trace_any(const DevAccel& A, const float* d_rays, int64_t n, uint8_t* d_hit,
@@ -109,13 +107,12 @@ cudaError_t launch_trace_any(const DevAccel& A, const float* d_rays, int64_t n, 
   if (n <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  if (A.wide)
-    k_trace_any<true><<<persistentGrid(k_trace_any<true>, n), kTraceBlock, 0, stream>>>(
+  return withLayout(A.wide, [&](auto L) {
+    constexpr int LY = decltype(L)::value;
+    k_trace_any<LY><<<persistentGrid(k_trace_any<LY>, n), kTraceBlock, 0, stream>>>(
         A, d_rays, n, d_hit, d_counter);
-  else
-    k_trace_any<false><<<persistentGrid(k_trace_any<false>, n), kTraceBlock, 0, stream>>>(
-        A, d_rays, n, d_hit, d_counter);
-  return cudaGetLastError();
+    return cudaGetLastError();
+  });
 }
 
 }  // namespace bgpu

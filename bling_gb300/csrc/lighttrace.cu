@@ -129,12 +129,12 @@ __global__ void k_lt_reset(unsigned long long* counters, int next_live) {
   if (t == 3) counters[L_NEXT_SHADOW] = 0;
 }
 
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_lt_trace(DevAccel A, LtSlots st, int in,
                                                       unsigned long long* __restrict__ counters) {
   const int32_t* __restrict__ queue = st.live[in];
   int64_t n = (int64_t)counters[L_LIVE0 + in];
-  traceWarpPersistent<false, WIDE, false>(
+  traceWarpPersistent<false, LAYOUT, false>(
       A, n, counters + L_NEXT_TRACE, [&](int64_t q) { return loadRay7(st.ray, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         st.hit[queue[q]] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
@@ -226,13 +226,13 @@ __global__ void __launch_bounds__(128, 4) k_lt_vertex(DevAccel A, DevShading S, 
 
 // occluded (Scene.hs:45-47) for the camera connections; the visible ones
 // are splatted
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_lt_shadow(DevAccel A, LtSlots st,
                                                        float* __restrict__ splat_xyz,
                                                        unsigned long long* __restrict__ counters) {
   const int32_t* __restrict__ queue = st.shadow;
   int64_t n = (int64_t)counters[L_SHADOW];
-  traceWarpPersistent<true, WIDE, false>(
+  traceWarpPersistent<true, LAYOUT, false>(
       A, n, counters + L_NEXT_SHADOW,
       [&](int64_t q) {
         const float4* p = reinterpret_cast<const float4*>(st.sray + 8 * (size_t)queue[q]);
@@ -310,8 +310,12 @@ int light_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, cons
   int sms = 0;
   RET_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   const int block = 128;
-  unsigned g_trace = A.wide ? residentGrid(k_lt_trace<true>, sms) : residentGrid(k_lt_trace<false>, sms);
-  unsigned g_shadow = A.wide ? residentGrid(k_lt_shadow<true>, sms) : residentGrid(k_lt_shadow<false>, sms);
+  unsigned g_trace = withLayout(A.wide, [&](auto L) {
+    return residentGrid(k_lt_trace<decltype(L)::value>, sms);
+  });
+  unsigned g_shadow = withLayout(A.wide, [&](auto L) {
+    return residentGrid(k_lt_shadow<decltype(L)::value>, sms);
+  });
   unsigned g_vertex = residentGrid(k_lt_vertex, sms);
   unsigned g_emit = (unsigned)std::max(1, sms * 8);
   for (int64_t base = 0; base < a.photons; base += (int64_t)ws.capacity) {
@@ -329,15 +333,13 @@ int light_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, cons
       k_lt_reset<<<1, 32, 0, stream>>>(counters, L_LIVE0 + (1 - in));
       unsigned gt = std::min(g_trace, cap_blocks), gs = std::min(g_shadow, cap_blocks),
                gv = std::min(g_vertex, cap_blocks);
-      if (A.wide)
-        k_lt_trace<true><<<gt, block, 0, stream>>>(A, st, in, counters);
-      else
-        k_lt_trace<false><<<gt, block, 0, stream>>>(A, st, in, counters);
+      withLayout(A.wide, [&](auto L) {
+        k_lt_trace<decltype(L)::value><<<gt, block, 0, stream>>>(A, st, in, counters);
+      });
       k_lt_vertex<<<gv, block, 0, stream>>>(A, S, P, st, depth, in, counters);
-      if (A.wide)
-        k_lt_shadow<true><<<gs, block, 0, stream>>>(A, st, d_splat, counters);
-      else
-        k_lt_shadow<false><<<gs, block, 0, stream>>>(A, st, d_splat, counters);
+      withLayout(A.wide, [&](auto L) {
+        k_lt_shadow<decltype(L)::value><<<gs, block, 0, stream>>>(A, st, d_splat, counters);
+      });
       RET_CUDA(cudaGetLastError());
       if (depth >= 7 && (depth & 3) == 3) {
         unsigned long long live = 0;

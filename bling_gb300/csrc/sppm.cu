@@ -173,11 +173,11 @@ __device__ __forceinline__ int64_t nodeCount(const unsigned long long* counters,
   return (int64_t)min(counters[S_NODES0 + q], (unsigned long long)cap);
 }
 
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_sp_camtrace(DevAccel A, CamNodes nb, int in, size_t cap,
                                                          unsigned long long* __restrict__ counters) {
   int64_t n = nodeCount(counters, in, cap);
-  traceWarpPersistent<false, WIDE, false>(
+  traceWarpPersistent<false, LAYOUT, false>(
       A, n, counters + S_NEXT_TRACE, [&](int64_t q) { return loadRay7(nb.ray, (int)q); },
       [&](int64_t q, const RayQueryResult& res) {
         nb.hit[q] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
@@ -452,12 +452,12 @@ __global__ void k_sp_preset(unsigned long long* counters, int next) {
   if (threadIdx.x == 1) counters[S_NEXT_TRACE] = 0;
 }
 
-template <bool WIDE>
+template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_sp_ptrace(DevAccel A, SpPhotons ph, int in,
                                                        unsigned long long* __restrict__ counters) {
   const int32_t* __restrict__ queue = ph.live[in];
   int64_t n = (int64_t)counters[S_PLIVE0 + in];
-  traceWarpPersistent<false, WIDE, false>(
+  traceWarpPersistent<false, LAYOUT, false>(
       A, n, counters + S_NEXT_TRACE, [&](int64_t q) { return loadRay7(ph.ray, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
         ph.hit[queue[q]] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
@@ -770,9 +770,9 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
   int sms = 0;
   RET_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   const int block = 128;
-  const bool wide = A.wide != 0;
-  unsigned g_trace = wide ? residentGrid(k_sp_camtrace<true>, sms, block)
-                          : residentGrid(k_sp_camtrace<false>, sms, block);
+  unsigned g_trace = withLayout(A.wide, [&](auto L) {
+    return residentGrid(k_sp_camtrace<decltype(L)::value>, sms, block);
+  });
   unsigned g_shade = residentGrid(k_sp_camshade, sms, block);
   unsigned g_wide = (unsigned)std::max(1, sms * 8);
 
@@ -810,12 +810,10 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
       int in = d & 1;
       k_sp_reset<<<1, 32, 0, stream>>>(counters, S_NODES0 + (1 - in));
       unsigned nb = (unsigned)std::max<size_t>(1, (ws.cam_nodes + block - 1) / block);
-      if (wide)
-        k_sp_camtrace<true><<<std::min(g_trace, nb), block, 0, stream>>>(A, cs.nb[in], in, cs.NC,
-                                                                          counters);
-      else
-        k_sp_camtrace<false><<<std::min(g_trace, nb), block, 0, stream>>>(A, cs.nb[in], in, cs.NC,
-                                                                           counters);
+      withLayout(A.wide, [&](auto L) {
+        k_sp_camtrace<decltype(L)::value><<<std::min(g_trace, nb), block, 0, stream>>>(
+            A, cs.nb[in], in, cs.NC, counters);
+      });
       k_sp_camshade<<<std::min(g_shade, nb), block, 0, stream>>>(A, S, P, cs, hp, px.r2, px.count, in, d,
                                                                a.max_depth, counters);
       RET_CUDA(cudaGetLastError());
@@ -944,8 +942,9 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
     Q.sn = sn;
     Q.wc = V3{a.wc[0], a.wc[1], a.wc[2]};
     Q.wr = a.wr;
-    unsigned g_pt = wide ? residentGrid(k_sp_ptrace<true>, sms, block)
-                         : residentGrid(k_sp_ptrace<false>, sms, block);
+    unsigned g_pt = withLayout(A.wide, [&](auto L) {
+      return residentGrid(k_sp_ptrace<decltype(L)::value>, sms, block);
+    });
     unsigned g_vx = residentGrid(k_sp_vertex, sms, block);
     for (int64_t base = 0; base < nphot; base += (int64_t)ws.photon_cap) {
       int64_t count = std::min<int64_t>((int64_t)ws.photon_cap, nphot - base);
@@ -959,10 +958,10 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
         int in = depth & 1;
         unsigned cap_blocks = (unsigned)std::max<int64_t>(1, (n_cur + block - 1) / block);
         k_sp_preset<<<1, 32, 0, stream>>>(counters, S_PLIVE0 + (1 - in));
-        if (wide)
-          k_sp_ptrace<true><<<std::min(g_pt, cap_blocks), block, 0, stream>>>(A, ph, in, counters);
-        else
-          k_sp_ptrace<false><<<std::min(g_pt, cap_blocks), block, 0, stream>>>(A, ph, in, counters);
+        withLayout(A.wide, [&](auto L) {
+          k_sp_ptrace<decltype(L)::value><<<std::min(g_pt, cap_blocks), block, 0, stream>>>(
+              A, ph, in, counters);
+        });
         k_sp_vertex<<<std::min(g_vx, cap_blocks), block, 0, stream>>>(A, S, Q, ph, hp, hs, in, depth,
                                                                      counters);
         unsigned warp_blocks = (unsigned)std::max<int64_t>(1, (n_cur + 3) / 4);  // 4 warps a block

@@ -147,7 +147,7 @@ __device__ __forceinline__ float qbyte(uint32_t word, uint32_t sel) {
 // share the node layout); otherwise all rays walk A.
 constexpr int kSentinel = INT32_MIN;
 
-template <bool ANY, bool WIDE, bool COUNT, class LoadRay, class Emit,
+template <bool ANY, int LAYOUT, bool COUNT, class LoadRay, class Emit,
           class AccelOf = std::nullptr_t>
 __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n,
                                                     unsigned long long* __restrict__ next_ray,
@@ -155,7 +155,10 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
                                                     TraversalCounts* cnt = nullptr,
                                                     AccelOf accel_of = nullptr) {
   constexpr bool PER_LANE = !std::is_same<AccelOf, std::nullptr_t>::value;
+  constexpr bool WIDE = LAYOUT == LAYOUT_WIDE;
+  constexpr bool COMPACT = LAYOUT == LAYOUT_COMPACT;
   const float4* l_nodes = nullptr;
+  const float4* l_nodesC = nullptr;
   const uint4* l_nodes8 = nullptr;
   const float4* l_slots = nullptr;
   const DShape* l_shapes = nullptr;
@@ -169,6 +172,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
   Ray r;
   V3 inv;
   int oct = 0;
+  int zmask = 0;  // axes whose direction component is zero (inv = +-inf)
   float best_t = 0, bb1 = 0, bb2 = 0;
   int best_prim = -1;
   // The top kSharedStack entries of each lane's stack live in shared memory
@@ -216,6 +220,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
           } else {
             inv = V3{1.0f / r.d.x, 1.0f / r.d.y, 1.0f / r.d.z};
             oct = (signbit(inv.x) ? 1 : 0) | (signbit(inv.y) ? 2 : 0) | (signbit(inv.z) ? 4 : 0);
+            zmask = (isinf(inv.x) ? 1 : 0) | (isinf(inv.y) ? 2 : 0) | (isinf(inv.z) ? 4 : 0);
             best_t = r.tmax;
             best_prim = -1;
             bb1 = bb2 = 0.0f;
@@ -223,12 +228,13 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
             if constexpr (PER_LANE) {
               const DevAccel* la = accel_of(rid);
               l_nodes = la->nodes;
+              l_nodesC = la->nodesC;
               l_nodes8 = la->nodes8;
               l_slots = la->slots;
               l_shapes = la->shapes;
-              cur = WIDE ? la->root8 : la->root_ref;
+              cur = WIDE ? la->root8 : (COMPACT ? la->rootC : la->root_ref);
             } else {
-              cur = WIDE ? A.root8 : A.root_ref;
+              cur = WIDE ? A.root8 : (COMPACT ? A.rootC : A.root_ref);
             }
             leaf = kSentinel;
           }
@@ -294,6 +300,81 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
             }
           }
           cur = first != kSentinel ? first : pop();
+        } else if (COMPACT) {
+          // 32-byte quantised node (bvh.h): child box slab distances
+          // t = q * (scale / d) + (p - o) / d, as the 8-wide layout
+          float4 a, b;
+          ldg256(TW_ACC(nodesC) + 2 * (size_t)cur, a, b);
+          const uint32_t w3 = __float_as_uint(a.w);
+          const float sx = __uint_as_float((w3 & 0xffu) << 23) * inv.x;
+          const float sy = __uint_as_float(((w3 >> 8) & 0xffu) << 23) * inv.y;
+          const float sz = __uint_as_float(((w3 >> 16) & 0xffu) << 23) * inv.z;
+          const float bx = (a.x - r.o.x) * inv.x;
+          const float by = (a.y - r.o.y) * inv.y;
+          const float bz = (a.z - r.o.z) * inv.z;
+          // q bytes: c0 lo.xyz hi.xyz in b.x (4) and b.y (2), c1 in b.y (2) and b.z (4)
+          const uint32_t q0 = __float_as_uint(b.x), q1 = __float_as_uint(b.y),
+                         q2 = __float_as_uint(b.z);
+          const float c0lx = qbyte(q0, 0x7650u), c0ly = qbyte(q0, 0x7651u),
+                      c0lz = qbyte(q0, 0x7652u), c0hx = qbyte(q0, 0x7653u),
+                      c0hy = qbyte(q1, 0x7650u), c0hz = qbyte(q1, 0x7651u),
+                      c1lx = qbyte(q1, 0x7652u), c1ly = qbyte(q1, 0x7653u),
+                      c1lz = qbyte(q2, 0x7650u), c1hx = qbyte(q2, 0x7651u),
+                      c1hy = qbyte(q2, 0x7652u), c1hz = qbyte(q2, 0x7653u);
+          const bool nxh = oct & 1, nyh = oct & 2, nzh = oct & 4;  // near plane is hi
+          // per axis: near and far distance of child 0 and child 1
+          float nx0 = fmaf(nxh ? c0hx : c0lx, sx, bx), fx0 = fmaf(nxh ? c0lx : c0hx, sx, bx);
+          float ny0 = fmaf(nyh ? c0hy : c0ly, sy, by), fy0 = fmaf(nyh ? c0ly : c0hy, sy, by);
+          float nz0 = fmaf(nzh ? c0hz : c0lz, sz, bz), fz0 = fmaf(nzh ? c0lz : c0hz, sz, bz);
+          float nx1 = fmaf(nxh ? c1hx : c1lx, sx, bx), fx1 = fmaf(nxh ? c1lx : c1hx, sx, bx);
+          float ny1 = fmaf(nyh ? c1hy : c1ly, sy, by), fy1 = fmaf(nyh ? c1ly : c1hy, sy, by);
+          float nz1 = fmaf(nzh ? c1hz : c1lz, sz, bz), fz1 = fmaf(nzh ? c1lz : c1hz, sz, bz);
+          if (zmask) {
+            // a zero direction component (inv = +-inf) makes those distances
+            // 0 * inf or inf - inf: decide that slab by the origin instead,
+            // inside when it lies between the child's decoded planes (rounded
+            // outward), for all t; outside for none
+            auto slab = [&](float ql, float qh, float e_bits, float p, float o, float& n,
+                            float& f) {
+              bool in = __fmaf_rd(ql, e_bits, p) <= o && o <= __fmaf_ru(qh, e_bits, p);
+              n = in ? -INFINITY : INFINITY;
+              f = in ? INFINITY : -INFINITY;
+            };
+            if (zmask & 1) {
+              const float e = __uint_as_float((w3 & 0xffu) << 23);
+              slab(c0lx, c0hx, e, a.x, r.o.x, nx0, fx0);
+              slab(c1lx, c1hx, e, a.x, r.o.x, nx1, fx1);
+            }
+            if (zmask & 2) {
+              const float e = __uint_as_float(((w3 >> 8) & 0xffu) << 23);
+              slab(c0ly, c0hy, e, a.y, r.o.y, ny0, fy0);
+              slab(c1ly, c1hy, e, a.y, r.o.y, ny1, fy1);
+            }
+            if (zmask & 4) {
+              const float e = __uint_as_float(((w3 >> 16) & 0xffu) << 23);
+              slab(c0lz, c0hz, e, a.z, r.o.z, nz0, fz0);
+              slab(c1lz, c1hz, e, a.z, r.o.z, nz1, fz1);
+            }
+          }
+          float n0 = widenNear(fmaxf(fmaxf(nx0, ny0), nz0));
+          float f0 = widenFar(fminf(fminf(fx0, fy0), fz0));
+          float n1 = widenNear(fmaxf(fmaxf(nx1, ny1), nz1));
+          float f1 = widenFar(fminf(fminf(fx1, fy1), fz1));
+          bool h0 = fmaxf(n0, r.tmin) <= fminf(f0, best_t);
+          bool h1 = fmaxf(n1, r.tmin) <= fminf(f1, best_t);
+          const uint32_t meta = w3 >> 24, w7 = __float_as_uint(b.w);
+          const bool l0 = meta & 1u, l1 = meta & 2u;
+          int r0 = l0 ? ~(int)w7 : cur + 1;
+          int r1 = l1 ? ~(int)(w7 + (meta >> 2)) : (l0 ? cur + 1 : (int)w7);
+          if (h0 && h1) {
+            bool swap = n1 < n0;
+            cur = swap ? r1 : r0;
+            push(swap ? r0 : r1);
+          } else if (h0 || h1) {
+            cur = h0 ? r0 : r1;
+          } else {
+            cur = pop();
+          }
         } else {
           const float4* nd = TW_ACC(nodes) + 4 * (size_t)cur;  // 64-byte aligned
           float4 a, b, c, refs;

@@ -54,6 +54,8 @@ typedef struct bling_film bling_film;
 
 /* bling_opts.flags */
 #define BLING_FLAG_WIDE_BVH 1u /* 8-wide quantised BVH layout instead of the binary one */
+#define BLING_FLAG_COMPACT_BVH 4u /* binary BVH in 32-byte quantised nodes (one 256-bit
+                                     load per visit) instead of 64-byte float nodes */
 #define BLING_FLAG_GPU_BVH 2u  /* build the BVH on the GPU (Morton order and PLOC
                                   clustering, binary layout, one primitive per
                                   leaf) instead of the host's binned SAH; not with
@@ -525,7 +527,8 @@ int bling_server_debug_fail_step(bling_server* server, int32_t after_steps);
 /* ---- host helpers for building scenes (no GPU needed) ---- */
 /* Builds the BVH of n primitive boxes (lo/hi: 3n floats each) on the host and
  * checks its structure: each primitive in exactly one leaf, every stored box
- * (binary and quantised 8-wide) containing its subtree.  stats (5 entries):
+ * (binary, quantised 8-wide and 32-byte quantised binary) containing its
+ * subtree.  stats (5 entries):
  * binary inner nodes, wide nodes (0 when the wide layout was skipped), binary
  * depth, wide depth, leaves.  Returns 0 or a negative code of the first
  * violation.  The replacement of mkKdTree (Primitive/KdTree.hs:107-112) as a

@@ -37,14 +37,24 @@ def gpu_built_ctx():
     ctx.close()
 
 
-@pytest.fixture(params=["binary", "wide", "gpu-built"])
+@pytest.fixture(scope="module")
+def compact_ctx():
+    """A fourth context whose scenes use 32-byte quantised binary nodes."""
+    from bling_gb300.api import Context
+    ctx = Context(device=0, compact_bvh=True)
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(params=["binary", "wide", "gpu-built", "compact"])
 def ctx(request, gpu_ctx):
-    """Both BVH layouts, and the tree built on the GPU, must give the
+    """Every BVH layout, and the tree built on the GPU, must give the
     oracle's answers: traversal is conservative, so the answer does not
     depend on the tree."""
     if request.param == "binary":
         return gpu_ctx
-    return request.getfixturevalue("wide_ctx" if request.param == "wide" else "gpu_built_ctx")
+    return request.getfixturevalue({"wide": "wide_ctx", "gpu-built": "gpu_built_ctx",
+                                    "compact": "compact_ctx"}[request.param])
 
 
 def _bits(a):
