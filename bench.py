@@ -716,7 +716,8 @@ def run_render_profile(args):
     from bling_gb300 import scene as S
     from bling_gb300.api import Context
     w, h, side = args.render_size
-    ctx = Context(device=0)
+    ctx = Context(device=0, bin_rays=args.bin_rays, compact_bvh=args.compact_bvh,
+                  gpu_bvh=args.gpu_bvh)
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     g = ctx.scene(S.heightfield_scene(width=w, height=h))
@@ -724,12 +725,15 @@ def run_render_profile(args):
     film = ctx.film(w, h)
     g.render_pass(film, p, 0)
     s0 = g.stats()
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(args.steps):
         g.render_pass(film, p, k + 1)
+    torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     s1 = g.stats()
     print(json.dumps({"workload": f"heightfield {w}x{h} {side * side}spp", "passes": args.steps,
+                      "bin_rays": args.bin_rays, "gpu_bvh": args.gpu_bvh,
                       "ms_per_pass": dt / args.steps * 1e3,
                       "path_samples_per_s": (s1["path_samples"] - s0["path_samples"]) / dt,
                       "rays_closest": s1["rays_closest"] - s0["rays_closest"],
@@ -976,6 +980,8 @@ def main():
     ap.add_argument("--compact-bvh", action="store_true",
                     help="32-byte quantised binary BVH nodes")
     ap.add_argument("--gpu-bvh", action="store_true", help="build the BVH on the GPU")
+    ap.add_argument("--bin-rays", action="store_true",
+                    help="path integrator: Morton-ordered bounce rays")
     ap.add_argument("--no-light", action="store_true", help="skip the light-tracer workload")
     ap.add_argument("--light-photons", type=int, default=1 << 22)
     ap.add_argument("--light-profile", action="store_true",

@@ -23,6 +23,7 @@ BLING_ERR_STATE = -6
 FLAG_WIDE_BVH = 1
 FLAG_GPU_BVH = 2
 FLAG_COMPACT_BVH = 4
+FLAG_BIN_RAYS = 8
 
 MAT_MATTE, MAT_PLASTIC, MAT_METAL, MAT_GLASS, MAT_MIRROR = 0, 1, 2, 3, 4
 MAT_SHINY_METAL, MAT_TRANS_MATTE = 5, 6

@@ -140,14 +140,17 @@ class Context:
     """A CUDA device plus one stream (``bling_ctx``)."""
 
     def __init__(self, device: int = 0, block_size: int = 0, bvh_leaf_size: int = 0,
-                 wide_bvh: bool = False, gpu_bvh: bool = False, compact_bvh: bool = False):
+                 wide_bvh: bool = False, gpu_bvh: bool = False, compact_bvh: bool = False,
+                 bin_rays: bool = False):
         """gpu_bvh: scenes build their BVH on the GPU (BLING_FLAG_GPU_BVH);
-        compact_bvh: 32-byte quantised binary nodes (BLING_FLAG_COMPACT_BVH)"""
+        compact_bvh: 32-byte quantised binary nodes (BLING_FLAG_COMPACT_BVH);
+        bin_rays: Morton-ordered bounce rays in render passes (BLING_FLAG_BIN_RAYS)"""
         L = lib()
         o = abi.Opts()
         o.device, o.block_size, o.bvh_leaf_size = device, block_size, bvh_leaf_size
         o.flags = ((abi.FLAG_WIDE_BVH if wide_bvh else 0) | (abi.FLAG_GPU_BVH if gpu_bvh else 0) |
-                   (abi.FLAG_COMPACT_BVH if compact_bvh else 0))
+                   (abi.FLAG_COMPACT_BVH if compact_bvh else 0) |
+                   (abi.FLAG_BIN_RAYS if bin_rays else 0))
         self.wide_bvh = wide_bvh
         self.gpu_bvh = gpu_bvh
         self.compact_bvh = compact_bvh

@@ -294,7 +294,8 @@ int bling_ctx_create(bling_ctx** out, const bling_opts* opts) {
     const uint32_t f = c->opts.flags;
     const int layouts = ((f & BLING_FLAG_WIDE_BVH) ? 1 : 0) + ((f & BLING_FLAG_GPU_BVH) ? 1 : 0) +
                         ((f & BLING_FLAG_COMPACT_BVH) ? 1 : 0);
-    if (layouts > 1 || (f & ~(BLING_FLAG_WIDE_BVH | BLING_FLAG_GPU_BVH | BLING_FLAG_COMPACT_BVH))) {
+    if (layouts > 1 || (f & ~(BLING_FLAG_WIDE_BVH | BLING_FLAG_GPU_BVH | BLING_FLAG_COMPACT_BVH |
+                              BLING_FLAG_BIN_RAYS))) {
       set_err(c.get(), BLING_ERR_INVALID_ARG,
               "bling_opts.flags: at most one of BLING_FLAG_WIDE_BVH, BLING_FLAG_GPU_BVH and "
               "BLING_FLAG_COMPACT_BVH, and no unknown flags");
@@ -1089,8 +1090,10 @@ int bling_render_pass_camera(bling_scene* s, bling_film* f, const bling_render_p
   auto t0 = std::chrono::steady_clock::now();
   DevShading sh = s->shading;
   if (camera) sh.camera = *camera;
+  const float box[6] = {s->lo[0], s->lo[1], s->lo[2], s->hi[0], s->hi[1], s->hi[2]};
+  const bool bin = (c->opts.flags & BLING_FLAG_BIN_RAYS) != 0;
   int rc = integrator_render_pass(c->stream, s->accel, sh, *p, pass, f->d_film, f->width,
-                                  f->height, c->ws, res, c->err);
+                                  f->height, c->ws, res, c->err, bin ? box : nullptr);
   if (rc) return rc;
   if (f->d_acc) {  // the pass's FP32 sums into the FP64 totals
     CK(c, film_fold(f, c->stream));

@@ -35,20 +35,25 @@
 
 namespace bgpu {
 
-// the pass's 16x16 filter table sits between the counters and the slots
+// the pass's 16x16 filter table and the ray-binning counters sit between
+// the counters and the slots
 constexpr size_t kFilterBytes = 256 * sizeof(float);
+constexpr int kRayBinBits = 15;  // direction octant (3 bits) x 16^3 origin cells
+constexpr int kRayBins = 1 << kRayBinBits;
+constexpr size_t kRayBinBytes = kRayBins * sizeof(unsigned);
 
-// lays counters, the filter table, slots and queues out in one buffer of
-// slotBytes(cap) bytes
+// lays counters, the filter table, the bin counters, slots and queues out in
+// one buffer of slotBytes(cap) bytes
 static size_t slotBytes(size_t cap) {
-  return kCounterBytes + kFilterBytes + (kSlotWords + kQueueWords) * 4 * cap;
+  return kCounterBytes + kFilterBytes + kRayBinBytes + (kSlotWords + kQueueWords) * 4 * cap;
 }
 
 static void carve(unsigned char* base, size_t cap, Slots& st, Queues& q,
-                  unsigned long long*& counters, float*& filter) {
+                  unsigned long long*& counters, float*& filter, unsigned*& bins) {
   counters = (unsigned long long*)base;
   filter = (float*)(base + kCounterBytes);
-  float* w = (float*)(base + kCounterBytes + kFilterBytes);
+  bins = (unsigned*)(base + kCounterBytes + kFilterBytes);
+  float* w = (float*)(base + kCounterBytes + kFilterBytes + kRayBinBytes);
   carveSlots(w, cap, st);
   int32_t* qw = (int32_t*)w;
   q.live[0] = qw;
@@ -129,6 +134,99 @@ __global__ void __launch_bounds__(128) k_class_scatter(const int32_t* __restrict
   }
 }
 
+// ---- ray binning (BLING_FLAG_BIN_RAYS): a bounce's live queue in the order
+// of (direction octant, Morton code of the origin's cell in a 16^3 grid over
+// the scene's bounds), so that the rays of a warp start near one another and
+// head the same way and share the BVH nodes they fetch.  A counting sort: one
+// counting pass (keys kept in the queue's class array, which is free until
+// the shading sort), a scan and a scatter.  Order within a bin is arbitrary;
+// it only changes which warp traces a ray.
+struct BinFrame {
+  float lo[3], scale[3];  // cell = (o - lo) * scale, clamped to [0, 15]
+};
+
+__device__ __forceinline__ uint32_t spread4(uint32_t v) {  // 4 bits -> every third bit
+  return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4) | ((v & 8u) << 6);
+}
+
+__device__ __forceinline__ uint32_t rayBinKey(const Ray& r, const BinFrame& F) {
+  const float o[3] = {r.o.x, r.o.y, r.o.z}, d[3] = {r.d.x, r.d.y, r.d.z};
+  uint32_t cell = 0, oct = 0;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    float u = (o[a] - F.lo[a]) * F.scale[a];
+    u = fminf(fmaxf(u, 0.0f), 15.0f);  // NaN -> 0
+    cell |= spread4((uint32_t)u) << a;
+    oct |= (signbit(d[a]) ? 1u : 0u) << a;
+  }
+  return (oct << 12) | cell;
+}
+
+__global__ void __launch_bounds__(128) k_raybin_count(Slots st, const int32_t* __restrict__ queue,
+                                                      const unsigned long long* __restrict__ qcount,
+                                                      BinFrame F, int32_t* __restrict__ keys,
+                                                      unsigned* __restrict__ bins) {
+  const int64_t n = (int64_t)*qcount;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nround = (n + stride - 1) / stride * stride;
+  const int lane = threadIdx.x & 31;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
+    uint32_t key = 0xffffffffu;
+    if (q < n) {
+      key = rayBinKey(loadRay7(st.ray, queue[q]), F);
+      keys[q] = (int32_t)key;
+    }
+    unsigned grp = __match_any_sync(0xffffffffu, key);  // one atomic per distinct key
+    if (key != 0xffffffffu && lane == __ffs(grp) - 1) atomicAdd(bins + key, (unsigned)__popc(grp));
+  }
+}
+
+// exclusive scan of the kRayBins counters in place (one block of 1024)
+__global__ void __launch_bounds__(1024) k_raybin_scan(unsigned* __restrict__ bins) {
+  __shared__ unsigned part[1024];
+  constexpr int per = kRayBins / 1024;
+  const int t = threadIdx.x;
+  unsigned sum = 0;
+  for (int k = 0; k < per; k++) sum += bins[t * per + k];
+  part[t] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    unsigned v = t >= off ? part[t - off] : 0u;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  unsigned run = part[t] - sum;
+  for (int k = 0; k < per; k++) {
+    unsigned v = bins[t * per + k];
+    bins[t * per + k] = run;
+    run += v;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_raybin_scatter(const int32_t* __restrict__ queue,
+                                                        const unsigned long long* __restrict__ qcount,
+                                                        const int32_t* __restrict__ keys,
+                                                        unsigned* __restrict__ bins,
+                                                        int32_t* __restrict__ out) {
+  const int64_t n = (int64_t)*qcount;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t nround = (n + stride - 1) / stride * stride;
+  const int lane = threadIdx.x & 31;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
+    uint32_t key = q < n ? (uint32_t)keys[q] : 0xffffffffu;
+    unsigned grp = __match_any_sync(0xffffffffu, key);
+    int leader = __ffs(grp) - 1;
+    unsigned base = 0;
+    if (key != 0xffffffffu && lane == leader) base = atomicAdd(bins + key, (unsigned)__popc(grp));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (key != 0xffffffffu) {
+      unsigned pos = base + __popc(grp & ((1u << lane) - 1u));
+      if ((int64_t)pos < n) out[pos] = queue[q];  // always, for consistent counts
+    }
+  }
+}
+
 // closest hit of the live paths' rays (scIntersect)
 template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
@@ -176,11 +274,12 @@ __global__ void __launch_bounds__(128, 10) k_trace_mis(DevAccel A, Slots st,
 
 // one vertex of every live path, up to its shadow and MIS rays (Path.hs:49-87)
 __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, PassParams P, Slots st,
-                                               Queues Q, int depth, int live_in,
+                                               Queues Q, const int32_t* __restrict__ qin,
+                                               int depth, int live_in,
                                                float* __restrict__ film, const float* filter,
                                                unsigned long long* __restrict__ counters) {
+  // qin: the live paths in shading-class order
   int64_t n = (int64_t)counters[live_in];
-  const int32_t* __restrict__ qin = Q.sorted;  // the live paths in shading-class order
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;  // whole warps stay together for the appends
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
@@ -272,7 +371,8 @@ Grids grids(int device, int sms) {
 // the bounces of one chunk of path samples
 cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S, PassParams P,
                      Slots st, Queues Q, unsigned long long* counters, int64_t count, int max_depth,
-                     float* d_film, const float* d_filter, const Grids& G) {
+                     float* d_film, const float* d_filter, const Grids& G, unsigned* d_bins,
+                     const BinFrame* bin) {
   const int block = 128;
   unsigned g_ray = (unsigned)std::min<int64_t>((count + block - 1) / block, (int64_t)G.raygen);
   k_raygen<<<g_ray, block, 0, stream>>>(P, S.camera, st, count, Q.live[0], counters);
@@ -284,15 +384,26 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
     k_bounce_reset<<<1, 32, 0, stream>>>(counters, C_LIVE0 + (1 - in));
     unsigned gt = std::min(G.trace, cap_blocks), gs = std::min(G.shadow, cap_blocks),
              gm = std::min(G.mis, cap_blocks);
+    // the bounce's queue: binned into Q.sorted (bounces after the camera's,
+    // whose rays are in pixel order already), then shading-class sorted into
+    // whichever of the two queues is free
+    const unsigned long long* qn = counters + C_LIVE0 + in;
+    int32_t* traced = Q.live[in];
+    int32_t* shaded = Q.sorted;
+    if (bin && depth > 0) {
+      cudaMemsetAsync(d_bins, 0, kRayBinBytes, stream);
+      k_raybin_count<<<G.raygen, block, 0, stream>>>(st, Q.live[in], qn, *bin, Q.cls, d_bins);
+      k_raybin_scan<<<1, 1024, 0, stream>>>(d_bins);
+      k_raybin_scatter<<<G.raygen, block, 0, stream>>>(Q.live[in], qn, Q.cls, d_bins, Q.sorted);
+      traced = Q.sorted;
+      shaded = Q.live[in];
+    }
     withLayout(A.wide, [&](auto L) {
-      k_trace<decltype(L)::value><<<gt, block, 0, stream>>>(A, st, Q.live[in],
-                                                           counters + C_LIVE0 + in, counters);
+      k_trace<decltype(L)::value><<<gt, block, 0, stream>>>(A, st, traced, qn, counters);
     });
-    k_class_count<<<G.raygen, block, 0, stream>>>(A, S, st, Q.live[in], counters + C_LIVE0 + in,
-                                                   Q.cls, counters);
-    k_class_scatter<<<G.raygen, block, 0, stream>>>(Q.live[in], counters + C_LIVE0 + in, Q.cls,
-                                                     Q.sorted, counters);
-    k_shade<<<std::min(G.shade, cap_blocks), block, 0, stream>>>(A, S, P, st, Q, depth,
+    k_class_count<<<G.raygen, block, 0, stream>>>(A, S, st, traced, qn, Q.cls, counters);
+    k_class_scatter<<<G.raygen, block, 0, stream>>>(traced, qn, Q.cls, shaded, counters);
+    k_shade<<<std::min(G.shade, cap_blocks), block, 0, stream>>>(A, S, P, st, Q, shaded, depth,
                                                                   C_LIVE0 + in, d_film, d_filter,
                                                                   counters);
     withLayout(A.wide, [&](auto L) {
@@ -396,7 +507,8 @@ static int ensureWorkspace(IntegratorWorkspace& ws, size_t cap, std::string& err
 
 int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S,
                            const bling_render_params& p, uint64_t pass, float* d_film, int fw,
-                           int fh, IntegratorWorkspace& ws, PassResult& res, std::string& err) {
+                           int fh, IntegratorWorkspace& ws, PassResult& res, std::string& err,
+                           const float* bin_box) {
   int device = 0;
   RET_CUDA(cudaGetDevice(&device));
   RET_CUDA(loadCieConstants(device));
@@ -418,7 +530,15 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
   Queues Q;
   unsigned long long* counters;
   float* d_filter;
-  carve((unsigned char*)ws.buffer, ws.capacity, st, Q, counters, d_filter);
+  unsigned* d_bins;
+  carve((unsigned char*)ws.buffer, ws.capacity, st, Q, counters, d_filter, d_bins);
+  BinFrame frame;
+  if (bin_box)
+    for (int a = 0; a < 3; a++) {
+      float ext = bin_box[3 + a] - bin_box[a];
+      frame.lo[a] = bin_box[a];
+      frame.scale[a] = ext > 0 ? 16.0f / ext : 0.0f;
+    }
   float tbl[256];
   filterTableHost(p.filter_kind, p.filter_params, P.fw, P.fh, tbl);
   RET_CUDA(cudaMemcpyAsync(d_filter, tbl, sizeof tbl, cudaMemcpyHostToDevice, stream));
@@ -429,7 +549,8 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
   for (uint64_t base = 0; base < total; base += ws.capacity) {
     int64_t count = (int64_t)std::min<uint64_t>(ws.capacity, total - base);
     P.chunk_base = base;
-    RET_CUDA(runChunk(stream, A, S, P, st, Q, counters, count, p.max_depth, d_film, d_filter, G));
+    RET_CUDA(runChunk(stream, A, S, P, st, Q, counters, count, p.max_depth, d_film, d_filter, G,
+                      d_bins, bin_box ? &frame : nullptr));
   }
   unsigned long long cnt[C_COUNT];
   RET_CUDA(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, stream));
@@ -453,7 +574,7 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
 // device) race on it.
 constexpr size_t kNoAllocSlots = size_t(1) << 16;
 constexpr size_t kNoAllocBytes =
-    kCounterBytes + kFilterBytes + (kSlotWords + kQueueWords) * 4 * kNoAllocSlots;
+    kCounterBytes + kFilterBytes + kRayBinBytes + (kSlotWords + kQueueWords) * 4 * kNoAllocSlots;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
@@ -526,7 +647,8 @@ int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const
   Queues Q;
   unsigned long long* counters;
   float* d_filter;
-  carve(scratch, kNoAllocSlots, st, Q, counters, d_filter);
+  unsigned* d_bins;
+  carve(scratch, kNoAllocSlots, st, Q, counters, d_filter, d_bins);
   float tbl[256];
   filterTableHost(p.filter_kind, p.filter_params, P.fw, P.fh, tbl);
   RET_CUDA(cudaMemcpyAsync(d_filter, tbl, sizeof tbl, cudaMemcpyHostToDevice, stream));
@@ -536,7 +658,7 @@ int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const
   Grids G = grids(device, sms);
   P.chunk_base = 0;
   RET_CUDA(runChunk(stream, A, S, P, st, Q, counters, (int64_t)total, p.max_depth, d_film, d_filter,
-                    G));
+                    G, d_bins, nullptr));
   unsigned long long cnt[C_COUNT];
   RET_CUDA(cudaMemcpyAsync(cnt, counters, sizeof cnt, cudaMemcpyDeviceToHost, stream));
   RET_CUDA(cudaStreamSynchronize(stream));

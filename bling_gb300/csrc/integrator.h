@@ -125,9 +125,12 @@ int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
                             const std::vector<int32_t>& shape_light, std::vector<void*>& owned,
                             DevShading& out, std::string& err);
 
+// bin_box (6 floats: the scene's world bounds lo.xyz, hi.xyz) turns on ray
+// binning of the bounces after the camera's (BLING_FLAG_BIN_RAYS); null: off
 int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S,
                            const bling_render_params& p, uint64_t pass, float* d_film, int fw,
-                           int fh, IntegratorWorkspace& ws, PassResult& res, std::string& err);
+                           int fh, IntegratorWorkspace& ws, PassResult& res, std::string& err,
+                           const float* bin_box = nullptr);
 
 void integrator_workspace_free(IntegratorWorkspace& ws);
 

@@ -56,6 +56,9 @@ typedef struct bling_film bling_film;
 #define BLING_FLAG_WIDE_BVH 1u /* 8-wide quantised BVH layout instead of the binary one */
 #define BLING_FLAG_COMPACT_BVH 4u /* binary BVH in 32-byte quantised nodes (one 256-bit
                                      load per visit) instead of 64-byte float nodes */
+#define BLING_FLAG_BIN_RAYS 8u /* path integrator: sort each bounce's rays after the
+                                  camera's by direction octant and origin cell
+                                  (Morton order) before tracing them */
 #define BLING_FLAG_GPU_BVH 2u  /* build the BVH on the GPU (Morton order and PLOC
                                   clustering, binary layout, one primitive per
                                   leaf) instead of the host's binned SAH; not with
