@@ -29,7 +29,7 @@ MAT_MATTE, MAT_PLASTIC, MAT_METAL, MAT_GLASS, MAT_MIRROR = 0, 1, 2, 3, 4
 MAT_SHINY_METAL, MAT_TRANS_MATTE = 5, 6
 MAT_SUBSTRATE, MAT_BLACKBODY = 7, 8  # substrate: ka in kt, urough in roughness, vrough in sigma, depth in ior
 SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_DISK, SHAPE_CYLINDER = 0, 1, 2, 3, 4
-LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE = 0, 1, 2
+LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE, LIGHT_SUNSKY = 0, 1, 2, 3
 FILTER_BOX, FILTER_GAUSS, FILTER_MITCHELL, FILTER_SINC, FILTER_TRIANGLE = 0, 1, 2, 3, 4
 SAMPLER_STRATIFIED, SAMPLER_RANDOM = 0, 1
 ABI_VERSION = 4  # BLING_ABI_VERSION of include/bling_gpu.h
@@ -65,7 +65,7 @@ class ShapeDesc(C.Structure):
 class LightDesc(C.Structure):
     _fields_ = [("kind", C.c_int32), ("spectrum", F16), ("vec", C.c_float * 3),
                 ("env", C.POINTER(C.c_float)), ("env_w", C.c_int32), ("env_h", C.c_int32),
-                ("w2l", M16), ("l2w", M16)]
+                ("w2l", M16), ("l2w", M16), ("east", C.c_float * 3), ("turbidity", C.c_float)]
 
 
 class CameraDesc(C.Structure):

@@ -101,6 +101,8 @@ def lib():
         getattr(L, fn).restype = C.c_int
     L.bling_rgb_to_spectrum.argtypes = [C.c_int32, C.c_float, C.c_float, C.c_float, P(C.c_float)]
     L.bling_spectrum_to_xyz.argtypes = [P(C.c_float), P(C.c_float)]
+    L.bling_sunsky_eval.argtypes = [P(C.c_float), P(C.c_float), C.c_float, C.c_float, C.c_float,
+                                    P(C.c_float)]
     L.bling_batch_create.argtypes = [vp, P(abi.BatchOpts), P(vp)]
     L.bling_batch_destroy.argtypes = [vp]
     L.bling_batch_submit.argtypes = [vp, vp, vp, P(abi.RenderParams), P(abi.CameraDesc), C.c_uint64,

@@ -18,7 +18,8 @@ The subset is what the GPU path renders:
 * primitives: ``mesh`` and ``shape`` (box, cylinder, disk, quad, sphere);
 * materials: matte, plastic, metal, glass, mirror, shinyMetal, transMatte,
   with ``constant`` textures;
-* lights: directional, point, and infinite with a ``constant`` map;
+* lights: directional, point, and infinite with a ``constant`` or ``sunSky``
+  map;
 * spectra: ``rgbR``/``rgbI`` (decimal or ``%rrggbb``), ``spd { l v, ... }``,
   ``temp``;
 * the sampler renderer (``stratified``/``random``) with the ``path``
@@ -648,6 +649,9 @@ class _Parser:
                 w2l = self.p_transform()
                 t.expect("l")
                 env = t.block(self._env_map)
+                if isinstance(env, dict):  # mkSunSkyLight east sunDir turbidity
+                    return Light(abi.LIGHT_SUNSKY, vec=env["sunDir"], east=env["east"],
+                                 turbidity=env["turbidity"], w2l=w2l)
                 return Light(abi.LIGHT_INFINITE, env=env, w2l=w2l)
             raise t.error(f"unknown light type {kind}")
         self.s.lights.insert(0, t.block(body))
@@ -657,7 +661,11 @@ class _Parser:
         kind = t.word()
         if kind == "constant":  # constSpectrumMap2d: a 1 x 1 map (Texture.hs:131-132)
             return self.p_spectrum().reshape(1, 1, BANDS)
-        if kind in ("file", "sunSky", "rgbeFile"):
+        if kind == "sunSky":  # MaterialParser.hs:266-270
+            east = tuple(float(x) for x in t.named_vec("east"))
+            sun = tuple(float(x) for x in t.named_vec("sunDir"))
+            return {"east": east, "sunDir": sun, "turbidity": float(t.named_flt("turbidity"))}
+        if kind in ("file", "rgbeFile"):
             raise Unsupported(f"environment map {kind}: the GPU path takes constant maps from "
                               ".bling files (image maps through bling_light_desc.env)")
         raise t.error(f"unknown map type {kind}")

@@ -374,6 +374,10 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
     return set_err(c, BLING_ERR_INVALID_ARG, "negative counts");
   if (d->n_materials > 0 && !d->materials)
     return set_err(c, BLING_ERR_INVALID_ARG, "null material array");
+  if (d->n_lights > 0 && !d->lights) return set_err(c, BLING_ERR_INVALID_ARG, "null light array");
+  for (int i = 0; i < d->n_lights; i++)
+    if (d->lights[i].kind < BLING_LIGHT_DIRECTIONAL || d->lights[i].kind > BLING_LIGHT_SUNSKY)
+      return set_err(c, BLING_ERR_INVALID_ARG, "light %d: unknown kind %d", i, d->lights[i].kind);
   for (int i = 0; i < d->n_materials; i++)
     if (d->materials[i].kind < BLING_MAT_MATTE || d->materials[i].kind > BLING_MAT_BLACKBODY ||
         (d->materials[i].kd_texture != BLING_TEX_CONSTANT &&
@@ -1259,6 +1263,12 @@ int bling_bvh_selftest(const float* lo, const float* hi, int64_t n, int32_t max_
   stats[3] = bo.wide_depth;
   stats[4] = bo.leaves;
   return validate_bvh(bi, bo);
+}
+void bling_sunsky_eval(const float east[3], const float sun_dir[3], float turbidity, float u,
+                       float v, float out[BLING_BANDS]) {
+  SkyModel m;
+  skyInit(east, sun_dir, turbidity, m);
+  skyEval(m, u, v, out);
 }
 void bling_rgb_to_spectrum(int32_t illum, float r, float g, float b, float out[BLING_BANDS]) {
   const uint32_t* t = illum ? BLING_RGB_ILLUM_BITS : BLING_RGB_REFL_BITS;

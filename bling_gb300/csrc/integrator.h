@@ -7,6 +7,7 @@
 
 #include "../../include/bling_gpu.h"
 #include "internal.h"
+#include "sunsky.h"
 
 namespace bgpu {
 
@@ -93,6 +94,9 @@ struct DLight {
   const float* marg_cdf;   // env_h + 1
   float marg_int;
   float pad;
+  // sun/sky (BLING_LIGHT_SUNSKY): the map is this model, evaluated at
+  // continuous (u, v); env is null and env_w x env_h only size the Dist2D
+  const SkyModel* sky;
 };
 
 struct DevShading {

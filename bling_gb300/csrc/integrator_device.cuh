@@ -1095,6 +1095,16 @@ __device__ __forceinline__ const float* envTexel(const DLight& l, float u, float
   y = max(0, min(l.env_h - 1, y));
   return l.env + 16 * ((size_t)y * l.env_w + x);
 }
+// texMapEval of an infinite light's map at (u, v): the texel of an image
+// map (getPixel, Texture.hs:96-101), or the sun/sky model at (u, v)
+static __device__ BLING_OUTLINE Spec envEval(const DLight& l, float u, float v) {
+  if (l.sky) {
+    Spec s;
+    skyEval(*l.sky, u, v, s.v);
+    return s;
+  }
+  return sLoad(envTexel(l, u, v));
+}
 // upperBound + sampleContinuous1D (Montecarlo.hs:53-73); findIndex (>= u)
 // on a non-decreasing CDF is its lower bound
 static __device__ void sampleContinuous1D(const float* func, const float* cdf, int n, float fi, float u,
@@ -1172,7 +1182,7 @@ static __device__ BLING_OUTLINE LightSample lightSample(const DevAccel& A, const
   float phi = u * 2.0f * kPi, theta = v * kPi;
   float sint = sinf(theta);
   if (sint == 0) return ls;
-  ls.li = sLoad(envTexel(l, u, v));
+  ls.li = envEval(l, u, v);
   V3 dl{sinf(theta) * cosf(phi), sinf(theta) * sinf(phi), cosf(theta)};
   ls.wi = transVector(l.l2w, dl);
   ls.ray = Ray{p, ls.wi, eps, INFINITY};
@@ -1184,7 +1194,7 @@ static __device__ BLING_OUTLINE Spec lightLe(const DLight& l, V3 d) {
   if (l.kind != DLIGHT_INFINITE) return sConst(0);
   V3 wh = normalize(transVector(l.w2l, d));
   float phi = sphericalPhi(wh), theta = sphericalTheta(wh);
-  return sLoad(envTexel(l, phi / (2.0f * kPi), theta / kPi));
+  return envEval(l, phi / (2.0f * kPi), theta / kPi);
 }
 // pdf (Light.hs:215-229)
 static __device__ BLING_OUTLINE float lightPdf(const DevAccel& A, const DLight& l, V3 p, V3 wi) {

@@ -61,7 +61,7 @@ static __device__ void lightEmit(const DevAccel& A, const DevShading& S, const D
     pd = 0;
     return;
   }
-  r = sLoad(envTexel(l, u, v));
+  r = envEval(l, u, v);
   float phi = u * 2.0f * kPi, theta = v * kPi;  // cartToSph
   V3 dl{sinf(theta) * cosf(phi), sinf(theta) * sinf(phi), cosf(theta)};
   V3 d = transVector(l.l2w, dl);

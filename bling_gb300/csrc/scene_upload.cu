@@ -135,26 +135,41 @@ int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
     memcpy(o.vec, l.vec, 12);
     memcpy(o.w2l, l.w2l, 64);
     memcpy(o.l2w, l.l2w, 64);
-    if (l.kind == BLING_LIGHT_INFINITE) {
-      int w = l.env_w, h = l.env_h;
-      if (w <= 0 || h <= 0 || !l.env) {
+    if (l.kind == BLING_LIGHT_INFINITE || l.kind == BLING_LIGHT_SUNSKY) {
+      const bool sky = l.kind == BLING_LIGHT_SUNSKY;
+      int w = sky ? kSkyMapW : l.env_w, h = sky ? kSkyMapH : l.env_h;
+      if (!sky && (w <= 0 || h <= 0 || !l.env)) {
         err = "infinite light without an environment map";
         return BLING_ERR_INVALID_ARG;
       }
+      o.kind = BLING_LIGHT_INFINITE;  // one kind on the device; `sky` tells the maps apart
       o.env_w = w;
       o.env_h = h;
       void* p;
-      if ((rc = up(l.env, (size_t)w * h * 64, &p))) return rc;
-      o.env = (const float*)p;
-      // mkInfiniteAreaLight's Dist2D over sY of each texel (Light.hs:76-82,
-      // Montecarlo.hs:79-88)
+      SkyModel model;
+      if (sky) {  // mkSunSkyLight east sunDir turbidity (SunSky.hs:12-24)
+        skyInit(l.east, l.vec, l.turbidity, model);
+        if ((rc = up(&model, sizeof model, &p))) return rc;
+        o.sky = (const SkyModel*)p;
+      } else {
+        if ((rc = up(l.env, (size_t)w * h * 64, &p))) return rc;
+        o.env = (const float*)p;
+      }
+      // mkInfiniteAreaLight's Dist2D over sY of the map at each raster
+      // position (x / w, y / h) (Light.hs:72-82, Montecarlo.hs:79-88)
       std::vector<float> func((size_t)w * h), cdf((size_t)h * (w + 1)), cint(h), mcdf(h + 1);
       for (int v = 0; v < h; v++) {
         for (int u = 0; u < w; u++) {
           float uu = (float)u / (float)w, vv = (float)v / (float)h;
-          int x = std::max(0, std::min(w - 1, (int)floorf(uu * (float)w)));
-          int y = std::max(0, std::min(h - 1, (int)floorf(vv * (float)h)));
-          func[(size_t)v * w + u] = sYHost(l.env + 16 * ((size_t)y * w + x));
+          if (sky) {
+            float texel[16];
+            skyEval(model, uu, vv, texel);
+            func[(size_t)v * w + u] = sYHost(texel);
+          } else {
+            int x = std::max(0, std::min(w - 1, (int)floorf(uu * (float)w)));
+            int y = std::max(0, std::min(h - 1, (int)floorf(vv * (float)h)));
+            func[(size_t)v * w + u] = sYHost(l.env + 16 * ((size_t)y * w + x));
+          }
         }
         mkDist1D(&func[(size_t)v * w], w, &cdf[(size_t)v * (w + 1)], cint[v]);
       }

@@ -117,6 +117,51 @@ def hexf(x: np.float32) -> str:
     return f"__bling_f32(0x{bits:08x}u) /* {float(x)!r} */"
 
 
+def eval_regular_spd(l0, l1, amps, l):
+    """``evalSpd (RegularSpd l0 l1 amps) l`` (Spectrum.hs:271-280)."""
+    n = len(amps)
+    if l <= l0:
+        return amps[0]
+    if l >= l1:
+        return amps[-1]
+    d1 = F(1) / ((l1 - l0) / F(n - 1))
+    x = (l - l0) * d1
+    b0 = int(np.floor(x))
+    b1 = min(b0 + 1, n - 1)
+    dx = x - F(b0)
+    return (F(1) - dx) * amps[b0] + dx * amps[b1]
+
+
+def spd_to_xyz(spd, cie):
+    """``spdToXYZ`` (Spectrum.hs:318-326): sums over 360..830 nm in steps of
+    1 nm, each a left fold from 0, divided by the sum of y-bar"""
+    lam = [F(l) for l in range(360, 831)]
+    vs = [eval_regular_spd(*spd, l) for l in lam]
+    xs = [eval_regular_spd(F(360), F(830), cie["X"], l) for l in lam]
+    ys = [eval_regular_spd(F(360), F(830), cie["Y"], l) for l in lam]
+    zs = [eval_regular_spd(F(360), F(830), cie["Z"], l) for l in lam]
+    yint = F(0)
+    for v in ys:
+        yint = yint + v
+    acc = []
+    for cmf in (xs, ys, zs):
+        a = F(0)
+        for c, v in zip(cmf, vs):
+            a = a + c * v
+        acc.append(a / yint)
+    return acc
+
+
+def parse_spd(src: str, name: str):
+    """``name = mkSpd' l0 l1 [ ... ]``: (l0, l1, amplitudes)"""
+    m = re.search(r"^" + name + r"\s*=\s*mkSpd'\s+(\S+)\s+(\S+)\s*\[(.*?)\]", src, re.S | re.M)
+    if not m:
+        raise SystemExit(f"SPD {name} not found")
+    body = re.sub(r"--[^\n]*", "", m.group(3))
+    toks = [t.strip() for t in body.replace("\n", " ").split(",") if t.strip()]
+    return f32_of_decimal(m.group(1)), f32_of_decimal(m.group(2)), [f32_of_decimal(t) for t in toks]
+
+
 def main(argv):
     if len(argv) < 2:
         raise SystemExit("usage: gen_spectrum_tables.py <bling's src/lib/Graphics/Bling/Spectrum.hs>"
@@ -137,6 +182,12 @@ def main(argv):
     ysum = F(0)
     for v in tables["cieY"]:
         ysum = ysum + v
+    # the CIE daylight basis S0, S1, S2 as XYZ (s0XYZ/s1XYZ/s2XYZ,
+    # Spectrum.hs:234-241), for chromaticityToXYZ (Spectrum.hs:243-251)
+    cie = {axis: parse_list(src, f"cie{axis}Values") for axis in "XYZ"}
+    s012 = []
+    for name in ("cieS0", "cieS1", "cieS2"):
+        s012 += spd_to_xyz(parse_spd(src, name), cie)
 
     lines = [
         "/* Generated by bling_gb300/gen_spectrum_tables.py from bling's Spectrum.hs.",
@@ -178,6 +229,8 @@ def main(argv):
     illum = [tables[n] for n in BASIS_NAMES[7:]]
     emit("BLING_RGB_REFL_BITS", [v for t in refl for v in t])
     emit("BLING_RGB_ILLUM_BITS", [v for t in illum for v in t])
+    lines.append("/* X, Y, Z of the CIE daylight components S0, S1, S2 (spdToXYZ) */")
+    emit("BLING_CIE_S012_XYZ_BITS", s012)
     lines.append("")
     out_path.write_text("\n".join(lines) + "\n")
     print(f"wrote {out_path}")

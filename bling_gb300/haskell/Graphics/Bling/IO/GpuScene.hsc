@@ -100,15 +100,19 @@ data FlatShape = FlatShape
 -- | a primitive, in primitive-list order
 data FlatPrim = PrimMesh !FlatMesh | PrimShape !FlatShape deriving (Show, Eq)
 
--- | @bling_light_desc@: directional, point or infinite (with its lat-long
---   map of @envW * envH * 16@ floats and world-to-light transform pair)
+-- | @bling_light_desc@: directional, point, infinite (with its lat-long
+--   map of @envW * envH * 16@ floats and world-to-light transform pair) or
+--   sun/sky (@mkSunSkyLight east sunDir turbidity@: sun direction in
+--   'flVec', 'flEast', 'flTurbidity')
 data FlatLight = FlatLight
-   { flKind     :: !Int32
-   , flSpectrum :: ![Float]
-   , flVec      :: ![Float]
-   , flEnv      :: !(Maybe (Int32, Int32, SV.Vector Float))
-   , flW2L      :: ![Float]
-   , flL2W      :: ![Float]
+   { flKind      :: !Int32
+   , flSpectrum  :: ![Float]
+   , flVec       :: ![Float]
+   , flEnv       :: !(Maybe (Int32, Int32, SV.Vector Float))
+   , flW2L       :: ![Float]
+   , flL2W       :: ![Float]
+   , flEast      :: ![Float]
+   , flTurbidity :: !Float
    } deriving (Show, Eq)
 
 -- | @bling_camera_desc@: the matrices of 'ProjectiveCamera' (Camera.hs:24-31)
@@ -315,6 +319,8 @@ pokeLight p (l, pe) = do
    #{poke bling_light_desc, env_h} p (maybe 0 (\(_, h, _) -> h) (flEnv l))
    pokeFloats (#{ptr bling_light_desc, w2l} p) 16 (flW2L l)
    pokeFloats (#{ptr bling_light_desc, l2w} p) 16 (flL2W l)
+   pokeFloats (#{ptr bling_light_desc, east} p) 3 (flEast l)
+   #{poke bling_light_desc, turbidity} p (CFloat $ flTurbidity l)
 
 -- | Lays the flat scene out as a @bling_scene_desc@ for the duration of the
 --   callback (for @bling_scene_create@, which copies everything it needs).

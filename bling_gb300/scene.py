@@ -52,9 +52,11 @@ class Shape:
 class Light:
     kind: int
     spectrum: np.ndarray = field(default_factory=lambda: constant(0))
-    vec: tuple = (0.0, 0.0, 0.0)
+    vec: tuple = (0.0, 0.0, 0.0)    # sun/sky: the sun's direction
     env: np.ndarray | None = None  # (h, w, 16) float32
     w2l: xf.Transform | None = None
+    east: tuple = (0.0, 0.0, 0.0)   # sun/sky: the east direction
+    turbidity: float = 0.0          # sun/sky
 
 
 @dataclass
@@ -170,6 +172,8 @@ class Scene:
             w2l = l.w2l or xf.identity()
             d.w2l[:] = w2l.m.tolist()
             d.l2w[:] = w2l.inv.tolist()
+            d.east[:] = [float(x) for x in l.east]
+            d.turbidity = float(l.turbidity)
         order = None
         if self.prim_order is not None:
             order = np.asarray(self.prim_order, dtype=np.int32)

@@ -153,17 +153,23 @@ typedef struct bling_shape_desc {
 enum {
   BLING_LIGHT_DIRECTIONAL = 0, /* mkDirectional spectrum dir */
   BLING_LIGHT_POINT = 1,       /* mkPointLight spectrum pos */
-  BLING_LIGHT_INFINITE = 2     /* mkInfiniteAreaLight map w2l */
+  BLING_LIGHT_INFINITE = 2,    /* mkInfiniteAreaLight map w2l */
+  BLING_LIGHT_SUNSKY = 3       /* mkInfiniteAreaLight (mkSunSkyLight east sunDir turbidity) w2l
+                                  (SunSky.hs:12-24): Perez's sky and the solar disc, evaluated
+                                  at continuous directions; vec = sunDir */
 };
 
 typedef struct bling_light_desc {
   int32_t kind;
   float spectrum[BLING_BANDS]; /* directional/point radiance/intensity */
-  float vec[3];                /* directional: normalised direction; point: position */
+  float vec[3];                /* directional: normalised direction; point: position;
+                                  sun/sky: the sun's direction */
   const float* env;            /* infinite: env_w * env_h * 16 floats, row v, column u */
   int32_t env_w, env_h;
-  float w2l[16];               /* infinite: world-to-light */
-  float l2w[16];               /* infinite: light-to-world */
+  float w2l[16];               /* infinite, sun/sky: world-to-light */
+  float l2w[16];               /* infinite, sun/sky: light-to-world */
+  float east[3];               /* sun/sky: the east direction */
+  float turbidity;             /* sun/sky: the sky's turbidity */
 } bling_light_desc;
 
 /* A projective camera (ProjectiveCamera, Camera.hs:23-31; mkProjective,
@@ -538,6 +544,12 @@ int bling_server_debug_fail_step(bling_server* server, int32_t after_steps);
  * testable unit. */
 int bling_bvh_selftest(const float* lo, const float* hi, int64_t n, int32_t max_leaf,
                        int64_t* stats);
+/* The sun/sky map of mkSunSkyLight east sunDir turbidity at (u, v)
+ * (SunSky.hs:12-24), computed on the host.  BLING_LIGHT_SUNSKY lights
+ * evaluate the same expression on the device, where sinf/cosf/acosf/expf/
+ * powf may round differently in the last bit. */
+void bling_sunsky_eval(const float east[3], const float sun_dir[3], float turbidity, float u,
+                       float v, float out[BLING_BANDS]);
 /* rgbToSpectrumRefl / rgbToSpectrumIllum (Spectrum.hs:140-159) */
 void bling_rgb_to_spectrum(int32_t illuminant, float r, float g, float b, float out[BLING_BANDS]);
 /* spectrumToXYZ (Spectrum.hs:349-355) */

@@ -572,6 +572,189 @@ struct Prim {
   V p1, p2, p3;
 };
 
+// ------------------------------------------------------------ sun and sky
+// mkSunSkyLight (SunSky.hs:12-158): the Perez sky plus a solar disc as a
+// continuous lat-long map.
+struct SkyData {  // SunSky.hs:28-37, plus the disc direction and spectrum
+  V sunDir;       // normalize (worldToLocal basis (normalize sunDir))
+  V discDir;      // normalize (worldToLocal basis sunDir)
+  float sunTheta;
+  float perezx[5], perezy[5], perezY[5];
+  float zenithx, zenithy, zenithY;
+  Spec sunR;
+};
+
+// sunThetaMax2 (SunSky.hs:39-43)
+static float sunThetaMax2() {
+  float sint2 = 6.955e5f / 1.496e8f;
+  return sqrtf(hmax(0.0f, 1.0f - sint2));
+}
+
+// evalSpd of an IrregularSpd (Spectrum.hs:258-269)
+static float spdIrregular(const float* ls, const float* vs, int n, float l) {
+  if (l <= ls[0]) return vs[0];
+  if (l >= ls[n - 1]) return vs[n - 1];
+  int lo = 0, hi = n - 1, i;
+  for (;;) {  // fi lo hi
+    int mid = (lo + hi) / 2;
+    if (lo == mid) {
+      i = lo;
+      break;
+    }
+    if (ls[mid] == l) {
+      i = mid;
+      break;
+    }
+    if (ls[mid] < l)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  float t = (l - ls[i]) / (ls[i + 1] - ls[i]);
+  return lerp(t, vs[i], vs[i + 1]);
+}
+// evalSpd of a RegularSpd (Spectrum.hs:271-280)
+static float spdRegular(float l0, float l1, const float* amps, int n, float l) {
+  if (l <= l0) return amps[0];
+  if (l >= l1) return amps[n - 1];
+  float d1 = 1.0f / ((l1 - l0) / (float)(n - 1));
+  float x = (l - l0) * d1;
+  int b0 = (int)std::floor(x);
+  int b1 = std::min(b0 + 1, n - 1);
+  float dx = x - (float)b0;
+  return (1.0f - dx) * amps[b0] + dx * amps[b1];
+}
+
+// solCurve, koCurve, kgCurve, kwaCurve (SunSky.hs:127-157)
+static const float SOL[] = {165.5f, 162.3f, 211.2f, 258.8f, 258.2f, 242.3f, 267.6f, 296.6f,
+                            305.4f, 300.6f, 306.6f, 288.3f, 287.1f, 278.2f, 271.0f, 272.3f,
+                            263.6f, 255.0f, 250.6f, 253.1f, 253.5f, 251.3f, 246.3f, 241.7f,
+                            236.8f, 232.1f, 228.2f, 223.4f, 219.7f, 215.3f, 211.0f, 207.3f,
+                            202.4f, 198.7f, 194.3f, 190.7f, 186.3f, 182.6f};
+static const float KO_L[] = {300, 305, 310, 315, 320, 325, 330, 335, 340, 345, 350, 355, 445,
+                             450, 455, 460, 465, 470, 475, 480, 485, 490, 495, 500, 505, 510,
+                             515, 520, 525, 530, 535, 540, 545, 550, 555, 560, 565, 570, 575,
+                             580, 585, 590, 595, 600, 605, 610, 620, 630, 640, 650, 660, 670,
+                             680, 690, 700, 710, 720, 730, 740, 750, 760, 770, 780, 790};
+static const float KO_A[] = {10.0f,  4.8f,   2.7f,   1.35f,  0.8f,   0.380f, 0.160f, 0.075f,
+                             0.04f,  0.019f, 0.007f, 0.0f,   0.003f, 0.003f, 0.004f, 0.006f,
+                             0.008f, 0.009f, 0.012f, 0.014f, 0.017f, 0.021f, 0.025f, 0.03f,
+                             0.035f, 0.04f,  0.045f, 0.048f, 0.057f, 0.063f, 0.07f,  0.075f,
+                             0.08f,  0.085f, 0.095f, 0.103f, 0.110f, 0.12f,  0.122f, 0.12f,
+                             0.118f, 0.115f, 0.12f,  0.125f, 0.130f, 0.12f,  0.105f, 0.09f,
+                             0.079f, 0.067f, 0.057f, 0.048f, 0.036f, 0.028f, 0.023f, 0.018f,
+                             0.014f, 0.011f, 0.010f, 0.009f, 0.007f, 0.004f, 0.0f,   0.0f};
+static const float KG_L[] = {759, 760, 770, 771};
+static const float KG_A[] = {0.0f, 3.0f, 0.210f, 0.0f};
+static const float KWA_L[] = {689, 690, 700, 710, 720, 730, 740, 750, 760, 770, 780, 790, 800};
+static const float KWA_A[] = {0.0f,      0.160e-1f, 0.240e-1f, 0.125e-1f, 0.100e+1f,
+                              0.870f,    0.610e-1f, 0.100e-2f, 0.100e-4f, 0.100e-4f,
+                              0.600e-3f, 0.175e-1f, 0.360e-1f};
+
+// sf of sunSpectrum' (SunSky.hs:102-125)
+static float sunSpd(float t, float turb, float l) {
+  float m = 1.0f / (cosf(t) + 0.000940f * powf(1.6386f - t, -1.253f));
+  float tR = expf(-(m * 0.008735f * powf(l / 1000.0f, -4.08f)));
+  float alpha = 1.3f;
+  float beta = 0.04608365822050f * turb - 0.04586025928522f;
+  float tA = expf(-(m * beta * powf(l / 1000.0f, -alpha)));
+  float lozone = 0.35f;
+  float tO = expf(-(m * spdIrregular(KO_L, KO_A, 64, l) * lozone));
+  float kg = spdIrregular(KG_L, KG_A, 4, l);
+  float tG = expf(-(1.41f * kg * m / powf(1.0f + 118.93f * kg * m, 0.45f)));
+  float kwa = spdIrregular(KWA_L, KWA_A, 13, l);
+  float w = 2.0f;
+  float tWA = expf(-(0.2385f * kwa * w * m / powf(1.0f + 20.07f * kwa * w * m, 0.45f)));
+  return spdRegular(380.0f, 750.0f, SOL, 38, l) * tR * tA * tO * tG * tWA;
+}
+
+// initSky and sunSpectrum' with the basis coordinateSystem' up east
+// (SunSky.hs:17-24, 45-65, 96-101; Math.hs:427-441)
+static SkyData initSkyData(V east, V sdw, float t) {
+  V w = normalize(normalize(mkV(0, 1, 0)));
+  V u = normalize(cross(normalize(east), w));
+  V v = cross(w, u);
+  auto toLocal = [&](V a) { return mkV(dot(a, u), dot(a, v), dot(a, w)); };
+  SkyData s;
+  s.sunDir = normalize(toLocal(normalize(sdw)));
+  s.discDir = normalize(toLocal(sdw));
+  float st = acosf(clampf(s.sunDir.z, -1, 1));
+  float st2 = st * st, st3 = st * st * st, t2 = t * t;
+  float chi = (4.0f / 9.0f - t / 120.0f) * (PI - 2.0f * st);
+  s.sunTheta = st;
+  const float pY[5] = {0.17872f * t - 1.46303f, -0.35540f * t + 0.42749f,
+                       -0.02266f * t + 5.32505f, 0.12064f * t - 2.57705f,
+                       -0.06696f * t + 0.37027f};
+  const float px[5] = {-0.01925f * t - 0.25922f, -0.06651f * t + 0.00081f,
+                       -0.00041f * t + 0.21247f, -0.06409f * t - 0.89887f,
+                       -0.00325f * t + 0.04517f};
+  const float py[5] = {-0.01669f * t - 0.26078f, -0.09495f * t + 0.00921f,
+                       -0.00792f * t + 0.21023f, -0.04405f * t - 1.65369f,
+                       -0.01092f * t + 0.05291f};
+  for (int i = 0; i < 5; i++) {
+    s.perezY[i] = pY[i];
+    s.perezx[i] = px[i];
+    s.perezy[i] = py[i];
+  }
+  s.zenithY = ((4.04530f * t - 4.97100f) * tanf(chi) - 0.2155f * t + 2.4192f) * 1000.0f;
+  s.zenithx = (0.00165f * st3 - 0.00374f * st2 + 0.00208f * st) * t2 +
+              (-0.02902f * st3 + 0.06377f * st2 - 0.03202f * st + 0.00394f) * t +
+              (0.11693f * st3 - 0.21196f * st2 + 0.06052f * st + 0.25885f);
+  s.zenithy = (0.00275f * st3 - 0.00610f * st2 + 0.00316f * st) * t2 +
+              (-0.04212f * st3 + 0.08970f * st2 - 0.04153f * st + 0.00515f) * t +
+              (0.15346f * st3 - 0.26756f * st2 + 0.06669f * st + 0.26688f);
+  // sunSpectrum': fromSpd (mkSpdFunc sf), each band avgSpd = the mean of the
+  // function at the band's two ends (Spectrum.hs:316, 329-335)
+  s.sunR = BLACK;
+  if (!(s.sunDir.z < 0)) {
+    for (int i = 0; i < 16; i++) {
+      float l0 = lerp((float)i / 16.0f, 400.0f, 700.0f);
+      float l1 = lerp((float)(i + 1) / 16.0f, 400.0f, 700.0f);
+      s.sunR.v[i] = (sunSpd(st, t, l0) + sunSpd(st, t, l1)) * 0.5f;
+    }
+  }
+  return s;
+}
+
+// perez (SunSky.hs:81-86)
+static float perez(const float* p, float sunT, float t, float g, float lvz) {
+  float csg = cosf(g), cst = cosf(sunT);
+  float num = (1.0f + p[0] * expf(p[1] / cosf(t))) * (1.0f + p[2] * expf(p[3] * g)) + p[4] * csg * csg;
+  float den = (1.0f + p[0] * expf(p[1])) * (1.0f + p[2] * expf(p[3] * sunT)) + p[4] * cst * cst;
+  return lvz * num / den;
+}
+
+// skySpectrum (SunSky.hs:67-79) with chromaticityToXYZ (Spectrum.hs:229-251)
+// and xyzToSpectrum (Spectrum.hs:357-358)
+static Spec skySpectrum(const SkyData& s, V dir) {
+  float dz = -dir.z;
+  if (dz < 1e-4f) return BLACK;
+  float theta = acosf(dz);
+  float gamma = acosf(clampf(dot(dir, s.sunDir), -1, 1));
+  float x = perez(s.perezx, s.sunTheta, theta, gamma, s.zenithx);
+  float y = perez(s.perezy, s.sunTheta, theta, gamma, s.zenithy);
+  float yy = perez(s.perezY, s.sunTheta, theta, gamma, s.zenithY) * 1e-4f;
+  float m1 = (-1.3515f - 1.7703f * x + 5.9114f * y) / (0.0241f + 0.2562f * x - 0.7341f * y);
+  float m2 = (0.03f - 31.4424f * x + 30.0717f * y) / (0.0241f + 0.2562f * x - 0.7341f * y);
+  const uint32_t* S = BLING_CIE_S012_XYZ_BITS;
+  float cx = tbl(S, 0) + m1 * tbl(S, 3) + m2 * tbl(S, 6);
+  float cy = tbl(S, 1) + m1 * tbl(S, 4) + m2 * tbl(S, 7);
+  float cz = tbl(S, 2) + m1 * tbl(S, 5) + m2 * tbl(S, 8);
+  float X = cx * yy / cy, Z = cz * yy / cy;
+  float r, g, b;
+  xyzToRgb(X, yy, Z, r, g, b);
+  return rgbToSpectrum(true, r, g, b);
+}
+
+// eval of mkSunSkyLight at (u, v): sky plus the disc (SunSky.hs:18-20, 88-94)
+static Spec sunSkyEval(const SkyData& s, float u, float v) {
+  float phi = u * 2.0f * PI, theta = v * PI;  // cartToSph (Types.hs:31-33)
+  V dir = mkV(sinf(theta) * cosf(phi), sinf(theta) * sinf(phi), cosf(theta));  // sphToDir
+  Spec r = skySpectrum(s, dir);
+  float d = dot(s.discDir * mkV(1, 1, -1), dir);
+  return r + (d > sunThetaMax2() ? s.sunR : BLACK);
+}
+
 struct Light {
   int kind;  // BLING_LIGHT_* or 100 = area
   Spec spec;
@@ -581,6 +764,8 @@ struct Light {
   // infinite
   std::vector<Spec> env;
   int w, h;
+  bool sky;  // the map is mkSunSkyLight's function rather than env
+  SkyData skyd;
   Xf w2l;
   // Dist2D (Montecarlo.hs:75-106)
   std::vector<std::vector<float>> cfunc, ccdf;
@@ -1751,7 +1936,9 @@ static float sphericalPhi(V v) {
   return p < 0 ? p + 2.0f * PI : p;
 }
 // the lat-long map lookup: nearest texel (u in [0,1) across, v in [0,1) down)
+// of an image map, or the sun/sky function at (u, v)
 static Spec envLookup(const Light& l, float u, float v) {
+  if (l.sky) return sunSkyEval(l.skyd, u, v);
   int x = (int)floorf(u * (float)l.w), y = (int)floorf(v * (float)l.h);
   x = std::max(0, std::min(l.w - 1, x));
   y = std::max(0, std::min(l.h - 1, y));
@@ -2427,11 +2614,20 @@ int orc_scene_create(const bling_scene_desc* d, orc_scene** out) {
     l.shape = -1;
     l.id = -1;
     l.w = l.h = 0;
-    if (ld.kind == BLING_LIGHT_INFINITE) {
-      l.w = ld.env_w;
-      l.h = ld.env_h;
-      l.env.resize((size_t)l.w * l.h);
-      for (size_t k = 0; k < l.env.size(); k++) memcpy(l.env[k].v, ld.env + 16 * k, 64);
+    l.sky = false;
+    if (ld.kind == BLING_LIGHT_INFINITE || ld.kind == BLING_LIGHT_SUNSKY) {
+      if (ld.kind == BLING_LIGHT_SUNSKY) {  // mkDiscreteTextureMap2d (640, 480) eval
+        l.kind = BLING_LIGHT_INFINITE;
+        l.sky = true;
+        l.skyd = initSkyData(mkV(ld.east[0], ld.east[1], ld.east[2]), l.vec, ld.turbidity);
+        l.w = 640;
+        l.h = 480;
+      } else {
+        l.w = ld.env_w;
+        l.h = ld.env_h;
+        l.env.resize((size_t)l.w * l.h);
+        for (size_t k = 0; k < l.env.size(); k++) memcpy(l.env[k].v, ld.env + 16 * k, 64);
+      }
       memcpy(l.w2l.m, ld.w2l, 64);
       memcpy(l.w2l.i, ld.l2w, 64);
       // mkInfiniteAreaLight: dist = mkDist2D (texSize) (sY . eval) (Light.hs:76-82)
@@ -3098,6 +3294,13 @@ int orc_sppm_pass(const orc_scene* S, const bling_sppm_params* sp, int32_t width
   return BLING_OK;
 }
 
+void orc_sunsky_eval(const float east[3], const float sun_dir[3], float turbidity, float u,
+                     float v, float out[16]) {
+  SkyData sd = initSkyData(mkV(east[0], east[1], east[2]),
+                           mkV(sun_dir[0], sun_dir[1], sun_dir[2]), turbidity);
+  Spec s = sunSkyEval(sd, u, v);
+  memcpy(out, s.v, 64);
+}
 void orc_rgb_to_spectrum(int illum, float r, float g, float b, float out[16]) {
   Spec s = rgbToSpectrum(illum != 0, r, g, b);
   memcpy(out, s.v, 64);

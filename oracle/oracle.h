@@ -84,6 +84,9 @@ int orc_sppm_pass(const orc_scene* s, const bling_sppm_params* params, int32_t w
 
 /* restated helpers, for known-answer tests */
 void orc_rgb_to_spectrum(int illum, float r, float g, float b, float out[16]);
+/* mkSunSkyLight east sunDir turbidity evaluated at (u, v) */
+void orc_sunsky_eval(const float east[3], const float sun_dir[3], float turbidity, float u,
+                     float v, float out[16]);
 void orc_spectrum_to_xyz(const float s[16], float xyz[3]);
 void orc_xyz_to_rgb(const float xyz[3], float rgb[3]);
 float orc_filter_eval(int kind, const float* params, float x, float y);

@@ -54,6 +54,8 @@ def lib():
         L.orc_sample_li.argtypes = [C.c_void_p, P(abi.RenderParams), C.c_uint64, C.c_int, C.c_int,
                                     C.c_int, P(C.c_float), P(C.c_float), P(C.c_float)]
         L.orc_rgb_to_spectrum.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, P(C.c_float)]
+        L.orc_sunsky_eval.argtypes = [P(C.c_float), P(C.c_float), C.c_float, C.c_float, C.c_float,
+                                      P(C.c_float)]
         L.orc_spectrum_to_xyz.argtypes = [P(C.c_float), P(C.c_float)]
         L.orc_xyz_to_rgb.argtypes = [P(C.c_float), P(C.c_float)]
         L.orc_filter_eval.argtypes = [C.c_int, P(C.c_float), C.c_float, C.c_float]

@@ -5,8 +5,9 @@ A fixture holds what bling_gb300.blingfile.parse makes of a .bling file: the
 materials (bling_material records as bytes), meshes (vertices, indices,
 normals, uvs, material), shapes (kind, parameters, object-to-world transform
 and its inverse, material, emission), lights (kind, spectrum, vector,
-environment map, world-to-light transform), the primitive order, the camera
-inputs (camera-to-world, lens radius, focal distance, field of view) and the
+environment map, world-to-light transform, sun/sky east and turbidity), the
+primitive order, the camera inputs (camera-to-world, lens radius, focal
+distance, field of view) and the
 job's image size, filter, sampler and depths.
 """
 from __future__ import annotations
@@ -62,7 +63,9 @@ def save(job: B.Job, path: Path, source: str) -> None:
         if l.w2l is not None:
             arrays[f"light{k}_xf"] = np.stack([l.w2l.m, l.w2l.inv])
         meta["lights"].append({"kind": l.kind, "vec": [float(np.float32(v)) for v in l.vec],
-                               "env": l.env is not None, "w2l": l.w2l is not None})
+                               "env": l.env is not None, "w2l": l.w2l is not None,
+                               "east": [float(np.float32(v)) for v in l.east],
+                               "turbidity": float(np.float32(l.turbidity))})
     c2w, lr, fd, fov = job.camera_view
     arrays["camera_c2w"] = np.stack([c2w.m, c2w.inv])
     meta["camera"] = {"lens_radius": float(lr), "focal_distance": float(fd), "fov": float(fov)}
@@ -92,7 +95,9 @@ def load(path: Path) -> B.Job:
         x = z[f"light{k}_xf"] if l["w2l"] else None
         sc.lights.append(S.Light(l["kind"], z[f"light{k}_s"], tuple(l["vec"]),
                                  z[f"light{k}_env"] if l["env"] else None,
-                                 xf.Transform(x[0], x[1]) if x is not None else None))
+                                 xf.Transform(x[0], x[1]) if x is not None else None,
+                                 east=tuple(l.get("east", (0.0, 0.0, 0.0))),
+                                 turbidity=l.get("turbidity", 0.0)))
     sc.prim_order = meta["prim_order"]
     c = z["camera_c2w"]
     cam = meta["camera"]

@@ -206,7 +206,7 @@ def test_other_renderers_parse_and_are_named():
      "tex2 { constant rgbR 0 0 0 } } k { constant rgbR 1 1 1 } rough { constant 0.1 } }",
      "checker"),
     ("prim { julia c 0 0 0 0 epsilon 0.1 iterations 4 }", "julia"),
-    ("light { infinite { } l { sunSky east 0 0 1 sunDir 0 1 0 turbidity 2 } }", "sunSky"),
+    ("light { infinite { } l { file \"sky.png\" } }", "file"),
 ])
 def test_unsupported_constructs_are_named(src, what):
     with pytest.raises(B.Unsupported, match=what):

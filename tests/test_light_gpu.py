@@ -121,6 +121,16 @@ def test_every_light_and_material_vs_oracle(gpu_ctx):
     _counts_close(g.stats(), st[0], 300_000)
 
 
+def test_sunsky_light_pass_vs_oracle(gpu_ctx):
+    """photons leave the sun/sky through its Dist2D and the map evaluated on
+    the device (Light.hs:161-185)"""
+    from test_sunsky import sunsky_scene
+    sc = sunsky_scene(64, 48)
+    film, g, so, st = _both(gpu_ctx, sc, 64, 48, 200_000, seed=4)
+    _compare(film.read_splats(), so, rel=2e-3, frac=0.9)
+    _counts_close(g.stats(), st[0], 200_000)
+
+
 def test_passes_accumulate_and_clear(gpu_ctx):
     sc = S.cornell_room(32, 32)
     film, g, so, st = _both(gpu_ctx, sc, 32, 32, 50_000, seed=2, passes=3)

@@ -377,6 +377,19 @@ def test_graph_paper_diffuse_colour_vs_oracle(gpu_ctx):
     _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
 
 
+def test_sunsky_light_vs_oracle(gpu_ctx):
+    """the sun/sky map (SunSky.hs) evaluated on the device wherever the
+    light's le and sample need it; the importance distribution over its
+    640 x 480 raster"""
+    from test_sunsky import sunsky_scene
+    sc = sunsky_scene(64, 48)
+    p = S.render_params(64, 48, (2, 2), max_depth=5, sample_depth=2, rr_depth=2, seed=11)
+    fg, fo, st_g, st_o = _render_both(gpu_ctx, sc, p)
+    _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
+    assert st_g["nonfinite_drops"] == 0
+    assert fo[..., 2].mean() > 0
+
+
 @pytest.mark.parametrize("scene", ["cornell", "heightfield"])
 def test_ray_binning_renders_the_same(gpu_ctx, scene):
     """BLING_FLAG_BIN_RAYS only reorders which warp traces which ray: the

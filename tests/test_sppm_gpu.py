@@ -101,6 +101,14 @@ def test_specular_branching_and_materials_vs_oracle(gpu_ctx):
     assert sts[0]["hitpoints"] > 0
 
 
+def test_sunsky_sppm_vs_oracle(gpu_ctx):
+    from test_sunsky import sunsky_scene
+    sc = sunsky_scene(40, 30)
+    sp = abi.sppm_params(100_000, max_depth=4, radius=0.1, alpha=0.7, seed=9)
+    film, g, ref, sts = _both(gpu_ctx, sc, 40, 30, sp, passes=2)
+    _check(film, g, ref, sts, rel=2e-3, frac=0.9)
+
+
 def test_sppm_converges_to_the_path_tracer(gpu_ctx):
     W = H = 48
     sc = S.cornell_room(W, H)

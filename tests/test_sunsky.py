@@ -1,0 +1,174 @@
+"""The sun/sky light (mkSunSkyLight, SunSky.hs:12-158): Perez's sky and a
+solar disc as the continuous map of an infinite light.
+
+CPU: the library's host evaluation (bling_sunsky_eval, the same expression the
+device evaluates) equals the oracle's independent restatement bit for bit over
+a (u, v) grid, for suns above and below the horizon; the sky is black above
+the map's horizon and the disc is black when the sun is below it; the .bling
+reader's sunSky arm (MaterialParser.hs:266-270) gives a BLING_LIGHT_SUNSKY
+light; the oracle renders a sun/sky scene.
+GPU (test_render_gpu.py, test_sppm_gpu.py): renders of a sun/sky scene against
+the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from bling_gb300 import abi
+from bling_gb300 import blingfile as B
+from bling_gb300 import scene as S
+from bling_gb300 import transform as xf
+from bling_gb300.spectrum import rgb_to_spectrum
+from oracle import oracle as O
+
+P = C.POINTER(C.c_float)
+
+# (east, sunDir, turbidity): the sun high, low, behind the east axis, below
+# the horizon
+SKIES = [((0, 0, 1), (0, 0.3, 1), 12.0),
+         ((1, 0, 0), (0.2, 0.8, -0.3), 2.0),
+         ((0, 0, -1), (0.5, 0.1, 0.2), 6.5),
+         ((0, 0, 1), (0, -0.3, 1), 4.0)]
+
+
+def _lib():
+    from bling_gb300 import api
+    return api.lib()
+
+
+def _eval(fn, east, sun, turb, u, v):
+    out = np.zeros(16, np.float32)
+    fn((C.c_float * 3)(*east), (C.c_float * 3)(*sun), C.c_float(turb), C.c_float(u),
+       C.c_float(v), out.ctypes.data_as(P))
+    return out
+
+
+def _local_sun(east, sun):
+    """normalize (worldToLocal (coordinateSystem' up east) sunDir), in numpy
+    (float64: only to find the disc's (u, v), not compared bit for bit)"""
+    w = np.array([0.0, 1.0, 0.0])
+    e = np.asarray(east, float) / np.linalg.norm(east)
+    u = np.cross(e, w)
+    u /= np.linalg.norm(u)
+    v = np.cross(w, u)
+    s = np.asarray(sun, float)
+    loc = np.array([s @ u, s @ v, s @ w])
+    return loc / np.linalg.norm(loc)
+
+
+def _disc_uv(east, sun):
+    """(u, v) of the map direction at the disc's centre, (sx, sy, -sz)"""
+    s = _local_sun(east, sun)
+    d = np.array([s[0], s[1], -s[2]])
+    phi = np.arctan2(d[1], d[0]) % (2 * np.pi)
+    theta = np.arccos(np.clip(d[2], -1, 1))
+    return np.float32(phi / (2 * np.pi)), np.float32(theta / np.pi)
+
+
+@pytest.mark.parametrize("east,sun,turb", SKIES)
+def test_library_equals_oracle_bit_for_bit(east, sun, turb):
+    L, OL = _lib(), O.lib()
+    us = np.linspace(0, 1, 61, dtype=np.float32)
+    vs = np.linspace(0, 1, 47, dtype=np.float32)
+    du, dv = _disc_uv(east, sun)
+    pts = [(u, v) for u in us for v in vs] + [(du, dv), (np.float32(0.999999), np.float32(0.5))]
+    for u, v in pts:
+        a = _eval(L.bling_sunsky_eval, east, sun, turb, u, v)
+        b = _eval(OL.orc_sunsky_eval, east, sun, turb, u, v)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (u, v, a, b)
+        assert np.isfinite(a).all()
+
+
+@pytest.mark.parametrize("east,sun,turb", SKIES[:3])
+def test_sky_black_above_the_map_horizon_and_disc_bright(east, sun, turb):
+    OL = O.lib()
+    for u in np.linspace(0, 1, 33, dtype=np.float32):
+        for v in np.linspace(0, 0.49, 17, dtype=np.float32):
+            assert not _eval(OL.orc_sunsky_eval, east, sun, turb, u, v).any()
+    du, dv = _disc_uv(east, sun)
+    disc = _eval(OL.orc_sunsky_eval, east, sun, turb, du, dv)
+    # beside the disc (half a turn of u away, same height): the sky alone
+    sky = _eval(OL.orc_sunsky_eval, east, sun, turb, (du + np.float32(0.5)) % 1, dv)
+    assert (disc > sky).all() and disc.max() > 10 * sky.max()
+
+
+def test_sun_below_the_horizon_has_no_disc():
+    east, sun, turb = SKIES[3]
+    OL = O.lib()
+    du, dv = _disc_uv(east, sun)
+    # the disc's centre is in the map's upper half, where the sky is black too
+    assert dv < 0.5
+    assert not _eval(OL.orc_sunsky_eval, east, sun, turb, du, dv).any()
+    # the sky itself is not black (the Perez fit, evaluated for a sun below
+    # the horizon, goes negative here, as the reference's does)
+    assert _eval(OL.orc_sunsky_eval, east, sun, turb, np.float32(0.3), np.float32(0.8)).any()
+
+
+def test_turbidity_changes_the_sky():
+    OL = O.lib()
+    a = _eval(OL.orc_sunsky_eval, (0, 0, 1), (0, 0.3, 1), 2.0, np.float32(0.1), np.float32(0.7))
+    b = _eval(OL.orc_sunsky_eval, (0, 0, 1), (0, 0.3, 1), 12.0, np.float32(0.1), np.float32(0.7))
+    assert not np.array_equal(a, b)
+
+
+SCENE = """
+imageSize 32 24
+renderer { sampler sampled { sampler { stratified 2 2 } integrator { path maxDepth 4 sampleDepth 2 } } }
+transform { lookAt { pos 1 3 -5 look 0 0 -1 up 0 1 0 } }
+camera { perspective fov 60 lensRadius 0 focalDistance 5 }
+light { infinite { rotateX -90 }
+   l { sunSky east 0 0 1 sunDir 0 0.3 1 turbidity 7.5 } }
+newTransform { rotateX 90 }
+material { matte kd { constant rgbR 0.5 0.5 0.5 } sigma { constant 0 } }
+prim { shape { quad 10 10 } }
+newTransform { translate 0 1 0 }
+material { plastic kd { constant rgbR 0.1 0.4 0.3 } ks { constant rgbR 0.4 0.4 0.4 }
+           rough { constant 0.05 } }
+prim { shape { sphere radius 1 } }
+"""
+
+
+def test_reader_sunsky_arm():
+    job = B.parse(SCENE)
+    (l,) = job.scene.lights
+    assert l.kind == abi.LIGHT_SUNSKY
+    assert l.east == (0.0, 0.0, 1.0) and l.vec == (0.0, np.float32(0.3), 1.0)
+    assert l.turbidity == np.float32(7.5)
+    assert np.array_equal(l.w2l.m, xf.rotate_x(-90).m)
+    d, _keep = job.scene.desc()
+    assert d.lights[0].kind == abi.LIGHT_SUNSKY and d.lights[0].turbidity == np.float32(7.5)
+    assert list(d.lights[0].east) == [0.0, 0.0, 1.0]
+
+
+def sunsky_scene(w=32, h=24):
+    """a floor, a plastic sphere and the sun/sky of SunSky.hs's example
+    parameters (east +z, sun (0, 0.3, 1), turbidity 12, the map turned
+    rotateX -90)"""
+    s = S.Scene()
+    floor = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.6, 0.6, 0.6)))
+    plastic = s.add_material(abi.MAT_PLASTIC, kd=rgb_to_spectrum((0.05, 0.4, 0.35)),
+                             ks=rgb_to_spectrum((0.5, 0.5, 0.5)), roughness=0.01)
+    v = np.array([[-8, 0, -8], [8, 0, -8], [8, 0, 8], [-8, 0, 8]], np.float32)
+    s.add_mesh(v, [0, 1, 2, 0, 2, 3], floor)
+    s.prim_order = [0, ~s.add_shape(abi.SHAPE_SPHERE, (1.0,), xf.translate(0, 1, 0), plastic)]
+    s.lights = [S.Light(abi.LIGHT_SUNSKY, vec=(0.0, 0.3, 1.0), east=(0.0, 0.0, 1.0),
+                        turbidity=12.0, w2l=xf.rotate_x(-90))]
+    c2w = xf.look_at((1, 3, -5), (0, 0.5, 0), (0, 1, 0))
+    c2w, r2c = xf.perspective_camera(c2w, 0.0, 1.0, 60.0, w, h)
+    s.set_camera(c2w, r2c)
+    return s
+
+
+def test_oracle_renders_a_sunsky_scene():
+    p = S.render_params(32, 24, (1, 1), max_depth=3, sample_depth=2, rr_depth=2, seed=3)
+    film, st = O.OracleScene(sunsky_scene()).render_pass(p, 0)
+    assert np.isfinite(film).all()
+    assert film[..., 2].mean() > 0
+    assert st["path_samples"] >= 32 * 24
+
+
+def test_oracle_parsed_scene_renders():
+    job = B.parse(SCENE)
+    p = S.render_params(job.width, job.height, (1, 1), max_depth=3, sample_depth=2, rr_depth=2)
+    film, _ = O.OracleScene(job.scene).render_pass(p, 0)
+    assert np.isfinite(film).all() and film[..., 2].mean() > 0
