@@ -368,6 +368,10 @@ def measure_render(ctx, stream, args):
             "scene_create_ms": round(s1["scene_build_ms"], 1),
             "nonfinite_drops": s1["nonfinite_drops"],
             "film": "fp64-compensated" if fp64 else "fp32"}
+        if s1["nonfinite_pass"] >= 0:  # the latest pass's first dropped sample
+            out[name]["nonfinite_first"] = {"pass": s1["nonfinite_pass"],
+                                            "pixel": list(s1["nonfinite_pixel"]),
+                                            "sample": s1["nonfinite_sample"]}
         if fp64:  # the large mesh: the same pass over a BVH built on the GPU
             out[name]["gpu_built_bvh"] = _gpu_built_pass(sc, p, stream)
         if not args.no_cpu_baseline:

@@ -32,7 +32,7 @@ SHAPE_SPHERE, SHAPE_QUAD, SHAPE_BOX, SHAPE_DISK, SHAPE_CYLINDER = 0, 1, 2, 3, 4
 LIGHT_DIRECTIONAL, LIGHT_POINT, LIGHT_INFINITE, LIGHT_SUNSKY = 0, 1, 2, 3
 FILTER_BOX, FILTER_GAUSS, FILTER_MITCHELL, FILTER_SINC, FILTER_TRIANGLE = 0, 1, 2, 3, 4
 SAMPLER_STRATIFIED, SAMPLER_RANDOM = 0, 1
-ABI_VERSION = 4  # BLING_ABI_VERSION of include/bling_gpu.h
+ABI_VERSION = 5  # BLING_ABI_VERSION of include/bling_gpu.h
 
 
 class Opts(C.Structure):
@@ -97,7 +97,9 @@ class Stats(C.Structure):
                 ("bvh_build_ms", C.c_double), ("last_pass_ms", C.c_double),
                 ("bvh_nodes", C.c_uint64), ("bvh_leaf_prims", C.c_uint64),
                 ("device_bytes", C.c_uint64), ("light_splats", C.c_uint64),
-                ("scene_build_ms", C.c_double)]
+                ("scene_build_ms", C.c_double), ("nonfinite_pass", C.c_int64),
+                ("nonfinite_pixel", C.c_int32 * 2), ("nonfinite_sample", C.c_int32),
+                ("reserved_stats", C.c_int32)]
 
 
 class SppmParams(C.Structure):

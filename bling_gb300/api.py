@@ -220,7 +220,9 @@ class GpuScene:
     def stats(self) -> dict:
         s = abi.Stats()
         self.ctx.check(lib().bling_scene_stats(self.h, C.byref(s)))
-        return {k: getattr(s, k) for k, _ in abi.Stats._fields_}
+        out = {k: getattr(s, k) for k, _ in abi.Stats._fields_ if k != "reserved_stats"}
+        out["nonfinite_pixel"] = tuple(s.nonfinite_pixel)
+        return out
 
     # --- ray queries over host arrays (SoA float32 (8, n)) ---
     def closest(self, rays: np.ndarray, with_bary: bool = True):

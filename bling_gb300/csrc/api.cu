@@ -625,6 +625,8 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
   CK(c, cudaStreamSynchronize(c->stream));
   auto t1 = std::chrono::steady_clock::now();
   S->stats.bvh_build_ms = bvh_ms;
+  S->stats.nonfinite_pass = -1;
+  S->stats.nonfinite_pixel[0] = S->stats.nonfinite_pixel[1] = S->stats.nonfinite_sample = -1;
   S->stats.scene_build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   S->stats.bvh_nodes = (uint64_t)S->n_nodes;
   S->stats.bvh_leaf_prims = (uint64_t)n_slots;
@@ -1074,6 +1076,15 @@ int bling_light_pass(bling_scene* s, bling_film* f, const bling_light_params* p,
   return BLING_OK;
 }
 
+// the latest render pass that dropped a sample, and that pass's first one
+static void note_dropped(bling_scene* s, uint64_t pass, const PassResult& res) {
+  if (res.nf_x < 0) return;
+  s->stats.nonfinite_pass = (int64_t)pass;
+  s->stats.nonfinite_pixel[0] = res.nf_x;
+  s->stats.nonfinite_pixel[1] = res.nf_y;
+  s->stats.nonfinite_sample = res.nf_n;
+}
+
 int bling_render_pass(bling_scene* s, bling_film* f, const bling_render_params* p, uint64_t pass) {
   return bling_render_pass_camera(s, f, p, nullptr, pass);
 }
@@ -1110,6 +1121,7 @@ int bling_render_pass_camera(bling_scene* s, bling_film* f, const bling_render_p
   s->stats.path_samples += res.path_samples;
   s->stats.nonfinite_drops += res.nonfinite;
   s->stats.degenerate_rays += res.degenerate;
+  note_dropped(s, pass, res);
   return BLING_OK;
 }
 
@@ -1136,6 +1148,7 @@ int bling_render_pass_noalloc(bling_scene* s, const bling_render_params* p, uint
   s->stats.path_samples += res.path_samples;
   s->stats.nonfinite_drops += res.nonfinite;
   s->stats.degenerate_rays += res.degenerate;
+  note_dropped(s, pass, res);
   return BLING_OK;
 }
 

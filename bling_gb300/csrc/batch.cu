@@ -436,7 +436,7 @@ __global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJob
       const BatchSceneDev& SC = scenes[S.scene[q]];
       unsigned long long g = S.gidx[q];
       o = shadeVertex(SC.A, SC.S, J.P, st, (int)q, g, S.depth[q], c, [&](const Spec& L) {
-        splatSample(J.film, J.P, g, L, c + C_NONFINITE, JobFilter{J.filter});
+        splatSample(J.film, J.P, g, L, c, JobFilter{J.filter});
         fin = true;
       });
     }
@@ -476,7 +476,7 @@ __global__ void __launch_bounds__(128, 3) k_bresolve(BatchCtl* ctl,
       cont = resolveVertex(
           SC.A, SC.S, st, q, c,
           [&](const Spec& L) {
-            splatSample(J.film, J.P, g, L, c + C_NONFINITE, JobFilter{J.filter});
+            splatSample(J.film, J.P, g, L, c, JobFilter{J.filter});
             fin = true;
           },
           Tn, Ln);

@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, Pass
       s = qin[q];
       uint64_t g = P.chunk_base + (uint64_t)s;  // slots never move
       o = shadeVertex(A, S, P, st, s, g, depth, counters, [&](const Spec& L) {
-        splatSample(film, P, g, L, counters + C_NONFINITE, TableFilter{filter});
+        splatSample(film, P, g, L, counters, TableFilter{filter});
       });
     }
     queueAppend(o.shadow, s, Q.shadow, counters + C_SHADOW);
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(128) k_resolve(DevAccel A, DevShading S, PassP
       cont = resolveVertex(
           A, S, st, s, counters,
           [&](const Spec& L) {
-            splatSample(film, P, g, L, counters + C_NONFINITE, TableFilter{filter});
+            splatSample(film, P, g, L, counters, TableFilter{filter});
           },
           Tn, Ln);
       if (cont) {
@@ -505,6 +505,17 @@ static int ensureWorkspace(IntegratorWorkspace& ws, size_t cap, std::string& err
   return BLING_ERR_OOM;
 }
 
+// the pixel and sample number of the lowest dropped sample index g, kept
+// as ~g in C_FIRST_NONFINITE (decodeSample's order)
+static void firstDropped(const PassParams& P, unsigned long long v, PassResult& res) {
+  if (!v) return;
+  uint64_t g = ~(uint64_t)v;
+  uint64_t pix = g / (uint64_t)P.spp;
+  res.nf_n = (int32_t)(g % (uint64_t)P.spp);
+  res.nf_x = P.x0 + (int32_t)(pix % (uint64_t)P.nx);
+  res.nf_y = P.y0 + (int32_t)(pix / (uint64_t)P.nx);
+}
+
 int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S,
                            const bling_render_params& p, uint64_t pass, float* d_film, int fw,
                            int fh, IntegratorWorkspace& ws, PassResult& res, std::string& err,
@@ -560,6 +571,7 @@ int integrator_render_pass(cudaStream_t stream, const DevAccel& A, const DevShad
   res.nonfinite = cnt[C_NONFINITE];
   res.degenerate = cnt[C_DEGENERATE];
   res.path_samples = total;
+  firstDropped(P, cnt[C_FIRST_NONFINITE], res);
   return BLING_OK;
 }
 
@@ -667,6 +679,7 @@ int integrator_render_pass_noalloc(cudaStream_t stream, const DevAccel& A, const
   res.nonfinite = cnt[C_NONFINITE];
   res.degenerate = cnt[C_DEGENERATE];
   res.path_samples = total;
+  firstDropped(P, cnt[C_FIRST_NONFINITE], res);
   return BLING_OK;
 }
 

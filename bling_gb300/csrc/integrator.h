@@ -113,6 +113,9 @@ struct DevShading {
 
 struct PassResult {
   uint64_t rays_closest, rays_any, path_samples, nonfinite, degenerate;
+  // the pass's first dropped (NaN/Inf) sample: pixel and sample number, or
+  // nf_x = -1 when none was dropped
+  int32_t nf_x = -1, nf_y = -1, nf_n = -1;
 };
 
 // Device buffer reused across passes (grow-only), owned by a context: the

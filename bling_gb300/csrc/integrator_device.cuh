@@ -1232,15 +1232,16 @@ struct TableFilter {
 // (mkImageTile/addTile, Image.hs:108-120,178-199): the footprint is clipped to
 // the tile's pixel range and to the film.  filt(i) reads entry i of the 16x16
 // filter table.
+// Returns false when the sample is dropped as NaN/Inf.
 template <class Filter>
-__device__ void filmAddT(float* __restrict__ film, const PassParams& P, int ix, int iy, float sx,
+__device__ bool filmAddT(float* __restrict__ film, const PassParams& P, int ix, int iy, float sx,
                          float sy, const Spec& L, unsigned long long* nonfinite, Filter filt) {
   bool bad = false;
 #pragma unroll
   for (int i = 0; i < 16; i++) bad = bad || isnan(L.v[i]) || isinf(L.v[i]);
   if (bad) {
     atomicAdd(nonfinite, 1ull);
-    return;
+    return false;
   }
   float a = 0, b = 0, c = 0;
 #pragma unroll
@@ -1278,6 +1279,7 @@ __device__ void filmAddT(float* __restrict__ film, const PassParams& P, int ix, 
       atomicAdd(px + 3, smz * w);
     }
   }
+  return true;
 }
 
 }  // namespace bgpu

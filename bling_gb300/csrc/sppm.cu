@@ -285,8 +285,8 @@ __global__ void __launch_bounds__(128) k_sp_camfilm(PassParams P, SpCam cs, int6
                                                     unsigned long long* counters) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
        i += (int64_t)gridDim.x * blockDim.x)
-    splatSample(film, P, P.chunk_base + (uint64_t)i, loadBands(cs.Ls, (int)i),
-                counters + S_NONFINITE, TableFilter{filter});
+    splatSampleAt(film, P, P.chunk_base + (uint64_t)i, loadBands(cs.Ls, (int)i),
+                  counters + S_NONFINITE, TableFilter{filter});
 }
 
 // ------------------------------------------------------------------ spatial hash

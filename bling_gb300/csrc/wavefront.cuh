@@ -49,6 +49,7 @@ struct Queues {
 enum : int {
   C_LIVE0 = 0, C_LIVE1 = 1, C_CLOSEST = 2, C_ANY = 3, C_NONFINITE = 4, C_NEXT_TRACE = 5,
   C_SHADOW = 6, C_MIS = 7, C_RESOLVE = 8, C_NEXT_SHADOW = 9, C_NEXT_MIS = 10, C_DEGENERATE = 11,
+  C_FIRST_NONFINITE = 12,  // ~g of the pass's lowest dropped sample g (0: none), by atomicMax
   C_COUNT = 16
 };
 
@@ -282,18 +283,30 @@ __device__ __forceinline__ Ray cameraRay(const PassParams& P, const bling_camera
   return transRay(cam.c2w, ray);
 }
 
-// the film splat of sample g (the raster position is recomputed from the sampler)
+// the film splat of sample g (the raster position is recomputed from the
+// sampler); false when the sample is dropped as NaN/Inf (counted in
+// *nonfinite)
 template <class Filter>
-__device__ __forceinline__ void splatSample(float* film, const PassParams& P, uint64_t g,
-                                            const Spec& L, unsigned long long* nonfinite,
-                                            Filter filt) {
+__device__ __forceinline__ bool splatSampleAt(float* film, const PassParams& P, uint64_t g,
+                                              const Spec& L, unsigned long long* nonfinite,
+                                              Filter filt) {
   int ix, iy;
   uint32_t sn;
   decodeSample(P, g, ix, iy, sn);
   Sampler smp = mkSampler(P, ix, iy, sn);
   float sx, sy, lu, lv;
   pixelSample(P, smp, ix, iy, sx, sy, lu, lv);
-  filmAddT(film, P, ix, iy, sx, sy, L, nonfinite, filt);
+  return filmAddT(film, P, ix, iy, sx, sy, L, nonfinite, filt);
+}
+// splatSampleAt with the path integrator's counters: a dropped sample counts
+// in counters[C_NONFINITE] and the lowest such g is kept in
+// counters[C_FIRST_NONFINITE]
+template <class Filter>
+__device__ __forceinline__ void splatSample(float* film, const PassParams& P, uint64_t g,
+                                            const Spec& L, unsigned long long* counters,
+                                            Filter filt) {
+  if (!splatSampleAt(film, P, g, L, counters + C_NONFINITE, filt))
+    atomicMax(counters + C_FIRST_NONFINITE, ~(unsigned long long)g);
 }
 
 // the pass constants of render parameters (imageWindow', Image.hs:170-176;

@@ -204,6 +204,21 @@ def camera_desc(c2w: xf.Transform, r2c: xf.Transform, lens_radius=0.0, focal_dis
     return c
 
 
+def crop_camera(cam: abi.CameraDesc, x0: int, y0: int) -> abi.CameraDesc:
+    """The camera of a window of the image whose top-left pixel is (x0, y0):
+    raster (x, y) of the window is raster (x + x0, y + y0) of the full image,
+    so a film of the window's size gets exactly those pixels' camera rays."""
+    r2c = xf.Transform(np.asarray(cam.r2c, np.float32), np.asarray(cam.r2c_inv, np.float32))
+    r2c = xf.concat(xf.translate(x0, y0, 0), r2c)  # the shift first, then r2c
+    c = abi.CameraDesc.from_buffer_copy(cam)
+    c.r2c[:] = r2c.m.tolist()
+    c.r2c_inv[:] = r2c.inv.tolist()
+    if cam.pixel_area:
+        w2r = xf.Transform(np.asarray(cam.w2r, np.float32), np.zeros(16, np.float32))
+        c.w2r[:] = xf.concat(w2r, xf.translate(-x0, -y0, 0)).m.tolist()
+    return c
+
+
 def render_params(width, height, strata=(4, 4), max_depth=5, sample_depth=3, rr_depth=7,
                   filter_kind=abi.FILTER_BOX, filter_params=(0, 0, 0, 0), seed=1,
                   sampler=abi.SAMPLER_STRATIFIED):

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define BLING_ABI_VERSION 4
+#define BLING_ABI_VERSION 5
 
 #define BLING_OK 0
 #define BLING_ERR_INVALID_ARG (-1)
@@ -251,6 +251,14 @@ typedef struct bling_stats {
   uint64_t device_bytes;
   uint64_t light_splats;    /* splats of light and SPPM passes added to the splat image */
   double scene_build_ms;    /* all of bling_scene_create: checks, BVH, uploads */
+  /* The latest render pass (bling_render_pass, bling_render_pass_noalloc)
+   * that dropped a NaN/Inf sample, -1 if none has, and that pass's first
+   * dropped sample: its pixel and its sample number within the pixel (the
+   * sample the oracle or a debugger can replay). */
+  int64_t nonfinite_pass;
+  int32_t nonfinite_pixel[2];
+  int32_t nonfinite_sample;
+  int32_t reserved_stats;
 } bling_stats;
 
 /* ---- context ---- */

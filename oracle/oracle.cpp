@@ -2413,12 +2413,17 @@ static void filterTable(int kind, const float* fp, float* out) {
   }
 }
 
+// The pixel sums are binary32 as in the reference (T = float), or binary64
+// (T = double) for reference renders with many samples per pixel: each
+// binary32 product w * XYZ is then added in double precision.
+template <class T>
 struct FilmImg {  // MImage (Image.hs:64-71), pixel part
   int w, h, ox, oy;
-  float* p;
+  T* p;
 };
 // addSample (Image.hs:250-299); returns false when dropped as NaN/Inf
-static bool addSample(FilmImg& img, const float* tblv, float fw, float fh, float sx, float sy,
+template <class T>
+static bool addSample(FilmImg<T>& img, const float* tblv, float fw, float fh, float sx, float sy,
                       const Spec& ss) {
   if (sNaN(ss) || sInf(ss)) return false;
   float smx, smy, smz;
@@ -2437,11 +2442,11 @@ static bool addSample(FilmImg& img, const float* tblv, float fw, float fh, float
       float fx = fabsf(((float)x - dx) * ifw * 16.0f);
       int ix = std::min((int)floorf(fx), 15);
       float w = tblv[iy * 16 + ix];
-      float* px = img.p + 4 * ((size_t)(x - img.ox) + (size_t)(y - img.oy) * img.w);
-      px[0] = px[0] + w;
-      px[1] = px[1] + smx * w;
-      px[2] = px[2] + smy * w;
-      px[3] = px[3] + smz * w;
+      T* px = img.p + 4 * ((size_t)(x - img.ox) + (size_t)(y - img.oy) * img.w);
+      px[0] = px[0] + (T)w;
+      px[1] = px[1] + (T)(smx * w);
+      px[2] = px[2] + (T)(smy * w);
+      px[3] = px[3] + (T)(smz * w);
     }
   }
   return true;
@@ -2889,8 +2894,8 @@ int orc_sample_li(const orc_scene* s, const bling_render_params* p, uint64_t pas
 // gets its samples, each added to its tile's image (mkImageTile, addSample),
 // and the tiles are added to the film in order (addTile).  sampleFn(smp, ix,
 // iy, tile, sx, sy, C) returns one sample's radiance.
-template <class SampleFn>
-static int renderTiles(const orc_scene* S, const bling_render_params* p, uint64_t pass, float* film,
+template <class Acc, class SampleFn>
+static int renderTiles(const orc_scene* S, const bling_render_params* p, uint64_t pass, Acc* film,
                        int row_begin, int row_end, int nth, int ntiles_hint, SampleFn sampleFn,
                        uint64_t* path_samples, uint64_t* rays_closest, uint64_t* rays_any) {
   (void)S;
@@ -2914,7 +2919,7 @@ static int renderTiles(const orc_scene* S, const bling_render_params* p, uint64_
     rb = y0;
     re = y1 + 1;
   }
-  std::vector<std::vector<float>> timgs(tiles.size());
+  std::vector<std::vector<Acc>> timgs(tiles.size());
   std::vector<int> tw(tiles.size()), th(tiles.size()), tox(tiles.size()), toy(tiles.size());
   std::atomic<uint64_t> nps{0}, ncl{0}, nany{0};
   parallelFor(tiles.size(), nth, [&](size_t ti) {
@@ -2930,8 +2935,8 @@ static int renderTiles(const orc_scene* S, const bling_render_params* p, uint64_
     toy[ti] = py0;
     Counters C;
     uint64_t ps = 0;
-    if (w > 0 && h > 0) timgs[ti].assign((size_t)w * h * 4, 0.0f);
-    FilmImg img{w, h, px0, py0, timgs[ti].data()};
+    if (w > 0 && h > 0) timgs[ti].assign((size_t)w * h * 4, (Acc)0);
+    FilmImg<Acc> img{w, h, px0, py0, timgs[ti].data()};
     for (int iy = T.ys; iy <= T.ye; iy++) {
       if (iy < rb || iy >= re) continue;
       for (int ix = T.xs; ix <= T.xe; ix++)
@@ -2971,11 +2976,10 @@ static size_t extentTiles(const bling_render_params* p) {
   return (size_t)((x1 - x0) / 16 + 1) * (size_t)((y1 - y0) / 16 + 1);
 }
 
-extern "C" {
-
-int orc_render_pass(const orc_scene* S, const bling_render_params* p, uint64_t pass, float* film,
-                    int row_begin, int row_end, int nth, uint64_t* path_samples,
-                    uint64_t* rays_closest, uint64_t* rays_any) {
+template <class T>
+static int renderPass(const orc_scene* S, const bling_render_params* p, uint64_t pass, T* film,
+                      int row_begin, int row_end, int nth, uint64_t* path_samples,
+                      uint64_t* rays_closest, uint64_t* rays_any) {
   if (p->strata_x <= 0 || p->strata_y <= 0 || p->width <= 0 || p->height <= 0)
     return BLING_ERR_INVALID_ARG;
   return renderTiles(
@@ -2984,6 +2988,17 @@ int orc_render_pass(const orc_scene* S, const bling_render_params* p, uint64_t p
         return traceSample(S, p, smp, ix, iy, sx, sy, C);
       },
       path_samples, rays_closest, rays_any);
+}
+extern "C" {
+
+int orc_render_pass(const orc_scene* S, const bling_render_params* p, uint64_t pass, float* film,
+                    int row_begin, int row_end, int nth, uint64_t* path_samples,
+                    uint64_t* rays_closest, uint64_t* rays_any) {
+  return renderPass(S, p, pass, film, row_begin, row_end, nth, path_samples, rays_closest, rays_any);
+}
+int orc_render_pass_f64(const orc_scene* S, const bling_render_params* p, uint64_t pass,
+                        double* film, int nth, uint64_t* path_samples) {
+  return renderPass(S, p, pass, film, 0, 0, nth, path_samples, nullptr, nullptr);
 }
 
 }  // extern "C"

@@ -60,6 +60,10 @@ int orc_render_pass(const orc_scene* s, const bling_render_params* p, uint64_t p
                     uint64_t* path_samples, uint64_t* rays_closest, uint64_t* rays_any);
 
 /* radiance of one camera sample: li as XYZ plus the raster position */
+/* orc_render_pass over the whole image into a binary64 film (the tile and
+ * film sums in double precision), for reference renders of many passes */
+int orc_render_pass_f64(const orc_scene* s, const bling_render_params* p, uint64_t pass,
+                        double* film, int nthreads, uint64_t* path_samples);
 int orc_sample_li(const orc_scene* s, const bling_render_params* p, uint64_t pass, int px,
                   int py, int n, float* out_xyz, float* out_raster, float* out_spectrum);
 

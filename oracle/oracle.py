@@ -44,6 +44,8 @@ def lib():
         L.orc_render_pass.argtypes = [C.c_void_p, P(abi.RenderParams), C.c_uint64, P(C.c_float),
                                       C.c_int, C.c_int, C.c_int, P(C.c_uint64), P(C.c_uint64),
                                       P(C.c_uint64)]
+        L.orc_render_pass_f64.argtypes = [C.c_void_p, P(abi.RenderParams), C.c_uint64,
+                                          P(C.c_double), C.c_int, P(C.c_uint64)]
         L.orc_light_pass.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64, C.c_uint64,
                                      C.c_int32, C.c_int64, C.c_int64, P(C.c_float), C.c_int,
                                      P(C.c_uint64)]
@@ -161,6 +163,19 @@ class OracleScene:
         if rc != 0:
             raise ValueError(f"orc_render_pass failed: {rc}")
         return film, {"path_samples": ps.value, "rays_closest": rc_.value, "rays_any": ra.value}
+
+    def render_pass_f64(self, params, pass_index=0, film=None, nthreads=0):
+        """render_pass into a float64 film (tile and film sums in double)"""
+        if film is None:
+            film = np.zeros((params.height, params.width, 4), np.float64)
+        assert film.dtype == np.float64 and film.flags.c_contiguous
+        ps = C.c_uint64()
+        rc = lib().orc_render_pass_f64(self.h, C.byref(params), pass_index,
+                                       film.ctypes.data_as(C.POINTER(C.c_double)), nthreads,
+                                       C.byref(ps))
+        if rc != 0:
+            raise ValueError(f"orc_render_pass_f64 failed: {rc}")
+        return film, {"path_samples": ps.value}
 
     def light_pass(self, width, height, photons, seed=0, pass_index=0, max_depth=0, splats=None,
                    first=0, count=None, nthreads=0):

@@ -31,7 +31,7 @@ DEFAULT_SOURCE = Path("/root/reference/examples")
 
 # the examples whose scene content the GPU path renders
 EXAMPLES = ["blackbody-emission", "cornell-box", "cornell-box-specular", "matte-test",
-            "plastic-test", "trans-matte"]
+            "plastic-test", "race", "trans-matte"]
 
 NEUTRAL_RENDERER = ("renderer { sampler sampled { sampler { stratified 1 1 } "
                     "integrator { path maxDepth 5 sampleDepth 3 } } }")

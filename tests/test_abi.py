@@ -43,7 +43,7 @@ def test_library_exports_every_declared_symbol(so):
 def test_abi_version(so):
     from bling_gb300 import abi
     so.bling_abi_version.restype = C.c_int
-    assert so.bling_abi_version() == abi.ABI_VERSION == 4
+    assert so.bling_abi_version() == abi.ABI_VERSION == 5
     hdr = (ROOT / "include" / "bling_gpu.h").read_text()
     assert f"#define BLING_ABI_VERSION {abi.ABI_VERSION}" in hdr
     # bling_render_params: 8 int32, 4 float, uint64 seed, int32 sampler_kind, int32 reserved

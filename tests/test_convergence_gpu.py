@@ -9,16 +9,26 @@
   (`depth == md = return l`, Integrator/Path.hs:51), so the sphere is
   black and the background (a miss on the camera ray) still sees the
   environment.
-* Convergence: a 4096-spp GPU render of the Cornell room (FP64-compensated
-  film) against a 16384-spp render of the CPU oracle with the same seedless
-  scene but independent random streams, summed in float64 over its passes.
-  Relative RMSE (over pixels and X, Y, Z, divided by the reference's mean)
-  must be within 1%, the bar for converged images; the measured value is
-  printed.
+* Convergence: a 4096-spp GPU render of the 256 x 256 Cornell room
+  (FP64-compensated film) against the oracle's 16384-spp render of the same
+  scene into float64 films, with independent random streams (the committed
+  fixture tests/golden/cornell256_oracle_16k.npz, made by
+  make_cornell_reference.py).  Per-pixel means agree within 3 sigma; the
+  linear relative RMSE beyond the Monte Carlo noise is within 1%; and the
+  output image (gamma 2.2, clamped, 8 bit) is within 1% RMSE of the
+  reference's.  The raw linear relative RMSE is printed beside its noise
+  floor: at 4096 spp the per-pixel noise of this scene alone is about 1.4%
+  of the image mean, so the raw linear figure cannot reach 1% at this spp.
+* The large-mesh geometry: the full 8.4M-triangle heightfield and 4096
+  spheres at a small image size, GPU against oracle with independent random
+  streams, per-pixel means within 3 sigma.
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
+from bling_gb300 import image
 from bling_gb300 import scene as S
 from oracle.oracle import OracleScene
 
@@ -63,42 +73,43 @@ def _pass_estimates(films):
     return np.stack([f[..., 1:] / np.where(f[..., :1] > 0, f[..., :1], 1) for f in films])
 
 
-def test_4096spp_converges_to_the_16k_oracle_render(gpu_ctx):
-    """GPU: 32 passes of 128 spp (4096 spp, FP64 film).  Oracle: 32 passes of
-    512 spp (16384 spp) with another seed, so the two share no random
-    numbers.  Per pixel and channel, z = (mean_gpu - mean_ref) /
-    sqrt(var_gpu + var_ref), the variances of the means estimated from the
-    spread of the pass estimates (31 degrees of freedom each).
+GOLDEN = Path(__file__).resolve().parent / "golden"
 
-    * per-pixel means agree within 3 sigma: at most 2% of the values have
-      |z| > 3 (0.5% expected for 31 degrees of freedom), and the mean of z^2
-      is within [0.8, 1.35] (1.07 expected);
-    * the image RMSE beyond noise is within 1%: the measured squared error
-      minus the expected noise (the mean of var_gpu + var_ref), square-rooted
-      and divided by the reference's mean, is at most 1%.  The raw relative
-      RMSE (noise included) is printed next to it.
+
+def test_4096spp_converges_to_the_16k_fp64_oracle_render(gpu_ctx):
+    """GPU: 32 passes of 128 spp (4096 spp, FP64 film), seed 5.  Reference:
+    the oracle's 32 passes of 512 spp (16384 spp, float64 films), seed 99,
+    as per-pixel means and variances of the mean.  Per pixel and channel,
+    z = (mean_gpu - mean_ref) / sqrt(var_gpu + var_ref).
+
+    * at most 2% of the values have |z| > 3 (0.5% expected for 31 degrees
+      of freedom) and the mean of z^2 is within [0.8, 1.35] (1.07 expected);
+    * linear relative RMSE beyond noise (the squared error minus the
+      expected noise, square-rooted, over the reference's mean) <= 1%;
+    * display RMSE: both images resolved to RGB (xyzToRgb), gamma 2.2,
+      clamped and quantised to 8 bits as the reference writes them; the RMSE
+      over pixels and channels, in units of full scale, <= 1%.
     """
-    n_pass = 32
-    sc = S.cornell_room(24, 24)
+    ref = np.load(GOLDEN / "cornell256_oracle_16k.npz")
+    mr, vr = ref["mean"].astype(np.float64), ref["var_mean"].astype(np.float64)
+    assert int(ref["spp"]) == 16384
+    n_pass, size = 32, mr.shape[0]
+    sc = S.cornell_room(size, size)
     g = gpu_ctx.scene(sc)
-    f = gpu_ctx.film(24, 24, fp64=True)
-    p = S.cornell_params(24, 24)  # depth 5, Russian roulette after bounce 3
-    p2 = S.render_params(24, 24, (16, 8), max_depth=p.max_depth, sample_depth=p.sample_depth,
-                         rr_depth=p.rr_depth, seed=5)  # 128 spp per pass
-    prev = np.zeros((24, 24, 4), np.float64)
+    f = gpu_ctx.film(size, size, fp64=True)
+    base = S.cornell_params(size, size)  # depth 5, Russian roulette after bounce 3
+    p = S.render_params(size, size, (16, 8), max_depth=base.max_depth,
+                        sample_depth=base.sample_depth, rr_depth=base.rr_depth,
+                        filter_kind=base.filter_kind, seed=5)  # 128 spp per pass
+    prev = np.zeros((size, size, 4), np.float64)
     gpu_films = []
     for k in range(n_pass):
-        g.render_pass(f, p2, k)
+        g.render_pass(f, p, k)
         cur = f.read_f64()
         gpu_films.append(cur - prev)
         prev = cur
-    o = OracleScene(sc)
-    po = S.render_params(24, 24, (32, 16), max_depth=p.max_depth, sample_depth=p.sample_depth,
-                         rr_depth=p.rr_depth, seed=99)  # 512 spp per pass
-    ref_films = [o.render_pass(po, k)[0].astype(np.float64) for k in range(n_pass)]
-    eg, er = _pass_estimates(gpu_films), _pass_estimates(ref_films)
-    mg, mr = eg.mean(0), er.mean(0)
-    vg, vr = eg.var(0, ddof=1) / n_pass, er.var(0, ddof=1) / n_pass
+    eg = _pass_estimates(gpu_films)
+    mg, vg = eg.mean(0), eg.var(0, ddof=1) / n_pass
     z = (mg - mr) / np.sqrt(vg + vr)
     frac3 = float(np.mean(np.abs(z) > 3))
     z2 = float(np.mean(z ** 2))
@@ -107,9 +118,55 @@ def test_4096spp_converges_to_the_16k_oracle_render(gpu_ctx):
     scale = float(np.mean(mr))
     raw = np.sqrt(mse) / scale
     excess = np.sqrt(max(0.0, mse - noise)) / scale
-    print(f"4096-spp GPU vs 16384-spp oracle: relative RMSE {raw:.4%} (noise floor "
-          f"{np.sqrt(noise) / scale:.4%}, beyond noise {excess:.4%}); |z|>3: {frac3:.3%}; "
-          f"mean z^2 {z2:.3f}")
+    # the output images: the full film's own estimate (all 4096 spp)
+    full = prev[..., 1:] / prev[..., :1]
+    rgb_g = image.to_rgb8(_xyz_to_rgb(full)).astype(np.float64)
+    rgb_r = image.to_rgb8(_xyz_to_rgb(mr)).astype(np.float64)
+    disp = float(np.sqrt(np.mean((rgb_g - rgb_r) ** 2)) / 255.0)
+    print(f"4096-spp GPU vs 16384-spp FP64 oracle, {size}x{size}: linear relative RMSE "
+          f"{raw:.4%} (noise floor {np.sqrt(noise) / scale:.4%}, beyond noise {excess:.4%}); "
+          f"display RMSE {disp:.4%} of full scale; |z|>3: {frac3:.3%}; mean z^2 {z2:.3f}")
     assert frac3 <= 0.02, frac3
     assert 0.8 <= z2 <= 1.35, z2
     assert excess <= 0.01, excess
+    assert disp <= 0.01, disp
+
+
+def _xyz_to_rgb(xyz):
+    """xyzToRgb (Spectrum.hs:162-168) in float32, per pixel"""
+    x, y, z = (xyz[..., i].astype(np.float32) for i in range(3))
+    F = np.float32
+    r = F(3.240479) * x - F(1.537150) * y - F(0.498535) * z
+    g = F(-0.969256) * x + F(1.875991) * y + F(0.041556) * z
+    b = F(0.055648) * x - F(0.204043) * y + F(1.057311) * z
+    return np.stack([r, g, b], -1)
+
+
+def test_heightfield_full_geometry_independent_streams(gpu_ctx):
+    """the full large-mesh geometry (8.4M triangles, 4096 spheres, sky and
+    sun) at 40 x 24: 24 passes of 4 spp on each side with independent seeds;
+    per-pixel luminance means within 3 sigma for all but 2% of pixels and no
+    bias in the mean z"""
+    w, h, passes = 40, 24, 24
+    sc = S.heightfield_scene(ns=2048, n_spheres=4096, width=w, height=h, env_size=(256, 128))
+    g = gpu_ctx.scene(sc)
+    o = OracleScene(sc)
+    film = gpu_ctx.film(w, h)
+    yg, yo = [], []
+    for k in range(passes):
+        film.clear()
+        g.render_pass(film, S.heightfield_params(w, h, spp_side=2, seed=21), k)
+        fg = film.read()
+        yg.append(fg[..., 2] / fg[..., 0])
+        fo, _ = o.render_pass(S.heightfield_params(w, h, spp_side=2, seed=4242), k)
+        yo.append(fo[..., 2] / fo[..., 0])
+    yg, yo = np.asarray(yg, np.float64), np.asarray(yo, np.float64)
+    se = np.sqrt(yg.var(0, ddof=1) / passes + yo.var(0, ddof=1) / passes)
+    ok = se > 0
+    z = (yg.mean(0) - yo.mean(0))[ok] / se[ok]
+    # pixels with zero variance on both sides (pure sky) must agree exactly
+    assert np.allclose(yg.mean(0)[~ok], yo.mean(0)[~ok], rtol=1e-5)
+    print(f"heightfield 8.4M tris, 40x24, 96 spp each side: |z|>3 {np.mean(np.abs(z) > 3):.3%}, "
+          f"mean z {np.mean(z):.3f}, mean z^2 {np.mean(z ** 2):.3f}")
+    assert np.mean(np.abs(z) > 3) <= 0.02
+    assert abs(np.mean(z)) < 0.15

@@ -25,7 +25,7 @@ FIXTURES = F.fixtures()
 NAMES = [p.stem for p in FIXTURES]
 # scenes with glossy or specular paths, whose paths a last-bit difference of a
 # transcendental sends elsewhere more often
-GLOSSY = {"cornell-box-specular", "plastic-test", "trans-matte"}
+GLOSSY = {"cornell-box-specular", "plastic-test", "race", "trans-matte"}
 
 
 def reduced(job, longest=64):
@@ -66,7 +66,9 @@ def _record(job):
                 s.material, None if s.emission is None else s.emission.tobytes()]
     for lt in sc.lights:
         out += [lt.kind, np.asarray(lt.spectrum, np.float32).tobytes(),
-                np.float32(lt.vec).tobytes()]
+                np.float32(lt.vec).tobytes(), np.float32(lt.east).tobytes(),
+                np.float32(lt.turbidity).tobytes(),
+                None if lt.w2l is None else lt.w2l.m.tobytes()]
     out += [list(sc.prim_order), bytes(sc.camera), job.width, job.height, job.filter_kind]
     return out
 

@@ -377,6 +377,41 @@ def test_graph_paper_diffuse_colour_vs_oracle(gpu_ctx):
     _compare(fg, fo, rel=2e-3, frac=0.9, exact_weights=True)
 
 
+def test_first_dropped_sample_is_reported(gpu_ctx):
+    """a point light whose band 3 is NaN makes every lit sample's radiance
+    NaN, which the film drops (Image.hs:253-256); the scene statistics name
+    the pass and its lowest dropped sample (pixels row by row, then sample
+    number), which is the first non-finite sample of the oracle's replay"""
+    s = S.Scene()
+    m = s.add_material(abi.MAT_MATTE, kd=rgb_to_spectrum((0.5, 0.5, 0.5)))
+    s.add_mesh(np.array([[-4, 0, -4], [4, 0, -4], [4, 0, 4], [-4, 0, 4]], np.float32),
+               [0, 1, 2, 0, 2, 3], m)
+    bad = constant(2.0)
+    bad[3] = np.nan
+    s.lights = [S.Light(abi.LIGHT_POINT, bad, vec=(0.0, 2.0, 0.0))]
+    w, h = 24, 16
+    s.set_perspective(xf.look_at((0, 1, -6), (0, 0.9, 0), (0, 1, 0)), 0.0, 1.0, 50.0, w, h)
+    p = S.render_params(w, h, (2, 2), max_depth=2, sample_depth=3, rr_depth=3, seed=3)
+    g = gpu_ctx.scene(s)
+    assert g.stats()["nonfinite_pass"] == -1
+    film = gpu_ctx.film(w, h)
+    g.render_pass(film, p, 7)
+    st = g.stats()
+    o = OracleScene(s)
+    first, dropped = None, 0
+    for y in range(h):
+        for x in range(w):
+            for n in range(4):
+                spec = o.sample_li(p, 7, x, y, n)[2]
+                if not np.isfinite(spec).all():
+                    dropped += 1
+                    first = first or (x, y, n)
+    assert first is not None and first[1] > 0  # the top rows see only the empty sky
+    assert st["nonfinite_drops"] == dropped
+    assert st["nonfinite_pass"] == 7
+    assert (*st["nonfinite_pixel"], st["nonfinite_sample"]) == first
+
+
 def test_sunsky_light_vs_oracle(gpu_ctx):
     """the sun/sky map (SunSky.hs) evaluated on the device wherever the
     light's le and sample need it; the importance distribution over its

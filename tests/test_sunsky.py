@@ -153,9 +153,7 @@ def sunsky_scene(w=32, h=24):
     s.prim_order = [0, ~s.add_shape(abi.SHAPE_SPHERE, (1.0,), xf.translate(0, 1, 0), plastic)]
     s.lights = [S.Light(abi.LIGHT_SUNSKY, vec=(0.0, 0.3, 1.0), east=(0.0, 0.0, 1.0),
                         turbidity=12.0, w2l=xf.rotate_x(-90))]
-    c2w = xf.look_at((1, 3, -5), (0, 0.5, 0), (0, 1, 0))
-    c2w, r2c = xf.perspective_camera(c2w, 0.0, 1.0, 60.0, w, h)
-    s.set_camera(c2w, r2c)
+    s.set_perspective(xf.look_at((1, 3, -5), (0, 0.5, 0), (0, 1, 0)), 0.0, 1.0, 60.0, w, h)
     return s
 
 
