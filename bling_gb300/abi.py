@@ -44,10 +44,27 @@ class Material(C.Structure):
     _fields_ = [("kind", C.c_int32), ("sigma", C.c_float), ("roughness", C.c_float),
                 ("ior", C.c_float), ("kd", F16), ("ks", F16), ("kt", F16), ("eta", F16),
                 ("k", F16), ("kd_texture", C.c_int32), ("kd_tex_params", C.c_float * 9),
-                ("kd2", F16)]
+                ("kd2", F16), ("tex", C.c_int32 * 8), ("bump", C.c_int32),
+                ("reserved_tex", C.c_int32)]
 
 
 TEX_CONSTANT, TEX_CHECKER, TEX_GRAPH_PAPER = 0, 1, 2
+# bling_material.tex slots
+SLOT_KD, SLOT_KS, SLOT_KT, SLOT_ETA, SLOT_K, SLOT_SIGMA, SLOT_ROUGHNESS, SLOT_IOR = range(8)
+# bling_texture kinds: spectrum-valued, then scalar-valued
+TEXN_CONSTANT, TEXN_BLEND, TEXN_CHECKER, TEXN_GRAPH_PAPER, TEXN_GRADIENT, TEXN_IMAGE = range(6)
+TEXN_SCALAR, TEXN_SCALE, TEXN_PERLIN, TEXN_FBM, TEXN_CELL_NOISE, TEXN_CRYSTAL, \
+    TEXN_IMAGE_SCALAR = range(16, 23)
+MAP_UV, MAP_PLANAR, MAP_IDENTITY3D = 0, 1, 2
+DIST_EUCLIDIAN, DIST_EUCLIDIAN2, DIST_MANHATTAN, DIST_CHEBYSHEV = 0, 1, 2, 3
+TEX_MAX_DEPTH = 8
+
+
+class Texture(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("a", C.c_int32), ("b", C.c_int32), ("c", C.c_int32),
+                ("ivalue", C.c_int32), ("map_kind", C.c_int32), ("map", C.c_float * 16),
+                ("p", C.c_float * 4), ("spectrum", F16), ("data", C.POINTER(C.c_float)),
+                ("pixels", C.POINTER(C.c_uint8)), ("width", C.c_int32), ("height", C.c_int32)]
 
 
 class MeshDesc(C.Structure):
@@ -79,7 +96,9 @@ class SceneDesc(C.Structure):
                 ("shapes", C.POINTER(ShapeDesc)), ("n_shapes", C.c_int32),
                 ("materials", C.POINTER(Material)), ("n_materials", C.c_int32),
                 ("lights", C.POINTER(LightDesc)), ("n_lights", C.c_int32),
-                ("prim_order", C.POINTER(C.c_int32)), ("camera", CameraDesc)]
+                ("prim_order", C.POINTER(C.c_int32)), ("camera", CameraDesc),
+                ("textures", C.POINTER(Texture)), ("n_textures", C.c_int32),
+                ("reserved_desc", C.c_int32)]
 
 
 class RenderParams(C.Structure):

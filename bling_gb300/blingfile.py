@@ -17,13 +17,16 @@ The subset is what the GPU path renders:
   ``prim``;
 * primitives: ``mesh`` and ``shape`` (box, cylinder, disk, quad, sphere);
 * materials: matte, plastic, metal, glass, mirror, shinyMetal, transMatte,
-  with ``constant`` textures;
+  substrate, blackbody and bumpMap, every parameter a texture: constant,
+  blend, checker, gradient, graphPaper and (PNG) image spectra; constant,
+  scale, perlin, fbm, cellNoise, crystal and (PNG) image scalars; uv, planar
+  and identity mappings;
 * lights: directional, point, and infinite with a ``constant`` or ``sunSky``
   map;
 * spectra: ``rgbR``/``rgbI`` (decimal or ``%rrggbb``), ``spd { l v, ... }``,
-  ``temp``;
-* the sampler renderer (``stratified``/``random``) with the ``path``
-  integrator.
+  ``temp``, ``blackbody``;
+* the renderers ``sampler`` (``stratified``/``random`` with the ``path``
+  integrator), ``light`` and ``sppm``.
 
 Anything else raises :class:`Unsupported` naming the construct; a file whose
 renderer is not the path integrator parses, and :attr:`Job.renderer` names
@@ -38,10 +41,10 @@ from pathlib import Path
 
 import numpy as np
 
-from . import abi
+from . import abi, image
 from . import transform as xf
 from .gen_spectrum_tables import BANDS, LAMBDA_END, LAMBDA_START, f32_of_decimal, lerp
-from .scene import Light, Scene, render_params
+from .scene import Light, Scene, identity_mapping, planar_mapping, render_params, uv_mapping
 from .spectrum import constant, rgb_to_spectrum
 
 F = np.float32
@@ -49,6 +52,12 @@ F = np.float32
 
 class BlingFileError(ValueError):
     """A syntax error in a .bling file."""
+
+
+@dataclass(frozen=True)
+class _Node:
+    """a parsed texture that is not constant: its node in Scene.textures"""
+    index: int
 
 
 class Unsupported(BlingFileError):
@@ -514,109 +523,210 @@ class _Parser:
         return (self.t.flt(), self.t.flt(), self.t.flt())
 
     # -- materials (MaterialParser.hs) ----------------------------------
-    def _spectrum_texture(self, name, checker=False):
-        """a constant spectrum texture; with checker=True also `checker sx sy
-        sz tex1 {constant ..} tex2 {constant ..}` (checkerBoard,
-        MaterialParser.hs:209), returned as (tex1, ((sx, sy, sz), tex2))"""
+    # A texture parses to its constant (a spectrum or a float) when it is
+    # `constant`, else to a _Node: a node of the scene's texture expressions.
+    def _spectrum_texture(self, name):
+        """pSpectrumTexture name (MaterialParser.hs:202-226)"""
         t = self.t
+        sc = self.scene
 
         def body():
             kind = t.word()
-            if kind == "checker" and checker:
-                scale = t.vec()
-                t1 = self._spectrum_texture("tex1")
-                t2 = self._spectrum_texture("tex2")
-                return (t1, ("checker", (tuple(scale), t2)))
-            if kind == "graphPaper" and checker:  # MaterialParser.hs:220-224
+            if kind == "constant":
+                return self.p_spectrum()
+            if kind == "blend":  # spectrumBlend tex1 tex2 f
+                a = self._spectrum_texture("tex1")
+                b = self._spectrum_texture("tex2")
+                f = self._scalar_texture("f")
+                return _Node(sc.tex_blend(self._snode(a), self._snode(b), self._fnode(f)))
+            if kind == "image":
+                px, mapping = t.block(lambda: self._image(rgb=True))
+                return _Node(sc.tex_image(px, mapping))
+            if kind == "checker":
+                scale = tuple(t.vec())
+                a = self._spectrum_texture("tex1")
+                b = self._spectrum_texture("tex2")
+                return _Node(sc.tex_checker(scale, self._snode(a), self._snode(b)))
+            if kind == "gradient":
+                f = self._scalar_texture("f")
+                steps = t.named_block("steps", self._gradient_steps)
+                return _Node(sc.tex_gradient(steps, self._fnode(f)))
+            if kind == "graphPaper":
                 lw = t.flt()
-
-                def mapping():
-                    mk = t.word()
-                    if mk != "planar":
-                        raise Unsupported(f"texture mapping {mk}: graph paper takes planar mappings")
-                    return (t.vec(), t.vec(), (t.flt(), t.flt()))
-                vu, vv, off = t.named_block("map", mapping)
-                t1 = self._spectrum_texture("tex1")
-                t2 = self._spectrum_texture("tex2")
-                return (t1, ("graph", (lw, vu, vv, off, t2)))
-            if kind != "constant":
-                raise Unsupported(f"texture {kind} ({name}): the GPU path renders constant "
-                                  "textures and checkerboard diffuse colours")
-            return self.p_spectrum()
+                mapping = self._mapping2d("map")
+                a = self._spectrum_texture("tex1")
+                b = self._spectrum_texture("tex2")
+                return _Node(sc.tex_graph_paper(lw, mapping, self._snode(a), self._snode(b)))
+            raise t.error(f"unknown texture type {kind}")
         return t.named_block(name, body)
 
-    @staticmethod
-    def _kd(v):
-        """(kd, texture keyword arguments of add_material) of a kd texture"""
-        if not isinstance(v, tuple):
-            return v, {}
-        kd, (kind, args) = v
-        return kd, ({"kd_checker": args} if kind == "checker" else {"kd_graph": args})
+    def _scalar_texture(self, name):
+        """pScalarTexture name (MaterialParser.hs:120-163)"""
+        t = self.t
+        sc = self.scene
 
-    def _scalar_texture(self, name) -> np.float32:
+        def body():
+            kind = t.word()
+            if kind == "constant":
+                return t.flt()
+            if kind == "image":
+                px, mapping = t.block(lambda: self._image(rgb=False))
+                return _Node(sc.tex_image_scalar(px, mapping))
+            if kind == "cellNoise":
+                dname = t.word()
+                dists = {"euclidian": abi.DIST_EUCLIDIAN, "euclidian2": abi.DIST_EUCLIDIAN2,
+                         "manhattan": abi.DIST_MANHATTAN, "chebyshev": abi.DIST_CHEBYSHEV}
+                if dname not in dists:
+                    raise t.error(f"unknown distance function {dname}")
+                return _Node(sc.tex_cell_noise(dists[dname], self._mapping3d("map")))
+            if kind == "fbm":
+                octaves = t.named_int("octaves")
+                omega = t.named_flt("omega")
+                return _Node(sc.tex_fbm(octaves, omega, self._mapping3d("map")))
+            if kind == "perlin":
+                return _Node(sc.tex_perlin(self._mapping3d("map")))
+            if kind == "crystal":
+                octaves = t.named_int("octaves")
+                return _Node(sc.tex_crystal(octaves, self._mapping2d("map")))
+            if kind == "scale":
+                a, f = t.flt(), t.flt()
+                tex = self._scalar_texture("tex")
+                return _Node(sc.tex_scale(a, f, self._fnode(tex)))
+            raise t.error(f"unknown texture type {kind}")
+        return t.named_block(name, body)
+
+    def _snode(self, v) -> int:
+        """a spectrum texture as a node (a constant becomes one)"""
+        return v.index if isinstance(v, _Node) else self.scene.tex_constant(v)
+
+    def _fnode(self, v) -> int:
+        return v.index if isinstance(v, _Node) else self.scene.tex_scalar(v)
+
+    def _mapping2d(self, name):
+        """pTextureMapping2d (MaterialParser.hs:168-186)"""
         t = self.t
 
         def body():
             kind = t.word()
-            if kind != "constant":
-                raise Unsupported(f"texture {kind} ({name}): the GPU path renders constant "
-                                  "textures")
-            return t.flt()
+            if kind == "planar":
+                vu, vv = t.vec(), t.vec()
+                return planar_mapping(vu, vv, t.flt(), t.flt())
+            if kind == "uv":
+                su, sv, ou, ov = t.flt(), t.flt(), t.flt(), t.flt()
+                return uv_mapping(su, sv, ou, ov)
+            raise t.error(f"unknown 2d mapping {kind}")
         return t.named_block(name, body)
+
+    def _mapping3d(self, name):
+        """pTextureMapping3d: identity with its transform (MaterialParser.hs:188-194)"""
+        t = self.t
+
+        def body():
+            kind = t.word()
+            if kind != "identity":
+                raise t.error(f"unknown 3d mapping {kind}")
+            return identity_mapping(self.p_transform())
+        return t.named_block(name, body)
+
+    def _gradient_steps(self):
+        """`pos spectrum` pairs separated by commas (MaterialParser.hs:213-218)"""
+        steps = []
+        t = self.t
+        while not t.at("}"):
+            pos = t.flt()
+            steps.append((pos, self.p_spectrum()))
+            if t.at(","):
+                t.next()
+        return steps
+
+    def _image(self, rgb: bool):
+        """`file "name"` and the 2D mapping: readImageTextureMap (8-bit RGB,
+        RGBA with the alpha dropped) or readImageScalarMap (8-bit grey)
+        (Texture.hs:110-126).  PNG files only."""
+        t = self.t
+        t.expect("file")
+        kind, val, line = t.next()
+        if kind != "str":
+            raise BlingFileError(f"line {line}: expected a file name, got {val!r}")
+        path = self.s.base / val[1:-1]
+        if path.suffix.lower() != ".png":
+            raise Unsupported(f"image {path.name}: PNG images are read")
+        px = image.read_png(path)
+        if rgb:
+            if px.ndim == 2 or px.shape[2] not in (3, 4):
+                raise BlingFileError(f"line {line}: {path.name}: not an RGB image")
+            px = px[..., :3]
+        elif px.ndim != 2:
+            raise BlingFileError(f"line {line}: {path.name}: not a grey image")
+        return px, self._mapping2d("map")
 
     def p_material(self):
         self.s.material = self.t.block(self._material_body)
 
-    def _material_body(self) -> int:
+    def _material_body(self, bump=None) -> int:
+        """pMaterial' (MaterialParser.hs:28-40); `bump` the displacement node
+        of an enclosing bumpMap"""
         t = self.t
         kind = t.word()
         sc = self.scene
+        tex = {}
+
+        def val(v, slot, default):
+            """the constant of a parameter, or its node in tex"""
+            if isinstance(v, _Node):
+                tex[slot] = v.index
+                return default
+            return v
+
+        def spec(name, slot):
+            return val(self._spectrum_texture(name), slot, None)
+
+        def flt(name, slot):
+            return float(val(self._scalar_texture(name), slot, 0.0))
+
+        def add(mkind, **kw):
+            return sc.add_material(mkind, tex=tex, bump=bump, **kw)
+        if kind == "bumpMap":  # pBumpMap: bumpMapped d m (MaterialParser.hs:42-46)
+            if bump is not None:
+                raise Unsupported("material bumpMap of a bumpMap: one displacement per material")
+            d = self._scalar_texture("bump")
+            return self._material_body(bump=self._fnode(d))
         if kind == "matte":
-            kd, chk = self._kd(self._spectrum_texture("kd", checker=True))
-            sig = self._scalar_texture("sigma")
-            return sc.add_material(abi.MAT_MATTE, kd=kd, sigma=float(sig), **chk)
+            kd = spec("kd", "kd")
+            return add(abi.MAT_MATTE, kd=kd, sigma=flt("sigma", "sigma"))
         if kind == "plastic":
-            kd, chk = self._kd(self._spectrum_texture("kd", checker=True))
-            ks = self._spectrum_texture("ks")
-            rough = self._scalar_texture("rough")
-            return sc.add_material(abi.MAT_PLASTIC, kd=kd, ks=ks, roughness=float(rough), **chk)
+            kd = spec("kd", "kd")
+            ks = spec("ks", "ks")
+            return add(abi.MAT_PLASTIC, kd=kd, ks=ks, roughness=flt("rough", "roughness"))
         if kind == "metal":
-            eta = self._spectrum_texture("eta")
-            k = self._spectrum_texture("k")
-            rough = self._scalar_texture("rough")
-            return sc.add_material(abi.MAT_METAL, eta=eta, k=k, roughness=float(rough))
+            eta = spec("eta", "eta")
+            k = spec("k", "k")
+            return add(abi.MAT_METAL, eta=eta, k=k, roughness=flt("rough", "roughness"))
         if kind == "glass":
             ior = self._scalar_texture("ior")
-            kr = self._spectrum_texture("kr")
-            kt = self._spectrum_texture("kt")
-            return sc.add_material(abi.MAT_GLASS, ks=kr, kt=kt, ior=float(ior))
+            kr = spec("kr", "ks")
+            kt = spec("kt", "kt")
+            return add(abi.MAT_GLASS, ks=kr, kt=kt, ior=float(val(ior, "ior", 1.5)))
         if kind == "mirror":
-            kr = self._spectrum_texture("kr")
-            return sc.add_material(abi.MAT_MIRROR, ks=kr)
+            return add(abi.MAT_MIRROR, ks=spec("kr", "ks"))
         if kind == "shinyMetal":
-            kr = self._spectrum_texture("kr")
-            ks = self._spectrum_texture("ks")
-            rough = self._scalar_texture("rough")
-            return sc.add_material(abi.MAT_SHINY_METAL, kd=kr, ks=ks, roughness=float(rough))
+            kr = spec("kr", "kd")
+            ks = spec("ks", "ks")
+            return add(abi.MAT_SHINY_METAL, kd=kr, ks=ks, roughness=flt("rough", "roughness"))
         if kind == "transMatte":
-            kr = self._spectrum_texture("kr")
-            kt = self._spectrum_texture("kt")
-            ks = self._scalar_texture("ks")
-            return sc.add_material(abi.MAT_TRANS_MATTE, kd=kr, kt=kt, sigma=float(ks))
+            kr = spec("kr", "kd")
+            kt = spec("kt", "kt")
+            return add(abi.MAT_TRANS_MATTE, kd=kr, kt=kt, sigma=flt("ks", "sigma"))
         if kind == "substrate":  # pSubstrateMaterial (MaterialParser.hs:50-58)
-            kd, chk = self._kd(self._spectrum_texture("kd", checker=True))
-            ks = self._spectrum_texture("ks")
-            ka = self._spectrum_texture("ka")
-            ur = self._scalar_texture("urough")
-            vr = self._scalar_texture("vrough")
-            depth = self._scalar_texture("depth")
-            return sc.add_material(abi.MAT_SUBSTRATE, kd=kd, ks=ks, kt=ka, roughness=float(ur),
-                                   sigma=float(vr), ior=float(depth), **chk)
+            kd = spec("kd", "kd")
+            ks = spec("ks", "ks")
+            ka = spec("ka", "kt")
+            ur = flt("urough", "roughness")
+            vr = flt("vrough", "sigma")
+            depth = flt("depth", "ior")
+            return add(abi.MAT_SUBSTRATE, kd=kd, ks=ks, kt=ka, roughness=ur, sigma=vr, ior=depth)
         if kind == "blackbody":
-            return sc.add_material(abi.MAT_BLACKBODY)
-        if kind == "bumpMap":
-            raise Unsupported(f"material {kind}: the GPU path renders constant materials without "
-                              "bump maps")
+            return add(abi.MAT_BLACKBODY)
         raise t.error(f"unknown material type {kind}")
 
     def p_emission(self):

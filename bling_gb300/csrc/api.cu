@@ -362,6 +362,82 @@ int bling_ctx_set_stream(bling_ctx* c, void* stream) {
   return BLING_OK;
 }
 
+// ---- texture expressions: node kinds, children before parents and of the
+// right value type, mappings, sizes, depth; material slots name nodes of the
+// slot's type
+static bool tex_is_scalar(int kind) { return kind >= BLING_TEXN_SCALAR && kind <= BLING_TEXN_IMAGE_SCALAR; }
+static bool tex_is_spectrum(int kind) { return kind >= BLING_TEXN_CONSTANT && kind <= BLING_TEXN_IMAGE; }
+static bool check_textures(const bling_scene_desc& d, std::string& err) {
+  char buf[160];
+  auto fail = [&](int i, const char* what) {
+    snprintf(buf, sizeof buf, "texture %d: %s", i, what);
+    err = buf;
+    return false;
+  };
+  if (d.n_textures < 0 || (d.n_textures > 0 && !d.textures)) {
+    err = "bad texture array";
+    return false;
+  }
+  std::vector<int> depth(d.n_textures, 1);
+  for (int i = 0; i < d.n_textures; i++) {
+    const bling_texture& t = d.textures[i];
+    if (!tex_is_scalar(t.kind) && !tex_is_spectrum(t.kind)) return fail(i, "unknown kind");
+    // the children each kind reads: 'S' spectrum, 'F' scalar, '-' none
+    const char* want = "---";
+    switch (t.kind) {
+      case BLING_TEXN_BLEND: want = "SSF"; break;
+      case BLING_TEXN_CHECKER:
+      case BLING_TEXN_GRAPH_PAPER: want = "SS-"; break;
+      case BLING_TEXN_GRADIENT: want = "--F"; break;
+      case BLING_TEXN_SCALE: want = "F--"; break;
+      default: break;
+    }
+    const int ch[3] = {t.a, t.b, t.c};
+    for (int k = 0; k < 3; k++) {
+      if (want[k] == '-') continue;
+      if (ch[k] < 0 || ch[k] >= i) return fail(i, "a child must be an earlier node");
+      int ck = d.textures[ch[k]].kind;
+      if (want[k] == 'S' ? !tex_is_spectrum(ck) : !tex_is_scalar(ck))
+        return fail(i, "a child has the wrong value type");
+      depth[i] = std::max(depth[i], depth[ch[k]] + 1);
+    }
+    if (depth[i] > BLING_TEX_MAX_DEPTH) return fail(i, "deeper than BLING_TEX_MAX_DEPTH");
+    bool map2d = t.kind == BLING_TEXN_GRAPH_PAPER || t.kind == BLING_TEXN_IMAGE ||
+                 t.kind == BLING_TEXN_CRYSTAL || t.kind == BLING_TEXN_IMAGE_SCALAR;
+    bool map3d = t.kind == BLING_TEXN_PERLIN || t.kind == BLING_TEXN_FBM ||
+                 t.kind == BLING_TEXN_CELL_NOISE;
+    if (map2d && t.map_kind != BLING_MAP_UV && t.map_kind != BLING_MAP_PLANAR)
+      return fail(i, "needs a uv or planar mapping");
+    if (map3d && t.map_kind != BLING_MAP_IDENTITY3D) return fail(i, "needs an identity3d mapping");
+    if ((t.kind == BLING_TEXN_FBM || t.kind == BLING_TEXN_CRYSTAL) &&
+        (t.ivalue < 0 || t.ivalue > 64))
+      return fail(i, "octaves out of 0..64");
+    if (t.kind == BLING_TEXN_CELL_NOISE && (t.ivalue < BLING_DIST_EUCLIDIAN || t.ivalue > BLING_DIST_CHEBYSHEV))
+      return fail(i, "unknown distance function");
+    if (t.kind == BLING_TEXN_GRADIENT && (t.ivalue < 1 || !t.data))
+      return fail(i, "a gradient needs steps");
+    if ((t.kind == BLING_TEXN_IMAGE || t.kind == BLING_TEXN_IMAGE_SCALAR) &&
+        (t.width <= 0 || t.height <= 0 || !t.pixels))
+      return fail(i, "an image needs pixels");
+  }
+  for (int i = 0; i < d.n_materials; i++) {
+    const bling_material& m = d.materials[i];
+    for (int s = 0; s < 9; s++) {
+      int r = s < 8 ? m.tex[s] : m.bump;
+      if (r == 0) continue;
+      bool ok = r >= 1 && r <= d.n_textures;
+      if (ok) ok = s < 5 ? tex_is_spectrum(d.textures[r - 1].kind) : tex_is_scalar(d.textures[r - 1].kind);
+      if (!ok) {
+        snprintf(buf, sizeof buf, "material %d: %s %d names no %s texture node", i,
+                 s < 8 ? "slot" : "bump", s, s < 5 ? "spectrum" : "scalar");
+        err = buf;
+        return false;
+      }
+    }
+  }
+  return true;
+}
+
 int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** out) {
   if (!c || !d || !out) return BLING_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> g(c->mu);
@@ -387,6 +463,10 @@ int bling_scene_create(bling_ctx* c, const bling_scene_desc* d, bling_scene** ou
             d->materials[i].kind == BLING_MAT_SUBSTRATE))))
       return set_err(c, BLING_ERR_INVALID_ARG, "material %d: unknown kind %d", i,
                      d->materials[i].kind);
+  {
+    std::string terr;
+    if (!check_textures(*d, terr)) return set_err(c, BLING_ERR_INVALID_ARG, "%s", terr.c_str());
+  }
   for (int i = 0; i < d->n_meshes; i++) {
     const bling_mesh_desc& m = d->meshes[i];
     if (m.n_indices % 3 != 0)

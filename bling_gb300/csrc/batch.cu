@@ -413,6 +413,8 @@ __device__ __forceinline__ void pathsDone(bool fin, int job, BatchCtl* ctl,
   if (b && lane == 0) atomicAdd(&ctl->finished, (unsigned long long)__popc(b));
 }
 
+// TEX: some registered scene has textured materials
+template <bool TEX>
 __global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJobDev* __restrict__ jobs,
                                                 const BatchSceneDev* __restrict__ scenes,
                                                 Slots tmp, PathStates ps, BatchQueues Q,
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJob
       const BatchJobDev& J = jobs[job];
       const BatchSceneDev& SC = scenes[S.scene[q]];
       unsigned long long g = S.gidx[q];
-      o = shadeVertex(SC.A, SC.S, J.P, st, (int)q, g, S.depth[q], c, [&](const Spec& L) {
+      o = shadeVertex<TEX>(SC.A, SC.S, J.P, st, (int)q, g, S.depth[q], c, [&](const Spec& L) {
         splatSample(J.film, J.P, g, L, c, JobFilter{J.filter});
         fin = true;
       });
@@ -536,6 +538,7 @@ struct BatchEngine {
   BatchQueues q{};
   std::vector<uint64_t> scene_keys;  // scene serial numbers, by table index
   int wide = -1;  // node layout of the registered scenes
+  bool textured = false;  // some registered scene has textured materials
   // host mirror of the job table
   unsigned long long end_sample = 0, job_lo = 0, job_hi = 0;
   struct JobHost {
@@ -601,8 +604,12 @@ cudaError_t enqueueIterationT(BatchEngine* b, int use_cond, unsigned long long m
   k_bclass_count<<<b->g_bin, 128, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
   k_bin_scan<<<1, 1024, 0, s>>>(b->q.bins);
   k_bclass_scatter<<<b->g_bin, 128, 0, s>>>(b->d_ctl, b->q);
-  k_bshade<<<b->g_shade, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps, b->q,
-                                     b->d_job_done);
+  if (b->textured)
+    k_bshade<true><<<b->g_shade, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps,
+                                             b->q, b->d_job_done);
+  else
+    k_bshade<false><<<b->g_shade, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps,
+                                              b->q, b->d_job_done);
   k_btrace_shadow<LAYOUT><<<b->g_shadow, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
   k_btrace_mis<LAYOUT><<<b->g_mis, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
   k_bresolve<<<b->g_resolve, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps, b->q,
@@ -623,7 +630,7 @@ int launchShapes(BatchEngine* b, std::string& err) {
   const int bl = b->cfg.block;
   withLayout(b->wide, [&](auto L) { shapesFor<decltype(L)::value>(b, sms); });
   unsigned cap_blocks = (unsigned)std::max<int64_t>(1, (b->cap + bl - 1) / bl);
-  b->g_shade = std::min(residentBlocks(k_bshade, bl, sms), cap_blocks);
+  b->g_shade = std::min(residentBlocks(k_bshade<false>, bl, sms), cap_blocks);
   b->g_resolve = std::min(residentBlocks(k_bresolve, bl, sms), cap_blocks);
   b->g_regen = std::min(residentBlocks(k_regen, bl, sms), cap_blocks);
   b->g_bin = std::min<unsigned>((unsigned)sms * 16u,
@@ -810,6 +817,19 @@ int batch_scene(BatchEngine* b, uint64_t key, const DevAccel& A, const DevShadin
     return BLING_ERR_INVALID_ARG;
   }
   b->wide = wide;
+  if (S.textured && !b->textured) {
+    // the iteration graph was captured with the untextured shading kernel
+    b->textured = true;
+    if (b->exec) {
+      BRET(cudaStreamSynchronize(b->stream));
+      cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+    }
+    if (b->graph) {
+      cudaGraphDestroy(b->graph);
+      b->graph = nullptr;
+    }
+  }
   BatchSceneDev h;
   memset(&h, 0, sizeof h);
   h.A = A;

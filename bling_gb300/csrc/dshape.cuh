@@ -18,17 +18,21 @@ struct DShape {
   float w2o[16];
 };
 
-// the local differential geometry of a shape hit (the used fields of DG)
+// the local differential geometry of a shape hit (DifferentialGeometry.hs:26-36)
 struct DGeo {
   V3 p, n, dpdu, dpdv;
+  float u, v;
+  V3 dndu, dndv;
 };
 
 // mkDg (DifferentialGeometry.hs:41-51)
-BHD DGeo mkDg(V3 p, V3 dpdu, V3 dpdv) { return DGeo{p, normalize(cross(dpdu, dpdv)), dpdu, dpdv}; }
-// mkDg' (DifferentialGeometry.hs:53-56)
+BHD DGeo mkDg(V3 p, float u, float v, V3 dpdu, V3 dpdv, V3 dndu, V3 dndv) {
+  return DGeo{p, normalize(cross(dpdu, dpdv)), dpdu, dpdv, u, v, dndu, dndv};
+}
+// mkDg' (DifferentialGeometry.hs:53-56): u = v = 0, no normal derivatives
 BHD DGeo mkDg2(V3 p, V3 n) {
   LC c = coordinateSystem(n);
-  return DGeo{p, n, c.s, c.t};
+  return DGeo{p, n, c.s, c.t, 0.0f, 0.0f, V3{0, 0, 0}, V3{0, 0, 0}};
 }
 
 // solveQuadric (Math.hs:124-139)
@@ -150,7 +154,10 @@ BHD bool shapeIntersect(const DShape& s, const Ray& ray, float& t_out, float& e_
       if (fabsf(p.x) > sx || fabsf(p.y) > sy) return false;
       t_out = t;
       e_out = 5e-4f * t;
-      if (WANT_DG) *dg = mkDg(p, v3(sx, 0, 0), v3(0, sy, 0));
+      if (WANT_DG) {  // u, v across the quad (Shape.hs:169-171)
+        float u = (sx + p.x) / (2.0f * sx), v = (sy + p.y) / (2.0f * sy);
+        *dg = mkDg(p, u, v, v3(sx, 0, 0), v3(0, sy, 0), v3(0, 0, 0), v3(0, 0, 0));
+      }
       return true;
     }
     default: {  // sphere
@@ -176,7 +183,22 @@ BHD bool shapeIntersect(const DShape& s, const Ray& ray, float& t_out, float& e_
         V3 dpdu{-phiMax * p.y, phiMax * p.x, 0};
         float k = thetaMax - thetaMin;
         V3 dpdv = V3{p.z * cosphi, p.z * sinphi, -r * sinf(theta)} * V3{k, k, k};
-        *dg = mkDg(p, dpdu, dpdv);
+        float u = atan2p(p.y, p.x) / phiMax, v = (theta - thetaMin) / k;
+        // the normal's derivatives from the fundamental forms (Shape.hs:209-229)
+        V3 d2Pduu = V3{-phiMax * phiMax, -phiMax * phiMax, -phiMax * phiMax} * V3{p.x, p.y, 0};
+        float cuv = k * p.z * phiMax;
+        V3 d2Pduv = V3{cuv, cuv, cuv} * V3{-sinphi, cosphi, 0};
+        float cvv = -k * k;
+        V3 d2Pdvv = V3{cvv, cvv, cvv} * V3{p.x, p.y, p.z};
+        float E1 = dot(dpdu, dpdu), F1 = dot(dpdu, dpdv), G1 = dot(dpdv, dpdv);
+        V3 n1 = normalize(cross(dpdu, dpdv));
+        float e = dot(n1, d2Pduu), f = dot(n1, d2Pduv), g = dot(n1, d2Pdvv);
+        float invEGF2 = 1.0f / (E1 * G1 - F1 * F1);
+        float a = (f * F1 - e * G1) * invEGF2, b = (e * F1 - f * E1) * invEGF2;
+        float c = (g * F1 - f * G1) * invEGF2, d = (f * F1 - g * E1) * invEGF2;
+        V3 dndu = V3{a, a, a} * dpdu + V3{b, b, b} * dpdv;
+        V3 dndv = V3{c, c, c} * dpdu + V3{d, d, d} * dpdv;
+        *dg = mkDg(p, u, v, dpdu, dpdv, dndu, dndv);
       }
       return true;
     }

@@ -273,6 +273,7 @@ __global__ void __launch_bounds__(128, 10) k_trace_mis(DevAccel A, Slots st,
 }
 
 // one vertex of every live path, up to its shadow and MIS rays (Path.hs:49-87)
+template <bool TEX>
 __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, PassParams P, Slots st,
                                                Queues Q, const int32_t* __restrict__ qin,
                                                int depth, int live_in,
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, Pass
     if (q < n) {
       s = qin[q];
       uint64_t g = P.chunk_base + (uint64_t)s;  // slots never move
-      o = shadeVertex(A, S, P, st, s, g, depth, counters, [&](const Spec& L) {
+      o = shadeVertex<TEX>(A, S, P, st, s, g, depth, counters, [&](const Spec& L) {
         splatSample(film, P, g, L, counters, TableFilter{filter});
       });
     }
@@ -357,7 +358,7 @@ Grids grids(int device, int sms) {
                        residentGrid(k_trace_shadow<LAYOUT_COMPACT>, sms)});
   g.mis = std::min({residentGrid(k_trace_mis<LAYOUT_BINARY>, sms), residentGrid(k_trace_mis<LAYOUT_WIDE>, sms),
                     residentGrid(k_trace_mis<LAYOUT_COMPACT>, sms)});
-  g.shade = residentGrid(k_shade, sms);
+  g.shade = residentGrid(k_shade<false>, sms);
   g.resolve = residentGrid(k_resolve, sms);
   g.raygen = (unsigned)std::max(1, sms * 8);
   if (device >= 0 && device < 64) {
@@ -403,9 +404,12 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
     });
     k_class_count<<<G.raygen, block, 0, stream>>>(A, S, st, traced, qn, Q.cls, counters);
     k_class_scatter<<<G.raygen, block, 0, stream>>>(traced, qn, Q.cls, shaded, counters);
-    k_shade<<<std::min(G.shade, cap_blocks), block, 0, stream>>>(A, S, P, st, Q, shaded, depth,
-                                                                  C_LIVE0 + in, d_film, d_filter,
-                                                                  counters);
+    if (S.textured)
+      k_shade<true><<<std::min(G.shade, cap_blocks), block, 0, stream>>>(
+          A, S, P, st, Q, shaded, depth, C_LIVE0 + in, d_film, d_filter, counters);
+    else
+      k_shade<false><<<std::min(G.shade, cap_blocks), block, 0, stream>>>(
+          A, S, P, st, Q, shaded, depth, C_LIVE0 + in, d_film, d_filter, counters);
     withLayout(A.wide, [&](auto L) {
       k_trace_shadow<decltype(L)::value><<<gs, block, 0, stream>>>(A, st, Q.shadow, counters);
       k_trace_mis<decltype(L)::value><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);

@@ -18,6 +18,22 @@ struct DMaterial {
   int kd_tex;           // BLING_TEX_*
   float kd_par[9];      // the texture's parameters (bling_material.kd_tex_params)
   float kd2[16];        // the texture's second spectrum
+  int tex[8];           // bling_material.tex: texture node + 1 per parameter slot, 0 constant
+  int bump;             // displacement node + 1, 0 none
+  int textured;         // any tex or bump: the derived spectra are made per hit
+};
+
+// a texture node on the device (bling_texture; texture.cuh evaluates it)
+struct DTex {
+  int kind, a, b, c, ivalue, map_kind;
+  float map[16];
+  float p[4];
+  float spectrum[16];
+  // gradient: ivalue steps of 17 floats (position, spectrum), sorted by
+  // position; image: width x height spectra (pixelSpectrum of each pixel,
+  // Texture.hs:87-89); grey image: width x height values (pixel / 255)
+  const float* data;
+  int width, height;
 };
 
 // Spectra a material derives from its constant parameters, once at upload
@@ -27,15 +43,16 @@ struct DMaterial {
 //    kd) for the specular lobe (Fresnel.hs:72-78);
 //  * translucent matte (Material.hs:43-53): kd <- r = sClamp 0 1 kr,
 //    kt <- t = sClamp 0 1 kt * (white - r).
-// Haskell's clamp, min and max order (max lo (min hi x)) is kept.
-inline float ghcClamp(float x, float lo, float hi) {
+// Haskell's clamp, min and max order (max lo (min hi x)) is kept.  A
+// textured material derives them per hit, after its textures are evaluated.
+BLING_HD inline float ghcClamp(float x, float lo, float hi) {
   float m = hi <= x ? hi : x;  // min hi x
   return lo <= m ? m : lo;     // max lo m
 }
-inline void deriveMaterialSpectra(DMaterial& m) {
+BLING_HD inline void deriveMaterialSpectra(DMaterial& m) {
   if (m.kind == BLING_MAT_SHINY_METAL) {
     float kr[16];
-    memcpy(kr, m.kd, sizeof kr);
+    for (int i = 0; i < 16; i++) kr[i] = m.kd[i];
     for (int i = 0; i < 16; i++) {
       float rs = sqrtf(ghcClamp(m.ks[i], 0.0f, 0.999f));
       float refl = ghcClamp(m.ks[i], 0.0f, 0.999f);
@@ -64,8 +81,8 @@ inline void deriveMaterialSpectra(DMaterial& m) {
     }
     float u = 0.0f <= m.rough ? m.rough : 0.0f, v = 0.0f <= m.sigma ? m.sigma : 0.0f;
     float ex = 1.0f / u, ey = 1.0f / v;
-    m.rough = (ex > 10000 || std::isnan(ex)) ? 10000.0f : ex;  // fixExponent (Microfacet.hs:126-128)
-    m.sigma = (ey > 10000 || std::isnan(ey)) ? 10000.0f : ey;
+    m.rough = (ex > 10000 || ex != ex) ? 10000.0f : ex;  // fixExponent (Microfacet.hs:126-128)
+    m.sigma = (ey > 10000 || ey != ey) ? 10000.0f : ey;
   }
 }
 
@@ -101,6 +118,8 @@ struct DLight {
 
 struct DevShading {
   const DMaterial* materials;
+  const DTex* tex;  // the scene's texture nodes
+  int textured;     // some material is textured: shading kernels take the textured variant
   const DMesh* meshes;
   const int2* prim_info;   // (owner, triangle): owner >= 0 mesh, < 0 ~shape
   const float* shape_emission;  // 16 per shape

@@ -16,6 +16,7 @@
 #include "dshape.cuh"
 #include "integrator.h"
 #include "spectrum_tables.h"
+#include "texture.cuh"
 #include "trace.cuh"
 
 namespace bgpu {
@@ -618,10 +619,10 @@ struct Bsdf {
   V3 p, ng;
 };
 
-// mkBsdf' with the material's BxDFs (Material.hs:32-127)
-static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial* __restrict__ mats, int mi, V3 dgg_n, V3 dgs_p,
-                             V3 dgs_n, V3 dgs_dpdu) {
-  const DMaterial& m = mats[mi];
+// mkBsdf' with the material's BxDFs (Material.hs:32-127).  The Bsdf keeps
+// pointers into m, which must outlive it.
+static __device__ BLING_OUTLINE Bsdf materialBsdf(const DMaterial& m, V3 dgg_n, V3 dgs_p, V3 dgs_n,
+                                                  V3 dgs_dpdu) {
   Bsdf b;
   b.n = 0;
   V3 sn = normalize(dgs_dpdu);
@@ -928,8 +929,17 @@ struct HitGeom {
 
 // builds the intersection's DG for primitive `prim` hit at t (TriangleMesh.hs:182-207,
 // Geometry.hs:33-36, triangleShadingGeometry TriangleMesh.hs:122-134)
-static __device__ BLING_OUTLINE HitGeom hitGeometry(const DevAccel& A, const DevShading& S, const Ray& r, int prim,
-                               float t, float b1, float b2) {
+// the rest of the shading geometry that textured materials read: surface
+// parameters and the derivatives bump mapping tilts
+struct TexFrame {
+  float u, v;
+  V3 sdpdv, dndu, dndv;
+};
+
+template <bool FRAME>
+static __device__ __forceinline__ HitGeom hitGeometryT(const DevAccel& A, const DevShading& S,
+                                                       const Ray& r, int prim, float t, float b1,
+                                                       float b2, TexFrame* tf) {
   HitGeom g;
   int2 info = __ldg(S.prim_info + prim);
   if (info.x < 0) {
@@ -940,9 +950,17 @@ static __device__ BLING_OUTLINE HitGeom hitGeometry(const DevAccel& A, const Dev
     ro.tmax = INFINITY;
     shapeIntersect<true>(sh, ro, tt, e, &dg);
     g.eps = e;
+    // transDg o2w (DifferentialGeometry.hs:71-81)
     g.p = transPoint(sh.o2w, dg.p);
     g.n = normalize(transNormal(sh.w2o, dg.n));
     g.sdpdu = transVector(sh.o2w, dg.dpdu);
+    if (FRAME) {
+      tf->sdpdv = transVector(sh.o2w, dg.dpdv);
+      tf->dndu = transNormal(sh.w2o, dg.dndu);
+      tf->dndv = transNormal(sh.w2o, dg.dndv);
+      tf->u = dg.u;
+      tf->v = dg.v;
+    }
     g.sp = g.p;
     g.sn = g.n;
     g.material = sh.material;
@@ -985,6 +1003,13 @@ static __device__ BLING_OUTLINE HitGeom hitGeometry(const DevAccel& A, const Dev
   g.sp = g.p;
   g.sn = g.n;
   g.sdpdu = dpdu;
+  if (FRAME) {  // the interpolated (u, v) (TriangleMesh.hs:198-201); dndu = dndv = 0
+    float b0 = 1.0f - b1 - b2;
+    tf->u = b0 * uv00 + b1 * uv10 + b2 * uv20;
+    tf->v = b0 * uv01 + b1 * uv11 + b2 * uv21;
+    tf->sdpdv = dpdv;
+    tf->dndu = tf->dndv = V3{0, 0, 0};
+  }
   g.material = m.material;
   g.light_id = -1;
   g.shape = -1;
@@ -998,16 +1023,101 @@ static __device__ BLING_OUTLINE HitGeom hitGeometry(const DevAccel& A, const Dev
     V3 ns = normalize(transNormal(ident, nsp));
     V3 ssp = normalize(dpdu);
     V3 tsp = cross(ssp, ns);
-    V3 ss;
+    V3 ss, ts;
     if (sqLen(tsp) > 0) {
-      ss = cross(normalize(tsp), ns);
+      ts = normalize(tsp);
+      ss = cross(ts, ns);
     } else {
-      ss = coordinateSystem(ns).s;
+      LC c = coordinateSystem(ns);
+      ss = c.s;
+      ts = c.t;
     }
     g.sn = ns;
     g.sdpdu = ss;
+    if (FRAME) tf->sdpdv = ts;
   }
   return g;
+}
+static __device__ BLING_OUTLINE HitGeom hitGeometry(const DevAccel& A, const DevShading& S,
+                                                    const Ray& r, int prim, float t, float b1,
+                                                    float b2) {
+  return hitGeometryT<false>(A, S, r, prim, t, b1, b2, nullptr);
+}
+static __device__ BLING_OUTLINE void hitTexFrame(const DevAccel& A, const DevShading& S,
+                                                 const Ray& r, int prim, float t, float b1,
+                                                 float b2, TexFrame& tf) {
+  hitGeometryT<true>(A, S, r, prim, t, b1, b2, &tf);
+}
+
+// ------------------------------------------------------------------ textured materials
+// bump d dgg dgs (Reflection.hs:347-377): the displacement at the shading
+// point and one hundredth of a step along u and along v tilts dpdu and dpdv
+// along the shading normal; the new normal is turned to the side of the
+// geometric one.  (The shifted points' normals do not enter: textures read
+// only p, u and v.)
+static __device__ void bumpShading(const DTex* T, int d, const TexFrame& f, HitGeom& g) {
+  const float du = 0.01f, dv = 0.01f;
+  TexGeo gs{g.sp, f.u, f.v};
+  TexGeo geu{g.sp + sv(du, g.sdpdu), f.u + du, f.v};
+  TexGeo gev{g.sp + sv(dv, f.sdpdv), f.u, f.v + dv};
+  float uDisp = texScalar(T, d, geu), vDisp = texScalar(T, d, gev), disp = texScalar(T, d, gs);
+  float vscale = (vDisp - disp) / dv;
+  V3 dpdv = f.sdpdv + sv(vscale, g.sn);
+  float uscale = (uDisp - disp) / du;
+  V3 dpdu = g.sdpdu + sv(uscale, g.sn);
+  V3 nn = normalize(cross(dpdu, dpdv));
+  if (dot(nn, g.n) < 0) nn = -nn;  // faceForward nn' (dgN dgg)
+  g.sn = nn;
+  g.sdpdu = dpdu;
+}
+
+// material mi with its textures evaluated at tg (Material.hs: every texture
+// takes dgs) and its derived spectra made, in `scratch`
+static __device__ __noinline__ const DMaterial* texturedMaterial(const DevShading& S, int mi,
+                                                                  const TexGeo& tg,
+                                                                  DMaterial& scratch) {
+  const DMaterial& m = S.materials[mi];
+  scratch = m;
+  float* spectra[5] = {scratch.kd, scratch.ks, scratch.kt, scratch.eta, scratch.k};
+  for (int slot = 0; slot < 5; slot++)
+    if (m.tex[slot]) texSpectrum(S.tex, m.tex[slot] - 1, tg, spectra[slot]);
+  if (m.tex[0]) scratch.kd_tex = BLING_TEX_CONSTANT;
+  if (m.tex[5]) scratch.sigma = texScalar(S.tex, m.tex[5] - 1, tg);
+  if (m.tex[6]) scratch.rough = texScalar(S.tex, m.tex[6] - 1, tg);
+  if (m.tex[7]) scratch.ior = texScalar(S.tex, m.tex[7] - 1, tg);
+  deriveMaterialSpectra(scratch);
+  return &scratch;
+}
+
+// A textured material at hit g (prim hit by r at t, b1, b2): the bump tilts
+// g's shading frame, the textures are evaluated at the hit, the result goes
+// to `scratch`; uv, if given, receives the hit's (u, v).  Kept out of line:
+// the kernels that shade pay only for the test in hitMaterial.
+static __device__ __noinline__ const DMaterial* resolveTextured(const DevAccel& A,
+                                                                const DevShading& S, const Ray& r,
+                                                                int prim, float t, float b1,
+                                                                float b2, HitGeom& g,
+                                                                DMaterial& scratch, float* uv) {
+  const DMaterial& m = S.materials[g.material];
+  TexFrame f;
+  hitTexFrame(A, S, r, prim, t, b1, b2, f);
+  if (uv) {
+    uv[0] = f.u;
+    uv[1] = f.v;
+  }
+  if (m.bump) bumpShading(S.tex, m.bump - 1, f, g);
+  return texturedMaterial(S, g.material, TexGeo{g.sp, f.u, f.v}, scratch);
+}
+// The material of hit g: the scene's record, or for a textured material
+// (bumpMapped, or parameters that name texture nodes) its resolution at the
+// hit in `scratch`.
+__device__ __forceinline__ const DMaterial* hitMaterial(const DevAccel& A, const DevShading& S,
+                                                        const Ray& r, int prim, float t, float b1,
+                                                        float b2, HitGeom& g, DMaterial& scratch,
+                                                        float* uv = nullptr) {
+  const DMaterial* m = S.materials + g.material;
+  if (!m->textured) return m;
+  return resolveTextured(A, S, r, prim, t, b1, b2, g, scratch, uv);
 }
 
 // ------------------------------------------------------------------ lights

@@ -143,7 +143,9 @@ __global__ void __launch_bounds__(128, 10) k_lt_trace(DevAccel A, LtSlots st, in
 }
 
 // nextVertex (LightTracer.hs:73-110) of every live photon at vertex `depth`,
-// with its camera connection (connectCam, LightTracer.hs:57-71)
+// with its camera connection (connectCam, LightTracer.hs:57-71).  TEX: the
+// scene has textured materials.
+template <bool TEX>
 __global__ void __launch_bounds__(128, 4) k_lt_vertex(DevAccel A, DevShading S, LtParams P,
                                                       LtSlots st, int depth, int in,
                                                       unsigned long long* __restrict__ counters) {
@@ -173,7 +175,10 @@ __global__ void __launch_bounds__(128, 4) k_lt_vertex(DevAccel A, DevShading S, 
         float pcont = depth > 3 ? 0.8f : 1.0f;
         Ray ray = loadRay7(st.ray, s);
         HitGeom hg = hitGeometry(A, S, ray, prim, hit.x, hit.z, hit.w);
-        Bsdf bsdf = materialBsdf(S.materials, hg.material, hg.n, hg.sp, hg.sn, hg.sdpdu);
+        DMaterial tm;  // a textured material, resolved at this hit
+        const DMaterial* mat = S.materials + hg.material;
+        if constexpr (TEX) mat = hitMaterial(A, S, ray, prim, hit.x, hit.z, hit.w, hg, tm);
+        Bsdf bsdf = materialBsdf(*mat, hg.n, hg.sp, hg.sn, hg.sdpdu);
         float4 w4 = st.wi[s];
         V3 wi{w4.x, w4.y, w4.z};
         V3 p = bsdf.p;
@@ -316,7 +321,7 @@ int light_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, cons
   unsigned g_shadow = withLayout(A.wide, [&](auto L) {
     return residentGrid(k_lt_shadow<decltype(L)::value>, sms);
   });
-  unsigned g_vertex = residentGrid(k_lt_vertex, sms);
+  unsigned g_vertex = residentGrid(k_lt_vertex<false>, sms);
   unsigned g_emit = (unsigned)std::max(1, sms * 8);
   for (int64_t base = 0; base < a.photons; base += (int64_t)ws.capacity) {
     int64_t count = std::min<int64_t>((int64_t)ws.capacity, a.photons - base);
@@ -336,7 +341,10 @@ int light_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, cons
       withLayout(A.wide, [&](auto L) {
         k_lt_trace<decltype(L)::value><<<gt, block, 0, stream>>>(A, st, in, counters);
       });
-      k_lt_vertex<<<gv, block, 0, stream>>>(A, S, P, st, depth, in, counters);
+      if (S.textured)
+        k_lt_vertex<true><<<gv, block, 0, stream>>>(A, S, P, st, depth, in, counters);
+      else
+        k_lt_vertex<false><<<gv, block, 0, stream>>>(A, S, P, st, depth, in, counters);
       withLayout(A.wide, [&](auto L) {
         k_lt_shadow<decltype(L)::value><<<gs, block, 0, stream>>>(A, st, d_splat, counters);
       });

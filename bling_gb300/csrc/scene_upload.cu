@@ -81,7 +81,68 @@ int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
     o.kd_tex = m.kd_texture;
     memcpy(o.kd_par, m.kd_tex_params, 36);
     memcpy(o.kd2, m.kd2, 64);
-    deriveMaterialSpectra(o);
+    o.textured = m.bump != 0;
+    for (int k = 0; k < 8; k++) {
+      o.tex[k] = m.tex[k];
+      o.textured |= m.tex[k] != 0;
+    }
+    o.bump = m.bump;
+    if (!o.textured) deriveMaterialSpectra(o);  // textured ones derive per hit
+    out.textured |= o.textured;
+  }
+  // texture nodes, with the images and gradients they read
+  if (d.n_textures > 0) {
+    std::vector<DTex> tex(d.n_textures);
+    for (int i = 0; i < d.n_textures; i++) {
+      const bling_texture& t = d.textures[i];
+      DTex& o = tex[i];
+      memset(&o, 0, sizeof o);
+      o.kind = t.kind;
+      o.a = t.a;
+      o.b = t.b;
+      o.c = t.c;
+      o.ivalue = t.ivalue;
+      o.map_kind = t.map_kind;
+      memcpy(o.map, t.map, sizeof o.map);
+      memcpy(o.p, t.p, sizeof o.p);
+      memcpy(o.spectrum, t.spectrum, sizeof o.spectrum);
+      o.width = t.width;
+      o.height = t.height;
+      std::vector<float> data;
+      if (t.kind == BLING_TEXN_GRADIENT) {
+        // mkGradient: the steps sorted by position, ties in their given order
+        std::vector<int> idx(t.ivalue);
+        for (int k = 0; k < t.ivalue; k++) idx[k] = k;
+        std::stable_sort(idx.begin(), idx.end(),
+                         [&](int x, int y) { return t.data[17 * x] < t.data[17 * y]; });
+        data.resize((size_t)17 * t.ivalue);
+        for (int k = 0; k < t.ivalue; k++) memcpy(&data[17 * k], t.data + 17 * idx[k], 68);
+      } else if (t.kind == BLING_TEXN_IMAGE) {
+        // pixelSpectrum: rgbToSpectrumRefl (unGamma (r/255, g/255, b/255))
+        // (Texture.hs:87-89, Spectrum.hs:118-120), once per pixel
+        size_t n = (size_t)t.width * t.height;
+        data.resize(16 * n);
+        for (size_t k = 0; k < n; k++) {
+          float c[3];
+          for (int j = 0; j < 3; j++) c[j] = powf((float)t.pixels[3 * k + j] / 255.0f, 2.2f);
+          bling_rgb_to_spectrum(0, c[0], c[1], c[2], &data[16 * k]);
+        }
+      } else if (t.kind == BLING_TEXN_IMAGE_SCALAR) {  // getPixelScalar: pixel / 255
+        size_t n = (size_t)t.width * t.height;
+        data.resize(n);
+        for (size_t k = 0; k < n; k++) data[k] = (float)t.pixels[k] / 255.0f;
+      }
+      if (!data.empty()) {
+        void* p;
+        if ((rc = up(data.data(), data.size() * 4, &p))) return rc;
+        RET_CUDA(cudaStreamSynchronize(stream));  // `data` is a temporary
+        o.data = (const float*)p;
+      }
+    }
+    void* dt;
+    if ((rc = up(tex.data(), tex.size() * sizeof(DTex), &dt))) return rc;
+    RET_CUDA(cudaStreamSynchronize(stream));
+    out.tex = (const DTex*)dt;
   }
   void* dm;
   if ((rc = up(mats.data(), mats.size() * sizeof(DMaterial), &dm))) return rc;

@@ -186,6 +186,7 @@ __global__ void __launch_bounds__(128, 10) k_sp_camtrace(DevAccel A, CamNodes nb
 }
 
 // traceCam / followCam (SPPM.hs:77-131) for the nodes at tree depth `depth`
+template <bool TEX>
 __global__ void __launch_bounds__(128, 4) k_sp_camshade(DevAccel A, DevShading S, PassParams P,
                                                         SpCam cs, SpHp hp, const float* __restrict__ r2s,
                                                         int64_t stat_count, int in, int depth, int md,
@@ -198,6 +199,8 @@ __global__ void __launch_bounds__(128, 4) k_sp_camshade(DevAccel A, DevShading S
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
     bool rec = false, child[2] = {false, false};
     HitGeom hg;
+    DMaterial tm;  // a textured material, resolved at the hit
+    float huv[2] = {0.0f, 0.0f};  // its (u, v)
     Bsdf bsdf;
     Spec T;
     Ray ray;
@@ -231,7 +234,9 @@ __global__ void __launch_bounds__(128, 4) k_sp_camshade(DevAccel A, DevShading S
         if (!isBlack(L)) atomicAddBands(cs.Ls, s, L);
       } else {
         hg = hitGeometry(A, S, ray, prim, hit.x, hit.z, hit.w);
-        bsdf = materialBsdf(S.materials, hg.material, hg.n, hg.sp, hg.sn, hg.sdpdu);
+        const DMaterial* mat = S.materials + hg.material;
+        if constexpr (TEX) mat = hitMaterial(A, S, ray, prim, hit.x, hit.z, hit.w, hg, tm, huv);
+        bsdf = materialBsdf(*mat, hg.n, hg.sp, hg.sn, hg.sdpdu);
         Spec L = T * intLe(S, hg, ray.d);
         if (!isBlack(L)) atomicAddBands(cs.Ls, s, L);
         rec = bsdfHasNonSpecular(bsdf);
@@ -258,8 +263,9 @@ __global__ void __launch_bounds__(128, 4) k_sp_camshade(DevAccel A, DevShading S
       float r2 = (si >= 0 && si < stat_count) ? r2s[si] : 0.0f;
       V3 p = bsdf.p, wo = -ray.d;
       hp.p[hpos] = make_float4(p.x, p.y, p.z, r2);
-      hp.pix[hpos] = make_float4(sx, sy, __int_as_float(hg.material), 0.0f);
-      hp.w[hpos] = make_float4(wo.x, wo.y, wo.z, 0.0f);
+      // the shading geometry after any bump, and (u, v) in the spare lanes
+      hp.pix[hpos] = make_float4(sx, sy, __int_as_float(hg.material), huv[0]);
+      hp.w[hpos] = make_float4(wo.x, wo.y, wo.z, huv[1]);
       hp.ng[hpos] = make_float4(hg.n.x, hg.n.y, hg.n.z, 0.0f);
       hp.sn[hpos] = make_float4(hg.sn.x, hg.sn.y, hg.sn.z, 0.0f);
       hp.sd[hpos] = make_float4(hg.sdpdu.x, hg.sdpdu.y, hg.sdpdu.z, 0.0f);
@@ -468,6 +474,7 @@ __global__ void __launch_bounds__(128, 10) k_sp_ptrace(DevAccel A, SpPhotons ph,
 // followPhoton (SPPM.hs:195-243) at photon vertex `depth`: the hit, the
 // number of hit points its lookup finds (their splats follow in k_sp_splat)
 // and the continuation
+template <bool TEX>
 __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, PhotonParams Q,
                                                       SpPhotons ph, SpHp hp, SpHash hs, int in,
                                                       int depth,
@@ -492,7 +499,10 @@ __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, 
         Ray ray = loadRay7(ph.ray, s);
         V3 wi = -ray.d;
         HitGeom hg = hitGeometry(A, S, ray, prim, hit.x, hit.z, hit.w);
-        Bsdf bsdf = materialBsdf(S.materials, hg.material, hg.n, hg.sp, hg.sn, hg.sdpdu);
+        DMaterial tm;  // a textured material, resolved at this hit
+        const DMaterial* mat = S.materials + hg.material;
+        if constexpr (TEX) mat = hitMaterial(A, S, ray, prim, hit.x, hit.z, hit.w, hg, tm);
+        Bsdf bsdf = materialBsdf(*mat, hg.n, hg.sp, hg.sn, hg.sdpdu);
         V3 p = bsdf.p;
         long long b = -1;
         if (bsdfHasNonSpecular(bsdf) && hs.cnt > 0) {
@@ -528,6 +538,7 @@ __global__ void __launch_bounds__(128, 4) k_sp_vertex(DevAccel A, DevShading S, 
 // the splat of one (photon, hit point) pair: hpF * f * li / (|wi.ng| r^2 pi)
 // at the hit point's pixel (splatSample, Image.hs:201-221), and the photon
 // count of that pixel
+template <bool TEX>
 __device__ __forceinline__ void splatPair(const DevShading& S, const PassParams& P,
                                           const SpPhotons& ph, const SpHp& hp, const float* li_in,
                                           int s, int h, float* __restrict__ splat,
@@ -537,8 +548,15 @@ __device__ __forceinline__ void splatPair(const DevShading& S, const PassParams&
   V3 wi{gw.x, gw.y, gw.z};
   float4 hpp = hp.p[h], pix = hp.pix[h], w4 = hp.w[h], ng4 = hp.ng[h], sn4 = hp.sn[h], sd4 = hp.sd[h];
   float r2 = hpp.w;
-  Bsdf hb = materialBsdf(S.materials, __float_as_int(pix.z), V3{ng4.x, ng4.y, ng4.z},
-                         V3{hpp.x, hpp.y, hpp.z}, V3{sn4.x, sn4.y, sn4.z}, V3{sd4.x, sd4.y, sd4.z});
+  // the hit point's material: a textured one re-evaluated at its stored
+  // shading point and (u, v), its bump already in the stored frame
+  int mi = __float_as_int(pix.z);
+  DMaterial tm;
+  const DMaterial* mat = S.materials + mi;
+  if constexpr (TEX)
+    if (mat->textured) mat = texturedMaterial(S, mi, TexGeo{V3{hpp.x, hpp.y, hpp.z}, pix.w, w4.w}, tm);
+  Bsdf hb = materialBsdf(*mat, V3{ng4.x, ng4.y, ng4.z}, V3{hpp.x, hpp.y, hpp.z},
+                         V3{sn4.x, sn4.y, sn4.z}, V3{sd4.x, sd4.y, sd4.z});
   Spec f = evalBsdf<false>(hb, V3{w4.x, w4.y, w4.z}, wi);
   Spec l = sScale(loadBands(hp.F, h) * f * loadBands(li_in, s), 1.0f / (gw.w * r2 * kPi));
   float px = pix.x, py = pix.y;
@@ -572,6 +590,7 @@ __device__ __forceinline__ void splatPair(const DevShading& S, const PassParams&
 // points within their radius go to the warp's queue in shared memory, and
 // every 32 queued pairs are splatted by the whole warp (one pair per lane).
 constexpr int kGatherBlock = 128;
+template <bool TEX>
 __global__ void __launch_bounds__(kGatherBlock) k_sp_gather(DevShading S, PassParams P, SpPhotons ph,
                                                             SpHp hp, SpHash hs, int in, int depth,
                                                             float* __restrict__ splat,
@@ -608,7 +627,7 @@ __global__ void __launch_bounds__(kGatherBlock) k_sp_gather(DevShading S, PassPa
       __syncwarp();
       if (qn >= 32) {  // a full warp of splats, then the rest to the front of the queue
         int2 pr = wq[lane];
-        splatPair(S, P, ph, hp, li_in, pr.x, pr.y, splat, m, stat_count, counters);
+        splatPair<TEX>(S, P, ph, hp, li_in, pr.x, pr.y, splat, m, stat_count, counters);
         __syncwarp();
         int2 rest = lane + 32 < qn ? wq[lane + 32] : make_int2(0, 0);
         __syncwarp();
@@ -620,7 +639,7 @@ __global__ void __launch_bounds__(kGatherBlock) k_sp_gather(DevShading S, PassPa
   }
   if (lane < qn) {
     int2 pr = wq[lane];
-    splatPair(S, P, ph, hp, li_in, pr.x, pr.y, splat, m, stat_count, counters);
+    splatPair<TEX>(S, P, ph, hp, li_in, pr.x, pr.y, splat, m, stat_count, counters);
   }
 }
 
@@ -773,7 +792,7 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
   unsigned g_trace = withLayout(A.wide, [&](auto L) {
     return residentGrid(k_sp_camtrace<decltype(L)::value>, sms, block);
   });
-  unsigned g_shade = residentGrid(k_sp_camshade, sms, block);
+  unsigned g_shade = residentGrid(k_sp_camshade<false>, sms, block);
   unsigned g_wide = (unsigned)std::max(1, sms * 8);
 
   // ---- 1. camera pass, in chunks of samples; a chunk whose node queue or
@@ -814,8 +833,12 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
         k_sp_camtrace<decltype(L)::value><<<std::min(g_trace, nb), block, 0, stream>>>(
             A, cs.nb[in], in, cs.NC, counters);
       });
-      k_sp_camshade<<<std::min(g_shade, nb), block, 0, stream>>>(A, S, P, cs, hp, px.r2, px.count, in, d,
-                                                               a.max_depth, counters);
+      if (S.textured)
+        k_sp_camshade<true><<<std::min(g_shade, nb), block, 0, stream>>>(
+            A, S, P, cs, hp, px.r2, px.count, in, d, a.max_depth, counters);
+      else
+        k_sp_camshade<false><<<std::min(g_shade, nb), block, 0, stream>>>(
+            A, S, P, cs, hp, px.r2, px.count, in, d, a.max_depth, counters);
       RET_CUDA(cudaGetLastError());
     }
     unsigned long long c2[S_COUNT];
@@ -945,7 +968,7 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
     unsigned g_pt = withLayout(A.wide, [&](auto L) {
       return residentGrid(k_sp_ptrace<decltype(L)::value>, sms, block);
     });
-    unsigned g_vx = residentGrid(k_sp_vertex, sms, block);
+    unsigned g_vx = residentGrid(k_sp_vertex<false>, sms, block);
     for (int64_t base = 0; base < nphot; base += (int64_t)ws.photon_cap) {
       int64_t count = std::min<int64_t>((int64_t)ws.photon_cap, nphot - base);
       Q.chunk_base = (uint64_t)base;
@@ -962,11 +985,18 @@ int sppm_pass(cudaStream_t stream, const DevAccel& A, const DevShading& S, const
           k_sp_ptrace<decltype(L)::value><<<std::min(g_pt, cap_blocks), block, 0, stream>>>(
               A, ph, in, counters);
         });
-        k_sp_vertex<<<std::min(g_vx, cap_blocks), block, 0, stream>>>(A, S, Q, ph, hp, hs, in, depth,
-                                                                     counters);
         unsigned warp_blocks = (unsigned)std::max<int64_t>(1, (n_cur + 3) / 4);  // 4 warps a block
-        k_sp_gather<<<std::min(g_wide * 2, warp_blocks), kGatherBlock, 0, stream>>>(
-            S, P, ph, hp, hs, in, depth, d_splat, px.m, px.count, counters);
+        if (S.textured) {
+          k_sp_vertex<true><<<std::min(g_vx, cap_blocks), block, 0, stream>>>(
+              A, S, Q, ph, hp, hs, in, depth, counters);
+          k_sp_gather<true><<<std::min(g_wide * 2, warp_blocks), kGatherBlock, 0, stream>>>(
+              S, P, ph, hp, hs, in, depth, d_splat, px.m, px.count, counters);
+        } else {
+          k_sp_vertex<false><<<std::min(g_vx, cap_blocks), block, 0, stream>>>(
+              A, S, Q, ph, hp, hs, in, depth, counters);
+          k_sp_gather<false><<<std::min(g_wide * 2, warp_blocks), kGatherBlock, 0, stream>>>(
+              S, P, ph, hp, hs, in, depth, d_splat, px.m, px.count, counters);
+        }
         RET_CUDA(cudaGetLastError());
         unsigned long long live = (unsigned long long)n_cur;
         if (depth >= 3 && (depth & 3) == 3) {  // the live count, every fourth bounce

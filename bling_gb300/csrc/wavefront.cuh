@@ -323,8 +323,9 @@ struct VertexOut {
 // and one BSDF sample for MIS (sampleOneLight/estimateDirect,
 // Scene.hs:61-118), Russian roulette and the continuation sample.  Stores
 // the deferred terms in the slot and says which rays to trace; a path that
-// ends here is handed to finish(L).
-template <class Finish>
+// ends here is handed to finish(L).  TEX: the scene has textured materials
+// (the variant without them makes no out-of-line call).
+template <bool TEX, class Finish>
 __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevShading& S,
                                                  const PassParams& P, const Slots& st, int s,
                                                  uint64_t g, int depth,
@@ -356,17 +357,20 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
     return out;
   }
   float thit = hit.x, b1 = hit.z, b2 = hit.w;
+  HitGeom gm = hitGeometry(A, S, ray, prim, thit, b1, b2);
+  V3 rd = ray.d;
+  storeBands(st.intl, s, specular ? intLe(S, gm, rd) : sConst(0));
+  DMaterial tm;  // a textured material, resolved at this hit
+  const DMaterial* mat = S.materials + gm.material;
+  if constexpr (TEX) mat = hitMaterial(A, S, ray, prim, thit, b1, b2, gm, tm);
+  V3 wo = -rd;
   float lNumU = rnd1(smp, 1 + 4 * depth);
   float ld1, ld2;
   rnd2(smp, 1 + 3 * depth, ld1, ld2);
   float lBsdfCompU = rnd1(smp, 2 + 4 * depth);
   float lb1, lb2;
   rnd2(smp, 2 + 3 * depth, lb1, lb2);
-  HitGeom gm = hitGeometry(A, S, ray, prim, thit, b1, b2);
-  V3 rd = ray.d;
-  storeBands(st.intl, s, specular ? intLe(S, gm, rd) : sConst(0));
-  V3 wo = -rd;
-  Bsdf bsdf = materialBsdf(S.materials, gm.material, gm.n, gm.sp, gm.sn, gm.sdpdu);
+  Bsdf bsdf = materialBsdf(*mat, gm.n, gm.sp, gm.sn, gm.sdpdu);
   V3 nn = bsdf.cs.n, p = bsdf.p;
   float eps = gm.eps;
   int flags = 0;

@@ -17,8 +17,10 @@ the ones a GHC build of the reference holds in memory:
   ``floor(n * ((l - s0) / (s1 - s0)))`` clamped to ``[0, n]``, summed left to
   right (``V.sum`` is a strict left fold).
 
-It only needs the reference's ``Spectrum.hs`` as text and is run once, in a
-checkout that has it; the generated header is committed::
+It also copies Perlin's noise permutation (``noisePerms``) out of the
+``Texture.hs`` beside ``Spectrum.hs``.  It only needs those two files as
+text and is run once, in a checkout that has them; the generated header is
+committed::
 
     python bling_gb300/gen_spectrum_tables.py /path/to/bling/src/lib/Graphics/Bling/Spectrum.hs
 """
@@ -231,6 +233,20 @@ def main(argv):
     emit("BLING_RGB_ILLUM_BITS", [v for t in illum for v in t])
     lines.append("/* X, Y, Z of the CIE daylight components S0, S1, S2 (spdToXYZ) */")
     emit("BLING_CIE_S012_XYZ_BITS", s012)
+    # Perlin's permutation of noisePerms (Texture.hs:395-413), the list l of
+    # `V.fromList (l ++ l)`; its second copy is index & 255
+    tex = src_path.with_name("Texture.hs").read_text()
+    m = re.search(r"^noisePerms\s*=.*?where\s*l\s*=\s*\[(.*?)\]", tex, re.S | re.M)
+    if not m:
+        raise SystemExit("noisePerms not found in Texture.hs")
+    perm = [int(t) for t in m.group(1).replace("\n", " ").split(",") if t.strip()]
+    assert sorted(perm) == list(range(256)), "noisePerms is not a permutation of 0..255"
+    lines.append("/* noisePerms' permutation of 0..255 (Texture.hs:395-413), as an")
+    lines.append(" * initializer list for host and device arrays */")
+    lines.append("#define BLING_NOISE_PERM_LIST \\")
+    for k in range(0, 256, 16):
+        tail = ", \\" if k + 16 < 256 else ""
+        lines.append("   " + ", ".join(str(v) for v in perm[k:k + 16]) + tail)
     lines.append("")
     out_path.write_text("\n".join(lines) + "\n")
     print(f"wrote {out_path}")

@@ -27,7 +27,7 @@
 module Graphics.Bling.IO.GpuScene (
    -- * The flat scene
    FlatScene(..), FlatPrim(..), FlatMesh(..), FlatShape(..), FlatMaterial(..),
-   FlatLight(..), FlatCamera(..), emptyFlatScene,
+   FlatLight(..), FlatCamera(..), FlatTexture(..), emptyFlatScene,
 
    -- * Marshalling
    SceneDesc, RenderParams(..), withSceneDesc, withRenderParams,
@@ -59,7 +59,9 @@ bands = #{const BLING_BANDS}
 -- | @bling_material@: kind (@BLING_MAT_*@), scalars and 16-band spectra;
 --   the diffuse colour of matte, plastic and substrate may be a checker
 --   board or graph paper of two spectra (@kd_texture@, @kd_tex_params@,
---   @kd2@)
+--   @kd2@).  Any parameter may instead name a texture of 'fsTextures'
+--   ('fmTex', slot @BLING_SLOT_*@, node index + 1, 0 for the constant), and
+--   'fmBump' the displacement of @bumpMapped@ (node index + 1, or 0)
 data FlatMaterial = FlatMaterial
    { fmKind        :: !Int32
    , fmSigma       :: !Float
@@ -73,6 +75,25 @@ data FlatMaterial = FlatMaterial
    , fmKdTexture   :: !Int32
    , fmKdTexParams :: ![Float]   -- ^ 9 entries
    , fmKd2         :: ![Float]
+   , fmTex         :: ![Int32]   -- ^ 8 entries
+   , fmBump        :: !Int32
+   } deriving (Show, Eq)
+
+-- | @bling_texture@: one node of a texture expression (@BLING_TEXN_*@),
+--   its children by index into 'fsTextures' (each before its parent), the
+--   mapping, its numbers, and the pixels of an image (8-bit RGB or grey,
+--   rows top to bottom) or the steps of a gradient (position and spectrum,
+--   17 floats each)
+data FlatTexture = FlatTexture
+   { ftKind     :: !Int32
+   , ftChildren :: !(Int32, Int32, Int32)
+   , ftIValue   :: !Int32
+   , ftMapKind  :: !Int32
+   , ftMap      :: ![Float]  -- ^ 16 entries
+   , ftP        :: ![Float]  -- ^ 4 entries
+   , ftSpectrum :: ![Float]
+   , ftSteps    :: !(Maybe (SV.Vector Float))
+   , ftPixels   :: !(Maybe (Int32, Int32, SV.Vector Word8))
    } deriving (Show, Eq)
 
 -- | @bling_mesh_desc@: world-space vertices (3 per vertex), indices (a
@@ -129,13 +150,14 @@ data FlatCamera = FlatCamera
 
 data FlatScene = FlatScene
    { fsMaterials :: ![FlatMaterial]  -- ^ indexed by the primitives' material
+   , fsTextures  :: ![FlatTexture]   -- ^ indexed by the materials' 'fmTex' and 'fmBump'
    , fsPrims     :: ![FlatPrim]      -- ^ newest first, as @prims@ of PState
    , fsLights    :: ![FlatLight]     -- ^ newest first, as @lights@ of PState
    , fsCamera    :: !FlatCamera
    } deriving (Show, Eq)
 
 emptyFlatScene :: FlatCamera -> FlatScene
-emptyFlatScene = FlatScene [] [] []
+emptyFlatScene = FlatScene [] [] [] []
 
 --------------------------------------------------------------------------------
 -- Storable instances of the fixed-size records
@@ -164,6 +186,9 @@ instance Storable FlatMaterial where
       #{poke bling_material, kd_texture} p (fmKdTexture m)
       pokeFloats (#{ptr bling_material, kd_tex_params} p) 9 (fmKdTexParams m)
       pokeFloats (#{ptr bling_material, kd2} p) bands (fmKd2 m)
+      pokeArray (#{ptr bling_material, tex} p) (take 8 (fmTex m ++ repeat 0))
+      #{poke bling_material, bump} p (fmBump m)
+      #{poke bling_material, reserved_tex} p (0 :: Int32)
    peek p = FlatMaterial
       <$> #{peek bling_material, kind} p
       <*> (unF <$> #{peek bling_material, sigma} p)
@@ -177,6 +202,8 @@ instance Storable FlatMaterial where
       <*> #{peek bling_material, kd_texture} p
       <*> peekFloats (#{ptr bling_material, kd_tex_params} p) 9
       <*> peekFloats (#{ptr bling_material, kd2} p) bands
+      <*> peekArray 8 (#{ptr bling_material, tex} p)
+      <*> #{peek bling_material, bump} p
 
 unF :: CFloat -> Float
 unF = realToFrac
@@ -309,6 +336,30 @@ pokeMesh p (m, pv, pi', pn, pu) = do
    #{poke bling_mesh_desc, material} p (fmeshMaterial m)
    #{poke bling_mesh_desc, reserved} p (0 :: Int32)
 
+withTextures :: [FlatTexture] -> ([(FlatTexture, Ptr Float, Ptr Word8)] -> IO a) -> IO a
+withTextures [] k = k []
+withTextures (t:ts) k =
+   withVec (ftSteps t) $ \ps ->
+   withVec (fmap (\(_, _, v) -> v) (ftPixels t)) $ \px ->
+   withTextures ts $ \rest -> k ((t, ps, px) : rest)
+
+pokeTexture :: Ptr () -> (FlatTexture, Ptr Float, Ptr Word8) -> IO ()
+pokeTexture p (t, ps, px) = do
+   let (a, b, c) = ftChildren t
+   #{poke bling_texture, kind} p (ftKind t)
+   #{poke bling_texture, a} p a
+   #{poke bling_texture, b} p b
+   #{poke bling_texture, c} p c
+   #{poke bling_texture, ivalue} p (ftIValue t)
+   #{poke bling_texture, map_kind} p (ftMapKind t)
+   pokeFloats (#{ptr bling_texture, map} p) 16 (ftMap t)
+   pokeFloats (#{ptr bling_texture, p} p) 4 (ftP t)
+   pokeFloats (#{ptr bling_texture, spectrum} p) bands (ftSpectrum t)
+   #{poke bling_texture, data} p ps
+   #{poke bling_texture, pixels} p px
+   #{poke bling_texture, width} p (maybe 0 (\(w, _, _) -> w) (ftPixels t))
+   #{poke bling_texture, height} p (maybe 0 (\(_, h, _) -> h) (ftPixels t))
+
 pokeLight :: Ptr () -> (FlatLight, Ptr Float) -> IO ()
 pokeLight p (l, pe) = do
    #{poke bling_light_desc, kind} p (flKind l)
@@ -330,6 +381,8 @@ withSceneDesc :: FlatScene -> (Ptr SceneDesc -> IO a) -> IO a
 withSceneDesc sc k =
    withMeshes meshes $ \ms ->
    withEnvs (fsLights sc) $ \envs ->
+   withTextures (fsTextures sc) $ \txs ->
+   allocaBytes (max 1 (length txs) * #{size bling_texture}) $ \pTex ->
    allocaBytes (max 1 (length ms) * #{size bling_mesh_desc}) $ \pMeshes ->
    allocaArray (max 1 (length shapes)) $ \pShapes ->
    allocaArray (max 1 (length (fsMaterials sc))) $ \pMats ->
@@ -342,6 +395,7 @@ withSceneDesc sc k =
       pokeArray pMats (fsMaterials sc)
       zipWithM_ (\i le -> pokeLight (pLights `plusPtr` (i * #{size bling_light_desc})) le)
                 [0 ..] (zip (fsLights sc) envs)
+      zipWithM_ (\i t -> pokeTexture (pTex `plusPtr` (i * #{size bling_texture})) t) [0 ..] txs
       #{poke bling_scene_desc, meshes} d pMeshes
       #{poke bling_scene_desc, n_meshes} d (fromIntegral (length ms) :: Int32)
       #{poke bling_scene_desc, shapes} d pShapes
@@ -352,6 +406,9 @@ withSceneDesc sc k =
       #{poke bling_scene_desc, n_lights} d (fromIntegral (length (fsLights sc)) :: Int32)
       #{poke bling_scene_desc, prim_order} d pOrder
       #{poke bling_scene_desc, camera} d (fsCamera sc)
+      #{poke bling_scene_desc, textures} d pTex
+      #{poke bling_scene_desc, n_textures} d (fromIntegral (length txs) :: Int32)
+      #{poke bling_scene_desc, reserved_desc} d (0 :: Int32)
       k (castPtr d)
    where
       meshes = [m | PrimMesh m <- fsPrims sc]

@@ -78,27 +78,69 @@ def write_png(path: str | Path, rgb8: np.ndarray) -> None:
     Path(path).write_bytes(png)
 
 
+def _paeth(a: int, b: int, c: int) -> int:
+    """the Paeth predictor (PNG specification, filter type 4)"""
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    if pa <= pb and pa <= pc:
+        return a
+    return b if pb <= pc else c
+
+
 def read_png(path: str | Path) -> np.ndarray:
-    """Reads back an 8-bit RGB PNG with filter type 0 (as write_png writes)."""
+    """Reads an 8-bit, non-interlaced PNG (RFC 2083): grey (h, w), grey with
+    alpha (h, w, 2), RGB (h, w, 3), RGBA (h, w, 4), or a palette image as RGB.
+    Every scanline filter (none, sub, up, average, Paeth) is undone."""
     data = Path(path).read_bytes()
     if data[:8] != b"\x89PNG\r\n\x1a\n":
         raise ValueError("not a PNG file")
-    pos, idat, w, h = 8, b"", 0, 0
+    pos, idat, w, h, ctype, palette = 8, b"", 0, 0, 0, None
     while pos < len(data):
         (n,) = struct.unpack(">I", data[pos:pos + 4])
         kind, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
         if kind == b"IHDR":
-            w, h, depth, ctype = struct.unpack(">IIBB", body[:10])
-            if (depth, ctype) != (8, 2):
-                raise ValueError("only 8-bit RGB PNGs are read")
+            w, h, depth, ctype, _, _, interlace = struct.unpack(">IIBBBBB", body[:13])
+            if depth != 8 or interlace != 0 or ctype not in (0, 2, 3, 4, 6):
+                raise ValueError("only 8-bit, non-interlaced PNGs are read")
+        elif kind == b"PLTE":
+            palette = np.frombuffer(body, np.uint8).reshape(-1, 3)
         elif kind == b"IDAT":
             idat += body
+        elif kind == b"IEND":
+            break
         pos += 12 + n
-    raw = zlib.decompress(idat)
-    rows = np.frombuffer(raw, np.uint8).reshape(h, 1 + 3 * w)
-    if np.any(rows[:, 0] != 0):
-        raise ValueError("only filter type 0 is read")
-    return rows[:, 1:].reshape(h, w, 3).copy()
+    ch = {0: 1, 2: 3, 3: 1, 4: 2, 6: 4}[ctype]
+    stride = w * ch
+    raw = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(h, 1 + stride)
+    out = np.zeros((h, stride), np.uint8)
+    prev = np.zeros(stride, np.int32)
+    for y in range(h):
+        ft, line = raw[y, 0], raw[y, 1:].astype(np.int32)
+        if ft == 0:
+            cur = line
+        elif ft == 2:
+            cur = (line + prev) & 255
+        else:  # sub, average and Paeth read the reconstructed bytes to the left
+            cur = np.zeros(stride, np.int32)
+            for i in range(stride):
+                left = cur[i - ch] if i >= ch else 0
+                if ft == 1:
+                    pred = left
+                elif ft == 3:
+                    pred = (left + prev[i]) >> 1
+                elif ft == 4:
+                    pred = _paeth(left, prev[i], prev[i - ch] if i >= ch else 0)
+                else:
+                    raise ValueError(f"unknown PNG filter type {ft}")
+                cur[i] = (line[i] + pred) & 255
+        out[y] = cur
+        prev = cur
+    img = out.reshape(h, w, ch)
+    if ctype == 3:
+        if palette is None:
+            raise ValueError("palette PNG without PLTE")
+        return palette[img[..., 0]].copy()
+    return img[..., 0].copy() if ch == 1 else img.copy()
 
 
 def rgbe_encode(rgb: np.ndarray) -> np.ndarray:

@@ -60,8 +60,43 @@ class Light:
 
 
 @dataclass
+class Texture:
+    """one node of a texture expression (bling_texture, Texture.hs)"""
+    kind: int
+    children: tuple = (-1, -1, -1)
+    ivalue: int = 0
+    mapping: tuple = (abi.MAP_UV, ())   # (BLING_MAP_*, numbers) of the node's mapping
+    p: tuple = ()
+    spectrum: np.ndarray | None = None
+    steps: np.ndarray | None = None      # gradient: (n, 17) float32 (position, spectrum)
+    pixels: np.ndarray | None = None     # image: (h, w, 3) or (h, w) uint8, rows top to bottom
+
+
+# texture mappings (Texture.hs:147-176)
+def uv_mapping(su=1.0, sv=1.0, ou=0.0, ov=0.0) -> tuple:
+    """uvMapping (su, sv) (ou, ov)"""
+    return (abi.MAP_UV, (su, sv, ou, ov))
+
+
+def planar_mapping(vu, vv, ou=0.0, ov=0.0) -> tuple:
+    """planarMapping (vu, vv) (ou, ov)"""
+    return (abi.MAP_PLANAR, (*vu, *vv, ou, ov))
+
+
+def identity_mapping(w2t: xf.Transform | None = None) -> tuple:
+    """identityMapping3d w2t: the world-to-texture transform of the point"""
+    return (abi.MAP_IDENTITY3D, tuple((w2t or xf.identity()).m.tolist()))
+
+
+SLOTS = {"kd": abi.SLOT_KD, "ks": abi.SLOT_KS, "kt": abi.SLOT_KT, "eta": abi.SLOT_ETA,
+         "k": abi.SLOT_K, "sigma": abi.SLOT_SIGMA, "roughness": abi.SLOT_ROUGHNESS,
+         "ior": abi.SLOT_IOR}
+
+
+@dataclass
 class Scene:
     materials: list = field(default_factory=list)
+    textures: list = field(default_factory=list)
     meshes: list = field(default_factory=list)
     shapes: list = field(default_factory=list)
     lights: list = field(default_factory=list)
@@ -71,11 +106,15 @@ class Scene:
 
     # --- builders -------------------------------------------------------
     def add_material(self, kind, kd=None, ks=None, kt=None, eta=None, k=None, sigma=0.0,
-                     roughness=0.0, ior=1.5, kd_checker=None, kd_graph=None) -> int:
+                     roughness=0.0, ior=1.5, kd_checker=None, kd_graph=None, tex=None,
+                     bump=None) -> int:
         """kd_checker: (scale (sx, sy, sz), second spectrum) makes kd the
         checkerBoard scale kd kd2 texture (Texture.hs:209-219); kd_graph:
         (lw, vu, vv, (ou, ov), line spectrum) makes it graphPaper lw
-        (planarMapping (vu, vv) (ou, ov)) kd lines (Texture.hs:172-207)"""
+        (planarMapping (vu, vv) (ou, ov)) kd lines (Texture.hs:172-207).
+        tex: {slot name: texture node} for the parameters given by texture
+        expressions (slot names of SLOTS); bump: the scalar node of
+        bumpMapped (Reflection.hs:344-377)."""
         m = abi.Material()
         m.kind, m.sigma, m.roughness, m.ior = kind, sigma, roughness, ior
         for name, v in (("kd", kd), ("ks", ks), ("kt", kt), ("eta", eta), ("k", k)):
@@ -91,8 +130,70 @@ class Scene:
             m.kd_texture = abi.TEX_GRAPH_PAPER
             m.kd_tex_params[:] = [float(np.float32(x)) for x in [lw, *vu, *vv, ou, ov]]
             m.kd2[:] = np.asarray(lines, np.float32).tolist()
+        for name, node in (tex or {}).items():
+            m.tex[SLOTS[name]] = node + 1
+        if bump is not None:
+            m.bump = bump + 1
         self.materials.append(m)
         return len(self.materials) - 1
+
+    # --- texture expressions: each returns the node's index ----------------
+    def add_texture(self, t: Texture) -> int:
+        self.textures.append(t)
+        return len(self.textures) - 1
+
+    def tex_constant(self, spectrum) -> int:
+        return self.add_texture(Texture(abi.TEXN_CONSTANT, spectrum=np.asarray(spectrum, np.float32)))
+
+    def tex_scalar(self, v) -> int:
+        return self.add_texture(Texture(abi.TEXN_SCALAR, p=(v,)))
+
+    def tex_blend(self, a, b, f) -> int:
+        """spectrumBlend a b f"""
+        return self.add_texture(Texture(abi.TEXN_BLEND, (a, b, f)))
+
+    def tex_checker(self, scale, a, b) -> int:
+        """checkerBoard (sx, sy, sz) a b"""
+        return self.add_texture(Texture(abi.TEXN_CHECKER, (a, b, -1), p=tuple(scale)))
+
+    def tex_graph_paper(self, lw, mapping, paper, lines) -> int:
+        return self.add_texture(Texture(abi.TEXN_GRAPH_PAPER, (paper, lines, -1), mapping=mapping,
+                                        p=(lw,)))
+
+    def tex_gradient(self, steps, f) -> int:
+        """gradient (mkGradient [(position, spectrum)]) f"""
+        st = np.array([[pos, *np.asarray(sp, np.float32)] for pos, sp in steps], np.float32)
+        return self.add_texture(Texture(abi.TEXN_GRADIENT, (-1, -1, f), ivalue=len(steps), steps=st))
+
+    def tex_image(self, pixels, mapping) -> int:
+        """imageTexture of an 8-bit RGB image, (h, w, 3)"""
+        px = np.ascontiguousarray(pixels, np.uint8)
+        assert px.ndim == 3 and px.shape[2] == 3
+        return self.add_texture(Texture(abi.TEXN_IMAGE, mapping=mapping, pixels=px))
+
+    def tex_image_scalar(self, pixels, mapping) -> int:
+        """imageTexture of an 8-bit grey image, (h, w)"""
+        px = np.ascontiguousarray(pixels, np.uint8)
+        assert px.ndim == 2
+        return self.add_texture(Texture(abi.TEXN_IMAGE_SCALAR, mapping=mapping, pixels=px))
+
+    def tex_scale(self, a, s, t) -> int:
+        """scaleTexture a s t: a + s * t"""
+        return self.add_texture(Texture(abi.TEXN_SCALE, (t, -1, -1), p=(a, s)))
+
+    def tex_perlin(self, mapping3d=None) -> int:
+        return self.add_texture(Texture(abi.TEXN_PERLIN, mapping=mapping3d or identity_mapping()))
+
+    def tex_fbm(self, octaves, omega, mapping3d=None) -> int:
+        return self.add_texture(Texture(abi.TEXN_FBM, ivalue=octaves, p=(omega,),
+                                        mapping=mapping3d or identity_mapping()))
+
+    def tex_cell_noise(self, dist, mapping3d=None) -> int:
+        return self.add_texture(Texture(abi.TEXN_CELL_NOISE, ivalue=dist,
+                                        mapping=mapping3d or identity_mapping()))
+
+    def tex_crystal(self, octaves, mapping) -> int:
+        return self.add_texture(Texture(abi.TEXN_CRYSTAL, ivalue=octaves, mapping=mapping))
 
     def add_mesh(self, vertices, indices, material, normals=None, uvs=None) -> int:
         v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
@@ -186,7 +287,28 @@ class Scene:
         sd.prim_order = abi.iptr(order)
         if self.camera is not None:
             sd.camera = self.camera
-        keep += [meshes, shapes, mats, lights]
+        texs = (abi.Texture * max(1, len(self.textures)))()
+        for k, t in enumerate(self.textures):
+            d = texs[k]
+            d.kind = t.kind
+            d.a, d.b, d.c = t.children
+            d.ivalue = t.ivalue
+            d.map_kind = t.mapping[0]
+            d.map[:len(t.mapping[1])] = [float(x) for x in t.mapping[1]]
+            d.p[:len(t.p)] = [float(x) for x in t.p]
+            if t.spectrum is not None:
+                d.spectrum[:] = np.asarray(t.spectrum, np.float32).tolist()
+            if t.steps is not None:
+                st = np.ascontiguousarray(t.steps, np.float32)
+                keep.append(st)
+                d.data = abi.fptr(st)
+            if t.pixels is not None:
+                px = np.ascontiguousarray(t.pixels, np.uint8)
+                keep.append(px)
+                d.pixels = px.ctypes.data_as(C.POINTER(C.c_uint8))
+                d.height, d.width = px.shape[0], px.shape[1]
+        sd.textures, sd.n_textures = texs, len(self.textures)
+        keep += [meshes, shapes, mats, lights, texs]
         return sd, keep
 
 

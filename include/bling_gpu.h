@@ -75,7 +75,9 @@ typedef struct bling_opts {
 /* ---- scene description (flat; replaces the closure records of
  *      Primitive.hs:21-27 / Reflection.hs:42 that cannot cross an FFI) ---- */
 
-/* Materials (src/lib/Graphics/Bling/Material.hs). Textures are constant. */
+/* Materials (src/lib/Graphics/Bling/Material.hs).  Each parameter is the
+ * constant field below or, through bling_material.tex, a texture expression
+ * (bling_texture) evaluated at every hit's shading geometry. */
 enum {
   BLING_MAT_MATTE = 0,   /* mkMatte kd sigma            (Material.hs:32-41) */
   BLING_MAT_PLASTIC = 1, /* mkPlastic kd ks roughness   (Material.hs:76-87) */
@@ -112,8 +114,69 @@ typedef struct bling_material {
   int32_t kd_texture;
   float kd_tex_params[9];
   float kd2[BLING_BANDS];
+  /* Textured parameters: tex[slot] = 0 keeps the constant field, n + 1 takes
+   * node n of bling_scene_desc.textures (a spectrum-valued node for the
+   * spectrum slots, a scalar-valued one for the scalar slots).  The slots
+   * follow the fields above: BLING_SLOT_KD .. BLING_SLOT_IOR.  A textured kd
+   * replaces kd_texture. */
+  int32_t tex[8];
+  /* bumpMapped d material (Reflection.hs:344-377): bump = n + 1 makes the
+   * scalar node n the displacement, 0 for none */
+  int32_t bump;
+  int32_t reserved_tex;
 } bling_material;
 enum { BLING_TEX_CONSTANT = 0, BLING_TEX_CHECKER = 1, BLING_TEX_GRAPH_PAPER = 2 };
+enum {
+  BLING_SLOT_KD = 0, BLING_SLOT_KS = 1, BLING_SLOT_KT = 2, BLING_SLOT_ETA = 3, BLING_SLOT_K = 4,
+  BLING_SLOT_SIGMA = 5, BLING_SLOT_ROUGHNESS = 6, BLING_SLOT_IOR = 7
+};
+
+/* Texture expressions (Texture.hs; the grammar of MaterialParser.hs:120-240).
+ * A scene's textures are one array of nodes.  A node names its children by
+ * index; every child comes before its parent in the array (child index <
+ * node index), and a tree is at most BLING_TEX_MAX_DEPTH nodes deep.  The
+ * mappings read the shading geometry: uv (u, v of the surface), planar and
+ * identity3d (the shading point p in world space). */
+#define BLING_TEX_MAX_DEPTH 8
+enum {
+  /* spectrum-valued */
+  BLING_TEXN_CONSTANT = 0,    /* constant spectrum */
+  BLING_TEXN_BLEND = 1,       /* spectrumBlend a b c: c scalar (Texture.hs:134-145) */
+  BLING_TEXN_CHECKER = 2,     /* checkerBoard (p[0] p[1] p[2]) a b (Texture.hs:209-219) */
+  BLING_TEXN_GRAPH_PAPER = 3, /* graphPaper p[0] map a b (Texture.hs:187-207): a paper, b lines */
+  BLING_TEXN_GRADIENT = 4,    /* gradient (mkGradient steps) c (Texture.hs:221-248): c scalar;
+                                 ivalue steps of 17 floats (position, spectrum) in data */
+  BLING_TEXN_IMAGE = 5,       /* imageTexture of an RGB image, map (Texture.hs:87-108,128-129):
+                                 width x height pixels, r g b bytes per pixel, in pixels */
+  /* scalar-valued */
+  BLING_TEXN_SCALAR = 16,     /* constant p[0] */
+  BLING_TEXN_SCALE = 17,      /* scaleTexture p[0] p[1] a: p[0] + p[1] * a (Texture.hs:178-179) */
+  BLING_TEXN_PERLIN = 18,     /* noiseTexture (identityMapping3d map) (Texture.hs:340-413) */
+  BLING_TEXN_FBM = 19,        /* fbm ivalue p[0] over identityMapping3d map (Texture.hs:328-337) */
+  BLING_TEXN_CELL_NOISE = 20, /* cellNoise (BLING_DIST_ ivalue) (identityMapping3d map)
+                                 (Texture.hs:250-300) */
+  BLING_TEXN_CRYSTAL = 21,    /* quasiCrystal ivalue map (Texture.hs:302-326) */
+  BLING_TEXN_IMAGE_SCALAR = 22 /* imageTexture of a grey image, map: one byte per pixel */
+};
+enum { BLING_MAP_UV = 0, BLING_MAP_PLANAR = 1, BLING_MAP_IDENTITY3D = 2 };
+enum {
+  BLING_DIST_EUCLIDIAN = 0, BLING_DIST_EUCLIDIAN2 = 1, BLING_DIST_MANHATTAN = 2,
+  BLING_DIST_CHEBYSHEV = 3
+};
+typedef struct bling_texture {
+  int32_t kind;             /* BLING_TEXN_* */
+  int32_t a, b, c;          /* children, -1 where the kind has none */
+  int32_t ivalue;           /* octaves (fbm, crystal), distance (cell noise), steps (gradient) */
+  int32_t map_kind;         /* BLING_MAP_* of image, graph paper, crystal, noise nodes */
+  float map[16];            /* uv (uvMapping): su sv ou ov; planar (planarMapping): vu(3)
+                               vv(3) ou ov; identity3d (identityMapping3d): the world-to-texture
+                               matrix, row-major */
+  float p[4];               /* the kind's numbers (see the kinds) */
+  float spectrum[BLING_BANDS]; /* constant */
+  const float* data;        /* gradient steps */
+  const uint8_t* pixels;    /* image pixels, rows top to bottom */
+  int32_t width, height;    /* image size */
+} bling_texture;
 
 /* A triangle mesh (mkTriangleMesh, Primitive/TriangleMesh.hs:39-60).
  * Vertices and normals are already in world space (the reference applies
@@ -203,6 +266,9 @@ typedef struct bling_scene_desc {
   int32_t n_lights;
   const int32_t* prim_order; /* n_meshes + n_shapes entries, or NULL */
   bling_camera_desc camera;
+  const bling_texture* textures; /* the texture nodes materials refer to */
+  int32_t n_textures;
+  int32_t reserved_desc;
 } bling_scene_desc;
 
 /* Pixel filters (Filter.hs:12-21). */

@@ -250,19 +250,24 @@ static void rnd2(const Sampler& s, int n, float& u, float& v) {
 }
 
 // ---------------------------------------------------------------- geometry
-struct DG {  // DifferentialGeometry (DifferentialGeometry.hs:26-36), the used fields
+struct DG {  // DifferentialGeometry (DifferentialGeometry.hs:26-36)
   V p, n;
-  V dpdu, dpdv;
+  float u, v;
+  V dpdu, dpdv, dndu, dndv;
   bool tri;
   float b1, b2;
 };
 // mkDg: n = normalize (dpdu x dpdv) (DifferentialGeometry.hs:41-51)
-static DG mkDg(V p, V dpdu, V dpdv) {
+static DG mkDg(V p, float u, float v, V dpdu, V dpdv, V dndu, V dndv) {
   DG g;
   g.p = p;
   g.n = normalize(cross(dpdu, dpdv));
+  g.u = u;
+  g.v = v;
   g.dpdu = dpdu;
   g.dpdv = dpdv;
+  g.dndu = dndu;
+  g.dndv = dndv;
   g.tri = false;
   g.b1 = g.b2 = 0;
   return g;
@@ -273,8 +278,10 @@ static DG mkDg2(V p, V n) {
   DG g;
   g.p = p;
   g.n = n;
+  g.u = g.v = 0;
   g.dpdu = c.s;
   g.dpdv = c.t;
+  g.dndu = g.dndv = V{0, 0, 0};
   g.tri = false;
   g.b1 = g.b2 = 0;
   return g;
@@ -286,6 +293,8 @@ static DG transDg(const float* m, const float* mi, const DG& g) {
   r.n = normalize(transNormal(mi, g.n));
   r.dpdu = transVector(m, g.dpdu);
   r.dpdv = transVector(m, g.dpdv);
+  r.dndu = transNormal(mi, g.dndu);
+  r.dndv = transNormal(mi, g.dndv);
   return r;
 }
 
@@ -436,7 +445,9 @@ static bool shapeIntersect(const Shape& s, const Ray& ray, float& t_out, float& 
       if (fabsf(p.x) > sx || fabsf(p.y) > sy) return false;
       t_out = t;
       e_out = 5e-4f * t;
-      dg = mkDg(p, mkV(sx, 0, 0), mkV(0, sy, 0));
+      // u = (sx + px) / (2 sx), v = (sy + py) / (2 sy) (Shape.hs:164-171)
+      dg = mkDg(p, (sx + p.x) / (2.0f * sx), (sy + p.y) / (2.0f * sy), mkV(sx, 0, 0),
+                mkV(0, sy, 0), V{0, 0, 0}, V{0, 0, 0});
       return true;
     }
     default: {  // sphere
@@ -460,9 +471,23 @@ static bool shapeIntersect(const Shape& s, const Ray& ray, float& t_out, float& 
       V dpdv = V{p.z * cosphi, p.z * sinphi, -r * sinf(theta)} * V{thetaMax - thetaMin,
                                                                  thetaMax - thetaMin,
                                                                  thetaMax - thetaMin};
+      float phi = atan2p(p.y, p.x);
+      float u = phi / phiMax, v = (theta - thetaMin) / (thetaMax - thetaMin);
+      // dndu, dndv from the fundamental forms (Shape.hs:209-229)
+      float kk = thetaMax - thetaMin;
+      auto vp = [](float x) { return V{x, x, x}; };  // vpromote
+      V d2Pduu = vp(-phiMax * phiMax) * mkV(p.x, p.y, 0);
+      V d2Pduv = vp(kk * p.z * phiMax) * mkV(-sinphi, cosphi, 0);
+      V d2Pdvv = vp(-kk * kk) * mkV(p.x, p.y, p.z);
+      float e1 = dot(dpdu, dpdu), f1 = dot(dpdu, dpdv), g1 = dot(dpdv, dpdv);
+      V n1 = normalize(cross(dpdu, dpdv));
+      float e = dot(n1, d2Pduu), f = dot(n1, d2Pduv), g = dot(n1, d2Pdvv);
+      float invEGF2 = 1.0f / (e1 * g1 - f1 * f1);
+      V dndu = vp((f * f1 - e * g1) * invEGF2) * dpdu + vp((e * f1 - f * e1) * invEGF2) * dpdv;
+      V dndv = vp((g * f1 - f * g1) * invEGF2) * dpdu + vp((f * f1 - g * e1) * invEGF2) * dpdv;
       t_out = t;
       e_out = 5e-4f * t;
-      dg = mkDg(p, dpdu, dpdv);
+      dg = mkDg(p, u, v, dpdu, dpdv, dndu, dndv);
       return true;
     }
   }
@@ -563,6 +588,18 @@ struct Material {
   int kd_tex;
   float kd_par[9];
   Spec kd2;
+  int tex[8];  // texture node + 1 per parameter slot (bling_material.tex)
+  int bump;    // displacement node + 1
+};
+
+// a texture expression node (bling_texture)
+struct TexNode {
+  int kind, a, b, c, ivalue, map_kind;
+  float map[16], p[4];
+  Spec spectrum;
+  std::vector<float> steps;    // gradient: (position, spectrum) x ivalue, sorted by position
+  std::vector<uint8_t> pixels;  // image
+  int w, h;
 };
 
 struct Prim {
@@ -790,6 +827,7 @@ struct orc_scene {
   std::vector<Mesh> meshes;
   std::vector<Shape> shapes;
   std::vector<Material> mats;
+  std::vector<TexNode> tex;
   std::vector<Light> lights;
   std::vector<Prim> prims;
   bling_camera_desc cam;
@@ -857,7 +895,10 @@ static void triHitDG(const orc_scene& S, const Prim& pr, const Ray& r, float t, 
     dpdu = sv(invDet, sv(dv2, dp1) - sv(dv1, dp2));
     dpdv = sv(invDet, sv(-du2, dp1) + sv(du1, dp2));
   }
-  dg = mkDg(rayAt(r, t), dpdu, dpdv);
+  float b0 = 1.0f - b1 - b2;  // the interpolated (u, v) (TriangleMesh.hs:198-201)
+  float tu = b0 * uv00 + b1 * uv10 + b2 * uv20;
+  float tv = b0 * uv01 + b1 * uv11 + b2 * uv21;
+  dg = mkDg(rayAt(r, t), tu, tv, dpdu, dpdv, V{0, 0, 0}, V{0, 0, 0});
   dg.tri = true;
   dg.b1 = b1;
   dg.b2 = b2;
@@ -1626,6 +1667,267 @@ static Spec frApproxK(const Spec& r) {
   return o;
 }
 
+// ---------------------------------------------------------------- textures
+// Texture.hs restated: the mappings, Perlin noise and fBm, Worley cell noise,
+// the quasi-crystal, gradients, blends, checkers, graph paper and images.
+static const uint8_t NOISE_PERM[256] = {BLING_NOISE_PERM_LIST};
+
+// noiseWeight (Texture.hs:378-382)
+static float noiseWeight(float t) {
+  float t3 = t * t * t;
+  float t4 = t3 * t;
+  return 6.0f * t4 * t - 15.0f * t4 + 10.0f * t3;
+}
+// grad (Texture.hs:384-393); noisePerms is the permutation written twice
+static float grad(int x, int y, int z, float dx, float dy, float dz) {
+  auto P = [](int i) { return (int)NOISE_PERM[i % 256]; };
+  int h = P(P(P(x) + y) + z) & 15;
+  float u = (h < 8 || h == 12 || h == 13) ? dx : dy;
+  float v = (h < 4 || h == 12 || h == 13) ? dy : dz;
+  return ((h & 1) != 0 ? -u : u) + ((h & 2) != 0 ? -v : v);
+}
+// perlin3d (Texture.hs:348-376)
+static float perlin3d(float x, float y, float z) {
+  long long ix0 = (long long)std::floor(x), iy0 = (long long)std::floor(y),
+            iz0 = (long long)std::floor(z);
+  float dx = x - (float)ix0, dy = y - (float)iy0, dz = z - (float)iz0;
+  int ix = (int)(ix0 & 255), iy = (int)(iy0 & 255), iz = (int)(iz0 & 255);
+  float w000 = grad(ix, iy, iz, dx, dy, dz);
+  float w100 = grad(ix + 1, iy, iz, dx - 1, dy, dz);
+  float w010 = grad(ix, iy + 1, iz, dx, dy - 1, dz);
+  float w110 = grad(ix + 1, iy + 1, iz, dx - 1, dy - 1, dz);
+  float w001 = grad(ix, iy, iz + 1, dx, dy, dz - 1);
+  float w101 = grad(ix + 1, iy, iz + 1, dx - 1, dy, dz - 1);
+  float w011 = grad(ix, iy + 1, iz + 1, dx, dy - 1, dz - 1);
+  float w111 = grad(ix + 1, iy + 1, iz + 1, dx - 1, dy - 1, dz - 1);
+  float wx = noiseWeight(dx), wy = noiseWeight(dy), wz = noiseWeight(dz);
+  float x00 = lerp(wx, w000, w100), x10 = lerp(wx, w010, w110);
+  float x01 = lerp(wx, w001, w101), x11 = lerp(wx, w011, w111);
+  return lerp(wz, lerp(wy, x00, x10), lerp(wy, x01, x11));
+}
+// fbm (Texture.hs:328-337): sum (take octaves terms), the sum a left fold from 0
+static float fbm(int octaves, float omega, V p) {
+  float sum = 0.0f, l = 1.0f, o = 1.0f;
+  for (int k = 0; k < octaves; k++) {
+    sum = sum + o * perlin3d(p.x * l, p.y * l, p.z * l);
+    l = 1.99f * l;  // iterate (1.99 *) 1
+    o = omega * o;  // iterate (omega *) 1
+  }
+  return sum;
+}
+// cellNoise (Texture.hs:250-300): Int is 64 bits
+static float cellNoise(int dist, V p) {
+  auto lcg = [](long long x) { return (1103515245LL * x + 12345LL) % 4294967296LL; };
+  auto hash = [](long long x, long long y, long long z) {
+    long long h = (x * 73856093LL) ^ (y * 19349663LL) ^ (z * 83492791LL);
+    return std::llabs(h) % 4294967296LL;
+  };
+  auto prob = [](long long v) {
+    static const long long lim[8] = {393325350LL,  1022645910LL, 1861739990LL, 2700834071LL,
+                                     3372109335LL, 3819626178LL, 4075350088LL, 4203212043LL};
+    for (int k = 0; k < 8; k++)
+      if (v < lim[k]) return k + 1;
+    return 9;
+  };
+  auto distf = [&](V a, V b) {
+    V d = a - b;
+    switch (dist) {
+      case BLING_DIST_EUCLIDIAN2: return sqLen(d);
+      case BLING_DIST_MANHATTAN: return fabsf(d.x) + fabsf(d.y) + fabsf(d.z);
+      case BLING_DIST_CHEBYSHEV: return hmax(hmax(fabsf(d.x), fabsf(d.y)), fabsf(d.z));
+      default: return len(d);
+    }
+  };
+  long long ox = (long long)std::floor(p.x), oy = (long long)std::floor(p.y),
+            oz = (long long)std::floor(p.z);
+  std::vector<float> ds;
+  for (int x = -1; x <= 1; x++)
+    for (int y = -1; y <= 1; y++)
+      for (int z = -1; z <= 1; z++) {
+        long long cx = x + ox, cy = y + oy, cz = z + oz;
+        long long us = lcg(hash(cx, cy, cz));
+        int n = prob(us);
+        long long u0 = us;
+        for (int k = 0; k < n; k++) {
+          long long u1 = lcg(u0), u2 = lcg(u1), u3 = lcg(u2);
+          V pt{(float)cx + (float)u1 / 4294967296.0f, (float)cy + (float)u2 / 4294967296.0f,
+               (float)cz + (float)u3 / 4294967296.0f};
+          ds.push_back(distf(p, pt));
+          u0 = u3;
+        }
+      }
+  float m = ds[0];  // minimum = foldl1 min
+  for (size_t k = 1; k < ds.size(); k++) m = hmin(m, ds[k]);
+  return m;
+}
+// quasiCrystal (Texture.hs:302-326); the angles as base-4.9's
+// numericEnumFromThen makes them (each next one m + m - n)
+static float quasiCrystal(int octaves, float x, float y) {
+  std::vector<float> angles;
+  float n0 = 0.0f, m0 = PI / (float)octaves;
+  for (int k = 0; k < octaves; k++) {
+    angles.push_back(n0);
+    float nx = m0 + m0 - n0;
+    n0 = m0;
+    m0 = nx;
+  }
+  float sum = 0.0f;
+  for (float th : angles) {
+    float cth = cosf(th), sth = sinf(th);
+    sum = sum + (cosf(cth * x + sth * y) + 1.0f) / 2.0f;
+  }
+  long long k = (long long)sum;  // properFraction: truncation
+  float v = sum - (float)k;
+  if (v < 0) {
+    k = k - 1;
+    v = 1.0f + v;
+  }
+  return (k % 2 != 0) ? 1.0f - v : v;
+}
+
+struct TexPoint {  // what textures read of the shading DG
+  V p;
+  float u, v;
+};
+// uvMapping / planarMapping (Texture.hs:160-176)
+static void map2d(const TexNode& t, const TexPoint& g, float& s, float& r) {
+  if (t.map_kind == BLING_MAP_PLANAR) {
+    s = dot(g.p, V{t.map[0], t.map[1], t.map[2]}) + t.map[6];
+    r = dot(g.p, V{t.map[3], t.map[4], t.map[5]}) + t.map[7];
+  } else {
+    s = t.map[0] * g.u + t.map[2];
+    r = t.map[1] * g.v + t.map[3];
+  }
+}
+// identityMapping3d (Texture.hs:150-154)
+static V map3d(const TexNode& t, const TexPoint& g) { return transPoint(t.map, g.p); }
+// getPixel's pixel index (Texture.hs:91-101): mod' (floor (u w)) w,
+// mod' (floor (-v h)) h
+static size_t pixelIndex(const TexNode& t, float s, float r) {
+  auto modp = [](long long a, long long b) {
+    long long q = a / b, rem = a - q * b;
+    if (rem != 0 && ((rem < 0) != (b < 0))) rem += b;  // Haskell's div floors
+    return rem;
+  };
+  long long px = modp((long long)std::floor(s * (float)t.w), t.w);
+  long long py = modp((long long)std::floor((-r) * (float)t.h), t.h);
+  return (size_t)py * t.w + (size_t)px;
+}
+
+static float scalarTex(const orc_scene& S, int i, const TexPoint& g) {
+  const TexNode& t = S.tex[i];
+  switch (t.kind) {
+    case BLING_TEXN_SCALE: return t.p[0] + t.p[1] * scalarTex(S, t.a, g);
+    case BLING_TEXN_PERLIN: {
+      V q = map3d(t, g);
+      return perlin3d(q.x, q.y, q.z);
+    }
+    case BLING_TEXN_FBM: return fbm(t.ivalue, t.p[0], map3d(t, g));
+    case BLING_TEXN_CELL_NOISE: return cellNoise(t.ivalue, map3d(t, g));
+    case BLING_TEXN_CRYSTAL: {
+      float s, r;
+      map2d(t, g, s, r);
+      return quasiCrystal(t.ivalue, s, r);
+    }
+    case BLING_TEXN_IMAGE_SCALAR: {  // getPixelScalar: x / 255
+      float s, r;
+      map2d(t, g, s, r);
+      return (float)t.pixels[pixelIndex(t, s, r)] / 255.0f;
+    }
+    default: return t.p[0];
+  }
+}
+static Spec spectrumTex(const orc_scene& S, int i, const TexPoint& g) {
+  const TexNode& t = S.tex[i];
+  switch (t.kind) {
+    case BLING_TEXN_BLEND: {  // spectrumBlend
+      Spec v1 = spectrumTex(S, t.a, g), v2 = spectrumTex(S, t.b, g);
+      float x = scalarTex(S, t.c, g);
+      if (x <= 0) return v1;
+      if (x >= 1) return v2;
+      return sScale(v1, 1.0f - x) + sScale(v2, x);
+    }
+    case BLING_TEXN_CHECKER: {  // checkerBoard: Haskell's mod 2 of the floor sum
+      long long c = (long long)std::floor(g.p.x * t.p[0]) + (long long)std::floor(g.p.y * t.p[1]) +
+                    (long long)std::floor(g.p.z * t.p[2]);
+      return ((c % 2) + 2) % 2 == 0 ? spectrumTex(S, t.a, g) : spectrumTex(S, t.b, g);
+    }
+    case BLING_TEXN_GRAPH_PAPER: {
+      float x, z;
+      map2d(t, g, x, z);
+      float xf = fabsf(x - (float)(long long)x), zf = fabsf(z - (float)(long long)z);
+      float lo = t.p[0] / 2.0f, hi = 1.0f - lo;
+      return (xf < lo || zf < lo || xf > hi || zf > hi) ? spectrumTex(S, t.b, g)
+                                                        : spectrumTex(S, t.a, g);
+    }
+    case BLING_TEXN_GRADIENT: {
+      float f = scalarTex(S, t.c, g);
+      int n = t.ivalue;
+      auto pos = [&](int k) { return t.steps[17 * k]; };
+      auto col = [&](int k) {
+        Spec c;
+        memcpy(c.v, &t.steps[17 * k + 1], 64);
+        return c;
+      };
+      float gmin = pos(0), gmax = pos(0);  // V.minimum / V.maximum of the positions
+      for (int k = 1; k < n; k++) {
+        gmin = hmin(gmin, pos(k));
+        gmax = hmax(gmax, pos(k));
+      }
+      if (f <= gmin) return col(0);
+      if (f >= gmax) return col(n - 1);
+      int idx = 0;
+      while (idx < n && !(pos(idx) > f)) idx++;  // findIndex ((> f) . fst)
+      float w = (f - pos(idx - 1)) / (pos(idx) - pos(idx - 1));
+      return sScale(col(idx - 1), 1.0f - w) + sScale(col(idx), w);
+    }
+    case BLING_TEXN_IMAGE: {  // pixelSpectrum = rgbToSpectrumRefl . unGamma
+      float s, r;
+      map2d(t, g, s, r);
+      const uint8_t* px = &t.pixels[3 * pixelIndex(t, s, r)];
+      float c[3];
+      for (int k = 0; k < 3; k++) c[k] = powf((float)px[k] / 255.0f, 2.2f);
+      return rgbToSpectrum(false, c[0], c[1], c[2]);
+    }
+    default: return t.spectrum;
+  }
+}
+
+// bump (Reflection.hs:347-377) of dgs by the scalar node d; dgg's normal
+// orients the result
+static void bump(const orc_scene& S, int d, const DG& dgg, DG& dgs) {
+  const float du = 0.01f, dv = 0.01f;
+  TexPoint geu{dgs.p + sv(du, dgs.dpdu), dgs.u + du, dgs.v};
+  TexPoint gev{dgs.p + sv(dv, dgs.dpdv), dgs.u, dgs.v + dv};
+  TexPoint gs{dgs.p, dgs.u, dgs.v};
+  float uDisp = scalarTex(S, d, geu), vDisp = scalarTex(S, d, gev), disp = scalarTex(S, d, gs);
+  float vscale = (vDisp - disp) / dv;
+  V dpdv = dgs.dpdv + sv(vscale, dgs.n);
+  float uscale = (uDisp - disp) / du;
+  V dpdu = dgs.dpdu + sv(uscale, dgs.n);
+  V nn = normalize(cross(dpdu, dpdv));
+  if (dot(nn, dgg.n) < 0) nn = -nn;  // faceForward
+  dgs.n = nn;
+  dgs.dpdu = dpdu;
+  dgs.dpdv = dpdv;
+}
+
+// the material at a hit: bumpMapped applies its bump to dgs, then every
+// textured parameter is its texture at dgs
+static Material hitMaterial(const orc_scene& S, int mi, const DG& dgg, DG& dgs) {
+  Material m = S.mats[mi];
+  if (m.bump) bump(S, m.bump - 1, dgg, dgs);
+  TexPoint g{dgs.p, dgs.u, dgs.v};
+  Spec* spectra[5] = {&m.kd, &m.ks, &m.kt, &m.eta, &m.k};
+  for (int k = 0; k < 5; k++)
+    if (m.tex[k]) *spectra[k] = spectrumTex(S, m.tex[k] - 1, g);
+  if (m.tex[0]) m.kd_tex = BLING_TEX_CONSTANT;
+  if (m.tex[5]) m.sigma = scalarTex(S, m.tex[5] - 1, g);
+  if (m.tex[6]) m.rough = scalarTex(S, m.tex[6] - 1, g);
+  if (m.tex[7]) m.ior = scalarTex(S, m.tex[7] - 1, g);
+  return m;
+}
+
 static Bsdf materialBsdf(const Material& m0, const DG& dgg, const DG& dgs) {
   // the kd texture at the shading point
   const Material& m = m0;
@@ -2132,7 +2434,8 @@ static Spec pathLi(const orc_scene& S, const Sampler& smp, Ray ray, int md, int 
     const Prim& pr = S.prims[it.prim];
     int mat = pr.is_shape ? S.shapes[pr.index].material : S.meshes[pr.index].material;
     DG dgs = shadingGeometry(S, pr, it.dg);
-    Bsdf bsdf = materialBsdf(S.mats[mat], it.dg, dgs);
+    Material mm = hitMaterial(S, mat, it.dg, dgs);
+    Bsdf bsdf = materialBsdf(mm, it.dg, dgs);
     V n = bsdf.cs.n;
     V p = bsdf.p;
     float eps = it.eps;
@@ -2331,7 +2634,8 @@ static void tracePhoton(const orc_scene& S, uint64_t seed, uint64_t pass, uint64
     const Prim& pr = S.prims[it.prim];
     int mat = pr.is_shape ? S.shapes[pr.index].material : S.meshes[pr.index].material;
     DG dgs = shadingGeometry(S, pr, it.dg);
-    Bsdf bsdf = materialBsdf(S.mats[mat], it.dg, dgs);
+    Material mm = hitMaterial(S, mat, it.dg, dgs);
+    Bsdf bsdf = materialBsdf(mm, it.dg, dgs);
     V p = bsdf.p;
     BsdfSample bs = sampleBsdf(bsdf, wi, ubc, ubd1, ubd2, true);  // sampleAdjBsdf
     Spec li2 = sScale(li * bs.f, 1.0f / pcont);
@@ -2569,7 +2873,37 @@ int orc_scene_create(const bling_scene_desc* d, orc_scene** out) {
     m.kd_tex = bm.kd_texture;
     memcpy(m.kd_par, bm.kd_tex_params, 36);
     memcpy(m.kd2.v, bm.kd2, 64);
+    memcpy(m.tex, bm.tex, sizeof m.tex);
+    m.bump = bm.bump;
     S->mats.push_back(m);
+  }
+  for (int i = 0; i < d->n_textures; i++) {
+    const bling_texture& t = d->textures[i];
+    TexNode n;
+    n.kind = t.kind;
+    n.a = t.a;
+    n.b = t.b;
+    n.c = t.c;
+    n.ivalue = t.ivalue;
+    n.map_kind = t.map_kind;
+    memcpy(n.map, t.map, 64);
+    memcpy(n.p, t.p, 16);
+    memcpy(n.spectrum.v, t.spectrum, 64);
+    n.w = t.width;
+    n.h = t.height;
+    if (t.kind == BLING_TEXN_GRADIENT) {
+      // mkGradient: sortBy (compare `on` fst), a stable sort (Texture.hs:228-234)
+      std::vector<std::pair<float, int>> key;
+      for (int k = 0; k < t.ivalue; k++) key.push_back({t.data[17 * k], k});
+      std::stable_sort(key.begin(), key.end(),
+                       [](const std::pair<float, int>& x, const std::pair<float, int>& y) {
+                         return x.first < y.first;
+                       });
+      for (auto& kv : key) n.steps.insert(n.steps.end(), t.data + 17 * kv.second, t.data + 17 * kv.second + 17);
+    }
+    if (t.kind == BLING_TEXN_IMAGE) n.pixels.assign(t.pixels, t.pixels + (size_t)3 * t.width * t.height);
+    if (t.kind == BLING_TEXN_IMAGE_SCALAR) n.pixels.assign(t.pixels, t.pixels + (size_t)t.width * t.height);
+    S->tex.push_back(std::move(n));
   }
   for (int i = 0; i < d->n_meshes; i++) {
     const bling_mesh_desc& md = d->meshes[i];
@@ -3100,7 +3434,8 @@ struct CamTree {
     const Prim& pr = S->prims[it.prim];
     int mat = pr.is_shape ? S->shapes[pr.index].material : S->meshes[pr.index].material;
     DG dgs = shadingGeometry(*S, pr, it.dg);
-    Bsdf bsdf = materialBsdf(S->mats[mat], it.dg, dgs);
+    Material mm = hitMaterial(*S, mat, it.dg, dgs);
+    Bsdf bsdf = materialBsdf(mm, it.dg, dgs);
     Spec ls = t * intLe(*S, it, ray.d);
     if (bsdfHasNonSpecular(bsdf)) {
       int64_t si = st->idx(sx, sy);
@@ -3241,7 +3576,8 @@ int orc_sppm_pass(const orc_scene* S, const bling_sppm_params* sp, int32_t width
             const Prim& pr = S->prims[it.prim];
             int mat = pr.is_shape ? S->shapes[pr.index].material : S->meshes[pr.index].material;
             DG dgs = shadingGeometry(*S, pr, it.dg);
-            Bsdf bsdf = materialBsdf(S->mats[mat], it.dg, dgs);
+            Material mm = hitMaterial(*S, mat, it.dg, dgs);
+            Bsdf bsdf = materialBsdf(mm, it.dg, dgs);
             V p = bsdf.p;
             if (bsdfHasNonSpecular(bsdf)) {  // hashLookup (SPPM.hs:307-314)
               float cx = fabsf((p.x - lo.x) * invSize), cy = fabsf((p.y - lo.y) * invSize),
@@ -3309,6 +3645,20 @@ int orc_sppm_pass(const orc_scene* S, const bling_sppm_params* sp, int32_t width
   return BLING_OK;
 }
 
+int orc_texture_eval(const orc_scene* s, int node, const float p[3], float u, float v,
+                     float out[16]) {
+  if (!s || node < 0 || node >= (int)s->tex.size()) return BLING_ERR_INVALID_ARG;
+  TexPoint g{V{p[0], p[1], p[2]}, u, v};
+  int kind = s->tex[node].kind;
+  if (kind >= BLING_TEXN_SCALAR) {
+    memset(out, 0, 64);
+    out[0] = scalarTex(*s, node, g);
+  } else {
+    Spec r = spectrumTex(*s, node, g);
+    memcpy(out, r.v, 64);
+  }
+  return BLING_OK;
+}
 void orc_sunsky_eval(const float east[3], const float sun_dir[3], float turbidity, float u,
                      float v, float out[16]) {
   SkyData sd = initSkyData(mkV(east[0], east[1], east[2]),

@@ -88,6 +88,10 @@ int orc_sppm_pass(const orc_scene* s, const bling_sppm_params* params, int32_t w
 
 /* restated helpers, for known-answer tests */
 void orc_rgb_to_spectrum(int illum, float r, float g, float b, float out[16]);
+/* texture node `node` of the scene at shading point p and surface (u, v):
+ * 16 bands for spectrum nodes, out[0] for scalar ones */
+int orc_texture_eval(const orc_scene* s, int node, const float p[3], float u, float v,
+                     float out[16]);
 /* mkSunSkyLight east sunDir turbidity evaluated at (u, v) */
 void orc_sunsky_eval(const float east[3], const float sun_dir[3], float turbidity, float u,
                      float v, float out[16]);

@@ -59,6 +59,8 @@ def lib():
         L.orc_sunsky_eval.argtypes = [P(C.c_float), P(C.c_float), C.c_float, C.c_float, C.c_float,
                                       P(C.c_float)]
         L.orc_spectrum_to_xyz.argtypes = [P(C.c_float), P(C.c_float)]
+        L.orc_texture_eval.argtypes = [C.c_void_p, C.c_int, P(C.c_float), C.c_float, C.c_float,
+                                       P(C.c_float)]
         L.orc_xyz_to_rgb.argtypes = [P(C.c_float), P(C.c_float)]
         L.orc_filter_eval.argtypes = [C.c_int, P(C.c_float), C.c_float, C.c_float]
         L.orc_filter_eval.restype = C.c_float
@@ -86,6 +88,7 @@ def fp(a):
 class OracleScene:
     def __init__(self, scene):
         self._desc, self._keep = scene.desc()
+        self.kinds = [t.kind for t in getattr(scene, "textures", [])]
         self.h = C.c_void_p()
         rc = lib().orc_scene_create(C.byref(self._desc), C.byref(self.h))
         if rc != 0:
@@ -221,6 +224,16 @@ class OracleScene:
             raise ValueError(f"orc_sppm_pass failed: {rc}")
         return film, splats, state, {"rays_closest": st[0], "hitpoints": st[1], "splats": st[2],
                                      "nonfinite": st[3]}
+
+    def texture(self, node, p, u=0.0, v=0.0):
+        """texture node `node` at shading point p, surface (u, v): 16 bands
+        for spectrum nodes, a float for scalar ones"""
+        out = np.zeros(16, np.float32)
+        pp = np.asarray(p, np.float32)
+        rc = lib().orc_texture_eval(self.h, node, fp(pp), float(u), float(v), fp(out))
+        if rc != 0:
+            raise ValueError(f"orc_texture_eval failed: {rc}")
+        return out if self.kinds[node] < abi.TEXN_SCALAR else np.float32(out[0])
 
     def sample_li(self, params, pass_index, px, py, n):
         xyz = np.zeros(3, np.float32)

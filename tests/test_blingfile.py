@@ -165,19 +165,25 @@ def test_substrate_and_blackbody():
     assert np.array_equal(np.asarray(sub.kt, F), rgb_to_spectrum((F(0.1), F(0.1), F(0.1))))
 
 
-def test_checkerboard_diffuse_colour():
+def test_checkerboard_and_graph_paper_diffuse_colours_are_texture_nodes():
     j = B.parse("material { matte kd { checker 2 2 2 tex1 { constant rgbR 0.8 0.8 0.8 } "
                 "tex2 { constant rgbR 0.1 0.1 0.1 } } sigma { constant 0 } } "
                 "prim { shape { sphere radius 1 } }")
     m = j.scene.materials[0]
-    assert m.kd_texture == abi.TEX_CHECKER and list(m.kd_tex_params)[:3] == [2.0, 2.0, 2.0]
+    tx = j.scene.textures
+    node = m.tex[abi.SLOT_KD] - 1
+    assert tx[node].kind == abi.TEXN_CHECKER and tx[node].p == (2.0, 2.0, 2.0)
+    a, b, _ = tx[node].children
+    assert np.array_equal(tx[b].spectrum, rgb_to_spectrum((F(0.1), F(0.1), F(0.1))))
+    assert tx[a].kind == tx[b].kind == abi.TEXN_CONSTANT and a < node and b < node
     j = B.parse("material { plastic kd { graphPaper 0.1 map { planar 1 0 0 0 0 1 0.5 0.25 } "
                 "tex1 { constant rgbR 0.9 0.9 0.9 } tex2 { constant rgbR 0.1 0.1 0.4 } } "
                 "ks { constant rgbR 0.2 0.2 0.2 } rough { constant 0.1 } }")
     g = j.scene.materials[0]
-    assert g.kd_texture == abi.TEX_GRAPH_PAPER
-    assert list(g.kd_tex_params) == [float(F(0.1)), 1, 0, 0, 0, 0, 1, 0.5, 0.25]
-    assert np.array_equal(np.asarray(m.kd2, F), rgb_to_spectrum((F(0.1), F(0.1), F(0.1))))
+    t = j.scene.textures[g.tex[abi.SLOT_KD] - 1]
+    assert t.kind == abi.TEXN_GRAPH_PAPER and t.p == (F(0.1),)
+    assert t.mapping == (abi.MAP_PLANAR, (1, 0, 0, 0, 0, 1, F(0.5), F(0.25)))
+    assert g.tex[abi.SLOT_KS] == 0 and g.tex[abi.SLOT_ROUGHNESS] == 0
 
 
 def test_constant_spd_gives_a_flat_spectrum():
@@ -200,11 +206,10 @@ def test_other_renderers_parse_and_are_named():
 
 
 @pytest.mark.parametrize("src,what", [
-    ("material { bumpMap { scale 0.1 tex { constant 1 } } material { matte kd { constant 1 } "
-     "sigma { constant 0 } } }", "bumpMap"),
-    ("material { metal eta { checker 1 1 1 tex1 { constant rgbR 1 1 1 } "
-     "tex2 { constant rgbR 0 0 0 } } k { constant rgbR 1 1 1 } rough { constant 0.1 } }",
-     "checker"),
+    ("material { bumpMap bump { constant 1 } bumpMap bump { constant 1 } matte "
+     "kd { constant rgbR 1 1 1 } sigma { constant 0 } }", "bumpMap"),
+    ("material { matte kd { image { file \"wood.jpg\" map { uv 1 1 0 0 } } } "
+     "sigma { constant 0 } }", "PNG"),
     ("prim { julia c 0 0 0 0 epsilon 0.1 iterations 4 }", "julia"),
     ("light { infinite { } l { file \"sky.png\" } }", "file"),
 ])

@@ -25,7 +25,7 @@ HEADER = ROOT / "include" / "bling_gpu.h"
 WRITTEN = {"bling_material": abi.Material, "bling_mesh_desc": abi.MeshDesc,
            "bling_shape_desc": abi.ShapeDesc, "bling_light_desc": abi.LightDesc,
            "bling_camera_desc": abi.CameraDesc, "bling_scene_desc": abi.SceneDesc,
-           "bling_render_params": abi.RenderParams}
+           "bling_render_params": abi.RenderParams, "bling_texture": abi.Texture}
 
 
 def hsc_directives():

@@ -25,7 +25,7 @@ from bling_gb300 import abi
 from bling_gb300 import scene as S
 from bling_gb300 import transform as xf
 from bling_gb300.spectrum import constant, rgb_to_spectrum
-from oracle.oracle import OracleScene
+from oracle.oracle import OracleScene, _extent
 
 pytestmark = pytest.mark.gpu
 
@@ -399,14 +399,15 @@ def test_first_dropped_sample_is_reported(gpu_ctx):
     st = g.stats()
     o = OracleScene(s)
     first, dropped = None, 0
-    for y in range(h):
-        for x in range(w):
+    x0, x1, y0, y1 = _extent(p)  # the sample extent: a pixel wider than the image
+    for y in range(y0, y1 + 1):
+        for x in range(x0, x1 + 1):
             for n in range(4):
                 spec = o.sample_li(p, 7, x, y, n)[2]
                 if not np.isfinite(spec).all():
                     dropped += 1
                     first = first or (x, y, n)
-    assert first is not None and first[1] > 0  # the top rows see only the empty sky
+    assert first is not None and first[1] > y0  # the top rows see only the empty sky
     assert st["nonfinite_drops"] == dropped
     assert st["nonfinite_pass"] == 7
     assert (*st["nonfinite_pixel"], st["nonfinite_sample"]) == first
