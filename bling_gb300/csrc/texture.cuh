@@ -2,9 +2,10 @@
 // bump mapping (Reflection.hs:344-377).  A material parameter that names a
 // texture node is evaluated per hit at the shading geometry: the shading
 // point p (world space) and the surface parameters (u, v).  Nodes form
-// trees (children before parents, depth checked at upload), evaluated by
-// bounded recursion in the reference's operation order; images and gradients
-// are read from device arrays the scene upload prepares.
+// trees (children before parents, depth checked at upload), evaluated in the
+// reference's operation order by functions unrolled over the depth, so no
+// call is recursive and the stack each kernel needs is known; images and
+// gradients are read from device arrays the scene upload prepares.
 #pragma once
 #include "dmath.cuh"
 #include "integrator.h"
@@ -170,12 +171,32 @@ __device__ __forceinline__ size_t texel(const DTex& t, float s, float r) {
   return (size_t)py * t.width + (size_t)px;
 }
 
+// The evaluators are templates over the depth left (D): a node at depth D
+// evaluates its children at D - 1, so the call graph has no cycle and the
+// kernels' stack size is known at compile time.  Trees are at most
+// BLING_TEX_MAX_DEPTH deep (checked at upload), so D = 0 is never reached.
+template <int D>
+__device__ __noinline__ float texScalarD(const DTex* __restrict__ T, int i, const TexGeo& g);
+template <int D>
+__device__ __noinline__ void texSpectrumD(const DTex* __restrict__ T, int i, const TexGeo& g,
+                                          float* out);
+template <>
+__device__ __forceinline__ float texScalarD<0>(const DTex* __restrict__, int, const TexGeo&) {
+  return 0.0f;
+}
+template <>
+__device__ __forceinline__ void texSpectrumD<0>(const DTex* __restrict__, int, const TexGeo&,
+                                                float* out) {
+  for (int k = 0; k < 16; k++) out[k] = 0.0f;
+}
+
 // a scalar-valued node at g
-static __device__ __noinline__ float texScalar(const DTex* __restrict__ T, int i, const TexGeo& g) {
+template <int D>
+__device__ __noinline__ float texScalarD(const DTex* __restrict__ T, int i, const TexGeo& g) {
   const DTex& t = T[i];
   switch (t.kind) {
     case 17:  // scaleTexture a s tex
-      return t.p[0] + t.p[1] * texScalar(T, t.a, g);
+      return t.p[0] + t.p[1] * texScalarD<D - 1>(T, t.a, g);
     case 18: {  // noiseTexture
       V3 q = texMap3d(t, g);
       return perlin3d(q.x, q.y, q.z);
@@ -200,27 +221,28 @@ static __device__ __noinline__ float texScalar(const DTex* __restrict__ T, int i
 }
 
 // a spectrum-valued node at g, into out
-static __device__ __noinline__ void texSpectrum(const DTex* __restrict__ T, int i, const TexGeo& g,
-                                                float* out) {
+template <int D>
+__device__ __noinline__ void texSpectrumD(const DTex* __restrict__ T, int i, const TexGeo& g,
+                                          float* out) {
   const DTex& t = T[i];
   switch (t.kind) {
     case 1: {  // spectrumBlend t1 t2 f
-      float x = texScalar(T, t.c, g);
+      float x = texScalarD<D - 1>(T, t.c, g);
       if (x <= 0) {
-        texSpectrum(T, t.a, g, out);
+        texSpectrumD<D - 1>(T, t.a, g, out);
       } else if (x >= 1) {
-        texSpectrum(T, t.b, g, out);
+        texSpectrumD<D - 1>(T, t.b, g, out);
       } else {
         float v1[16], v2[16];
-        texSpectrum(T, t.a, g, v1);
-        texSpectrum(T, t.b, g, v2);
+        texSpectrumD<D - 1>(T, t.a, g, v1);
+        texSpectrumD<D - 1>(T, t.b, g, v2);
         for (int k = 0; k < 16; k++) out[k] = v1[k] * (1.0f - x) + v2[k] * x;
       }
       return;
     }
     case 2: {  // checkerBoard: floor (x sx) + floor (y sy) + floor (z sz), even -> t1
       long long c = floorInt(g.p.x * t.p[0]) + floorInt(g.p.y * t.p[1]) + floorInt(g.p.z * t.p[2]);
-      texSpectrum(T, (c & 1) == 0 ? t.a : t.b, g, out);
+      texSpectrumD<D - 1>(T, (c & 1) == 0 ? t.a : t.b, g, out);
       return;
     }
     case 3: {  // graphPaper lw m paper lines
@@ -228,11 +250,11 @@ static __device__ __noinline__ void texSpectrum(const DTex* __restrict__ T, int 
       texMap2d(t, g, x, z);
       float xf = fabsf(x - truncf(x)), zf = fabsf(z - truncf(z));  // properFraction
       float lo = t.p[0] / 2.0f, hi = 1.0f - lo;
-      texSpectrum(T, (xf < lo || zf < lo || xf > hi || zf > hi) ? t.b : t.a, g, out);
+      texSpectrumD<D - 1>(T, (xf < lo || zf < lo || xf > hi || zf > hi) ? t.b : t.a, g, out);
       return;
     }
     case 4: {  // gradient
-      float f = texScalar(T, t.c, g);
+      float f = texScalarD<D - 1>(T, t.c, g);
       const float* st = t.data;
       int n = t.ivalue;
       float pmin = st[0], pmax = st[17 * (n - 1)];
@@ -263,6 +285,15 @@ static __device__ __noinline__ void texSpectrum(const DTex* __restrict__ T, int 
       for (int k = 0; k < 16; k++) out[k] = t.spectrum[k];
       return;
   }
+}
+
+// the evaluators for a tree's root
+__device__ __forceinline__ float texScalar(const DTex* __restrict__ T, int i, const TexGeo& g) {
+  return texScalarD<BLING_TEX_MAX_DEPTH>(T, i, g);
+}
+__device__ __forceinline__ void texSpectrum(const DTex* __restrict__ T, int i, const TexGeo& g,
+                                            float* out) {
+  texSpectrumD<BLING_TEX_MAX_DEPTH>(T, i, g, out);
 }
 
 }  // namespace bgpu
