@@ -31,10 +31,19 @@ __device__ __forceinline__ Spec sConst(float c) {
   for (int i = 0; i < 16; i++) s.v[i] = c;
   return s;
 }
-__device__ __forceinline__ Spec sLoad(const float* p) {
+__device__ __forceinline__ Spec sLoad(const float* p) {  // p in global memory
   Spec s;
 #pragma unroll
   for (int i = 0; i < 16; i++) s.v[i] = __ldg(p + i);
+  return s;
+}
+// a material spectrum a BxDF points at: the scene's record in global memory,
+// or a textured material resolved into the shading thread's local memory,
+// so generic loads rather than the read-only global path
+__device__ __forceinline__ Spec sLoadAny(const float* p) {
+  Spec s;
+#pragma unroll
+  for (int i = 0; i < 16; i++) s.v[i] = p[i];
   return s;
 }
 __device__ __forceinline__ Spec operator+(const Spec& a, const Spec& b) {
@@ -315,7 +324,7 @@ enum { FR_NOOP, FR_DIEL, FR_COND };
 
 struct BxDF {
   int kind, type;
-  const float* r;  // spectrum in global memory, null = white
+  const float* r;  // spectrum of the material (global or local memory), null = white
   float A, B;      // Oren-Nayar
   float ei, et;    // dielectric Fresnel / transmission
   float e;         // Blinn exponent
@@ -328,7 +337,7 @@ struct BxDF {
 __device__ __forceinline__ V3 otherHemisphere(V3 w) { return V3{w.x, w.y, -w.z}; }
 __device__ __forceinline__ Spec bxR(const BxDF& b) {
   if (!b.r) return sConst(1.0f);
-  Spec s = sLoad(b.r);
+  Spec s = sLoadAny(b.r);
   return b.clampR ? sClamp01(s) : s;
 }
 
@@ -358,7 +367,7 @@ __device__ __forceinline__ Spec rTimesFresnel(const BxDF& b, float cosi) {
   Spec out;
 #pragma unroll
   for (int i = 0; i < 16; i++) {
-    float eta = __ldg(b.eta + i), k = __ldg(b.k + i);
+    float eta = b.eta[i], k = b.k[i];
     float tmpF = eta * eta + k * k;
     float tmp = (eta * eta + k * k) * (acosi * acosi);
     float ec2 = eta * (2.0f * acosi);
@@ -443,7 +452,7 @@ __device__ __forceinline__ void anisoSample(float ex, float ey, float u1, float 
 // the distribution's exponents in A and B, the coating depth in e
 __device__ __forceinline__ Spec fblendEval(const BxDF& b, V3 wo, V3 wi) {
   float costi = absCosTheta(wi), costo = absCosTheta(wo);
-  Spec rd = sLoad(b.r), rs = sLoad(b.eta), ra = sLoad(b.k);
+  Spec rd = sLoadAny(b.r), rs = sLoadAny(b.eta), ra = sLoadAny(b.k);
   Spec a = sConst(1.0f);
   if (b.e > 0) {
     float x = -(b.e * (costi + costo) / (costi * costo));
