@@ -182,3 +182,24 @@ def test_run_returns_timeout_at_its_iteration_bound_and_continues_later(gpu_ctx)
     ref, _ = _alone(gpu_ctx, g, p, 0)
     _same(film.read(), ref)
     b.close()
+
+
+@pytest.mark.parametrize("mode", [abi.BATCH_GRAPH, abi.BATCH_DEVICE_LOOP])
+def test_textured_scene_joins_a_running_batch(gpu_ctx, mode):
+    """a batch whose graph was captured for untextured scenes takes the
+    textured shading kernel once a scene with textures is registered; every
+    job still renders what it renders alone"""
+    from texture_scenes import textured_scene
+    cornell = gpu_ctx.scene(S.cornell_room(40, 32))
+    tex = gpu_ctx.scene(textured_scene(40, 28))
+    pc = S.cornell_params(40, 32, spp_side=2, max_depth=5, rr_depth=3, seed=3)
+    pt = S.render_params(40, 28, (2, 2), max_depth=5, sample_depth=2, rr_depth=3, seed=6)
+    b = Batch(gpu_ctx, slots=2048, graph_mode=mode, iters_per_launch=4)
+    fc, ft = gpu_ctx.film(40, 32), gpu_ctx.film(40, 28)
+    b.submit(cornell, fc, pc, 0)
+    b.step(2)
+    b.submit(tex, ft, pt, 1)
+    b.run()
+    _same(fc.read(), _alone(gpu_ctx, cornell, pc, 0)[0])
+    _same(ft.read(), _alone(gpu_ctx, tex, pt, 1)[0])
+    b.close()

@@ -30,7 +30,9 @@ def textured_scene(w=48, h=32, bump=True):
     cheb = s.tex_cell_noise(abi.DIST_CHEBYSHEV, S.identity_mapping(xf.scale(6, 6, 6)))
     crystal = s.tex_crystal(5, S.uv_mapping(12, 12, 0, 0))
     blend = s.tex_blend(red, blue, s.tex_scale(0.5, 1.0, noise))
-    checker = s.tex_checker((4.0, 4.0, 4.0), white, blend)
+    # the floor lies in y = 0, where floor (4 y) flips with the sign of the
+    # hit point's rounding residue: the checker ignores y
+    checker = s.tex_checker((4.0, 0.0, 4.0), white, blend)
     grad = s.tex_gradient([(0.0, rgb(0.1, 0.1, 0.1)), (0.3, rgb(0.9, 0.5, 0.1)),
                            (0.15, rgb(0.2, 0.7, 0.2)), (0.6, rgb(0.9, 0.9, 0.9))], cells)
     img = s.tex_image(image_pixels(), S.uv_mapping(3, 2, 0.1, 0))
