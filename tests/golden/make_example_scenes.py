@@ -30,8 +30,8 @@ from bling_gb300 import blingfile as B  # noqa: E402
 DEFAULT_SOURCE = Path("/root/reference/examples")
 
 # the examples whose scene content the GPU path renders
-EXAMPLES = ["blackbody-emission", "cornell-box", "cornell-box-specular", "matte-test",
-            "plastic-test", "race", "trans-matte"]
+EXAMPLES = ["blackbody-emission", "bumpmap", "cellnoise", "cornell-box", "cornell-box-specular",
+            "glass-torus", "matte-test", "plastic-test", "race", "substrate", "trans-matte"]
 
 NEUTRAL_RENDERER = ("renderer { sampler sampled { sampler { stratified 1 1 } "
                     "integrator { path maxDepth 5 sampleDepth 3 } } }")

@@ -6,7 +6,8 @@ materials (bling_material records as bytes), meshes (vertices, indices,
 normals, uvs, material), shapes (kind, parameters, object-to-world transform
 and its inverse, material, emission), lights (kind, spectrum, vector,
 environment map, world-to-light transform, sun/sky east and turbidity), the
-primitive order, the camera inputs (camera-to-world, lens radius, focal
+texture nodes (kind, children, mapping, numbers, spectrum, gradient steps,
+image pixels), the primitive order, the camera inputs (camera-to-world, lens radius, focal
 distance, field of view) and the
 job's image size, filter, sampler and depths.
 """
@@ -66,6 +67,18 @@ def save(job: B.Job, path: Path, source: str) -> None:
                                "env": l.env is not None, "w2l": l.w2l is not None,
                                "east": [float(np.float32(v)) for v in l.east],
                                "turbidity": float(np.float32(l.turbidity))})
+    meta["textures"] = []
+    for k, t in enumerate(sc.textures):
+        if t.spectrum is not None:
+            arrays[f"tex{k}_s"] = np.asarray(t.spectrum, np.float32)
+        if t.steps is not None:
+            arrays[f"tex{k}_steps"] = np.asarray(t.steps, np.float32)
+        if t.pixels is not None:
+            arrays[f"tex{k}_px"] = np.asarray(t.pixels, np.uint8)
+        meta["textures"].append({"kind": t.kind, "children": list(map(int, t.children)),
+                                 "ivalue": int(t.ivalue), "map_kind": int(t.mapping[0]),
+                                 "map": [float(np.float32(x)) for x in t.mapping[1]],
+                                 "p": [float(np.float32(x)) for x in t.p]})
     c2w, lr, fd, fov = job.camera_view
     arrays["camera_c2w"] = np.stack([c2w.m, c2w.inv])
     meta["camera"] = {"lens_radius": float(lr), "focal_distance": float(fd), "fov": float(fov)}
@@ -98,6 +111,14 @@ def load(path: Path) -> B.Job:
                                  xf.Transform(x[0], x[1]) if x is not None else None,
                                  east=tuple(l.get("east", (0.0, 0.0, 0.0))),
                                  turbidity=l.get("turbidity", 0.0)))
+    for k, t in enumerate(meta.get("textures", [])):
+        sc.textures.append(S.Texture(
+            t["kind"], tuple(t["children"]), t["ivalue"],
+            (t["map_kind"], tuple(np.float32(x) for x in t["map"])),
+            tuple(np.float32(x) for x in t["p"]),
+            z[f"tex{k}_s"] if f"tex{k}_s" in z else None,
+            z[f"tex{k}_steps"] if f"tex{k}_steps" in z else None,
+            z[f"tex{k}_px"] if f"tex{k}_px" in z else None))
     sc.prim_order = meta["prim_order"]
     c = z["camera_c2w"]
     cam = meta["camera"]

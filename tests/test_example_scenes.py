@@ -25,7 +25,8 @@ FIXTURES = F.fixtures()
 NAMES = [p.stem for p in FIXTURES]
 # scenes with glossy or specular paths, whose paths a last-bit difference of a
 # transcendental sends elsewhere more often
-GLOSSY = {"cornell-box-specular", "plastic-test", "race", "trans-matte"}
+GLOSSY = {"bumpmap", "cellnoise", "cornell-box-specular", "glass-torus", "plastic-test", "race",
+          "substrate", "trans-matte"}
 
 
 def reduced(job, longest=64):
@@ -69,6 +70,12 @@ def _record(job):
                 np.float32(lt.vec).tobytes(), np.float32(lt.east).tobytes(),
                 np.float32(lt.turbidity).tobytes(),
                 None if lt.w2l is None else lt.w2l.m.tobytes()]
+    for t in sc.textures:
+        out += [t.kind, tuple(t.children), t.ivalue, t.mapping[0],
+                np.float32(t.mapping[1]).tobytes(), np.float32(t.p).tobytes(),
+                None if t.spectrum is None else np.float32(t.spectrum).tobytes(),
+                None if t.steps is None else np.float32(t.steps).tobytes(),
+                None if t.pixels is None else np.asarray(t.pixels, np.uint8).tobytes()]
     out += [list(sc.prim_order), bytes(sc.camera), job.width, job.height, job.filter_kind]
     return out
 
