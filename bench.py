@@ -524,12 +524,24 @@ def _extent_samples(p):
     return extent_samples(p)
 
 
-def _films_equal(a, b):
-    """equal samples up to the order of float additions (box-filter weights exact)"""
+def _films_equal(a, b, spp=1):
+    """equal samples up to the order of float additions (box-filter weights
+    exact): a sum of n binary32 terms in another order differs by at most
+    about n * 2^-24 of the sum of their magnitudes, so the relative bar grows
+    with the samples per pixel (at least 1e-5)"""
+    return _film_diff(a, b, spp)["equal"]
+
+
+def _film_diff(a, b, spp=1):
     if not np.array_equal(a[..., 0], b[..., 0]):
-        return False
+        return {"equal": False, "weights_differ": True}
+    rtol = max(1e-5, 2.0 * spp * 2.0 ** -24)
     scale = float(np.abs(b[..., 1:]).max()) + 1e-30
-    return bool(np.allclose(a[..., 1:], b[..., 1:], rtol=1e-5, atol=1e-6 * scale))
+    err = np.abs(a[..., 1:] - b[..., 1:])
+    ok = err <= 1e-6 * scale + rtol * np.abs(b[..., 1:])
+    rel = float((err / (np.abs(b[..., 1:]) + 1e-6 * scale)).max())
+    return {"equal": bool(ok.all()), "rtol": rtol, "max_rel_err": rel,
+            "values_off": int((~ok).sum())}
 
 
 def measure_batched(args):
@@ -587,7 +599,8 @@ def measure_batched(args):
     b.run()
     batch_s = time.perf_counter() - t0
     bst = b.stats()
-    equal = all(_films_equal(f.read(), r) for f, r in zip(films, ref))
+    equal = all(_films_equal(f.read(), r, p.strata_x * p.strata_y)
+                for f, r, p in zip(films, ref, params))
     b.close()
     out = {
         "instances": len(inst), "triangles": sum(i.n_tris for i in inst),
@@ -687,7 +700,10 @@ def _serve(args, ctx, scenes, gs, jobs, rate):
     first = min(r[1]["submitted"] for r in res)
     last = max(r[1]["finished"] for r in res)
     lat = [r[1]["finished"] - r[1]["submitted"] for r in res]
-    equal = all(_films_equal(r[0], ref) for r, ref in zip(res, refs))
+    diffs = [_film_diff(r[0], ref, j.params.strata_x * j.params.strata_y)
+             for r, ref, j in zip(res, refs, jobs)]
+    equal = all(d["equal"] for d in diffs)
+    worst = max(range(len(diffs)), key=lambda k: diffs[k].get("max_rel_err", float("inf")))
     tot = sum(samples)
     plain_span = max(j.arrival for j in jobs) + 0.0
     plain_make = max(plain_lat[k] + jobs[k].arrival for k in range(len(jobs)))
@@ -707,6 +723,7 @@ def _serve(args, ctx, scenes, gs, jobs, rate):
                           "path_samples_per_s": round(tot / sum(service), 1)},
         "speedup": round((tot / (last - first)) / (tot / sum(service)), 3),
         "equal_images": equal,
+        "largest_film_difference": {"job": worst, **diffs[worst]},
     }
 
 
@@ -865,6 +882,13 @@ def run_ours(args):
         "kernel_ms": round(closest_s * 1e3, 4),
         "hbm_peak": hbm_peak, "hbm_peak_source": peak_kind,
         "frac_of_hbm": round(achieved / hbm_peak, 4)})
+    # the same kernel with 32 B counted per node visit, whatever the layout
+    # reads (B_ray = 32 + 8 + 32 N_nodes + 48 N_prims)
+    per_visit32 = 32 + 8 + 32 * counts["nodes_per_ray"] + 48 * counts["slots_per_ray"]
+    ach32 = per_visit32 * N_RAYS / closest_s / 1e9
+    roof["per_node_32B"] = {"algorithmic_bytes_per_ray": round(per_visit32, 1),
+                            "achieved": round(ach32, 1),
+                            "frac": round(ach32 / roof["peak"], 4)}
 
     if rank == 0:
         cpu = None
