@@ -15,7 +15,9 @@ The subset is what the GPU path renders:
 * objects: ``filter``, ``imageSize``, ``renderer``, ``transform``,
   ``newTransform``, ``camera``, ``light``, ``material``, ``emission``,
   ``prim``;
-* primitives: ``mesh`` and ``shape`` (box, cylinder, disk, quad, sphere);
+* primitives: ``mesh``, ``shape`` (box, cylinder, disk, quad, sphere),
+  ``heightMap`` (fbm and scale elevation maps, tessellated on the host) and
+  ``waveFront`` (Wavefront .obj files with a material map);
 * materials: matte, plastic, metal, glass, mirror, shinyMetal, transMatte,
   substrate, blackbody and bumpMap, every parameter a texture: constant,
   blend, checker, gradient, graphPaper and (PNG) image spectra; constant,
@@ -41,7 +43,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import abi, image
+from . import abi, image, noise
 from . import transform as xf
 from .gen_spectrum_tables import BANDS, LAMBDA_END, LAMBDA_START, f32_of_decimal, lerp
 from .scene import Light, Scene, identity_mapping, planar_mapping, render_params, uv_mapping
@@ -791,7 +793,11 @@ class _Parser:
             self._mesh()
         elif kind == "shape":
             self._shape()
-        elif kind in ("bezier", "heightMap", "julia", "mandelbulb", "waveFront"):
+        elif kind == "heightMap":
+            self._height_map()
+        elif kind == "waveFront":
+            self._wave_front()
+        elif kind in ("bezier", "julia", "mandelbulb"):
             raise Unsupported(f"primitive {kind}: the GPU path renders meshes and shapes")
         else:
             raise t.error(f"unknown primitive type {kind}")
@@ -817,6 +823,106 @@ class _Parser:
         v = np.asarray(verts, np.float32).reshape(-1, 3)
         m = self.scene.add_mesh(v, np.asarray(idx, np.int32), self._material())
         self.s.blocks.insert(0, ("mesh", m))
+
+    # -- scalar maps for heightMap (pScalarMap2d, MaterialParser.hs:228-245)
+    def _scalar_map2d(self):
+        """a function of float32 arrays (x, y) -> elevation"""
+        t = self.t
+
+        def body():
+            kind = t.word()
+            if kind == "fbm":  # texMap3dTo2d (fbm octaves omega) z
+                z = t.flt()
+                octaves = t.named_int("octaves")
+                omega = t.named_flt("omega")
+                return lambda x, y: noise.fbm(octaves, omega, x, y, np.full_like(x, z))
+            if kind == "scale":
+                f = t.flt()
+                m = self._scalar_map2d()
+                return lambda x, y: F(f) * m(x, y)
+            raise t.error(f"unknown scalar map type{kind}")
+        return t.block(body)
+
+    def _height_map(self):
+        """heightMap ns nt elevation transform (PrimitiveParser.hs:39-45,
+        Heightmap.hs:15-49): an ns x nt grid over [0, 1]^2 lifted by the
+        elevation, shading normals from central differences, uvs, built with
+        mkTriangleMesh in the given transform"""
+        t = self.t
+        ns, nt = t.integ(), t.integ()
+        elev = self._scalar_map2d()
+        tr = self.p_transform()
+        fns, fnt = F(ns), F(nt)
+        xs = np.arange(ns, dtype=F) / (fns - F(1))
+        zs = np.arange(nt, dtype=F) / (fnt - F(1))
+        X, Z = np.meshgrid(xs, zs)  # [z, x]: coords z-major, as the comprehension
+        X, Z = X.reshape(-1), Z.reshape(-1)
+        pts = np.stack([X, elev(X, Z), Z], -1)
+        ex, ez = F(1) / fns, F(1) / fnt
+        dx = elev(X - ex, Z) - elev(X + ex, Z)
+        dz = elev(X, Z - ez) - elev(X, Z + ez)
+        nrm = -_normalize_rows(np.stack([dx, np.full_like(dx, ex + ez), dz], -1))
+        uvs = np.stack([X / (fns - F(1)), Z / (fns - F(1))], -1)  # both over ns - 1
+        x, y = np.meshgrid(np.arange(ns - 1), np.arange(nt - 1))
+        x, y = x.reshape(-1), y.reshape(-1)
+        v = lambda a, b: a + b * ns  # noqa: E731
+        idx = np.stack([v(x, y), v(x + 1, y), v(x + 1, y + 1),
+                        v(x, y), v(x + 1, y + 1), v(x, y + 1)], -1).reshape(-1)
+        m = self.scene.add_mesh(_trans_points(tr, pts), idx.astype(np.int32), self._material(),
+                                normals=_trans_normals(tr, nrm), uvs=uvs)
+        self.s.blocks.insert(0, ("mesh", m))
+
+    def _wave_front(self):
+        """waveFront "file" materials { "name" { material } ... }
+        (PrimitiveParser.hs:69-72, IO/WaveFront.hs): the file's faces fanned
+        into triangles, grouped by `usemtl` into runs of one material (names
+        missing from the map take the current material), vertices moved by
+        the current transform.  Every triangle keeps its own corners' uvs and
+        normals, so the corners become vertices of their own; as the
+        reference reads them, a triangle's third corner takes the uv and
+        normal indices of its second, normals are not transformed, and the
+        last run is cut to the face count less its starting corner index."""
+        t = self.t
+        kind, val, line = t.next()
+        if kind != "str":
+            raise BlingFileError(f"line {line}: expected a file name, got {val!r}")
+        path = self.s.base / val[1:-1]
+        t.expect("materials")
+
+        def body():
+            mats = {}
+            while not t.at("}"):
+                k, name, ln = t.next()
+                if k != "str":
+                    raise BlingFileError(f"line {ln}: expected a material name, got {name!r}")
+                mats[name[1:-1]] = t.block(self._material_body)
+            return mats
+        mats = t.block(body)
+        obj = _read_obj(path)
+        default = self._material()
+        P = _trans_points(self.s.transform, obj["v"]) if len(obj["v"]) else obj["v"]
+        corners = obj["corners"]  # (n, 3): point, uv, normal index per face corner, 0-based
+        n_tri = len(corners) // 3
+        # matIntervals: runs from each usemtl's corner count; the last one ends
+        # at the triangle count (WaveFront.hs:95-99, 111)
+        starts = [("default", 0)] + obj["mtls"]
+        ends = [c for _, c in obj["mtls"]] + [n_tri]
+        meshes = []
+        for (name, s0), e in zip(starts, ends):
+            if e - s0 <= 0:
+                continue
+            tris = list(range(s0, s0 + (e - s0), 3))  # [s, s+3 .. s+l-1], corner indices
+            tris = [i for i in tris if i + 2 < len(corners)]
+            if not tris:
+                continue
+            mat = mats.get(name, default)
+            meshes += _obj_meshes(P, obj["vn"], obj["vt"], corners, tris, mat)
+        for mesh in meshes:
+            m = self.scene.add_mesh(*mesh)
+            self.s.blocks.insert(0, ("mesh", m))
+        # blocks are newest first: this primitive's meshes in their own order
+        k = len(meshes)
+        self.s.blocks[:k] = self.s.blocks[:k][::-1]
 
     def _shape(self):
         t = self.t
@@ -848,6 +954,120 @@ class _Parser:
         sh = self.scene.add_shape(kind, tuple(float(p) for p in params), self.s.transform,
                                   self._material(), emission=self.s.emit)
         self.s.blocks.insert(0, ("shape", sh))
+
+
+def _trans_points(t: xf.Transform, p) -> np.ndarray:
+    """trans_point of an (n, 3) array, float32, same operation order"""
+    m = [F(x) for x in t.m]
+    x, y, z = (np.asarray(p[:, k], F) for k in range(3))
+
+    def row(r):
+        return ((m[4 * r] * x + m[4 * r + 1] * y) + m[4 * r + 2] * z) + m[4 * r + 3]
+    xp, yp, zp, wp = row(0), row(1), row(2), row(3)
+    one = wp == F(1)
+    out = np.stack([np.where(one, xp, xp / wp), np.where(one, yp, yp / wp),
+                    np.where(one, zp, zp / wp)], -1)
+    return out.astype(F)
+
+
+def _trans_normals(t: xf.Transform, n) -> np.ndarray:
+    """transNormal (Transform.hs:266-272) of an (n, 3) array: the transposed
+    inverse, float32"""
+    mi = [F(x) for x in t.inv]
+    x, y, z = (np.asarray(n[:, k], F) for k in range(3))
+    return np.stack([(mi[0] * x + mi[4] * y) + mi[8] * z, (mi[1] * x + mi[5] * y) + mi[9] * z,
+                     (mi[2] * x + mi[6] * y) + mi[10] * z], -1).astype(F)
+
+
+def _normalize_rows(v) -> np.ndarray:
+    """normalize (Math.hs:349-353) of each row, float32"""
+    v = np.asarray(v, F)
+    sl = (v[:, 0] * v[:, 0] + v[:, 1] * v[:, 1]) + v[:, 2] * v[:, 2]
+    il = F(1) / np.sqrt(np.where(sl != 0, sl, F(1)))
+    out = v * il[:, None]
+    out[sl == 0] = (0, 1, 0)
+    return out.astype(F)
+
+
+def _read_obj(path: Path) -> dict:
+    """The lines of a Wavefront .obj file that waveFrontParser reads
+    (IO/WaveFront.hs:128-211): v, vn (normalised), vt (v defaults to 1), f
+    (fanned; point/uv/normal indices 1-based, a missing one 0, so -1 here),
+    usemtl (the material's name and the corner count so far); other lines
+    are skipped"""
+    v, vn, vt, corners, mtls = [], [], [], [], []
+    for raw in path.read_text().splitlines():
+        parts = raw.split()
+        if not parts:
+            continue
+        key = parts[0]
+        if key == "v":
+            v.append([f32_of_decimal(x) for x in parts[1:4]])
+        elif key == "vn":
+            vn.append([f32_of_decimal(x) for x in parts[1:4]])
+        elif key == "vt":
+            vt.append((f32_of_decimal(parts[1]),
+                       f32_of_decimal(parts[2]) if len(parts) > 2 else F(1)))
+        elif key == "f":
+            idx = []
+            for tok in parts[1:]:
+                fs = tok.split("/")
+                p = int(fs[0])
+                uv = int(fs[1]) if len(fs) > 1 and fs[1] else 0
+                nn = int(fs[2]) if len(fs) > 2 and fs[2] else 0
+                idx.append((p - 1, uv - 1, nn - 1))
+            for k in range(1, len(idx) - 1):  # triangulate: a fan
+                corners += [idx[0], idx[k], idx[k + 1]]
+        elif key == "usemtl":
+            mtls.append((raw.split(None, 1)[1].strip() if len(parts) > 1 else "", len(corners)))
+    vn_arr = _normalize_rows(np.asarray(vn, F).reshape(-1, 3)) if vn else np.zeros((0, 3), F)
+    return {"v": np.asarray(v, F).reshape(-1, 3), "vn": vn_arr, "vt": np.asarray(vt, F).reshape(-1, 2),
+            "corners": np.asarray(corners, np.int64).reshape(-1, 3), "mtls": mtls}
+
+
+def _obj_meshes(P, VN, VT, corners, tris, mat):
+    """the triangles at corner indices `tris` (one run of a material) as
+    meshes of three vertices per triangle, split where the presence of
+    normals changes (a mesh has normals for all its vertices or none)"""
+    out = []
+    run = []
+
+    def flush():
+        if not run:
+            return
+        has_n = run[0][1]
+        verts, nrm, uvs = [], [], []
+        for i, _ in run:
+            c = corners[i:i + 3]
+            # wfTriUVs / wfTriNormals: corners i, i+1 and i+1 (WaveFront.hs:51-76)
+            ui = (c[0][1], c[1][1], c[1][1])
+            ni = (c[0][2], c[1][2], c[1][2])
+            verts += [P[c[0][0]], P[c[1][0]], P[c[2][0]]]
+            if min(ui) >= 0:
+                uvs += [VT[ui[0]], VT[ui[1]], VT[ui[2]]]
+            else:  # triangleDefaultUVs
+                uvs += [(0, 0), (1, 0), (1, 1)]
+            if has_n:
+                nrm += [VN[ni[0]], VN[ni[1]], VN[ni[2]]]
+        k = len(run)
+        out.append((np.asarray(verts, F).reshape(-1, 3), np.arange(3 * k, dtype=np.int32), mat,
+                    np.asarray(nrm, F).reshape(-1, 3) if has_n else None,
+                    np.asarray(uvs, F).reshape(-1, 2)))
+        run.clear()
+    for i in tris:
+        c = corners[i:i + 3]
+        ni = (c[0][2], c[1][2], c[1][2])
+        if max(ni) < 0:
+            has_n = False
+        elif min(ni) >= 0:
+            has_n = True
+        else:
+            raise BlingFileError("a face gives normals for some corners only")
+        if run and run[0][1] != has_n:
+            flush()
+        run.append((i, has_n))
+    flush()
+    return out
 
 
 def parse(text: str, base_path: str | Path = ".") -> Job:

@@ -31,7 +31,8 @@ DEFAULT_SOURCE = Path("/root/reference/examples")
 
 # the examples whose scene content the GPU path renders
 EXAMPLES = ["blackbody-emission", "bumpmap", "cellnoise", "cornell-box", "cornell-box-specular",
-            "glass-torus", "matte-test", "plastic-test", "race", "substrate", "trans-matte"]
+            "cornell-box-underwater", "ducky", "glass-torus", "heightmap", "matte-test",
+            "plastic-test", "race", "substrate", "trans-matte"]
 
 NEUTRAL_RENDERER = ("renderer { sampler sampled { sampler { stratified 1 1 } "
                     "integrator { path maxDepth 5 sampleDepth 3 } } }")

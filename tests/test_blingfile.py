@@ -249,3 +249,66 @@ def test_reference_cornell_box_example_parses():
         B.Job(j.scene, 24, 24, abi.FILTER_BOX, (0, 0, 0, 0), "path", strata=(1, 1),
               max_depth=3).params(), 0)
     assert np.isfinite(film).all()
+
+
+def test_wave_front_meshes(tmp_path):
+    """waveFront (IO/WaveFront.hs): faces fanned, runs by usemtl, positions
+    moved by the current transform, normals as read (normalised), a
+    triangle's third corner taking its second corner's uv and normal, and
+    the last run cut to the triangle count less its first corner index"""
+    (tmp_path / "m.obj").write_text("""# two quads and a triangle
+v 0 0 0
+v 1 0 0
+v 1 1 0
+v 0 1 0
+v 2 0 0
+vt 0.25 0.5
+vt 0.75
+vn 0 0 2
+vn 0 1 0
+usemtl A
+f 1/1/1 2/2/1 3/1/2 4/2/2
+usemtl B
+f 2//2 5//2 3//1
+""")
+    j = B.parse('newTransform { translate 0 0 5 }\n'
+                'prim { waveFront "m.obj" materials { "A" { matte kd { constant rgbR 1 0 0 } '
+                'sigma { constant 0 } } } }', tmp_path)
+    sc = j.scene
+    # runs: A from corner 0 to corner 6 (two triangles), B from corner 6 to
+    # the triangle count 3 -- negative, so B's triangle is dropped
+    assert sc.n_triangles == 2 and len(sc.meshes) == 1
+    (m,) = sc.meshes
+    assert sc.materials[m.material].kind == abi.MAT_MATTE
+    assert np.array_equal(m.vertices[:3], np.array([[0, 0, 5], [1, 0, 5], [1, 1, 5]], F))
+    # corners (1, 2, 3): uvs (vt1, vt2, vt2), normals (vn1, vn1, vn1)
+    assert np.array_equal(m.uvs[:3], np.array([[0.25, 0.5], [0.75, 1], [0.75, 1]], F))
+    assert np.array_equal(m.normals[:3], np.array([[0, 0, 1]] * 3, F))
+    # the fan's second triangle: corners (1, 3, 4), uv/normal of corner 3 twice
+    assert np.array_equal(m.vertices[3:], np.array([[0, 0, 5], [1, 1, 5], [0, 1, 5]], F))
+    assert np.array_equal(m.normals[3:], np.array([[0, 0, 1], [0, 1, 0], [0, 1, 0]], F))
+    # the material map falls back to the current material for unknown names
+    j2 = B.parse('prim { waveFront "m.obj" materials { } }', tmp_path)
+    assert j2.scene.materials[j2.scene.meshes[0].material].kind == abi.MAT_MATTE
+
+
+def test_height_map_mesh():
+    """heightMap ns nt elevation transform (Heightmap.hs:15-49)"""
+    from bling_gb300 import noise
+    j = B.parse("prim { heightMap 5 4 { scale 2 { fbm 0.5 octaves 2 omega 0.5 } } "
+                "{ scale 3 1 3 } }")
+    (m,) = j.scene.meshes
+    assert len(m.vertices) == 20 and len(m.indices) == 3 * 2 * 4 * 3
+    # the grid is z-major; x = i / (ns - 1), z = k / (nt - 1)
+    x, z = F(2) / F(4), F(1) / F(3)
+    y = F(2) * noise.fbm(2, 0.5, np.array([x], F), np.array([z], F), np.array([0.5], F))[0]
+    assert np.array_equal(m.vertices[1 * 5 + 2], np.array([F(3) * x, y, F(3) * z], F))
+    assert m.indices[:6].tolist() == [0, 1, 6, 0, 6, 5]
+    # uvs over ns - 1 on both axes (the reference divides z by fns - 1 too)
+    assert np.array_equal(m.uvs[5 * 3 + 4], np.array([F(1) / F(4), F(1) / F(4)], F))
+    # shading normals: -(normalize (dx, ex + ez, dz)), so below the surface,
+    # through transNormal of the scale (x and z divided by 3)
+    assert (m.normals[:, 1] < 0).all()
+    n0 = B._normalize_rows(np.array([[0, F(1) / F(5) + F(1) / F(4), 0]], F))
+    flat = np.isclose(m.normals[:, 0], 0) & np.isclose(m.normals[:, 2], 0)
+    assert np.allclose(m.normals[flat], -n0) if flat.any() else True

@@ -25,8 +25,8 @@ FIXTURES = F.fixtures()
 NAMES = [p.stem for p in FIXTURES]
 # scenes with glossy or specular paths, whose paths a last-bit difference of a
 # transcendental sends elsewhere more often
-GLOSSY = {"bumpmap", "cellnoise", "cornell-box-specular", "glass-torus", "plastic-test", "race",
-          "substrate", "trans-matte"}
+GLOSSY = {"bumpmap", "cellnoise", "cornell-box-specular", "cornell-box-underwater", "ducky",
+          "glass-torus", "heightmap", "plastic-test", "race", "substrate", "trans-matte"}
 
 
 def reduced(job, longest=64):
