@@ -87,7 +87,7 @@ struct BatchQueues {
   int32_t* cls;        // shading class per position
   unsigned int* bins;  // kBins counters / offsets
 };
-constexpr size_t kQueueWordsB = 6;
+constexpr size_t kQueueWordsB = 7;  // the shadow queue takes two
 
 // vertex temporaries (everything of Slots but T, L and ray), single-buffered
 constexpr size_t kTempWords = kSlotWords - 16 - 16 - 8;
@@ -321,14 +321,13 @@ __global__ void __launch_bounds__(128) k_btrace_shadow(BatchCtl* ctl,
   const PathState& S = ps.b[ctl->cur];
   int64_t n = (int64_t)ctl->c[C_SHADOW];
   const int32_t* __restrict__ queue = Q.shadow;
-  traceWarpPersistent<true, LAYOUT, false>(
+  traceWarpPersistent<true, LAYOUT, false, true>(
       scenes[0].A, n, ctl->c + C_NEXT_SHADOW,
-      [&](int64_t q) { return loadShadowRay(tmp, queue[q]); },
+      [&](int64_t q, bool& by_intersect) { return loadOcclusionRay(tmp, queue[q], by_intersect); },
       [&](int64_t q, const RayQueryResult& res) {
-        tmp.svis[queue[q]] = res.hit ? 0 : 1;
-        if (res.prim == kDegenerateRay) atomicAdd(ctl->c + C_DEGENERATE, 1ull);
+        storeOcclusion(tmp, queue[q], res, ctl->c + C_DEGENERATE);
       },
-      nullptr, [&](int64_t q) { return &scenes[S.scene[queue[q]]].A; });
+      nullptr, [&](int64_t q) { return &scenes[S.scene[occlusionSlot(queue[q])]].A; });
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ctl->c + C_ANY, (unsigned long long)n);
 }
 
@@ -427,7 +426,7 @@ __global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJob
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += stride) {
-    VertexOut o{false, false, false};
+    VertexOut o{false, false, false, false};
     bool fin = false;
     int job = -1;
     int q = 0;
@@ -443,6 +442,7 @@ __global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJob
       });
     }
     queueAppend(o.shadow, (int)q, Q.shadow, c + C_SHADOW);
+    queueAppend(o.mis_any, ~(int)q, Q.shadow, c + C_SHADOW);
     queueAppend(o.mis, (int)q, Q.mis, c + C_MIS);
     queueAppend(o.resolve, (int)q, Q.resolve, c + C_RESOLVE);
     pathsDone(fin, job, ctl, job_done);
@@ -764,7 +764,7 @@ int batch_create(int device, cudaStream_t stream, const BatchConfig& cfg, BatchE
   t.svis = (int32_t*)take(1);
   t.mray = take(8);
   t.mhit = reinterpret_cast<float4*>(take(4));
-  b->q.shadow = (int32_t*)take(1);
+  b->q.shadow = (int32_t*)take(2);  // shadow rays and occlusion-only MIS rays
   b->q.mis = (int32_t*)take(1);
   b->q.resolve = (int32_t*)take(1);
   b->q.keys = (uint32_t*)take(1);

@@ -13,8 +13,9 @@
 //                   one BSDF sample for MIS (sampleOneLight/estimateDirect,
 //                   Scene.hs:61-118), Russian roulette and the continuation
 //                   sample; queues the shadow ray, the MIS ray and the vertex
-//   k_trace_shadow  any hit of the shadow rays (occluded)
-//   k_trace_mis     closest hit of the MIS rays
+//   k_trace_shadow  any hit of the shadow rays (occluded), and of the MIS rays
+//                   toward lights other than area lights (whether they hit)
+//   k_trace_mis     closest hit of the MIS rays toward area lights
 //   k_resolve       adds the vertex's radiance, updates the throughput,
 //                   queues the continuing paths and splats finished ones into
 //                   the film (addSample, Image.hs:250-299)
@@ -58,11 +59,11 @@ static void carve(unsigned char* base, size_t cap, Slots& st, Queues& q,
   int32_t* qw = (int32_t*)w;
   q.live[0] = qw;
   q.live[1] = qw + cap;
-  q.shadow = qw + 2 * cap;
-  q.mis = qw + 3 * cap;
-  q.resolve = qw + 4 * cap;
-  q.sorted = qw + 5 * cap;
-  q.cls = qw + 6 * cap;
+  q.shadow = qw + 2 * cap;  // 2 cap entries: shadow rays and occlusion-only MIS rays
+  q.mis = qw + 4 * cap;
+  q.resolve = qw + 5 * cap;
+  q.sorted = qw + 6 * cap;
+  q.cls = qw + 7 * cap;
 }
 
 __device__ __forceinline__ unsigned* classCounts(unsigned long long* counters) {
@@ -242,22 +243,23 @@ __global__ void __launch_bounds__(128, 10) k_trace(DevAccel A, Slots st, const i
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_CLOSEST, (unsigned long long)n);
 }
 
-// occlusion of the shadow rays (occluded, Scene.hs:45-47)
+// occlusion of the shadow rays (occluded, Scene.hs:45-47) and whether the
+// MIS rays toward lights other than area lights hit anything
 template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_trace_shadow(DevAccel A, Slots st,
                                                       const int32_t* __restrict__ queue,
                                                       unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_SHADOW];
-  traceWarpPersistent<true, LAYOUT, false>(
-      A, n, counters + C_NEXT_SHADOW, [&](int64_t q) { return loadShadowRay(st, queue[q]); },
+  traceWarpPersistent<true, LAYOUT, false, true>(
+      A, n, counters + C_NEXT_SHADOW,
+      [&](int64_t q, bool& by_intersect) { return loadOcclusionRay(st, queue[q], by_intersect); },
       [&](int64_t q, const RayQueryResult& res) {
-        st.svis[queue[q]] = res.hit ? 0 : 1;
-        if (res.prim == kDegenerateRay) atomicAdd(counters + C_DEGENERATE, 1ull);
+        storeOcclusion(st, queue[q], res, counters + C_DEGENERATE);
       });
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_ANY, (unsigned long long)n);
 }
 
-// closest hit of the BSDF-sampled MIS rays
+// closest hit of the BSDF-sampled MIS rays toward area lights
 template <int LAYOUT>
 __global__ void __launch_bounds__(128, 10) k_trace_mis(DevAccel A, Slots st,
                                                    const int32_t* __restrict__ queue,
@@ -284,7 +286,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, Pass
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;  // whole warps stay together for the appends
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
-    VertexOut o{false, false, false};
+    VertexOut o{false, false, false, false};
     int s = 0;
     if (q < n) {
       s = qin[q];
@@ -294,6 +296,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, Pass
       });
     }
     queueAppend(o.shadow, s, Q.shadow, counters + C_SHADOW);
+    queueAppend(o.mis_any, ~s, Q.shadow, counters + C_SHADOW);
     queueAppend(o.mis, s, Q.mis, counters + C_MIS);
     queueAppend(o.resolve, s, Q.resolve, counters + C_RESOLVE);
   }

@@ -76,6 +76,12 @@ __device__ __forceinline__ bool isBlack(const Spec& s) {
   for (int i = 0; i < 16; i++) b = b && (s.v[i] == 0);
   return b;
 }
+__device__ __forceinline__ bool allFinite(const Spec& s) {
+  bool b = true;
+#pragma unroll
+  for (int i = 0; i < 16; i++) b = b && isfinite(s.v[i]);
+  return b;
+}
 __device__ __forceinline__ Spec sClamp01(const Spec& a) {
   Spec s;
 #pragma unroll

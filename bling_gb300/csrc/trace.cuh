@@ -145,9 +145,14 @@ __device__ __forceinline__ float qbyte(uint32_t word, uint32_t sel) {
 // With an `accel_of` functor (ray index -> const DevAccel*) every lane walks
 // the scene of its own ray (batches of jobs over several scenes, which must
 // share the node layout); otherwise all rays walk A.
+// MIXED (any-hit walks only): `load(q, by_intersect)` also says, per ray,
+// which predicate answers an analytic shape: Shape.intersects (false, the
+// occlusion test) or Shape.intersect (true: whether a closest-hit query would
+// find a hit).  The two differ, e.g. a box does not `intersect` a ray that
+// starts inside it, while it `intersects` it.  Triangles answer both alike.
 constexpr int kSentinel = INT32_MIN;
 
-template <bool ANY, int LAYOUT, bool COUNT, class LoadRay, class Emit,
+template <bool ANY, int LAYOUT, bool COUNT, bool MIXED = false, class LoadRay, class Emit,
           class AccelOf = std::nullptr_t>
 __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n,
                                                     unsigned long long* __restrict__ next_ray,
@@ -169,6 +174,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
   constexpr int kStack = WIDE ? kWideStack : kTraversalStack;
   int64_t rid = -1;
   bool exhausted = false;
+  bool by_intersect = false;  // MIXED: this ray's shapes answer by Shape.intersect
   Ray r;
   V3 inv;
   int oct = 0;
@@ -213,7 +219,10 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
         unsigned long long my = base + (unsigned long long)__popc(m & lt_mask);
         if ((int64_t)my < n) {
           rid = (int64_t)my;
-          r = load(rid);
+          if constexpr (MIXED)
+            r = load(rid, by_intersect);
+          else
+            r = load(rid);
           if (degenerateRay(r)) {
             emit(rid, RayQueryResult{true, NAN, 0.0f, 0.0f, kDegenerateRay});
             rid = -1;  // take another ray next round
@@ -429,7 +438,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
           } else {
             const DShape& sh = TW_ACC(shapes)[__float_as_int(s0.x)];
             Ray ro = transRay(sh.w2o, Ray{r.o, r.d, r.tmin, ANY ? r.tmax : best_t});
-            if (ANY) {
+            if (ANY && !(MIXED && by_intersect)) {
               hit = shapeIntersects(sh, ro);
             } else {
               float e;

@@ -14,7 +14,9 @@
 
 namespace bgpu {
 
-enum : int { VF_SHADOW = 1, VF_MIS = 2, VF_CONT = 4 };
+// VF_LE: the vertex saw emission (a specular path hit an area light); its
+// spectrum is in intl, which is neither written nor read otherwise
+enum : int { VF_SHADOW = 1, VF_MIS = 2, VF_CONT = 4, VF_LE = 8 };
 
 struct Slots {
   size_t cap;
@@ -54,7 +56,7 @@ enum : int {
 };
 
 constexpr size_t kSlotWords = 16 * 6 + 8 + 4 + 3 + 8 + 1 + 8 + 4;  // per slot, 4-byte words
-constexpr size_t kQueueWords = 7;
+constexpr size_t kQueueWords = 8;  // the shadow queue takes two
 // counters: C_COUNT 8-byte counters, then the shading-class counts and
 // cursors (kShadeClasses 4-byte entries each, 16 reserved)
 constexpr size_t kCounterBytes = 256;
@@ -315,8 +317,31 @@ int integrator_pass_params(const bling_render_params& p, uint64_t pass, int fw, 
                            PassParams& P, std::string& err);
 
 struct VertexOut {
-  bool shadow, mis, resolve;
+  bool shadow, mis, mis_any, resolve;
 };
+
+// Entries of the shadow queue: a slot s (its shadow ray, visibility into
+// svis), or ~s for an MIS ray that needs only whether it meets anything (a
+// light other than an area light: its radiance along the ray does not depend
+// on what the ray hits, only on whether it hits), answered into mhit like a
+// closest hit whose distance and barycentrics nobody reads.  The shadow
+// kernel walks them with the any-hit traversal in MIXED mode: an MIS entry's
+// shapes answer by Shape.intersect, as the closest-hit query of
+// sampleBsdfMis (Scene.hs:71-82) would, a shadow ray's by Shape.intersects.
+__device__ __forceinline__ int occlusionSlot(int e) { return e >= 0 ? e : ~e; }
+__device__ __forceinline__ Ray loadOcclusionRay(const Slots& st, int e, bool& by_intersect) {
+  by_intersect = e < 0;
+  return e >= 0 ? loadShadowRay(st, e) : loadRay7(st.mray, ~e);
+}
+__device__ __forceinline__ void storeOcclusion(const Slots& st, int e, const RayQueryResult& res,
+                                               unsigned long long* degenerate) {
+  if (e >= 0) {
+    st.svis[e] = res.hit ? 0 : 1;
+    if (res.prim == kDegenerateRay) atomicAdd(degenerate, 1ull);
+  } else {
+    st.mhit[~e] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
+  }
+}
 
 // First half of one vertex of the path in slot s at bounce `depth`
 // (Path.hs:49-87): emission on specular paths, the BSDF, one light sample
@@ -330,7 +355,7 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
                                                  const PassParams& P, const Slots& st, int s,
                                                  uint64_t g, int depth,
                                                  unsigned long long* counters, Finish finish) {
-  VertexOut out{false, false, false};
+  VertexOut out{false, false, false, false};
   int ix, iy;
   uint32_t sn;
   decodeSample(P, g, ix, iy, sn);
@@ -359,7 +384,11 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
   float thit = hit.x, b1 = hit.z, b2 = hit.w;
   HitGeom gm = hitGeometry(A, S, ray, prim, thit, b1, b2);
   V3 rd = ray.d;
-  storeBands(st.intl, s, specular ? intLe(S, gm, rd) : sConst(0));
+  int flags = 0;
+  if (specular && gm.light_id >= 0) {
+    storeBands(st.intl, s, intLe(S, gm, rd));
+    flags |= VF_LE;
+  }
   DMaterial tm;  // a textured material, resolved at this hit
   const DMaterial* mat = S.materials + gm.material;
   if constexpr (TEX) mat = hitMaterial(A, S, ray, prim, thit, b1, b2, gm, tm);
@@ -373,7 +402,6 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
   Bsdf bsdf = materialBsdf(*mat, gm.n, gm.sp, gm.sn, gm.sdpdu);
   V3 nn = bsdf.cs.n, p = bsdf.p;
   float eps = gm.eps;
-  int flags = 0;
   int lc = S.n_lights;
   int ln = 0;
   if (lc > 0) {
@@ -398,18 +426,31 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
         flags |= VF_SHADOW;
       }
     }
-    // sampleBsdfMis (Scene.hs:71-82), the hit deferred
+    // sampleBsdfMis (Scene.hs:71-82), the hit deferred.  Only an area
+    // light's term depends on which primitive the ray hits (a closest-hit
+    // query); an infinite light's on whether it hits at all (any hit).  A
+    // point or directional light emits along no ray (le is zero), so its
+    // term is f * 0 scaled by the weight: zero whatever the ray meets unless
+    // f or the weight is not finite or the ray is degenerate (a NaN sample);
+    // only then is the ray traced.
     BsdfSample bm = sampleBsdf(bsdf, wo, lBsdfCompU, lb1, lb2);
     if (!(bm.pdf == 0 || isBlack(bm.f))) {
-      storeBands(st.bsf, s, bm.f);
-      st.bsw[s] = powerHeuristic(bm.pdf, lightPdf(A, l, p, bm.wi));
-      storeRay(st.mray, s, Ray{p, bm.wi, eps, INFINITY});
-      flags |= VF_MIS;
+      float w = powerHeuristic(bm.pdf, lightPdf(A, l, p, bm.wi));
+      Ray mr{p, bm.wi, eps, INFINITY};
+      bool area = l.kind == DLIGHT_AREA;
+      if (area || l.kind == DLIGHT_INFINITE || !(isfinite(w) && allFinite(bm.f)) ||
+          degenerateRay(mr)) {
+        storeBands(st.bsf, s, bm.f);
+        st.bsw[s] = w;
+        storeRay(st.mray, s, mr);
+        flags |= VF_MIS;
+        out.mis = area;
+        out.mis_any = !area;
+      }
     }
   }
   // Russian roulette and the continuation (Path.hs:68-87)
-  Spec T = loadBands(st.T, s);
-  float pc = depth <= P.rr_depth ? 1.0f : hmin(0.75f, sY(T));
+  float pc = depth <= P.rr_depth ? 1.0f : hmin(0.75f, sY(loadBands(st.T, s)));
   float x = rnd1(smp, 3 + 4 * depth);
   if (!(x > pc)) {
     float uc = rnd1(smp, 0 + 4 * depth);
@@ -426,7 +467,6 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
   }
   st.vflags[s] = flags | (ln << 8);
   out.shadow = (flags & VF_SHADOW) != 0;
-  out.mis = (flags & VF_MIS) != 0;
   out.resolve = true;
   return out;
 }
@@ -474,7 +514,9 @@ __device__ __forceinline__ bool resolveVertex(const DevAccel& A, const DevShadin
   }
   Spec ed = lsv + bsv;  // estimateDirect = ls + bs (Scene.hs:95)
   Spec direct = lc == 1 ? ed : (lc > 1 ? sScale(ed, (float)lc) : sConst(0));
-  Spec lHere = loadBands(st.intl, s) + direct;
+  // intl is zero without VF_LE, and 0 + direct is direct (up to the sign of
+  // a zero, which the film's sums do not keep)
+  Spec lHere = (vf & VF_LE) ? loadBands(st.intl, s) + direct : direct;
   Spec T = loadBands(st.T, s);
   Spec Lr = loadBands(st.L, s) + T * lHere;
   if (vf & VF_CONT) {

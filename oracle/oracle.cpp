@@ -2359,6 +2359,26 @@ static int intLightId(const orc_scene& S, const Isect& it) {
   return s.emissive ? s.light_id : -1;
 }
 
+// Ray counts of the MIS ray, as the GPU integrator queries it (the answer
+// is the same either way; this only sets which counter it goes to): a
+// closest-hit query toward an area light, an any-hit query toward an
+// infinite light, and none toward a point or directional light when the
+// term f * le * weight is zero whatever the ray meets (le is zero; f and the
+// weight finite, the ray without NaN), else an any-hit query.
+static void countMisRay(const orc_scene& S, const Light& l, V p, const BsdfSample& b,
+                        const Ray& ray, Counters& C) {
+  if (l.kind == LIGHT_AREA) {
+    C.closest++;
+    return;
+  }
+  bool finite = std::isfinite(powerHeuristic(b.pdf, lightPdf(S, l, p, b.wi)));
+  for (int i = 0; i < 16; i++) finite = finite && std::isfinite(b.f.v[i]);
+  bool nan_ray = std::isnan(ray.o.x) || std::isnan(ray.o.y) || std::isnan(ray.o.z) ||
+                 std::isnan(ray.d.x) || std::isnan(ray.d.y) || std::isnan(ray.d.z) ||
+                 std::isnan(ray.tmin) || std::isnan(ray.tmax);
+  if (l.kind == BLING_LIGHT_INFINITE || !finite || nan_ray) C.any++;
+}
+
 // estimateDirect = sampleLightMis + sampleBsdfMis (Scene.hs:61-99)
 static Spec estimateDirect(const orc_scene& S, int li, V p, float eps, V n, V wo, const Bsdf& bsdf,
                            float ld1, float ld2, float ubc, float ubd1, float ubd2, Counters& C) {
@@ -2387,7 +2407,7 @@ static Spec estimateDirect(const orc_scene& S, int li, V p, float eps, V n, V wo
     if (!(b.pdf == 0 || isBlack(b.f))) {
       Ray ray{p, b.wi, eps, INF};
       Isect hit;
-      C.closest++;
+      countMisRay(S, l, p, b, ray, C);
       bool h = sceneIntersect(S, ray, hit);
       auto sc = [&](const Spec& lr) {
         float lPdf = lightPdf(S, l, p, b.wi);
