@@ -65,8 +65,21 @@ __device__ __forceinline__ float fmaxNaN(float a, float b) {
 // Widens a box's entry/exit distances by kBoxSlack (relative).  An infinite
 // bound stays infinite: n - |n| * s alone would turn +inf into inf - inf =
 // NaN and let a missed box pass.
-__device__ __forceinline__ float widenNear(float n) { return fminf(n, n - fabsf(n) * kBoxSlack); }
-__device__ __forceinline__ float widenFar(float f) { return fmaxf(f, f + fabsf(f) * kBoxSlack); }
+__device__ __forceinline__ float widenNear(float n) { return fminf(n, fmaf(-fabsf(n), kBoxSlack, n)); }
+__device__ __forceinline__ float widenFar(float f) { return fmaxf(f, fmaf(fabsf(f), kBoxSlack, f)); }
+
+// three-operand forms (sm_100 and later): one instruction for a box's entry
+// or exit over its three slabs
+__device__ __forceinline__ float fmax3NaN(float a, float b, float c) {
+  float r;
+  asm("max.NaN.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+__device__ __forceinline__ float fmin3NaN(float a, float b, float c) {
+  float r;
+  asm("min.NaN.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
 
 // Slab interval of a box.  A ray with a zero direction component (inv = +-inf)
 // is inside that slab for all t when the origin lies strictly between its
@@ -81,8 +94,8 @@ __device__ __forceinline__ void boxInterval(float lox, float hix, float loy, flo
   float x0 = (lox - o.x) * inv.x, x1 = (hix - o.x) * inv.x;
   float y0 = (loy - o.y) * inv.y, y1 = (hiy - o.y) * inv.y;
   float z0 = (loz - o.z) * inv.z, z1 = (hiz - o.z) * inv.z;
-  float n = fmaxNaN(fmaxNaN(fminNaN(x0, x1), fminNaN(y0, y1)), fminNaN(z0, z1));
-  float f = fminNaN(fminNaN(fmaxNaN(x0, x1), fmaxNaN(y0, y1)), fmaxNaN(z0, z1));
+  float n = fmax3NaN(fminNaN(x0, x1), fminNaN(y0, y1), fminNaN(z0, z1));
+  float f = fmin3NaN(fmaxNaN(x0, x1), fmaxNaN(y0, y1), fmaxNaN(z0, z1));
   tn = widenNear(n);
   tf = widenFar(f);
 }
@@ -254,9 +267,10 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
     }
     if (!__any_sync(FULL, rid >= 0 || !exhausted)) return;
     // ---- node phase
-    for (;;) {
+    // the vote at the end of a step implies this one for the next step
+    bool go = __any_sync(FULL, rid >= 0 && cur >= 0);
+    while (go) {
       bool work = rid >= 0 && cur >= 0;
-      if (!__any_sync(FULL, work)) break;
       if (work) {
         if (COUNT) cnt->nodes++;
         if (WIDE) {
@@ -412,7 +426,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
         }
       }
       // leave the node phase once no lane both lacks a leaf and has nodes to visit
-      if (!__any_sync(FULL, rid >= 0 && leaf == kSentinel && cur >= 0)) break;
+      go = __any_sync(FULL, rid >= 0 && leaf == kSentinel && cur >= 0);
     }
     // ---- leaf phase
     for (;;) {
