@@ -926,9 +926,10 @@ def run_ours(args):
 
 def traversal_counts(g, rays):
     """Nodes visited and leaf slots tested per closest-hit ray, counted by the
-    instrumented traversal on a 256k-ray subsample."""
+    instrumented traversal (depth-first, each leaf tested when reached) on the
+    first 1M rays."""
     try:
-        return g.traversal_counts(np.ascontiguousarray(rays[:, : 1 << 18]))
+        return g.traversal_counts(np.ascontiguousarray(rays[:, : 1 << 20]))
     except AttributeError:
         return {"nodes_per_ray": float("nan"), "slots_per_ray": float("nan")}
 

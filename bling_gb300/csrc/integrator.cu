@@ -415,7 +415,8 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
           A, S, P, st, Q, shaded, depth, C_LIVE0 + in, d_film, d_filter, counters);
     withLayout(A.wide, [&](auto L) {
       k_trace_shadow<decltype(L)::value><<<gs, block, 0, stream>>>(A, st, Q.shadow, counters);
-      k_trace_mis<decltype(L)::value><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);
+      if (S.n_area_lights > 0)  // else the closest-hit MIS queue stays empty
+        k_trace_mis<decltype(L)::value><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);
     });
     k_resolve<<<std::min(G.resolve, cap_blocks), block, 0, stream>>>(A, S, P, st, Q,
                                                                       C_LIVE0 + (1 - in), d_film,

@@ -125,6 +125,7 @@ struct DevShading {
   const float* shape_emission;  // 16 per shape
   const DLight* lights;
   int32_t n_lights;
+  int32_t n_area_lights;  // MIS rays need closest hits only toward these
   int32_t n_materials;
   bling_camera_desc camera;
   size_t bytes;

@@ -255,6 +255,7 @@ int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
     o.kind = DLIGHT_AREA;
     o.shape = ~v;
     lights.push_back(o);
+    out.n_area_lights++;
   }
   void* dl;
   if ((rc = up(lights.data(), lights.size() * sizeof(DLight), &dl))) return rc;

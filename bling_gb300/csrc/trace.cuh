@@ -270,7 +270,9 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
     // the vote at the end of a step implies this one for the next step
     bool go = __any_sync(FULL, rid >= 0 && cur >= 0);
     while (go) {
-      bool work = rid >= 0 && cur >= 0;
+      // COUNT walks in plain depth-first order: a lane stops at its first
+      // leaf, which the leaf phase tests before any further node is visited
+      bool work = rid >= 0 && cur >= 0 && (!COUNT || leaf == kSentinel);
       if (work) {
         if (COUNT) cnt->nodes++;
         if (WIDE) {

@@ -368,7 +368,10 @@ int bling_trace_any_device(bling_scene* scene, const float* d_rays, size_t n, ui
 
 /* Work of the closest-hit traversal on a batch of host rays, as the
  * reference's dbgTraverse counts it (Primitive/KdTree.hs:252-281): BVH nodes
- * visited and leaf primitives tested, summed over the batch. */
+ * visited and leaf primitives tested, summed over the batch.  The walk is
+ * depth-first with each leaf tested as soon as it is reached, as a CPU walk
+ * of the same tree would go (the query kernels postpone leaves to keep a
+ * warp's lanes together, which can visit a few more nodes). */
 int bling_trace_counts(bling_scene* scene, const float* rays, size_t n, uint64_t* nodes_visited,
                        uint64_t* prims_tested);
 
