@@ -230,7 +230,7 @@ __global__ void __launch_bounds__(128) k_raybin_scatter(const int32_t* __restric
 
 // closest hit of the live paths' rays (scIntersect)
 template <int LAYOUT>
-__global__ void __launch_bounds__(128, 10) k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
+__global__ void __launch_bounds__(128, 8) k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
                                                const unsigned long long* __restrict__ qcount,
                                                unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)*qcount;
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(128, 10) k_trace(DevAccel A, Slots st, const i
 // occlusion of the shadow rays (occluded, Scene.hs:45-47) and whether the
 // MIS rays toward lights other than area lights hit anything
 template <int LAYOUT>
-__global__ void __launch_bounds__(128, 10) k_trace_shadow(DevAccel A, Slots st,
+__global__ void __launch_bounds__(128, 8) k_trace_shadow(DevAccel A, Slots st,
                                                       const int32_t* __restrict__ queue,
                                                       unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_SHADOW];
@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(128, 10) k_trace_shadow(DevAccel A, Slots st,
 
 // closest hit of the BSDF-sampled MIS rays toward area lights
 template <int LAYOUT>
-__global__ void __launch_bounds__(128, 10) k_trace_mis(DevAccel A, Slots st,
+__global__ void __launch_bounds__(128, 8) k_trace_mis(DevAccel A, Slots st,
                                                    const int32_t* __restrict__ queue,
                                                    unsigned long long* __restrict__ counters) {
   int64_t n = (int64_t)counters[C_MIS];

@@ -214,6 +214,10 @@ def test_parsed_bling_scene_vs_oracle(gpu_ctx):
     _compare(fg, fo, rel=2e-3, frac=0.9)
     assert st_g["path_samples"] == st_o[0]["path_samples"]
     assert st_g["nonfinite_drops"] == 0
+    # MIS rays: closest-hit queries toward the area light, any-hit toward the
+    # sky, none toward the directional light; the oracle counts alike
+    for k in ("rays_closest", "rays_any"):
+        assert abs(st_g[k] - st_o[0][k]) <= 0.01 * st_o[0][k], (k, st_g[k], st_o[0][k])
 
 
 def test_mirror_material_vs_oracle(gpu_ctx):

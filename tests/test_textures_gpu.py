@@ -53,6 +53,11 @@ def test_textures_at_the_first_vertex(gpu_ctx):
     assert np.array_equal(fg[..., 0], fo[..., 0])
     _close(fg[..., 1:], fo[..., 1:], 1e-3, 0.97)
     assert st["nonfinite_drops"] == 0
+    # a point light and a sky: MIS rays toward the sky are any-hit queries,
+    # toward the point light none (their term is zero); same counts as the oracle
+    _, st_o = OracleScene(sc).render_pass(p, 0)
+    for k in ("rays_closest", "rays_any"):
+        assert abs(st[k] - st_o[k]) <= 0.01 * st_o[k], (k, st[k], st_o[k])
 
 
 def test_textured_paths(gpu_ctx):
