@@ -130,7 +130,7 @@ __global__ void k_lt_reset(unsigned long long* counters, int next_live) {
 }
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(128, 10) k_lt_trace(DevAccel A, LtSlots st, int in,
+__global__ void __launch_bounds__(128, 8) k_lt_trace(DevAccel A, LtSlots st, int in,
                                                       unsigned long long* __restrict__ counters) {
   const int32_t* __restrict__ queue = st.live[in];
   int64_t n = (int64_t)counters[L_LIVE0 + in];
@@ -232,7 +232,7 @@ __global__ void __launch_bounds__(128, 4) k_lt_vertex(DevAccel A, DevShading S, 
 // occluded (Scene.hs:45-47) for the camera connections; the visible ones
 // are splatted
 template <int LAYOUT>
-__global__ void __launch_bounds__(128, 10) k_lt_shadow(DevAccel A, LtSlots st,
+__global__ void __launch_bounds__(128, 8) k_lt_shadow(DevAccel A, LtSlots st,
                                                        float* __restrict__ splat_xyz,
                                                        unsigned long long* __restrict__ counters) {
   const int32_t* __restrict__ queue = st.shadow;

@@ -174,7 +174,7 @@ __device__ __forceinline__ int64_t nodeCount(const unsigned long long* counters,
 }
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(128, 10) k_sp_camtrace(DevAccel A, CamNodes nb, int in, size_t cap,
+__global__ void __launch_bounds__(128, 8) k_sp_camtrace(DevAccel A, CamNodes nb, int in, size_t cap,
                                                          unsigned long long* __restrict__ counters) {
   int64_t n = nodeCount(counters, in, cap);
   traceWarpPersistent<false, LAYOUT, false>(
@@ -459,7 +459,7 @@ __global__ void k_sp_preset(unsigned long long* counters, int next) {
 }
 
 template <int LAYOUT>
-__global__ void __launch_bounds__(128, 10) k_sp_ptrace(DevAccel A, SpPhotons ph, int in,
+__global__ void __launch_bounds__(128, 8) k_sp_ptrace(DevAccel A, SpPhotons ph, int in,
                                                        unsigned long long* __restrict__ counters) {
   const int32_t* __restrict__ queue = ph.live[in];
   int64_t n = (int64_t)counters[S_PLIVE0 + in];
