@@ -8,7 +8,8 @@
 // paths from stage to stage.  Each bounce (one vertex of every live path,
 // nextVertex, Path.hs:49-87) is five launches:
 //
-//   k_trace         closest hit of the bounce rays (scIntersect)
+//   k_trace         closest hit of the bounce rays (scIntersect), and each
+//                   path's shading class, which k_class_scatter sorts by
 //   k_shade         emission on specular paths, the BSDF, one light sample and
 //                   one BSDF sample for MIS (sampleOneLight/estimateDirect,
 //                   Scene.hs:61-118), Russian roulette and the continuation
@@ -96,25 +97,6 @@ __global__ void k_bounce_reset(unsigned long long* counters, int next_live) {
   if (t == 5) counters[C_NEXT_SHADOW] = 0;
   if (t == 6) counters[C_NEXT_MIS] = 0;
   if (t < 32) classCounts(counters)[t] = 0;  // class counts [0, 16) and cursors [16, 32)
-}
-
-// shading class of every live path (after its closest hit)
-__global__ void __launch_bounds__(128) k_class_count(DevAccel A, DevShading S, Slots st,
-                                                     const int32_t* __restrict__ queue,
-                                                     const unsigned long long* __restrict__ qcount,
-                                                     int32_t* __restrict__ cls,
-                                                     unsigned long long* __restrict__ counters) {
-  int64_t n = (int64_t)*qcount;
-  int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t nround = (n + stride - 1) / stride * stride;
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
-    int c = -1;
-    if (q < n) {
-      c = shadeClass(A, S, hitPrim(st.hit, queue[q]));
-      cls[q] = c;
-    }
-    classCount(c, classCounts(counters));
-  }
 }
 
 // the live queue in shading-class order
@@ -228,18 +210,31 @@ __global__ void __launch_bounds__(128) k_raybin_scatter(const int32_t* __restric
   }
 }
 
-// closest hit of the live paths' rays (scIntersect)
+// closest hit of the live paths' rays (scIntersect); as each ray finishes,
+// its path's shading class goes to cls (by queue position) and is counted,
+// per block in shared memory, then once per class and block
 template <int LAYOUT>
-__global__ void __launch_bounds__(128, 8) k_trace(DevAccel A, Slots st, const int32_t* __restrict__ queue,
+__global__ void __launch_bounds__(128, 8) k_trace(DevAccel A, DevShading S, Slots st,
+                                               const int32_t* __restrict__ queue,
                                                const unsigned long long* __restrict__ qcount,
+                                               int32_t* __restrict__ cls,
                                                unsigned long long* __restrict__ counters) {
+  __shared__ unsigned s_counts[kShadeClasses];
+  if (threadIdx.x < kShadeClasses) s_counts[threadIdx.x] = 0;
+  __syncthreads();
   int64_t n = (int64_t)*qcount;
   traceWarpPersistent<false, LAYOUT, false>(
       A, n, counters + C_NEXT_TRACE, [&](int64_t q) { return loadRay7(st.ray, queue[q]); },
       [&](int64_t q, const RayQueryResult& res) {
-        int s = queue[q];
-        st.hit[s] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
+        float4 rec = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
+        st.hit[queue[q]] = rec;
+        int c = shadeClass(A, S, __float_as_int(rec.y));
+        cls[q] = c;
+        atomicAdd(s_counts + c, 1u);
       });
+  __syncthreads();  // every warp has left its walk
+  if (threadIdx.x < kShadeClasses && s_counts[threadIdx.x])
+    atomicAdd(classCounts(counters) + threadIdx.x, s_counts[threadIdx.x]);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_CLOSEST, (unsigned long long)n);
 }
 
@@ -403,9 +398,8 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
       shaded = Q.live[in];
     }
     withLayout(A.wide, [&](auto L) {
-      k_trace<decltype(L)::value><<<gt, block, 0, stream>>>(A, st, traced, qn, counters);
+      k_trace<decltype(L)::value><<<gt, block, 0, stream>>>(A, S, st, traced, qn, Q.cls, counters);
     });
-    k_class_count<<<G.raygen, block, 0, stream>>>(A, S, st, traced, qn, Q.cls, counters);
     k_class_scatter<<<G.raygen, block, 0, stream>>>(traced, qn, Q.cls, shaded, counters);
     if (S.textured)
       k_shade<true><<<std::min(G.shade, cap_blocks), block, 0, stream>>>(
