@@ -79,15 +79,14 @@ struct PathStates {
 };
 
 struct BatchQueues {
-  int32_t* shadow;
-  int32_t* mis;
+  int32_t* shadow;     // 2 cap entries: shadow rays and MIS rays (occlusionSlot)
   int32_t* resolve;
   uint32_t* keys;      // bin key per path
   int32_t* order;      // positions of the current buffer in shading-class order
   int32_t* cls;        // shading class per position
   unsigned int* bins;  // kBins counters / offsets
 };
-constexpr size_t kQueueWordsB = 7;  // the shadow queue takes two
+constexpr size_t kQueueWordsB = 6;  // the shadow queue takes two
 
 // vertex temporaries (everything of Slots but T, L and ray), single-buffered
 constexpr size_t kTempWords = kSlotWords - 16 - 16 - 8;
@@ -151,10 +150,8 @@ __global__ void k_iter_begin(BatchCtl* ctl, unsigned long long cap) {
   ctl->c[C_LIVE0 + 1 - cur] = 0;
   ctl->c[C_NEXT_TRACE] = 0;
   ctl->c[C_SHADOW] = 0;
-  ctl->c[C_MIS] = 0;
   ctl->c[C_RESOLVE] = 0;
   ctl->c[C_NEXT_SHADOW] = 0;
-  ctl->c[C_NEXT_MIS] = 0;
   for (int k = 0; k < 32; k++) ctl->cls[k] = 0;
 }
 
@@ -323,7 +320,9 @@ __global__ void __launch_bounds__(128) k_btrace_shadow(BatchCtl* ctl,
   const int32_t* __restrict__ queue = Q.shadow;
   traceWarpPersistent<true, LAYOUT, false, true>(
       scenes[0].A, n, ctl->c + C_NEXT_SHADOW,
-      [&](int64_t q, bool& by_intersect) { return loadOcclusionRay(tmp, queue[q], by_intersect); },
+      [&](int64_t q, bool& by_intersect, int& rank_prim) {
+        return loadOcclusionRay(tmp, queue[q], by_intersect, rank_prim);
+      },
       [&](int64_t q, const RayQueryResult& res) {
         storeOcclusion(tmp, queue[q], res, ctl->c + C_DEGENERATE);
       },
@@ -331,23 +330,6 @@ __global__ void __launch_bounds__(128) k_btrace_shadow(BatchCtl* ctl,
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ctl->c + C_ANY, (unsigned long long)n);
 }
 
-template <int LAYOUT>
-__global__ void __launch_bounds__(128) k_btrace_mis(BatchCtl* ctl,
-                                                    const BatchSceneDev* __restrict__ scenes,
-                                                    Slots tmp, PathStates ps, BatchQueues Q) {
-  const PathState& S = ps.b[ctl->cur];
-  int64_t n = (int64_t)ctl->c[C_MIS];
-  const int32_t* __restrict__ queue = Q.mis;
-  traceWarpPersistent<false, LAYOUT, false>(
-      scenes[0].A, n, ctl->c + C_NEXT_MIS,
-      [&](int64_t q) { return loadRay7(tmp.mray, queue[q]); },
-      [&](int64_t q, const RayQueryResult& res) {
-        int s = queue[q];
-        tmp.mhit[s] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
-      },
-      nullptr, [&](int64_t q) { return &scenes[S.scene[queue[q]]].A; });
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ctl->c + C_CLOSEST, (unsigned long long)n);
-}
 
 // Shading order of the current buffer: paths sorted by (job, shading class).
 // Shading reads each path's job parameters and scene tables through the job
@@ -426,7 +408,7 @@ __global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJob
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nround; i += stride) {
-    VertexOut o{false, false, false, false};
+    VertexOut o{false, false, false};
     bool fin = false;
     int job = -1;
     int q = 0;
@@ -442,8 +424,7 @@ __global__ void __launch_bounds__(128, 3) k_bshade(BatchCtl* ctl, const BatchJob
       });
     }
     queueAppend(o.shadow, (int)q, Q.shadow, c + C_SHADOW);
-    queueAppend(o.mis_any, ~(int)q, Q.shadow, c + C_SHADOW);
-    queueAppend(o.mis, (int)q, Q.mis, c + C_MIS);
+    queueAppend(o.mis, ~(int)q, Q.shadow, c + C_SHADOW);
     queueAppend(o.resolve, (int)q, Q.resolve, c + C_RESOLVE);
     pathsDone(fin, job, ctl, job_done);
   }
@@ -549,7 +530,7 @@ struct BatchEngine {
   std::vector<unsigned long long> totals;  // sample count of every job ever submitted
   bool ctl_dirty = true;
   // launch shapes
-  unsigned g_trace = 0, g_shadow = 0, g_mis = 0, g_shade = 0, g_resolve = 0, g_regen = 0,
+  unsigned g_trace = 0, g_shadow = 0, g_shade = 0, g_resolve = 0, g_regen = 0,
            g_bin = 0;
   // graphs
   cudaGraph_t graph = nullptr;
@@ -581,7 +562,6 @@ void shapesFor(BatchEngine* b, int sms) {
   const int bl = b->cfg.block;
   b->g_trace = residentBlocks(k_btrace<LAYOUT>, bl, sms);
   b->g_shadow = residentBlocks(k_btrace_shadow<LAYOUT>, bl, sms);
-  b->g_mis = residentBlocks(k_btrace_mis<LAYOUT>, bl, sms);
 }
 
 // one iteration's launches, in order, on b->stream
@@ -611,7 +591,6 @@ cudaError_t enqueueIterationT(BatchEngine* b, int use_cond, unsigned long long m
     k_bshade<false><<<b->g_shade, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps,
                                               b->q, b->d_job_done);
   k_btrace_shadow<LAYOUT><<<b->g_shadow, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
-  k_btrace_mis<LAYOUT><<<b->g_mis, bl, 0, s>>>(b->d_ctl, b->d_scenes, b->tmp, b->ps, b->q);
   k_bresolve<<<b->g_resolve, bl, 0, s>>>(b->d_ctl, b->d_jobs, b->d_scenes, b->tmp, b->ps, b->q,
                                          b->d_job_done);
   k_iter_end<<<1, 32, 0, s>>>(b->d_ctl, b->cond, use_cond, max_iters);
@@ -637,7 +616,6 @@ int launchShapes(BatchEngine* b, std::string& err) {
                                 (unsigned)std::max<int64_t>(1, (b->cap + 127) / 128));
   b->g_trace = std::min(b->g_trace, cap_blocks);
   b->g_shadow = std::min(b->g_shadow, cap_blocks);
-  b->g_mis = std::min(b->g_mis, cap_blocks);
   return BLING_OK;
 }
 
@@ -764,8 +742,7 @@ int batch_create(int device, cudaStream_t stream, const BatchConfig& cfg, BatchE
   t.svis = (int32_t*)take(1);
   t.mray = take(8);
   t.mhit = reinterpret_cast<float4*>(take(4));
-  b->q.shadow = (int32_t*)take(2);  // shadow rays and occlusion-only MIS rays
-  b->q.mis = (int32_t*)take(1);
+  b->q.shadow = (int32_t*)take(2);  // shadow rays and MIS rays
   b->q.resolve = (int32_t*)take(1);
   b->q.keys = (uint32_t*)take(1);
   b->q.order = (int32_t*)take(1);

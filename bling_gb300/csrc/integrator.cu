@@ -14,9 +14,8 @@
 //                   one BSDF sample for MIS (sampleOneLight/estimateDirect,
 //                   Scene.hs:61-118), Russian roulette and the continuation
 //                   sample; queues the shadow ray, the MIS ray and the vertex
-//   k_trace_shadow  any hit of the shadow rays (occluded), and of the MIS rays
-//                   toward lights other than area lights (whether they hit)
-//   k_trace_mis     closest hit of the MIS rays toward area lights
+//   k_trace_shadow  any hit of the shadow rays (occluded), and the MIS rays'
+//                   occlusion queries (wavefront.cuh, occlusionSlot)
 //   k_resolve       adds the vertex's radiance, updates the throughput,
 //                   queues the continuing paths and splats finished ones into
 //                   the film (addSample, Image.hs:250-299)
@@ -60,11 +59,10 @@ static void carve(unsigned char* base, size_t cap, Slots& st, Queues& q,
   int32_t* qw = (int32_t*)w;
   q.live[0] = qw;
   q.live[1] = qw + cap;
-  q.shadow = qw + 2 * cap;  // 2 cap entries: shadow rays and occlusion-only MIS rays
-  q.mis = qw + 4 * cap;
-  q.resolve = qw + 5 * cap;
-  q.sorted = qw + 6 * cap;
-  q.cls = qw + 7 * cap;
+  q.shadow = qw + 2 * cap;  // 2 cap entries: shadow rays and MIS rays
+  q.resolve = qw + 4 * cap;
+  q.sorted = qw + 5 * cap;
+  q.cls = qw + 6 * cap;
 }
 
 __device__ __forceinline__ unsigned* classCounts(unsigned long long* counters) {
@@ -92,10 +90,8 @@ __global__ void k_bounce_reset(unsigned long long* counters, int next_live) {
   if (t == 0) counters[next_live] = 0;
   if (t == 1) counters[C_NEXT_TRACE] = 0;
   if (t == 2) counters[C_SHADOW] = 0;
-  if (t == 3) counters[C_MIS] = 0;
   if (t == 4) counters[C_RESOLVE] = 0;
   if (t == 5) counters[C_NEXT_SHADOW] = 0;
-  if (t == 6) counters[C_NEXT_MIS] = 0;
   if (t < 32) classCounts(counters)[t] = 0;  // class counts [0, 16) and cursors [16, 32)
 }
 
@@ -247,26 +243,13 @@ __global__ void __launch_bounds__(128, 8) k_trace_shadow(DevAccel A, Slots st,
   int64_t n = (int64_t)counters[C_SHADOW];
   traceWarpPersistent<true, LAYOUT, false, true>(
       A, n, counters + C_NEXT_SHADOW,
-      [&](int64_t q, bool& by_intersect) { return loadOcclusionRay(st, queue[q], by_intersect); },
+      [&](int64_t q, bool& by_intersect, int& rank_prim) {
+        return loadOcclusionRay(st, queue[q], by_intersect, rank_prim);
+      },
       [&](int64_t q, const RayQueryResult& res) {
         storeOcclusion(st, queue[q], res, counters + C_DEGENERATE);
       });
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_ANY, (unsigned long long)n);
-}
-
-// closest hit of the BSDF-sampled MIS rays toward area lights
-template <int LAYOUT>
-__global__ void __launch_bounds__(128, 8) k_trace_mis(DevAccel A, Slots st,
-                                                   const int32_t* __restrict__ queue,
-                                                   unsigned long long* __restrict__ counters) {
-  int64_t n = (int64_t)counters[C_MIS];
-  traceWarpPersistent<false, LAYOUT, false>(
-      A, n, counters + C_NEXT_MIS, [&](int64_t q) { return loadRay7(st.mray, queue[q]); },
-      [&](int64_t q, const RayQueryResult& res) {
-        int s = queue[q];
-        st.mhit[s] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
-      });
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + C_CLOSEST, (unsigned long long)n);
 }
 
 // one vertex of every live path, up to its shadow and MIS rays (Path.hs:49-87)
@@ -281,7 +264,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, Pass
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int64_t nround = (n + stride - 1) / stride * stride;  // whole warps stay together for the appends
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
-    VertexOut o{false, false, false, false};
+    VertexOut o{false, false, false};
     int s = 0;
     if (q < n) {
       s = qin[q];
@@ -291,8 +274,7 @@ __global__ void __launch_bounds__(128, 4) k_shade(DevAccel A, DevShading S, Pass
       });
     }
     queueAppend(o.shadow, s, Q.shadow, counters + C_SHADOW);
-    queueAppend(o.mis_any, ~s, Q.shadow, counters + C_SHADOW);
-    queueAppend(o.mis, s, Q.mis, counters + C_MIS);
+    queueAppend(o.mis, ~s, Q.shadow, counters + C_SHADOW);
     queueAppend(o.resolve, s, Q.resolve, counters + C_RESOLVE);
   }
 }
@@ -338,7 +320,7 @@ unsigned residentGrid(K kernel, int sms) {
 }
 
 struct Grids {
-  unsigned trace, shadow, mis, shade, resolve, raygen;
+  unsigned trace, shadow, shade, resolve, raygen;
 };
 Grids g_grids[64];
 bool g_grids_ready[64] = {false};
@@ -354,8 +336,6 @@ Grids grids(int device, int sms) {
   g.shadow = std::min({residentGrid(k_trace_shadow<LAYOUT_BINARY>, sms),
                        residentGrid(k_trace_shadow<LAYOUT_WIDE>, sms),
                        residentGrid(k_trace_shadow<LAYOUT_COMPACT>, sms)});
-  g.mis = std::min({residentGrid(k_trace_mis<LAYOUT_BINARY>, sms), residentGrid(k_trace_mis<LAYOUT_WIDE>, sms),
-                    residentGrid(k_trace_mis<LAYOUT_COMPACT>, sms)});
   g.shade = residentGrid(k_shade<false>, sms);
   g.resolve = residentGrid(k_resolve, sms);
   g.raygen = (unsigned)std::max(1, sms * 8);
@@ -381,8 +361,7 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
   for (int depth = 0; depth <= max_depth; depth++) {
     int in = depth & 1;
     k_bounce_reset<<<1, 32, 0, stream>>>(counters, C_LIVE0 + (1 - in));
-    unsigned gt = std::min(G.trace, cap_blocks), gs = std::min(G.shadow, cap_blocks),
-             gm = std::min(G.mis, cap_blocks);
+    unsigned gt = std::min(G.trace, cap_blocks), gs = std::min(G.shadow, cap_blocks);
     // the bounce's queue: binned into Q.sorted (bounces after the camera's,
     // whose rays are in pixel order already), then shading-class sorted into
     // whichever of the two queues is free
@@ -409,8 +388,6 @@ cudaError_t runChunk(cudaStream_t stream, const DevAccel& A, const DevShading& S
           A, S, P, st, Q, shaded, depth, C_LIVE0 + in, d_film, d_filter, counters);
     withLayout(A.wide, [&](auto L) {
       k_trace_shadow<decltype(L)::value><<<gs, block, 0, stream>>>(A, st, Q.shadow, counters);
-      if (S.n_area_lights > 0)  // else the closest-hit MIS queue stays empty
-        k_trace_mis<decltype(L)::value><<<gm, block, 0, stream>>>(A, st, Q.mis, counters);
     });
     k_resolve<<<std::min(G.resolve, cap_blocks), block, 0, stream>>>(A, S, P, st, Q,
                                                                       C_LIVE0 + (1 - in), d_film,

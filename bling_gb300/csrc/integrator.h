@@ -125,8 +125,8 @@ struct DevShading {
   const float* shape_emission;  // 16 per shape
   const DLight* lights;
   int32_t n_lights;
-  int32_t n_area_lights;  // MIS rays need closest hits only toward these
   int32_t n_materials;
+  const int32_t* shape_prim;  // per shape: its primitive ID (MIS queries rank against it)
   bling_camera_desc camera;
   size_t bytes;
 };

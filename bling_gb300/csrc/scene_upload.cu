@@ -178,6 +178,13 @@ int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
   void* dinfo;
   if ((rc = up(info.data(), info.size() * sizeof(int2), &dinfo))) return rc;
   out.prim_info = (const int2*)dinfo;
+  // the primitive ID of every shape
+  std::vector<int32_t> shape_prim(std::max<size_t>(1, d.n_shapes), -1);
+  for (size_t i = 0; i < prim_owner.size(); i++)
+    if (prim_owner[i] < 0) shape_prim[~prim_owner[i]] = (int32_t)i;
+  void* dsp;
+  if ((rc = up(shape_prim.data(), shape_prim.size() * 4, &dsp))) return rc;
+  out.shape_prim = (const int32_t*)dsp;
   // shape emission
   std::vector<float> em(16 * std::max<size_t>(1, d.n_shapes), 0.0f);
   for (int i = 0; i < d.n_shapes; i++) memcpy(&em[16 * i], d.shapes[i].emission, 64);
@@ -255,7 +262,6 @@ int integrator_upload_scene(cudaStream_t stream, const bling_scene_desc& d,
     o.kind = DLIGHT_AREA;
     o.shape = ~v;
     lights.push_back(o);
-    out.n_area_lights++;
   }
   void* dl;
   if ((rc = up(lights.data(), lights.size() * sizeof(DLight), &dl))) return rc;

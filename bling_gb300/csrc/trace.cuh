@@ -158,11 +158,14 @@ __device__ __forceinline__ float qbyte(uint32_t word, uint32_t sel) {
 // With an `accel_of` functor (ray index -> const DevAccel*) every lane walks
 // the scene of its own ray (batches of jobs over several scenes, which must
 // share the node layout); otherwise all rays walk A.
-// MIXED (any-hit walks only): `load(q, by_intersect)` also says, per ray,
-// which predicate answers an analytic shape: Shape.intersects (false, the
-// occlusion test) or Shape.intersect (true: whether a closest-hit query would
-// find a hit).  The two differ, e.g. a box does not `intersect` a ray that
-// starts inside it, while it `intersects` it.  Triangles answer both alike.
+// MIXED (any-hit walks only): `load(q, by_intersect, rank_prim)` also says,
+// per ray, which predicate answers an analytic shape: Shape.intersects
+// (false, the occlusion test) or Shape.intersect (true: whether a closest-hit
+// query would find a hit).  The two differ, e.g. a box does not `intersect` a
+// ray that starts inside it, while it `intersects` it.  Triangles answer both
+// alike.  With rank_prim >= 0 a hit counts only if a closest-hit query would
+// rank it before a hit of primitive rank_prim at tmax: at t < tmax, or at
+// tmax with a larger primitive ID (the tie rule of the closest-hit walk).
 constexpr int kSentinel = INT32_MIN;
 
 template <bool ANY, int LAYOUT, bool COUNT, bool MIXED = false, class LoadRay, class Emit,
@@ -188,6 +191,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
   int64_t rid = -1;
   bool exhausted = false;
   bool by_intersect = false;  // MIXED: this ray's shapes answer by Shape.intersect
+  int rank_prim = -1;         // MIXED: hits must rank before this primitive's at tmax
   Ray r;
   V3 inv;
   int oct = 0;
@@ -233,7 +237,7 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
         if ((int64_t)my < n) {
           rid = (int64_t)my;
           if constexpr (MIXED)
-            r = load(rid, by_intersect);
+            r = load(rid, by_intersect, rank_prim);
           else
             r = load(rid);
           if (degenerateRay(r)) {
@@ -461,6 +465,8 @@ __device__ __forceinline__ void traceWarpPersistent(const DevAccel& A, int64_t n
               hit = shapeIntersect<false>(sh, ro, t, e, nullptr);
             }
           }
+          if (MIXED && rank_prim >= 0)  // ranked against a hit of rank_prim at tmax
+            hit = hit && (t < r.tmax || prim > rank_prim);
           if (hit) {
             if (ANY) {
               best_prim = prim;

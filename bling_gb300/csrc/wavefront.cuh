@@ -40,8 +40,7 @@ struct Slots {
 
 struct Queues {
   int32_t* live[2];  // paths to trace this bounce / next bounce
-  int32_t* shadow;
-  int32_t* mis;
+  int32_t* shadow;   // 2 cap entries: shadow rays and MIS rays (occlusionSlot)
   int32_t* resolve;
   int32_t* sorted;   // the live paths in shading-class order
   int32_t* cls;      // shading class per live queue entry
@@ -50,13 +49,13 @@ struct Queues {
 // counters (unsigned long long): queue sizes and statistics
 enum : int {
   C_LIVE0 = 0, C_LIVE1 = 1, C_CLOSEST = 2, C_ANY = 3, C_NONFINITE = 4, C_NEXT_TRACE = 5,
-  C_SHADOW = 6, C_MIS = 7, C_RESOLVE = 8, C_NEXT_SHADOW = 9, C_NEXT_MIS = 10, C_DEGENERATE = 11,
+  C_SHADOW = 6, C_RESOLVE = 8, C_NEXT_SHADOW = 9, C_DEGENERATE = 11,
   C_FIRST_NONFINITE = 12,  // ~g of the pass's lowest dropped sample g (0: none), by atomicMax
   C_COUNT = 16
 };
 
 constexpr size_t kSlotWords = 16 * 6 + 8 + 4 + 3 + 8 + 1 + 8 + 4;  // per slot, 4-byte words
-constexpr size_t kQueueWords = 8;  // the shadow queue takes two
+constexpr size_t kQueueWords = 7;  // the shadow queue takes two
 // counters: C_COUNT 8-byte counters, then the shading-class counts and
 // cursors (kShadeClasses 4-byte entries each, 16 reserved)
 constexpr size_t kCounterBytes = 256;
@@ -179,11 +178,13 @@ __device__ __forceinline__ Ray loadRay7(const float* base, int s) {
   float4 a = p[0], b = p[1];
   return Ray{V3{a.x, a.y, a.z}, V3{a.w, b.x, b.y}, fabsf(b.z), INFINITY};
 }
-__device__ __forceinline__ Ray loadShadowRay(const Slots& st, int s) {
-  const float4* p = reinterpret_cast<const float4*>(st.sray + 8 * (size_t)s);
+// a whole ray record (o, d, tmin, tmax)
+__device__ __forceinline__ Ray loadRay8(const float* base, int s) {
+  const float4* p = reinterpret_cast<const float4*>(base + 8 * (size_t)s);
   float4 a = p[0], b = p[1];
   return Ray{V3{a.x, a.y, a.z}, V3{a.w, b.x, b.y}, b.z, b.w};
 }
+__device__ __forceinline__ Ray loadShadowRay(const Slots& st, int s) { return loadRay8(st.sray, s); }
 
 // warp-aggregated append (every lane of the warp calls it)
 __device__ __forceinline__ void queueAppend(bool live, int slot, int32_t* __restrict__ queue,
@@ -317,29 +318,44 @@ int integrator_pass_params(const bling_render_params& p, uint64_t pass, int fw, 
                            PassParams& P, std::string& err);
 
 struct VertexOut {
-  bool shadow, mis, mis_any, resolve;
+  bool shadow, mis, resolve;
 };
 
 // Entries of the shadow queue: a slot s (its shadow ray, visibility into
-// svis), or ~s for an MIS ray that needs only whether it meets anything (a
-// light other than an area light: its radiance along the ray does not depend
-// on what the ray hits, only on whether it hits), answered into mhit like a
-// closest hit whose distance and barycentrics nobody reads.  The shadow
-// kernel walks them with the any-hit traversal in MIXED mode: an MIS entry's
-// shapes answer by Shape.intersect, as the closest-hit query of
-// sampleBsdfMis (Scene.hs:71-82) would, a shadow ray's by Shape.intersects.
+// svis), or ~s for the slot's MIS ray.  The closest-hit query of
+// sampleBsdfMis (Scene.hs:71-82) only matters through whether its answer is
+// the sampled light, or, for a light that is not an area light, whether
+// there is any answer, so each MIS ray becomes an occlusion query:
+//  * toward an area light whose shape the ray meets at t_L (the shape's own
+//    Shape.intersect, as the traversal computes it): is there a primitive
+//    that a closest-hit query would rank before it, i.e. one hit at t < t_L
+//    or at t_L with a larger primitive ID (nearest', Primitive.hs:29-43)?
+//    mhit holds the light's hit (t_L, its primitive) until an occluder
+//    replaces it;
+//  * otherwise: is there any hit at all?  mhit holds a miss until a hit
+//    replaces it.
+// The shadow kernel walks both with the any-hit traversal in MIXED mode: an
+// MIS entry's shapes answer by Shape.intersect, as the closest-hit query
+// would, a shadow ray's by Shape.intersects; the primitive an area light
+// entry ranks against comes from its mhit record.
 __device__ __forceinline__ int occlusionSlot(int e) { return e >= 0 ? e : ~e; }
-__device__ __forceinline__ Ray loadOcclusionRay(const Slots& st, int e, bool& by_intersect) {
+__device__ __forceinline__ Ray loadOcclusionRay(const Slots& st, int e, bool& by_intersect,
+                                                int& rank_prim) {
   by_intersect = e < 0;
-  return e >= 0 ? loadShadowRay(st, e) : loadRay7(st.mray, ~e);
+  if (e >= 0) {
+    rank_prim = -1;
+    return loadShadowRay(st, e);
+  }
+  rank_prim = __float_as_int(st.mhit[~e].y);  // the light's primitive, or -1
+  return loadRay8(st.mray, ~e);
 }
 __device__ __forceinline__ void storeOcclusion(const Slots& st, int e, const RayQueryResult& res,
                                                unsigned long long* degenerate) {
   if (e >= 0) {
     st.svis[e] = res.hit ? 0 : 1;
     if (res.prim == kDegenerateRay) atomicAdd(degenerate, 1ull);
-  } else {
-    st.mhit[~e] = hitRecord(res.hit, res.t, res.prim, res.b1, res.b2);
+  } else if (res.hit) {
+    st.mhit[~e] = hitRecord(true, res.t, res.prim, res.b1, res.b2);
   }
 }
 
@@ -355,7 +371,7 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
                                                  const PassParams& P, const Slots& st, int s,
                                                  uint64_t g, int depth,
                                                  unsigned long long* counters, Finish finish) {
-  VertexOut out{false, false, false, false};
+  VertexOut out{false, false, false};
   int ix, iy;
   uint32_t sn;
   decodeSample(P, g, ix, iy, sn);
@@ -426,26 +442,40 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
         flags |= VF_SHADOW;
       }
     }
-    // sampleBsdfMis (Scene.hs:71-82), the hit deferred.  Only an area
-    // light's term depends on which primitive the ray hits (a closest-hit
-    // query); an infinite light's on whether it hits at all (any hit).  A
-    // point or directional light emits along no ray (le is zero), so its
-    // term is f * 0 scaled by the weight: zero whatever the ray meets unless
-    // f or the weight is not finite or the ray is degenerate (a NaN sample);
-    // only then is the ray traced.
+    // sampleBsdfMis (Scene.hs:71-82), the hit deferred as an occlusion
+    // query (occlusionSlot above).  An area light's term counts only when
+    // the closest hit is its shape, so a ray that misses the shape needs no
+    // query unless the term could be NaN; an infinite light's term needs to
+    // know whether the ray hits anything.  A point or directional light
+    // emits along no ray (le is zero), so its term is f * 0 scaled by the
+    // weight: zero whatever the ray meets unless f or the weight is not
+    // finite or the ray is degenerate (a NaN sample); only then is the ray
+    // traced.
     BsdfSample bm = sampleBsdf(bsdf, wo, lBsdfCompU, lb1, lb2);
     if (!(bm.pdf == 0 || isBlack(bm.f))) {
       float w = powerHeuristic(bm.pdf, lightPdf(A, l, p, bm.wi));
       Ray mr{p, bm.wi, eps, INFINITY};
-      bool area = l.kind == DLIGHT_AREA;
-      if (area || l.kind == DLIGHT_INFINITE || !(isfinite(w) && allFinite(bm.f)) ||
-          degenerateRay(mr)) {
+      float4 rec = hitRecord(false, 0.0f, -1, 0.0f, 0.0f);
+      bool query = false;
+      if (l.kind == DLIGHT_AREA) {
+        const DShape& sh = A.shapes[l.shape];
+        float tl, el;
+        if (shapeIntersect<false>(sh, transRay(sh.w2o, mr), tl, el, nullptr)) {
+          mr.tmax = tl;
+          rec = hitRecord(true, tl, S.shape_prim[l.shape], 0.0f, 0.0f);
+          query = true;
+        }
+      }
+      if (!query)
+        query = l.kind == DLIGHT_INFINITE || !(isfinite(w) && allFinite(bm.f)) ||
+                degenerateRay(mr);
+      if (query) {
         storeBands(st.bsf, s, bm.f);
         st.bsw[s] = w;
         storeRay(st.mray, s, mr);
+        st.mhit[s] = rec;
         flags |= VF_MIS;
-        out.mis = area;
-        out.mis_any = !area;
+        out.mis = true;
       }
     }
   }

@@ -2360,16 +2360,22 @@ static int intLightId(const orc_scene& S, const Isect& it) {
 }
 
 // Ray counts of the MIS ray, as the GPU integrator queries it (the answer
-// is the same either way; this only sets which counter it goes to): a
-// closest-hit query toward an area light, an any-hit query toward an
-// infinite light, and none toward a point or directional light when the
-// term f * le * weight is zero whatever the ray meets (le is zero; f and the
-// weight finite, the ray without NaN), else an any-hit query.
+// is the same either way; this only sets which counter it goes to): an
+// any-hit query up to the light toward an area light whose shape the ray
+// meets, an any-hit query toward an infinite light, and none otherwise when
+// the term is zero whatever the ray meets (an area light it misses or a
+// point or directional light: le is zero; f and the weight finite, the ray
+// without NaN), else an any-hit query.
 static void countMisRay(const orc_scene& S, const Light& l, V p, const BsdfSample& b,
                         const Ray& ray, Counters& C) {
   if (l.kind == LIGHT_AREA) {
-    C.closest++;
-    return;
+    const Shape& s = S.shapes[l.shape];
+    float t, e;
+    DG dg;
+    if (shapeIntersect(s, transRay(s.o2w.i, ray), t, e, dg)) {
+      C.any++;
+      return;
+    }
   }
   bool finite = std::isfinite(powerHeuristic(b.pdf, lightPdf(S, l, p, b.wi)));
   for (int i = 0; i < 16; i++) finite = finite && std::isfinite(b.f.v[i]);
