@@ -65,11 +65,16 @@ int ensure_scratch(bling_ctx* c, size_t bytes) {
 // ---- host-buffer ray queries, chunked so that copies overlap traversal
 //
 // The rays (SoA, 8 floats per ray) are copied in, traced and their results
-// copied out chunk by chunk through kPipeBuffers staging buffers: while the
-// kernel traces chunk k on the context's stream, chunk k+1 is copied in on
-// one copy stream and chunk k-1's results are copied out on another.
+// copied out chunk by chunk through kPipeBuffers staging buffers: while a
+// kernel traces chunk k, chunk k+1 is copied in on one copy stream and chunk
+// k-1's results are copied out on another.  Consecutive chunks are traced on
+// two compute streams in turn (the context's and compute2), each buffer with
+// its own work counter (d_counter[1 + buffer]), so that a chunk's blocks take
+// the SMs its predecessor's last warps leave idle instead of waiting for the
+// whole predecessor.
 constexpr int kPipeBuffers = 3;
 constexpr size_t kPipeChunk = size_t(1) << 21;  // rays per chunk
+static_assert(1 + kPipeBuffers <= 256 / 8, "the context's 256-byte counter block holds the chunk counters");
 
 struct QueryOut {
   void* host;
@@ -82,6 +87,7 @@ int ensure_pipeline(bling_ctx* c) {
   if (c->copy_in) return BLING_OK;
   cudaError_t e = cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->compute2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_start, cudaEventDisableTiming);
   for (int b = 0; b < kPipeBuffers && e == cudaSuccess; b++) {
     e = cudaEventCreateWithFlags(&c->ev_in[b], cudaEventDisableTiming);
@@ -96,18 +102,20 @@ int ensure_pipeline(bling_ctx* c) {
 void destroy_pipeline(bling_ctx* c) {
   if (c->copy_in) cudaStreamDestroy(c->copy_in);
   if (c->copy_out) cudaStreamDestroy(c->copy_out);
+  if (c->compute2) cudaStreamDestroy(c->compute2);
   if (c->ev_start) cudaEventDestroy(c->ev_start);
   for (int b = 0; b < kPipeBuffers; b++) {
     if (c->ev_in[b]) cudaEventDestroy(c->ev_in[b]);
     if (c->ev_run[b]) cudaEventDestroy(c->ev_run[b]);
     if (c->ev_out[b]) cudaEventDestroy(c->ev_out[b]);
   }
-  c->copy_in = c->copy_out = nullptr;
+  c->copy_in = c->copy_out = c->compute2 = nullptr;
 }
 
-// launch(d_rays, count, d_outs) enqueues the query kernel of one chunk on
-// c->stream; outs[j] receives bytes_per_ray bytes per ray.  Called with c->mu
-// held; returns once every result is in host memory.
+// launch(d_rays, count, d_outs, d_counter, stream) enqueues the query kernel
+// of one chunk on `stream` with work counter d_counter; outs[j] receives
+// bytes_per_ray bytes per ray.  Called with c->mu held; returns once every
+// result is in host memory.
 template <class Launch>
 int pipelined_query(bling_ctx* c, const float* rays, size_t n, const QueryOut* outs, int n_outs,
                     Launch launch) {
@@ -139,16 +147,17 @@ int pipelined_query(bling_ctx* c, const float* rays, size_t n, const QueryOut* o
       CK(c, cudaMemcpyAsync(d_r + row * cn, rays + row * n + i, cn * sizeof(float),
                             cudaMemcpyHostToDevice, c->copy_in));
     CK(c, cudaEventRecord(c->ev_in[b], c->copy_in));
-    CK(c, cudaStreamWaitEvent(c->stream, c->ev_in[b], 0));
-    CK(c, launch(d_r, (int64_t)cn, d_out));
-    CK(c, cudaEventRecord(c->ev_run[b], c->stream));
+    cudaStream_t ks = (k & 1) ? c->compute2 : c->stream;
+    CK(c, cudaStreamWaitEvent(ks, c->ev_in[b], 0));
+    CK(c, launch(d_r, (int64_t)cn, d_out, c->d_counter + 1 + b, ks));
+    CK(c, cudaEventRecord(c->ev_run[b], ks));
     CK(c, cudaStreamWaitEvent(c->copy_out, c->ev_run[b], 0));
     for (int j = 0; j < n_outs; j++)
       CK(c, cudaMemcpyAsync((char*)outs[j].host + i * outs[j].bytes_per_ray, d_out[j],
                             cn * outs[j].bytes_per_ray, cudaMemcpyDeviceToHost, c->copy_out));
     CK(c, cudaEventRecord(c->ev_out[b], c->copy_out));
   }
-  // the last copy-out follows the last kernel, which follows every earlier one
+  // every copy-out follows its chunk's kernel; the last one follows them all
   CK(c, cudaStreamSynchronize(c->copy_out));
   return BLING_OK;
 }
@@ -772,11 +781,12 @@ int bling_trace_closest(bling_scene* s, const float* rays, size_t n, float* t, i
   CK(c, cudaSetDevice(c->device));
   QueryOut outs[3] = {{t, 4}, {prim, 4}, {b1b2, 8}};
   int rc = pipelined_query(c, rays, n, outs, b1b2 ? 3 : 2,
-                           [&](const float* d_r, int64_t cn, void** d_out) {
+                           [&](const float* d_r, int64_t cn, void** d_out,
+                               unsigned long long* d_counter, cudaStream_t ks) {
                              return launch_trace_closest(s->accel, d_r, cn, (float*)d_out[0],
                                                          (int32_t*)d_out[1],
                                                          b1b2 ? (float*)d_out[2] : nullptr,
-                                                         c->d_counter, c->stream);
+                                                         d_counter, ks);
                            });
   if (rc) return rc;
   s->stats.rays_closest += n;
@@ -791,9 +801,10 @@ int bling_trace_any(bling_scene* s, const float* rays, size_t n, uint8_t* hit) {
   CK(c, cudaSetDevice(c->device));
   QueryOut outs[1] = {{hit, 1}};
   int rc = pipelined_query(c, rays, n, outs, 1,
-                           [&](const float* d_r, int64_t cn, void** d_out) {
+                           [&](const float* d_r, int64_t cn, void** d_out,
+                               unsigned long long* d_counter, cudaStream_t ks) {
                              return launch_trace_any(s->accel, d_r, cn, (uint8_t*)d_out[0],
-                                                     c->d_counter, c->stream);
+                                                     d_counter, ks);
                            });
   if (rc) return rc;
   s->stats.rays_any += n;

@@ -27,6 +27,7 @@ struct bling_ctx {
   unsigned long long* d_counter = nullptr;
   // copy streams and events of the chunked host-buffer queries (made on first use)
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaStream_t compute2 = nullptr;  // every other chunk of a host-buffer query
   cudaEvent_t ev_start = nullptr;
   cudaEvent_t ev_in[3] = {nullptr, nullptr, nullptr};
   cudaEvent_t ev_run[3] = {nullptr, nullptr, nullptr};
