@@ -345,6 +345,11 @@ void bling_scene_destroy(bling_scene* scene);
 
 /* ---- ray queries over host buffers (SoA rays: ox oy oz dx dy dz tmin tmax,
  *      each n floats, i.e. rays[k*n + i]) ----
+ * The rays go through the device in chunks: copied in and out on two copy
+ * streams of the context and traced alternately on the context's stream and
+ * a second compute stream of its own, all ordered after the work already
+ * queued on the context's stream.  The call returns when every result is in
+ * host memory. */
  * bling_trace_closest replaces `scIntersect` (Scene.hs:49-51) on a batch:
  * the nearest hit, ties to the larger primitive ID as the reference's
  * `nearest'` fold does (Primitive.hs:29-43, TriangleMesh.hs:166).
