@@ -349,7 +349,7 @@ void bling_scene_destroy(bling_scene* scene);
  * streams of the context and traced alternately on the context's stream and
  * a second compute stream of its own, all ordered after the work already
  * queued on the context's stream.  The call returns when every result is in
- * host memory. */
+ * host memory.
  * bling_trace_closest replaces `scIntersect` (Scene.hs:49-51) on a batch:
  * the nearest hit, ties to the larger primitive ID as the reference's
  * `nearest'` fold does (Primitive.hs:29-43, TriangleMesh.hs:166).
