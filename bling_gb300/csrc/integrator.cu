@@ -95,21 +95,37 @@ __global__ void k_bounce_reset(unsigned long long* counters, int next_live) {
   if (t < 32) classCounts(counters)[t] = 0;  // class counts [0, 16) and cursors [16, 32)
 }
 
-// the live queue in shading-class order
+// the live queue in shading-class order: each block ranks its entries per
+// class in shared memory (warp-aggregated), then reserves one range per class
+// present with a single global atomic
 __global__ void __launch_bounds__(128) k_class_scatter(const int32_t* __restrict__ queue,
                                                        const unsigned long long* __restrict__ qcount,
                                                        const int32_t* __restrict__ cls,
                                                        int32_t* __restrict__ sorted,
                                                        unsigned long long* __restrict__ counters) {
   __shared__ unsigned off[kShadeClasses];
+  __shared__ unsigned s_cnt[kShadeClasses], s_base[kShadeClasses];
   classOffsets(classCounts(counters), off);
+  unsigned* cursor = classCounts(counters) + 16;
   int64_t n = (int64_t)*qcount;
   int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t nround = (n + stride - 1) / stride * stride;
+  int64_t nround = (n + stride - 1) / stride * stride;  // the same trip count in every thread
+  const int lane = threadIdx.x & 31;
   for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nround; q += stride) {
+    if (threadIdx.x < kShadeClasses) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
     int c = q < n ? cls[q] : -1;
-    int p = classSlot(c, off, classCounts(counters) + 16);
-    if (c >= 0) sorted[p] = queue[q];
+    unsigned grp = __match_any_sync(0xffffffffu, c);
+    int leader = __ffs(grp) - 1;
+    unsigned wbase = 0;
+    if (c >= 0 && lane == leader) wbase = atomicAdd(s_cnt + c, (unsigned)__popc(grp));
+    wbase = __shfl_sync(0xffffffffu, wbase, leader);
+    __syncthreads();
+    if (threadIdx.x < kShadeClasses && s_cnt[threadIdx.x])
+      s_base[threadIdx.x] = atomicAdd(cursor + threadIdx.x, s_cnt[threadIdx.x]);
+    __syncthreads();
+    if (c >= 0) sorted[off[c] + s_base[c] + wbase + __popc(grp & ((1u << lane) - 1))] = queue[q];
+    __syncthreads();  // s_cnt and s_base are rewritten by the next trip
   }
 }
 
