@@ -310,15 +310,16 @@ __global__ void __launch_bounds__(128) k_resolve(DevAccel A, DevShading S, PassP
       s = Q.resolve[q];
       uint64_t g = P.chunk_base + (uint64_t)s;
       Spec Tn, Ln;
-      cont = resolveVertex(
+      bool l_same = false;
+      cont = resolveVertex<true>(
           A, S, st, s, counters,
           [&](const Spec& L) {
             splatSample(film, P, g, L, counters, TableFilter{filter});
           },
-          Tn, Ln);
+          Tn, Ln, &l_same);
       if (cont) {
         storeBands(st.T, s, Tn);
-        storeBands(st.L, s, Ln);
+        if (!l_same) storeBands(st.L, s, Ln);
       }
     }
     queueAppend(cont, s, Q.live[live_out], counters + live_out);

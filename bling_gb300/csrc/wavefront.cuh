@@ -505,11 +505,14 @@ __device__ __forceinline__ VertexOut shadeVertex(const DevAccel& A, const DevSha
 // its shadow and MIS rays are traced and computes the new throughput.
 // Returns true when the path continues, with its throughput and radiance in
 // Tn and Ln (the caller stores them); a path that ends is handed to finish(L).
-template <class Finish>
+// KEEP_L (paths that stay in their slot): a continuing path that gains no
+// radiance here, with a finite throughput, keeps L + T * 0 = L in place: *l_same
+// is set and neither L nor Ln is touched.
+template <bool KEEP_L = false, class Finish>
 __device__ __forceinline__ bool resolveVertex(const DevAccel& A, const DevShading& S,
                                               const Slots& st, int s,
                                               unsigned long long* counters, Finish finish,
-                                              Spec& Tn, Spec& Ln) {
+                                              Spec& Tn, Spec& Ln, bool* l_same = nullptr) {
   size_t c = st.cap;
   int vf = st.vflags[s];
   int lc = S.n_lights;
@@ -548,6 +551,11 @@ __device__ __forceinline__ bool resolveVertex(const DevAccel& A, const DevShadin
   // a zero, which the film's sums do not keep)
   Spec lHere = (vf & VF_LE) ? loadBands(st.intl, s) + direct : direct;
   Spec T = loadBands(st.T, s);
+  if (KEEP_L && (vf & VF_CONT) && isBlack(lHere) && allFinite(T)) {
+    Tn = sScale(loadBands(st.fc, s) * T, st.invpc[s]);
+    *l_same = true;
+    return true;
+  }
   Spec Lr = loadBands(st.L, s) + T * lHere;
   if (vf & VF_CONT) {
     Tn = sScale(loadBands(st.fc, s) * T, st.invpc[s]);
